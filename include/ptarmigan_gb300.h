@@ -1,0 +1,226 @@
+/* ptarmigan_gb300 — C ABI of the GB300 (sm_103a) collision-loop engine.
+ *
+ * This is the drop-in boundary for ptarmigan's per-particle collision loop.
+ * The reference has no FFI layer; the function it replaces is the generic
+ *
+ *     fn collide<F: Field, R: Rng>(field: &F, incident: Particle, rng: &mut R,
+ *                                  current_id: &mut u64, options: CollideOptions)
+ *         -> Shower                                        (src/main.rs:134)
+ *
+ * mapped over a rank's primaries by src/main.rs:1118-1135 and summed into a
+ * ParticleBunch.  ptg_collide_batch() takes that whole map: a batch of
+ * primaries in, every surviving particle of every shower out.
+ *
+ * Conventions
+ *   - Units follow the reference: positions are four-vectors (ct, x, y, z) in
+ *     metres, momenta are normalised four-momenta u = p/(m c), Stokes vectors
+ *     are [I, Q, U, V] in the reference's global basis.
+ *   - Four-vectors are passed row-major, [n][4] doubles.
+ *   - Errors are returned as ptg_status; the library never aborts.  A
+ *     particle whose physics fails (out-of-table lookup, rejection-loop cap)
+ *     is retired with a per-particle status code, mirroring the reference's
+ *     panics (nonlinear_compton/mod.rs:32-35 and friends) without killing the
+ *     run.
+ *   - One context per host thread; calls on a context are serialised on its
+ *     CUDA stream.  The context is not thread-safe.
+ *   - Determinism: the same (seed, primaries, options) produce the same
+ *     physics bit for bit; only the ids given to secondaries (which are
+ *     drawn from a device counter) and the order of the output depend on
+ *     scheduling.  Random numbers come from counter-based Philox4x32-10
+ *     streams, so results are not bit-equal to the reference's Xoshiro256**.
+ */
+#ifndef PTARMIGAN_GB300_H
+#define PTARMIGAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTG_ABI_VERSION 1
+
+typedef enum {
+    PTG_OK = 0,
+    PTG_ERR_INVALID_ARGUMENT = 1,
+    PTG_ERR_OUT_OF_TABLE = 2,    /* a rate or CDF lookup left its table */
+    PTG_ERR_SANITY = 3,          /* kinematics check failed */
+    PTG_ERR_REJECTION_CAP = 4,   /* a rejection loop hit its iteration cap */
+    PTG_ERR_QUEUE_OVERFLOW = 5,  /* shower buffer could not grow */
+    PTG_ERR_CUDA = 6,
+    PTG_ERR_NO_DEVICE = 7,
+    PTG_ERR_TABLES = 8,          /* table files missing or malformed */
+    PTG_ERR_UNSUPPORTED = 9,     /* option combination not built yet */
+    PTG_ERR_ALLOC = 10
+} ptg_status;
+
+/* src/main.rs:1042-1060 picks the field model from (focusing, lcfa). */
+typedef enum {
+    PTG_PLANE_WAVE = 0,         /* LMA, 1D    field/plane_wave.rs */
+    PTG_FAST_PLANE_WAVE = 1,    /* LCFA, 1D   field/fast_plane_wave.rs */
+    PTG_FOCUSED_LASER = 2,      /* LMA, 3D    field/focused_laser.rs */
+    PTG_FAST_FOCUSED_LASER = 3  /* LCFA, 3D   field/fast_focused_laser.rs */
+} ptg_field_model;
+
+typedef enum { PTG_POL_LINEAR = 0, PTG_POL_CIRCULAR = 1 } ptg_polarization;          /* field/mod.rs:24-28 */
+typedef enum { PTG_ENV_COS2 = 0, PTG_ENV_FLATTOP = 1, PTG_ENV_GAUSSIAN = 2 } ptg_envelope; /* field/mod.rs:42-47 */
+typedef enum { PTG_ELECTRON = 0, PTG_POSITRON = 1, PTG_PHOTON = 2 } ptg_species;     /* particle/mod.rs:33-38 */
+
+/* Laser constructor arguments (main.rs:1042-1060).  n_cycles follows the
+ * reference's meaning for the envelope: cos^2 and flattop take the number of
+ * cycles, gaussian takes c * fwhm_duration / wavelength (main.rs:444-461). */
+typedef struct {
+    int32_t model;            /* ptg_field_model */
+    int32_t polarization;     /* ptg_polarization */
+    int32_t envelope;         /* ptg_envelope */
+    int32_t finite_bandwidth; /* control:bandwidth_correction (LMA only) */
+    double a0;
+    double wavelength;        /* metres */
+    double waist;             /* metres; ignored by plane waves */
+    double n_cycles;
+    double pol_angle;         /* radians; 0 for circular */
+    double chirp_b;           /* plane waves only */
+} ptg_laser_desc;
+
+/* CollideOptions, src/main.rs:71-105, one field per reference field, plus
+ * max_generation (tracking depth: primaries are generation 0; a particle of
+ * generation > max_generation is recorded but not tracked; -1 = no limit). */
+typedef struct {
+    double dt_multiplier;
+    double rate_increase;
+    double t_stop;            /* seconds; +inf for none */
+    double min_energy;        /* MeV */
+    double max_angle;         /* radians */
+    int32_t multiplicity;     /* -1 = no selection */
+    int32_t discard_bg_e;
+    int32_t discard_bg_ph;
+    int32_t rr;
+    int32_t tracking_photons;
+    int32_t tracking_secondaries;
+    int32_t keep_decayed_photons;
+    int32_t pol_resolved;
+    int32_t rotate_stokes_pars;
+    int32_t classical;
+    int32_t gaunt_factor;
+    int32_t max_generation;
+} ptg_collide_options;
+
+/* A set of particles.  On input (primaries) the caller fills species, r, u,
+ * pol, weight, id and parent_id; r0/u0 may be NULL (then r0 = r, u0 =
+ * (1,0,0,0), as Particle::create leaves them; particle/mod.rs:108-128).  On
+ * output the library fills every array. */
+typedef struct {
+    size_t n;
+    int32_t* species;          /* [n] ptg_species */
+    double* r;                 /* [n][4] position, metres */
+    double* u;                 /* [n][4] normalised momentum */
+    double* r0;                /* [n][4] position at creation */
+    double* u0;                /* [n][4] momentum at creation */
+    double* pol;               /* [n][4] Stokes vector */
+    double* weight;            /* [n] */
+    double* payload;           /* [n] a_eff at creation */
+    double* parent_chi;        /* [n] */
+    double* interaction_count; /* [n] */
+    double* work;              /* [n] absorbed energy, units of m c^2 */
+    uint64_t* id;              /* [n] */
+    uint64_t* parent_id;       /* [n] */
+    uint64_t* primary;         /* [n] output: index of the shower's primary in the input batch */
+    uint64_t* stream;          /* [n] output: random-stream id (deterministic particle key) */
+    int32_t* generation;       /* [n] output: 0 for primaries */
+    int32_t* flags;            /* [n] output: bit 0 = decayed intermediate photon */
+    int32_t* status;           /* [n] output: ptg_status of this particle */
+} ptg_particles;
+
+/* Event counters of one batch (the roofline's work model). */
+typedef struct {
+    uint64_t n_primaries;
+    uint64_t n_out;            /* particles in the output set */
+    uint64_t n_created;        /* particles ever created, primaries included */
+    uint64_t lepton_steps;
+    uint64_t photon_steps;
+    uint64_t emissions;
+    uint64_t pair_events;
+    uint64_t rejections;       /* rejection-loop iterations */
+    uint64_t particle_errors;  /* particles retired with status != PTG_OK */
+    uint32_t waves;            /* generations launched */
+    uint32_t reserved;
+    double absorbed_energy;    /* sum of work over all particles, MeV */
+    double device_ms;          /* kernel time of the batch */
+} ptg_run_stats;
+
+typedef struct ptg_ctx ptg_ctx;
+
+typedef struct {
+    int32_t device;            /* CUDA ordinal */
+    int32_t block_size;        /* 0 = autotuned default */
+    int32_t blocks_per_sm;     /* 0 = autotuned default */
+    int32_t reserved;
+    size_t initial_capacity;   /* 0 = library default (particles) */
+} ptg_device_cfg;
+
+/* Library version and ABI. */
+int ptg_abi_version(void);
+const char* ptg_status_string(ptg_status s);
+const char* ptg_last_error(void);
+
+/* Context lifetime.  Replaces the per-rank set-up in main.rs:1036-1066. */
+ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out);
+ptg_status ptg_context_destroy(ptg_ctx* ctx);
+
+/* Loads the rate and CDF tables (the LMA tables are data files; the LCFA
+ * tables are compiled in).  dir = NULL uses the directory shipped next to
+ * the library. */
+ptg_status ptg_load_tables(ptg_ctx* ctx, const char* dir);
+
+/* main.rs:1118-1135 for one batch: collide() over every primary, host
+ * buffers in and out.  `out` arrays are allocated by the library and must
+ * be released with ptg_particles_free().  `seed` keys the random streams
+ * (the role of control:rng_seed); `id_base` is the first id handed to
+ * secondaries (the reference starts current_id at the number of primaries,
+ * main.rs:1070). */
+ptg_status ptg_collide_batch(ptg_ctx* ctx, const ptg_laser_desc* laser, const ptg_collide_options* opts,
+                             const ptg_particles* primaries, uint64_t seed, uint64_t id_base,
+                             ptg_particles* out, ptg_run_stats* stats);
+
+/* The same with every buffer already on the device: `d_primaries` holds
+ * device pointers; the shower stays in library-owned device memory until
+ * the next call on this context and is described by `d_out` (device
+ * pointers, valid until then).  Used to time the kernels with inputs
+ * resident in HBM. */
+ptg_status ptg_collide_batch_device(ptg_ctx* ctx, const ptg_laser_desc* laser, const ptg_collide_options* opts,
+                                    const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
+                                    ptg_particles* d_out, ptg_run_stats* stats);
+
+/* Frees arrays allocated by ptg_collide_batch. */
+void ptg_particles_free(ptg_particles* p);
+
+/* Field::max_timestep (field/<model>.rs) for a laser, in seconds (or 1.0 where the
+ * reference returns None), and Field::ideal_initial_z, in metres. */
+ptg_status ptg_laser_timestep(const ptg_laser_desc* laser, double* dt);
+ptg_status ptg_laser_initial_z(const ptg_laser_desc* laser, double* z0);
+
+/* The CUDA stream the context launches on (a cudaStream_t). */
+void* ptg_context_stream(ptg_ctx* ctx);
+
+/* Diagnostics entry points used by the parity tests: evaluate one field
+ * model's E, B, a at n positions, and push n particles one step
+ * (Field::fields / Field::push), on the device, host buffers in and out. */
+ptg_status ptg_eval_fields(ptg_ctx* ctx, const ptg_laser_desc* laser, size_t n, const double* r,
+                           double* E, double* B, double* a);
+ptg_status ptg_push_steps(ptg_ctx* ctx, const ptg_laser_desc* laser, size_t n, double* r, double* u,
+                          double rqm, double dt, int32_t eqn, int32_t nsteps, double* work);
+
+/* Rate and sampler diagnostics (deterministic quantities checked against
+ * the FP64 oracle): LCFA photon rate at (chi, gamma) and the sampled photon
+ * energy for given uniforms; LCFA pair probability (unpolarised). */
+ptg_status ptg_lcfa_photon_rate(ptg_ctx* ctx, size_t n, const double* chi, const double* gamma, double* rate);
+ptg_status ptg_lcfa_photon_sample(ptg_ctx* ctx, size_t n, const double* chi, const double* gamma,
+                                  const double* rand3, double* omega, double* theta);
+ptg_status ptg_lcfa_pair_t(ptg_ctx* ctx, size_t n, const double* chi, double* t_par, double* t_perp);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PTARMIGAN_GB300_H */

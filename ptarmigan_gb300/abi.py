@@ -1,0 +1,223 @@
+"""ctypes mirror of ``include/ptarmigan_gb300.h``.
+
+The structures here are the C ABI's, field for field; the host-side Python
+API (:mod:`ptarmigan_gb300.api`) fills them from numpy arrays.
+"""
+
+import ctypes as C
+import math
+
+import numpy as np
+
+PTG_OK = 0
+PTG_ERR_INVALID_ARGUMENT = 1
+PTG_ERR_OUT_OF_TABLE = 2
+PTG_ERR_SANITY = 3
+PTG_ERR_REJECTION_CAP = 4
+PTG_ERR_QUEUE_OVERFLOW = 5
+PTG_ERR_CUDA = 6
+PTG_ERR_NO_DEVICE = 7
+PTG_ERR_TABLES = 8
+PTG_ERR_UNSUPPORTED = 9
+PTG_ERR_ALLOC = 10
+
+PLANE_WAVE, FAST_PLANE_WAVE, FOCUSED_LASER, FAST_FOCUSED_LASER = 0, 1, 2, 3
+LINEAR, CIRCULAR = 0, 1
+COS2, FLATTOP, GAUSSIAN = 0, 1, 2
+ELECTRON, POSITRON, PHOTON = 0, 1, 2
+
+# EquationOfMotion, field/mod.rs:61-65
+LORENTZ, LANDAU_LIFSHITZ, MODIFIED_LANDAU_LIFSHITZ = 0, 1, 2
+
+
+class LaserDesc(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32),
+        ("polarization", C.c_int32),
+        ("envelope", C.c_int32),
+        ("finite_bandwidth", C.c_int32),
+        ("a0", C.c_double),
+        ("wavelength", C.c_double),
+        ("waist", C.c_double),
+        ("n_cycles", C.c_double),
+        ("pol_angle", C.c_double),
+        ("chirp_b", C.c_double),
+    ]
+
+
+class CollideOptions(C.Structure):
+    _fields_ = [
+        ("dt_multiplier", C.c_double),
+        ("rate_increase", C.c_double),
+        ("t_stop", C.c_double),
+        ("min_energy", C.c_double),
+        ("max_angle", C.c_double),
+        ("multiplicity", C.c_int32),
+        ("discard_bg_e", C.c_int32),
+        ("discard_bg_ph", C.c_int32),
+        ("rr", C.c_int32),
+        ("tracking_photons", C.c_int32),
+        ("tracking_secondaries", C.c_int32),
+        ("keep_decayed_photons", C.c_int32),
+        ("pol_resolved", C.c_int32),
+        ("rotate_stokes_pars", C.c_int32),
+        ("classical", C.c_int32),
+        ("gaunt_factor", C.c_int32),
+        ("max_generation", C.c_int32),
+    ]
+
+
+_DP = C.POINTER(C.c_double)
+_I32P = C.POINTER(C.c_int32)
+_U64P = C.POINTER(C.c_uint64)
+
+
+class Particles(C.Structure):
+    _fields_ = [
+        ("n", C.c_size_t),
+        ("species", _I32P),
+        ("r", _DP),
+        ("u", _DP),
+        ("r0", _DP),
+        ("u0", _DP),
+        ("pol", _DP),
+        ("weight", _DP),
+        ("payload", _DP),
+        ("parent_chi", _DP),
+        ("interaction_count", _DP),
+        ("work", _DP),
+        ("id", _U64P),
+        ("parent_id", _U64P),
+        ("primary", _U64P),
+        ("stream", _U64P),
+        ("generation", _I32P),
+        ("flags", _I32P),
+        ("status", _I32P),
+    ]
+
+
+class RunStats(C.Structure):
+    _fields_ = [
+        ("n_primaries", C.c_uint64),
+        ("n_out", C.c_uint64),
+        ("n_created", C.c_uint64),
+        ("lepton_steps", C.c_uint64),
+        ("photon_steps", C.c_uint64),
+        ("emissions", C.c_uint64),
+        ("pair_events", C.c_uint64),
+        ("rejections", C.c_uint64),
+        ("particle_errors", C.c_uint64),
+        ("waves", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("absorbed_energy", C.c_double),
+        ("device_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
+class DeviceCfg(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("block_size", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("reserved", C.c_int32),
+        ("initial_capacity", C.c_size_t),
+    ]
+
+
+# Array layout of each Particles field: (name, dtype, columns)
+PARTICLE_FIELDS = [
+    ("species", np.int32, 1),
+    ("r", np.float64, 4),
+    ("u", np.float64, 4),
+    ("r0", np.float64, 4),
+    ("u0", np.float64, 4),
+    ("pol", np.float64, 4),
+    ("weight", np.float64, 1),
+    ("payload", np.float64, 1),
+    ("parent_chi", np.float64, 1),
+    ("interaction_count", np.float64, 1),
+    ("work", np.float64, 1),
+    ("id", np.uint64, 1),
+    ("parent_id", np.uint64, 1),
+    ("primary", np.uint64, 1),
+    ("stream", np.uint64, 1),
+    ("generation", np.int32, 1),
+    ("flags", np.int32, 1),
+    ("status", np.int32, 1),
+]
+
+_CT = {np.float64: _DP, np.int32: _I32P, np.uint64: _U64P}
+
+
+def empty_arrays(n):
+    """Host arrays for every Particles field, n rows."""
+    out = {}
+    for name, dt, cols in PARTICLE_FIELDS:
+        shape = (n, cols) if cols > 1 else (n,)
+        out[name] = np.zeros(shape, dtype=dt)
+    return out
+
+
+def particles_view(arrays, n=None):
+    """A Particles struct pointing at the given numpy arrays (kept alive by
+    the caller).  Missing fields are NULL."""
+    p = Particles()
+    first = next(iter(arrays.values()))
+    p.n = len(first) if n is None else n
+    for name, dt, _cols in PARTICLE_FIELDS:
+        a = arrays.get(name)
+        if a is None:
+            setattr(p, name, C.cast(None, _CT[dt]))
+            continue
+        if a.dtype != dt or not a.flags["C_CONTIGUOUS"]:
+            raise TypeError("field %s must be a C-contiguous %s array" % (name, np.dtype(dt).name))
+        setattr(p, name, a.ctypes.data_as(_CT[dt]))
+    return p
+
+
+def laser_desc(model, a0, wavelength, polarization=LINEAR, envelope=None, waist=math.inf, n_cycles=None,
+               fwhm_duration=None, pol_angle=0.0, chirp_b=0.0, finite_bandwidth=False):
+    """Builds a LaserDesc the way main.rs:405-470 reads laser keys."""
+    focusing = model in (FOCUSED_LASER, FAST_FOCUSED_LASER)
+    if envelope is None:
+        envelope = GAUSSIAN if focusing else COS2
+    if envelope == GAUSSIAN and fwhm_duration is not None:
+        n_cycles = 2.997925e8 * fwhm_duration / wavelength
+    if n_cycles is None:
+        raise ValueError("n_cycles (or fwhm_duration for a gaussian envelope) is required")
+    if polarization == CIRCULAR:
+        pol_angle = 0.0
+    if focusing:
+        chirp_b = 0.0
+    return LaserDesc(model, polarization, envelope, int(finite_bandwidth), a0, wavelength, waist, n_cycles,
+                     pol_angle, chirp_b)
+
+
+def collide_options(**kw):
+    """CollideOptions with the reference's defaults (main.rs:339-400, 1102-1117)."""
+    o = CollideOptions()
+    o.dt_multiplier = 1.0
+    o.rate_increase = 1.0
+    o.t_stop = math.inf
+    o.min_energy = 0.0
+    o.max_angle = math.pi
+    o.multiplicity = -1
+    o.discard_bg_e = 0
+    o.discard_bg_ph = 0
+    o.rr = 1
+    o.tracking_photons = 1
+    o.tracking_secondaries = 1
+    o.keep_decayed_photons = 0
+    o.pol_resolved = 0
+    o.rotate_stokes_pars = 1
+    o.classical = 0
+    o.gaunt_factor = 0
+    o.max_generation = -1
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
