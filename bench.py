@@ -1,0 +1,292 @@
+"""Benchmark of the collision loop: collided primaries/s (showers included).
+
+Workload (one "step" = one batch through the collision loop): the focused
+LCFA shower — 1e6 electrons at 10 GeV, 1% rms energy spread, 2 x 2 x 20 um
+rms, 50 urad divergence, head-on with a linearly polarised focused Gaussian
+laser (FastFocusedLaser) a0 = 10, w0 = 4 um, 0.8 um, 30 fs FWHM; LCFA
+emission and pair creation on, secondaries tracked to generation 2; FP64
+push.  Inputs are seeded synthetic beams with those distributions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` times ptg_collide_batch_device with the
+primaries resident in HBM; `e2e` times ptg_collide_batch (host buffers in
+and out, host<->device copies inside the timed region).  --impl reference
+times the CPU restatement of the reference's collision loop (the reference
+is Rust and no Rust toolchain is available) on all host cores.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "collided primaries/s incl. showers"
+UNIT = "primaries/s"
+N_PRIMARIES = 1_000_000
+WORKLOAD = "focused LCFA shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; FastFocusedLaser a0=10 w0=4 um 0.8 um 30 fs LP; pairs on; generations<=2"
+
+
+def workload(n, seed):
+    from ptarmigan_gb300 import abi, beam
+    laser = abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(10.0)
+    prim = beam.build(n, g, sigma=0.01 * g, radius=2e-6, length=20e-6, rms_div=50e-6, laser=laser, seed=seed)
+    opts = abi.collide_options(max_generation=2)
+    return laser, opts, prim
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, name in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_run(n_sample, seed, threads):
+    """The oracle (CPU restatement of the reference) on a sample."""
+    from oracle import oracle
+    oracle.build()
+    laser, opts, prim = workload(n_sample, seed)
+    t0 = time.perf_counter()
+    _, st = oracle.collide(laser, opts, prim, seed=seed, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_sample / dt, st, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = cpu_threads()
+    n_sample = max(64, args.cpu_sample_per_core * threads)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_run(min(n_sample, 16 * threads), 99, threads)
+    vals = []
+    t_all = 0.0
+    for k in range(args.steps):
+        v, st, dt = cpu_run(n_sample, 1000 + k, threads)
+        vals.append(v)
+        t_all += dt
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_primaries_per_step": n_sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d primaries per step of the same workload, oracle C++ FP64 restatement of "
+                                   "src/main.rs:134-289 (the Rust reference cannot be built: no cargo/rustc)" % n_sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def nbytes(d):
+    return int(sum(v.nbytes for v in d.values()))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_PRIMARIES)
+    ap.add_argument("--cpu-sample-per-core", type=int, default=600)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    dist_on = world > 1
+    if dist_on:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local_rank)
+
+    from ptarmigan_gb300 import abi, build, engine
+    build.build()
+    eng = engine.Engine(device=local_rank)
+    stream = torch.cuda.ExternalStream(eng.stream_ptr, device=local_rank)
+
+    # weak scaling: every rank collides its own, disjoint set of primaries
+    laser, opts, prim = workload(args.n, seed=1 + rank)
+    id_base = args.n * world + rank * (1 << 40)
+    dev = torch.device("cuda", local_rank)
+    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist_on:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (also sizes the shower store)
+    for w in range(args.warmup):
+        _, st = eng.collide_device(laser, opts, d_prim, seed=100 + w, id_base=id_base)
+
+    # device-resident timing: CUDA events on the engine's stream
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    stats = []
+    kern_ms = []
+    sampler = ClockSampler(local_rank)
+    barrier()
+    with sampler:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+        for k in range(args.steps):
+            _, st = eng.collide_device(laser, opts, d_prim, seed=1000 + k, id_base=id_base)
+            stats.append(st)
+            kern_ms.append(st["device_ms"])
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    t_ms = ev0.elapsed_time(ev1)
+    if dist_on:
+        t = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = args.n * world * args.steps / (t_ms / 1e3)
+
+    # end-to-end through the host API: H2D of the primaries and D2H of the
+    # shower inside the timed region
+    h2d = nbytes(prim)
+    barrier()
+    t0 = time.perf_counter()
+    d2h = 0
+    for k in range(max(1, min(args.steps, 2))):
+        out, st_e = eng.collide(laser, opts, prim, seed=2000 + k, id_base=id_base)
+        d2h = nbytes(out)
+    e2e_steps = max(1, min(args.steps, 2))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist_on:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = args.n * world * e2e_steps / e2e_s
+
+    # roofline of the dominant kernel (the LCFA wave): FP64 work per launch
+    # from the event counts, over the wave time measured above
+    pk, pk_kind = peaks()
+    st0 = stats[-1]
+    fp64_model = json.load(open(os.path.join(ROOT, "profiles", "fp64_opcount.json"))) if os.path.exists(
+        os.path.join(ROOT, "profiles", "fp64_opcount.json")) else None
+    roofline = None
+    if fp64_model:
+        flops = (st0["lepton_steps"] * fp64_model["per_lepton_step"] + st0["photon_steps"] * fp64_model["per_photon_step"]
+                 + st0["emissions"] * fp64_model["per_emission"] + st0["pair_events"] * fp64_model["per_pair_event"])
+        achieved = flops / (np.mean(kern_ms) / 1e3) / 1e12
+        peak = fp64_model.get("fp64_peak_tflops")
+        roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": (achieved / peak) if peak else None, "traffic": fp64_model.get("traffic_bytes_per_launch"),
+                    "peak_source": fp64_model.get("peak_source")}
+
+    launches = int(sum(2 + s["waves"] for s in stats))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_primaries_per_gpu": args.n, "parallelism": "replicas x%d" % world,
+                   "l2": "inputs and shower store larger than L2 (no flush needed)",
+                   "events_per_step": {k: stats[-1][k] for k in ("lepton_steps", "photon_steps", "emissions",
+                                                                 "pair_events", "n_created", "n_out", "waves")}},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": sampler.summary(),
+        "roofline": roofline,
+        "peaks": {"source": pk_kind, "hbm_gbs": pk.get("hbm_gbs")},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        n_sample = max(64, args.cpu_sample_per_core * threads)
+        v, st_c, dt = cpu_run(n_sample, 7, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d primaries of the same workload (%.1f s), oracle C++ FP64 restatement "
+                                          "of the collision loop on %d host threads" % (n_sample, dt, threads)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist_on:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,383 @@
+// The collision loop (src/main.rs:134-289) as a wave of a persistent
+// kernel.  One thread owns one particle at a time and steps it through the
+// field until it leaves (Field::contains) or decays; when it is done the
+// thread takes the next particle of the wave from a global cursor, so lanes
+// stay busy although trajectories differ in length.  Secondaries are
+// appended to the shower store with one atomic per warp and form the next
+// wave.  Waves alternate leptons -> photons -> leptons ...
+#pragma once
+#include "ptg_fields.cuh"
+#include "ptg_lcfa.cuh"
+#include "ptg_lma.cuh"
+
+namespace ptg {
+
+enum { SP_ELECTRON = 0, SP_POSITRON = 1, SP_PHOTON = 2 };
+enum { FLAG_INTERMEDIATE = 1, FLAG_DROP = 2 };
+enum { ST_OK = 0, ST_OUT_OF_TABLE = 2, ST_SANITY = 3, ST_REJECTION_CAP = 4, ST_UNSUPPORTED = 9 };
+
+// Shower store, structure of arrays.  Four-vectors are component-major:
+// component c of particle i is at v[c * cap + i].
+struct Store {
+    double *r, *u, *r0, *u0, *pol;
+    double *weight, *payload, *parent_chi, *icount, *work;
+    unsigned long long *id, *parent_id, *primary, *stream;
+    int *species, *generation, *flags, *status;
+    unsigned long long cap;
+};
+
+struct Counters {
+    unsigned long long n_total;  // particles in the store
+    unsigned long long next;     // wave cursor
+    unsigned long long overflow; // appends that did not fit
+    unsigned long long lepton_steps, photon_steps, emissions, pair_events, rejections, errors;
+    unsigned long long n_out;    // compaction cursor
+};
+
+struct StepOptions {
+    double dt;                // max_timestep * dt_multiplier
+    double t_stop;            // seconds
+    double rate_increase;
+    int eqn;                  // EQN_*
+    int classical_mode;       // RadiationMode::Classical
+    int classical;            // options.classical
+    int electron_recoils;
+    int tracking_photons;
+    int pol_resolved;
+    int rotate_stokes;
+    int tracking_secondaries;
+    int max_generation;       // -1: no limit
+    int keep_decayed;
+};
+
+struct WaveArgs {
+    FieldParams f;
+    StepOptions o;
+    Store s;
+    Counters* c;
+    const PairGL* gl;
+    const LmaTables* lma;
+    unsigned long long seed;
+    unsigned long long lo, hi;     // wave = store slots [lo, hi)
+    unsigned long long n_primaries, id_base;
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append of `count` slots per calling lane (all calling
+// lanes must pass the same count).  Returns this lane's first slot.
+__device__ __forceinline__ unsigned long long append_slots(Counters* c, unsigned count) {
+    unsigned mask = __activemask();
+    unsigned leader = __ffs(mask) - 1;
+    unsigned rank = __popc(mask & ((1u << lane_id()) - 1u));
+    unsigned long long base = 0;
+    if (lane_id() == leader) base = atomicAdd(&c->n_total, (unsigned long long)(count * __popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + (unsigned long long)rank * count;
+}
+
+__device__ __forceinline__ void put4(double* v, unsigned long long cap, unsigned long long i, d4 x) {
+    v[i] = x.t;
+    v[cap + i] = x.x;
+    v[2 * cap + i] = x.y;
+    v[3 * cap + i] = x.z;
+}
+__device__ __forceinline__ d4 get4(const double* v, unsigned long long cap, unsigned long long i) {
+    return d4{v[i], v[cap + i], v[2 * cap + i], v[3 * cap + i]};
+}
+
+struct Lane {
+    d4 r, u, pol;
+    double weight, icount, work;
+    unsigned long long slot, stream, id;
+    uint32_t step;
+    int species, gen, status, flags;
+    bool decayed;
+};
+
+__device__ __forceinline__ bool lane_untracked(const WaveArgs& a, const Lane& L) {
+    return (!a.o.tracking_secondaries && L.gen > 0) || (a.o.max_generation >= 0 && L.gen > a.o.max_generation);
+}
+
+__device__ __forceinline__ void spawn(const WaveArgs& a, unsigned long long slot, int species, d4 r, d4 u, d4 u0,
+                                      d4 pol, double weight, double payload, double parent_chi, double work,
+                                      unsigned long long parent_id, unsigned long long primary,
+                                      unsigned long long stream, int gen) {
+    const Store& s = a.s;
+    unsigned long long cap = s.cap;
+    put4(s.r, cap, slot, r);
+    put4(s.r0, cap, slot, r);
+    put4(s.u, cap, slot, u);
+    put4(s.u0, cap, slot, u0);
+    put4(s.pol, cap, slot, pol);
+    s.weight[slot] = weight;
+    s.payload[slot] = payload;
+    s.parent_chi[slot] = parent_chi;
+    s.icount[slot] = 0.0;
+    s.work[slot] = work;
+    s.id[slot] = a.id_base + (slot - a.n_primaries);
+    s.parent_id[slot] = parent_id;
+    s.primary[slot] = primary;
+    s.stream[slot] = stream;
+    s.species[slot] = species;
+    s.generation[slot] = gen;
+    s.flags[slot] = 0;
+    s.status[slot] = ST_OK;
+}
+
+// One charged-particle step: main.rs:170-206.  Returns false when the
+// particle is finished.
+template <int MODEL>
+__device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit) {
+    const FieldParams& f = a.f;
+    double rqm = (L.species == SP_ELECTRON ? ELECTRON_CHARGE : -ELECTRON_CHARGE) / ELECTRON_MASS;
+    double dt = a.o.dt;
+    d4 r, u;
+    double dt_actual, dwork;
+    Draws rng;
+    rng.begin(a.seed, L.stream, L.step);
+    bool emitted = false;
+    d4 k = d4{0, 0, 0, 0}, upr = d4{0, 0, 0, 0};
+    d3 kpol = mk3(0, 0, 0);
+    double a_eff = 0.0, chi = 0.0, absorption = 0.0;
+    if (MODEL == M_FAST_PLANE_WAVE || MODEL == M_FAST_FOCUSED_LASER) {
+        // Field::push default (field/mod.rs:147-152)
+        double h = 0.5 * SPEED_OF_LIGHT * dt / L.u.t;
+        d4 rh = d4{L.r.t + h * L.u.t, L.r.x + h * L.u.x, L.r.y + h * L.u.y, L.r.z + h * L.u.z};
+        d3 E, B;
+        double aa;
+        lcfa_fields(f, rh, &E, &B, &aa);
+        vay_push(rh, L.u, E, B, rqm, dt, a.o.eqn, [](double c) { return gaunt_factor(c); }, &r, &u, &dwork);
+        dt_actual = dt;
+        // lcf.rs:85-134 at the new position
+        lcfa_fields(f, r, &E, &B, &a_eff);
+        d3 beta = mk3(u.x / u.t, u.y / u.t, u.z / u.t);
+        double eb = dot(E, beta);
+        double E_rf_sqd = norm_sqr(E + SPEED_OF_LIGHT * cross(beta, B)) - eb * eb;
+        chi = E_rf_sqd > 0.0 ? u.t * sqrt(E_rf_sqd) / CRITICAL_FIELD : 0.0;
+        double prob = a.o.classical_mode ? dt_actual * lcfa_classical_rate(chi, u.t) : dt_actual * lcfa_photon_rate(chi, u.t);
+        if (rng.next() < prob) {
+            double r1 = rng.next(), r2 = rng.next(), r3 = rng.next();
+            double omega_mc2, theta;
+            if (a.o.classical_mode)
+                lcfa_classical_sample(chi, u.t, r1, r2, r3, &omega_mc2, &theta);
+            else
+                lcfa_photon_sample(chi, u.t, r1, r2, r3, &omega_mc2, &theta);
+            if (theta >= 0.0) {
+                double cphi = 2.0 * PI * r3;
+                d3 lng = normalize(beta);
+                d3 w = -normalize(E - (dot(lng, E) / sqrt(norm_sqr(E))) * lng + SPEED_OF_LIGHT * cross(beta, B));
+                double sp, cp;
+                sincos(cphi, &sp, &cp);
+                d3 perp = rotate_around(w, lng, sp, cp);
+                double st, ct;
+                sincos(theta, &st, &ct);
+                d3 k3 = omega_mc2 * (ct * lng + st * perp);
+                k = d4{sqrt(dot(k3, k3)), k3.x, k3.y, k3.z};
+                kpol = lcfa_stokes(k, chi, u.t, beta, w, a.o.classical_mode != 0);
+                upr = d4{u.t - k.t, u.x - k.x, u.y - k.y, u.z - k.z};
+                emitted = true;
+            }
+        }
+    } else {
+        lma_push(f, L.r, L.u, rqm, dt, a.o.eqn, &r, &u, &dt_actual, &dwork);
+        int st = lma_radiate(f, *a.lma, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr, &kpol,
+                             &a_eff, &chi, &absorption, rej);
+        if (st != ST_OK) {
+            L.status = st;
+            L.r = r;
+            L.u = u;
+            return;
+        }
+    }
+    if (emitted) {
+        unsigned long long slot = append_slots(a.c, 1);
+        if (slot < a.s.cap) {
+            spawn(a, slot, SP_PHOTON, r, k, d4{0, 0, 0, 0}, d4{1.0, kpol.x, kpol.y, kpol.z}, L.weight, a_eff, chi, 0.0,
+                  L.id, a.s.primary[L.slot], child_stream(L.stream, L.step, 0), L.gen + 1);
+        } else {
+            atomicAdd(&a.c->overflow, 1ull);
+        }
+        ++*nemit;
+        if (a.o.electron_recoils) u = upr;
+        L.icount += 1.0;
+        if (!a.o.classical) L.work += absorption;
+    }
+    L.r = r;
+    L.u = u;
+    L.work += dwork;
+}
+
+// One photon step: main.rs:214-256.
+template <int MODEL>
+__device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* npair) {
+    const FieldParams& f = a.f;
+    double dt = a.o.dt;
+    Draws rng;
+    rng.begin(a.seed, L.stream, L.step);
+    d4 ell = L.u;
+    double h = SPEED_OF_LIGHT * dt / ell.t;
+    d4 r = d4{L.r.t + h * ell.t, L.r.x + h * ell.x, L.r.y + h * ell.y, L.r.z + h * ell.z};
+    d4 pol = a.o.pol_resolved ? L.pol : d4{1.0, 0.0, 0.0, 0.0};
+    double prob = 0.0;
+    d4 pol_new = pol;
+    bool created = false;
+    d4 ue, up;
+    double frac = 1.0, a_eff = 0.0, chi = 0.0, absorption = 0.0;
+    if (MODEL == M_FAST_PLANE_WAVE || MODEL == M_FAST_FOCUSED_LASER) {
+        // lcf.rs:144-193
+        d3 E, B;
+        lcfa_fields(f, r, &E, &B, &a_eff);
+        d3 n = normalize(mk3(ell.x, ell.y, ell.z));
+        d3 a_perp = E - dot(E, n) * n + SPEED_OF_LIGHT * cross(n, B);
+        double E_rf_sqd = norm_sqr(a_perp);
+        if (E_rf_sqd > 0.0) {
+            chi = ell.t * sqrt(E_rf_sqd) / CRITICAL_FIELD;
+            prob = lcfa_pair_probability(ell, pol, chi, a_perp, dt, &pol_new);
+        }
+        double ri = (prob * a.o.rate_increase > 0.1) ? 0.1 / prob : a.o.rate_increase;
+        if (rng.next() < prob * ri) {
+            double gamma_p, cos_theta, cphi;
+            if (!lcfa_pair_sample(ell, pol, chi, a_perp, rng, *a.gl, &gamma_p, &cos_theta, &cphi, rej)) {
+                L.status = ST_REJECTION_CAP;
+                L.r = r;
+                return;
+            }
+            double sin_theta = sqrt(1.0 - cos_theta * cos_theta);
+            double upm = gamma_p * sqrt(1.0 - 1.0 / (gamma_p * gamma_p));
+            d3 e1 = normalize(a_perp);
+            d3 e2 = cross(n, e1);
+            double sp, cp;
+            sincos(cphi, &sp, &cp);
+            d3 p3 = upm * (cos_theta * n + (sin_theta * cp) * e1 + (sin_theta * sp) * e2);
+            d3 e3 = mk3(ell.x, ell.y, ell.z) - p3;
+            up = d4{sqrt(1.0 + dot(p3, p3)), p3.x, p3.y, p3.z};
+            ue = d4{sqrt(1.0 + dot(e3, e3)), e3.x, e3.y, e3.z};
+            frac = 1.0 / ri;
+            created = true;
+        }
+    } else {
+        int st = lma_pair_create(f, *a.lma, r, ell, pol, dt, rng, a.o.rate_increase, &prob, &pol_new, &created, &ue,
+                                 &up, &frac, &a_eff, &chi, &absorption, rej);
+        if (st != ST_OK) {
+            L.status = st;
+            L.r = r;
+            return;
+        }
+    }
+    if (created) {
+        unsigned long long slot = append_slots(a.c, 2);
+        if (slot + 1 < a.s.cap) {
+            unsigned long long prim = a.s.primary[L.slot];
+            d4 unpol = d4{1.0, 0.0, 0.0, 0.0};
+            d4 rest = d4{1.0, 0.0, 0.0, 0.0};
+            spawn(a, slot, SP_ELECTRON, r, ue, rest, unpol, frac * L.weight, a_eff, chi, 0.5 * absorption, L.id, prim,
+                  child_stream(L.stream, L.step, 1), L.gen + 1);
+            spawn(a, slot + 1, SP_POSITRON, r, up, rest, unpol, frac * L.weight, a_eff, chi, 0.5 * absorption, L.id,
+                  prim, child_stream(L.stream, L.step, 2), L.gen + 1);
+        } else {
+            atomicAdd(&a.c->overflow, 2ull);
+        }
+        ++*npair;
+        if (frac == 1.0)
+            L.decayed = true;
+        else
+            L.weight = L.weight * (1.0 - frac);
+    }
+    if (a.o.rotate_stokes && a.o.pol_resolved) L.pol = pol_new;
+    L.icount += prob;
+    L.r = r;
+}
+
+__device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
+    unsigned long long i = a.lo + atomicAdd(&a.c->next, 1ull);
+    if (i >= a.hi) return false;
+    const Store& s = a.s;
+    L.slot = i;
+    L.r = get4(s.r, s.cap, i);
+    L.u = get4(s.u, s.cap, i);
+    L.pol = get4(s.pol, s.cap, i);
+    L.weight = s.weight[i];
+    L.icount = s.icount[i];
+    L.work = s.work[i];
+    L.stream = s.stream[i];
+    L.id = s.id[i];
+    L.species = s.species[i];
+    L.gen = s.generation[i];
+    L.status = s.status[i];
+    L.flags = s.flags[i];
+    L.step = 0;
+    L.decayed = false;
+    return true;
+}
+
+__device__ __forceinline__ void lane_store(const WaveArgs& a, Lane& L) {
+    const Store& s = a.s;
+    unsigned long long i = L.slot;
+    put4(s.r, s.cap, i, L.r);
+    put4(s.u, s.cap, i, L.u);
+    put4(s.pol, s.cap, i, L.pol);
+    s.weight[i] = L.weight;
+    s.icount[i] = L.icount;
+    s.work[i] = L.work;
+    s.status[i] = L.status;
+    s.flags[i] = L.flags;
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
+    Lane L;
+    uint32_t rej = 0, nemit = 0, npair = 0;
+    unsigned long long lsteps = 0, psteps = 0, nerr = 0;
+    bool have = lane_load(a, L);
+    while (have) {
+        bool done;
+        if (L.status != ST_OK || lane_untracked(a, L)) {
+            done = true;
+        } else if (L.species != SP_PHOTON) {
+            done = !(contains(a.f, L.r) && L.r.t / SPEED_OF_LIGHT < a.o.t_stop);
+            if (!done) {
+                lepton_step<MODEL>(a, L, &rej, &nemit);
+                ++L.step;
+                ++lsteps;
+                done = L.status != ST_OK;
+            }
+        } else {
+            done = !(contains(a.f, L.r) && L.r.t / SPEED_OF_LIGHT < a.o.t_stop && !L.decayed && a.o.tracking_photons);
+            if (!done) {
+                photon_step<MODEL>(a, L, &rej, &npair);
+                ++L.step;
+                ++psteps;
+                done = L.status != ST_OK;
+            }
+        }
+        if (done) {
+            if (L.status != ST_OK) ++nerr;
+            // a decayed photon leaves the output, or becomes an intermediate
+            if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
+            lane_store(a, L);
+            have = lane_load(a, L);
+        }
+    }
+    // warp reduction of the counters: one atomic per warp
+    __syncwarp();
+    const unsigned m = 0xffffffffu;
+    for (int o = 16; o > 0; o >>= 1) {
+        lsteps += __shfl_down_sync(m, lsteps, o);
+        psteps += __shfl_down_sync(m, psteps, o);
+        nerr += __shfl_down_sync(m, nerr, o);
+        rej += __shfl_down_sync(m, rej, o);
+        nemit += __shfl_down_sync(m, nemit, o);
+        npair += __shfl_down_sync(m, npair, o);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&a.c->lepton_steps, lsteps);
+        atomicAdd(&a.c->photon_steps, psteps);
+        atomicAdd(&a.c->errors, nerr);
+        atomicAdd(&a.c->rejections, (unsigned long long)rej);
+        atomicAdd(&a.c->emissions, (unsigned long long)nemit);
+        atomicAdd(&a.c->pair_events, (unsigned long long)npair);
+    }
+}
+
+}  // namespace ptg

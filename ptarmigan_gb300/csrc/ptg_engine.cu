@@ -1,0 +1,1006 @@
+// Host side of the engine and the extern "C" boundary declared in
+// include/ptarmigan_gb300.h.
+//
+// A batch runs as:  primaries (row-major, host or device) -> shower store
+// (SoA) -> waves of collide_wave until no particle is left to track ->
+// per-shower filters of main.rs:271-282 -> compaction into row-major
+// output arrays.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <dlfcn.h>
+#include <string>
+#include <vector>
+
+#include "../../include/ptarmigan_gb300.h"
+#include "ptg_collide.cuh"
+
+using namespace ptg;
+
+static thread_local std::string g_last_error;
+
+static ptg_status set_err(ptg_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define CUDA_TRY(expr)                                                                           \
+    do {                                                                                         \
+        cudaError_t _e = (expr);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return set_err(PTG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+    } while (0)
+
+struct ptg_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int block = 128;
+    int blocks_per_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // shower store
+    Store s{};
+    void* store_mem = nullptr;
+    unsigned long long cap = 0;
+    // row-major output (device) of the last batch
+    void* out_mem = nullptr;
+    unsigned long long out_cap = 0;
+    ptg_particles d_out{};
+    // staging for host primaries (row-major)
+    void* in_mem = nullptr;
+    unsigned long long in_cap = 0;
+    ptg_particles d_in{};
+    // primaries' initial momenta for the angle filter, per-shower counts
+    double* init_u = nullptr;
+    unsigned long long* shower_count = nullptr;
+    unsigned long long init_cap = 0;
+    Counters* counters = nullptr;
+    Counters* h_counters = nullptr;  // pinned
+    PairGL* gl = nullptr;
+    LmaTables* lma_dev = nullptr;
+    LmaTables lma_host{};
+    std::vector<void*> table_bufs;
+    bool tables_loaded = false;
+};
+
+// ------------------------------------------------------------ helpers ---
+static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
+    FieldParams f{};
+    f.model = d.model;
+    f.circular = d.polarization == PTG_POL_CIRCULAR;
+    f.envelope = d.envelope;
+    f.finite_bandwidth = d.finite_bandwidth;
+    f.a0 = d.a0;
+    f.k = 2.0 * PI / d.wavelength;
+    f.omega = SPEED_OF_LIGHT * f.k;
+    f.duration = d.n_cycles * d.wavelength / SPEED_OF_LIGHT;
+    bool focused = d.model == PTG_FOCUSED_LASER || d.model == PTG_FAST_FOCUSED_LASER;
+    bool lcfa = d.model == PTG_FAST_PLANE_WAVE || d.model == PTG_FAST_FOCUSED_LASER;
+    f.n_cycles = focused ? SPEED_OF_LIGHT * f.duration * f.k / (2.0 * PI) : d.n_cycles;
+    f.waist = d.waist;
+    f.zr = 0.5 * f.k * d.waist * d.waist;
+    f.eps = d.waist / f.zr;
+    f.pol_angle = (lcfa && f.circular) ? 0.0 : d.pol_angle;
+    f.cos_pa = std::cos(f.pol_angle);
+    f.sin_pa = std::sin(f.pol_angle);
+    f.chirp_b = focused ? 0.0 : d.chirp_b;
+    f.E0 = ELECTRON_MASS * SPEED_OF_LIGHT * f.omega * d.a0 / ELEMENTARY_CHARGE;
+    f.B0 = f.E0 / SPEED_OF_LIGHT;
+    f.amp = (ELECTRON_MASS * SPEED_OF_LIGHT_SQD * f.k * d.a0) / ELEMENTARY_CHARGE;
+    double nc = f.n_cycles;
+    f.max_phase = d.envelope == PTG_ENV_COS2 ? PI * nc : (d.envelope == PTG_ENV_FLATTOP ? PI * (nc + 1.0) : 6.0 * PI * nc);
+    f.bandwidth = 0.0;
+    if (!lcfa && d.finite_bandwidth) {
+        double n_fwhm = d.envelope == PTG_ENV_COS2 ? 0.36405666377387671305 * nc : nc;
+        f.bandwidth = std::sqrt(0.5 * LN_2) / (PI * n_fwhm);
+    }
+    // Gaussian LCFA focused envelope exp(-2 ln2 phi^2 / tau^2) < 1e-300
+    // beyond |phi| = tau sqrt(300 ln 10 / (2 ln 2)); there E and B are zero
+    // in FP64 to every bit that reaches u.
+    f.env_cut = 0.0;
+    if (d.model == PTG_FAST_FOCUSED_LASER && d.envelope == PTG_ENV_GAUSSIAN) {
+        double tau = f.omega * f.duration;
+        f.env_cut = tau * std::sqrt(300.0 * std::log(10.0) / (2.0 * LN_2));
+    }
+    // Field::max_timestep
+    double dt;
+    switch (d.model) {
+        case PTG_PLANE_WAVE: dt = (d.envelope == PTG_ENV_FLATTOP ? 0.2 : 1.0) / (SPEED_OF_LIGHT * f.k); break;
+        case PTG_FOCUSED_LASER: dt = (d.envelope == PTG_ENV_FLATTOP ? 0.2 : 1.0) / f.omega; break;
+        case PTG_FAST_PLANE_WAVE: {
+            double chirp = 1.0 + 2.0 * d.chirp_b * PI * d.n_cycles;
+            dt = 1.0 / (SPEED_OF_LIGHT * f.k * chirp) * std::fmin(SQRT_3 / (5.0 * ALPHA_FINE * d.a0), 0.1);
+            break;
+        }
+        default: dt = 1.0 / f.omega * std::fmin(SQRT_3 / (5.0 * ALPHA_FINE * d.a0), 0.1);
+    }
+    *dt_max = dt;
+    return f;
+}
+
+static ptg_status check_laser(const ptg_laser_desc* d) {
+    if (!d) return set_err(PTG_ERR_INVALID_ARGUMENT, "laser is NULL");
+    if (d->model < 0 || d->model > 3) return set_err(PTG_ERR_INVALID_ARGUMENT, "unknown field model");
+    if (d->envelope < 0 || d->envelope > 2) return set_err(PTG_ERR_INVALID_ARGUMENT, "unknown envelope");
+    if (!(d->a0 > 0.0) || !(d->wavelength > 0.0) || !(d->n_cycles > 0.0))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "a0, wavelength and n_cycles must be positive");
+    bool focused = d->model == PTG_FOCUSED_LASER || d->model == PTG_FAST_FOCUSED_LASER;
+    if (focused && !(d->waist > 0.0 && std::isfinite(d->waist)))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "focused lasers need a finite waist");
+    if (d->envelope == PTG_ENV_FLATTOP && d->n_cycles < 1.0)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "'n_cycles' must be >= 1.0 for flattop lasers");
+    return PTG_OK;
+}
+
+// ------------------------------------------------------------ kernels ---
+__global__ void k_load_primaries(Store s, ptg_particles in, unsigned long long n, unsigned long long id_base,
+                                 double* init_u, unsigned long long* shower_count) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long cap = s.cap;
+    d4 r = d4{in.r[4 * i], in.r[4 * i + 1], in.r[4 * i + 2], in.r[4 * i + 3]};
+    d4 u = d4{in.u[4 * i], in.u[4 * i + 1], in.u[4 * i + 2], in.u[4 * i + 3]};
+    int sp = in.species[i];
+    put4(s.r, cap, i, r);
+    put4(s.u, cap, i, u);
+    put4(s.r0, cap, i, in.r0 ? d4{in.r0[4 * i], in.r0[4 * i + 1], in.r0[4 * i + 2], in.r0[4 * i + 3]} : r);
+    d4 u0 = sp == SP_PHOTON ? d4{0, 0, 0, 0} : d4{1, 0, 0, 0};
+    if (in.u0) u0 = d4{in.u0[4 * i], in.u0[4 * i + 1], in.u0[4 * i + 2], in.u0[4 * i + 3]};
+    put4(s.u0, cap, i, u0);
+    put4(s.pol, cap, i, in.pol ? d4{in.pol[4 * i], in.pol[4 * i + 1], in.pol[4 * i + 2], in.pol[4 * i + 3]} : d4{1, 0, 0, 0});
+    s.weight[i] = in.weight ? in.weight[i] : 1.0;
+    s.payload[i] = 0.0;
+    s.parent_chi[i] = 0.0;
+    s.icount[i] = 0.0;
+    s.work[i] = 0.0;
+    unsigned long long id = in.id ? in.id[i] : i;
+    s.id[i] = id;
+    s.parent_id[i] = in.parent_id ? in.parent_id[i] : id;
+    s.primary[i] = i;
+    s.stream[i] = primary_stream(id_base + i);
+    s.species[i] = sp;
+    s.generation[i] = 0;
+    s.flags[i] = 0;
+    s.status[i] = (sp < 0 || sp > 2) ? 1 : ST_OK;
+    init_u[4 * i] = u.t, init_u[4 * i + 1] = u.x, init_u[4 * i + 2] = u.y, init_u[4 * i + 3] = u.z;
+    shower_count[i] = 0;
+}
+
+struct FilterArgs {
+    Store s;
+    const double* init_u;
+    unsigned long long* shower_count;
+    unsigned long long n;
+    double min_energy, cos_max_angle;
+    int discard_bg_e, discard_bg_ph, multiplicity;
+};
+
+__device__ __forceinline__ bool filter_keep(const FilterArgs& a, unsigned long long i, bool* counted) {
+    const Store& s = a.s;
+    int fl = s.flags[i];
+    *counted = false;
+    if (fl & FLAG_DROP) return false;
+    if (fl & FLAG_INTERMEDIATE) return true;
+    int gen = s.generation[i], sp = s.species[i];
+    // main.rs:202-204 and :258-260: background primaries
+    if (gen == 0 && sp != SP_PHOTON && a.discard_bg_e && !(s.icount[i] > 0.0)) return false;
+    if (gen == 0 && sp == SP_PHOTON && a.discard_bg_ph) return false;
+    if (s.status[i] != ST_OK) return true;
+    // main.rs:271-276
+    unsigned long long p = s.primary[i];
+    d3 n0 = normalize(mk3(a.init_u[4 * p + 1], a.init_u[4 * p + 2], a.init_u[4 * p + 3]));
+    d4 u = get4(s.u, s.cap, i);
+    d3 n = normalize(mk3(u.x, u.y, u.z));
+    bool keep = ELECTRON_MASS_MEV * u.t > a.min_energy && dot(n0, n) > a.cos_max_angle;
+    *counted = keep;
+    return keep;
+}
+
+__global__ void k_filter_count(FilterArgs a) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    bool counted;
+    filter_keep(a, i, &counted);
+    if (counted) atomicAdd(&a.shower_count[a.s.primary[i]], 1ull);
+}
+
+__global__ void k_compact(FilterArgs a, Counters* c, ptg_particles o, unsigned long long out_cap) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool keep = false;
+    if (i < a.n) {
+        bool counted;
+        keep = filter_keep(a, i, &counted);
+        // main.rs:278-283: multiplicity selection drops whole showers
+        if (keep && a.multiplicity >= 0 && !(a.s.flags[i] & FLAG_INTERMEDIATE) &&
+            a.shower_count[a.s.primary[i]] != (unsigned long long)a.multiplicity + 1)
+            keep = false;
+    }
+    unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (ballot == 0) return;
+    unsigned lane = threadIdx.x & 31u;
+    unsigned leader = __ffs(ballot) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&c->n_out, (unsigned long long)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!keep) return;
+    unsigned long long j = base + __popc(ballot & ((1u << lane) - 1u));
+    if (j >= out_cap) return;
+    const Store& s = a.s;
+    unsigned long long cap = s.cap;
+    for (int k = 0; k < 4; ++k) {
+        o.r[4 * j + k] = s.r[k * cap + i];
+        o.u[4 * j + k] = s.u[k * cap + i];
+        o.r0[4 * j + k] = s.r0[k * cap + i];
+        o.u0[4 * j + k] = s.u0[k * cap + i];
+        o.pol[4 * j + k] = s.pol[k * cap + i];
+    }
+    o.species[j] = s.species[i];
+    o.weight[j] = s.weight[i];
+    o.payload[j] = s.payload[i];
+    o.parent_chi[j] = s.parent_chi[i];
+    o.interaction_count[j] = s.icount[i];
+    o.work[j] = s.work[i];
+    o.id[j] = s.id[i];
+    o.parent_id[j] = s.parent_id[i];
+    o.primary[j] = s.primary[i];
+    o.stream[j] = s.stream[i];
+    o.generation[j] = s.generation[i];
+    o.flags[j] = s.flags[i];
+    o.status[j] = s.status[i];
+}
+
+__global__ void k_sum_work(Store s, unsigned long long n, double* out) {
+    double acc = 0.0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        acc += s.work[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31u) == 0) atomicAdd(out, acc);
+}
+
+// -------------------------------------------------------- diagnostics ---
+__global__ void k_eval_fields(FieldParams f, unsigned long long n, const double* r, double* E, double* B, double* a) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d4 rr = d4{r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]};
+    d3 e, b;
+    double aa;
+    if (f.model == M_FAST_PLANE_WAVE || f.model == M_FAST_FOCUSED_LASER) {
+        lcfa_fields(f, rr, &e, &b, &aa);
+    } else {
+        e = mk3(0, 0, 0);
+        b = mk3(0, 0, 0);
+        aa = sqrt(lma_a_sqd(f, rr));
+    }
+    E[3 * i] = e.x, E[3 * i + 1] = e.y, E[3 * i + 2] = e.z;
+    B[3 * i] = b.x, B[3 * i + 1] = b.y, B[3 * i + 2] = b.z;
+    a[i] = aa;
+}
+
+__global__ void k_push_steps(FieldParams f, unsigned long long n, double* r, double* u, double rqm, double dt, int eqn,
+                             int nsteps, double* work) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    d4 rr = d4{r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]};
+    d4 uu = d4{u[4 * i], u[4 * i + 1], u[4 * i + 2], u[4 * i + 3]};
+    double w = 0.0;
+    bool lcfa = f.model == M_FAST_PLANE_WAVE || f.model == M_FAST_FOCUSED_LASER;
+    for (int s = 0; s < nsteps; ++s) {
+        d4 ro, uo;
+        double dw, dto;
+        if (lcfa) {
+            double h = 0.5 * SPEED_OF_LIGHT * dt / uu.t;
+            d4 rh = d4{rr.t + h * uu.t, rr.x + h * uu.x, rr.y + h * uu.y, rr.z + h * uu.z};
+            d3 E, B;
+            double aa;
+            lcfa_fields(f, rh, &E, &B, &aa);
+            vay_push(rh, uu, E, B, rqm, dt, eqn, [](double c) { return gaunt_factor(c); }, &ro, &uo, &dw);
+        } else {
+            lma_push(f, rr, uu, rqm, dt, eqn, &ro, &uo, &dto, &dw);
+        }
+        rr = ro;
+        uu = uo;
+        w += dw;
+    }
+    r[4 * i] = rr.t, r[4 * i + 1] = rr.x, r[4 * i + 2] = rr.y, r[4 * i + 3] = rr.z;
+    u[4 * i] = uu.t, u[4 * i + 1] = uu.x, u[4 * i + 2] = uu.y, u[4 * i + 3] = uu.z;
+    if (work) work[i] = w;
+}
+
+__global__ void k_photon_rate(unsigned long long n, const double* chi, const double* gamma, double* rate) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) rate[i] = lcfa_photon_rate(chi[i], gamma[i]);
+}
+
+__global__ void k_photon_sample(unsigned long long n, const double* chi, const double* gamma, const double* rand3,
+                                double* omega, double* theta) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) lcfa_photon_sample(chi[i], gamma[i], rand3[3 * i], rand3[3 * i + 1], rand3[3 * i + 2], &omega[i], &theta[i]);
+}
+
+__global__ void k_pair_t(unsigned long long n, const double* chi, double* tpar, double* tperp) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) lcfa_auxiliary_t(chi[i], &tpar[i], &tperp[i]);
+}
+
+// ---------------------------------------------------------- storage -----
+static void carve_store(Store* s, void* mem, unsigned long long cap) {
+    char* p = (char*)mem;
+    auto take = [&](size_t bytes) {
+        char* q = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return (void*)q;
+    };
+    s->cap = cap;
+    s->r = (double*)take(32 * cap);
+    s->u = (double*)take(32 * cap);
+    s->r0 = (double*)take(32 * cap);
+    s->u0 = (double*)take(32 * cap);
+    s->pol = (double*)take(32 * cap);
+    s->weight = (double*)take(8 * cap);
+    s->payload = (double*)take(8 * cap);
+    s->parent_chi = (double*)take(8 * cap);
+    s->icount = (double*)take(8 * cap);
+    s->work = (double*)take(8 * cap);
+    s->id = (unsigned long long*)take(8 * cap);
+    s->parent_id = (unsigned long long*)take(8 * cap);
+    s->primary = (unsigned long long*)take(8 * cap);
+    s->stream = (unsigned long long*)take(8 * cap);
+    s->species = (int*)take(4 * cap);
+    s->generation = (int*)take(4 * cap);
+    s->flags = (int*)take(4 * cap);
+    s->status = (int*)take(4 * cap);
+}
+
+static size_t particles_bytes(unsigned long long cap) {
+    // 5 four-vectors, 5 doubles, 4 u64, 5 i32, each padded to 256 B
+    return (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 5 * 4) * cap + 19 * 256;
+}
+
+static void carve_particles(ptg_particles* p, void* mem, unsigned long long cap) {
+    char* q = (char*)mem;
+    auto take = [&](size_t bytes) {
+        char* t = q;
+        q += (bytes + 255) & ~(size_t)255;
+        return (void*)t;
+    };
+    p->n = 0;
+    p->r = (double*)take(32 * cap);
+    p->u = (double*)take(32 * cap);
+    p->r0 = (double*)take(32 * cap);
+    p->u0 = (double*)take(32 * cap);
+    p->pol = (double*)take(32 * cap);
+    p->weight = (double*)take(8 * cap);
+    p->payload = (double*)take(8 * cap);
+    p->parent_chi = (double*)take(8 * cap);
+    p->interaction_count = (double*)take(8 * cap);
+    p->work = (double*)take(8 * cap);
+    p->id = (uint64_t*)take(8 * cap);
+    p->parent_id = (uint64_t*)take(8 * cap);
+    p->primary = (uint64_t*)take(8 * cap);
+    p->stream = (uint64_t*)take(8 * cap);
+    p->species = (int32_t*)take(4 * cap);
+    p->generation = (int32_t*)take(4 * cap);
+    p->flags = (int32_t*)take(4 * cap);
+    p->status = (int32_t*)take(4 * cap);
+}
+
+static ptg_status ensure_store(ptg_ctx* c, unsigned long long cap) {
+    if (c->cap >= cap) return PTG_OK;
+    if (c->store_mem) cudaFree(c->store_mem);
+    c->store_mem = nullptr;
+    c->cap = 0;
+    size_t bytes = (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 4 * 4) * cap + 18 * 256;
+    if (cudaMalloc(&c->store_mem, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "could not allocate the shower store (" + std::to_string(bytes) + " bytes)");
+    }
+    carve_store(&c->s, c->store_mem, cap);
+    c->cap = cap;
+    return PTG_OK;
+}
+
+static ptg_status ensure_out(ptg_ctx* c, unsigned long long cap) {
+    if (c->out_cap >= cap) return PTG_OK;
+    if (c->out_mem) cudaFree(c->out_mem);
+    c->out_mem = nullptr;
+    c->out_cap = 0;
+    size_t bytes = particles_bytes(cap);
+    if (cudaMalloc(&c->out_mem, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "could not allocate the output buffers");
+    }
+    carve_particles(&c->d_out, c->out_mem, cap);
+    c->out_cap = cap;
+    return PTG_OK;
+}
+
+static ptg_status ensure_init(ptg_ctx* c, unsigned long long n) {
+    if (c->init_cap >= n) return PTG_OK;
+    if (c->init_u) cudaFree(c->init_u);
+    if (c->shower_count) cudaFree(c->shower_count);
+    c->init_u = nullptr;
+    c->shower_count = nullptr;
+    c->init_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->init_u, 32 * n));
+    CUDA_TRY(cudaMalloc(&c->shower_count, 8 * n));
+    c->init_cap = n;
+    return PTG_OK;
+}
+
+// ----------------------------------------------------------- tables -----
+static bool read_ptgt(const std::string& path, std::vector<double>* data, std::vector<uint32_t>* shape) {
+    FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) return false;
+    char magic[4];
+    uint32_t nd = 0;
+    bool ok = std::fread(magic, 1, 4, fp) == 4 && std::memcmp(magic, "PTGT", 4) == 0 && std::fread(&nd, 4, 1, fp) == 1 &&
+              nd > 0 && nd < 8;
+    size_t n = 1;
+    if (ok) {
+        shape->resize(nd);
+        ok = std::fread(shape->data(), 4, nd, fp) == nd;
+        for (uint32_t d : *shape) n *= d;
+    }
+    if (ok) {
+        data->resize(n);
+        ok = std::fread(data->data(), 8, n, fp) == n;
+    }
+    std::fclose(fp);
+    return ok;
+}
+
+static std::string default_table_dir() {
+    Dl_info info;
+    if (dladdr((void*)&default_table_dir, &info) && info.dli_fname) {
+        std::string p(info.dli_fname);
+        size_t slash = p.rfind('/');
+        std::string dir = slash == std::string::npos ? "." : p.substr(0, slash);
+        // the library lives in ptarmigan_gb300/_build/; tables in ptarmigan_gb300/tables/data
+        return dir + "/../tables/data";
+    }
+    return "ptarmigan_gb300/tables/data";
+}
+
+// -------------------------------------------------------------- ABI -----
+// Definitions below inherit C linkage from their declarations in
+// include/ptarmigan_gb300.h.
+
+int ptg_abi_version(void) { return PTG_ABI_VERSION; }
+
+const char* ptg_status_string(ptg_status s) {
+    switch (s) {
+        case PTG_OK: return "ok";
+        case PTG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PTG_ERR_OUT_OF_TABLE: return "lookup outside the rate/CDF table";
+        case PTG_ERR_SANITY: return "kinematics sanity check failed";
+        case PTG_ERR_REJECTION_CAP: return "rejection loop reached its iteration cap";
+        case PTG_ERR_QUEUE_OVERFLOW: return "shower store overflow";
+        case PTG_ERR_CUDA: return "CUDA error";
+        case PTG_ERR_NO_DEVICE: return "no CUDA device";
+        case PTG_ERR_TABLES: return "tables missing or malformed";
+        case PTG_ERR_UNSUPPORTED: return "unsupported option combination";
+        case PTG_ERR_ALLOC: return "device allocation failed";
+    }
+    return "unknown status";
+}
+
+const char* ptg_last_error(void) { return g_last_error.c_str(); }
+
+ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out) {
+    if (!out) return set_err(PTG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    ptg_ctx* c = new ptg_ctx;
+    c->device = cfg ? cfg->device : 0;
+    if (c->device < 0 || c->device >= ndev) {
+        delete c;
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
+    c->num_sms = prop.multiProcessorCount;
+    if (cfg && cfg->block_size > 0) c->block = cfg->block_size;
+    if (cfg && cfg->blocks_per_sm > 0) c->blocks_per_sm = cfg->blocks_per_sm;
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&c->ev0));
+    CUDA_TRY(cudaEventCreate(&c->ev1));
+    CUDA_TRY(cudaMalloc(&c->counters, sizeof(Counters)));
+    CUDA_TRY(cudaMallocHost(&c->h_counters, sizeof(Counters)));
+    // Gauss-Laguerre node constants of the pair spectrum
+    PairGL gl;
+    double nodes[32], weights[32];
+    CUDA_TRY(cudaMemcpyFromSymbol(nodes, PTG_GL_NODES, sizeof(nodes)));
+    CUDA_TRY(cudaMemcpyFromSymbol(weights, PTG_GL_WEIGHTS, sizeof(weights)));
+    for (int k = 0; k < 32; ++k) {
+        double t = nodes[k];
+        gl.w[k] = weights[k];
+        gl.t[k] = t;
+        gl.c23[k] = std::cosh(2.0 * t / 3.0);
+        gl.c13_over_c1[k] = std::cosh(t / 3.0) / std::cosh(t);
+        gl.c1[k] = std::cosh(t);
+    }
+    CUDA_TRY(cudaMalloc(&c->gl, sizeof(PairGL)));
+    CUDA_TRY(cudaMemcpy(c->gl, &gl, sizeof(PairGL), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&c->lma_dev, sizeof(LmaTables)));
+    CUDA_TRY(cudaMemset(c->lma_dev, 0, sizeof(LmaTables)));
+    size_t init = cfg && cfg->initial_capacity ? cfg->initial_capacity : (1u << 20);
+    ptg_status st = ensure_store(c, init);
+    if (st != PTG_OK) {
+        ptg_context_destroy(c);
+        return st;
+    }
+    *out = c;
+    return PTG_OK;
+}
+
+ptg_status ptg_context_destroy(ptg_ctx* c) {
+    if (!c) return PTG_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->store_mem);
+    cudaFree(c->out_mem);
+    cudaFree(c->in_mem);
+    cudaFree(c->init_u);
+    cudaFree(c->shower_count);
+    cudaFree(c->counters);
+    cudaFreeHost(c->h_counters);
+    cudaFree(c->gl);
+    cudaFree(c->lma_dev);
+    for (void* p : c->table_bufs) cudaFree(p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PTG_OK;
+}
+
+void* ptg_context_stream(ptg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    std::string d = dir ? dir : default_table_dir();
+    struct Want {
+        const char* name;
+        const double** slot;
+        size_t count;
+        bool required;
+    } wants[] = {
+        {"nlc_lp_rate", &c->lma_host.nlc_lp_rate, 68 * 61, true},
+        {"nlc_lp_cdf", &c->lma_host.nlc_lp_cdf, 4148 * 16 * 2, true},
+        {"nlc_cp_rate", &c->lma_host.nlc_cp_rate, 70 * 61, true},
+        {"nlc_cp_cdf", &c->lma_host.nlc_cp_cdf, 4270 * 32 * 2, false},
+        {"bw_cp_total", &c->lma_host.bw_cp_total, 121 * 74 * 2, true},
+        {"bw_lp_total", &c->lma_host.bw_lp_total, 61 * 25 * 2, true},
+        {"bw_lp_cdf", &c->lma_host.bw_lp_cdf, 1525 * 16 * 3, true},
+        {"bw_lp_mid_total", &c->lma_host.bw_lp_mid_total, 157 * 36 * 2, true},
+        {"bw_lp_mid_cdf", &c->lma_host.bw_lp_mid_cdf, 5652 * 16 * 3, false},
+    };
+    CUDA_TRY(cudaSetDevice(c->device));
+    for (auto& w : wants) {
+        std::vector<double> data;
+        std::vector<uint32_t> shape;
+        std::string path = d + "/" + w.name + ".ptgt";
+        if (!read_ptgt(path, &data, &shape)) {
+            if (w.required) return set_err(PTG_ERR_TABLES, "cannot read table " + path);
+            *w.slot = nullptr;
+            continue;
+        }
+        if (data.size() != w.count) return set_err(PTG_ERR_TABLES, "table " + path + " has the wrong size");
+        void* p = nullptr;
+        CUDA_TRY(cudaMalloc(&p, 8 * data.size()));
+        CUDA_TRY(cudaMemcpy(p, data.data(), 8 * data.size(), cudaMemcpyHostToDevice));
+        c->table_bufs.push_back(p);
+        *w.slot = (const double*)p;
+    }
+    CUDA_TRY(cudaMemcpy(c->lma_dev, &c->lma_host, sizeof(LmaTables), cudaMemcpyHostToDevice));
+    c->tables_loaded = true;
+    return PTG_OK;
+}
+
+ptg_status ptg_laser_timestep(const ptg_laser_desc* laser, double* dt) {
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    make_field(*laser, dt);
+    return PTG_OK;
+}
+
+ptg_status ptg_laser_initial_z(const ptg_laser_desc* d, double* z0) {
+    ptg_status st = check_laser(d);
+    if (st != PTG_OK) return st;
+    double dt;
+    FieldParams f = make_field(*d, &dt);
+    double wl = 2.0 * PI / f.k;
+    double nc = f.n_cycles;
+    *z0 = d->envelope == PTG_ENV_COS2 ? 0.5 * wl * nc : (d->envelope == PTG_ENV_FLATTOP ? 0.5 * wl * (nc + 1.0) : 2.0 * wl * nc);
+    return PTG_OK;
+}
+
+static int grid_for(ptg_ctx* c, const void* kernel) {
+    int per_sm = c->blocks_per_sm;
+    if (per_sm <= 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, c->block, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    return per_sm * c->num_sms;
+}
+
+template <int MODEL>
+static cudaError_t launch_wave(ptg_ctx* c, const WaveArgs& a) {
+    int grid = grid_for(c, (const void*)collide_wave<MODEL>);
+    unsigned long long n = a.hi - a.lo;
+    unsigned long long need = (n + c->block - 1) / c->block;
+    if ((unsigned long long)grid > need) grid = (int)need;
+    if (grid < 1) grid = 1;
+    collide_wave<MODEL><<<grid, c->block, 0, c->stream>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
+    switch (a.f.model) {
+        case M_PLANE_WAVE: return launch_wave<M_PLANE_WAVE>(c, a);
+        case M_FAST_PLANE_WAVE: return launch_wave<M_FAST_PLANE_WAVE>(c, a);
+        case M_FOCUSED_LASER: return launch_wave<M_FOCUSED_LASER>(c, a);
+        default: return launch_wave<M_FAST_FOCUSED_LASER>(c, a);
+    }
+}
+
+// Runs a batch whose primaries are described by device pointers `d_in`.
+static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
+                            const ptg_particles* d_in, uint64_t seed, uint64_t id_base, ptg_run_stats* stats) {
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    if (!o) return set_err(PTG_ERR_INVALID_ARGUMENT, "options is NULL");
+    if (!d_in || !d_in->species || !d_in->r || !d_in->u)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
+    bool lcfa = laser->model == PTG_FAST_PLANE_WAVE || laser->model == PTG_FAST_FOCUSED_LASER;
+    if (o->gaunt_factor && !lcfa)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "Gaunt factor correction is only available under the LCFA");
+    if (!(o->rate_increase >= 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "increase in pair creation rate must be >= 1.0");
+    if (o->rate_increase > 1.0 && o->multiplicity >= 0)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "event biasing is incompatible with multiplicity selection");
+    if (!lcfa && !c->tables_loaded) {
+        st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    unsigned long long n = d_in->n;
+    double dt_max;
+    FieldParams f = make_field(*laser, &dt_max);
+    WaveArgs a{};
+    a.f = f;
+    a.o.dt = dt_max * o->dt_multiplier;
+    a.o.t_stop = o->t_stop;
+    a.o.rate_increase = o->rate_increase;
+    a.o.eqn = (o->classical && o->rr) ? (o->gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
+    a.o.classical_mode = o->classical && !o->gaunt_factor;
+    a.o.classical = o->classical;
+    a.o.electron_recoils = !o->classical && o->rr;
+    a.o.tracking_photons = o->tracking_photons;
+    a.o.pol_resolved = o->pol_resolved;
+    a.o.rotate_stokes = o->rotate_stokes_pars;
+    a.o.tracking_secondaries = o->tracking_secondaries;
+    a.o.max_generation = o->max_generation;
+    a.o.keep_decayed = o->keep_decayed_photons;
+    a.gl = c->gl;
+    a.lma = c->lma_dev;
+    a.seed = seed;
+    a.n_primaries = n;
+    a.id_base = id_base;
+    unsigned long long want = c->cap;
+    if (want < 8 * n + 1024) want = 8 * n + 1024;
+    st = ensure_init(c, n > 0 ? n : 1);
+    if (st != PTG_OK) return st;
+    CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        st = ensure_store(c, want);
+        if (st != PTG_OK) return st;
+        a.s = c->s;
+        a.c = c->counters;
+        CUDA_TRY(cudaMemsetAsync(c->counters, 0, sizeof(Counters), c->stream));
+        unsigned long long nt = n;
+        CUDA_TRY(cudaMemcpyAsync(&c->counters->n_total, &nt, 8, cudaMemcpyHostToDevice, c->stream));
+        if (n > 0) {
+            k_load_primaries<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->s, *d_in, n, id_base, c->init_u,
+                                                                                c->shower_count);
+            CUDA_TRY(cudaGetLastError());
+        }
+        unsigned long long lo = 0, hi = n;
+        uint32_t waves = 0;
+        bool overflow = false;
+        while (lo < hi) {
+            a.lo = lo;
+            a.hi = hi;
+            CUDA_TRY(cudaMemsetAsync(&c->counters->next, 0, 8, c->stream));
+            CUDA_TRY(launch_wave_model(c, a));
+            ++waves;
+            CUDA_TRY(cudaMemcpyAsync(c->h_counters, c->counters, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+            CUDA_TRY(cudaStreamSynchronize(c->stream));
+            if (c->h_counters->overflow) {
+                overflow = true;
+                break;
+            }
+            lo = hi;
+            hi = c->h_counters->n_total;
+        }
+        if (overflow) {
+            // deterministic streams: rerunning with a larger store gives the same shower
+            want = 2 * (c->h_counters->n_total > want ? c->h_counters->n_total : want);
+            continue;
+        }
+        unsigned long long total = hi;
+        st = ensure_out(c, total > 0 ? total : 1);
+        if (st != PTG_OK) return st;
+        FilterArgs fa;
+        fa.s = c->s;
+        fa.init_u = c->init_u;
+        fa.shower_count = c->shower_count;
+        fa.n = total;
+        fa.min_energy = o->min_energy;
+        fa.cos_max_angle = std::cos(o->max_angle);
+        fa.discard_bg_e = o->discard_bg_e;
+        fa.discard_bg_ph = o->discard_bg_ph;
+        fa.multiplicity = o->multiplicity;
+        unsigned blocks = (unsigned)((total + 255) / 256);
+        if (blocks == 0) blocks = 1;
+        if (o->multiplicity >= 0) {
+            k_filter_count<<<blocks, 256, 0, c->stream>>>(fa);
+            CUDA_TRY(cudaGetLastError());
+        }
+        k_compact<<<blocks, 256, 0, c->stream>>>(fa, c->counters, c->d_out, c->out_cap);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(c->h_counters, c->counters, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        c->d_out.n = c->h_counters->n_out;
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            stats->n_primaries = n;
+            stats->n_out = c->h_counters->n_out;
+            stats->n_created = total;
+            stats->lepton_steps = c->h_counters->lepton_steps;
+            stats->photon_steps = c->h_counters->photon_steps;
+            stats->emissions = c->h_counters->emissions;
+            stats->pair_events = c->h_counters->pair_events;
+            stats->rejections = c->h_counters->rejections;
+            stats->particle_errors = c->h_counters->errors;
+            stats->waves = waves;
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+            stats->device_ms = ms;
+        }
+        return PTG_OK;
+    }
+    return set_err(PTG_ERR_QUEUE_OVERFLOW, "shower store kept overflowing");
+}
+
+ptg_status ptg_collide_batch_device(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
+                                    const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
+                                    ptg_particles* d_out, ptg_run_stats* stats) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    ptg_status st = run_batch(c, laser, o, d_primaries, seed, id_base, stats);
+    if (st != PTG_OK) return st;
+    if (d_out) *d_out = c->d_out;
+    return PTG_OK;
+}
+
+static ptg_status stage_primaries(ptg_ctx* c, const ptg_particles* h) {
+    unsigned long long n = h->n;
+    if (n > c->in_cap) {
+        if (c->in_mem) cudaFree(c->in_mem);
+        c->in_mem = nullptr;
+        c->in_cap = 0;
+        CUDA_TRY(cudaMalloc(&c->in_mem, particles_bytes(n)));
+        carve_particles(&c->d_in, c->in_mem, n);
+        c->in_cap = n;
+    }
+    ptg_particles d = c->d_in;
+    d.n = n;
+    auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) == cudaSuccess;
+    };
+    if (!h->species || !h->r || !h->u) return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
+    bool ok = up(d.species, h->species, 4 * n) && up(d.r, h->r, 32 * n) && up(d.u, h->u, 32 * n);
+    if (h->r0) ok = ok && up(d.r0, h->r0, 32 * n); else d.r0 = nullptr;
+    if (h->u0) ok = ok && up(d.u0, h->u0, 32 * n); else d.u0 = nullptr;
+    if (h->pol) ok = ok && up(d.pol, h->pol, 32 * n); else d.pol = nullptr;
+    if (h->weight) ok = ok && up(d.weight, h->weight, 8 * n); else d.weight = nullptr;
+    if (h->id) ok = ok && up(d.id, h->id, 8 * n); else d.id = nullptr;
+    if (h->parent_id) ok = ok && up(d.parent_id, h->parent_id, 8 * n); else d.parent_id = nullptr;
+    if (!ok) return set_err(PTG_ERR_CUDA, "host-to-device copy of the primaries failed");
+    c->d_in = d;
+    c->d_in.r0 = d.r0, c->d_in.u0 = d.u0;
+    return PTG_OK;
+}
+
+ptg_status ptg_collide_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
+                             const ptg_particles* primaries, uint64_t seed, uint64_t id_base, ptg_particles* out,
+                             ptg_run_stats* stats) {
+    if (!c || !primaries || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    ptg_status st = stage_primaries(c, primaries);
+    if (st != PTG_OK) return st;
+    ptg_particles din = c->d_in;
+    // restore carved pointers for the next staging (optional fields may be NULL now)
+    carve_particles(&c->d_in, c->in_mem, c->in_cap);
+    st = run_batch(c, laser, o, &din, seed, id_base, stats);
+    if (st != PTG_OK) return st;
+    size_t m = c->d_out.n;
+    std::memset(out, 0, sizeof(*out));
+    out->n = m;
+    size_t sz = m ? m : 1;
+    out->species = (int32_t*)std::malloc(4 * sz);
+    out->r = (double*)std::malloc(32 * sz);
+    out->u = (double*)std::malloc(32 * sz);
+    out->r0 = (double*)std::malloc(32 * sz);
+    out->u0 = (double*)std::malloc(32 * sz);
+    out->pol = (double*)std::malloc(32 * sz);
+    out->weight = (double*)std::malloc(8 * sz);
+    out->payload = (double*)std::malloc(8 * sz);
+    out->parent_chi = (double*)std::malloc(8 * sz);
+    out->interaction_count = (double*)std::malloc(8 * sz);
+    out->work = (double*)std::malloc(8 * sz);
+    out->id = (uint64_t*)std::malloc(8 * sz);
+    out->parent_id = (uint64_t*)std::malloc(8 * sz);
+    out->primary = (uint64_t*)std::malloc(8 * sz);
+    out->stream = (uint64_t*)std::malloc(8 * sz);
+    out->generation = (int32_t*)std::malloc(4 * sz);
+    out->flags = (int32_t*)std::malloc(4 * sz);
+    out->status = (int32_t*)std::malloc(4 * sz);
+    if (!out->species || !out->r || !out->u || !out->r0 || !out->u0 || !out->pol || !out->weight || !out->payload ||
+        !out->parent_chi || !out->interaction_count || !out->work || !out->id || !out->parent_id || !out->primary ||
+        !out->stream || !out->generation || !out->flags || !out->status) {
+        ptg_particles_free(out);
+        return set_err(PTG_ERR_ALLOC, "host allocation of the output failed");
+    }
+    const ptg_particles& d = c->d_out;
+    auto down = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+    };
+    if (m) {
+        CUDA_TRY(down(out->species, d.species, 4 * m));
+        CUDA_TRY(down(out->r, d.r, 32 * m));
+        CUDA_TRY(down(out->u, d.u, 32 * m));
+        CUDA_TRY(down(out->r0, d.r0, 32 * m));
+        CUDA_TRY(down(out->u0, d.u0, 32 * m));
+        CUDA_TRY(down(out->pol, d.pol, 32 * m));
+        CUDA_TRY(down(out->weight, d.weight, 8 * m));
+        CUDA_TRY(down(out->payload, d.payload, 8 * m));
+        CUDA_TRY(down(out->parent_chi, d.parent_chi, 8 * m));
+        CUDA_TRY(down(out->interaction_count, d.interaction_count, 8 * m));
+        CUDA_TRY(down(out->work, d.work, 8 * m));
+        CUDA_TRY(down(out->id, d.id, 8 * m));
+        CUDA_TRY(down(out->parent_id, d.parent_id, 8 * m));
+        CUDA_TRY(down(out->primary, d.primary, 8 * m));
+        CUDA_TRY(down(out->stream, d.stream, 8 * m));
+        CUDA_TRY(down(out->generation, d.generation, 4 * m));
+        CUDA_TRY(down(out->flags, d.flags, 4 * m));
+        CUDA_TRY(down(out->status, d.status, 4 * m));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (stats) {
+        double sum = 0.0;
+        for (size_t i = 0; i < m; ++i) sum += out->work[i];
+        stats->absorbed_energy = sum * ELECTRON_MASS_MEV;
+    }
+    return PTG_OK;
+}
+
+void ptg_particles_free(ptg_particles* p) {
+    if (!p) return;
+    std::free(p->species);
+    std::free(p->r);
+    std::free(p->u);
+    std::free(p->r0);
+    std::free(p->u0);
+    std::free(p->pol);
+    std::free(p->weight);
+    std::free(p->payload);
+    std::free(p->parent_chi);
+    std::free(p->interaction_count);
+    std::free(p->work);
+    std::free(p->id);
+    std::free(p->parent_id);
+    std::free(p->primary);
+    std::free(p->stream);
+    std::free(p->generation);
+    std::free(p->flags);
+    std::free(p->status);
+    std::memset(p, 0, sizeof(*p));
+}
+
+// ---------------------------------------------------- diagnostics ABI ---
+template <typename F>
+static ptg_status with_device_buffers(ptg_ctx* c, std::vector<std::pair<void*, size_t>> bufs, F f) {
+    std::vector<void*> d(bufs.size(), nullptr);
+    ptg_status st = PTG_OK;
+    for (size_t i = 0; i < bufs.size(); ++i) {
+        if (cudaMalloc(&d[i], bufs[i].second ? bufs[i].second : 8) != cudaSuccess) {
+            cudaGetLastError();
+            st = set_err(PTG_ERR_ALLOC, "diagnostic buffer allocation failed");
+            break;
+        }
+        if (bufs[i].first) cudaMemcpy(d[i], bufs[i].first, bufs[i].second, cudaMemcpyHostToDevice);
+    }
+    if (st == PTG_OK) {
+        f(d);
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) st = set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+        for (size_t i = 0; i < bufs.size() && st == PTG_OK; ++i)
+            if (bufs[i].first) cudaMemcpy(bufs[i].first, d[i], bufs[i].second, cudaMemcpyDeviceToHost);
+    }
+    for (void* p : d) cudaFree(p);
+    return st;
+}
+
+ptg_status ptg_eval_fields(ptg_ctx* c, const ptg_laser_desc* laser, size_t n, const double* r, double* E, double* B,
+                           double* a) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    double dt;
+    FieldParams f = make_field(*laser, &dt);
+    cudaSetDevice(c->device);
+    std::vector<double> rr(r, r + 4 * n);
+    return with_device_buffers(c, {{rr.data(), 32 * n}, {E, 24 * n}, {B, 24 * n}, {a, 8 * n}}, [&](std::vector<void*>& d) {
+        k_eval_fields<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(f, n, (double*)d[0], (double*)d[1],
+                                                                              (double*)d[2], (double*)d[3]);
+    });
+}
+
+ptg_status ptg_push_steps(ptg_ctx* c, const ptg_laser_desc* laser, size_t n, double* r, double* u, double rqm,
+                          double dt, int32_t eqn, int32_t nsteps, double* work) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    double dtm;
+    FieldParams f = make_field(*laser, &dtm);
+    cudaSetDevice(c->device);
+    std::vector<double> wk(n, 0.0);
+    st = with_device_buffers(c, {{r, 32 * n}, {u, 32 * n}, {wk.data(), 8 * n}}, [&](std::vector<void*>& d) {
+        k_push_steps<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(f, n, (double*)d[0], (double*)d[1], rqm, dt,
+                                                                             eqn, nsteps, (double*)d[2]);
+    });
+    if (st == PTG_OK && work) std::memcpy(work, wk.data(), 8 * n);
+    return st;
+}
+
+ptg_status ptg_lcfa_photon_rate(ptg_ctx* c, size_t n, const double* chi, const double* gamma, double* rate) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    cudaSetDevice(c->device);
+    std::vector<double> a(chi, chi + n), b(gamma, gamma + n);
+    return with_device_buffers(c, {{a.data(), 8 * n}, {b.data(), 8 * n}, {rate, 8 * n}}, [&](std::vector<void*>& d) {
+        k_photon_rate<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(n, (double*)d[0], (double*)d[1], (double*)d[2]);
+    });
+}
+
+ptg_status ptg_lcfa_photon_sample(ptg_ctx* c, size_t n, const double* chi, const double* gamma, const double* rand3,
+                                  double* omega, double* theta) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    cudaSetDevice(c->device);
+    std::vector<double> a(chi, chi + n), b(gamma, gamma + n), r(rand3, rand3 + 3 * n);
+    return with_device_buffers(c, {{a.data(), 8 * n}, {b.data(), 8 * n}, {r.data(), 24 * n}, {omega, 8 * n}, {theta, 8 * n}},
+                               [&](std::vector<void*>& d) {
+                                   k_photon_sample<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(
+                                       n, (double*)d[0], (double*)d[1], (double*)d[2], (double*)d[3], (double*)d[4]);
+                               });
+}
+
+ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_par, double* t_perp) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    cudaSetDevice(c->device);
+    std::vector<double> a(chi, chi + n);
+    return with_device_buffers(c, {{a.data(), 8 * n}, {t_par, 8 * n}, {t_perp, 8 * n}}, [&](std::vector<void*>& d) {
+        k_pair_t<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(n, (double*)d[0], (double*)d[1], (double*)d[2]);
+    });
+}
+

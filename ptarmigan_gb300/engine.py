@@ -1,0 +1,221 @@
+"""Python binding of the C ABI (``include/ptarmigan_gb300.h``).
+
+``Engine`` owns one device context.  ``collide()`` is the reference's
+collision loop over a batch (src/main.rs:1118-1135 mapping ``collide`` over
+the primaries): host arrays in, the surviving shower particles out.  There
+is no CPU path: if the library is not built or no GPU is visible the
+constructor raises.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .build import LIB_PATH
+
+_lib = None
+
+_EXPORTS = [
+    "ptg_abi_version", "ptg_status_string", "ptg_last_error", "ptg_context_create", "ptg_context_destroy",
+    "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
+    "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_eval_fields", "ptg_push_steps",
+    "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t",
+]
+
+
+class PtgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (status %d): %s" % (load().ptg_status_string(status).decode(), status, message))
+        self.status = status
+
+
+def load(path=None):
+    """Loads the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("ptarmigan_gb300 library not built (%s); run ptarmigan_gb300.build.build()" % path)
+    L = C.CDLL(path)
+    DP = C.POINTER(C.c_double)
+    st = C.c_int
+    ctxp = C.c_void_p
+    L.ptg_abi_version.restype = C.c_int
+    L.ptg_status_string.restype = C.c_char_p
+    L.ptg_status_string.argtypes = [C.c_int]
+    L.ptg_last_error.restype = C.c_char_p
+    L.ptg_context_create.restype = st
+    L.ptg_context_create.argtypes = [C.POINTER(abi.DeviceCfg), C.POINTER(C.c_void_p)]
+    L.ptg_context_destroy.restype = st
+    L.ptg_context_destroy.argtypes = [ctxp]
+    L.ptg_load_tables.restype = st
+    L.ptg_load_tables.argtypes = [ctxp, C.c_char_p]
+    for name in ("ptg_collide_batch", "ptg_collide_batch_device"):
+        f = getattr(L, name)
+        f.restype = st
+        f.argtypes = [ctxp, C.POINTER(abi.LaserDesc), C.POINTER(abi.CollideOptions), C.POINTER(abi.Particles),
+                      C.c_uint64, C.c_uint64, C.POINTER(abi.Particles), C.POINTER(abi.RunStats)]
+    L.ptg_particles_free.restype = None
+    L.ptg_particles_free.argtypes = [C.POINTER(abi.Particles)]
+    L.ptg_laser_timestep.restype = st
+    L.ptg_laser_timestep.argtypes = [C.POINTER(abi.LaserDesc), DP]
+    L.ptg_laser_initial_z.restype = st
+    L.ptg_laser_initial_z.argtypes = [C.POINTER(abi.LaserDesc), DP]
+    L.ptg_context_stream.restype = C.c_void_p
+    L.ptg_context_stream.argtypes = [ctxp]
+    L.ptg_eval_fields.restype = st
+    L.ptg_eval_fields.argtypes = [ctxp, C.POINTER(abi.LaserDesc), C.c_size_t, DP, DP, DP, DP]
+    L.ptg_push_steps.restype = st
+    L.ptg_push_steps.argtypes = [ctxp, C.POINTER(abi.LaserDesc), C.c_size_t, DP, DP, C.c_double, C.c_double,
+                                 C.c_int32, C.c_int32, DP]
+    L.ptg_lcfa_photon_rate.restype = st
+    L.ptg_lcfa_photon_rate.argtypes = [ctxp, C.c_size_t, DP, DP, DP]
+    L.ptg_lcfa_photon_sample.restype = st
+    L.ptg_lcfa_photon_sample.argtypes = [ctxp, C.c_size_t, DP, DP, DP, DP, DP]
+    L.ptg_lcfa_pair_t.restype = st
+    L.ptg_lcfa_pair_t.argtypes = [ctxp, C.c_size_t, DP, DP, DP]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a, shape):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(shape))
+
+
+class Engine:
+    """One device context (stream, shower store, tables)."""
+
+    def __init__(self, device=0, block_size=0, blocks_per_sm=0, initial_capacity=0):
+        L = load()
+        cfg = abi.DeviceCfg(device, block_size, blocks_per_sm, 0, initial_capacity)
+        h = C.c_void_p()
+        self._check(L.ptg_context_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.L = L
+
+    def _check(self, status):
+        if status != abi.PTG_OK:
+            raise PtgError(status, load().ptg_last_error().decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.ptg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream_ptr(self):
+        return self.L.ptg_context_stream(self._h)
+
+    def load_tables(self, directory=None):
+        self._check(self.L.ptg_load_tables(self._h, directory.encode() if directory else None))
+
+    # -- the collision loop ----------------------------------------------
+    def collide(self, laser, options, primaries, seed, id_base=None):
+        """Runs collide() over every primary (dict of numpy arrays with the
+        abi.PARTICLE_FIELDS names).  Returns (arrays, stats dict)."""
+        n = len(primaries["species"])
+        if id_base is None:
+            id_base = n
+        view = abi.particles_view(primaries, n)
+        out = abi.Particles()
+        st = abi.RunStats()
+        self._check(self.L.ptg_collide_batch(self._h, C.byref(laser), C.byref(options), C.byref(view), seed, id_base,
+                                             C.byref(out), C.byref(st)))
+        try:
+            m = out.n
+            arrays = {}
+            for name, dt, cols in abi.PARTICLE_FIELDS:
+                ptr = getattr(out, name)
+                shape = (m, cols) if cols > 1 else (m,)
+                if m == 0:
+                    arrays[name] = np.zeros(shape, dtype=dt)
+                    continue
+                buf = np.ctypeslib.as_array(ptr, shape=shape)
+                arrays[name] = np.array(buf, dtype=dt, copy=True)
+        finally:
+            self.L.ptg_particles_free(C.byref(out))
+        return arrays, st.as_dict()
+
+    def collide_device(self, laser, options, d_primaries, seed, id_base=None):
+        """Device-resident variant: `d_primaries` maps field names to CUDA
+        tensors (row-major [n][4] for four-vectors).  Returns (Particles with
+        device pointers valid until the next call, stats dict)."""
+        n = int(d_primaries["species"].shape[0])
+        if id_base is None:
+            id_base = n
+        view = abi.Particles()
+        view.n = n
+        for name, dt, _cols in abi.PARTICLE_FIELDS:
+            t = d_primaries.get(name)
+            ct = {np.float64: C.POINTER(C.c_double), np.int32: C.POINTER(C.c_int32),
+                  np.uint64: C.POINTER(C.c_uint64)}[dt]
+            setattr(view, name, C.cast(C.c_void_p(t.data_ptr()) if t is not None else None, ct))
+        out = abi.Particles()
+        st = abi.RunStats()
+        self._check(self.L.ptg_collide_batch_device(self._h, C.byref(laser), C.byref(options), C.byref(view), seed,
+                                                    id_base, C.byref(out), C.byref(st)))
+        return out, st.as_dict()
+
+    # -- diagnostics -----------------------------------------------------
+    def fields(self, laser, r):
+        r = _f64(r, (-1, 4))
+        n = len(r)
+        E, B, a = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        self._check(self.L.ptg_eval_fields(self._h, C.byref(laser), n, _dp(r), _dp(E), _dp(B), _dp(a)))
+        return E, B, a
+
+    def push_steps(self, laser, r, u, rqm, dt, nsteps, eqn=abi.LORENTZ):
+        r = _f64(r, (-1, 4)).copy()
+        u = _f64(u, (-1, 4)).copy()
+        work = np.zeros(len(r))
+        self._check(self.L.ptg_push_steps(self._h, C.byref(laser), len(r), _dp(r), _dp(u), rqm, dt, eqn, nsteps,
+                                          _dp(work)))
+        return r, u, work
+
+    def lcfa_photon_rate(self, chi, gamma):
+        chi, gamma = _f64(chi, (-1,)), _f64(gamma, (-1,))
+        out = np.zeros(len(chi))
+        self._check(self.L.ptg_lcfa_photon_rate(self._h, len(chi), _dp(chi), _dp(gamma), _dp(out)))
+        return out
+
+    def lcfa_photon_sample(self, chi, gamma, rand3):
+        chi, gamma, rand3 = _f64(chi, (-1,)), _f64(gamma, (-1,)), _f64(rand3, (-1, 3))
+        om, th = np.zeros(len(chi)), np.zeros(len(chi))
+        self._check(self.L.ptg_lcfa_photon_sample(self._h, len(chi), _dp(chi), _dp(gamma), _dp(rand3), _dp(om),
+                                                  _dp(th)))
+        return om, th
+
+    def lcfa_pair_t(self, chi):
+        chi = _f64(chi, (-1,))
+        a, b = np.zeros(len(chi)), np.zeros(len(chi))
+        self._check(self.L.ptg_lcfa_pair_t(self._h, len(chi), _dp(chi), _dp(a), _dp(b)))
+        return a, b
+
+
+def laser_timestep(laser):
+    dt = C.c_double()
+    st = load().ptg_laser_timestep(C.byref(laser), C.byref(dt))
+    if st != abi.PTG_OK:
+        raise PtgError(st, load().ptg_last_error().decode())
+    return dt.value
+
+
+def laser_initial_z(laser):
+    z = C.c_double()
+    st = load().ptg_laser_initial_z(C.byref(laser), C.byref(z))
+    if st != abi.PTG_OK:
+        raise PtgError(st, load().ptg_last_error().decode())
+    return z.value

@@ -1,0 +1,219 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the FP64
+oracle on the same inputs.
+
+Deterministic quantities (fields, pushes, rates, sampler outputs for given
+uniforms) are compared element by element with the tolerance written in
+each test.  The collision loop is compared particle by particle: the GPU and
+the oracle draw from the same counter-based streams, so each secondary is
+identified by its stream id on both sides.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from ptarmigan_gb300 import abi, beam
+
+pytestmark = pytest.mark.gpu
+
+C_LIGHT = 2.997925e8
+RQM_E = -1.602177e-19 / 9.109383e-31
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from ptarmigan_gb300 import build, engine
+    build.build()
+    e = engine.Engine()
+    e.load_tables()
+    yield e
+    e.close()
+
+
+def _lasers():
+    return [
+        abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
+                       fwhm_duration=30e-15),
+        abi.laser_desc(abi.FAST_FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6,
+                       fwhm_duration=30e-15),
+        abi.laser_desc(abi.FAST_FOCUSED_LASER, 20.0, 0.8e-6, abi.LINEAR, abi.COS2, waist=5e-6, n_cycles=10.0,
+                       pol_angle=0.3),
+        abi.laser_desc(abi.FAST_PLANE_WAVE, 1.0, 0.8e-6, abi.LINEAR, abi.COS2, n_cycles=30.87),
+        abi.laser_desc(abi.FAST_PLANE_WAVE, 3.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, n_cycles=8.0),
+        abi.laser_desc(abi.FAST_PLANE_WAVE, 2.0, 0.8e-6, abi.LINEAR, abi.FLATTOP, n_cycles=6.0, chirp_b=1e-3),
+    ]
+
+
+def _positions(laser, n, seed):
+    rng = np.random.default_rng(seed)
+    lam = laser.wavelength
+    z = rng.uniform(-8 * lam, 8 * lam, n)
+    t = rng.uniform(-8 * lam, 8 * lam, n)
+    x = rng.normal(0, 2e-6, n)
+    y = rng.normal(0, 2e-6, n)
+    return np.stack([t, x, y, z], axis=1)
+
+
+@pytest.mark.parametrize("li", range(6))
+def test_lcfa_fields_match_oracle(eng, orc, li):
+    laser = _lasers()[li]
+    r = _positions(laser, 400, li)
+    E, B, a = eng.fields(laser, r)
+    scale_e = np.abs(E).max()
+    scale_b = np.abs(B).max()
+    for i in range(len(r)):
+        Eo, Bo, ao = orc.fields(laser, r[i])
+        # FP64 against FP64: agreement to rounding, relative to the field scale
+        assert np.all(np.abs(E[i] - Eo) <= 1e-12 * scale_e), (i, E[i], Eo)
+        assert np.all(np.abs(B[i] - Bo) <= 1e-12 * scale_b), (i, B[i], Bo)
+        assert abs(a[i] - ao) <= 1e-12 * max(1.0, ao)
+
+
+@pytest.mark.parametrize("model,pol,env", [(abi.PLANE_WAVE, abi.LINEAR, abi.COS2),
+                                           (abi.FOCUSED_LASER, abi.CIRCULAR, abi.GAUSSIAN),
+                                           (abi.FOCUSED_LASER, abi.LINEAR, abi.FLATTOP)])
+def test_lma_a_sqd_matches_oracle(eng, orc, model, pol, env):
+    laser = abi.laser_desc(model, 5.0, 0.8e-6, pol, env, waist=3e-6, n_cycles=12.0)
+    r = _positions(laser, 300, 7)
+    _, _, a = eng.fields(laser, r)
+    for i in range(len(r)):
+        ao = math.sqrt(orc.a_sqd(laser, r[i]))
+        assert abs(a[i] - ao) <= 1e-13 * max(1.0, ao)
+
+
+def _beam_start(laser, n, gamma, seed):
+    return beam.build(n, gamma, sigma=0.01 * gamma, radius=2e-6, length=5e-6, rms_div=50e-6, laser=laser,
+                      seed=seed)
+
+
+@pytest.mark.parametrize("li,eqn", [(0, abi.LORENTZ), (1, abi.LORENTZ), (3, abi.LORENTZ), (4, abi.LANDAU_LIFSHITZ),
+                                    (0, abi.MODIFIED_LANDAU_LIFSHITZ)])
+def test_classical_trajectories_match_oracle(eng, orc, li, eqn):
+    """Emission off: full crossings of the pulse, FP64 push error <= 1e-10
+    relative against the oracle."""
+    laser = _lasers()[li]
+    dt = orc.max_timestep(laser)
+    z0 = orc.initial_z(laser)
+    prim = _beam_start(laser, 64, 2000.0, li)
+    # enough steps to cross the whole pulse: the phase k.r grows by about
+    # 2 k c dt per step for a head-on ultrarelativistic particle
+    k = 2 * math.pi / laser.wavelength
+    nc = laser.n_cycles
+    max_phase = {abi.COS2: math.pi * nc, abi.FLATTOP: math.pi * (nc + 1), abi.GAUSSIAN: 6 * math.pi * nc}[laser.envelope]
+    phase0 = min(k * (r[0] - r[3]) for r in prim["r"])
+    nsteps = min(int((max_phase - phase0) / (2 * k * C_LIGHT * dt)) + 10, 40000)
+    r_g, u_g, w_g = eng.push_steps(laser, prim["r"], prim["u"], RQM_E, dt, nsteps, eqn)
+    r_o, u_o, w_o = orc.push_steps(laser, prim["r"], prim["u"], RQM_E, dt, nsteps, eqn)
+    assert z0 > 0
+    for i in range(len(r_g)):
+        assert np.max(np.abs(u_g[i] - u_o[i])) <= 1e-10 * np.linalg.norm(u_o[i]), (i, u_g[i], u_o[i])
+        assert np.max(np.abs(r_g[i] - r_o[i])) <= 1e-10 * np.linalg.norm(r_o[i]), (i, r_g[i], r_o[i])
+
+
+@pytest.mark.parametrize("model,pol,env,eqn", [(abi.PLANE_WAVE, abi.LINEAR, abi.COS2, abi.LANDAU_LIFSHITZ),
+                                               (abi.FOCUSED_LASER, abi.CIRCULAR, abi.GAUSSIAN, abi.LORENTZ),
+                                               (abi.FOCUSED_LASER, abi.LINEAR, abi.GAUSSIAN, abi.LANDAU_LIFSHITZ)])
+def test_lma_trajectories_match_oracle(eng, orc, model, pol, env, eqn):
+    laser = abi.laser_desc(model, 5.0, 0.8e-6, pol, env, waist=3e-6, n_cycles=12.0)
+    dt = orc.max_timestep(laser)
+    prim = _beam_start(laser, 64, 5000.0, 3)
+    nsteps = 800
+    r_g, u_g, w_g = eng.push_steps(laser, prim["r"], prim["u"], RQM_E, dt, nsteps, eqn)
+    r_o, u_o, w_o = orc.push_steps(laser, prim["r"], prim["u"], RQM_E, dt, nsteps, eqn)
+    for i in range(len(r_g)):
+        assert np.max(np.abs(u_g[i] - u_o[i])) <= 1e-10 * np.linalg.norm(u_o[i])
+        assert np.max(np.abs(r_g[i] - r_o[i])) <= 1e-10 * np.linalg.norm(r_o[i])
+        assert abs(w_g[i] - w_o[i]) <= 1e-9 * max(1e-3, abs(w_o[i]))
+
+
+def test_lcfa_photon_rate_matches_oracle(eng, orc):
+    chi = np.exp(np.linspace(math.log(1e-4), math.log(500.0), 777))
+    gamma = np.full_like(chi, 1000.0)
+    got = eng.lcfa_photon_rate(chi, gamma)
+    for c, g in zip(chi, got):
+        ref = orc.lcfa_photon_rate(c, 1000.0)
+        assert abs(g - ref) <= 1e-13 * ref
+
+
+def test_lcfa_pair_t_matches_oracle(eng, orc):
+    chi = np.exp(np.linspace(math.log(5e-3), math.log(300.0), 555))
+    tp, tq = eng.lcfa_pair_t(chi)
+    for c, a, b in zip(chi, tp, tq):
+        ra, rb = orc.lcfa_pair_t(c)
+        assert abs(a - ra) <= 1e-13 * max(ra, 1e-300)
+        assert abs(b - rb) <= 1e-13 * max(rb, 1e-300)
+
+
+def test_lcfa_photon_sample_matches_oracle(eng, orc):
+    rng = np.random.default_rng(5)
+    n = 3000
+    chi = np.exp(rng.uniform(math.log(0.005), math.log(300.0), n))
+    gamma = np.exp(rng.uniform(math.log(50.0), math.log(5e4), n))
+    rand3 = rng.random((n, 3))
+    om, th = eng.lcfa_photon_sample(chi, gamma, rand3)
+    for i in range(n):
+        o, t, _ = orc.lcfa_photon_sample(chi[i], gamma[i], *rand3[i])
+        assert abs(om[i] - o) <= 1e-12 * o, i
+        if t is None:
+            assert th[i] < 0
+        else:
+            assert abs(th[i] - t) <= 1e-9 * max(t, 1e-12), i
+
+
+def _config1_small(n, seed=1):
+    laser = abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(10.0)
+    prim = beam.build(n, g, sigma=0.01 * g, radius=2e-6, length=20e-6, rms_div=50e-6, laser=laser, seed=seed)
+    return laser, prim
+
+
+def _match_by_stream(a, b):
+    ia = {int(s): i for i, s in enumerate(a["stream"])}
+    ib = {int(s): i for i, s in enumerate(b["stream"])}
+    common = sorted(set(ia) & set(ib))
+    return common, ia, ib
+
+
+@pytest.mark.parametrize("rate_increase", [1.0, 200.0])
+def test_collide_matches_oracle_particle_by_particle(eng, orc, rate_increase):
+    laser, prim = _config1_small(48)
+    opts = abi.collide_options(max_generation=2, rate_increase=rate_increase)
+    gout, gst = eng.collide(laser, opts, prim, seed=11)
+    oout, ost = orc.collide(laser, opts, prim, seed=11, threads=8)
+    assert gst["lepton_steps"] + gst["photon_steps"] > 0
+    assert abs(len(gout["species"]) - len(oout["species"])) <= max(2, 0.02 * len(oout["species"]))
+    common, ia, ib = _match_by_stream(gout, oout)
+    assert len(common) >= 0.98 * len(oout["species"])
+    bad = 0
+    for s in common:
+        i, j = ia[s], ib[s]
+        assert gout["species"][i] == oout["species"][j]
+        scale = np.linalg.norm(oout["u"][j])
+        if np.max(np.abs(gout["u"][i] - oout["u"][j])) > 1e-8 * scale:
+            bad += 1
+    # an event decision can flip where u is within rounding of the probability
+    assert bad <= max(1, 0.01 * len(common))
+    assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.02, abs=2)
+
+
+def test_collide_is_deterministic(eng):
+    laser, prim = _config1_small(64, seed=3)
+    opts = abi.collide_options(max_generation=2, rate_increase=100.0)
+    a, sa = eng.collide(laser, opts, prim, seed=5)
+    b, sb = eng.collide(laser, opts, prim, seed=5)
+    oa, ob = np.argsort(a["stream"]), np.argsort(b["stream"])
+    for k in ("species", "u", "r", "pol", "weight", "work", "stream"):
+        assert np.array_equal(a[k][oa], b[k][ob]), k
+    assert sa["emissions"] == sb["emissions"]
+
+
+def test_collide_options_filters(eng, orc):
+    laser, prim = _config1_small(40, seed=4)
+    opts = abi.collide_options(max_generation=2, min_energy=50.0, max_angle=0.01, discard_bg_e=1)
+    gout, _ = eng.collide(laser, opts, prim, seed=2)
+    oout, _ = orc.collide(laser, opts, prim, seed=2, threads=4)
+    assert len(gout["species"]) == pytest.approx(len(oout["species"]), abs=2)
+    e = 0.510999 * gout["u"][:, 0]
+    assert np.all(e > 50.0)
