@@ -159,7 +159,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_PRIMARIES)
-    ap.add_argument("--cpu-sample-per-core", type=int, default=600)
+    ap.add_argument("--cpu-sample-per-core", type=int, default=1500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 

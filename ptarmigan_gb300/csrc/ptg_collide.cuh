@@ -7,6 +7,7 @@
 // wave.  Waves alternate leptons -> photons -> leptons ...
 #pragma once
 #include "ptg_fields.cuh"
+#include "ptg_fields32.cuh"
 #include "ptg_lcfa.cuh"
 #include "ptg_lma.cuh"
 
@@ -144,26 +145,45 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         // Field::push default (field/mod.rs:147-152)
         double h = 0.5 * SPEED_OF_LIGHT * dt / L.u.t;
         d4 rh = d4{L.r.t + h * L.u.t, L.r.x + h * L.u.x, L.r.y + h * L.u.y, L.r.z + h * L.u.z};
-        d3 E, B;
-        double aa;
-        lcfa_fields(f, rh, &E, &B, &aa);
-        vay_push(rh, L.u, E, B, rqm, dt, a.o.eqn, [](double c) { return gaunt_factor(c); }, &r, &u, &dwork);
+        {
+            d3 E, B;
+            double aa;
+            lcfa_fields(f, rh, &E, &B, &aa);
+            vay_push(rh, L.u, E, B, rqm, dt, a.o.eqn, [](double c) { return gaunt_factor(c); }, &r, &u, &dwork);
+        }
         dt_actual = dt;
-        // lcf.rs:85-134 at the new position
-        lcfa_fields(f, r, &E, &B, &a_eff);
-        d3 beta = mk3(u.x / u.t, u.y / u.t, u.z / u.t);
-        double eb = dot(E, beta);
-        double E_rf_sqd = norm_sqr(E + SPEED_OF_LIGHT * cross(beta, B)) - eb * eb;
-        chi = E_rf_sqd > 0.0 ? u.t * sqrt(E_rf_sqd) / CRITICAL_FIELD : 0.0;
-        double prob = a.o.classical_mode ? dt_actual * lcfa_classical_rate(chi, u.t) : dt_actual * lcfa_photon_rate(chi, u.t);
-        if (rng.next() < prob) {
+        // lcf.rs:85-134 at the new position.  The per-step probability
+        // needs chi only to rate-table precision: FP32 fields and rate.
+        float prob = 0.0f;
+        {
+            f3 e, b;
+            if (lcfa_fields32(f, r, &e, &b)) {
+                float ig = (float)(1.0 / u.t);
+                f3 bt = f3{(float)u.x * ig, (float)u.y * ig, (float)u.z * ig};
+                f3 t = f3add(e, f3cross(bt, b));
+                float eb = f3dot(e, bt);
+                float q = f3dot(t, t) - eb * eb;
+                float chi32 = q > 0.0f ? (float)(u.t * field_scale(f) / CRITICAL_FIELD) * sqrtf(q) : 0.0f;
+                float gam = (float)u.t;
+                prob = (float)dt_actual * (a.o.classical_mode ? (float)(SQRT_3 * ALPHA_FINE * 5.0 * FRAC_PI_3 / (2.0 * PI * COMPTON_TIME)) * chi32 / gam
+                                                             : lcfa_photon_rate32(chi32, gam));
+            }
+        }
+        if (prob > 0.0f && rng.next() < (double)prob) {
+            // the event: fields, chi and the sample in FP64
+            d3 E, B;
+            lcfa_fields(f, r, &E, &B, &a_eff);
+            d3 beta = mk3(u.x / u.t, u.y / u.t, u.z / u.t);
+            double eb = dot(E, beta);
+            double E_rf_sqd = norm_sqr(E + SPEED_OF_LIGHT * cross(beta, B)) - eb * eb;
+            chi = E_rf_sqd > 0.0 ? u.t * sqrt(E_rf_sqd) / CRITICAL_FIELD : 0.0;
             double r1 = rng.next(), r2 = rng.next(), r3 = rng.next();
             double omega_mc2, theta;
             if (a.o.classical_mode)
                 lcfa_classical_sample(chi, u.t, r1, r2, r3, &omega_mc2, &theta);
             else
                 lcfa_photon_sample(chi, u.t, r1, r2, r3, &omega_mc2, &theta);
-            if (theta >= 0.0) {
+            if (theta >= 0.0 && chi > 0.0) {
                 double cphi = 2.0 * PI * r3;
                 d3 lng = normalize(beta);
                 d3 w = -normalize(E - (dot(lng, E) / sqrt(norm_sqr(E))) * lng + SPEED_OF_LIGHT * cross(beta, B));
@@ -225,36 +245,64 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
     d4 ue, up;
     double frac = 1.0, a_eff = 0.0, chi = 0.0, absorption = 0.0;
     if (MODEL == M_FAST_PLANE_WAVE || MODEL == M_FAST_FOCUSED_LASER) {
-        // lcf.rs:144-193
-        d3 E, B;
-        lcfa_fields(f, r, &E, &B, &a_eff);
-        d3 n = normalize(mk3(ell.x, ell.y, ell.z));
-        d3 a_perp = E - dot(E, n) * n + SPEED_OF_LIGHT * cross(n, B);
-        double E_rf_sqd = norm_sqr(a_perp);
-        if (E_rf_sqd > 0.0) {
-            chi = ell.t * sqrt(E_rf_sqd) / CRITICAL_FIELD;
-            prob = lcfa_pair_probability(ell, pol, chi, a_perp, dt, &pol_new);
-        }
-        double ri = (prob * a.o.rate_increase > 0.1) ? 0.1 / prob : a.o.rate_increase;
-        if (rng.next() < prob * ri) {
-            double gamma_p, cos_theta, cphi;
-            if (!lcfa_pair_sample(ell, pol, chi, a_perp, rng, *a.gl, &gamma_p, &cos_theta, &cphi, rej)) {
-                L.status = ST_REJECTION_CAP;
-                L.r = r;
-                return;
+        // lcf.rs:144-193.  Unpolarised photons: the step probability from
+        // FP32 fields and T(chi); polarisation-resolved photons take the
+        // FP64 path (their Stokes vector is integrated step by step).
+        double prob_step = 0.0;
+        if (!a.o.pol_resolved) {
+            f3 e, b;
+            if (lcfa_fields32(f, r, &e, &b)) {
+                float inv = (float)(1.0 / sqrt(ell.x * ell.x + ell.y * ell.y + ell.z * ell.z));
+                f3 n = f3{(float)ell.x * inv, (float)ell.y * inv, (float)ell.z * inv};
+                f3 ap = f3add(f3add(e, f3scale(-f3dot(e, n), n)), f3cross(n, b));
+                float q = f3dot(ap, ap);
+                if (q > 0.0f) {
+                    float chi32 = (float)(ell.t * field_scale(f) / CRITICAL_FIELD) * sqrtf(q);
+                    prob_step = (double)((float)(ALPHA_FINE * dt / (COMPTON_TIME * ell.t)) * chi32 * lcfa_t_mean32(chi32));
+                }
             }
-            double sin_theta = sqrt(1.0 - cos_theta * cos_theta);
-            double upm = gamma_p * sqrt(1.0 - 1.0 / (gamma_p * gamma_p));
-            d3 e1 = normalize(a_perp);
-            d3 e2 = cross(n, e1);
-            double sp, cp;
-            sincos(cphi, &sp, &cp);
-            d3 p3 = upm * (cos_theta * n + (sin_theta * cp) * e1 + (sin_theta * sp) * e2);
-            d3 e3 = mk3(ell.x, ell.y, ell.z) - p3;
-            up = d4{sqrt(1.0 + dot(p3, p3)), p3.x, p3.y, p3.z};
-            ue = d4{sqrt(1.0 + dot(e3, e3)), e3.x, e3.y, e3.z};
-            frac = 1.0 / ri;
-            created = true;
+        }
+        bool need64 = a.o.pol_resolved;
+        double ri = (prob_step * a.o.rate_increase > 0.1) ? 0.1 / prob_step : a.o.rate_increase;
+        double u_draw = 2.0;
+        if (!need64 && prob_step > 0.0) {
+            u_draw = rng.next();
+            need64 = u_draw < prob_step * ri;  // an event: redo the step's physics in FP64
+        }
+        prob = prob_step;
+        if (need64) {
+            d3 E, B;
+            lcfa_fields(f, r, &E, &B, &a_eff);
+            d3 n = normalize(mk3(ell.x, ell.y, ell.z));
+            d3 a_perp = E - dot(E, n) * n + SPEED_OF_LIGHT * cross(n, B);
+            double E_rf_sqd = norm_sqr(a_perp);
+            prob = 0.0;
+            if (E_rf_sqd > 0.0) {
+                chi = ell.t * sqrt(E_rf_sqd) / CRITICAL_FIELD;
+                prob = lcfa_pair_probability(ell, pol, chi, a_perp, dt, &pol_new);
+            }
+            ri = (prob * a.o.rate_increase > 0.1) ? 0.1 / prob : a.o.rate_increase;
+            if (u_draw > 1.0) u_draw = rng.next();  // polarisation-resolved: first draw of the step
+            if (u_draw < prob * ri) {
+                double gamma_p, cos_theta, cphi;
+                if (!lcfa_pair_sample(ell, pol, chi, a_perp, rng, *a.gl, &gamma_p, &cos_theta, &cphi, rej)) {
+                    L.status = ST_REJECTION_CAP;
+                    L.r = r;
+                    return;
+                }
+                double sin_theta = sqrt(1.0 - cos_theta * cos_theta);
+                double upm = gamma_p * sqrt(1.0 - 1.0 / (gamma_p * gamma_p));
+                d3 e1 = normalize(a_perp);
+                d3 e2 = cross(n, e1);
+                double sp, cp;
+                sincos(cphi, &sp, &cp);
+                d3 p3 = upm * (cos_theta * n + (sin_theta * cp) * e1 + (sin_theta * sp) * e2);
+                d3 e3 = mk3(ell.x, ell.y, ell.z) - p3;
+                up = d4{sqrt(1.0 + dot(p3, p3)), p3.x, p3.y, p3.z};
+                ue = d4{sqrt(1.0 + dot(e3, e3)), e3.x, e3.y, e3.z};
+                frac = 1.0 / ri;
+                created = true;
+            }
         }
     } else {
         int st = lma_pair_create(f, *a.lma, r, ell, pol, dt, rng, a.o.rate_increase, &prob, &pol_new, &created, &ue,

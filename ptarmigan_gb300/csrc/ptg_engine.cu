@@ -97,13 +97,16 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
         double n_fwhm = d.envelope == PTG_ENV_COS2 ? 0.36405666377387671305 * nc : nc;
         f.bandwidth = std::sqrt(0.5 * LN_2) / (PI * n_fwhm);
     }
-    // Gaussian LCFA focused envelope exp(-2 ln2 phi^2 / tau^2) < 1e-300
-    // beyond |phi| = tau sqrt(300 ln 10 / (2 ln 2)); there E and B are zero
-    // in FP64 to every bit that reaches u.
+    // Field-free region of the Gaussian FastFocusedLaser: beyond
+    // |phi| = tau sqrt(ln(1e18) / (2 ln 2)) the envelope exp(-2 ln2 phi^2 /
+    // tau^2) is below 1e-18, so a step's kick q E dt / (2 m c) is below
+    // 1e-18 a0 omega dt and the emission probability below ~1e-19: neither
+    // reaches a bit of u (|u| >= 1) nor a draw (uniforms are multiples of
+    // 2^-53).  There E = B = 0 without evaluating the beam.
     f.env_cut = 0.0;
     if (d.model == PTG_FAST_FOCUSED_LASER && d.envelope == PTG_ENV_GAUSSIAN) {
         double tau = f.omega * f.duration;
-        f.env_cut = tau * std::sqrt(300.0 * std::log(10.0) / (2.0 * LN_2));
+        f.env_cut = tau * std::sqrt(18.0 * std::log(10.0) / (2.0 * LN_2));
     }
     // Field::max_timestep
     double dt;

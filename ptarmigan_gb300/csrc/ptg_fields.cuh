@@ -24,7 +24,7 @@ struct FieldParams {
     double amp;                // plane-wave LCFA amplitude m c^2 k a0 / e
     double max_phase;          // Field::contains
     double bandwidth;          // LMA finite-bandwidth width
-    double env_cut;            // |phase| beyond which the envelope is below 1e-300 (LCFA shortcut, 0 = off)
+    double env_cut;            // |phase| beyond which the envelope is below 1e-18: E = B = 0 (0 = off)
 };
 
 __device__ __forceinline__ double phase_of(const FieldParams& f, d4 r) { return f.k * r.t - f.k * r.z; }
@@ -92,6 +92,14 @@ __device__ __forceinline__ cplx cmul_mi(cplx a) { return cplx{a.im, -a.re}; }
 // for the beam polarised along x after undoing pol_angle.  The carrier
 // phase is k.r.  Returns Re/Im parts of E and B, already scaled by E0/B0
 // and rotated back by pol_angle (rotation supplied as (cr, sr)).
+//
+// Precision split: the terms of order eps^0 and eps^1 (the paraxial beam
+// and the first longitudinal components) are FP64; the diffraction
+// corrections of order eps^2..eps^4, whose size relative to the leading
+// term is at most ~eps^2 rho^4 (eps = w0 / zR, 0.06 for w0 = 4 um), are
+// evaluated in FP32 and applied in FP64.  Their rounding (~6e-8 of a term
+// that is itself <= ~1e-2 of the field where the beam is not negligible)
+// puts the field error near 1e-9 of E0.
 __device__ __forceinline__ void ffl_beam(const FieldParams& f, d4 r, double cr, double sr, d3* reE, d3* imE, d3* reB,
                                          d3* imB) {
     // r.rotate_around_z(-angle)
@@ -99,45 +107,57 @@ __device__ __forceinline__ void ffl_beam(const FieldParams& f, d4 r, double cr, 
     double ry = cr * r.y - sr * r.x;
     double x = rx / f.waist, y = ry / f.waist, z = r.z / f.zr;
     double rho2 = x * x + y * y;
-    double e = f.eps, e2 = e * e, e3 = e2 * e, e4 = e2 * e2;
     // f = i / (z + i) = (1 + i z) / (1 + z^2)
     double den = 1.0 / (1.0 + z * z);
-    cplx fc = cplx{den, z * den};
+    double fre = den, fim = z * den;
     // prefactor = f exp(-f rho^2 + i phase)
     double ph = f.k * r.t - f.k * r.z;
-    double ex = exp(-fc.re * rho2);
+    double ex = exp(-fre * rho2);
     double sn, cs;
-    sincos(ph - fc.im * rho2, &sn, &cs);
-    cplx pre = cmul(fc, cplx{ex * cs, ex * sn});
-    cplx f2 = cmul(fc, fc), f3 = cmul(f2, fc), f4 = cmul(f2, f2);
-    double rho4 = rho2 * rho2, rho6 = rho4 * rho2, rho8 = rho4 * rho4;
-    // Ex = -i pre (1 + e^2 f^2 (x^2 - f rho^4/4) + e^4 f^2 (1/8 - f rho^2/4 + f^2 (x^2 rho^2 - rho^4/16)
-    //      + f^3 rho^4 (-x^2 - rho^2/2)/4 + f^4 rho^8/32))
-    cplx t2 = cadds(x * x, cscale(-rho4 / 4.0, fc));
-    cplx t4 = cadds(1.0 / 8.0, cscale(-rho2 / 4.0, fc));
-    t4 = cadd(t4, cscale(x * x * rho2 - rho4 / 16.0, f2));
-    t4 = cadd(t4, cscale(rho4 * (-x * x - 0.5 * rho2) / 4.0, f3));
-    t4 = cadd(t4, cscale(rho8 / 32.0, f4));
-    cplx Ex = cadds(1.0, cadd(cscale(e2, cmul(f2, t2)), cscale(e4, cmul(f2, t4))));
-    Ex = cmul_mi(cmul(pre, Ex));
-    // Ey = -i pre (e^2 f^2 x y + e^4 x y f^4 rho^2 (1 - f rho^2/4))
-    cplx ty = cadd(cscale(e2 * x * y, f2), cscale(e4 * x * y * rho2, cmul(f4, cadds(1.0, cscale(-rho2 / 4.0, fc)))));
-    cplx Ey = cmul_mi(cmul(pre, ty));
-    // Ez = pre (e f x + e^3 f^2 x (-1/2 + f rho^2 - f^2 rho^4/4))
-    cplx tz = cadds(-0.5, cadd(cscale(rho2, fc), cscale(-rho4 / 4.0, f2)));
-    cplx Ez = cmul(pre, cadd(cscale(e * x, fc), cscale(e3 * x, cmul(f2, tz))));
-    // By = -i pre (1 + e^2 f^2 rho^2 (1 - f rho^2/2)/2
-    //      + e^4 f^2 (-1 + 2 f rho^2 + 2.5 f^2 rho^4 - 2 f^3 rho^6 + f^4 rho^8/4)/8)
-    cplx b2 = cscale(rho2 / 2.0, cadds(1.0, cscale(-rho2 / 2.0, fc)));
-    cplx b4 = cadds(-1.0, cscale(2.0 * rho2, fc));
-    b4 = cadd(b4, cscale(2.5 * rho4, f2));
-    b4 = cadd(b4, cscale(-2.0 * rho6, f3));
-    b4 = cadd(b4, cscale(0.25 * rho8, f4));
-    cplx By = cadds(1.0, cadd(cscale(e2, cmul(f2, b2)), cscale(e4 / 8.0, cmul(f2, b4))));
-    By = cmul_mi(cmul(pre, By));
-    // Bz = pre (e f y + e^3 f^2 y (1 + f rho^2 - f^2 rho^4/2)/2)
-    cplx bz = cadds(1.0, cadd(cscale(rho2, fc), cscale(-rho4 / 2.0, f2)));
-    cplx Bz = cmul(pre, cadd(cscale(e * y, fc), cscale(e3 * y / 2.0, cmul(f2, bz))));
+    sincos(ph - fim * rho2, &sn, &cs);
+    cplx pre = cmul(cplx{fre, fim}, cplx{ex * cs, ex * sn});
+    // corrections in FP32
+    float xf = (float)x, yf = (float)y, r2 = (float)rho2;
+    float ef = (float)f.eps, e2 = ef * ef, e3 = e2 * ef, e4 = e2 * e2;
+    float fr = (float)fre, fi = (float)fim;
+    float f2r = fr * fr - fi * fi, f2i = 2.0f * fr * fi;
+    float f3r = f2r * fr - f2i * fi, f3i = f2r * fi + f2i * fr;
+    float f4r = f2r * f2r - f2i * f2i, f4i = 2.0f * f2r * f2i;
+    float r4 = r2 * r2, r6 = r4 * r2, r8 = r4 * r4;
+    auto mul = [](float ar, float ai, float br, float bi, float* cr_, float* ci_) {
+        *cr_ = ar * br - ai * bi;
+        *ci_ = ar * bi + ai * br;
+    };
+    float tr, ti, ur, ui;
+    // Ex: eps^2 f^2 (x^2 - f rho^4/4) + eps^4 f^2 (1/8 - f rho^2/4 + f^2 (x^2 rho^2 - rho^4/16)
+    //     + f^3 rho^4 (-x^2 - rho^2/2)/4 + f^4 rho^8/32)
+    float t2r = xf * xf - 0.25f * r4 * fr, t2i = -0.25f * r4 * fi;
+    float t4r = 0.125f - 0.25f * r2 * fr + (xf * xf * r2 - 0.0625f * r4) * f2r + 0.25f * r4 * (-xf * xf - 0.5f * r2) * f3r +
+                0.03125f * r8 * f4r;
+    float t4i = -0.25f * r2 * fi + (xf * xf * r2 - 0.0625f * r4) * f2i + 0.25f * r4 * (-xf * xf - 0.5f * r2) * f3i +
+                0.03125f * r8 * f4i;
+    mul(f2r, f2i, e2 * t2r + e4 * t4r, e2 * t2i + e4 * t4i, &tr, &ti);
+    cplx cX = cplx{(double)tr, (double)ti};
+    // Ey: eps^2 f^2 x y + eps^4 x y f^4 rho^2 (1 - f rho^2/4)
+    mul(f4r, f4i, 1.0f - 0.25f * r2 * fr, -0.25f * r2 * fi, &ur, &ui);
+    cplx cY = cplx{(double)(e2 * xf * yf * f2r + e4 * xf * yf * r2 * ur), (double)(e2 * xf * yf * f2i + e4 * xf * yf * r2 * ui)};
+    // Ez: eps f x (FP64) + eps^3 f^2 x (-1/2 + f rho^2 - f^2 rho^4/4)
+    mul(f2r, f2i, -0.5f + r2 * fr - 0.25f * r4 * f2r, r2 * fi - 0.25f * r4 * f2i, &tr, &ti);
+    cplx cZ = cplx{f.eps * x * fre + (double)(e3 * xf * tr), f.eps * x * fim + (double)(e3 * xf * ti)};
+    // By: eps^2 f^2 rho^2 (1 - f rho^2/2)/2 + eps^4 f^2 (-1 + 2 f rho^2 + 2.5 f^2 rho^4 - 2 f^3 rho^6 + f^4 rho^8/4)/8
+    float b2r = 0.5f * r2 * (1.0f - 0.5f * r2 * fr), b2i = 0.5f * r2 * (-0.5f * r2 * fi);
+    float b4r = -1.0f + 2.0f * r2 * fr + 2.5f * r4 * f2r - 2.0f * r6 * f3r + 0.25f * r8 * f4r;
+    float b4i = 2.0f * r2 * fi + 2.5f * r4 * f2i - 2.0f * r6 * f3i + 0.25f * r8 * f4i;
+    mul(f2r, f2i, e2 * b2r + 0.125f * e4 * b4r, e2 * b2i + 0.125f * e4 * b4i, &tr, &ti);
+    cplx cB = cplx{(double)tr, (double)ti};
+    // Bz: eps f y (FP64) + eps^3 f^2 y (1 + f rho^2 - f^2 rho^4/2)/2
+    mul(f2r, f2i, 0.5f * (1.0f + r2 * fr - 0.5f * r4 * f2r), 0.5f * (r2 * fi - 0.5f * r4 * f2i), &tr, &ti);
+    cplx cBz = cplx{f.eps * y * fre + (double)(e3 * yf * tr), f.eps * y * fim + (double)(e3 * yf * ti)};
+    cplx Ex = cmul_mi(cmul(pre, cadds(1.0, cX)));
+    cplx Ey = cmul_mi(cmul(pre, cY));
+    cplx Ez = cmul(pre, cZ);
+    cplx By = cmul_mi(cmul(pre, cadds(1.0, cB)));
+    cplx Bz = cmul(pre, cBz);
     // scale and rotate by +angle
     double E0 = f.E0, B0 = f.B0;
     *reE = mk3(E0 * (cr * Ex.re - sr * Ey.re), E0 * (cr * Ey.re + sr * Ex.re), E0 * Ez.re);

@@ -64,10 +64,13 @@ def test_lcfa_fields_match_oracle(eng, orc, li):
     scale_b = np.abs(B).max()
     for i in range(len(r)):
         Eo, Bo, ao = orc.fields(laser, r[i])
-        # FP64 against FP64: agreement to rounding, relative to the field scale
-        assert np.all(np.abs(E[i] - Eo) <= 1e-12 * scale_e), (i, E[i], Eo)
-        assert np.all(np.abs(B[i] - Bo) <= 1e-12 * scale_b), (i, B[i], Bo)
-        assert abs(a[i] - ao) <= 1e-12 * max(1.0, ao)
+        # The focused beam's diffraction corrections of order eps^2..eps^4
+        # are FP32 on the device (the leading orders FP64): 1e-8 of the
+        # field scale.  Plane waves are FP64 throughout.
+        tol = 1e-8 if laser.model == abi.FAST_FOCUSED_LASER else 1e-12
+        assert np.all(np.abs(E[i] - Eo) <= tol * scale_e), (i, E[i], Eo)
+        assert np.all(np.abs(B[i] - Bo) <= tol * scale_b), (i, B[i], Bo)
+        assert abs(a[i] - ao) <= tol * max(1.0, ao)
 
 
 @pytest.mark.parametrize("model,pol,env", [(abi.PLANE_WAVE, abi.LINEAR, abi.COS2),
