@@ -49,6 +49,7 @@ struct StepOptions {
     int tracking_secondaries;
     int max_generation;       // -1: no limit
     int keep_decayed;
+    int has_t_stop;           // t_stop is finite
 };
 
 struct WaveArgs {
@@ -90,6 +91,7 @@ __device__ __forceinline__ d4 get4(const double* v, unsigned long long cap, unsi
 struct Lane {
     d4 r, u, pol;
     double weight, icount, work;
+    double hph;  // photons: c dt / ell^0
     unsigned long long slot, stream, id;
     uint32_t step;
     int species, gen, status, flags;
@@ -145,7 +147,17 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         // Field::push default (field/mod.rs:147-152)
         double h = 0.5 * SPEED_OF_LIGHT * dt / L.u.t;
         d4 rh = d4{L.r.t + h * L.u.t, L.r.x + h * L.u.x, L.r.y + h * L.u.y, L.r.z + h * L.u.z};
-        {
+        if (f.env_cut > 0.0 && fabs(phase_of(f, rh)) > f.env_cut) {
+            // E = B = 0 at rh: lcf.rs:18-78 then leaves u unchanged bit for
+            // bit (every field term is an exact zero), recomputes gamma and
+            // drifts the second half step; no work is done.
+            u = L.u;
+            double g = sqrt(1.0 + (u.x * u.x + u.y * u.y + u.z * u.z));
+            u.t = g;
+            double h2 = 0.5 * SPEED_OF_LIGHT * dt / g;
+            r = d4{rh.t + h2 * u.t, rh.x + h2 * u.x, rh.y + h2 * u.y, rh.z + h2 * u.z};
+            dwork = 0.0;
+        } else {
             d3 E, B;
             double aa;
             lcfa_fields(f, rh, &E, &B, &aa);
@@ -236,7 +248,7 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
     Draws rng;
     rng.begin(a.seed, L.stream, L.step);
     d4 ell = L.u;
-    double h = SPEED_OF_LIGHT * dt / ell.t;
+    double h = L.hph;  // c dt / ell^0, fixed for a photon
     d4 r = d4{L.r.t + h * ell.t, L.r.x + h * ell.x, L.r.y + h * ell.y, L.r.z + h * ell.z};
     d4 pol = a.o.pol_resolved ? L.pol : d4{1.0, 0.0, 0.0, 0.0};
     double prob = 0.0;
@@ -356,6 +368,7 @@ __device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
     L.flags = s.flags[i];
     L.step = 0;
     L.decayed = false;
+    L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
     return true;
 }
 
@@ -383,7 +396,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
         if (L.status != ST_OK || lane_untracked(a, L)) {
             done = true;
         } else if (L.species != SP_PHOTON) {
-            done = !(contains(a.f, L.r) && L.r.t / SPEED_OF_LIGHT < a.o.t_stop);
+            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
             if (!done) {
                 lepton_step<MODEL>(a, L, &rej, &nemit);
                 ++L.step;
@@ -391,7 +404,8 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                 done = L.status != ST_OK;
             }
         } else {
-            done = !(contains(a.f, L.r) && L.r.t / SPEED_OF_LIGHT < a.o.t_stop && !L.decayed && a.o.tracking_photons);
+            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
+                     a.o.tracking_photons);
             if (!done) {
                 photon_step<MODEL>(a, L, &rej, &npair);
                 ++L.step;

@@ -682,6 +682,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
     a.f = f;
     a.o.dt = dt_max * o->dt_multiplier;
     a.o.t_stop = o->t_stop;
+    a.o.has_t_stop = std::isfinite(o->t_stop) ? 1 : 0;
     a.o.rate_increase = o->rate_increase;
     a.o.eqn = (o->classical && o->rr) ? (o->gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
     a.o.classical_mode = o->classical && !o->gaunt_factor;
