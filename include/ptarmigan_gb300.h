@@ -195,6 +195,38 @@ ptg_status ptg_collide_batch_device(ptg_ctx* ctx, const ptg_laser_desc* laser, c
 /* Frees arrays allocated by ptg_collide_batch. */
 void ptg_particles_free(ptg_particles* p);
 
+/* Allocation-free variant of ptg_collide_batch_device.  It has no
+ * counterpart in the reference.
+ *
+ * Some callers cannot let a library call cudaMalloc: a host program whose
+ * device memory is owned by another runtime's pool (a framework's caching
+ * allocator, or a driver that reserves the GPU's memory at start-up) would
+ * see such a call fail or fragment the pool, and cudaMalloc/cudaFree can
+ * synchronise the whole device, stalling the caller's other streams.  This
+ * entry point allocates nothing and needs no ptg_ctx: the caller passes the
+ * primaries and the output arrays as device buffers (`d_out` rows, each at
+ * least `out_capacity` long) and the CUDA stream to launch on (NULL for
+ * the default stream).  It covers the LCFA field models (FastPlaneWave,
+ * FastFocusedLaser); other models return PTG_ERR_UNSUPPORTED.
+ *
+ * Its working memory is one static device array of about 8.6 MB inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Limits: at most 4096 primaries per call (more is
+ * PTG_ERR_INVALID_ARGUMENT) and at most 32768 particles in a batch's
+ * showers, primaries included (more is PTG_ERR_QUEUE_OVERFLOW); a result
+ * longer than out_capacity is PTG_ERR_QUEUE_OVERFLOW with the needed row
+ * count in stats->n_out.
+ *
+ * The first call on each device sets that device up (it looks up the
+ * array's device address and uploads constants, with the device current);
+ * make that first call before any stream capture.  All calls share the
+ * array, and each call clears what must start at zero, so calls that
+ * overlap on the GPU (concurrent streams or host threads) race: serialise
+ * them. */
+ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* opts,
+                                     const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
+                                     ptg_particles* d_out, size_t out_capacity, void* stream, ptg_run_stats* stats);
+
 /* Field::max_timestep (field/<model>.rs) for a laser, in seconds (or 1.0 where the
  * reference returns None), and Field::ideal_initial_z, in metres. */
 ptg_status ptg_laser_timestep(const ptg_laser_desc* laser, double* dt);

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <dlfcn.h>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1008,3 +1009,209 @@ ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_pa
     });
 }
 
+
+// ------------------------------------------------ allocation-free batch ---
+// ptg_collide_batch_noalloc(): the LCFA collision loop for callers that
+// cannot allocate device memory.  Its working memory (wave counters, the
+// primaries' initial momenta, per-shower counts, the pair-spectrum node
+// constants and a fixed-size shower store) lives in one file-scope device
+// array.  Host code never dereferences that array's name: the device
+// address comes from cudaGetSymbolAddress() once per device.
+namespace {
+constexpr unsigned long long NOALLOC_MAX_PRIMARIES = 4096;
+constexpr unsigned long long NOALLOC_MAX_PARTICLES = 32768;  // shower store, primaries included
+constexpr size_t noalloc_align(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr size_t NOALLOC_STORE_BYTES = (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 4 * 4) * NOALLOC_MAX_PARTICLES + 18 * 256;
+constexpr size_t NOALLOC_OFF_COUNTERS = NOALLOC_STORE_BYTES;
+constexpr size_t NOALLOC_OFF_INIT_U = NOALLOC_OFF_COUNTERS + noalloc_align(sizeof(Counters));
+constexpr size_t NOALLOC_OFF_COUNTS = NOALLOC_OFF_INIT_U + noalloc_align(32 * NOALLOC_MAX_PRIMARIES);
+constexpr size_t NOALLOC_OFF_GL = NOALLOC_OFF_COUNTS + noalloc_align(8 * NOALLOC_MAX_PRIMARIES);
+constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_GL + noalloc_align(sizeof(PairGL));
+constexpr int NOALLOC_MAX_DEVICES = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+static std::mutex g_noalloc_mutex;
+static char* g_noalloc_base[NOALLOC_MAX_DEVICES];
+
+// Once per device, with that device current: look up the array's device
+// address and upload the pair-spectrum node constants into it.
+static ptg_status noalloc_setup(int dev, char** base) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return set_err(PTG_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    if (g_noalloc_base[dev]) {
+        *base = g_noalloc_base[dev];
+        return PTG_OK;
+    }
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || ptr == nullptr)
+        return set_err(PTG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    double nodes[32], weights[32];
+    CUDA_TRY(cudaMemcpyFromSymbol(nodes, PTG_GL_NODES, sizeof(nodes)));
+    CUDA_TRY(cudaMemcpyFromSymbol(weights, PTG_GL_WEIGHTS, sizeof(weights)));
+    PairGL gl;
+    for (int k = 0; k < 32; ++k) {
+        double t = nodes[k];
+        gl.w[k] = weights[k];
+        gl.t[k] = t;
+        gl.c23[k] = std::cosh(2.0 * t / 3.0);
+        gl.c13_over_c1[k] = std::cosh(t / 3.0) / std::cosh(t);
+        gl.c1[k] = std::cosh(t);
+    }
+    CUDA_TRY(cudaMemcpy((char*)ptr + NOALLOC_OFF_GL, &gl, sizeof(gl), cudaMemcpyHostToDevice));
+    g_noalloc_base[dev] = (char*)ptr;
+    *base = (char*)ptr;
+    return PTG_OK;
+}
+
+__global__ void k_noalloc_reset(Counters* c, unsigned long long n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *c = Counters{};
+        c->n_total = n;
+    }
+}
+
+template <int MODEL>
+static cudaError_t noalloc_wave(const WaveArgs& a, int grid_max, cudaStream_t s) {
+    unsigned long long n = a.hi - a.lo;
+    unsigned long long need = (n + 127) / 128;
+    int grid = (unsigned long long)grid_max > need ? (int)need : grid_max;
+    if (grid < 1) grid = 1;
+    collide_wave<MODEL><<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* o,
+                                     const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
+                                     ptg_particles* d_out, size_t out_capacity, void* stream, ptg_run_stats* stats) {
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    if (!o || !d_primaries || !d_out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (laser->model != PTG_FAST_PLANE_WAVE && laser->model != PTG_FAST_FOCUSED_LASER)
+        return set_err(PTG_ERR_UNSUPPORTED, "the allocation-free entry point covers the LCFA field models only");
+    if (!d_primaries->species || !d_primaries->r || !d_primaries->u)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
+    if (d_primaries->n > NOALLOC_MAX_PRIMARIES)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "the allocation-free entry point takes at most " +
+                                                     std::to_string(NOALLOC_MAX_PRIMARIES) + " primaries per call, got " +
+                                                     std::to_string(d_primaries->n));
+    if (!d_out->species || !d_out->r || !d_out->u || !d_out->r0 || !d_out->u0 || !d_out->pol || !d_out->weight ||
+        !d_out->payload || !d_out->parent_chi || !d_out->interaction_count || !d_out->work || !d_out->id ||
+        !d_out->parent_id || !d_out->primary || !d_out->stream || !d_out->generation || !d_out->flags || !d_out->status)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "every output array must be a device buffer of out_capacity rows");
+    if (!(o->rate_increase >= 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "increase in pair creation rate must be >= 1.0");
+    if (o->rate_increase > 1.0 && o->multiplicity >= 0)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "event biasing is incompatible with multiplicity selection");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    char* base = nullptr;
+    st = noalloc_setup(dev, &base);
+    if (st != PTG_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    int sms = 0, per_sm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+
+    Store store;
+    carve_store(&store, base, NOALLOC_MAX_PARTICLES);
+    Counters* counters = (Counters*)(base + NOALLOC_OFF_COUNTERS);
+    double* init_u = (double*)(base + NOALLOC_OFF_INIT_U);
+    unsigned long long* shower_count = (unsigned long long*)(base + NOALLOC_OFF_COUNTS);
+    const PairGL* gl = (const PairGL*)(base + NOALLOC_OFF_GL);
+
+    unsigned long long n = d_primaries->n;
+    double dt_max;
+    WaveArgs a{};
+    a.f = make_field(*laser, &dt_max);
+    a.o.dt = dt_max * o->dt_multiplier;
+    a.o.t_stop = o->t_stop;
+    a.o.has_t_stop = std::isfinite(o->t_stop) ? 1 : 0;
+    a.o.rate_increase = o->rate_increase;
+    a.o.eqn = (o->classical && o->rr) ? (o->gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
+    a.o.classical_mode = o->classical && !o->gaunt_factor;
+    a.o.classical = o->classical;
+    a.o.electron_recoils = !o->classical && o->rr;
+    a.o.tracking_photons = o->tracking_photons;
+    a.o.pol_resolved = o->pol_resolved;
+    a.o.rotate_stokes = o->rotate_stokes_pars;
+    a.o.tracking_secondaries = o->tracking_secondaries;
+    a.o.max_generation = o->max_generation;
+    a.o.keep_decayed = o->keep_decayed_photons;
+    a.s = store;
+    a.c = counters;
+    a.gl = gl;
+    a.lma = nullptr;
+    a.seed = seed;
+    a.n_primaries = n;
+    a.id_base = id_base;
+    const void* kern = laser->model == PTG_FAST_PLANE_WAVE ? (const void*)collide_wave<M_FAST_PLANE_WAVE>
+                                                           : (const void*)collide_wave<M_FAST_FOCUSED_LASER>;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0));
+    int grid_max = (per_sm > 0 ? per_sm : 1) * sms;
+
+    // the array keeps the previous call's contents: reset the counters
+    k_noalloc_reset<<<1, 32, 0, s>>>(counters, n);
+    CUDA_TRY(cudaGetLastError());
+    if (n > 0) {
+        k_load_primaries<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(store, *d_primaries, n, id_base, init_u, shower_count);
+        CUDA_TRY(cudaGetLastError());
+    }
+    Counters h{};
+    unsigned long long lo = 0, hi = n;
+    uint32_t waves = 0;
+    while (lo < hi) {
+        a.lo = lo;
+        a.hi = hi;
+        CUDA_TRY(cudaMemsetAsync(&counters->next, 0, 8, s));
+        CUDA_TRY(laser->model == PTG_FAST_PLANE_WAVE ? noalloc_wave<M_FAST_PLANE_WAVE>(a, grid_max, s)
+                                                     : noalloc_wave<M_FAST_FOCUSED_LASER>(a, grid_max, s));
+        ++waves;
+        CUDA_TRY(cudaMemcpyAsync(&h, counters, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (h.overflow)
+            return set_err(PTG_ERR_QUEUE_OVERFLOW, "the shower outgrew the allocation-free store (" +
+                                                       std::to_string(NOALLOC_MAX_PARTICLES) + " particles)");
+        lo = hi;
+        hi = h.n_total;
+    }
+    unsigned long long total = hi;
+    FilterArgs fa;
+    fa.s = store;
+    fa.init_u = init_u;
+    fa.shower_count = shower_count;
+    fa.n = total;
+    fa.min_energy = o->min_energy;
+    fa.cos_max_angle = std::cos(o->max_angle);
+    fa.discard_bg_e = o->discard_bg_e;
+    fa.discard_bg_ph = o->discard_bg_ph;
+    fa.multiplicity = o->multiplicity;
+    unsigned blocks = (unsigned)((total + 255) / 256);
+    if (blocks == 0) blocks = 1;
+    if (o->multiplicity >= 0) {
+        k_filter_count<<<blocks, 256, 0, s>>>(fa);
+        CUDA_TRY(cudaGetLastError());
+    }
+    k_compact<<<blocks, 256, 0, s>>>(fa, counters, *d_out, out_capacity);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(&h, counters, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->n_primaries = n;
+        stats->n_out = h.n_out;
+        stats->n_created = total;
+        stats->lepton_steps = h.lepton_steps;
+        stats->photon_steps = h.photon_steps;
+        stats->emissions = h.emissions;
+        stats->pair_events = h.pair_events;
+        stats->rejections = h.rejections;
+        stats->particle_errors = h.errors;
+        stats->waves = waves;
+    }
+    if (h.n_out > out_capacity)
+        return set_err(PTG_ERR_QUEUE_OVERFLOW, "the output needs " + std::to_string(h.n_out) + " rows, out_capacity is " +
+                                                   std::to_string(out_capacity));
+    d_out->n = h.n_out;
+    return PTG_OK;
+}
