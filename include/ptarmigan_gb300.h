@@ -251,6 +251,14 @@ ptg_status ptg_lcfa_photon_sample(ptg_ctx* ctx, size_t n, const double* chi, con
                                   const double* rand3, double* omega, double* theta);
 ptg_status ptg_lcfa_pair_t(ptg_ctx* ctx, size_t n, const double* chi, double* t_par, double* t_perp);
 
+/* Table maintenance: regenerates the CP nonlinear-Compton harmonic CDF
+ * table on the device.  The reference ships it as
+ * nonlinear_compton/cp/tables/cdf.rs, which is absent from its tree; this
+ * is its generator (nonlinear_compton/cp/mod.rs:472-612) on the GPU.
+ * cdf_out: [70*61][32][2] (eta-major grid, [n, cdf(n)] nodes);
+ * total_out: [70*61] total rates, to check against the shipped totals. */
+ptg_status ptg_regen_nlc_cp_cdf(ptg_ctx* ctx, double* cdf_out, double* total_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,12 +2,14 @@
 // smoke() and bench.py's CPU-baseline leg.  Built into
 // oracle/_build/liboracle.so; nothing in the product library links it.
 #include <atomic>
+#include <string>
 #include <cmath>
 #include <cstring>
 #include <thread>
 #include <vector>
 
 #include "fields.h"
+#include "lma.h"
 #include "physics.h"
 
 using namespace orc;
@@ -156,6 +158,64 @@ void orc_push_steps(const ptg_laser_desc* d, size_t n, double* r, double* u, dou
         put4(u + 4 * i, uu);
         if (work) work[i] = w;
     }
+}
+
+int orc_load_tables(const char* dir) {
+    std::string err;
+    return load_lma_tables(dir, &err) ? 0 : 1;
+}
+int orc_has_cp_cdf(void) { return g_lma.nlc_cp_cdf != nullptr; }
+
+double orc_bessel_j(double x, int n) { return bessel_j(x, n); }
+double orc_bessel_triple_j(int n, double x) { return bessel_triple_j_mid(n, x); }
+double orc_bessel_j_asymptotic(int n, double x) { return bessel_j_asymptotic(n, x); }
+void orc_bessel_j_pm(double x, int n, double* out3) { bessel_j_pm(x, n, &out3[0], &out3[1], &out3[2]); }
+
+double orc_cp_diff_partial_rate(int n, double a, double eta, double v) { return cp_diff_partial_rate(n, a, eta, v); }
+double orc_cp_ceiling(int n, double a, double eta) { return cp_ceiling_diff_partial_rate(n, a, eta); }
+double orc_cp_partial_rate(int n, double a, double eta) { return cp_partial_rate(n, a, eta); }
+double orc_cp_rate(double a, double eta) {
+    double r;
+    return cp_rate(a, eta, &r) ? r : NAN;
+}
+int orc_cp_invert(double a, double eta, double frac) { return cp_invert(a, eta, frac); }
+
+// One CP emission sample with the stream (seed, stream, step): n, s, theta, Stokes[4]
+int orc_cp_sample(double a, double eta, uint64_t seed, uint64_t stream, uint32_t step, double* out7) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n;
+    double s, th;
+    Stokes sv;
+    uint64_t rej = 0;
+    int st = cp_sample(a, eta, rng, &n, &s, &th, &sv, &rej);
+    out7[0] = n, out7[1] = s, out7[2] = th, out7[3] = sv.i, out7[4] = sv.q, out7[5] = sv.u, out7[6] = sv.v;
+    return st;
+}
+
+// LMA emission (nonlinear_compton::generate) for given k, q, with a stream
+int orc_nlc_generate(const double* k, const double* q, int pol, double pol_angle, uint64_t seed, uint64_t stream,
+                     uint32_t step, double* out9) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n;
+    V4 kp;
+    Stokes sv;
+    uint64_t rej = 0;
+    int st = nlc_generate(v4(k), v4(q), pol, pol_angle, false, rng, &n, &kp, &sv, &rej);
+    out9[0] = n;
+    put4(out9 + 1, kp);
+    out9[5] = sv.i, out9[6] = sv.q, out9[7] = sv.u, out9[8] = sv.v;
+    return st;
+}
+
+double orc_nlc_probability(const double* k, const double* q, double dt, int pol) {
+    double p;
+    return nlc_probability(v4(k), v4(q), dt, pol, false, &p) ? p : NAN;
 }
 
 struct OrcResult {

@@ -1,20 +1,888 @@
 // Oracle (test infrastructure only): see lma.h.
 #include "lma.h"
 
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../ptarmigan_gb300/tables/ptg_tables_small.h"
+
 namespace orc {
 
-int lma_radiate(const Laser&, const V4&, const V4&, double, DrawStream&, bool, bool* emitted, RadiationEvent*,
-                uint64_t*) {
-    *emitted = false;
-    return PTG_ERR_UNSUPPORTED;
+LmaTables g_lma;
+
+static inline double powi(double a, int b) {
+    bool recip = b < 0;
+    unsigned n = recip ? (unsigned)(-b) : (unsigned)b;
+    double r = 1.0;
+    while (true) {
+        if (n & 1u) r *= a;
+        n >>= 1;
+        if (n == 0) break;
+        a *= a;
+    }
+    return recip ? 1.0 / r : r;
+}
+static inline double sq(double x) { return x * x; }
+constexpr double FRAC_PI_2 = 1.57079632679489661923132169163975144;
+constexpr double FRAC_PI_4 = 0.785398163397448309615660845819875721;
+constexpr double SQRT_2 = 1.41421356237309504880168872420969808;
+
+// ----------------------------------------------------------- tables ----
+static std::vector<std::vector<double>> g_store;
+
+static bool read_ptgt(const std::string& path, std::vector<double>* data) {
+    FILE* fp = std::fopen(path.c_str(), "rb");
+    if (!fp) return false;
+    char magic[4];
+    uint32_t nd = 0;
+    bool ok = std::fread(magic, 1, 4, fp) == 4 && std::memcmp(magic, "PTGT", 4) == 0 && std::fread(&nd, 4, 1, fp) == 1 &&
+              nd > 0 && nd < 8;
+    size_t n = 1;
+    if (ok) {
+        std::vector<uint32_t> shape(nd);
+        ok = std::fread(shape.data(), 4, nd, fp) == nd;
+        for (uint32_t d : shape) n *= d;
+    }
+    if (ok) {
+        data->resize(n);
+        ok = std::fread(data->data(), 8, n, fp) == n;
+    }
+    std::fclose(fp);
+    return ok;
 }
 
-int lma_pair_create(const Laser&, const V4&, const V4&, const Stokes& pol, double, DrawStream&, double, double* prob,
-                    Stokes* pol_new, bool* created, PairEvent*, uint64_t*) {
+bool load_lma_tables(const std::string& dir, std::string* err) {
+    struct Want {
+        const char* name;
+        const double** slot;
+        size_t count;
+        bool required;
+    } wants[] = {
+        {"nlc_lp_rate", &g_lma.nlc_lp_rate, 68 * 61, true},
+        {"nlc_lp_cdf", &g_lma.nlc_lp_cdf, 4148 * 16 * 2, true},
+        {"nlc_cp_rate", &g_lma.nlc_cp_rate, 70 * 61, true},
+        {"nlc_cp_cdf", &g_lma.nlc_cp_cdf, 4270 * 32 * 2, false},
+        {"nlc_lp_classical_rate", &g_lma.nlc_lp_cl_rate, 61, true},
+        {"nlc_lp_classical_cdf", &g_lma.nlc_lp_cl_cdf, 61 * 16 * 2, true},
+        {"nlc_cp_classical_rate", &g_lma.nlc_cp_cl_rate, 61, true},
+        {"nlc_cp_classical_cdf", &g_lma.nlc_cp_cl_cdf, 61 * 32 * 2, true},
+        {"bw_cp_total", &g_lma.bw_cp_total, 121 * 74 * 2, true},
+        {"bw_lp_total", &g_lma.bw_lp_total, 61 * 25 * 2, true},
+        {"bw_lp_cdf", &g_lma.bw_lp_cdf, 1525 * 16 * 3, true},
+        {"bw_lp_mid_total", &g_lma.bw_lp_mid_total, 157 * 36 * 2, true},
+        {"bw_lp_mid_cdf", &g_lma.bw_lp_mid_cdf, 5652 * 16 * 3, false},
+    };
+    for (auto& w : wants) {
+        std::vector<double> data;
+        std::string path = dir + "/" + w.name + ".ptgt";
+        if (!read_ptgt(path, &data)) {
+            if (w.required) {
+                *err = "cannot read " + path;
+                return false;
+            }
+            continue;
+        }
+        if (data.size() != w.count) {
+            *err = path + " has the wrong size";
+            return false;
+        }
+        g_store.push_back(std::move(data));
+        *w.slot = g_store.back().data();
+    }
+    return true;
+}
+
+// ----------------------------------------------------------- Bessel ----
+// special_functions/bessel.rs:38-70
+static double j0(double x) {
+    if (x < 0.1) return 1.0 - x * x / 4.0 + x * x * x * x / 64.0;
+    if (x < 5.0) {
+        double s = 0.0;
+        for (int k = 0; k < 16; ++k)
+            s += PTG_GAUSS_16_WEIGHTS[k] * 0.5 * std::cos(-x * std::sin(FRAC_PI_2 * (PTG_GAUSS_16_NODES[k] + 1.0)));
+        return s;
+    }
+    if (x < 20.0) {
+        double s = 0.0;
+        for (int k = 0; k < 32; ++k)
+            s += PTG_GAUSS_32_WEIGHTS[k] * 0.5 * std::cos(-x * std::sin(FRAC_PI_2 * (PTG_GAUSS_32_NODES[k] + 1.0)));
+        return s;
+    }
+    double pre = std::sqrt(2.0 / (PI * x));
+    double phase = FRAC_PI_4 - x;
+    if (x < 60.0)
+        return pre * ((1.0 - 9.0 / (128.0 * x * x) + 3675.0 / (32768.0 * x * x * x * x) - 0.5725014209747314 * powi(x, -6)) *
+                          std::cos(phase) -
+                      (1.0 / (8.0 * x) - 75.0 / (1024.0 * x * x * x) + 0.2271080017089844 * powi(x, -5)) * std::sin(phase));
+    return pre * ((1.0 - 9.0 / (128.0 * x * x) + 3675.0 / (32768.0 * x * x * x * x)) * std::cos(phase) -
+                  (1.0 / (8.0 * x) - 75.0 / (1024.0 * x * x * x)) * std::sin(phase));
+}
+
+// special_functions/bessel.rs:72-112
+static double j1(double x) {
+    if (x < 0.1) return (x / 2.0) * (1.0 - x * x / 8.0 + x * x * x * x / 192.0);
+    if (x < 5.0) {
+        double s = 0.0;
+        for (int k = 0; k < 16; ++k) {
+            double t = FRAC_PI_2 * (PTG_GAUSS_16_NODES[k] + 1.0);
+            s += PTG_GAUSS_16_WEIGHTS[k] * 0.5 * std::cos(t - x * std::sin(t));
+        }
+        return s;
+    }
+    if (x < 20.0) {
+        double s = 0.0;
+        for (int k = 0; k < 32; ++k) {
+            double t = FRAC_PI_2 * (PTG_GAUSS_32_NODES[k] + 1.0);
+            s += PTG_GAUSS_32_WEIGHTS[k] * 0.5 * std::cos(t - x * std::sin(t));
+        }
+        return s;
+    }
+    double pre = std::sqrt(2.0 / (PI * x));
+    double phase = FRAC_PI_4 + x;
+    if (x < 60.0)
+        return pre * (-(1.0 + 15.0 / (128.0 * x * x) - 4725.0 / (32768.0 * x * x * x * x) + 0.6765925884246826 * powi(x, -6)) *
+                          std::cos(phase) +
+                      (3.0 / (8.0 * x) - 105.0 / (1024.0 * x * x * x) + 0.2775764465332031 * powi(x, -5)) * std::sin(phase));
+    return pre * (-(1.0 + 15.0 / (128.0 * x * x) - 4725.0 / (32768.0 * x * x * x * x)) * std::cos(phase) +
+                  (3.0 / (8.0 * x) - 105.0 / (1024.0 * x * x * x)) * std::sin(phase));
+}
+
+static inline int rem_euclid2(int n) { return ((n % 2) + 2) % 2; }
+
+// special_functions/bessel.rs:117-176: Miller's backward recurrence,
+// normalised by J0 + 2 sum J_2k = 1.
+static void triple_j(int n, double x, double* a, double* b, double* c) {
+    if (x == 0.0) {
+        *a = (n == 1) ? 1.0 : 0.0;
+        *b = (n == 0) ? 1.0 : 0.0;
+        *c = (n == -1) ? 1.0 : 0.0;
+        return;
+    }
+    double v = x / (double)n;
+    int nmax = 1 + n + (int)(5.0 / (1.0 - 0.9 * v));
+    if (rem_euclid2(nmax) != 0) nmax += 1;
+    int n_even = rem_euclid2(n) == 0 ? 1 : 0;
+    int k_stop = n - 1 - n_even;
+    double quad[4] = {1.0, 0.0, 0.0, 0.0};
+    double total = 0.0;
+    // (k_stop..=nmax).rev().step_by(2): nmax, nmax-2, ... >= k_stop
+    for (int k = nmax; k >= k_stop; k -= 2) {
+        quad[3] = quad[1];
+        quad[2] = quad[0];
+        quad[1] = (double)(2 * (k + 2)) * quad[2] / x - quad[3];
+        quad[0] = (double)(2 * (k + 1)) * quad[1] / x - quad[2];
+        total += quad[0];
+    }
+    int idx = n_even;
+    double t0 = quad[idx], t1 = quad[idx + 1], t2 = quad[idx + 2];
+    // (0..=k_stop).rev().step_by(2).skip(1): k_stop-2, k_stop-4, ... >= 0
+    if (k_stop >= 0) {
+        for (int k = k_stop - 2; k >= 0; k -= 2) {
+            quad[3] = quad[1];
+            quad[2] = quad[0];
+            quad[1] = (double)(2 * (k + 2)) * quad[2] / x - quad[3];
+            quad[0] = (double)(2 * (k + 1)) * quad[1] / x - quad[2];
+            total += quad[0];
+        }
+    }
+    double norm = 2.0 * total - quad[0];
+    if (std::isnan(norm)) {
+        *a = *b = *c = 0.0;
+    } else {
+        *a = t0 / norm;
+        *b = t1 / norm;
+        *c = t2 / norm;
+    }
+}
+
+// special_functions/bessel.rs:178-199: uniform asymptotic (Airy) expansion
+static double zeta_at(double z) {
+    if (z < 1.0) {
+        double tmp = std::log((1.0 + std::sqrt(1.0 - z * z)) / z) - std::sqrt(1.0 - z * z);
+        return std::pow(3.0 * tmp / 2.0, 2.0 / 3.0);
+    }
+    double tmp = std::sqrt(z * z - 1.0) - std::acos(1.0 / z);
+    return -std::pow(3.0 * tmp / 2.0, 2.0 / 3.0);
+}
+
+double bessel_j_asymptotic(int n, double x) {
+    double m = (double)n;
+    double z = x / m;
+    double zeta = zeta_at(z);
+    bool ok;
+    double arg = std::pow(m, 2.0 / 3.0) * zeta;
+    double ai = airy_ai(arg, &ok);
+    if (!ok) ai = 0.0;
+    double aip = airy_ai_prime(arg, &ok);
+    if (!ok) aip = 0.0;
+    double pre = 4.0 * zeta / (1.0 - z * z);
+    double bk = 5.0 / (48.0 * zeta * zeta) - (2.0 + 3.0 * z * z) / (24.0 * std::sqrt(zeta) * std::pow(1.0 - z * z, 1.5));
+    return std::pow(pre, 0.25) * (ai / std::pow(m, 1.0 / 3.0) - aip * bk / std::pow(m, 5.0 / 3.0));
+}
+
+double bessel_triple_j_mid(int n, double x) {
+    double a, b, c;
+    triple_j(n, x, &a, &b, &c);
+    return b;
+}
+
+// bessel.rs:26-34
+void bessel_j_pm(double x, int n, double* jm1, double* j, double* jp1) {
+    if (n < 1000) {
+        triple_j(n, x, jm1, j, jp1);
+    } else {
+        double jn = bessel_j_asymptotic(n, x);
+        double jp = bessel_j_asymptotic(n + 1, x);
+        *jm1 = (double)(2 * n) * jn / x - jp;
+        *j = jn;
+        *jp1 = jp;
+    }
+}
+
+// bessel.rs:18-24
+double bessel_j(double x, int n) {
+    if (n == 0) return j0(x);
+    if (n == 1) return j1(x);
+    return bessel_triple_j_mid(n, x);
+}
+
+// --------------------------------------------------- CP LMA emission ---
+// nonlinear_compton/cp/mod.rs:17-38
+double cp_diff_partial_rate(int n, double a, double eta, double v) {
+    if (v < 0.0 || v >= 1.0) return 0.0;
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double smax = sn / (1.0 + sn);
+    double vs = v * smax;
+    double z = std::sqrt(4.0 * powi((double)n, 2) * (a * a / (1.0 + a * a)) * (vs / (sn * (1.0 - vs))) *
+                         (1.0 - vs / (sn * (1.0 - vs))));
+    double jm, j, jp;
+    bessel_j_pm(z, n, &jm, &j, &jp);
+    return -smax * (powi(j, 2) + 0.5 * a * a * (1.0 + 0.5 * powi(vs, 2) / (1.0 - vs)) * (2.0 * powi(j, 2) - powi(jp, 2) - powi(jm, 2)));
+}
+
+// nonlinear_compton/cp/mod.rs:42-75
+double cp_ceiling_diff_partial_rate(int n, double a, double eta) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    int n_switch = (int)(32.3 * (1.0 + 0.476 * std::pow(a, 1.56)));
+    double mx;
+    if (sn < 2.0 || n < n_switch) {
+        double v_opt = (1.0 + sn) / (2.0 + sn);
+        double lower = -HUGE_VAL, upper = -HUGE_VAL;
+        for (int i = 0; i < 16; ++i) lower = std::max(lower, cp_diff_partial_rate(n, a, eta, i * v_opt / 16.0));
+        for (int i = 0; i < 16; ++i)
+            upper = std::max(upper, cp_diff_partial_rate(n, a, eta, v_opt + i * (1.0 - v_opt) / 16.0));
+        mx = std::max(lower, upper);
+    } else {
+        double lower = -HUGE_VAL, upper = -HUGE_VAL;
+        for (int k = 0; k < 16; ++k) {
+            double u = 0.5 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
+            lower = std::max(lower, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
+        }
+        for (int k = 0; k < 16; ++k) {
+            double u = (1.0 + sn) + 0.5 * 2.0 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
+            upper = std::max(upper, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
+        }
+        mx = std::max(lower, upper);
+    }
+    return 1.2 * mx;
+}
+
+// nonlinear_compton/cp/mod.rs:78-87
+double cp_spectrum_low_eta(int n, double a, double v) {
+    if (v < 0.0 || v >= 1.0) return 0.0;
+    double z = std::sqrt(4.0 * a * a * powi((double)n, 2) * v * (1.0 - v) / (1.0 + a * a));
+    double jm, j, jp;
+    bessel_j_pm(z, n, &jm, &j, &jp);
+    return n * (a * a * powi(jm, 2) - 2.0 * (1.0 + a * a) * powi(j, 2) + a * a * powi(jp, 2)) / (1.0 + a * a);
+}
+
+// nonlinear_compton/cp/mod.rs:92-136
+double cp_partial_rate(int n, double a, double eta) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    int n_switch = (int)(32.3 * (1.0 + 0.476 * std::pow(a, 1.56)));
+    double lower = 0.0, upper = 0.0;
+    if (sn < 2.0 || n < n_switch) {
+        double vmid = (1.0 + sn) / (2.0 + sn);
+        for (int k = 0; k < 32; ++k) {
+            double v = 0.5 * vmid * (PTG_GAUSS_32_NODES[k] + 1.0);
+            lower += 0.5 * vmid * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, v);
+        }
+        for (int k = 0; k < 32; ++k) {
+            double v = vmid + 0.5 * (1.0 - vmid) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            upper += 0.5 * (1.0 - vmid) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, v);
+        }
+    } else {
+        for (int k = 0; k < 32; ++k) {
+            double u = 0.5 * (1.0 + sn) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            lower += 0.5 * (1.0 + sn) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, u / (1.0 + u)) / powi(1.0 + u, 2);
+        }
+        for (int k = 0; k < 32; ++k) {
+            double u = (1.0 + sn) + 0.5 * 2.0 * (1.0 + sn) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            upper += 0.5 * 2.0 * (1.0 + sn) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, u / (1.0 + u)) /
+                     powi(1.0 + u, 2);
+        }
+    }
+    return lower + upper;
+}
+
+// nonlinear_compton/cp/classical.rs:22-43
+bool cp_classical_rate(double a, double eta, double* out) {
+    double x = std::log(a);
+    if (x < PTG_NLC_CL_MIN) {
+        *out = 2.0 * a * a * eta / 3.0;
+        return true;
+    }
+    int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    if (ix < 61 - 1) {
+        double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+        double f = (1.0 - dx) * g_lma.nlc_cp_cl_rate[ix] + dx * g_lma.nlc_cp_cl_rate[ix + 1];
+        *out = eta * std::exp(f);
+        return true;
+    }
+    return false;
+}
+
+// nonlinear_compton/cp/mod.rs:160-176, tables/mod.rs:11-35
+bool cp_rate(double a, double eta, double* out) {
+    const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
+    if (std::log(eta) < MIN1) return cp_classical_rate(a, eta, out);
+    if (std::log(a) < MIN0) {
+        *out = a * a * (2.0 + 8.0 * eta + 9.0 * eta * eta + eta * eta * eta) / (2.0 * eta * powi(1.0 + 2.0 * eta, 2)) -
+               a * a * (2.0 + 2.0 * eta - eta * eta) * std::log(1.0 + 2.0 * eta) / (4.0 * eta * eta);
+        return true;
+    }
+    bool contains = std::log(a) >= MIN0 && a < 20.0 && std::log(eta) >= MIN1 && eta < 2.0;
+    if (!contains) return false;
+    int ia = (int)((std::log(a) - MIN0) / S0);
+    int ie = (int)((std::log(eta) - MIN1) / S1);
+    if (ia >= 61 - 1 || ie >= 70 - 1) return false;
+    double da = (std::log(a) - MIN0) / S0 - ia;
+    double de = (std::log(eta) - MIN1) / S1 - ie;
+    const double* T = g_lma.nlc_cp_rate;
+    double f = (1.0 - da) * (1.0 - de) * T[ie * 61 + ia] + da * (1.0 - de) * T[ie * 61 + ia + 1] +
+               (1.0 - da) * de * T[(ie + 1) * 61 + ia] + da * de * T[(ie + 1) * 61 + ia + 1];
+    *out = std::exp(f);
+    return true;
+}
+
+// nonlinear_compton/cp/tables/mod.rs:37-45: [ln n, ln(-ln(1 - cdf))] of the first 31 rows
+static void cp_rescale(double frac, const double* table, double* frac2, double* out /*[31][2]*/) {
+    for (int i = 0; i < 31; ++i) {
+        out[2 * i] = std::log(table[2 * i]);
+        out[2 * i + 1] = std::log(-1.0 * std::log(1.0 - table[2 * i + 1]));
+    }
+    *frac2 = std::log(-1.0 * std::log(1.0 - frac));
+}
+
+// nonlinear_compton/cp/tables/mod.rs:47-121 (needs the regenerated CDF table)
+int cp_invert(double a, double eta, double frac) {
+    const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
+    const double* T = g_lma.nlc_cp_cdf;
+    if (std::log(a) <= MIN0) return 1;
+    auto corner = [&](int idx) {
+        const double* table = T + (size_t)idx * 64;
+        if (frac <= table[1]) return 0.9;
+        double f2, rs[62];
+        cp_rescale(frac, table, &f2, rs);
+        bool ok;
+        return std::exp(Pwmci(rs, 31, true).invert(f2, &ok));
+    };
+    if (std::log(eta) <= MIN1) {
+        int ix = (int)((std::log(a) - MIN0) / S0);
+        double dx = (std::log(a) - MIN0) / S0 - ix;
+        double n = corner(ix) * (1.0 - dx) + corner(ix + 1) * dx;
+        return (int)std::ceil(n);
+    }
+    int ix = (int)((std::log(a) - MIN0) / S0);
+    int iy = (int)((std::log(eta) - MIN1) / S1);
+    double dx = (std::log(a) - MIN0) / S0 - ix;
+    double dy = (std::log(eta) - MIN1) / S1 - iy;
+    int idx[4] = {61 * iy + ix, 61 * iy + ix + 1, 61 * (iy + 1) + ix, 61 * (iy + 1) + ix + 1};
+    double w[4] = {(1.0 - dx) * (1.0 - dy), dx * (1.0 - dy), (1.0 - dx) * dy, dx * dy};
+    double n = 0.0;
+    for (int k = 0; k < 4; ++k) n += corner(idx[k]) * w[k];
+    return (int)std::ceil(n);
+}
+
+// nonlinear_compton/cp/mod.rs:181-234
+int cp_sample(double a, double eta, DrawStream& rng, int* n_out, double* s_out, double* theta_out, Stokes* sv_out,
+              uint64_t* rej) {
+    if (!g_lma.nlc_cp_cdf) return PTG_ERR_TABLES;
+    int n = cp_invert(a, eta, rng.next());
+    double mx = cp_ceiling_diff_partial_rate(n, a, eta);
+    double v = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next(), u = rng.next();
+        if (u <= cp_diff_partial_rate(n, a, eta, vv) / mx) {
+            v = vv;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double s = v * (sn / (1.0 + sn));
+    double theta = 2.0 * PI * rng.next();
+    double z = std::sqrt((double)(4 * n * n) * (a * a / (1.0 + a * a)) * (s / (sn * (1.0 - s))) * (1.0 - s / (sn * (1.0 - s))));
+    double jm, j, jp;
+    bessel_j_pm(z, n, &jm, &j, &jp);
+    const double LASER_S3 = -1.0;
+    double xi0 = (1.0 - s + 1.0 / (1.0 - s)) * (jm * jm + jp * jp - 2.0 * j * j) - powi(2.0 * j / a, 2);
+    double xi1 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) + 8.0 * j * j * (1.0 - powi((double)n / z, 2) - 0.5 / (a * a));
+    double xi2 = 0.0;
+    double xi3 = LASER_S3 * (1.0 - s + 1.0 / (1.0 - s)) * (1.0 - 2.0 * s / (sn * (1.0 - s))) * (jm * jm - jp * jp);
+    Stokes sv(1.0, xi1 / xi0, xi2 / xi0, xi3 / xi0);
+    *sv_out = sv.rotate_by(FRAC_PI_2 + theta);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return PTG_OK;
+}
+
+// nonlinear_compton/lp/linear.rs:6-48
+double lp_linear_rate(double a, double eta) {
+    double eta2 = eta * eta, eta3 = eta2 * eta;
+    if (eta > 1.0e-3)
+        return (a * a / 8.0) *
+               (0.5 + 4.0 / eta - 0.5 / ((1.0 + 2.0 * eta) * (1.0 + 2.0 * eta)) + (1.0 - 2.0 / eta - 2.0 / eta2) * std::log(1.0 + 2.0 * eta));
+    return (a * a / 8.0) * (8.0 * eta / 3.0 - 16.0 * eta2 / 3.0 + 208.0 * eta3 / 15.0);
+}
+
+// ------------------------------------------------- LMA NLC dispatch ----
+// nonlinear_compton/mod.rs:19-47
+bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classical, double* p) {
+    double a_sqd = q * q - 1.0;
+    double a = a_sqd >= 0.0 ? std::sqrt(a_sqd) : 0.0;
+    double eta = k * q;
+    double dphi = dt * eta / (COMPTON_TIME * q.t);
+    double f;
+    bool ok;
+    if (pol == PTG_POL_CIRCULAR) {
+        ok = classical ? cp_classical_rate(a, eta, &f) : cp_rate(a, eta, &f);
+    } else {
+        return false;  // the LP rates are added with the LP sampler
+    }
+    if (!ok) return false;
+    *p = ALPHA_FINE * f * dphi / eta;
+    return true;
+}
+
+// nonlinear_compton/mod.rs:58-138
+int nlc_generate(const V4& k, const V4& q, int pol, double pol_angle, bool classical, DrawStream& rng, int* n_out,
+                 V4* k_out, Stokes* sv_out, uint64_t* rej) {
+    double a = std::sqrt(q * q - 1.0);
+    double eta = k * q;
+    int n;
+    double s, cphi;
+    Stokes sv;
+    int st;
+    if (pol == PTG_POL_CIRCULAR && !classical) {
+        st = cp_sample(a, eta, rng, &n, &s, &cphi, &sv, rej);
+    } else {
+        return PTG_ERR_UNSUPPORTED;
+    }
+    if (st != PTG_OK) return st;
+    double ell = n;
+    double p_zmf = classical ? ell * eta / std::sqrt(1.0 + a * a) : ell * eta / std::sqrt(1.0 + a * a + 2.0 * ell * eta);
+    double ct = classical ? 1.0 - s * (1.0 + a * a) / (ell * eta) : 1.0 - s * (1.0 + a * a + 2.0 * ell * eta) / (ell * eta);
+    if (!(ct <= 1.0 && ct >= -1.0)) return PTG_ERR_SANITY;
+    V4 u_zmf;
+    if (classical) {
+        u_zmf = q / std::sqrt(q.t * q.t - q.x * q.x - q.y * q.y - q.z * q.z);
+    } else {
+        V4 t = q + ell * k;
+        u_zmf = t / std::sqrt(t * t);
+    }
+    V3 along = classical ? (ell * k).boost_by(u_zmf).spatial().normalize() : -(q.boost_by(u_zmf).spatial().normalize());
+    V4 eps4(0.0, std::cos(pol_angle), std::sin(pol_angle), 0.0);
+    V3 eps = eps4.boost_by(u_zmf).spatial().normalize();
+    eps = along.cross(eps.cross(along)).normalize();
+    V3 perp = eps.rotate_around(along, cphi);
+    V3 kp = p_zmf * (ct * along + std::sqrt(1.0 - ct * ct) * perp);
+    V4 kprime = V4::lightlike(kp.x, kp.y, kp.z);
+    V4 rev(u_zmf.t, -u_zmf.x, -u_zmf.y, -u_zmf.z);
+    kprime = kprime.boost_by(rev);
+    sv = sv.rotate_by(-pol_angle);
+    sv = sv.from_lma_basis(kprime);
+    double s_new = (k * kprime) / (k * q);
+    double err = std::fabs(s - s_new) / s;
+    if (err >= 1.0e-2) return PTG_ERR_SANITY;
+    *n_out = n;
+    *k_out = kprime;
+    *sv_out = sv;
+    return PTG_OK;
+}
+
+double std_normal(DrawStream& rng) {
+    double u1 = rng.next(), u2 = rng.next();
+    return std::sqrt(-2.0 * std::log(1.0 - u1)) * std::cos(2.0 * PI * u2);
+}
+
+// plane_wave.rs:251-282, focused_laser.rs:260-281
+int lma_radiate(const Laser& L, const V4& r, const V4& u, double dt, DrawStream& rng, bool classical, bool* emitted,
+                RadiationEvent* ev, uint64_t* rej) {
+    *emitted = false;
+    double a = std::sqrt(L.a_sqd(r));
+    double chirp = 1.0;
+    if (L.d.model == PTG_PLANE_WAVE) {
+        double phase = L.wavevector * r;
+        chirp = 1.0 + 2.0 * L.d.chirp_b * phase;
+        if (chirp < 0.0 && a > 0.0) return PTG_ERR_SANITY;
+    }
+    double width = 1.0;
+    if (L.bandwidth != 0.0) {
+        width = 1.0 + L.bandwidth * std_normal(rng);
+        if (!(width > 0.0)) return PTG_ERR_SANITY;
+    }
+    V4 kappa = (SPEED_OF_LIGHT * COMPTON_TIME) * L.wavevector * chirp * width;
+    double prob;
+    if (!nlc_probability(kappa, u, dt, L.d.polarization, classical, &prob)) {
+        return L.d.polarization == PTG_POL_CIRCULAR ? PTG_ERR_OUT_OF_TABLE : PTG_ERR_UNSUPPORTED;
+    }
+    if (rng.next() < prob) {
+        int n;
+        V4 k;
+        Stokes pol;
+        int st = nlc_generate(kappa, u, L.d.polarization, L.d.pol_angle, classical, rng, &n, &k, &pol, rej);
+        if (st != PTG_OK) return st;
+        ev->k = k;
+        ev->u_prime = u + (double)n * kappa - k;
+        ev->pol = pol;
+        ev->a_eff = a;
+        ev->chi = a * (u * kappa);
+        ev->absorption = (double)n * kappa.t;
+        *emitted = true;
+    }
+    return PTG_OK;
+}
+
+// ------------------------------------------------- CP LMA pair creation --
+// pair_creation/cp/mod.rs:24-243 (DoubleDiffPartialRate) and :248-449 (TotalRate)
+static const double PAIR_LASER_S3 = -1.0;
+
+static void cpp_s_bounds(int n, double a, double eta, double* s_min, double* s_max) {
+    double sn = 2.0 * n * eta / (1.0 + powi(a, 2));
+    double smin = 0.5 * (1.0 - std::sqrt(1.0 - 4.0 / sn));
+    *s_min = std::min(smin, 0.5);
+    *s_max = 0.5;
+}
+
+static void cpp_elements(int n, double a, double eta, double s, double* unpol, double* d12, double* d3) {
+    double ell = n;
+    double sn = 2.0 * ell * eta / (1.0 + powi(a, 2));
+    double tmp = 1.0 / (sn * s * (1.0 - s));
+    double z = std::sqrt((4.0 * ell * ell) * (powi(a, 2) / (1.0 + powi(a, 2))) * tmp * (1.0 - tmp));
+    double jm, j, jp;
+    bessel_j_pm(z, n, &jm, &j, &jp);
+    *unpol = powi(j, 2) + 0.25 * powi(a, 2) * ((1.0 - s) / s + s / (1.0 - s)) * (powi(jm, 2) + powi(jp, 2) - 2.0 * powi(j, 2));
+    *d12 = (2.0 * powi(ell * a / z, 2) - (1.0 + powi(a, 2))) * powi(j, 2) - 0.5 * powi(a, 2) * (powi(jm, 2) + powi(jp, 2));
+    *d3 = 0.25 * powi(a, 2) * ((1.0 - s) / s + s / (1.0 - s)) * (1.0 - 2.0 / (sn * s * (1.0 - s))) * (powi(jm, 2) - powi(jp, 2));
+}
+
+// pair_creation/cp/mod.rs:66-72.  (2 theta).sin_cos() returns (sin, cos):
+// the reference binds them to (cos_2theta, sin_2theta) in that order.
+static double cpp_fully_resolved(int n, double a, double eta, double s, double theta, double sv1, double sv2, double sv3) {
+    double unpol, d12, d3;
+    cpp_elements(n, a, eta, s, &unpol, &d12, &d3);
+    double cos_2theta = std::sin(2.0 * theta), sin_2theta = std::cos(2.0 * theta);
+    return (unpol - (sv1 * cos_2theta + sv2 * sin_2theta) * d12 - PAIR_LASER_S3 * sv3 * d3) / (2.0 * PI);
+}
+
+static void cpp_over_theta(int n, double a, double eta, double s, double* re, double* im) {
+    double unpol, d12, d3;
+    cpp_elements(n, a, eta, s, &unpol, &d12, &d3);
+    *re = unpol - PAIR_LASER_S3 * d3;
+    *im = unpol + PAIR_LASER_S3 * d3;
+}
+
+static double cpp_over_theta_s3(int n, double a, double eta, double s, double sv3) {
+    double re, im;
+    cpp_over_theta(n, a, eta, s, &re, &im);
+    return 0.5 * (re * (1.0 + sv3) + im * (1.0 - sv3));
+}
+
+// pair_creation/cp/mod.rs:92-186
+void cp_pair_integrate(int n, double a, double eta, double* out_re, double* out_im) {
+    double ell = n;
+    double sn = 2.0 * ell * eta / (1.0 + a * a);
+    *out_re = 0.0, *out_im = 0.0;
+    if (sn <= 4.0) return;
+    double beta = powi(a, 4) * powi(1.0 / ell + 1.0, 2) + 16.0 * powi(a * a - 2.0, 2) / (sn * sn) - 8.0 * a * a * (a * a - 2.0) / sn;
+    beta = std::sqrt(beta) / (a * a - 2.0);
+    double alpha = (a * a + 2.0 * ell) / (ell * (2.0 - a * a)) - 4.0 / sn;
+    double tmp = alpha + beta;
+    double s_peak = 0.5 * (1.0 - std::sqrt(tmp));
+    double s_min, s_max;
+    cpp_s_bounds(n, a, eta, &s_min, &s_max);
+    auto seg = [&](double lo, double hi, double* re, double* im) {
+        double r = 0.0, i = 0.0;
+        for (int k = 0; k < 32; ++k) {
+            double s = 0.5 * (hi - lo) * PTG_GAUSS_32_NODES[k] + 0.5 * (lo + hi);
+            double sr, si;
+            cpp_over_theta(n, a, eta, s, &sr, &si);
+            r += 0.5 * (hi - lo) * PTG_GAUSS_32_WEIGHTS[k] * sr;
+            i += 0.5 * (hi - lo) * PTG_GAUSS_32_WEIGHTS[k] * si;
+        }
+        *re = r, *im = i;
+    };
+    if (std::isfinite(s_peak)) {
+        double s_mid = 2.0 * s_peak - s_min;
+        if (s_mid > s_max) {
+            double lr, li, ur, ui;
+            seg(s_min, s_peak, &lr, &li);
+            seg(s_peak, s_max, &ur, &ui);
+            *out_re = 2.0 * (ur + lr), *out_im = 2.0 * (ui + li);
+        } else {
+            double lr, li, mr, mi, ur, ui;
+            seg(s_min, s_peak, &lr, &li);
+            seg(s_peak, s_mid, &mr, &mi);
+            seg(s_mid, s_max, &ur, &ui);
+            *out_re = 2.0 * (lr + mr + ur), *out_im = 2.0 * (li + mi + ui);
+        }
+    } else {
+        double tr, ti;
+        seg(s_min, s_max, &tr, &ti);
+        *out_re = 2.0 * tr, *out_im = 2.0 * ti;
+    }
+}
+
+// pair_creation/cp/mod.rs:349-365
+static void cpp_sum_limits(double a, double eta, int* n_min, int* n_max) {
+    double nm = std::ceil(2.0 * (1.0 + a * a) / eta);
+    double range = 2.0 * (0.25 + a * a) / eta + 13.0 * a * (2.0 + a);
+    double test = 0.25 - (1.0 + a * a) / (2.0 * nm * eta);
+    if (test <= 2.220446049250313e-16) {
+        *n_min = (int)nm + 1;
+        *n_max = (int)(nm + 1.0 + range);
+    } else {
+        *n_min = (int)nm;
+        *n_max = (int)(nm + range);
+    }
+}
+
+static bool cpp_is_too_small(double a, double eta) {
+    return std::log10(eta) < -1.0 - powi(std::log10(a) + 2.0, 2) / 4.5;
+}
+
+void cp_pair_by_summation(double a, double eta, double f[2]) {
+    int n0, n1;
+    cpp_sum_limits(a, eta, &n0, &n1);
+    double re = 0.0, im = 0.0;
+    for (int n = n0; n <= n1; ++n) {
+        double r, i;
+        cp_pair_integrate(n, a, eta, &r, &i);
+        re += r, im += i;
+    }
+    f[0] = re, f[1] = im;
+}
+
+// pair_creation/cp/mod.rs:395-448; false where the reference panics
+bool cp_pair_by_lookup(double a, double eta, double f[2]) {
+    const double LMA = PTG_BW_CP_LN_MIN_A, LME = PTG_BW_CP_LN_MIN_ETA, SA = PTG_BW_CP_LN_A_STEP, SE = PTG_BW_CP_LN_ETA_STEP;
+    const int NC = 74, NR = 121;
+    const double* T = g_lma.bw_cp_total;
+    double x = std::log(a), y = std::log(eta);
+    if (x < LMA) return false;
+    if (y < LME) {
+        f[0] = f[1] = 0.0;
+        return true;
+    }
+    int ix = (int)((x - LMA) / SA), iy = (int)((y - LME) / SE);
+    if (!(ix < NC - 1 && iy < NR - 1)) return false;
+    auto P = [&](int r, int c, int k) { return T[((size_t)r * NC + c) * 2 + k]; };
+    if (a * eta > 2.0) {
+        double dx = (x - LMA) / SA - ix, dy = (y - LME) / SE - iy;
+        double w[4] = {(1.0 - dx) * (1.0 - dy), dx * (1.0 - dy), (1.0 - dx) * dy, dx * dy};
+        for (int k = 0; k < 2; ++k)
+            f[k] = std::exp(w[0] * P(iy, ix, k) + w[1] * P(iy, ix + 1, k) + w[2] * P(iy + 1, ix, k) + w[3] * P(iy + 1, ix + 1, k));
+    } else {
+        double a_min = std::exp(LMA + ix * SA), a_max = std::exp(LMA + (ix + 1) * SA);
+        double e_min = std::exp(LME + iy * SE), e_max = std::exp(LME + (iy + 1) * SE);
+        double dx = (a - a_min) / (a_max - a_min), dy = (eta - e_min) / (e_max - e_min);
+        double w[4] = {(1.0 - dx) * (1.0 - dy), dx * (1.0 - dy), (1.0 - dx) * dy, dx * dy};
+        for (int k = 0; k < 2; ++k) {
+            double g = w[0] / P(iy, ix, k) + w[1] / P(iy, ix + 1, k) + w[2] / P(iy + 1, ix, k) + w[3] / P(iy + 1, ix + 1, k);
+            f[k] = std::exp(1.0 / g);
+        }
+    }
+    return true;
+}
+
+// TotalRate::probability / value dispatch (pair_creation/cp/mod.rs:265-309)
+bool cp_pair_rates(double a, double eta, double f[2]) {
+    if (a < 0.02 || cpp_is_too_small(a, eta)) {
+        f[0] = f[1] = 0.0;
+        return true;
+    }
+    if (a < std::exp(PTG_BW_CP_LN_MIN_A)) {
+        cp_pair_by_summation(a, eta, f);
+        return true;
+    }
+    return cp_pair_by_lookup(a, eta, f);
+}
+
+// pair_creation/cp/mod.rs:280-309
+static double cpp_probability(const double f[2], double eta, const Stokes& sv, double dphi, Stokes* out) {
+    double f0 = f[0], f1 = f[1];
+    double prob = ALPHA_FINE * (0.5 * ((f0 + f1) + sv.v * (f0 - f1))) * dphi / eta;
+    double prob_avg = ALPHA_FINE * (0.5 * (f0 + f1)) * dphi / eta;
+    double delta = ALPHA_FINE * (0.5 * (f0 - f1)) * dphi / eta;
+    *out = Stokes(sv.i, sv.q * (1.0 - prob_avg) / (1.0 - prob), sv.u * (1.0 - prob_avg) / (1.0 - prob),
+                  (sv.v * (1.0 - prob_avg) - delta) / (1.0 - prob));
+    return prob;
+}
+
+// pair_creation/cp/mod.rs:191-243
+static int cpp_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3, DrawStream& rng,
+                              double* s_out, double* theta_out, uint64_t* rej) {
+    double s_min, s_max;
+    cpp_s_bounds(n, a, eta, &s_min, &s_max);
+    double mx = NAN;
+    for (int k = 0; k < 32; ++k) {
+        double s = 0.5 * (s_max - s_min) * PTG_GAUSS_32_NODES[k] + 0.5 * (s_min + s_max);
+        double v = cpp_over_theta_s3(n, a, eta, s, sv3);
+        mx = std::isnan(mx) ? v : (std::isnan(v) ? mx : std::max(mx, v));
+    }
+    mx *= 1.5;
+    double s = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double ss = s_min + (s_max - s_min) * rng.next();
+        double z = mx * rng.next();
+        if (z < cpp_over_theta_s3(n, a, eta, ss, sv3)) {
+            s = ss;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    if (rng.next() < 0.5) s = 1.0 - s;  // gen_range(0, 2) == 0
+    double theta_opt = 0.5 * std::atan2(sv2, sv1);
+    double tm = -HUGE_VAL;
+    for (int i = 0; i < 4; ++i) tm = std::max(tm, cpp_fully_resolved(n, a, eta, s, theta_opt + i * FRAC_PI_2, sv1, sv2, sv3));
+    tm *= 1.01;
+    double theta = 0.0;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double th = 2.0 * PI * rng.next();
+        double z = tm * rng.next();
+        if (z < cpp_fully_resolved(n, a, eta, s, th, sv1, sv2, sv3)) {
+            theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    *s_out = s;
+    *theta_out = theta;
+    return PTG_OK;
+}
+
+// pair_creation/cp/mod.rs:314-346: harmonic by explicit summation
+static int cpp_sample(double a, double eta, double sv1, double sv2, double sv3, DrawStream& rng, int* n_out, double* s,
+                      double* theta, uint64_t* rej) {
+    int n0, n1;
+    cpp_sum_limits(a, eta, &n0, &n1);
+    double f[2];
+    if (!cp_pair_rates(a, eta, f)) return PTG_ERR_OUT_OF_TABLE;
+    double target = 0.5 * (f[0] * (1.0 + sv3) + f[1] * (1.0 - sv3));
+    target = target * rng.next();
+    double cum = 0.0;
+    int index = -1;
+    for (int k = n0; k <= n1; ++k) {
+        double re, im;
+        cp_pair_integrate(k, a, eta, &re, &im);
+        cum += 0.5 * ((1.0 + sv3) * re + (1.0 - sv3) * im);
+        if (cum > target) {
+            index = k;
+            break;
+        }
+    }
+    if (index == -1) index = n1 - 1;
+    *n_out = index;
+    return cpp_sample_s_theta(index, a, eta, sv1, sv2, sv3, rng, s, theta, rej);
+}
+
+// pair_creation/mod.rs:21-42 (CP only: LP added with its sampler)
+bool bw_probability(const V4& ell, const Stokes& sv_in, const V4& k, double a, double dt, int pol, double pol_angle,
+                    double* prob, Stokes* sv_out) {
+    double eta = k * ell;
+    Stokes sv = sv_in.in_lma_basis(ell).rotate_by(pol_angle);
+    double dphi = eta * dt / (COMPTON_TIME * ell.t);
+    if (pol != PTG_POL_CIRCULAR) return false;
+    double f[2];
+    if (!cp_pair_rates(a, eta, f)) return false;
+    Stokes out;
+    *prob = cpp_probability(f, eta, sv, dphi, &out);
+    *sv_out = out.rotate_by(-pol_angle).from_lma_basis(ell);
+    return true;
+}
+
+// pair_creation/mod.rs:49-110
+int bw_generate(const V4& ell, const Stokes& sv_in, const V4& k, double a, int pol, double pol_angle, DrawStream& rng,
+                int* n_out, V4* q_out, uint64_t* rej) {
+    double eta = k * ell;
+    Stokes sv = sv_in.in_lma_basis(ell).rotate_by(pol_angle);
+    int n;
+    double s, cphi;
+    if (pol != PTG_POL_CIRCULAR) return PTG_ERR_UNSUPPORTED;
+    int st = cpp_sample(a, eta, sv.q, sv.u, sv.v, rng, &n, &s, &cphi, rej);
+    if (st != PTG_OK) return st;
+    double j = n;
+    double e_zmf = std::sqrt(0.5 * j * eta);
+    double p_zmf = std::sqrt(0.5 * j * eta - 1.0 - a * a);
+    double ct = (1.0 - 2.0 * s) * e_zmf / p_zmf;
+    if (!(ct <= 1.0 && ct >= -1.0)) return PTG_ERR_SANITY;
+    V4 t = ell + j * k;
+    V4 u_zmf = t / std::sqrt(t * t);
+    V3 along = -((j * k).boost_by(u_zmf).spatial().normalize());
+    V4 e4(0.0, std::cos(pol_angle), std::sin(pol_angle), 0.0);
+    V3 eps = e4.boost_by(u_zmf).spatial().normalize();
+    eps = along.cross(eps.cross(along)).normalize();
+    V3 perp = eps.rotate_around(along, cphi);
+    V3 q3 = p_zmf * (ct * along + std::sqrt(1.0 - ct * ct) * perp);
+    V4 q(std::sqrt(1.0 + a * a + q3.x * q3.x + q3.y * q3.y + q3.z * q3.z), q3.x, q3.y, q3.z);
+    q = q.boost_by(V4(u_zmf.t, -u_zmf.x, -u_zmf.y, -u_zmf.z));
+    double s_new = 1.0 - (k * q) / (k * ell);
+    if (!(std::fabs(s - s_new) / s < 1.0e-3)) return PTG_ERR_SANITY;
+    *n_out = n;
+    *q_out = q;
+    return PTG_OK;
+}
+
+// plane_wave.rs:284-316 / focused_laser.rs:283-306
+int lma_pair_create(const Laser& L, const V4& r, const V4& ell, const Stokes& pol, double dt, DrawStream& rng,
+                    double rate_increase, double* prob, Stokes* pol_new, bool* created, PairEvent* ev, uint64_t* rej) {
+    *created = false;
     *prob = 0.0;
     *pol_new = pol;
-    *created = false;
-    return PTG_ERR_UNSUPPORTED;
+    double a = std::sqrt(L.a_sqd(r));
+    double chirp = 1.0;
+    if (L.d.model == PTG_PLANE_WAVE) {
+        chirp = 1.0 + 2.0 * L.d.chirp_b * (L.wavevector * r);
+        if (chirp < 0.0 && a > 0.0) return PTG_ERR_SANITY;
+    }
+    V4 kappa = (SPEED_OF_LIGHT * COMPTON_TIME * chirp) * L.wavevector;
+    if (!bw_probability(ell, pol, kappa, a, dt, L.d.polarization, L.d.pol_angle, prob, pol_new))
+        return L.d.polarization == PTG_POL_CIRCULAR ? PTG_ERR_OUT_OF_TABLE : PTG_ERR_UNSUPPORTED;
+    double ri = (*prob * rate_increase > 0.1) ? 0.1 / *prob : rate_increase;
+    if (rng.next() < *prob * ri) {
+        int n;
+        V4 q;
+        int st = bw_generate(ell, pol, kappa, a, L.d.polarization, L.d.pol_angle, rng, &n, &q, rej);
+        if (st != PTG_OK) return st;
+        ev->u_e = ell + (double)n * kappa - q;
+        ev->u_p = q;
+        ev->frac = 1.0 / ri;
+        ev->a_eff = a;
+        ev->chi = a * (ell * kappa);
+        ev->absorption = (double)n * kappa.t;
+        *created = true;
+    }
+    return PTG_OK;
 }
 
 }  // namespace orc

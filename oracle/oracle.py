@@ -78,11 +78,28 @@ def lib():
         "orc_result_stats": (None, [vp, C.POINTER(abi.RunStats)]),
         "orc_result_copy": (None, [vp, C.POINTER(abi.Particles)]),
         "orc_result_free": (None, [vp]),
+        "orc_load_tables": (i, [C.c_char_p]),
+        "orc_has_cp_cdf": (i, []),
+        "orc_bessel_j": (d, [d, i]),
+        "orc_bessel_triple_j": (d, [i, d]),
+        "orc_bessel_j_asymptotic": (d, [i, d]),
+        "orc_bessel_j_pm": (None, [d, i, DP]),
+        "orc_cp_diff_partial_rate": (d, [i, d, d, d]),
+        "orc_cp_ceiling": (d, [i, d, d]),
+        "orc_cp_partial_rate": (d, [i, d, d]),
+        "orc_cp_rate": (d, [d, d]),
+        "orc_cp_invert": (i, [d, d, d]),
+        "orc_cp_sample": (i, [d, d, u64, u64, u32, DP]),
+        "orc_nlc_generate": (i, [DP, DP, i, d, u64, u64, u32, DP]),
+        "orc_nlc_probability": (d, [DP, DP, d, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
+    tables = os.path.join(ROOT, "ptarmigan_gb300", "tables", "data")
+    if L.orc_load_tables(tables.encode()) != 0:
+        raise RuntimeError("oracle could not load the LMA tables from " + tables)
     _lib = L
     return L
 
@@ -204,6 +221,67 @@ def primary_stream(i):
 
 def child_stream(parent, step, slot):
     return lib().orc_child_stream(parent, step, slot)
+
+
+# -- LMA ------------------------------------------------------------------
+def bessel_j(x, n):
+    return lib().orc_bessel_j(x, n)
+
+
+def bessel_triple_j(n, x):
+    return lib().orc_bessel_triple_j(n, x)
+
+
+def bessel_j_asymptotic(n, x):
+    return lib().orc_bessel_j_asymptotic(n, x)
+
+
+def bessel_j_pm(x, n):
+    out = np.zeros(3)
+    lib().orc_bessel_j_pm(x, n, _dp(out))
+    return out
+
+
+def cp_diff_partial_rate(n, a, eta, v):
+    return lib().orc_cp_diff_partial_rate(n, a, eta, v)
+
+
+def cp_ceiling(n, a, eta):
+    return lib().orc_cp_ceiling(n, a, eta)
+
+
+def cp_partial_rate(n, a, eta):
+    return lib().orc_cp_partial_rate(n, a, eta)
+
+
+def cp_rate(a, eta):
+    return lib().orc_cp_rate(a, eta)
+
+
+def has_cp_cdf():
+    return bool(lib().orc_has_cp_cdf())
+
+
+def cp_invert(a, eta, frac):
+    return lib().orc_cp_invert(a, eta, frac)
+
+
+def cp_sample(a, eta, seed, stream, step):
+    out = np.zeros(7)
+    rc = lib().orc_cp_sample(a, eta, seed, stream, step, _dp(out))
+    return rc, out
+
+
+def nlc_generate(k, q, pol, pol_angle, seed, stream, step):
+    k, q = _vec(k, 4), _vec(q, 4)
+    out = np.zeros(9)
+    rc = lib().orc_nlc_generate(_dp(k), _dp(q), pol, pol_angle, seed, stream, step, _dp(out))
+    return rc, out
+
+
+def nlc_probability(k, q, dt, pol):
+    k, q = _vec(k, 4), _vec(q, 4)
+    return lib().orc_nlc_probability(_dp(k), _dp(q), dt, pol)
 
 
 # -- fields ---------------------------------------------------------------

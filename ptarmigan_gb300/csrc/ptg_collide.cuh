@@ -92,6 +92,7 @@ struct Lane {
     d4 r, u, pol;
     double weight, icount, work;
     double hph;  // photons: c dt / ell^0
+    double hh;   // leptons: c dt / (2 u^0), the half-drift factor
     unsigned long long slot, stream, id;
     uint32_t step;
     int species, gen, status, flags;
@@ -144,8 +145,9 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
     d3 kpol = mk3(0, 0, 0);
     double a_eff = 0.0, chi = 0.0, absorption = 0.0;
     if (MODEL == M_FAST_PLANE_WAVE || MODEL == M_FAST_FOCUSED_LASER) {
-        // Field::push default (field/mod.rs:147-152)
-        double h = 0.5 * SPEED_OF_LIGHT * dt / L.u.t;
+        // Field::push default (field/mod.rs:147-152); h = c dt / (2 u^0) was
+        // computed by the previous step (or at load)
+        double h = L.hh;
         d4 rh = d4{L.r.t + h * L.u.t, L.r.x + h * L.u.x, L.r.y + h * L.u.y, L.r.z + h * L.u.z};
         if (f.env_cut > 0.0 && fabs(phase_of(f, rh)) > f.env_cut) {
             // E = B = 0 at rh: lcf.rs:18-78 then leaves u unchanged bit for
@@ -157,11 +159,12 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             double h2 = 0.5 * SPEED_OF_LIGHT * dt / g;
             r = d4{rh.t + h2 * u.t, rh.x + h2 * u.x, rh.y + h2 * u.y, rh.z + h2 * u.z};
             dwork = 0.0;
+            L.hh = h2;
         } else {
             d3 E, B;
             double aa;
             lcfa_fields(f, rh, &E, &B, &aa);
-            vay_push(rh, L.u, E, B, rqm, dt, a.o.eqn, [](double c) { return gaunt_factor(c); }, &r, &u, &dwork);
+            vay_push(rh, L.u, E, B, rqm, dt, a.o.eqn, [](double c) { return gaunt_factor(c); }, &r, &u, &dwork, &L.hh);
         }
         dt_actual = dt;
         // lcf.rs:85-134 at the new position.  The per-step probability
@@ -170,12 +173,12 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         {
             f3 e, b;
             if (lcfa_fields32(f, r, &e, &b)) {
-                float ig = (float)(1.0 / u.t);
+                float ig = 1.0f / (float)u.t;
                 f3 bt = f3{(float)u.x * ig, (float)u.y * ig, (float)u.z * ig};
                 f3 t = f3add(e, f3cross(bt, b));
                 float eb = f3dot(e, bt);
                 float q = f3dot(t, t) - eb * eb;
-                float chi32 = q > 0.0f ? (float)(u.t * field_scale(f) / CRITICAL_FIELD) * sqrtf(q) : 0.0f;
+                float chi32 = q > 0.0f ? ((float)u.t * (float)f.chi_scale) * sqrtf(q) : 0.0f;
                 float gam = (float)u.t;
                 prob = (float)dt_actual * (a.o.classical_mode ? (float)(SQRT_3 * ALPHA_FINE * 5.0 * FRAC_PI_3 / (2.0 * PI * COMPTON_TIME)) * chi32 / gam
                                                              : lcfa_photon_rate32(chi32, gam));
@@ -231,7 +234,10 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             atomicAdd(&a.c->overflow, 1ull);
         }
         ++*nemit;
-        if (a.o.electron_recoils) u = upr;
+        if (a.o.electron_recoils) {
+            u = upr;
+            L.hh = 0.5 * SPEED_OF_LIGHT * dt / u.t;
+        }
         L.icount += 1.0;
         if (!a.o.classical) L.work += absorption;
     }
@@ -264,13 +270,13 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
         if (!a.o.pol_resolved) {
             f3 e, b;
             if (lcfa_fields32(f, r, &e, &b)) {
-                float inv = (float)(1.0 / sqrt(ell.x * ell.x + ell.y * ell.y + ell.z * ell.z));
+                float inv = rsqrtf((float)(ell.x * ell.x + ell.y * ell.y + ell.z * ell.z));
                 f3 n = f3{(float)ell.x * inv, (float)ell.y * inv, (float)ell.z * inv};
                 f3 ap = f3add(f3add(e, f3scale(-f3dot(e, n), n)), f3cross(n, b));
                 float q = f3dot(ap, ap);
                 if (q > 0.0f) {
-                    float chi32 = (float)(ell.t * field_scale(f) / CRITICAL_FIELD) * sqrtf(q);
-                    prob_step = (double)((float)(ALPHA_FINE * dt / (COMPTON_TIME * ell.t)) * chi32 * lcfa_t_mean32(chi32));
+                    float chi32 = ((float)ell.t * (float)f.chi_scale) * sqrtf(q);
+                    prob_step = (double)((float)(ALPHA_FINE / COMPTON_TIME) * ((float)dt / (float)ell.t) * chi32 * lcfa_t_mean32(chi32));
                 }
             }
         }
@@ -369,6 +375,7 @@ __device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
     L.step = 0;
     L.decayed = false;
     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
+    L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
     return true;
 }
 

@@ -18,6 +18,7 @@
 
 #include "../../include/ptarmigan_gb300.h"
 #include "ptg_collide.cuh"
+#include "ptg_nlc.cuh"
 
 using namespace ptg;
 
@@ -84,6 +85,9 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     f.waist = d.waist;
     f.zr = 0.5 * f.k * d.waist * d.waist;
     f.eps = d.waist / f.zr;
+    f.inv_waist = 1.0 / d.waist;
+    f.inv_zr = 1.0 / f.zr;
+    f.inv_tau = 1.0 / (f.omega * f.duration);
     f.pol_angle = (lcfa && f.circular) ? 0.0 : d.pol_angle;
     f.cos_pa = std::cos(f.pol_angle);
     f.sin_pa = std::sin(f.pol_angle);
@@ -91,6 +95,7 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     f.E0 = ELECTRON_MASS * SPEED_OF_LIGHT * f.omega * d.a0 / ELEMENTARY_CHARGE;
     f.B0 = f.E0 / SPEED_OF_LIGHT;
     f.amp = (ELECTRON_MASS * SPEED_OF_LIGHT_SQD * f.k * d.a0) / ELEMENTARY_CHARGE;
+    f.chi_scale = (d.model == PTG_FAST_PLANE_WAVE ? f.amp : f.E0) / CRITICAL_FIELD;
     double nc = f.n_cycles;
     f.max_phase = d.envelope == PTG_ENV_COS2 ? PI * nc : (d.envelope == PTG_ENV_FLATTOP ? PI * (nc + 1.0) : 6.0 * PI * nc);
     f.bandwidth = 0.0;
@@ -582,6 +587,8 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
         {"nlc_lp_cdf", &c->lma_host.nlc_lp_cdf, 4148 * 16 * 2, true},
         {"nlc_cp_rate", &c->lma_host.nlc_cp_rate, 70 * 61, true},
         {"nlc_cp_cdf", &c->lma_host.nlc_cp_cdf, 4270 * 32 * 2, false},
+        {"nlc_lp_classical_rate", &c->lma_host.nlc_lp_cl_rate, 61, true},
+        {"nlc_cp_classical_rate", &c->lma_host.nlc_cp_cl_rate, 61, true},
         {"bw_cp_total", &c->lma_host.bw_cp_total, 121 * 74 * 2, true},
         {"bw_lp_total", &c->lma_host.bw_lp_total, 61 * 25 * 2, true},
         {"bw_lp_cdf", &c->lma_host.bw_lp_cdf, 1525 * 16 * 3, true},
@@ -1009,6 +1016,69 @@ ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_pa
     });
 }
 
+
+// ------------------------------------------------- table maintenance ---
+// Regenerates the CP harmonic CDF table on the device (the reference tree
+// lacks nonlinear_compton/cp/tables/cdf.rs; its generator is
+// nonlinear_compton/cp/mod.rs:472-612).  Grid: a = 0.02 * 10^(j/20),
+// j < 61; eta = 1e-3 * 10^(i/20), i < 70; n_max = 10 (1 + a^3).
+ptg_status ptg_regen_nlc_cp_cdf(ptg_ctx* c, double* cdf_out, double* total_out) {
+    if (!c || !cdf_out || !total_out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    const int NC = 61, NR = 70, NP = NC * NR;
+    std::vector<double> a_of(NP), eta_of(NP);
+    std::vector<int> nmax_of(NP);
+    std::vector<unsigned long long> off(NP);
+    std::vector<RegenChunk> chunks;
+    unsigned long long total_rows = 0;
+    for (int i = 0; i < NR; ++i) {
+        double eta = 1.0e-3 * std::pow(10.0, (double)i / 20.0);
+        for (int j = 0; j < NC; ++j) {
+            double a = 0.02 * std::pow(10.0, (double)j / 20.0);
+            int p = i * NC + j;
+            a_of[p] = a;
+            eta_of[p] = eta;
+            nmax_of[p] = (int)(10.0 * (1.0 + a * (a * a)));
+            off[p] = total_rows;
+            total_rows += nmax_of[p];
+            for (int n0 = 1; n0 <= nmax_of[p]; n0 += 256) chunks.push_back(RegenChunk{p, n0});
+        }
+    }
+    double *d_a = nullptr, *d_eta = nullptr, *d_rates = nullptr, *d_cum = nullptr, *d_cdf = nullptr, *d_tot = nullptr;
+    int* d_nmax = nullptr;
+    unsigned long long* d_off = nullptr;
+    RegenChunk* d_chunks = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_a), cudaFree(d_eta), cudaFree(d_rates), cudaFree(d_cum), cudaFree(d_cdf), cudaFree(d_tot);
+        cudaFree(d_nmax), cudaFree(d_off), cudaFree(d_chunks);
+    };
+    bool ok = cudaMalloc(&d_a, 8 * NP) == cudaSuccess && cudaMalloc(&d_eta, 8 * NP) == cudaSuccess &&
+              cudaMalloc(&d_nmax, 4 * NP) == cudaSuccess && cudaMalloc(&d_off, 8 * NP) == cudaSuccess &&
+              cudaMalloc(&d_rates, 8 * total_rows) == cudaSuccess && cudaMalloc(&d_cum, 16 * total_rows) == cudaSuccess &&
+              cudaMalloc(&d_cdf, 8 * 64 * NP) == cudaSuccess && cudaMalloc(&d_tot, 8 * NP) == cudaSuccess &&
+              cudaMalloc(&d_chunks, sizeof(RegenChunk) * chunks.size()) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cleanup();
+        return set_err(PTG_ERR_ALLOC, "table regeneration buffers");
+    }
+    cudaMemcpy(d_a, a_of.data(), 8 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_eta, eta_of.data(), 8 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_nmax, nmax_of.data(), 4 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_off, off.data(), 8 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_chunks, chunks.data(), sizeof(RegenChunk) * chunks.size(), cudaMemcpyHostToDevice);
+    k_regen_cp_partial<<<(unsigned)chunks.size(), 256, 0, c->stream>>>(d_chunks, d_a, d_eta, d_nmax, d_off, d_rates);
+    k_regen_cp_cdf<<<(NP + 63) / 64, 64, 0, c->stream>>>(NP, d_nmax, d_off, d_rates, d_cum, d_cdf, d_tot);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        cudaMemcpy(cdf_out, d_cdf, 8 * 64 * NP, cudaMemcpyDeviceToHost);
+        cudaMemcpy(total_out, d_tot, 8 * NP, cudaMemcpyDeviceToHost);
+    }
+    cleanup();
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    return PTG_OK;
+}
 
 // ------------------------------------------------ allocation-free batch ---
 // ptg_collide_batch_noalloc(): the LCFA collision loop for callers that

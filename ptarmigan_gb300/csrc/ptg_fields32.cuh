@@ -42,7 +42,7 @@ __device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr
                                            f3* imB) {
     double rx = cr * r.x + sr * r.y;
     double ry = cr * r.y - sr * r.x;
-    float x = (float)(rx / f.waist), y = (float)(ry / f.waist), z = (float)(r.z / f.zr);
+    float x = (float)(rx * f.inv_waist), y = (float)(ry * f.inv_waist), z = (float)(r.z * f.inv_zr);
     float rho2 = x * x + y * y;
     float e = (float)f.eps, e2 = e * e, e3 = e2 * e, e4 = e2 * e2;
     float den = 1.0f / (1.0f + z * z);
@@ -139,10 +139,9 @@ __device__ __forceinline__ bool lcfa_fields32(const FieldParams& f, d4 r, f3* e,
     // fast_focused_laser.rs:123-151 envelope, in FP32 after an FP64 argument
     float env, denv;
     if (f.envelope == ENV_GAUSSIAN) {
-        double tau = f.omega * f.duration;
-        double q = phase / tau;
-        env = expf((float)(-2.0 * LN_2 * q * q));
-        denv = (float)(-4.0 * LN_2 * q / tau) * env;
+        float q = (float)(phase * f.inv_tau);
+        env = expf(-2.0f * (float)LN_2 * q * q);
+        denv = (-4.0f * (float)LN_2 * (float)f.inv_tau) * q * env;
     } else {
         double de, dd;
         ffl_envelope(f, phase, &de, &dd);

@@ -1,30 +1,86 @@
-// LMA nonlinear Compton emission and Breit-Wheeler pair creation
-// (nonlinear_compton/*, pair_creation/*) on the device.
+// LMA emission and pair creation for the PlaneWave and FocusedLaser models:
+// the per-step probability at the local (a, eta) and, on an event, the
+// sample and its kinematics.
 #pragma once
 #include "ptg_fields.cuh"
 #include "ptg_math.cuh"
+#include "ptg_nlc.cuh"
 
 namespace ptg {
 
 // Device pointers to the LMA rate and CDF tables (loaded from data files).
 struct LmaTables {
-    const double* nlc_lp_rate;   // [68][61]
-    const double* nlc_lp_cdf;    // [4148][16][2]
-    const double* nlc_cp_rate;   // [70][61]
-    const double* nlc_cp_cdf;    // [4270][32][2] or null
-    const double* bw_cp_total;   // [121][74][2]
-    const double* bw_lp_total;   // [61][25][2]
-    const double* bw_lp_cdf;     // [1525][16][3]
+    const double* nlc_lp_rate;      // [68][61] ln rate
+    const double* nlc_lp_cdf;       // [4148][16][2]
+    const double* nlc_cp_rate;      // [70][61] ln rate
+    const double* nlc_cp_cdf;       // [4270][32][2] (regenerated)
+    const double* nlc_lp_cl_rate;   // [61]
+    const double* nlc_cp_cl_rate;   // [61]
+    const double* bw_cp_total;      // [121][74][2]
+    const double* bw_lp_total;      // [61][25][2]
+    const double* bw_lp_cdf;        // [1525][16][3]
     const double* bw_lp_mid_total;  // [157][36][2]
-    const double* bw_lp_mid_cdf;    // [5652][16][3] or null
+    const double* bw_lp_mid_cdf;    // [5652][16][3] (regenerated)
 };
 
-// plane_wave.rs:251-282 / focused_laser.rs:260-281
+__device__ __forceinline__ NlcTables nlc_view(const LmaTables& t) {
+    return NlcTables{t.nlc_lp_rate, t.nlc_lp_cdf, t.nlc_cp_rate, t.nlc_cp_cdf, t.nlc_cp_cl_rate, t.nlc_lp_cl_rate};
+}
+
+// Standard normal from two uniforms (Box-Muller), for the finite bandwidth.
+__device__ __forceinline__ double std_normal(Draws& rng) {
+    double u1 = rng.next(), u2 = rng.next();
+    return sqrt(-2.0 * log(1.0 - u1)) * cos(2.0 * PI * u2);
+}
+
+// plane_wave.rs:251-282 / focused_laser.rs:260-281 with
+// nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
+// Returns a ptg status (0 = ok).
 __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, d4 r, d4 u, double dt, Draws& rng,
-                                        bool classical, bool* emitted, d4* k, d4* u_prime, d3* pol, double* a_eff,
+                                        bool classical, bool* emitted, d4* k_out, d4* u_prime, d3* pol, double* a_eff,
                                         double* chi, double* absorption, uint32_t* rej) {
     *emitted = false;
-    return 9;  // PTG_ERR_UNSUPPORTED until the LMA samplers land
+    double a = sqrt(lma_a_sqd(f, r));
+    double chirp = 1.0;
+    if (f.model == M_PLANE_WAVE) {
+        chirp = 1.0 + 2.0 * f.chirp_b * phase_of(f, r);
+        if (chirp < 0.0 && a > 0.0) return 3;  // PTG_ERR_SANITY
+    }
+    double width = 1.0;
+    if (f.bandwidth != 0.0) {
+        width = 1.0 + f.bandwidth * std_normal(rng);
+        if (!(width > 0.0)) return 3;
+    }
+    double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp * width;
+    d4 kappa = d4{kk, 0.0, 0.0, kk};
+    double a2 = dot4(u, u) - 1.0;
+    double aq = a2 >= 0.0 ? sqrt(a2) : 0.0;
+    double eta = dot4(kappa, u);
+    double dphi = dt * eta / (COMPTON_TIME * u.t);
+    NlcTables nt = nlc_view(t);
+    double rate;
+    if (!f.circular) return 9;  // PTG_ERR_UNSUPPORTED: LP sampler not built
+    bool ok = classical ? cp_classical_rate(nt, aq, eta, &rate) : cp_rate(nt, aq, eta, &rate);
+    if (!ok) return 2;  // PTG_ERR_OUT_OF_TABLE
+    double prob = ALPHA_FINE * rate * dphi / eta;
+    if (rng.next() < prob) {
+        if (classical) return 9;
+        int n;
+        double s, cphi;
+        d3 sv;
+        int st = cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
+        if (st != 0) return st;
+        d4 k;
+        st = nlc_kinematics(kappa, u, aq, eta, n, s, cphi, sv, f.pol_angle, classical, &k, pol);
+        if (st != 0) return st;
+        *k_out = k;
+        *u_prime = d4{u.t + n * kappa.t - k.t, u.x + n * kappa.x - k.x, u.y + n * kappa.y - k.y, u.z + n * kappa.z - k.z};
+        *a_eff = a;
+        *chi = a * dot4(u, kappa);
+        *absorption = n * kappa.t;
+        *emitted = true;
+    }
+    return 0;
 }
 
 // plane_wave.rs:284-316 / focused_laser.rs:283-306
@@ -35,7 +91,7 @@ __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTable
     *prob = 0.0;
     *pol_new = pol;
     *created = false;
-    return 9;
+    return 9;  // PTG_ERR_UNSUPPORTED until the LMA pair samplers land
 }
 
 }  // namespace ptg

@@ -1,0 +1,442 @@
+// LMA nonlinear Compton scattering on the device: Bessel functions J_n,
+// the circularly polarised (CP) partial rates, total rate and sampler, and
+// the zero-momentum-frame kinematics that turn a sample into a photon.
+//
+// Follows special_functions/bessel.rs, nonlinear_compton/cp/mod.rs,
+// nonlinear_compton/cp/tables/mod.rs and nonlinear_compton/mod.rs (cited per
+// function).  All FP64: these run once per emission, not per step.
+#pragma once
+#include "ptg_lcfa.cuh"
+#include "ptg_math.cuh"
+
+namespace ptg {
+
+constexpr double FRAC_PI_2 = 1.57079632679489661923;
+constexpr double FRAC_PI_4 = 0.78539816339744830962;
+
+// ------------------------------------------------------------ Bessel ---
+// special_functions/bessel.rs:117-176: (J_{n-1}, J_n, J_{n+1})(x) by Miller's
+// backward recurrence normalised with J_0 + 2 sum J_2k = 1; O(n) work.
+__device__ __noinline__ void triple_j(int n, double x, double* a, double* b, double* c) {
+    if (x == 0.0) {
+        *a = (n == 1) ? 1.0 : 0.0;
+        *b = (n == 0) ? 1.0 : 0.0;
+        *c = (n == -1) ? 1.0 : 0.0;
+        return;
+    }
+    double v = x / (double)n;
+    int nmax = 1 + n + (int)(5.0 / (1.0 - 0.9 * v));
+    if ((nmax & 1) != 0) nmax += 1;
+    int n_even = (n & 1) == 0 ? 1 : 0;
+    int k_stop = n - 1 - n_even;
+    double q0 = 1.0, q1 = 0.0, q2 = 0.0, q3 = 0.0;
+    double total = 0.0;
+    double inv_x = 1.0 / x;
+    for (int k = nmax; k >= k_stop; k -= 2) {
+        q3 = q1;
+        q2 = q0;
+        q1 = (double)(2 * (k + 2)) * q2 * inv_x - q3;
+        q0 = (double)(2 * (k + 1)) * q1 * inv_x - q2;
+        total += q0;
+    }
+    double t0, t1, t2;
+    if (n_even) {
+        t0 = q1, t1 = q2, t2 = q3;
+    } else {
+        t0 = q0, t1 = q1, t2 = q2;
+    }
+    for (int k = k_stop - 2; k >= 0; k -= 2) {
+        q3 = q1;
+        q2 = q0;
+        q1 = (double)(2 * (k + 2)) * q2 * inv_x - q3;
+        q0 = (double)(2 * (k + 1)) * q1 * inv_x - q2;
+        total += q0;
+    }
+    double norm = 2.0 * total - q0;
+    if (isnan(norm)) {
+        *a = *b = *c = 0.0;
+    } else {
+        double in = 1.0 / norm;
+        *a = t0 * in;
+        *b = t1 * in;
+        *c = t2 * in;
+    }
+}
+
+// special_functions/bessel.rs:178-199: uniform asymptotic expansion (n >= 1000)
+__device__ __noinline__ double j_asymptotic(int n, double x) {
+    double m = (double)n;
+    double z = x / m;
+    double zeta;
+    if (z < 1.0) {
+        double r = sqrt(1.0 - z * z);
+        double tmp = log((1.0 + r) / z) - r;
+        zeta = pow(1.5 * tmp, 2.0 / 3.0);
+    } else {
+        double tmp = sqrt(z * z - 1.0) - acos(1.0 / z);
+        zeta = -pow(1.5 * tmp, 2.0 / 3.0);
+    }
+    double arg = pow(m, 2.0 / 3.0) * zeta;
+    double ai = arg >= 0.0 ? airy_ai(arg) : 0.0;
+    double aip = arg >= 0.0 ? airy_ai_prime(arg) : 0.0;
+    double pre = 4.0 * zeta / (1.0 - z * z);
+    double bk = 5.0 / (48.0 * zeta * zeta) - (2.0 + 3.0 * z * z) / (24.0 * sqrt(zeta) * pow(1.0 - z * z, 1.5));
+    return pow(pre, 0.25) * (ai / cbrt(m) - aip * bk / pow(m, 5.0 / 3.0));
+}
+
+// bessel.rs:26-34
+__device__ __forceinline__ void j_pm(double x, int n, double* jm1, double* j, double* jp1) {
+    if (n < 1000) {
+        triple_j(n, x, jm1, j, jp1);
+    } else {
+        double jn = j_asymptotic(n, x);
+        double jp = j_asymptotic(n + 1, x);
+        *jm1 = (double)(2 * n) * jn / x - jp;
+        *j = jn;
+        *jp1 = jp;
+    }
+}
+
+// ------------------------------------------------- CP partial rates ----
+// nonlinear_compton/cp/mod.rs:17-38: dW_n/dv, v = s / s_max
+__device__ __forceinline__ double cp_diff_partial_rate(int n, double a, double eta, double v) {
+    if (v < 0.0 || v >= 1.0) return 0.0;
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double smax = sn / (1.0 + sn);
+    double vs = v * smax;
+    double w = vs / (sn * (1.0 - vs));
+    double z = sqrt(4.0 * ((double)n * (double)n) * (a * a / (1.0 + a * a)) * w * (1.0 - w));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    return -smax * (j * j + 0.5 * a * a * (1.0 + 0.5 * vs * vs / (1.0 - vs)) * (2.0 * j * j - jp * jp - jm * jm));
+}
+
+// nonlinear_compton/cp/mod.rs:42-75
+__device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    int n_switch = (int)(32.3 * (1.0 + 0.476 * pow(a, 1.56)));
+    double mx = -HUGE_VAL;
+    if (sn < 2.0 || n < n_switch) {
+        double v_opt = (1.0 + sn) / (2.0 + sn);
+        for (int i = 0; i < 16; ++i) mx = fmax(mx, cp_diff_partial_rate(n, a, eta, i * v_opt / 16.0));
+        for (int i = 0; i < 16; ++i) mx = fmax(mx, cp_diff_partial_rate(n, a, eta, v_opt + i * (1.0 - v_opt) / 16.0));
+    } else {
+        for (int k = 0; k < 16; ++k) {
+            double u = 0.5 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
+            mx = fmax(mx, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
+        }
+        for (int k = 0; k < 16; ++k) {
+            double u = (1.0 + sn) + 0.5 * 2.0 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
+            mx = fmax(mx, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
+        }
+    }
+    return 1.2 * mx;
+}
+
+// nonlinear_compton/cp/mod.rs:92-136: integral of dW_n/dv over v (GL-32 x 2)
+__device__ __noinline__ double cp_partial_rate(int n, double a, double eta) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    int n_switch = (int)(32.3 * (1.0 + 0.476 * pow(a, 1.56)));
+    double lower = 0.0, upper = 0.0;
+    if (sn < 2.0 || n < n_switch) {
+        double vmid = (1.0 + sn) / (2.0 + sn);
+        for (int k = 0; k < 32; ++k) {
+            double v = 0.5 * vmid * (PTG_GAUSS_32_NODES[k] + 1.0);
+            lower += 0.5 * vmid * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, v);
+        }
+        for (int k = 0; k < 32; ++k) {
+            double v = vmid + 0.5 * (1.0 - vmid) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            upper += 0.5 * (1.0 - vmid) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, v);
+        }
+    } else {
+        for (int k = 0; k < 32; ++k) {
+            double u = 0.5 * (1.0 + sn) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            lower += 0.5 * (1.0 + sn) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, u / (1.0 + u)) /
+                     ((1.0 + u) * (1.0 + u));
+        }
+        for (int k = 0; k < 32; ++k) {
+            double u = (1.0 + sn) + (1.0 + sn) * (PTG_GAUSS_32_NODES[k] + 1.0);
+            upper += (1.0 + sn) * PTG_GAUSS_32_WEIGHTS[k] * cp_diff_partial_rate(n, a, eta, u / (1.0 + u)) /
+                     ((1.0 + u) * (1.0 + u));
+        }
+    }
+    return lower + upper;
+}
+
+// ------------------------------------------------------- CP rates ------
+struct NlcTables {
+    const double* lp_rate;   // [68][61] ln rate
+    const double* lp_cdf;    // [4148][16][2]
+    const double* cp_rate;   // [70][61] ln rate
+    const double* cp_cdf;    // [4270][32][2]
+    const double* cp_cl_rate;  // [61]
+    const double* lp_cl_rate;  // [61]
+};
+
+// nonlinear_compton/cp/classical.rs:22-43
+__device__ __forceinline__ bool cp_classical_rate(const NlcTables& t, double a, double eta, double* out) {
+    double x = log(a);
+    if (x < PTG_NLC_CL_MIN) {
+        *out = 2.0 * a * a * eta / 3.0;
+        return true;
+    }
+    int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    if (ix >= 60) return false;
+    double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    *out = eta * exp((1.0 - dx) * t.cp_cl_rate[ix] + dx * t.cp_cl_rate[ix + 1]);
+    return true;
+}
+
+// nonlinear_compton/cp/mod.rs:160-176 and tables/mod.rs:11-35
+__device__ __forceinline__ bool cp_rate(const NlcTables& t, double a, double eta, double* out) {
+    const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
+    double la = log(a), le = log(eta);
+    if (le < MIN1) return cp_classical_rate(t, a, eta, out);
+    if (la < MIN0) {
+        double q = 1.0 + 2.0 * eta;
+        *out = a * a * (2.0 + 8.0 * eta + 9.0 * eta * eta + eta * eta * eta) / (2.0 * eta * q * q) -
+               a * a * (2.0 + 2.0 * eta - eta * eta) * log(q) / (4.0 * eta * eta);
+        return true;
+    }
+    if (!(a < 20.0 && eta < 2.0)) return false;
+    int ia = (int)((la - MIN0) / S0);
+    int ie = (int)((le - MIN1) / S1);
+    if (ia >= 60 || ie >= 69) return false;
+    double da = (la - MIN0) / S0 - ia;
+    double de = (le - MIN1) / S1 - ie;
+    const double* T = t.cp_rate;
+    double f = (1.0 - da) * (1.0 - de) * T[ie * 61 + ia] + da * (1.0 - de) * T[ie * 61 + ia + 1] +
+               (1.0 - da) * de * T[(ie + 1) * 61 + ia] + da * de * T[(ie + 1) * 61 + ia + 1];
+    *out = exp(f);
+    return true;
+}
+
+// nonlinear_compton/cp/tables/mod.rs:37-121: harmonic index from the CDF
+// table (four grid corners, each inverted in [ln n, ln(-ln(1 - cdf))]).
+__device__ __noinline__ double cp_cdf_corner(const double* table, double frac) {
+    if (frac <= table[1]) return 0.9;
+    double rs[62];
+    for (int i = 0; i < 31; ++i) {
+        rs[2 * i] = log(table[2 * i]);
+        rs[2 * i + 1] = log(-1.0 * log(1.0 - table[2 * i + 1]));
+    }
+    double f2 = log(-1.0 * log(1.0 - frac));
+    double v = 0.0;
+    pw_invert(rs, 31, true, f2, &v);
+    return exp(v);
+}
+
+__device__ __noinline__ int cp_invert(const NlcTables& t, double a, double eta, double frac) {
+    const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
+    double la = log(a), le = log(eta);
+    if (la <= MIN0) return 1;
+    int ix = (int)((la - MIN0) / S0);
+    double dx = (la - MIN0) / S0 - ix;
+    if (le <= MIN1) {
+        double n = cp_cdf_corner(t.cp_cdf + (size_t)ix * 64, frac) * (1.0 - dx) +
+                   cp_cdf_corner(t.cp_cdf + (size_t)(ix + 1) * 64, frac) * dx;
+        return (int)ceil(n);
+    }
+    int iy = (int)((le - MIN1) / S1);
+    double dy = (le - MIN1) / S1 - iy;
+    double n = cp_cdf_corner(t.cp_cdf + (size_t)(61 * iy + ix) * 64, frac) * ((1.0 - dx) * (1.0 - dy)) +
+               cp_cdf_corner(t.cp_cdf + (size_t)(61 * iy + ix + 1) * 64, frac) * (dx * (1.0 - dy)) +
+               cp_cdf_corner(t.cp_cdf + (size_t)(61 * (iy + 1) + ix) * 64, frac) * ((1.0 - dx) * dy) +
+               cp_cdf_corner(t.cp_cdf + (size_t)(61 * (iy + 1) + ix + 1) * 64, frac) * (dx * dy);
+    return (int)ceil(n);
+}
+
+// nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
+__device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
+                                      double* theta_out, d3* sv_out, uint32_t* rej) {
+    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    double mx = cp_ceiling(n, a, eta);
+    double v = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next(), u = rng.next();
+        if (u <= cp_diff_partial_rate(n, a, eta, vv) / mx) {
+            v = vv;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;  // PTG_ERR_REJECTION_CAP
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double s = v * (sn / (1.0 + sn));
+    double theta = 2.0 * PI * rng.next();
+    double w = s / (sn * (1.0 - s));
+    double z = sqrt((double)(4 * n) * (double)n * (a * a / (1.0 + a * a)) * w * (1.0 - w));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    const double LASER_S3 = -1.0;
+    double nz = (double)n / z;
+    double xi0 = (1.0 - s + 1.0 / (1.0 - s)) * (jm * jm + jp * jp - 2.0 * j * j) - (2.0 * j / a) * (2.0 * j / a);
+    double xi1 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) + 8.0 * j * j * (1.0 - nz * nz - 0.5 / (a * a));
+    double xi3 = LASER_S3 * (1.0 - s + 1.0 / (1.0 - s)) * (1.0 - 2.0 * s / (sn * (1.0 - s))) * (jm * jm - jp * jp);
+    double q = xi1 / xi0, u = 0.0, vv = xi3 / xi0;
+    // rotate_by(pi/2 + theta): Stokes rotate by 2 angle
+    double s2, c2;
+    sincos(2.0 * (FRAC_PI_2 + theta), &s2, &c2);
+    *sv_out = mk3(c2 * q + s2 * u, -s2 * q + c2 * u, vv);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return 0;
+}
+
+// ------------------------------------------------------- ZMF kinematics -
+__device__ __forceinline__ double dot4(d4 a, d4 b) { return a.t * b.t - a.x * b.x - a.y * b.y - a.z * b.z; }
+
+// four_vector.rs:68-81
+__device__ __forceinline__ d4 boost_by(d4 v, d4 u) {
+    double gamma = u.t;
+    double beta = sqrt(1.0 - 1.0 / (gamma * gamma));
+    d3 n = normalize(mk3(u.x, u.y, u.z));
+    d3 z = mk3(v.x, v.y, v.z);
+    double nz = dot(n, z);
+    return d4{gamma * (v.t - beta * nz), z.x + (gamma - 1.0) * nz * n.x - gamma * beta * v.t * n.x,
+              z.y + (gamma - 1.0) * nz * n.y - gamma * beta * v.t * n.y,
+              z.z + (gamma - 1.0) * nz * n.z - gamma * beta * v.t * n.z};
+}
+
+// polarization.rs:101-155: Stokes parameters from the LMA basis
+__device__ __forceinline__ d3 stokes_from_lma_basis(d3 sv, d4 k) {
+    double k_minus = k.t - k.z;
+    double c = (k.z * k_minus - k.x * k.x) / (k_minus * hypot(k.x, k.z));
+    double sign = dsign(k.x * k.y);
+    c = fmin(fmax(c, -1.0), 1.0);
+    double s = -(sign * sqrt(1.0 - c * c));
+    double c2 = c * c - s * s, s2 = 2.0 * c * s;
+    return mk3(c2 * sv.x - s2 * sv.y, s2 * sv.x + c2 * sv.y, sv.z);
+}
+
+// nonlinear_compton/mod.rs:58-138 for a sampled (n, s, cphi, Stokes):
+// builds k' in the zero-momentum frame and boosts it to the lab.
+__device__ __noinline__ int nlc_kinematics(d4 k, d4 q, double a, double eta, int n, double s, double cphi, d3 sv,
+                                           double pol_angle, bool classical, d4* k_out, d3* sv_out) {
+    double ell = n;
+    double p_zmf = classical ? ell * eta / sqrt(1.0 + a * a) : ell * eta / sqrt(1.0 + a * a + 2.0 * ell * eta);
+    double ct = classical ? 1.0 - s * (1.0 + a * a) / (ell * eta) : 1.0 - s * (1.0 + a * a + 2.0 * ell * eta) / (ell * eta);
+    if (!(ct <= 1.0 && ct >= -1.0)) return 3;  // PTG_ERR_SANITY
+    d4 uz;
+    if (classical) {
+        double m = sqrt(dot4(q, q));
+        uz = d4{q.t / m, q.x / m, q.y / m, q.z / m};
+    } else {
+        d4 t = d4{q.t + ell * k.t, q.x + ell * k.x, q.y + ell * k.y, q.z + ell * k.z};
+        double m = sqrt(dot4(t, t));
+        uz = d4{t.t / m, t.x / m, t.y / m, t.z / m};
+    }
+    d3 along;
+    if (classical) {
+        d4 b = boost_by(d4{ell * k.t, ell * k.x, ell * k.y, ell * k.z}, uz);
+        along = normalize(mk3(b.x, b.y, b.z));
+    } else {
+        d4 b = boost_by(q, uz);
+        along = -normalize(mk3(b.x, b.y, b.z));
+    }
+    double sp, cp;
+    sincos(pol_angle, &sp, &cp);
+    d4 e4 = boost_by(d4{0.0, cp, sp, 0.0}, uz);
+    d3 eps = normalize(mk3(e4.x, e4.y, e4.z));
+    eps = normalize(cross(along, cross(eps, along)));
+    double sc, cc;
+    sincos(cphi, &sc, &cc);
+    d3 perp = rotate_around(eps, along, sc, cc);
+    d3 kp = p_zmf * (ct * along + sqrt(1.0 - ct * ct) * perp);
+    d4 kprime = d4{sqrt(dot(kp, kp)), kp.x, kp.y, kp.z};
+    kprime = boost_by(kprime, d4{uz.t, -uz.x, -uz.y, -uz.z});
+    // sv.rotate_by(-pol_angle), then into the global basis
+    double s2, c2;
+    sincos(-2.0 * pol_angle, &s2, &c2);
+    d3 r = mk3(c2 * sv.x + s2 * sv.y, -s2 * sv.x + c2 * sv.y, sv.z);
+    *sv_out = stokes_from_lma_basis(r, kprime);
+    double s_new = dot4(k, kprime) / dot4(k, q);
+    if (!(fabs(s - s_new) / s < 1.0e-2)) return 3;
+    *k_out = kprime;
+    return 0;
+}
+
+}  // namespace ptg
+
+namespace ptg {
+
+// -------------------------------------------------- table regeneration --
+// The CP harmonic CDF table (nonlinear_compton/cp/tables/cdf.rs) is not in
+// the reference tree; its generator is nonlinear_compton/cp/mod.rs:472-612.
+// Pass 1: one thread per (grid point, harmonic) computes the partial rate.
+struct RegenChunk {
+    int point;     // grid point index (eta row * 61 + a column)
+    int n0;        // first harmonic of this block
+};
+
+__global__ void k_regen_cp_partial(const RegenChunk* chunks, const double* a_of, const double* eta_of,
+                                   const int* nmax_of, const unsigned long long* offset_of, double* rates) {
+    RegenChunk ch = chunks[blockIdx.x];
+    int n = ch.n0 + (int)threadIdx.x;
+    if (n > nmax_of[ch.point]) return;
+    double a = a_of[ch.point], eta = eta_of[ch.point];
+    rates[offset_of[ch.point] + (n - 1)] = cp_partial_rate(n, a, eta);
+}
+
+// Pass 2: one thread per grid point: the cumulative sum in harmonic order
+// and the 32 CDF nodes of the reference's generator.
+__global__ void k_regen_cp_cdf(int npoints, const int* nmax_of, const unsigned long long* offset_of, const double* rates,
+                               double* cum /* [sum nmax][2] */, double* cdf_out /* [npoints][32][2] */,
+                               double* total_out /* [npoints] */) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoints) return;
+    int n_max = nmax_of[p];
+    const double* r = rates + offset_of[p];
+    double* c = cum + 2 * offset_of[p];
+    double cs = 0.0;
+    for (int n = 1; n <= n_max; ++n) {
+        cs = cs + r[n - 1];
+        c[2 * (n - 1)] = (double)n;
+        c[2 * (n - 1) + 1] = cs;
+    }
+    double rate = cs;
+    double* out = cdf_out + (size_t)p * 64;
+    out[0] = c[0];
+    out[1] = c[1] / rate;
+    double limit = c[2 * (n_max - 1)];
+    if (n_max <= 32) {
+        for (int i = 1; i <= 31; ++i) {
+            if (i < n_max) {
+                out[2 * i] = c[2 * i];
+                out[2 * i + 1] = c[2 * i + 1] / rate;
+            } else {
+                out[2 * i] = (double)(i + 1);
+                out[2 * i + 1] = 1.0;
+            }
+        }
+    } else if (n_max < 100) {
+        for (int i = 1; i <= 7; ++i) {
+            out[2 * i] = c[2 * i];
+            out[2 * i + 1] = c[2 * i + 1] / rate;
+        }
+        double delta = (log((double)n_max) - log(9.0)) / (31.0 - 8.0);
+        for (int i = 8; i <= 31; ++i) {
+            double n = fmin(exp(log(9.0) + (double)(i - 8) * delta), limit);
+            double v = 0.0;
+            pw_evaluate(c, n_max, false, n, &v);
+            out[2 * i] = n;
+            out[2 * i + 1] = v / rate;
+        }
+    } else {
+        double delta = log((double)n_max) / 31.0;
+        for (int i = 1; i <= 31; ++i) {
+            double n = fmin(exp((double)i * delta), limit);
+            double v = 0.0;
+            pw_evaluate(c, n_max, false, n, &v);
+            out[2 * i] = n;
+            out[2 * i + 1] = v / rate;
+        }
+    }
+    total_out[p] = rate;
+}
+
+}  // namespace ptg

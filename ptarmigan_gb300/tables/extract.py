@@ -171,6 +171,34 @@ SCALARS = [
     ("LCFA_PH_LN_DELTA_MIN", "src/lcfa/photon_emission/tables.rs", "LN_DELTA_MIN"),
     ("LCFA_PH_LN_DELTA_STEP", "src/lcfa/photon_emission/tables.rs", "LN_DELTA_STEP"),
     ("LCFA_PAIR_DELTA_LN_CHI", "src/lcfa/pair_creation/tables.rs", "DELTA_LN_CHI"),
+    # grids of the LMA tables (the data are in data/*.ptgt)
+    ("NLC_CL_MIN", "src/nonlinear_compton/cp/classical/rate_table.rs", "MIN"),
+    ("NLC_CL_STEP", "src/nonlinear_compton/cp/classical/rate_table.rs", "STEP"),
+    ("BW_CP_LN_MIN_A", "src/pair_creation/cp/total.rs", "LN_MIN_A"),
+    ("BW_CP_LN_MIN_ETA", "src/pair_creation/cp/total.rs", "LN_MIN_ETA"),
+    ("BW_CP_LN_A_STEP", "src/pair_creation/cp/total.rs", "LN_A_STEP"),
+    ("BW_CP_LN_ETA_STEP", "src/pair_creation/cp/total.rs", "LN_ETA_STEP"),
+    ("BW_LP_LN_MIN_A", "src/pair_creation/lp/tables/total.rs", "LN_MIN_A"),
+    ("BW_LP_LN_MIN_ETA", "src/pair_creation/lp/tables/total.rs", "LN_MIN_ETA"),
+    ("BW_LP_LN_A_STEP", "src/pair_creation/lp/tables/total.rs", "LN_A_STEP"),
+    ("BW_LP_LN_ETA_STEP", "src/pair_creation/lp/tables/total.rs", "LN_ETA_STEP"),
+    ("BW_LPM_LN_MIN_A", "src/pair_creation/lp/tables/mid_range/total.rs", "LN_MIN_A"),
+    ("BW_LPM_LN_MAX_ETA_PRIME", "src/pair_creation/lp/tables/mid_range/total.rs", "LN_MAX_ETA_PRIME"),
+    ("BW_LPM_LN_MIN_ETA_PRIME", "src/pair_creation/lp/tables/mid_range/total.rs", "LN_MIN_ETA_PRIME"),
+    ("BW_LPM_LN_A_STEP", "src/pair_creation/lp/tables/mid_range/total.rs", "LN_A_STEP"),
+    ("BW_LPM_ETA_PRIME_DENSITY", "src/pair_creation/lp/tables/mid_range/total.rs", "ETA_PRIME_DENSITY"),
+]
+
+# two-element grid constants [a, eta], written as NAME_0 and NAME_1
+PAIRS = [
+    ("NLC_LP_MIN", "src/nonlinear_compton/lp/rate_table.rs", "MIN"),
+    ("NLC_LP_STEP", "src/nonlinear_compton/lp/rate_table.rs", "STEP"),
+    ("NLC_LP_CDF_MIN", "src/nonlinear_compton/lp/cdf_table.rs", "MIN"),
+    ("NLC_LP_CDF_STEP", "src/nonlinear_compton/lp/cdf_table.rs", "STEP"),
+    ("NLC_CP_MIN", "src/nonlinear_compton/cp/tables/total.rs", "MIN"),
+    ("NLC_CP_STEP", "src/nonlinear_compton/cp/tables/total.rs", "STEP"),
+    ("BW_LP_CDF_MIN", "src/pair_creation/lp/tables/cdf.rs", "MIN"),
+    ("BW_LP_CDF_STEP", "src/pair_creation/lp/tables/cdf.rs", "STEP"),
 ]
 
 
@@ -199,12 +227,15 @@ def write_small_header(root, path):
         "#endif",
         "",
     ]
-    for cname, _rel, sym in [(c, r, s) for c, r, s in SCALARS]:
-        pass
     for cname, rel, sym in SCALARS:
         v = read_scalar(root, rel, sym)
         lines.append("/* %s :: %s */" % (rel, sym))
         lines.append("#define PTG_%s %s" % (cname, _c_double(v)))
+    for cname, rel, sym in PAIRS:
+        v = read_table(root, rel, sym, (2,))
+        lines.append("/* %s :: %s */" % (rel, sym))
+        lines.append("#define PTG_%s_0 %s" % (cname, _c_double(v[0])))
+        lines.append("#define PTG_%s_1 %s" % (cname, _c_double(v[1])))
     lines.append("")
     for cname, rel, sym, shape in SMALL_TABLES:
         vals = read_table(root, rel, sym, shape)
