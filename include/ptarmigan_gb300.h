@@ -251,6 +251,21 @@ ptg_status ptg_lcfa_photon_sample(ptg_ctx* ctx, size_t n, const double* chi, con
                                   const double* rand3, double* omega, double* theta);
 ptg_status ptg_lcfa_pair_t(ptg_ctx* ctx, size_t n, const double* chi, double* t_par, double* t_perp);
 
+/* Generalised Bessel function J(n-2..n+2, x, y) of
+ * special_functions/double_bessel.rs (DoubleBessel::around, mode 0; or
+ * DoubleBessel::evaluate, mode 1, which takes the saddle-point form where
+ * it applies), for 0 <= x <= n sqrt 2, 0 <= y <= n / 2.  j5: [count][5]. */
+ptg_status ptg_double_bessel(ptg_ctx* ctx, int32_t n, size_t count, const double* x, const double* y, int32_t mode,
+                             double* j5);
+
+/* Linearly polarised LMA emission sampler (nonlinear_compton/lp/mod.rs
+ * sample, with the CDF-table harmonic index) at peak amplitude a[i] and
+ * eta[i], drawing from the stream stream[i] at step `step`.
+ * out7: [count][n, s, theta, 1, xi1, xi2, xi3] in the LMA basis;
+ * status: [count] ptg_status per point. */
+ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
+                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
+
 /* Table maintenance: regenerates the CP nonlinear-Compton harmonic CDF
  * table on the device.  The reference ships it as
  * nonlinear_compton/cp/tables/cdf.rs, which is absent from its tree; this

@@ -218,6 +218,63 @@ double orc_nlc_probability(const double* k, const double* q, double dt, int pol)
     return nlc_probability(v4(k), v4(q), dt, pol, false, &p) ? p : NAN;
 }
 
+void orc_cp_pair_integrate(int n, double a, double eta, double* out2) { cp_pair_integrate(n, a, eta, &out2[0], &out2[1]); }
+void orc_cp_pair_by_summation(double a, double eta, double* out2) { cp_pair_by_summation(a, eta, out2); }
+int orc_cp_pair_by_lookup(double a, double eta, double* out2) { return cp_pair_by_lookup(a, eta, out2) ? 0 : 1; }
+int orc_cp_pair_rates(double a, double eta, double* out2) { return cp_pair_rates(a, eta, out2) ? 0 : 1; }
+
+// LMA pair probability (pair_creation::probability) and one generated positron
+double orc_bw_probability(const double* ell, const double* sv, const double* k, double a, double dt, int pol,
+                          double pol_angle, double* sv_out) {
+    double p;
+    Stokes out;
+    if (!bw_probability(v4(ell), Stokes(sv[0], sv[1], sv[2], sv[3]), v4(k), a, dt, pol, pol_angle, &p, &out)) return NAN;
+    sv_out[0] = out.i, sv_out[1] = out.q, sv_out[2] = out.u, sv_out[3] = out.v;
+    return p;
+}
+
+int orc_bw_generate(const double* ell, const double* sv, const double* k, double a, int pol, double pol_angle,
+                    uint64_t seed, uint64_t stream, uint32_t step, double* out5) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n;
+    V4 q;
+    uint64_t rej = 0;
+    int st = bw_generate(v4(ell), Stokes(sv[0], sv[1], sv[2], sv[3]), v4(k), a, pol, pol_angle, rng, &n, &q, &rej);
+    out5[0] = n;
+    put4(out5 + 1, q);
+    return st;
+}
+
+double orc_double_bessel_at(int n, double x_max, double y_max, double x, double y) {
+    return double_bessel_at(n, x_max, y_max, x, y);
+}
+double orc_double_bessel_evaluate(int n, double x, double y) { return double_bessel_evaluate(n, x, y); }
+double orc_double_bessel_spa(int n, double x, double y) { return double_bessel_spa(n, x, y); }
+double orc_lp_ceiling(int n, double a, double eta) { return lp_ceiling_at(n, a, eta); }
+void orc_lp_partial_rate(int n, double a, double eta, double* out2) { lp_partial_rate(n, a, eta, &out2[0], &out2[1]); }
+int orc_lp_sum_limit(double a, double eta) { return lp_sum_limit(a, eta); }
+double orc_lp_rate(double a, double eta) {
+    double r;
+    return lp_rate(a, eta, &r) ? r : NAN;
+}
+int orc_lp_harmonic_index(double a, double eta, double frac) { return lp_harmonic_index(a, eta, frac); }
+int orc_lp_sample(double a, double eta, uint64_t seed, uint64_t stream, uint32_t step, double* out7) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n;
+    double s, th;
+    Stokes sv;
+    uint64_t rej = 0;
+    int st = lp_sample(a, eta, rng, &n, &s, &th, &sv, &rej);
+    out7[0] = n, out7[1] = s, out7[2] = th, out7[3] = sv.i, out7[4] = sv.q, out7[5] = sv.u, out7[6] = sv.v;
+    return st;
+}
+
 struct OrcResult {
     std::vector<OracleParticle> parts;
     OracleStats stats;

@@ -452,6 +452,513 @@ double lp_linear_rate(double a, double eta) {
     return (a * a / 8.0) * (8.0 * eta / 3.0 - 16.0 * eta2 / 3.0 + 208.0 * eta3 / 15.0);
 }
 
+
+
+// Complex arithmetic with the semantics of num-complex 0.4.0 (the crate the
+// reference uses for the saddle-point double Bessel function): products by
+// the full formula, sqrt exact on the real axis, ln/exp through polar form,
+// acos(z) = -i ln(i sqrt(1 - z^2) + z).  Signed zeros follow IEEE, which
+// decides the branch of sqrt and therefore of acos for real z > 1.
+struct Cx {
+    double re, im;
+};
+static inline Cx cx_mul(Cx a, Cx b) { return Cx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+static inline Cx cx_add(Cx a, Cx b) { return Cx{a.re + b.re, a.im + b.im}; }
+static inline Cx cx_sub(Cx a, Cx b) { return Cx{a.re - b.re, a.im - b.im}; }
+static inline Cx cx_scale(double s, Cx a) { return Cx{s * a.re, s * a.im}; }
+static inline double cx_norm(Cx a) { return std::hypot(a.re, a.im); }
+static inline double cx_arg(Cx a) { return std::atan2(a.im, a.re); }
+static inline Cx cx_from_polar(double r, double t) { return Cx{r * std::cos(t), r * std::sin(t)}; }
+static inline Cx cx_ln(Cx a) { return Cx{std::log(cx_norm(a)), cx_arg(a)}; }
+static inline Cx cx_exp(Cx a) { return cx_from_polar(std::exp(a.re), a.im); }
+static inline Cx cx_sin(Cx a) { return Cx{std::sin(a.re) * std::cosh(a.im), std::cos(a.re) * std::sinh(a.im)}; }
+static inline Cx cx_sqrt(Cx a) {
+    if (a.im == 0.0) {
+        if (!std::signbit(a.re)) return Cx{std::sqrt(a.re), a.im};
+        double im = std::sqrt(-a.re);
+        return std::signbit(a.im) ? Cx{0.0, -im} : Cx{0.0, im};
+    }
+    if (a.re == 0.0) {
+        double x = std::sqrt(std::fabs(a.im) / 2.0);
+        return std::signbit(a.im) ? Cx{x, -x} : Cx{x, x};
+    }
+    return cx_from_polar(std::sqrt(cx_norm(a)), cx_arg(a) / 2.0);
+}
+static inline Cx cx_acos(Cx z) {
+    const Cx I{0.0, 1.0}, ONE{1.0, 0.0}, NEG_I{-0.0, -1.0};
+    return cx_mul(NEG_I, cx_ln(cx_add(cx_mul(cx_sqrt(cx_sub(ONE, cx_mul(z, z))), I), z)));
+}
+
+// ------------------------------------------------------- DoubleBessel --
+struct DoubleBessel;
+static double lp_ceiling(double a, double eta, DoubleBessel& dj);
+// special_functions/double_bessel.rs:7-410: J(n, x, y) = (1/pi) int_0^pi
+// cos(-n t + x cos t - y sin t) dt, for indices n-2..n+2
+struct DbElem {
+    double xi[3], lambda[2], f, g, h;
+};
+
+struct DoubleBessel {
+    int n, k_min;
+    double x_max, y_max;
+    std::vector<DbElem> tbl;
+    static constexpr int DELTA = 100;
+
+    DoubleBessel(int n_, double xm, double ym) : n(n_) {
+        int n_minus_bound = (int)std::floor(-2.0 * ym - xm);
+        int n_plus_bound = xm > 4.0 * (2.0 - SQRT_2) * ym ? (int)std::ceil(xm) : (int)std::ceil(2.0 * ym + xm * xm / (16.0 * ym));
+        int size = n_plus_bound - n_minus_bound + 2 * DELTA;
+        tbl.assign(size, DbElem{{1.0, 1.0, 1.0}, {1.0, 1.0}, 0.0, 0.0, 0.0});
+        k_min = n_minus_bound - DELTA;
+        x_max = std::fabs(xm);
+        y_max = std::fabs(ym);
+    }
+
+    // double_bessel.rs:142-246
+    void around(double x, double y, double j[5]) {
+        int n_minus = (int)std::floor(-2.0 * y - x);
+        int n_plus = (8.0 * y > x) ? (int)std::ceil(2.0 * y + x * x / (16.0 * y)) : (int)std::ceil(-2.0 * y + x);
+        size_t len = tbl.size();
+        for (size_t i = 1; i < len; ++i) {
+            int k = (int)i + k_min;
+            DbElem& t = tbl[i];
+            const DbElem& p = tbl[i - 1];
+            t.xi[0] = -x - 4.0 * y * y / p.xi[2];
+            t.xi[1] = 2.0 * (double)(k - 1) - 2.0 * y * p.xi[0] / p.xi[2];
+            t.xi[2] = -x - 2.0 * y * p.xi[1] / p.xi[2];
+            t.lambda[0] = t.xi[0] - 2.0 * y * t.xi[2] / p.lambda[1];
+            t.lambda[1] = t.xi[1] - p.lambda[0] * t.xi[2] / p.lambda[1];
+        }
+        double initial = n < 2000 ? 1.0e-100 : 1.0e-300;
+        tbl[len - 1].f = 0.0;
+        tbl[len - 2].f = 1.0 * initial;
+        tbl[len - 3].f = 2.0 * initial;
+        tbl[len - 1].g = 0.0;
+        tbl[len - 2].g = 1.0 / initial;
+        tbl[len - 3].g = -(2.0 * y * tbl[len - 1].g + tbl[len - 2].lambda[0] * tbl[len - 2].g) / tbl[len - 2].lambda[1];
+        int k_match = (n_plus + n_minus) / 2;
+        size_t i_match = (size_t)(k_match - k_min);
+        tbl[i_match].f = 0.0;
+        tbl[i_match].g = 0.0;
+        for (long i = (long)len - 4; i >= 0; --i) {
+            tbl[i].f = -(2.0 * y * tbl[i + 3].f + tbl[i + 2].xi[0] * tbl[i + 2].f + tbl[i + 2].xi[1] * tbl[i + 1].f) / tbl[i + 2].xi[2];
+            tbl[i].g = -(2.0 * y * tbl[i + 2].g + tbl[i + 1].lambda[0] * tbl[i + 1].g) / tbl[i + 1].lambda[1];
+            if (tbl[i].f > 1.0 && std::fabs(tbl[i_match].g) < 1.0e200) {
+                for (size_t jj = (size_t)i; jj < len; ++jj) {
+                    tbl[jj].f *= 1.0e-100;
+                    tbl[jj].g *= 1.0e100;
+                }
+            }
+        }
+        double f_match = tbl[i_match].f, g_match = tbl[i_match].g;
+        double sum_linear = 0.0, rss = 0.0;
+        for (size_t i = 0; i < i_match; ++i) {
+            tbl[i].h = tbl[i].g;
+            sum_linear += tbl[i].h;
+            rss = std::hypot(rss, tbl[i].h);
+        }
+        for (size_t i = i_match; i < len; ++i) {
+            tbl[i].h = g_match * tbl[i].f / f_match;
+            sum_linear += tbl[i].h;
+            rss = std::hypot(rss, tbl[i].h);
+        }
+        size_t it = (size_t)(n - k_min);
+        for (int q = 0; q < 5; ++q) {
+            const DbElem& t = tbl[it - 2 + q];
+            double val = signum(t.h / sum_linear) * std::fabs(t.h) / rss;
+            j[q] = std::isfinite(val) ? val : 0.0;
+        }
+    }
+
+    // double_bessel.rs:272-355 (saddle-point approximation)
+    static double j_spa(int ni, double x, double y) {
+        double n = ni;
+        if (n <= -2.0 * y + x) {
+            double ct = y > 0.0 ? x / (8.0 * y) - std::sqrt(x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y)) : n / x;
+            double th = std::acos(ct);
+            double f = x * std::sin(th) - y * std::sin(2.0 * th);
+            double d2f = -x * std::sin(th) + 4.0 * y * std::sin(2.0 * th);
+            double phi = FRAC_PI_4 * signum(d2f);
+            return std::cos(f - n * th + phi) * std::sqrt(2.0 / (PI * std::fabs(d2f)));
+        } else if (8.0 * y < x || n > 2.0 * y + x * x / (16.0 * y)) {
+            double disc = x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y);
+            Cx ct;
+            if (std::isnan(disc))
+                ct = Cx{n / x, 0.0};
+            else if (disc < 0.0)
+                ct = Cx{x / (8.0 * y), std::sqrt(-disc)};
+            else
+                ct = Cx{x / (8.0 * y) - std::sqrt(disc), 0.0};
+            const Cx I{0.0, 1.0};
+            Cx th = cx_acos(ct);
+            Cx th2 = cx_scale(2.0, th);
+            Cx f = cx_mul(I, cx_sub(cx_add(cx_scale(-n, th), cx_scale(x, cx_sin(th))), cx_scale(y, cx_sin(th2))));
+            Cx d2f = cx_mul(I, cx_add(cx_scale(-x, cx_sin(th)), cx_scale(4.0 * y, cx_sin(th2))));
+            Cx phase = cx_add(f, Cx{0.0, (PI - cx_arg(d2f)) / 2.0});
+            double term;
+            if (f.im == 0.0 && d2f.im == 0.0) {
+                term = 0.5 * std::exp(-f.re) * std::sqrt(2.0 / (PI * cx_norm(d2f)));
+            } else {
+                term = cx_exp(phase).re * std::sqrt(2.0 / (PI * cx_norm(d2f)));
+            }
+            return disc != 0.0 ? term : 0.0;
+        } else {
+            double r = std::sqrt(x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y));
+            double ct0 = x / (8.0 * y) - r, ct1 = x / (8.0 * y) + r;
+            double th0 = std::acos(ct0), th1 = std::acos(ct1);
+            double f0 = x * std::sin(th0) - y * std::sin(2.0 * th0), f1 = x * std::sin(th1) - y * std::sin(2.0 * th1);
+            double d0 = -x * std::sin(th0) + 4.0 * y * std::sin(2.0 * th0);
+            double d1 = -x * std::sin(th1) + 4.0 * y * std::sin(2.0 * th1);
+            double p0 = FRAC_PI_4 * signum(d0), p1 = FRAC_PI_4 * signum(d1);
+            return std::cos(f0 - n * th0 + p0) * std::sqrt(2.0 / (PI * std::fabs(d0))) +
+                   std::cos(f1 - n * th1 + p1) * std::sqrt(2.0 / (PI * std::fabs(d1)));
+        }
+    }
+
+    // double_bessel.rs:396-410
+    bool use_saddle_point(double x, double y) const {
+        if (n <= 10) return false;
+        double ne = n * (1.0 - std::sqrt(10.0 / n));
+        double xc = y > ne / 6.0 ? 4.0 * std::sqrt(y * (ne - 2.0 * y)) : ne + 2.0 * y;
+        return x < xc;
+    }
+
+    // double_bessel.rs:386-392
+    void evaluate(double x, double y, double j[5]) {
+        if (use_saddle_point(x, y)) {
+            for (int q = 0; q < 5; ++q) j[q] = j_spa(n - 2 + q, x, y);
+        } else {
+            around(x, y, j);
+        }
+    }
+};
+
+double double_bessel_at(int n, double x_max, double y_max, double x, double y) {
+    DoubleBessel dj(n, x_max, y_max);
+    double j[5];
+    dj.around(x, y, j);
+    return j[2];
+}
+
+double double_bessel_spa(int n, double x, double y) { return DoubleBessel::j_spa(n, x, y); }
+
+double lp_ceiling_at(int n, double a, double eta) {
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    return lp_ceiling(a, eta, dj);
+}
+
+double double_bessel_evaluate(int n, double x, double y) {
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    double j[5];
+    dj.evaluate(x, y, j);
+    return j[2];
+}
+
+// ------------------------------------------------- LP LMA emission ------
+// nonlinear_compton/lp/mod.rs:21-50
+static double lp_ddpr(double a, double eta, double s, double theta, DoubleBessel& dj) {
+    int n = dj.n;
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double wn = std::min(s / (sn * (1.0 - s)), 1.0);
+    double alpha = 2.0 * n * a * std::cos(theta) * std::sqrt(wn * (1.0 - wn)) / std::sqrt(1.0 + 0.5 * a * a);
+    double beta = a * a * s / (8.0 * eta * (1.0 - s));
+    double j[5];
+    dj.evaluate(alpha, beta, j);
+    double g0, g1, g2;
+    if (n % 2 == 0) {
+        g0 = j[2], g1 = -0.5 * (j[1] + j[3]), g2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        g0 = -j[2], g1 = 0.5 * (j[1] + j[3]), g2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    return (-g0 * g0 - a * a * (1.0 + 0.5 * s * s / (1.0 - s)) * (g0 * g2 - g1 * g1)) / (2.0 * PI);
+}
+
+// nonlinear_compton/lp/mod.rs:338-344
+int lp_sum_limit(double a, double eta) {
+    double m = 3.0 - 0.4 * std::pow(eta, 0.25);
+    double n_max = 6.0 * (1.0 + a * a) + 2.0 * std::pow(a, m);
+    return (int)std::ceil(n_max);
+}
+
+// nonlinear_compton/lp/mod.rs:53-140
+static double lp_ceiling(double a, double eta, DoubleBessel& dj) {
+    int n = dj.n;
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    double mx = -HUGE_VAL;
+    if (n == 1) {
+        mx = std::max(lp_ddpr(a, eta, 0.01 * smax, FRAC_PI_2, dj), lp_ddpr(a, eta, 0.99 * smax, FRAC_PI_2, dj));
+    } else if (a <= 2.0) {
+        for (int i = 1; i <= 32; ++i) mx = std::max(mx, lp_ddpr(a, eta, smax * (0.4 + 0.6 * i / 32.0), 0.0, dj));
+    } else if (a <= 5.0) {
+        int n_switch = (int)std::ceil(1.3 * std::pow(a, 1.2));
+        if (n < n_switch) {
+            double theta = FRAC_PI_2 * (1.0 - std::log((double)n) / std::log((double)n_switch));
+            for (int i = 0; i <= 32; ++i) mx = std::max(mx, lp_ddpr(a, eta, smax * i / 32.0, theta, dj));
+        } else {
+            double x_min = std::max(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.4);
+            int n_max = lp_sum_limit(a, eta);
+            int cnt = n < n_max / 2 ? 32 : 64;
+            for (int i = 1; i <= cnt; ++i) mx = std::max(mx, lp_ddpr(a, eta, smax * (x_min + (1.0 - x_min) * i / cnt), 0.0, dj));
+        }
+    } else {
+        int n_switch = (int)std::ceil(a * a);
+        if (n < n_switch) {
+            double nn = n, ns = n_switch;
+            double theta = FRAC_PI_2 * (std::pow(nn, -0.7) - std::pow(ns, -0.7)) / (1.0 - std::pow(ns, -0.7));
+            for (int i = 1; i <= 64; ++i) mx = std::max(mx, lp_ddpr(a, eta, smax * (0.3 + 0.7 * i / 64.0), theta, dj));
+        } else {
+            double x_min = std::max(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.3);
+            double x_peak = (1.0 + sn) / (2.0 + sn);
+            int len = n > 10 * n_switch ? 64 : (n > 3 * n_switch ? 42 : 32);
+            for (int i = 1; i <= len; ++i)
+                mx = std::max(mx, lp_ddpr(a, eta, smax * (x_min + (x_peak - x_min) * i / len), 0.0, dj));
+        }
+    }
+    return 1.15 * mx;
+}
+
+// nonlinear_compton/lp/mod.rs:142-302
+struct ThetaBound {
+    double s[16], f[16];
+
+    static double ln_double_bessel_x_zero(int ni, double y) {
+        double n = ni;
+        double z = std::sqrt(n / (4.0 * y) - 0.5);
+        const Cx I{0.0, 1.0};
+        Cx theta{FRAC_PI_2, std::log(std::sqrt(1.0 + z * z) - z)};
+        Cx s2 = cx_sin(cx_scale(2.0, theta));
+        Cx f = cx_mul(I, cx_sub(cx_scale(-n, theta), cx_scale(y, s2)));
+        Cx f2 = cx_mul(I, cx_scale(4.0 * y, s2));
+        double e = 0.5 * (PI - cx_arg(f2));
+        Cx phase = cx_add(f, cx_mul(I, Cx{e, 0.0}));
+        return std::log(std::sqrt(2.0 / (PI * cx_norm(f2)))) + phase.re + std::log(std::fabs(std::cos(phase.im)));
+    }
+
+    static ThetaBound for_harmonic(int n, double a, double eta) {
+        ThetaBound tb;
+        double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+        for (int i = 0; i < 16; ++i) {
+            double z = std::cos(PI * i / 15.0);
+            tb.s[i] = 0.5 * (z + 1.0) * sn / (1.0 + sn);
+            double wn = std::min(tb.s[i] / (sn * (1.0 - tb.s[i])), 1.0);
+            double x = 2.0 * n * a * std::sqrt(wn * (1.0 - wn)) / std::sqrt(1.0 + 0.5 * a * a);
+            double y = a * a * tb.s[i] / (8.0 * eta * (1.0 - tb.s[i]));
+            double x_crit = y > n / 6.0 ? 4.0 * std::sqrt(y) * std::sqrt(n - 2.0 * y) : n + 2.0 * y;
+            double ln_j_crit = std::log(0.443) - std::log((double)n) / 3.0;
+            double ln_j_bdy = (n % 2 == 0) ? ln_double_bessel_x_zero(n, y) : ln_double_bessel_x_zero(n + 1, y);
+            ln_j_bdy = std::fmin(ln_j_bdy, ln_j_crit);
+            double ct = 1.0 - x_crit * std::log(0.01) / (x * (ln_j_bdy - ln_j_crit));
+            ct = std::fmax(ct, -1.0);
+            tb.f[i] = std::acos(ct);
+            if (std::isnan(tb.f[i])) tb.f[i] = PI;
+        }
+        double f_min = tb.f[0];
+        for (int i = 1; i < 16; ++i) {
+            if (tb.f[i] < f_min)
+                f_min = tb.f[i];
+            else
+                tb.f[i] = f_min;
+        }
+        return tb;
+    }
+
+    double at(double arg) const {
+        double val = f[15];
+        for (int i = 1; i < 16; ++i) {
+            if (arg > s[i]) {
+                double w = (arg - s[i - 1]) / (s[i] - s[i - 1]);
+                val = w * f[i] + (1.0 - w) * f[i - 1];
+                break;
+            }
+        }
+        return std::fmin(val, FRAC_PI_2);
+    }
+};
+
+// nonlinear_compton/lp/mod.rs:306-400
+static void lp_single_diff(double a, double eta, double s, double theta_max, DoubleBessel& dj, double* integral, double* mx) {
+    double sum = 0.0, m = 0.0;
+    for (int k = 0; k < 32; ++k) {
+        double theta = 0.5 * (PTG_GAUSS_32_NODES[k] + 1.0) * theta_max;
+        double rate = lp_ddpr(a, eta, s, theta, dj);
+        sum += 4.0 * (0.5 * theta_max) * PTG_GAUSS_32_WEIGHTS[k] * rate;
+        m = std::max(m, rate);
+    }
+    *integral = sum;
+    *mx = m;
+}
+
+void lp_partial_rate(int n, double a, double eta, double* integral, double* mx) {
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    double s_peak = sn / (2.0 + sn);
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    ThetaBound tb = ThetaBound::for_harmonic(n, a, eta);
+    auto seg = [&](const double* nodes, const double* weights, int nn, double s0, double s1, double* I, double* M) {
+        double acc = 0.0, m = 0.0;
+        for (int k = 0; k < nn; ++k) {
+            double s = s0 + 0.5 * (s1 - s0) * (nodes[k] + 1.0);
+            double r, mm;
+            lp_single_diff(a, eta, s, tb.at(s), dj, &r, &mm);
+            acc += weights[k] * 0.5 * (s1 - s0) * r;
+            m = std::max(m, mm);
+        }
+        *I = acc;
+        *M = m;
+    };
+    if (sn < 1.0) {
+        double l, lm, u, um;
+        seg(PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32, 0.0, s_peak, &l, &lm);
+        seg(PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32, s_peak, smax, &u, &um);
+        *integral = u + l;
+        *mx = std::max(um, lm);
+    } else {
+        double l, lm, md, mm, u, um;
+        seg(PTG_GAUSS_16_NODES, PTG_GAUSS_16_WEIGHTS, 16, 0.0, smax - 2.0 * (smax - s_peak), &l, &lm);
+        seg(PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32, smax - 2.0 * (smax - s_peak), s_peak, &md, &mm);
+        seg(PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32, s_peak, smax, &u, &um);
+        *integral = l + md + u;
+        *mx = std::max(lm, std::max(mm, um));
+    }
+}
+
+// nonlinear_compton/lp/classical.rs:189-210
+bool lp_classical_rate(double a, double eta, double* out) {
+    double x = std::log(a);
+    if (x < PTG_NLC_CL_MIN) {
+        *out = a * a * eta / 3.0;
+        return true;
+    }
+    int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    if (ix >= 60) return false;
+    double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    *out = eta * std::exp((1.0 - dx) * g_lma.nlc_lp_cl_rate[ix] + dx * g_lma.nlc_lp_cl_rate[ix + 1]);
+    return true;
+}
+
+// nonlinear_compton/lp/mod.rs:399-463
+bool lp_rate(double a, double eta, double* out) {
+    const double MIN0 = PTG_NLC_LP_MIN_0, MIN1 = PTG_NLC_LP_MIN_1, S0 = PTG_NLC_LP_STEP_0, S1 = PTG_NLC_LP_STEP_1;
+    const double* T = g_lma.nlc_lp_rate;
+    double x = std::log(a), y = std::log(eta);
+    if (x < MIN0) {
+        *out = lp_linear_rate(a, eta);
+        return true;
+    }
+    int ix = (int)((x - MIN0) / S0);
+    double dx = (x - MIN0) / S0 - ix;
+    if (ix >= 60) return false;
+    if (y < MIN1) {
+        double f = (1.0 - dx) * T[ix] + dx * T[ix + 1];
+        *out = std::exp(f - MIN1) * eta;
+        return true;
+    }
+    int iy = (int)((y - MIN1) / S1);
+    if (ix < 61 - 1 && iy < 68 - 1) {
+        double dy = (y - MIN1) / S1 - iy;
+        double f = (1.0 - dx) * (1.0 - dy) * T[iy * 61 + ix] + dx * (1.0 - dy) * T[iy * 61 + ix + 1] +
+                   (1.0 - dx) * dy * T[(iy + 1) * 61 + ix] + dx * dy * T[(iy + 1) * 61 + ix + 1];
+        *out = std::exp(f);
+        return true;
+    }
+    return false;
+}
+
+// nonlinear_compton/lp/mod.rs:465-553
+static double lp_cdf_corner(const double* table, double frac, double a) {
+    if (frac <= table[1]) return 0.9;
+    bool ok;
+    if (a < 5.0) {
+        // the reference unwraps this inversion (a panic beyond the last node)
+        double n = Pwmci(table, 16).invert(frac, &ok);
+        return ok ? n : NAN;
+    }
+    double rs[30];
+    for (int i = 0; i < 15; ++i) {
+        rs[2 * i] = std::log(table[2 * i]);
+        rs[2 * i + 1] = std::log(-1.0 * std::log(1.0 - table[2 * i + 1]));
+    }
+    double f2 = std::log(-1.0 * std::log(1.0 - frac));
+    return std::exp(Pwmci(rs, 15, true).invert(f2, &ok));
+}
+
+int lp_harmonic_index(double a, double eta, double frac) {
+    const double MIN0 = PTG_NLC_LP_CDF_MIN_0, MIN1 = PTG_NLC_LP_CDF_MIN_1, S0 = PTG_NLC_LP_CDF_STEP_0, S1 = PTG_NLC_LP_CDF_STEP_1;
+    const double* T = g_lma.nlc_lp_cdf;
+    if (std::log(a) <= MIN0) return 1;
+    int ix = (int)((std::log(a) - MIN0) / S0);
+    double dx = (std::log(a) - MIN0) / S0 - ix;
+    if (ix >= 60) return -1;
+    if (std::log(eta) <= MIN1) {
+        double n = lp_cdf_corner(T + (size_t)ix * 32, frac, a) * (1.0 - dx) + lp_cdf_corner(T + (size_t)(ix + 1) * 32, frac, a) * dx;
+        return std::isfinite(n) ? (int)std::ceil(n) : -1;
+    }
+    int iy = (int)((std::log(eta) - MIN1) / S1);
+    if (61 * (iy + 1) + ix + 1 >= 4148) return -1;
+    double dy = (std::log(eta) - MIN1) / S1 - iy;
+    int idx[4] = {61 * iy + ix, 61 * iy + ix + 1, 61 * (iy + 1) + ix, 61 * (iy + 1) + ix + 1};
+    double w[4] = {(1.0 - dx) * (1.0 - dy), dx * (1.0 - dy), (1.0 - dx) * dy, dx * dy};
+    double n = 0.0;
+    for (int k = 0; k < 4; ++k) n += lp_cdf_corner(T + (size_t)idx[k] * 32, frac, a) * w[k];
+    return std::isfinite(n) ? (int)std::ceil(n) : -1;
+}
+
+// nonlinear_compton/lp/mod.rs:586-676
+int lp_sample(double a, double eta, DrawStream& rng, int* n_out, double* s_out, double* theta_out, Stokes* sv_out,
+              uint64_t* rej) {
+    int n = lp_harmonic_index(a, eta, rng.next());
+    if (n < 1) return PTG_ERR_OUT_OF_TABLE;
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    ThetaBound tb = ThetaBound::for_harmonic(n, a, eta);
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    double mx = lp_ceiling(a, eta, dj);
+    double s = 0.0, theta = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double ss = smax * rng.next();
+        double th = FRAC_PI_2 * rng.next();
+        if (th > tb.at(ss)) continue;
+        double z = mx * rng.next();
+        if (z < lp_ddpr(a, eta, ss, th, dj)) {
+            s = ss, theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    int quadrant = (int)(4.0 * rng.next());  // gen_range(0, 4)
+    if (quadrant == 1)
+        theta = PI - theta;
+    else if (quadrant == 2)
+        theta = PI + theta;
+    else if (quadrant == 3)
+        theta = 2.0 * PI - theta;
+    double wn = std::min(s / (sn * (1.0 - s)), 1.0);
+    double x = -2.0 * n * a * std::cos(theta) * std::sqrt(wn * (1.0 - wn)) / std::sqrt(1.0 + 0.5 * a * a);
+    double y = a * a * s / (8.0 * eta * (1.0 - s));
+    double j[5];
+    dj.evaluate(std::fabs(x), y, j);
+    double A0, A1, A2;
+    if (x > 0.0) {
+        A0 = j[2], A1 = 0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else if (n % 2 == 0) {
+        A0 = j[2], A1 = -0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        A0 = -j[2], A1 = 0.5 * (j[1] + j[3]), A2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    double u = std::sqrt(2.0 * n * eta * (1.0 - s) / s - (1.0 + 0.5 * a * a));
+    double xi0 = (1.0 - s + 1.0 / (1.0 - s)) * (powi(A1, 2) - A0 * A2) - 2.0 * powi(A0 / a, 2);
+    double xi1 = 2.0 * (powi(A1, 2) - A0 * A2) - 2.0 * (1.0 + 2.0 * u * u * powi(std::sin(theta), 2)) * powi(A0 / a, 2);
+    double xi2 = -1.0 * (2.0 * powi(u * A0 / a, 2) * std::sin(2.0 * theta) + 4.0 * u * A0 * A1 * std::sin(theta) / a);
+    *sv_out = Stokes(1.0, xi1 / xi0, xi2 / xi0, 0.0);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return PTG_OK;
+}
+
 // ------------------------------------------------- LMA NLC dispatch ----
 // nonlinear_compton/mod.rs:19-47
 bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classical, double* p) {
@@ -464,7 +971,7 @@ bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classica
     if (pol == PTG_POL_CIRCULAR) {
         ok = classical ? cp_classical_rate(a, eta, &f) : cp_rate(a, eta, &f);
     } else {
-        return false;  // the LP rates are added with the LP sampler
+        ok = classical ? lp_classical_rate(a * SQRT_2, eta, &f) : lp_rate(a * SQRT_2, eta, &f);
     }
     if (!ok) return false;
     *p = ALPHA_FINE * f * dphi / eta;
@@ -482,6 +989,8 @@ int nlc_generate(const V4& k, const V4& q, int pol, double pol_angle, bool class
     int st;
     if (pol == PTG_POL_CIRCULAR && !classical) {
         st = cp_sample(a, eta, rng, &n, &s, &cphi, &sv, rej);
+    } else if (pol == PTG_POL_LINEAR && !classical) {
+        st = lp_sample(a * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
     } else {
         return PTG_ERR_UNSUPPORTED;
     }
@@ -540,9 +1049,7 @@ int lma_radiate(const Laser& L, const V4& r, const V4& u, double dt, DrawStream&
     }
     V4 kappa = (SPEED_OF_LIGHT * COMPTON_TIME) * L.wavevector * chirp * width;
     double prob;
-    if (!nlc_probability(kappa, u, dt, L.d.polarization, classical, &prob)) {
-        return L.d.polarization == PTG_POL_CIRCULAR ? PTG_ERR_OUT_OF_TABLE : PTG_ERR_UNSUPPORTED;
-    }
+    if (!nlc_probability(kappa, u, dt, L.d.polarization, classical, &prob)) return PTG_ERR_OUT_OF_TABLE;
     if (rng.next() < prob) {
         int n;
         V4 k;

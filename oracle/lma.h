@@ -46,6 +46,20 @@ int cp_sample(double a, double eta, DrawStream& rng, int* n, double* s, double* 
 // nonlinear_compton/lp/linear.rs
 double lp_linear_rate(double a, double eta);
 
+// special_functions/double_bessel.rs
+double double_bessel_at(int n, double x_max, double y_max, double x, double y);
+double double_bessel_evaluate(int n, double x, double y);
+double double_bessel_spa(int n, double x, double y);
+double lp_ceiling_at(int n, double a, double eta);
+
+// nonlinear_compton/lp/mod.rs
+int lp_sum_limit(double a, double eta);
+void lp_partial_rate(int n, double a, double eta, double* integral, double* mx);
+bool lp_rate(double a, double eta, double* out);
+bool lp_classical_rate(double a, double eta, double* out);
+int lp_harmonic_index(double a, double eta, double frac);
+int lp_sample(double a, double eta, DrawStream& rng, int* n, double* s, double* theta, Stokes* sv, uint64_t* rej);
+
 // nonlinear_compton/mod.rs
 bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classical, double* p);
 int nlc_generate(const V4& k, const V4& q, int pol, double pol_angle, bool classical, DrawStream& rng, int* n,

@@ -92,6 +92,21 @@ def lib():
         "orc_cp_sample": (i, [d, d, u64, u64, u32, DP]),
         "orc_nlc_generate": (i, [DP, DP, i, d, u64, u64, u32, DP]),
         "orc_nlc_probability": (d, [DP, DP, d, i]),
+        "orc_cp_pair_integrate": (None, [i, d, d, DP]),
+        "orc_cp_pair_by_summation": (None, [d, d, DP]),
+        "orc_cp_pair_by_lookup": (i, [d, d, DP]),
+        "orc_cp_pair_rates": (i, [d, d, DP]),
+        "orc_bw_probability": (d, [DP, DP, DP, d, d, i, d, DP]),
+        "orc_bw_generate": (i, [DP, DP, DP, d, i, d, u64, u64, u32, DP]),
+        "orc_double_bessel_at": (d, [i, d, d, d, d]),
+        "orc_double_bessel_evaluate": (d, [i, d, d]),
+        "orc_double_bessel_spa": (d, [i, d, d]),
+        "orc_lp_ceiling": (d, [i, d, d]),
+        "orc_lp_partial_rate": (None, [i, d, d, DP]),
+        "orc_lp_sum_limit": (i, [d, d]),
+        "orc_lp_rate": (d, [d, d]),
+        "orc_lp_harmonic_index": (i, [d, d, d]),
+        "orc_lp_sample": (i, [d, d, u64, u64, u32, DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -282,6 +297,84 @@ def nlc_generate(k, q, pol, pol_angle, seed, stream, step):
 def nlc_probability(k, q, dt, pol):
     k, q = _vec(k, 4), _vec(q, 4)
     return lib().orc_nlc_probability(_dp(k), _dp(q), dt, pol)
+
+
+def cp_pair_integrate(n, a, eta):
+    out = np.zeros(2)
+    lib().orc_cp_pair_integrate(n, a, eta, _dp(out))
+    return out
+
+
+def cp_pair_by_summation(a, eta):
+    out = np.zeros(2)
+    lib().orc_cp_pair_by_summation(a, eta, _dp(out))
+    return out
+
+
+def cp_pair_by_lookup(a, eta):
+    out = np.zeros(2)
+    rc = lib().orc_cp_pair_by_lookup(a, eta, _dp(out))
+    return None if rc else out
+
+
+def cp_pair_rates(a, eta):
+    out = np.zeros(2)
+    rc = lib().orc_cp_pair_rates(a, eta, _dp(out))
+    return None if rc else out
+
+
+def bw_probability(ell, sv, k, a, dt, pol, pol_angle=0.0):
+    ell, sv, k = _vec(ell, 4), _vec(sv, 4), _vec(k, 4)
+    out = np.zeros(4)
+    p = lib().orc_bw_probability(_dp(ell), _dp(sv), _dp(k), a, dt, pol, pol_angle, _dp(out))
+    return p, out
+
+
+def bw_generate(ell, sv, k, a, pol, pol_angle, seed, stream, step):
+    ell, sv, k = _vec(ell, 4), _vec(sv, 4), _vec(k, 4)
+    out = np.zeros(5)
+    rc = lib().orc_bw_generate(_dp(ell), _dp(sv), _dp(k), a, pol, pol_angle, seed, stream, step, _dp(out))
+    return rc, out
+
+
+def double_bessel_at(n, x_max, y_max, x, y):
+    return lib().orc_double_bessel_at(n, x_max, y_max, x, y)
+
+
+def double_bessel_evaluate(n, x, y):
+    return lib().orc_double_bessel_evaluate(n, x, y)
+
+
+def double_bessel_spa(n, x, y):
+    return lib().orc_double_bessel_spa(n, x, y)
+
+
+def lp_ceiling(n, a, eta):
+    return lib().orc_lp_ceiling(n, a, eta)
+
+
+def lp_partial_rate(n, a, eta):
+    out = np.zeros(2)
+    lib().orc_lp_partial_rate(n, a, eta, _dp(out))
+    return out
+
+
+def lp_sum_limit(a, eta):
+    return lib().orc_lp_sum_limit(a, eta)
+
+
+def lp_rate(a, eta):
+    return lib().orc_lp_rate(a, eta)
+
+
+def lp_harmonic_index(a, eta, frac):
+    return lib().orc_lp_harmonic_index(a, eta, frac)
+
+
+def lp_sample(a, eta, seed, stream, step):
+    out = np.zeros(7)
+    rc = lib().orc_lp_sample(a, eta, seed, stream, step, _dp(out))
+    return rc, out
 
 
 # -- fields ---------------------------------------------------------------

@@ -1,0 +1,329 @@
+// LMA nonlinear Breit-Wheeler pair creation on the device (circular
+// polarisation): the double-differential partial rate, its integral, the
+// total rate by table lookup or by explicit harmonic summation, the Stokes
+// update of a photon that survives a step, and the positron sampler with its
+// zero-momentum-frame kinematics.
+//
+// Follows pair_creation/cp/mod.rs and pair_creation/mod.rs (cited per
+// function).  FP64: the probability is accumulated in FP64 and the rates
+// span hundreds of orders of magnitude.
+#pragma once
+#include "ptg_nlc.cuh"
+
+namespace ptg {
+
+constexpr double PAIR_LASER_S3 = -1.0;
+
+// pair_creation/cp/mod.rs:38-43
+__device__ __forceinline__ void bw_s_bounds(int n, double a, double eta, double* s_min, double* s_max) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    *s_min = fmin(0.5 * (1.0 - sqrt(1.0 - 4.0 / sn)), 0.5);
+    *s_max = 0.5;
+}
+
+// pair_creation/cp/mod.rs:47-64
+__device__ __forceinline__ void bw_elements(int n, double a, double eta, double s, double* unpol, double* d12,
+                                            double* d3) {
+    double ell = n;
+    double a2 = a * a;
+    double sn = 2.0 * ell * eta / (1.0 + a2);
+    double tmp = 1.0 / (sn * s * (1.0 - s));
+    double z = sqrt((4.0 * ell * ell) * (a2 / (1.0 + a2)) * tmp * (1.0 - tmp));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    double q = (1.0 - s) / s + s / (1.0 - s);
+    double la = ell * a / z;
+    *unpol = j * j + 0.25 * a2 * q * (jm * jm + jp * jp - 2.0 * j * j);
+    *d12 = (2.0 * la * la - (1.0 + a2)) * j * j - 0.5 * a2 * (jm * jm + jp * jp);
+    *d3 = 0.25 * a2 * q * (1.0 - 2.0 / (sn * s * (1.0 - s))) * (jm * jm - jp * jp);
+}
+
+// pair_creation/cp/mod.rs:66-72.  (2 theta).sin_cos() returns (sin, cos)
+// and the reference names them (cos_2theta, sin_2theta) in that order.
+__device__ __forceinline__ double bw_fully_resolved(int n, double a, double eta, double s, double theta, double sv1,
+                                                    double sv2, double sv3) {
+    double unpol, d12, d3;
+    bw_elements(n, a, eta, s, &unpol, &d12, &d3);
+    double sn2, cs2;
+    sincos(2.0 * theta, &sn2, &cs2);
+    return (unpol - (sv1 * sn2 + sv2 * cs2) * d12 - PAIR_LASER_S3 * sv3 * d3) / (2.0 * PI);
+}
+
+// pair_creation/cp/mod.rs:74-87: [S3 = +1, S3 = -1] components
+__device__ __forceinline__ void bw_over_theta(int n, double a, double eta, double s, double* re, double* im) {
+    double unpol, d12, d3;
+    bw_elements(n, a, eta, s, &unpol, &d12, &d3);
+    *re = unpol - PAIR_LASER_S3 * d3;
+    *im = unpol + PAIR_LASER_S3 * d3;
+}
+
+// pair_creation/cp/mod.rs:92-186: integral over s and theta, both S3 parts
+__device__ __noinline__ void bw_integrate(int n, double a, double eta, double* out_re, double* out_im) {
+    double ell = n;
+    double sn = 2.0 * ell * eta / (1.0 + a * a);
+    *out_re = 0.0, *out_im = 0.0;
+    if (sn <= 4.0) return;
+    double a2 = a * a;
+    double w1 = 1.0 / ell + 1.0;
+    double beta = a2 * a2 * w1 * w1 + 16.0 * (a2 - 2.0) * (a2 - 2.0) / (sn * sn) - 8.0 * a2 * (a2 - 2.0) / sn;
+    beta = sqrt(beta) / (a2 - 2.0);
+    double alpha = (a2 + 2.0 * ell) / (ell * (2.0 - a2)) - 4.0 / sn;
+    double s_peak = 0.5 * (1.0 - sqrt(alpha + beta));
+    double s_min, s_max;
+    bw_s_bounds(n, a, eta, &s_min, &s_max);
+    double lo[3], hi[3];
+    int nseg;
+    if (isfinite(s_peak)) {
+        double s_mid = 2.0 * s_peak - s_min;
+        if (s_mid > s_max) {
+            nseg = 2;
+            lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_max;
+        } else {
+            nseg = 3;
+            lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_mid, lo[2] = s_mid, hi[2] = s_max;
+        }
+    } else {
+        nseg = 1;
+        lo[0] = s_min, hi[0] = s_max;
+    }
+    double tr = 0.0, ti = 0.0;
+    for (int g = 0; g < nseg; ++g) {
+        double r = 0.0, i = 0.0;
+        double h = 0.5 * (hi[g] - lo[g]), m = 0.5 * (lo[g] + hi[g]);
+        for (int k = 0; k < 32; ++k) {
+            double sr, si;
+            bw_over_theta(n, a, eta, h * PTG_GAUSS_32_NODES[k] + m, &sr, &si);
+            r += h * PTG_GAUSS_32_WEIGHTS[k] * sr;
+            i += h * PTG_GAUSS_32_WEIGHTS[k] * si;
+        }
+        tr += r, ti += i;
+    }
+    *out_re = 2.0 * tr, *out_im = 2.0 * ti;
+}
+
+// pair_creation/cp/mod.rs:349-365
+__device__ __forceinline__ void bw_sum_limits(double a, double eta, int* n_min, int* n_max) {
+    double nm = ceil(2.0 * (1.0 + a * a) / eta);
+    double range = 2.0 * (0.25 + a * a) / eta + 13.0 * a * (2.0 + a);
+    double test = 0.25 - (1.0 + a * a) / (2.0 * nm * eta);
+    if (test <= 2.220446049250313e-16) {
+        *n_min = (int)nm + 1;
+        *n_max = (int)(nm + 1.0 + range);
+    } else {
+        *n_min = (int)nm;
+        *n_max = (int)(nm + range);
+    }
+}
+
+// pair_creation/cp/mod.rs:363-365: rate below exp(-200)
+__device__ __forceinline__ bool bw_is_too_small(double a, double eta) {
+    double q = log10(a) + 2.0;
+    return log10(eta) < -1.0 - q * q / 4.5;
+}
+
+// pair_creation/cp/mod.rs:385-393
+__device__ __noinline__ void bw_by_summation(double a, double eta, double* f0, double* f1) {
+    int n0, n1;
+    bw_sum_limits(a, eta, &n0, &n1);
+    double re = 0.0, im = 0.0;
+    for (int n = n0; n <= n1; ++n) {
+        double r, i;
+        bw_integrate(n, a, eta, &r, &i);
+        re += r, im += i;
+    }
+    *f0 = re, *f1 = im;
+}
+
+// pair_creation/cp/mod.rs:395-448; false where the reference panics
+__device__ __noinline__ bool bw_by_lookup(const double* T, double a, double eta, double* f0, double* f1) {
+    const double LMA = PTG_BW_CP_LN_MIN_A, LME = PTG_BW_CP_LN_MIN_ETA, SA = PTG_BW_CP_LN_A_STEP, SE = PTG_BW_CP_LN_ETA_STEP;
+    const int NC = 74, NR = 121;
+    double x = log(a), y = log(eta);
+    if (x < LMA) return false;
+    if (y < LME) {
+        *f0 = *f1 = 0.0;
+        return true;
+    }
+    int ix = (int)((x - LMA) / SA), iy = (int)((y - LME) / SE);
+    if (!(ix < NC - 1 && iy < NR - 1)) return false;
+    const double* p00 = T + ((size_t)iy * NC + ix) * 2;
+    const double* p01 = p00 + 2;
+    const double* p10 = p00 + 2 * NC;
+    const double* p11 = p10 + 2;
+    double f[2];
+    if (a * eta > 2.0) {
+        double dx = (x - LMA) / SA - ix, dy = (y - LME) / SE - iy;
+        double w0 = (1.0 - dx) * (1.0 - dy), w1 = dx * (1.0 - dy), w2 = (1.0 - dx) * dy, w3 = dx * dy;
+        for (int k = 0; k < 2; ++k) f[k] = exp(w0 * p00[k] + w1 * p01[k] + w2 * p10[k] + w3 * p11[k]);
+    } else {
+        double a_min = exp(LMA + ix * SA), a_max = exp(LMA + (ix + 1) * SA);
+        double e_min = exp(LME + iy * SE), e_max = exp(LME + (iy + 1) * SE);
+        double dx = (a - a_min) / (a_max - a_min), dy = (eta - e_min) / (e_max - e_min);
+        double w0 = (1.0 - dx) * (1.0 - dy), w1 = dx * (1.0 - dy), w2 = (1.0 - dx) * dy, w3 = dx * dy;
+        for (int k = 0; k < 2; ++k) f[k] = exp(1.0 / (w0 / p00[k] + w1 / p01[k] + w2 / p10[k] + w3 / p11[k]));
+    }
+    *f0 = f[0], *f1 = f[1];
+    return true;
+}
+
+// TotalRate::value / probability dispatch (pair_creation/cp/mod.rs:265-287)
+__device__ __forceinline__ bool bw_rates(const double* T, double a, double eta, double* f0, double* f1) {
+    if (a < 0.02 || bw_is_too_small(a, eta)) {
+        *f0 = *f1 = 0.0;
+        return true;
+    }
+    if (a < exp(PTG_BW_CP_LN_MIN_A)) {
+        bw_by_summation(a, eta, f0, f1);
+        return true;
+    }
+    return bw_by_lookup(T, a, eta, f0, f1);
+}
+
+// pair_creation/cp/mod.rs:191-243: s by rejection on the theta-integrated
+// spectrum, the side of s = 1/2, then theta by rejection.
+__device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3,
+                                              Draws& rng, double* s_out, double* theta_out, uint32_t* rej) {
+    double s_min, s_max;
+    bw_s_bounds(n, a, eta, &s_min, &s_max);
+    double mx = __longlong_as_double(0x7ff8000000000000LL);
+    for (int k = 0; k < 32; ++k) {
+        double s = 0.5 * (s_max - s_min) * PTG_GAUSS_32_NODES[k] + 0.5 * (s_min + s_max);
+        double re, im;
+        bw_over_theta(n, a, eta, s, &re, &im);
+        mx = fmax(mx, 0.5 * (re * (1.0 + sv3) + im * (1.0 - sv3)));
+    }
+    mx *= 1.5;
+    double s = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double ss = s_min + (s_max - s_min) * rng.next();
+        double z = mx * rng.next();
+        double re, im;
+        bw_over_theta(n, a, eta, ss, &re, &im);
+        if (z < 0.5 * (re * (1.0 + sv3) + im * (1.0 - sv3))) {
+            s = ss;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;
+    if (rng.next() < 0.5) s = 1.0 - s;
+    double theta_opt = 0.5 * atan2(sv2, sv1);
+    double tm = -HUGE_VAL;
+    for (int i = 0; i < 4; ++i) tm = fmax(tm, bw_fully_resolved(n, a, eta, s, theta_opt + i * FRAC_PI_2, sv1, sv2, sv3));
+    tm *= 1.01;
+    double theta = 0.0;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double th = 2.0 * PI * rng.next();
+        double z = tm * rng.next();
+        if (z < bw_fully_resolved(n, a, eta, s, th, sv1, sv2, sv3)) {
+            theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;
+    *s_out = s;
+    *theta_out = theta;
+    return 0;
+}
+
+// pair_creation/cp/mod.rs:314-346: harmonic by explicit summation
+__device__ __noinline__ int bw_sample(const double* T, double a, double eta, double sv1, double sv2, double sv3,
+                                      Draws& rng, int* n_out, double* s, double* theta, uint32_t* rej) {
+    int n0, n1;
+    bw_sum_limits(a, eta, &n0, &n1);
+    double f0, f1;
+    if (!bw_rates(T, a, eta, &f0, &f1)) return 2;
+    double target = 0.5 * (f0 * (1.0 + sv3) + f1 * (1.0 - sv3)) * rng.next();
+    double cum = 0.0;
+    int index = -1;
+    for (int k = n0; k <= n1; ++k) {
+        double re, im;
+        bw_integrate(k, a, eta, &re, &im);
+        cum += 0.5 * ((1.0 + sv3) * re + (1.0 - sv3) * im);
+        if (cum > target) {
+            index = k;
+            break;
+        }
+    }
+    if (index == -1) index = n1 - 1;
+    *n_out = index;
+    return bw_sample_s_theta(index, a, eta, sv1, sv2, sv3, rng, s, theta, rej);
+}
+
+// polarization.rs:101-130: Stokes parameters in the LMA basis
+__device__ __forceinline__ d4 stokes_in_lma_basis(d4 sv, d4 k) {
+    double k_minus = k.t - k.z;
+    double c = (k.z * k_minus - k.x * k.x) / (k_minus * hypot(k.x, k.z));
+    double sign = dsign(k.x * k.y);
+    c = fmin(fmax(c, -1.0), 1.0);
+    double s = sign * sqrt(1.0 - c * c);
+    double c2 = c * c - s * s, s2 = 2.0 * c * s;
+    return d4{sv.t, c2 * sv.x - s2 * sv.y, s2 * sv.x + c2 * sv.y, sv.z};
+}
+
+__device__ __forceinline__ d4 stokes_rotate_by(d4 sv, double theta) {
+    double s2, c2;
+    sincos(2.0 * theta, &s2, &c2);
+    return d4{sv.t, c2 * sv.x + s2 * sv.y, -s2 * sv.x + c2 * sv.y, sv.z};
+}
+
+// pair_creation/mod.rs:21-42 + cp/mod.rs:280-309 (CP).  Returns false out of table.
+__device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
+                                            double pol_angle, double* prob, d4* sv_out) {
+    double eta = dot4(k, ell);
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    double dphi = eta * dt / (COMPTON_TIME * ell.t);
+    double f0, f1;
+    if (!bw_rates(T, a, eta, &f0, &f1)) return false;
+    double c = ALPHA_FINE * dphi / eta;
+    double p = c * (0.5 * ((f0 + f1) + sv.z * (f0 - f1)));
+    double p_avg = c * (0.5 * (f0 + f1));
+    double delta = c * (0.5 * (f0 - f1));
+    d4 o = d4{sv.t, sv.x * (1.0 - p_avg) / (1.0 - p), sv.y * (1.0 - p_avg) / (1.0 - p), (sv.z * (1.0 - p_avg) - delta) / (1.0 - p)};
+    o = stokes_rotate_by(o, -pol_angle);
+    d3 g = stokes_from_lma_basis(mk3(o.x, o.y, o.z), ell);
+    *sv_out = d4{o.t, g.x, g.y, g.z};
+    *prob = p;
+    return true;
+}
+
+// pair_creation/mod.rs:49-110 (CP): the positron momentum
+__device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
+                                        int* n_out, d4* q_out, uint32_t* rej) {
+    double eta = dot4(k, ell);
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    int n;
+    double s, cphi;
+    int st = bw_sample(T, a, eta, sv.x, sv.y, sv.z, rng, &n, &s, &cphi, rej);
+    if (st != 0) return st;
+    double j = n;
+    double e_zmf = sqrt(0.5 * j * eta);
+    double p_zmf = sqrt(0.5 * j * eta - 1.0 - a * a);
+    double ct = (1.0 - 2.0 * s) * e_zmf / p_zmf;
+    if (!(ct <= 1.0 && ct >= -1.0)) return 3;
+    d4 t = d4{ell.t + j * k.t, ell.x + j * k.x, ell.y + j * k.y, ell.z + j * k.z};
+    double m = sqrt(dot4(t, t));
+    d4 uz = d4{t.t / m, t.x / m, t.y / m, t.z / m};
+    d4 jk = boost_by(d4{j * k.t, j * k.x, j * k.y, j * k.z}, uz);
+    d3 along = -normalize(mk3(jk.x, jk.y, jk.z));
+    double sp, cp;
+    sincos(pol_angle, &sp, &cp);
+    d4 e4 = boost_by(d4{0.0, cp, sp, 0.0}, uz);
+    d3 eps = normalize(mk3(e4.x, e4.y, e4.z));
+    eps = normalize(cross(along, cross(eps, along)));
+    double sc, cc;
+    sincos(cphi, &sc, &cc);
+    d3 perp = rotate_around(eps, along, sc, cc);
+    d3 q3 = p_zmf * (ct * along + sqrt(1.0 - ct * ct) * perp);
+    d4 q = d4{sqrt(1.0 + a * a + dot(q3, q3)), q3.x, q3.y, q3.z};
+    q = boost_by(q, d4{uz.t, -uz.x, -uz.y, -uz.z});
+    double s_new = 1.0 - dot4(k, q) / dot4(k, ell);
+    if (!(fabs(s - s_new) / s < 1.0e-3)) return 3;
+    *n_out = n;
+    *q_out = q;
+    return 0;
+}
+
+}  // namespace ptg

@@ -16,6 +16,9 @@ namespace ptg {
 enum { SP_ELECTRON = 0, SP_POSITRON = 1, SP_PHOTON = 2 };
 enum { FLAG_INTERMEDIATE = 1, FLAG_DROP = 2 };
 enum { ST_OK = 0, ST_OUT_OF_TABLE = 2, ST_SANITY = 3, ST_REJECTION_CAP = 4, ST_UNSUPPORTED = 9 };
+// A queue slot reserved by an append that overflowed the store: published
+// so that its consumer can retire it (the batch is rerun with a larger store).
+enum { ST_PHANTOM = 100 };
 
 // Shower store, structure of arrays.  Four-vectors are component-major:
 // component c of particle i is at v[c * cap + i].
@@ -24,6 +27,8 @@ struct Store {
     double *weight, *payload, *parent_chi, *icount, *work;
     unsigned long long *id, *parent_id, *primary, *stream;
     int *species, *generation, *flags, *status;
+    int* coll;              // collision of each particle (multi-collision queue)
+    unsigned int* ready;    // queue: slot written and published
     unsigned long long cap;
 };
 
@@ -33,6 +38,8 @@ struct Counters {
     unsigned long long overflow; // appends that did not fit
     unsigned long long lepton_steps, photon_steps, emissions, pair_events, rejections, errors;
     unsigned long long n_out;    // compaction cursor
+    unsigned long long completed; // queue: slots finished (children appended)
+    unsigned long long timeouts;  // queue: bounded waits that ran out
 };
 
 struct StepOptions {
@@ -59,6 +66,8 @@ struct WaveArgs {
     Counters* c;
     const PairGL* gl;
     const LmaTables* lma;
+    double* dbw;                   // DoubleBessel workspaces (LP LMA), one slot per resident lane
+    int db_cap;                    // orders per slot
     unsigned long long seed;
     unsigned long long lo, hi;     // wave = store slots [lo, hi)
     unsigned long long n_primaries, id_base;
@@ -96,6 +105,7 @@ struct Lane {
     unsigned long long slot, stream, id;
     uint32_t step;
     int species, gen, status, flags;
+    int coll;
     bool decayed;
 };
 
@@ -129,9 +139,32 @@ __device__ __forceinline__ void spawn(const WaveArgs& a, unsigned long long slot
     s.status[slot] = ST_OK;
 }
 
+// Queue mode: a spawned slot is published (collision index, then the ready
+// flag with release semantics) after its data is written.
+__device__ __forceinline__ void publish_slot(const WaveArgs& a, unsigned long long slot, int coll) {
+    a.s.coll[slot] = coll;
+    __threadfence();
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.s.ready + slot), "r"(1u) : "memory");
+}
+
+// Queue mode: slots of an append that did not fit.  Those inside the store
+// are published as phantoms; those beyond it are counted as finished here,
+// since no consumer will ever read them.
+__device__ __forceinline__ void retire_overflow(const WaveArgs& a, unsigned long long slot, unsigned count) {
+    for (unsigned q = 0; q < count; ++q) {
+        unsigned long long sl = slot + q;
+        if (sl < a.s.cap) {
+            a.s.status[sl] = ST_PHANTOM;
+            publish_slot(a, sl, 0);
+        } else {
+            atomicAdd(&a.c->completed, 1ull);
+        }
+    }
+}
+
 // One charged-particle step: main.rs:170-206.  Returns false when the
 // particle is finished.
-template <int MODEL>
+template <int MODEL, bool QUEUE = false>
 __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit) {
     const FieldParams& f = a.f;
     double rqm = (L.species == SP_ELECTRON ? ELECTRON_CHARGE : -ELECTRON_CHARGE) / ELECTRON_MASS;
@@ -216,8 +249,14 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         }
     } else {
         lma_push(f, L.r, L.u, rqm, dt, a.o.eqn, &r, &u, &dt_actual, &dwork);
-        int st = lma_radiate(f, *a.lma, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr, &kpol,
-                             &a_eff, &chi, &absorption, rej);
+        DbWork dbw{nullptr, 0};
+        if (a.dbw) {
+            size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+            dbw.base = a.dbw + warp * (size_t)a.db_cap * 5 * 32 + lane_id();
+            dbw.cap = a.db_cap;
+        }
+        int st = lma_radiate(f, *a.lma, dbw, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr,
+                             &kpol, &a_eff, &chi, &absorption, rej);
         if (st != ST_OK) {
             L.status = st;
             L.r = r;
@@ -230,8 +269,10 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         if (slot < a.s.cap) {
             spawn(a, slot, SP_PHOTON, r, k, d4{0, 0, 0, 0}, d4{1.0, kpol.x, kpol.y, kpol.z}, L.weight, a_eff, chi, 0.0,
                   L.id, a.s.primary[L.slot], child_stream(L.stream, L.step, 0), L.gen + 1);
+            if (QUEUE) publish_slot(a, slot, L.coll);
         } else {
             atomicAdd(&a.c->overflow, 1ull);
+            if (QUEUE) retire_overflow(a, slot, 1);
         }
         ++*nemit;
         if (a.o.electron_recoils) {
@@ -247,7 +288,7 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
 }
 
 // One photon step: main.rs:214-256.
-template <int MODEL>
+template <int MODEL, bool QUEUE = false>
 __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* npair) {
     const FieldParams& f = a.f;
     double dt = a.o.dt;
@@ -341,8 +382,13 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
                   child_stream(L.stream, L.step, 1), L.gen + 1);
             spawn(a, slot + 1, SP_POSITRON, r, up, rest, unpol, frac * L.weight, a_eff, chi, 0.5 * absorption, L.id,
                   prim, child_stream(L.stream, L.step, 2), L.gen + 1);
+            if (QUEUE) {
+                publish_slot(a, slot, L.coll);
+                publish_slot(a, slot + 1, L.coll);
+            }
         } else {
             atomicAdd(&a.c->overflow, 2ull);
+            if (QUEUE) retire_overflow(a, slot, 2);
         }
         ++*npair;
         if (frac == 1.0)

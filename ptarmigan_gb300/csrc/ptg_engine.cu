@@ -7,6 +7,7 @@
 // output arrays.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -64,6 +65,10 @@ struct ptg_ctx {
     PairGL* gl = nullptr;
     LmaTables* lma_dev = nullptr;
     LmaTables lma_host{};
+    // DoubleBessel workspaces for linearly polarised LMA emission
+    void* dbw = nullptr;
+    size_t dbw_bytes = 0;
+    int grid_cap = 0;  // > 0: the wave grid is capped (workspace budget)
     std::vector<void*> table_bufs;
     bool tables_loaded = false;
 };
@@ -335,6 +340,39 @@ __global__ void k_pair_t(unsigned long long n, const double* chi, double* tpar, 
     if (i < n) lcfa_auxiliary_t(chi[i], &tpar[i], &tperp[i]);
 }
 
+// J(n-2..n+2, x, y) per point: mode 0 by recurrence, 1 as the rate
+// evaluation selects (saddle point where it applies).
+__global__ void k_double_bessel(unsigned long long m, int n, int cap, const double* x, const double* y, int mode,
+                                double* ws, double* j5, int* ok) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap};
+    DbGeom g;
+    double j[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    bool good = db_geom(n, cap, &g) && (mode ? db_evaluate(g, w, x[i], y[i], j) : db_around(g, w, x[i], y[i], j));
+    for (int q = 0; q < 5; ++q) j5[5 * i + q] = j[q];
+    ok[i] = good ? 1 : 0;
+}
+
+// One LP harmonic/s/azimuth/Stokes sample per point (the draws of the
+// stream `stream[i]` at `step`).
+__global__ void k_lp_sample(unsigned long long m, int cap, const LmaTables* t, const double* a, const double* eta,
+                            unsigned long long seed, const unsigned long long* stream, unsigned step, double* ws,
+                            double* out7, int* status) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap};
+    Draws rng;
+    rng.begin(seed, stream[i], step);
+    int n = 0;
+    double s = 0.0, th = 0.0;
+    d3 sv = mk3(0.0, 0.0, 0.0);
+    uint32_t rej = 0;
+    status[i] = lp_sample(nlc_view(*t), w, a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
+    double* o = out7 + 7 * i;
+    o[0] = n, o[1] = s, o[2] = th, o[3] = 1.0, o[4] = sv.x, o[5] = sv.y, o[6] = sv.z;
+}
+
 // ---------------------------------------------------------- storage -----
 static void carve_store(Store* s, void* mem, unsigned long long cap) {
     char* p = (char*)mem;
@@ -564,6 +602,7 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     cudaFreeHost(c->h_counters);
     cudaFree(c->gl);
     cudaFree(c->lma_dev);
+    cudaFree(c->dbw);
     for (void* p : c->table_bufs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -647,6 +686,7 @@ static int grid_for(ptg_ctx* c, const void* kernel) {
 template <int MODEL>
 static cudaError_t launch_wave(ptg_ctx* c, const WaveArgs& a) {
     int grid = grid_for(c, (const void*)collide_wave<MODEL>);
+    if (c->grid_cap > 0 && grid > c->grid_cap) grid = c->grid_cap;
     unsigned long long n = a.hi - a.lo;
     unsigned long long need = (n + c->block - 1) / c->block;
     if ((unsigned long long)grid > need) grid = (int)need;
@@ -662,6 +702,44 @@ static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
         case M_FOCUSED_LASER: return launch_wave<M_FOCUSED_LASER>(c, a);
         default: return launch_wave<M_FAST_FOCUSED_LASER>(c, a);
     }
+}
+
+// Linearly polarised LMA emission evaluates J(n, x, y) by recurrence in a
+// per-lane workspace of 40 bytes per order.  Slots are sized for harmonics up
+// to 1.5x the reference's harmonic sum limit at 1.05 a0 (its eta -> 0 bound);
+// a sampled order beyond that retires the particle with PTG_ERR_UNSUPPORTED.
+// The workspace stays within min(8 GiB, free / 4), which may cap the grid.
+static ptg_status ensure_dbw(ptg_ctx* c, const ptg_laser_desc* laser, WaveArgs* a) {
+    double A = 1.05 * laser->a0;
+    int n_cap = (int)std::ceil(1.5 * (6.0 * (1.0 + A * A) + 2.0 * A * A * A)) + 16;
+    int cap = db_len_for(n_cap);
+    size_t per_warp = (size_t)cap * 5 * 32 * sizeof(double);
+    size_t warps_per_block = (size_t)(c->block + 31) / 32;
+    const void* kern = laser->model == PTG_PLANE_WAVE ? (const void*)collide_wave<M_PLANE_WAVE>
+                                                      : (const void*)collide_wave<M_FOCUSED_LASER>;
+    int grid = grid_for(c, kern);
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    size_t budget = std::min<size_t>((size_t)8 << 30, free_b / 4);
+    size_t max_blocks = budget / (per_warp * warps_per_block);
+    if (max_blocks < 1)
+        return set_err(PTG_ERR_ALLOC, "no room for one block of LP LMA workspaces at a0 = " + std::to_string(laser->a0));
+    if ((size_t)grid > max_blocks) grid = (int)max_blocks;
+    size_t need = per_warp * warps_per_block * (size_t)grid;
+    if (need > c->dbw_bytes) {
+        cudaFree(c->dbw);
+        c->dbw = nullptr;
+        c->dbw_bytes = 0;
+        if (cudaMalloc(&c->dbw, need) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PTG_ERR_ALLOC, "cannot allocate LP LMA workspaces (" + std::to_string(need) + " bytes)");
+        }
+        c->dbw_bytes = need;
+    }
+    a->dbw = (double*)c->dbw;
+    a->db_cap = cap;
+    c->grid_cap = grid;
+    return PTG_OK;
 }
 
 // Runs a batch whose primaries are described by device pointers `d_in`.
@@ -704,6 +782,13 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
     a.o.keep_decayed = o->keep_decayed_photons;
     a.gl = c->gl;
     a.lma = c->lma_dev;
+    a.dbw = nullptr;
+    a.db_cap = 0;
+    c->grid_cap = 0;
+    if (!lcfa && laser->polarization != PTG_POL_CIRCULAR) {
+        st = ensure_dbw(c, laser, &a);
+        if (st != PTG_OK) return st;
+    }
     a.seed = seed;
     a.n_primaries = n;
     a.id_base = id_base;
@@ -1005,6 +1090,55 @@ ptg_status ptg_lcfa_photon_sample(ptg_ctx* c, size_t n, const double* chi, const
                                    k_photon_sample<<<(unsigned)((n + 127) / 128) + 1, 128, 0, c->stream>>>(
                                        n, (double*)d[0], (double*)d[1], (double*)d[2], (double*)d[3], (double*)d[4]);
                                });
+}
+
+ptg_status ptg_double_bessel(ptg_ctx* c, int32_t n, size_t count, const double* x, const double* y, int32_t mode,
+                             double* j5) {
+    if (!c || !x || !y || !j5) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n < 1 || n > 1000000) return set_err(PTG_ERR_INVALID_ARGUMENT, "order out of range");
+    if (count == 0) return PTG_OK;
+    cudaSetDevice(c->device);
+    int cap = db_len_for(n);
+    size_t lanes = (count + 31) / 32 * 32;
+    std::vector<double> a(x, x + count), b(y, y + count);
+    std::vector<int> ok(count, 0);
+    ptg_status st = with_device_buffers(
+        c, {{a.data(), 8 * count}, {b.data(), 8 * count}, {nullptr, lanes * (size_t)cap * 40}, {j5, 40 * count},
+            {ok.data(), 4 * count}},
+        [&](std::vector<void*>& d) {
+            k_double_bessel<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
+                count, n, cap, (double*)d[0], (double*)d[1], mode, (double*)d[2], (double*)d[3], (int*)d[4]);
+        });
+    if (st != PTG_OK) return st;
+    for (size_t i = 0; i < count; ++i)
+        if (!ok[i]) return set_err(PTG_ERR_INVALID_ARGUMENT, "(x, y) outside 0 <= x <= n sqrt 2, 0 <= y <= n / 2");
+    return PTG_OK;
+}
+
+ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+    if (!c || !a || !eta || !stream || !out7 || !status) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (count == 0) return PTG_OK;
+    if (!c->tables_loaded) {
+        ptg_status st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    cudaSetDevice(c->device);
+    double amax = 0.0;
+    for (size_t i = 0; i < count; ++i) amax = std::max(amax, a[i]);
+    int n_cap = (int)std::ceil(1.5 * (6.0 * (1.0 + amax * amax) + 2.0 * amax * amax * amax)) + 16;
+    int cap = db_len_for(n_cap);
+    size_t lanes = (count + 31) / 32 * 32;
+    std::vector<double> va(a, a + count), ve(eta, eta + count);
+    std::vector<unsigned long long> vs(stream, stream + count);
+    return with_device_buffers(
+        c, {{va.data(), 8 * count}, {ve.data(), 8 * count}, {vs.data(), 8 * count}, {nullptr, lanes * (size_t)cap * 40},
+            {out7, 56 * count}, {status, 4 * count}},
+        [&](std::vector<void*>& d) {
+            k_lp_sample<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
+                count, cap, c->lma_dev, (double*)d[0], (double*)d[1], seed, (unsigned long long*)d[2], step,
+                (double*)d[3], (double*)d[4], (int*)d[5]);
+        });
 }
 
 ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_par, double* t_perp) {

@@ -4,6 +4,8 @@
 #pragma once
 #include "ptg_fields.cuh"
 #include "ptg_math.cuh"
+#include "ptg_bw.cuh"
+#include "ptg_lp.cuh"
 #include "ptg_nlc.cuh"
 
 namespace ptg {
@@ -35,10 +37,11 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
 
 // plane_wave.rs:251-282 / focused_laser.rs:260-281 with
 // nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
+// `dbw` is this lane's DoubleBessel workspace (linear polarisation only).
 // Returns a ptg status (0 = ok).
-__device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, d4 r, d4 u, double dt, Draws& rng,
-                                        bool classical, bool* emitted, d4* k_out, d4* u_prime, d3* pol, double* a_eff,
-                                        double* chi, double* absorption, uint32_t* rej) {
+__device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw, d4 r, d4 u,
+                                        double dt, Draws& rng, bool classical, bool* emitted, d4* k_out, d4* u_prime,
+                                        d3* pol, double* a_eff, double* chi, double* absorption, uint32_t* rej) {
     *emitted = false;
     double a = sqrt(lma_a_sqd(f, r));
     double chirp = 1.0;
@@ -59,16 +62,20 @@ __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t
     double dphi = dt * eta / (COMPTON_TIME * u.t);
     NlcTables nt = nlc_view(t);
     double rate;
-    if (!f.circular) return 9;  // PTG_ERR_UNSUPPORTED: LP sampler not built
-    bool ok = classical ? cp_classical_rate(nt, aq, eta, &rate) : cp_rate(nt, aq, eta, &rate);
+    bool ok;
+    if (f.circular)
+        ok = classical ? cp_classical_rate(nt, aq, eta, &rate) : cp_rate(nt, aq, eta, &rate);
+    else
+        ok = classical ? lp_classical_rate(nt, aq * SQRT_2, eta, &rate) : lp_rate(nt, aq * SQRT_2, eta, &rate);
     if (!ok) return 2;  // PTG_ERR_OUT_OF_TABLE
     double prob = ALPHA_FINE * rate * dphi / eta;
     if (rng.next() < prob) {
-        if (classical) return 9;
+        if (classical) return 9;  // PTG_ERR_UNSUPPORTED: classical LMA samplers not built
         int n;
         double s, cphi;
         d3 sv;
-        int st = cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
+        int st = f.circular ? cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
+                            : lp_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
         if (st != 0) return st;
         d4 k;
         st = nlc_kinematics(kappa, u, aq, eta, n, s, cphi, sv, f.pol_angle, classical, &k, pol);
@@ -83,7 +90,8 @@ __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t
     return 0;
 }
 
-// plane_wave.rs:284-316 / focused_laser.rs:283-306
+// plane_wave.rs:284-316 / focused_laser.rs:283-306 with
+// pair_creation::probability and generate (pair_creation/mod.rs:21-110).
 __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTables& t, d4 r, d4 ell, d4 pol, double dt,
                                             Draws& rng, double rate_increase, double* prob, d4* pol_new,
                                             bool* created, d4* ue, d4* up, double* frac, double* a_eff, double* chi,
@@ -91,7 +99,31 @@ __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTable
     *prob = 0.0;
     *pol_new = pol;
     *created = false;
-    return 9;  // PTG_ERR_UNSUPPORTED until the LMA pair samplers land
+    double a = sqrt(lma_a_sqd(f, r));
+    double chirp = 1.0;
+    if (f.model == M_PLANE_WAVE) {
+        chirp = 1.0 + 2.0 * f.chirp_b * phase_of(f, r);
+        if (chirp < 0.0 && a > 0.0) return 3;
+    }
+    double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp;
+    d4 kappa = d4{kk, 0.0, 0.0, kk};
+    if (!f.circular) return 9;  // PTG_ERR_UNSUPPORTED: LP pair sampler not built
+    if (!bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)) return 2;
+    double ri = (*prob * rate_increase > 0.1) ? 0.1 / *prob : rate_increase;
+    if (rng.next() < *prob * ri) {
+        int n;
+        d4 q;
+        int st = bw_generate(t.bw_cp_total, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej);
+        if (st != 0) return st;
+        *ue = d4{ell.t + n * kappa.t - q.t, ell.x + n * kappa.x - q.x, ell.y + n * kappa.y - q.y, ell.z + n * kappa.z - q.z};
+        *up = q;
+        *frac = 1.0 / ri;
+        *a_eff = a;
+        *chi = a * dot4(ell, kappa);
+        *absorption = n * kappa.t;
+        *created = true;
+    }
+    return 0;
 }
 
 }  // namespace ptg

@@ -1,0 +1,544 @@
+// Nonlinear Compton scattering in a linearly polarised background (LMA):
+// the generalised Bessel function J(n, x, y), the double-differential rate
+// in (s, theta), its rejection ceiling, the harmonic index from the CDF
+// table, and the sampler with the emitted photon's Stokes parameters.
+//
+// J(n, x, y) follows special_functions/double_bessel.rs: a forward
+// recurrence (five coefficients per order, kept in a per-lane workspace in
+// global memory), a backward recurrence for the two solutions f and g with
+// rescaling, and normalisation over all orders.  Here the backward pass
+// accumulates the normalisation sums as it goes instead of storing f, g and
+// h, so only the five forward coefficients need memory: 40 bytes per order,
+// about 3.83 n + 200 orders.  The workspace is lane-interleaved (element e,
+// coefficient c of a lane at base[(5 e + c) * 32]) so that a warp's
+// accesses coalesce.
+#pragma once
+#include "ptg_math.cuh"
+#include "ptg_nlc.cuh"
+
+namespace ptg {
+
+// ---------------------------------------------------------- complex -----
+// Complex arithmetic with the semantics of num-complex 0.4 (products by the
+// full formula, sqrt exact on the axes, ln and exp through polar form,
+// acos(z) = -i ln(i sqrt(1 - z^2) + z)); signed zeros pick the branch of
+// sqrt and hence of acos for real z > 1.
+struct cxd {
+    double re, im;
+};
+__host__ __device__ __forceinline__ cxd cx_mul(cxd a, cxd b) { return cxd{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__host__ __device__ __forceinline__ cxd cx_add(cxd a, cxd b) { return cxd{a.re + b.re, a.im + b.im}; }
+__host__ __device__ __forceinline__ cxd cx_sub(cxd a, cxd b) { return cxd{a.re - b.re, a.im - b.im}; }
+__host__ __device__ __forceinline__ cxd cx_scale(double s, cxd a) { return cxd{s * a.re, s * a.im}; }
+__host__ __device__ __forceinline__ double cx_norm(cxd a) { return hypot(a.re, a.im); }
+__host__ __device__ __forceinline__ double cx_arg(cxd a) { return atan2(a.im, a.re); }
+__host__ __device__ __forceinline__ cxd cx_from_polar(double r, double t) { return cxd{r * cos(t), r * sin(t)}; }
+__host__ __device__ __forceinline__ cxd cx_ln(cxd a) { return cxd{log(cx_norm(a)), cx_arg(a)}; }
+__host__ __device__ __forceinline__ cxd cx_exp(cxd a) { return cx_from_polar(exp(a.re), a.im); }
+__host__ __device__ __forceinline__ cxd cx_sin(cxd a) { return cxd{sin(a.re) * cosh(a.im), cos(a.re) * sinh(a.im)}; }
+__host__ __device__ __forceinline__ cxd cx_sqrt(cxd a) {
+    if (a.im == 0.0) {
+        if (!signbit(a.re)) return cxd{sqrt(a.re), a.im};
+        double im = sqrt(-a.re);
+        return signbit(a.im) ? cxd{0.0, -im} : cxd{0.0, im};
+    }
+    if (a.re == 0.0) {
+        double x = sqrt(fabs(a.im) / 2.0);
+        return signbit(a.im) ? cxd{x, -x} : cxd{x, x};
+    }
+    return cx_from_polar(sqrt(cx_norm(a)), cx_arg(a) / 2.0);
+}
+__host__ __device__ __forceinline__ cxd cx_acos(cxd z) {
+    const cxd I{0.0, 1.0}, ONE{1.0, 0.0}, NEG_I{-0.0, -1.0};
+    return cx_mul(NEG_I, cx_ln(cx_add(cx_mul(cx_sqrt(cx_sub(ONE, cx_mul(z, z))), I), z)));
+}
+
+// ----------------------------------------------------- DoubleBessel -----
+struct DbWork {
+    double* base;  // this lane's slot: coefficient c of order e at base[(5 e + c) * 32]
+    int cap;       // orders the slot holds
+};
+
+struct DbGeom {
+    int n, k_min, len;
+};
+
+// double_bessel.rs:39-83 (DoubleBessel::at_index with x_max = n sqrt 2,
+// y_max = n / 2).  Returns false if the workspace is too small.
+__host__ __device__ __forceinline__ bool db_geom(int n, int cap, DbGeom* g) {
+    double xm = n * SQRT_2, ym = n * 0.5;
+    int nmb = (int)floor(-2.0 * ym - xm);
+    int npb = xm > 4.0 * (2.0 - SQRT_2) * ym ? (int)ceil(xm) : (int)ceil(2.0 * ym + xm * xm / (16.0 * ym));
+    g->n = n;
+    g->len = npb - nmb + 200;
+    g->k_min = nmb - 100;
+    return g->len <= cap;
+}
+
+// Scaled sum of squares: value = scale * sqrt(ssq), overflow-safe.
+struct Ssq {
+    double scale, ssq;
+    __host__ __device__ __forceinline__ void add(double x) {
+        double ax = fabs(x);
+        if (ax == 0.0 || !(ax == ax)) {
+            if (!(ax == ax)) ssq = ax;
+            return;
+        }
+        if (ax > scale) {
+            double r = scale / ax;
+            ssq = 1.0 + ssq * r * r;
+            scale = ax;
+        } else {
+            double r = ax / scale;
+            ssq += r * r;
+        }
+    }
+    __host__ __device__ __forceinline__ double value() const { return scale * sqrt(ssq); }
+};
+
+// double_bessel.rs:142-246: J(n-2..n+2, x, y) by recurrence.  Returns false
+// on a workspace too small for n.
+__host__ __device__ __noinline__ bool db_around(const DbGeom& g, const DbWork& w, double x, double y, double j[5]) {
+    const int len = g.len;
+    double* W = w.base;
+#define DBW(e, c) W[((size_t)(e) * 5 + (c)) * 32]
+    // forward recurrence from the default element (all coefficients 1)
+    {
+        double p0 = 1.0, p1 = 1.0, p2 = 1.0, q0 = 1.0, q1 = 1.0;
+        for (int i = 1; i < len; ++i) {
+            int k = i + g.k_min;
+            double x0 = -x - 4.0 * y * y / p2;
+            double x1 = 2.0 * (double)(k - 1) - 2.0 * y * p0 / p2;
+            double x2 = -x - 2.0 * y * p1 / p2;
+            double l0 = x0 - 2.0 * y * x2 / q1;
+            double l1 = x1 - q0 * x2 / q1;
+            DBW(i, 0) = x0;
+            DBW(i, 1) = x1;
+            DBW(i, 2) = x2;
+            DBW(i, 3) = l0;
+            DBW(i, 4) = l1;
+            p0 = x0, p1 = x1, p2 = x2, q0 = l0, q1 = l1;
+        }
+    }
+    int n_minus = (int)floor(-2.0 * y - x);
+    int n_plus = (8.0 * y > x) ? (int)ceil(2.0 * y + x * x / (16.0 * y)) : (int)ceil(-2.0 * y + x);
+    int i_match = (n_plus + n_minus) / 2 - g.k_min;
+    int i_target = g.n - g.k_min;
+    if (i_match < 1 || i_match > len - 4 || i_target < 2 || i_target + 2 > len - 4) return false;
+    const double initial = g.n < 2000 ? 1.0e-100 : 1.0e-300;
+    // window: f[i+1], f[i+2], f[i+3]; g[i+1], g[i+2]
+    double f1 = 2.0 * initial, f2 = 1.0 * initial, f3 = 0.0;
+    double g2 = 1.0 / initial;
+    double g1 = -(2.0 * y * 0.0 + DBW(len - 2, 3) * g2) / DBW(len - 2, 4);
+    // sums over the f branch (orders >= i_match) and the g branch (< i_match)
+    double sum_f = f3 + f2 + f1, sum_g = 0.0;
+    Ssq sq_f{0.0, 1.0}, sq_g{0.0, 1.0};
+    sq_f.add(f3);
+    sq_f.add(f2);
+    sq_f.add(f1);
+    double g_match = 0.0, f_match = 0.0;
+    double tv[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // f or g at the five target orders
+    for (int i = len - 4; i >= 0; --i) {
+        double fi = -(2.0 * y * f3 + DBW(i + 2, 0) * f2 + DBW(i + 2, 1) * f1) / DBW(i + 2, 2);
+        double gi = -(2.0 * y * g2 + DBW(i + 1, 3) * g1) / DBW(i + 1, 4);
+        if (i >= i_match) {
+            sum_f += fi;
+            sq_f.add(fi);
+        } else {
+            sum_g += gi;
+            sq_g.add(gi);
+        }
+        if (i == i_match) {
+            g_match = gi;
+            f_match = fi;
+        }
+        int t = i - (i_target - 2);
+        if (t >= 0 && t < 5) tv[t] = i >= i_match ? fi : gi;
+        double gm_now = i > i_match ? 0.0 : g_match;
+        if (fi > 1.0 && fabs(gm_now) < 1.0e200) {
+            // every order >= i: f *= 1e-100, g *= 1e100
+            fi *= 1.0e-100, f1 *= 1.0e-100, f2 *= 1.0e-100;
+            gi *= 1.0e100, g1 *= 1.0e100;
+            sum_f *= 1.0e-100;
+            sq_f.scale *= 1.0e-100;
+            sum_g *= 1.0e100;
+            sq_g.scale *= 1.0e100;
+            if (i <= i_match) {
+                g_match *= 1.0e100;
+                f_match *= 1.0e-100;
+            }
+            for (int q = 0; q < 5; ++q) {
+                int e = i_target - 2 + q;
+                if (e >= i) tv[q] *= (e >= i_match) ? 1.0e-100 : 1.0e100;
+            }
+        }
+        f3 = f2, f2 = f1, f1 = fi;
+        g2 = g1, g1 = gi;
+    }
+#undef DBW
+    // g_match / f_match alone can overflow; sum_f / f_match and the f-branch
+    // norm over |f_match| stay near 1 (f peaks at the matching order)
+    double sum_linear = sum_g + g_match * (sum_f / f_match);
+    double rss = hypot(sq_g.value(), fabs(g_match) * (sq_f.value() / fabs(f_match)));
+    for (int q = 0; q < 5; ++q) {
+        int e = i_target - 2 + q;
+        double h = e < i_match ? tv[q] : g_match * tv[q] / f_match;
+        double r = h / sum_linear;
+        double sgn = r > 0.0 ? 1.0 : (r < 0.0 ? -1.0 : (signbit(r) ? -1.0 : 1.0));
+        double val = sgn * fabs(h) / rss;
+        j[q] = isfinite(val) ? val : 0.0;
+    }
+    return true;
+}
+
+// double_bessel.rs:272-355: saddle-point approximation for large order.
+__host__ __device__ __noinline__ double db_spa(int ni, double x, double y) {
+    double n = ni;
+    if (n <= -2.0 * y + x) {
+        double ct = y > 0.0 ? x / (8.0 * y) - sqrt(x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y)) : n / x;
+        double th = acos(ct);
+        double f = x * sin(th) - y * sin(2.0 * th);
+        double d2f = -x * sin(th) + 4.0 * y * sin(2.0 * th);
+        double phi = (PI / 4.0) * (d2f > 0.0 ? 1.0 : (d2f < 0.0 ? -1.0 : (signbit(d2f) ? -1.0 : 1.0)));
+        return cos(f - n * th + phi) * sqrt(2.0 / (PI * fabs(d2f)));
+    } else if (8.0 * y < x || n > 2.0 * y + x * x / (16.0 * y)) {
+        double disc = x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y);
+        cxd ct;
+        if (isnan(disc))
+            ct = cxd{n / x, 0.0};
+        else if (disc < 0.0)
+            ct = cxd{x / (8.0 * y), sqrt(-disc)};
+        else
+            ct = cxd{x / (8.0 * y) - sqrt(disc), 0.0};
+        const cxd I{0.0, 1.0};
+        cxd th = cx_acos(ct);
+        cxd s1 = cx_sin(th), s2 = cx_sin(cx_scale(2.0, th));
+        cxd f = cx_mul(I, cx_sub(cx_add(cx_scale(-n, th), cx_scale(x, s1)), cx_scale(y, s2)));
+        cxd d2f = cx_mul(I, cx_add(cx_scale(-x, s1), cx_scale(4.0 * y, s2)));
+        cxd phase = cx_add(f, cxd{0.0, (PI - cx_arg(d2f)) / 2.0});
+        double term;
+        if (f.im == 0.0 && d2f.im == 0.0)
+            term = 0.5 * exp(-f.re) * sqrt(2.0 / (PI * cx_norm(d2f)));
+        else
+            term = cx_exp(phase).re * sqrt(2.0 / (PI * cx_norm(d2f)));
+        return disc != 0.0 ? term : 0.0;
+    } else {
+        double r = sqrt(x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y));
+        double out = 0.0;
+        for (int b = 0; b < 2; ++b) {
+            double ct = x / (8.0 * y) + (b == 0 ? -r : r);
+            double th = acos(ct);
+            double f = x * sin(th) - y * sin(2.0 * th);
+            double d2f = -x * sin(th) + 4.0 * y * sin(2.0 * th);
+            double phi = (PI / 4.0) * (d2f > 0.0 ? 1.0 : (d2f < 0.0 ? -1.0 : (signbit(d2f) ? -1.0 : 1.0)));
+            out += cos(f - n * th + phi) * sqrt(2.0 / (PI * fabs(d2f)));
+        }
+        return out;
+    }
+}
+
+// double_bessel.rs:386-410
+__host__ __device__ __forceinline__ bool db_evaluate(const DbGeom& g, const DbWork& w, double x, double y, double j[5]) {
+    if (g.n > 10) {
+        double ne = g.n * (1.0 - sqrt(10.0 / g.n));
+        double xc = y > ne / 6.0 ? 4.0 * sqrt(y * (ne - 2.0 * y)) : ne + 2.0 * y;
+        if (x < xc) {
+            for (int q = 0; q < 5; ++q) j[q] = db_spa(g.n - 2 + q, x, y);
+            return true;
+        }
+    }
+    return db_around(g, w, x, y, j);
+}
+
+// ------------------------------------------------------ LP emission -----
+// nonlinear_compton/lp/mod.rs:21-50.  Returns NaN on a workspace failure.
+__device__ __noinline__ double lp_ddpr(double a, double eta, double s, double theta, const DbGeom& g, const DbWork& w) {
+    int n = g.n;
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double wn = fmin(s / (sn * (1.0 - s)), 1.0);
+    double alpha = 2.0 * n * a * cos(theta) * sqrt(wn * (1.0 - wn)) / sqrt(1.0 + 0.5 * a * a);
+    double beta = a * a * s / (8.0 * eta * (1.0 - s));
+    double j[5];
+    if (!db_evaluate(g, w, alpha, beta, j)) return NAN;
+    double g0, g1, g2;
+    if (n % 2 == 0) {
+        g0 = j[2], g1 = -0.5 * (j[1] + j[3]), g2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        g0 = -j[2], g1 = 0.5 * (j[1] + j[3]), g2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    return (-g0 * g0 - a * a * (1.0 + 0.5 * s * s / (1.0 - s)) * (g0 * g2 - g1 * g1)) / (2.0 * PI);
+}
+
+// f64::max, which ignores a NaN operand
+__device__ __forceinline__ double rmax(double a, double b) { return isnan(a) ? b : (isnan(b) ? a : fmax(a, b)); }
+
+// nonlinear_compton/lp/mod.rs:338-344
+__device__ __forceinline__ int lp_sum_limit(double a, double eta) {
+    double m = 3.0 - 0.4 * pow(eta, 0.25);
+    return (int)ceil(6.0 * (1.0 + a * a) + 2.0 * pow(a, m));
+}
+
+// nonlinear_compton/lp/mod.rs:53-140
+__device__ __noinline__ double lp_ceiling(double a, double eta, const DbGeom& g, const DbWork& w) {
+    int n = g.n;
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    double mx = NAN;
+    double theta = 0.0, x0 = 0.0, x1 = 1.0;  // s = smax * (x0 + (x1 - x0) i / cnt), i = i0..cnt
+    int i0 = 1, cnt = 32;
+    if (n == 1) {
+        mx = rmax(lp_ddpr(a, eta, 0.01 * smax, PI / 2.0, g, w), lp_ddpr(a, eta, 0.99 * smax, PI / 2.0, g, w));
+        return 1.15 * mx;
+    } else if (a <= 2.0) {
+        x0 = 0.4;
+    } else if (a <= 5.0) {
+        int n_switch = (int)ceil(1.3 * pow(a, 1.2));
+        if (n < n_switch) {
+            theta = (PI / 2.0) * (1.0 - log((double)n) / log((double)n_switch));
+            i0 = 0, x0 = 0.0;
+        } else {
+            x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.4);
+            cnt = n < lp_sum_limit(a, eta) / 2 ? 32 : 64;
+        }
+    } else {
+        int n_switch = (int)ceil(a * a);
+        if (n < n_switch) {
+            double ns = n_switch;
+            theta = (PI / 2.0) * (pow((double)n, -0.7) - pow(ns, -0.7)) / (1.0 - pow(ns, -0.7));
+            x0 = 0.3, cnt = 64;
+        } else {
+            x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.3);
+            x1 = (1.0 + sn) / (2.0 + sn);
+            cnt = n > 10 * n_switch ? 64 : (n > 3 * n_switch ? 42 : 32);
+        }
+    }
+    for (int i = i0; i <= cnt; ++i) {
+        double s;
+        if (a <= 2.0)
+            s = smax * (0.4 + 0.6 * (double)i / 32.0);
+        else if (a > 5.0 && n < (int)ceil(a * a))
+            s = smax * (0.3 + 0.7 * (double)i / 64.0);
+        else if (i0 == 0)
+            s = smax * (double)i / 32.0;
+        else
+            s = smax * (x0 + (x1 - x0) * (double)i / (double)cnt);
+        mx = rmax(mx, lp_ddpr(a, eta, s, theta, g, w));
+    }
+    return 1.15 * mx;
+}
+
+// nonlinear_compton/lp/mod.rs:142-302
+struct ThetaBound {
+    double s[16], f[16];
+    __device__ __forceinline__ double at(double arg) const {
+        double val = f[15];
+        for (int i = 1; i < 16; ++i) {
+            if (arg > s[i]) {
+                double wt = (arg - s[i - 1]) / (s[i] - s[i - 1]);
+                val = wt * f[i] + (1.0 - wt) * f[i - 1];
+                break;
+            }
+        }
+        return fmin(val, PI / 2.0);
+    }
+};
+
+__device__ __noinline__ double ln_double_bessel_x_zero(int ni, double y) {
+    double n = ni;
+    double z = sqrt(n / (4.0 * y) - 0.5);
+    const cxd I{0.0, 1.0};
+    cxd theta{PI / 2.0, log(sqrt(1.0 + z * z) - z)};
+    cxd s2 = cx_sin(cx_scale(2.0, theta));
+    cxd f = cx_mul(I, cx_sub(cx_scale(-n, theta), cx_scale(y, s2)));
+    cxd f2 = cx_mul(I, cx_scale(4.0 * y, s2));
+    double e = 0.5 * (PI - cx_arg(f2));
+    cxd phase = cx_add(f, cx_mul(I, cxd{e, 0.0}));
+    return log(sqrt(2.0 / (PI * cx_norm(f2)))) + phase.re + log(fabs(cos(phase.im)));
+}
+
+__device__ __noinline__ void theta_bound(int n, double a, double eta, ThetaBound* tb) {
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    for (int i = 0; i < 16; ++i) {
+        double z = cos(PI * i / 15.0);
+        double si = 0.5 * (z + 1.0) * sn / (1.0 + sn);
+        tb->s[i] = si;
+        double wn = fmin(si / (sn * (1.0 - si)), 1.0);
+        double x = 2.0 * n * a * sqrt(wn * (1.0 - wn)) / sqrt(1.0 + 0.5 * a * a);
+        double y = a * a * si / (8.0 * eta * (1.0 - si));
+        double x_crit = y > n / 6.0 ? 4.0 * sqrt(y) * sqrt(n - 2.0 * y) : n + 2.0 * y;
+        double ln_j_crit = log(0.443) - log((double)n) / 3.0;
+        double ln_j_bdy = ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y);
+        ln_j_bdy = fmin(ln_j_bdy, ln_j_crit);
+        double ct = 1.0 - x_crit * log(0.01) / (x * (ln_j_bdy - ln_j_crit));
+        ct = fmax(ct, -1.0);
+        double fi = acos(ct);
+        tb->f[i] = isnan(fi) ? PI : fi;
+    }
+    double f_min = tb->f[0];
+    for (int i = 1; i < 16; ++i) {
+        if (tb->f[i] < f_min)
+            f_min = tb->f[i];
+        else
+            tb->f[i] = f_min;
+    }
+}
+
+// nonlinear_compton/lp/linear.rs
+__device__ __forceinline__ double lp_linear_rate(double a, double eta) {
+    double eta2 = eta * eta, eta3 = eta2 * eta;
+    if (eta > 1.0e-3)
+        return (a * a / 8.0) * (0.5 + 4.0 / eta - 0.5 / ((1.0 + 2.0 * eta) * (1.0 + 2.0 * eta)) +
+                                (1.0 - 2.0 / eta - 2.0 / eta2) * log(1.0 + 2.0 * eta));
+    return (a * a / 8.0) * (8.0 * eta / 3.0 - 16.0 * eta2 / 3.0 + 208.0 * eta3 / 15.0);
+}
+
+// nonlinear_compton/lp/classical.rs:189-210
+__device__ __forceinline__ bool lp_classical_rate(const NlcTables& t, double a, double eta, double* out) {
+    double x = log(a);
+    if (x < PTG_NLC_CL_MIN) {
+        *out = a * a * eta / 3.0;
+        return true;
+    }
+    int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    if (ix >= 60) return false;
+    double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    *out = eta * exp((1.0 - dx) * t.lp_cl_rate[ix] + dx * t.lp_cl_rate[ix + 1]);
+    return true;
+}
+
+// nonlinear_compton/lp/mod.rs:414-457
+__device__ __forceinline__ bool lp_rate(const NlcTables& t, double a, double eta, double* out) {
+    const double MIN0 = PTG_NLC_LP_MIN_0, MIN1 = PTG_NLC_LP_MIN_1, S0 = PTG_NLC_LP_STEP_0, S1 = PTG_NLC_LP_STEP_1;
+    const double* T = t.lp_rate;
+    double x = log(a), y = log(eta);
+    if (x < MIN0) {
+        *out = lp_linear_rate(a, eta);
+        return true;
+    }
+    int ix = (int)((x - MIN0) / S0);
+    double dx = (x - MIN0) / S0 - ix;
+    if (ix >= 60) return false;
+    if (y < MIN1) {
+        *out = exp((1.0 - dx) * T[ix] + dx * T[ix + 1] - MIN1) * eta;
+        return true;
+    }
+    int iy = (int)((y - MIN1) / S1);
+    if (iy >= 67) return false;
+    double dy = (y - MIN1) / S1 - iy;
+    double f = (1.0 - dx) * (1.0 - dy) * T[iy * 61 + ix] + dx * (1.0 - dy) * T[iy * 61 + ix + 1] +
+               (1.0 - dx) * dy * T[(iy + 1) * 61 + ix] + dx * dy * T[(iy + 1) * 61 + ix + 1];
+    *out = exp(f);
+    return true;
+}
+
+// nonlinear_compton/lp/mod.rs:459-553: one grid corner of the harmonic CDF
+// (16 nodes of [n, cdf]); NaN where the reference's inversion would fail.
+__device__ __noinline__ double lp_cdf_corner(const double* table, double frac, double a) {
+    if (frac <= table[1]) return 0.9;
+    double v = 0.0;
+    if (a < 5.0) return pw_invert(table, 16, false, frac, &v) ? v : NAN;
+    double rs[30];
+    for (int i = 0; i < 15; ++i) {
+        rs[2 * i] = log(table[2 * i]);
+        rs[2 * i + 1] = log(-1.0 * log(1.0 - table[2 * i + 1]));
+    }
+    pw_invert(rs, 15, true, log(-1.0 * log(1.0 - frac)), &v);
+    return exp(v);
+}
+
+// Returns the harmonic order, or -1 if the lookup failed.
+__device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double a, double eta, double frac) {
+    const double MIN0 = PTG_NLC_LP_CDF_MIN_0, MIN1 = PTG_NLC_LP_CDF_MIN_1, S0 = PTG_NLC_LP_CDF_STEP_0,
+                 S1 = PTG_NLC_LP_CDF_STEP_1;
+    const double* T = t.lp_cdf;
+    double la = log(a), le = log(eta);
+    if (la <= MIN0) return 1;
+    int ix = (int)((la - MIN0) / S0);
+    double dx = (la - MIN0) / S0 - ix;
+    if (ix >= 60) return -1;
+    double n;
+    if (le <= MIN1) {
+        n = lp_cdf_corner(T + (size_t)ix * 32, frac, a) * (1.0 - dx) +
+            lp_cdf_corner(T + (size_t)(ix + 1) * 32, frac, a) * dx;
+    } else {
+        int iy = (int)((le - MIN1) / S1);
+        if ((size_t)(61 * (iy + 1) + ix + 1) >= 4148) return -1;
+        double dy = (le - MIN1) / S1 - iy;
+        n = lp_cdf_corner(T + (size_t)(61 * iy + ix) * 32, frac, a) * ((1.0 - dx) * (1.0 - dy)) +
+            lp_cdf_corner(T + (size_t)(61 * iy + ix + 1) * 32, frac, a) * (dx * (1.0 - dy)) +
+            lp_cdf_corner(T + (size_t)(61 * (iy + 1) + ix) * 32, frac, a) * ((1.0 - dx) * dy) +
+            lp_cdf_corner(T + (size_t)(61 * (iy + 1) + ix + 1) * 32, frac, a) * (dx * dy);
+    }
+    return isfinite(n) ? (int)ceil(n) : -1;
+}
+
+// nonlinear_compton/lp/mod.rs:586-676: harmonic, s, azimuth theta in
+// [0, 2 pi) and the Stokes vector (in the LMA basis) of the emitted photon.
+// Returns a ptg status.
+__device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w, double a, double eta, Draws& rng,
+                                      int* n_out, double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
+    if (t.lp_cdf == nullptr || w.base == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = lp_harmonic_index(t, a, eta, rng.next());
+    if (n < 1) return 2;  // PTG_ERR_OUT_OF_TABLE
+    DbGeom g;
+    if (!db_geom(n, w.cap, &g)) return 9;  // PTG_ERR_UNSUPPORTED: order beyond the workspace
+    ThetaBound tb;
+    theta_bound(n, a, eta, &tb);
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    double mx = lp_ceiling(a, eta, g, w);
+    double s = 0.0, theta = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double ss = smax * rng.next();
+        double th = (PI / 2.0) * rng.next();
+        if (th > tb.at(ss)) continue;
+        double z = mx * rng.next();
+        if (z < lp_ddpr(a, eta, ss, th, g, w)) {
+            s = ss, theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;  // PTG_ERR_REJECTION_CAP
+    int quadrant = (int)(4.0 * rng.next());
+    if (quadrant == 1)
+        theta = PI - theta;
+    else if (quadrant == 2)
+        theta = PI + theta;
+    else if (quadrant == 3)
+        theta = 2.0 * PI - theta;
+    double wn = fmin(s / (sn * (1.0 - s)), 1.0);
+    double x = -2.0 * n * a * cos(theta) * sqrt(wn * (1.0 - wn)) / sqrt(1.0 + 0.5 * a * a);
+    double y = a * a * s / (8.0 * eta * (1.0 - s));
+    double j[5];
+    if (!db_evaluate(g, w, fabs(x), y, j)) return 9;
+    double A0, A1, A2;
+    if (x > 0.0) {
+        A0 = j[2], A1 = 0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else if (n % 2 == 0) {
+        A0 = j[2], A1 = -0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        A0 = -j[2], A1 = 0.5 * (j[1] + j[3]), A2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    double u = sqrt(2.0 * n * eta * (1.0 - s) / s - (1.0 + 0.5 * a * a));
+    double st = sin(theta);
+    double xi0 = (1.0 - s + 1.0 / (1.0 - s)) * (A1 * A1 - A0 * A2) - 2.0 * (A0 / a) * (A0 / a);
+    double xi1 = 2.0 * (A1 * A1 - A0 * A2) - 2.0 * (1.0 + 2.0 * u * u * st * st) * (A0 / a) * (A0 / a);
+    double xi2 = -1.0 * (2.0 * (u * A0 / a) * (u * A0 / a) * sin(2.0 * theta) + 4.0 * u * A0 * A1 * st / a);
+    *sv_out = mk3(xi1 / xi0, xi2 / xi0, 0.0);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return 0;
+}
+
+// Orders a DoubleBessel workspace must hold for harmonics up to n.
+__host__ __device__ inline int db_len_for(int n) {
+    double xm = n * 1.4142135623730951, ym = n * 0.5;
+    int nmb = (int)floor(-2.0 * ym - xm);
+    int npb = xm > 4.0 * (2.0 - 1.4142135623730951) * ym ? (int)ceil(xm) : (int)ceil(2.0 * ym + xm * xm / (16.0 * ym));
+    return npb - nmb + 200;
+}
+
+}  // namespace ptg

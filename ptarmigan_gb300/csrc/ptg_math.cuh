@@ -22,6 +22,7 @@ constexpr double PI = 3.14159265358979323846;
 constexpr double FRAC_PI_3 = 1.04719755119659774615;
 constexpr double LN_2 = 0.693147180559945309417;
 constexpr double SQRT_3 = 1.73205080756887729353;
+constexpr double SQRT_2 = 1.41421356237309504880;
 
 // Cap on every rejection loop: the reference's loops are unbounded; here a
 // particle that exceeds the cap is retired with PTG_ERR_REJECTION_CAP.

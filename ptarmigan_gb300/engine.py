@@ -21,7 +21,7 @@ _EXPORTS = [
     "ptg_abi_version", "ptg_status_string", "ptg_last_error", "ptg_context_create", "ptg_context_destroy",
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_eval_fields", "ptg_push_steps",
-    "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t",
+    "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
 ]
 
 
@@ -77,6 +77,11 @@ def load(path=None):
     L.ptg_lcfa_photon_sample.argtypes = [ctxp, C.c_size_t, DP, DP, DP, DP, DP]
     L.ptg_lcfa_pair_t.restype = st
     L.ptg_lcfa_pair_t.argtypes = [ctxp, C.c_size_t, DP, DP, DP]
+    L.ptg_double_bessel.restype = st
+    L.ptg_double_bessel.argtypes = [ctxp, C.c_int32, C.c_size_t, DP, DP, C.c_int32, DP]
+    L.ptg_lp_sample.restype = st
+    L.ptg_lp_sample.argtypes = [ctxp, C.c_size_t, DP, DP, C.c_uint64, C.POINTER(C.c_uint64), C.c_uint32, DP,
+                                C.POINTER(C.c_int32)]
     _lib = L
     return L
 
@@ -197,6 +202,24 @@ class Engine:
         self._check(self.L.ptg_lcfa_photon_sample(self._h, len(chi), _dp(chi), _dp(gamma), _dp(rand3), _dp(om),
                                                   _dp(th)))
         return om, th
+
+    def double_bessel(self, n, x, y, mode=0):
+        """J(n-2..n+2, x, y) per point, shape [m, 5]."""
+        x, y = _f64(x, (-1,)), _f64(y, (-1,))
+        out = np.zeros((len(x), 5))
+        self._check(self.L.ptg_double_bessel(self._h, n, len(x), _dp(x), _dp(y), mode, _dp(out)))
+        return out
+
+    def lp_sample(self, a, eta, seed, streams, step):
+        """LP LMA samples: ([m, 7] = n, s, theta, 1, xi1, xi2, xi3; [m] status)."""
+        a, eta = _f64(a, (-1,)), _f64(eta, (-1,))
+        streams = np.ascontiguousarray(streams, dtype=np.uint64)
+        out = np.zeros((len(a), 7))
+        status = np.zeros(len(a), dtype=np.int32)
+        self._check(self.L.ptg_lp_sample(self._h, len(a), _dp(a), _dp(eta), seed,
+                                         streams.ctypes.data_as(C.POINTER(C.c_uint64)), step, _dp(out),
+                                         status.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out, status
 
     def lcfa_pair_t(self, chi):
         chi = _f64(chi, (-1,))

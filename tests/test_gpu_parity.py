@@ -220,3 +220,186 @@ def test_collide_options_filters(eng, orc):
     assert len(gout["species"]) == pytest.approx(len(oout["species"]), abs=2)
     e = 0.510999 * gout["u"][:, 0]
     assert np.all(e > 50.0)
+
+
+# LMA emission builds the photon in the zero-momentum frame of q + n k, whose
+# four-velocity comes from (q + n k)^2 ~ 1 + a^2 + 2 n eta, a difference of
+# squares of size gamma^2: one ulp of the electron's momentum moves the
+# photon by up to ~gamma^2 / (1 + a^2) ulp (1.5e-8 relative at gamma = 2e4,
+# a = 2, measured on the oracle).  LMA showers are compared at 5e-7.
+LMA_TOL = 5e-7
+
+
+def _compare_showers(gout, oout, tol=1e-8, frac_bad=0.02):
+    common, ia, ib = _match_by_stream(gout, oout)
+    n_ref = len(oout["species"])
+    assert len(common) >= 0.97 * n_ref, (len(common), n_ref, len(gout["species"]))
+    bad = 0
+    for s in common:
+        i, j = ia[s], ib[s]
+        assert gout["species"][i] == oout["species"][j]
+        scale = np.linalg.norm(oout["u"][j])
+        if np.max(np.abs(gout["u"][i] - oout["u"][j])) > tol * scale:
+            bad += 1
+    assert bad <= max(1, frac_bad * len(common)), (bad, len(common))
+    return len(common)
+
+
+@pytest.mark.parametrize("pol_resolved", [0, 1])
+def test_lma_cp_focused_emission_matches_oracle(eng, orc, pol_resolved):
+    """FocusedLaser, circular polarisation: LMA emission (CP harmonic
+    sampler with the regenerated CDF) and the secondaries' pair creation."""
+    if not orc.has_cp_cdf():
+        pytest.skip("CP CDF table missing")
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(60, g, sigma=0.001 * g, radius=1e-6, length=2e-6, rms_div=8e-6, laser=laser, seed=5)
+    opts = abi.collide_options(pol_resolved=pol_resolved, rate_increase=30.0)
+    gout, gst = eng.collide(laser, opts, prim, seed=17)
+    oout, ost = orc.collide(laser, opts, prim, seed=17, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["emissions"] > 40
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)
+
+
+@pytest.mark.parametrize("pol_resolved", [0, 1])
+def test_lma_cp_focused_pairs_match_oracle(eng, orc, pol_resolved):
+    """Photon beam on a CP focused laser: CP Breit-Wheeler probability
+    (lookup and explicit harmonic summation), Stokes update and positron
+    sampler."""
+    if not orc.has_cp_cdf():
+        pytest.skip("CP CDF table missing")
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(120, g, sigma=0.001 * g, radius=1e-6, length=2e-6, rms_div=8e-6, laser=laser, seed=9,
+                      species=abi.PHOTON, stokes=(0.3, 0.0, 0.5))
+    opts = abi.collide_options(pol_resolved=pol_resolved, rate_increase=100.0)
+    gout, gst = eng.collide(laser, opts, prim, seed=23)
+    oout, ost = orc.collide(laser, opts, prim, seed=23, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["pair_events"] >= 10
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["pair_events"] == pytest.approx(ost["pair_events"], rel=0.05, abs=2)
+    # photons that did not decay: their Stokes vectors and interaction counts
+    common, ia, ib = _match_by_stream(gout, oout)
+    for s_ in common:
+        i, j = ia[s_], ib[s_]
+        if oout["species"][j] == abi.PHOTON and oout["generation"][j] == 0:
+            assert np.max(np.abs(gout["pol"][i] - oout["pol"][j])) < 1e-9
+            assert abs(gout["interaction_count"][i] - oout["interaction_count"][j]) <= 1e-9 * max(
+                1e-12, abs(oout["interaction_count"][j]))
+
+
+def test_lma_cp_plane_wave_collide_matches_oracle(eng, orc):
+    if not orc.has_cp_cdf():
+        pytest.skip("CP CDF table missing")
+    laser = abi.laser_desc(abi.PLANE_WAVE, 2.0, 0.8e-6, abi.CIRCULAR, abi.COS2, n_cycles=8.0)
+    g = beam.gamma_from_energy(10.0)
+    prim = beam.build(24, g, sigma=0.001 * g, radius=0.0, length=2e-6, rms_div=0.0, laser=laser, seed=6)
+    opts = abi.collide_options(rate_increase=1000.0)
+    gout, gst = eng.collide(laser, opts, prim, seed=3)
+    oout, ost = orc.collide(laser, opts, prim, seed=3, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    _compare_showers(gout, oout, tol=LMA_TOL)
+
+
+# ---------------------------------------------- linear polarisation, LMA --
+from kat_double_bessel import DB_KAT, DB_KAT_ABS, db_err  # noqa: E402
+
+
+def test_double_bessel_device_kats(eng, orc):
+    """Device J(n, x, y) by recurrence against the reference's known answers
+    (double_bessel.rs:417-596, 1e-9) and the oracle (1e-11)."""
+    pts = {}
+    for n, fx, fy, t in DB_KAT:
+        pts.setdefault(n, []).append((fx * n * math.sqrt(2.0), fy * 0.5 * n, t))
+    for n, x, y, t in DB_KAT_ABS:
+        pts.setdefault(n, []).append((x, y, t))
+    for n, p in pts.items():
+        x = np.array([q[0] for q in p])
+        y = np.array([q[1] for q in p])
+        j = eng.double_bessel(n, x, y, mode=0)
+        for k, (xx, yy, t) in enumerate(p):
+            assert db_err(j[k, 2], t) < 1e-9, (n, xx, yy, j[k, 2], t)
+            ref = orc.double_bessel_at(n, n * math.sqrt(2.0), 0.5 * n, xx, yy)
+            assert abs(j[k, 2] - ref) <= 1e-10 * abs(ref), (n, xx, yy, j[k, 2], ref)
+
+
+@pytest.mark.parametrize("n", [12, 100, 700])
+def test_double_bessel_device_evaluate(eng, orc, n):
+    """The rate evaluation's J (saddle point where it applies) against the
+    oracle over the whole (x, y) domain of order n: relative 1e-10, with an
+    absolute floor of 1e-14 for the saddle-point form, whose cosine of an
+    O(n) phase turns last-bit differences of the device's sin/cos into
+    absolute errors near the zeros of J."""
+    rng = np.random.default_rng(n)
+    x = n * math.sqrt(2.0) * rng.random(200)
+    y = 0.5 * n * rng.random(200)
+    j = eng.double_bessel(n, x, y, mode=1)
+    for k in range(200):
+        ref = orc.double_bessel_evaluate(n, x[k], y[k])
+        assert abs(j[k, 2] - ref) <= 1e-10 * abs(ref) + 1e-14, (x[k], y[k], j[k, 2], ref)
+
+
+def test_lp_sampler_matches_oracle(eng, orc):
+    """LP harmonic (CDF table), (s, theta) by rejection under the ceiling,
+    and Stokes parameters: same streams, same samples."""
+    a_vals = [0.3, 0.8, 1.414, 2.5, 4.0, 6.0]
+    eta_vals = [2e-3, 0.03, 0.3]
+    a, eta, streams = [], [], []
+    for ai in a_vals:
+        for ei in eta_vals:
+            for k in range(24):
+                a.append(ai)
+                eta.append(ei)
+                streams.append(1000 * len(a) + k)
+    a, eta = np.array(a), np.array(eta)
+    streams = np.array(streams, dtype=np.uint64)
+    out, status = eng.lp_sample(a, eta, 99, streams, 7)
+    mism = 0
+    for i in range(len(a)):
+        rc, ref = orc.lp_sample(a[i], eta[i], 99, int(streams[i]), 7)
+        assert status[i] == rc
+        if out[i, 0] != ref[0]:
+            mism += 1
+            continue
+        assert abs(out[i, 1] - ref[1]) <= 1e-12 * ref[1]
+        if abs(out[i, 2] - ref[2]) > 1e-12 * max(ref[2], 1.0):
+            mism += 1
+            continue
+        assert np.max(np.abs(out[i, 4:6] - ref[4:6])) < 1e-9, (i, out[i], ref)
+    assert mism <= 0.01 * len(a)
+
+
+def test_lma_lp_plane_wave_matches_oracle(eng, orc):
+    """Linearly polarised plane wave (LMA), emission only, as in the
+    plane-wave benchmark: electrons at 5 GeV, a0 = 1."""
+    laser = abi.laser_desc(abi.PLANE_WAVE, 1.0, 0.8e-6, abi.LINEAR, abi.COS2, n_cycles=30.0)
+    g = beam.gamma_from_energy(5.0)
+    prim = beam.build(400, g, sigma=0.001 * g, radius=1e-6, length=10e-6, rms_div=0.0, laser=laser, seed=4)
+    opts = abi.collide_options(tracking_photons=0)
+    gout, gst = eng.collide(laser, opts, prim, seed=8)
+    oout, ost = orc.collide(laser, opts, prim, seed=8, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["emissions"] > 20
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)
+
+
+def test_lma_lp_focused_matches_oracle(eng, orc):
+    """Linearly polarised focused laser (LMA) at a0 = 3: harmonics beyond
+    the saddle-point threshold."""
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 3.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
+                           fwhm_duration=25e-15, pol_angle=0.3)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(40, g, sigma=0.001 * g, radius=1e-6, length=2e-6, rms_div=8e-6, laser=laser, seed=12)
+    opts = abi.collide_options(tracking_photons=0)
+    gout, gst = eng.collide(laser, opts, prim, seed=21)
+    oout, ost = orc.collide(laser, opts, prim, seed=21, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["emissions"] > 20
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)
