@@ -14,6 +14,22 @@ primaries resident in HBM; `e2e` times ptg_collide_batch (host buffers in
 and out, host<->device copies inside the timed region).  --impl reference
 times the CPU restatement of the reference's collision loop (the reference
 is Rust and no Rust toolchain is available) on all host cores.
+
+Other workloads (--workload), each one JSON line of the same metric:
+  plane_wave_lma  1e4 electrons at 5 GeV, 0.1% spread, 1 x 1 x 10 um, on a
+                  linearly polarised plane wave (LMA), a0 = 1, 0.8 um, cos^2
+                  envelope of 30 fs intensity FWHM (30.9 cycles), emission
+                  only.
+  a0_scan         64 collisions in one persistent queue launch: a0
+                  log-spaced 0.5..20, beams log-uniform 1e3..1e6 electrons
+                  (seeded) at 16.5 GeV, 0.1% spread, 2 x 2 x 20 um, 8 urad, on
+                  a circularly polarised focused Gaussian laser, w0 = 5 um,
+                  0.8 um, 25 fs; LMA below a0 = 5, LCFA above; pairs on.
+                  `plain_value` runs the same collisions one call each.
+  cp_shower       electrons at 16.5 GeV, 0.1% spread, 5 x 5 x 24 um, 8 urad,
+                  on a circularly polarised focused laser (LMA) a0 = 5, w0 =
+                  3 um, 0.8 um, 30 fs; Stokes parameters tracked, pairs on,
+                  all generations (--n primaries, default 1e6).
 """
 
 import argparse
@@ -170,6 +186,135 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def plane_wave_lma_workload(n, seed):
+    from ptarmigan_gb300 import abi, beam
+    # cos^2 envelope of total duration T: intensity FWHM = 0.364 T, so
+    # 30 fs FWHM is T = 82.4 fs = 30.9 cycles of 0.8 um light
+    laser = abi.laser_desc(abi.PLANE_WAVE, 1.0, 0.8e-6, abi.LINEAR, abi.COS2, n_cycles=30.9)
+    g = beam.gamma_from_energy(5.0)
+    prim = beam.build(n, g, sigma=0.001 * g, radius=1e-6, length=10e-6, rms_div=0.0, laser=laser, seed=seed)
+    opts = abi.collide_options(tracking_photons=0)
+    return laser, opts, prim
+
+
+def a0_scan_workload(seed, scale=1.0):
+    """64 collisions (laser, primaries) of the a0 scan; `scale` shrinks the
+    beams (for tests of the harness)."""
+    from ptarmigan_gb300 import abi, beam
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), 64))
+    colls, prims, first = [], [], 0
+    for k, a0 in enumerate(np.geomspace(0.5, 20.0, 64)):
+        model = abi.FOCUSED_LASER if a0 < 5.0 else abi.FAST_FOCUSED_LASER
+        laser = abi.laser_desc(model, float(a0), 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=5e-6, fwhm_duration=25e-15)
+        n = max(1, int(round(sizes[k] * scale)))
+        g = beam.gamma_from_energy(16.5)
+        p = beam.build(n, g, sigma=0.001 * g, radius=2e-6, length=20e-6, rms_div=8e-6, laser=laser,
+                       seed=int(seed * 1000 + k))
+        prims.append(p)
+        colls.append({"laser": laser, "seed": seed * 100 + k, "id_base": 1 << 40 | (k << 32), "first": first,
+                      "count": n})
+        first += n
+    prim = {key: np.concatenate([p[key] for p in prims]) for key in prims[0]}
+    return colls, abi.collide_options(), prim
+
+
+def cp_shower_workload(n, seed):
+    from ptarmigan_gb300 import abi, beam
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6, fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(n, g, sigma=0.001 * g, radius=5e-6, length=24e-6, rms_div=8e-6, laser=laser, seed=seed)
+    opts = abi.collide_options(pol_resolved=1, max_generation=-1)
+    return laser, opts, prim
+
+
+def run_extra(args):
+    """The non-default workloads: device time with CUDA events on the
+    engine's stream, inputs resident in HBM."""
+    import torch
+    from ptarmigan_gb300 import build, engine
+    build.build()
+    eng = engine.Engine(device=0)
+    stream = torch.cuda.ExternalStream(eng.stream_ptr, device=0)
+    dev = torch.device("cuda", 0)
+    sampler = ClockSampler(0)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        r = fn()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), r
+
+    line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic"}
+    if args.workload == "a0_scan":
+        colls, opts, prim = a0_scan_workload(1, scale=args.scale)
+        n = int(sum(c["count"] for c in colls))
+        d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+        tune, tune_ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=args.tune_fraction)
+        for _ in range(args.warmup):
+            eng.collide_multi_device(colls, opts, d_prim)
+        ms, stats = [], None
+        with sampler:
+            for _ in range(args.steps):
+                t, r = timed(lambda: eng.collide_multi_device(colls, opts, d_prim))
+                ms.append(t)
+                stats = r[3]
+        # the same collisions through the single-collision entry point
+        plain_ms = 0.0
+        for c in colls:
+            sub = {k: v[c["first"]:c["first"] + c["count"]] for k, v in d_prim.items()}
+            t, _ = timed(lambda: eng.collide_device(c["laser"], opts, sub, seed=c["seed"], id_base=c["id_base"]))
+            plain_ms += t
+        line.update({"value": n / (np.mean(ms) / 1e3), "ms_per_step": float(np.mean(ms)),
+                     "plain_value": n / (plain_ms / 1e3), "plain_ms": plain_ms,
+                     "config": {"workload": "a0_scan: 64 collisions, a0 0.5..20 log, beams log-uniform 1e3..1e6 "
+                                            "e- x%g, 16.5 GeV, CP focused w0=5 um 25 fs, LMA a0<5 / LCFA a0>=5, "
+                                            "pairs on, one persistent queue launch (graph)" % args.scale,
+                                "n_primaries": n, "autotuned": tune, "autotune_sample_ms": tune_ms,
+                                "events_per_step": {k: stats[k] for k in ("lepton_steps", "photon_steps",
+                                                                          "emissions", "pair_events", "n_created",
+                                                                          "n_out", "particle_errors")}},
+                     "gpu_launches": 7 * args.steps})
+    else:
+        if args.workload == "plane_wave_lma":
+            laser, opts, prim = plane_wave_lma_workload(args.n or 10_000, 1)
+            desc = "plane_wave_lma: 1e4 e- 5 GeV 0.1%, LP PlaneWave (LMA) a0=1 cos2 30.9 cycles, emission only"
+        else:
+            laser, opts, prim = cp_shower_workload(args.n or 1_000_000, 1)
+            desc = ("cp_shower: e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 30 fs; "
+                    "Stokes tracked, pairs on, all generations")
+        n = len(prim["species"])
+        d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+        for w in range(args.warmup):
+            eng.collide_device(laser, opts, d_prim, seed=100 + w)
+        ms, st = [], None
+        with sampler:
+            for k in range(args.steps):
+                t, r = timed(lambda: eng.collide_device(laser, opts, d_prim, seed=1000 + k))
+                ms.append(t)
+                st = r[1]
+        # the same batch through the persistent queue (one collision)
+        coll = [{"laser": laser, "seed": 1000, "id_base": n, "first": 0, "count": n}]
+        eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
+        eng.collide_multi_device(coll, opts, d_prim)
+        tq, rq = timed(lambda: eng.collide_multi_device(coll, opts, d_prim))
+        line.update({"value": n / (np.mean(ms) / 1e3), "ms_per_step": float(np.mean(ms)),
+                     "queue_value": n / (tq / 1e3),
+                     "config": {"workload": desc, "n_primaries": n,
+                                "events_per_step": {k: st[k] for k in ("lepton_steps", "photon_steps", "emissions",
+                                                                       "pair_events", "n_created", "n_out", "waves",
+                                                                       "particle_errors")}},
+                     "gpu_launches": int(sum([2 + st["waves"]]) * args.steps)})
+    line["clocks"] = sampler.summary()
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
 def nbytes(d):
     return int(sum(v.nbytes for v in d.values()))
 
@@ -183,7 +328,16 @@ def main():
     ap.add_argument("--n", type=int, default=N_PRIMARIES)
     ap.add_argument("--cpu-sample-per-core", type=int, default=1500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="lcfa_shower", choices=["lcfa_shower", "plane_wave_lma", "a0_scan",
+                                                                    "cp_shower"])
+    ap.add_argument("--scale", type=float, default=1.0, help="a0_scan: beam-size scale")
+    ap.add_argument("--tune-fraction", type=float, default=0.02, help="a0_scan: autotuner sample fraction")
     args = ap.parse_args()
+    if args.workload != "lcfa_shower" and args.impl == "gb300":
+        if args.n == N_PRIMARIES:
+            args.n = 0
+        run_extra(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

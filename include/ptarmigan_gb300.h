@@ -52,7 +52,8 @@ typedef enum {
     PTG_ERR_NO_DEVICE = 7,
     PTG_ERR_TABLES = 8,          /* table files missing or malformed */
     PTG_ERR_UNSUPPORTED = 9,     /* option combination not built yet */
-    PTG_ERR_ALLOC = 10
+    PTG_ERR_ALLOC = 10,
+    PTG_ERR_TIMEOUT = 11         /* a bounded wait in the queue kernel ran out */
 } ptg_status;
 
 /* src/main.rs:1042-1060 picks the field model from (focusing, lcfa). */
@@ -153,8 +154,8 @@ typedef struct ptg_ctx ptg_ctx;
 
 typedef struct {
     int32_t device;            /* CUDA ordinal */
-    int32_t block_size;        /* 0 = autotuned default */
-    int32_t blocks_per_sm;     /* 0 = autotuned default */
+    int32_t block_size;        /* 0 or 128: the collision kernels run 128 threads per block */
+    int32_t blocks_per_sm;     /* 0 = occupancy maximum */
     int32_t reserved;
     size_t initial_capacity;   /* 0 = library default (particles) */
 } ptg_device_cfg;
@@ -209,7 +210,7 @@ void ptg_particles_free(ptg_particles* p);
  * the default stream).  It covers the LCFA field models (FastPlaneWave,
  * FastFocusedLaser); other models return PTG_ERR_UNSUPPORTED.
  *
- * Its working memory is one static device array of about 8.6 MB inside the
+ * Its working memory is one static device array of about 8.9 MB inside the
  * library, which every GPU that loads the library holds until the process
  * exits.  Limits: at most 4096 primaries per call (more is
  * PTG_ERR_INVALID_ARGUMENT) and at most 32768 particles in a batch's
@@ -226,6 +227,62 @@ void ptg_particles_free(ptg_particles* p);
 ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* opts,
                                      const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
                                      ptg_particles* d_out, size_t out_capacity, void* stream, ptg_run_stats* stats);
+
+/* ------------------------------------------------ multi-collision queue ---
+ * Many independent collisions in one persistent launch.  No reference
+ * counterpart as one call: the reference runs one collision per process
+ * (main.rs:134-289 over one beam and one laser); here each collision is
+ * what a reference run with that laser, seed and beam would compute, and
+ * the batch shares one shower store and one work queue on the GPU.  Each
+ * collision's primaries are rows [first, first + count) of the batch's
+ * primaries; its primary streams are primary_stream(id_base + i), as in
+ * ptg_collide_batch with the same id_base, so a collision's shower matches
+ * the single-collision call particle for particle (same seed).  The step
+ * options are shared. */
+typedef struct {
+    ptg_laser_desc laser;
+    uint64_t seed;
+    uint64_t id_base;
+    uint64_t first;
+    uint64_t count;
+} ptg_collision;
+
+/* Launch shape of the queue kernel. */
+typedef struct {
+    int32_t variant;        /* 0: registers as needed; 1: capped for 3 blocks of 128 threads per SM */
+    int32_t blocks_per_sm;  /* 0 = occupancy maximum of the variant */
+    int32_t chunk;          /* tickets (store slots) a lane takes per grab: 1..64 */
+    int32_t use_graph;      /* replay the batch as a captured CUDA graph */
+} ptg_queue_cfg;
+
+/* Host buffers in and out: `out` is allocated by the library (free with
+ * ptg_particles_free) and holds the collisions' outputs one after another;
+ * collision k's rows are [out_offsets[k], out_offsets[k + 1]).  `stats`
+ * ([n_coll], may be NULL) gets each collision's counts, `total` (may be
+ * NULL) their sums and the batch's device time. */
+ptg_status ptg_collide_multi(ptg_ctx* ctx, size_t n_coll, const ptg_collision* coll, const ptg_collide_options* opts,
+                             const ptg_particles* primaries, ptg_particles* out, uint64_t* out_offsets,
+                             ptg_run_stats* stats, ptg_run_stats* total);
+
+/* Device-resident variant: primaries are device buffers; `d_out` receives
+ * device pointers into the context's output buffers, valid until the
+ * context's next batch; out_offsets, stats and total are host memory. */
+ptg_status ptg_collide_multi_device(ptg_ctx* ctx, size_t n_coll, const ptg_collision* coll,
+                                    const ptg_collide_options* opts, const ptg_particles* d_primaries,
+                                    ptg_particles* d_out, uint64_t* out_offsets, ptg_run_stats* stats,
+                                    ptg_run_stats* total);
+
+/* Sets (or reads, with cfg_out) the queue kernel's launch shape. */
+ptg_status ptg_queue_config(ptg_ctx* ctx, const ptg_queue_cfg* cfg, ptg_queue_cfg* cfg_out);
+
+/* Autotuner: times the queue kernel over candidate launch shapes (variant,
+ * blocks per SM, chunk) on a sample of the batch (the first
+ * ceil(sample_fraction * count) primaries of each collision, device
+ * buffers), keeps the fastest in the context and returns it with its
+ * device time per sample batch. */
+ptg_status ptg_queue_autotune(ptg_ctx* ctx, size_t n_coll, const ptg_collision* coll,
+                              const ptg_collide_options* opts, const ptg_particles* d_primaries,
+                              double sample_fraction, ptg_queue_cfg* best, double* best_ms);
 
 /* Field::max_timestep (field/<model>.rs) for a laser, in seconds (or 1.0 where the
  * reference returns None), and Field::ideal_initial_z, in metres. */

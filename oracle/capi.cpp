@@ -275,6 +275,28 @@ int orc_lp_sample(double a, double eta, uint64_t seed, uint64_t stream, uint32_t
     return st;
 }
 
+void orc_lp_pair_rates(double a, double eta, double* out2) {
+    if (!lp_pair_rates(a, eta, out2)) out2[0] = out2[1] = NAN;
+}
+void orc_lp_pair_dd_rate(int n, double a, double eta, double s, double theta, double* out2) {
+    lp_pair_dd_rate(n, a, eta, s, theta, out2);
+}
+void orc_lp_pair_partial_rate(int n, double a, double eta, double* out2) { lp_pair_partial_rate(n, a, eta, out2); }
+void orc_lp_pair_by_summation(double a, double eta, double* cdf48) { lp_pair_by_summation(a, eta, cdf48); }
+int orc_lp_pair_sample(double a, double eta, double sv1, double sv2, uint64_t seed, uint64_t stream, uint32_t step,
+                       double* out3) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n = 0;
+    double s = 0.0, th = 0.0;
+    uint64_t rej = 0;
+    int st = lp_pair_sample(a, eta, sv1, sv2, rng, &n, &s, &th, &rej);
+    out3[0] = n, out3[1] = s, out3[2] = th;
+    return st;
+}
+
 struct OrcResult {
     std::vector<OracleParticle> parts;
     OracleStats stats;

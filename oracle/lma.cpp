@@ -1313,17 +1313,730 @@ static int cpp_sample(double a, double eta, double sv1, double sv2, double sv3, 
     return cpp_sample_s_theta(index, a, eta, sv1, sv2, sv3, rng, s, theta, rej);
 }
 
+
+// ------------------------------------------------ LP Breit-Wheeler ----
+// pair_creation/lp/**: rates from the shipped tables (main and mid-range),
+// harmonic index by CDF inversion, (s, theta) by rejection.
+
+// Rust's `as i32` on f64: saturating, NaN -> 0.
+static int rust_as_i32(double x) {
+    if (std::isnan(x)) return 0;
+    if (x >= 2147483647.0) return 2147483647;
+    if (x <= -2147483648.0) return (-2147483647 - 1);
+    return (int)x;
+}
+
+// pair_creation/lp/tables/pol_dep.rs: a pair (S_1 = +1, S_1 = -1)
+struct PolDep {
+    double par, perp;
+    double interp(double sv1) const { return 0.5 * ((par + perp) + sv1 * (par - perp)); }
+};
+static inline PolDep pd(const double* v) { return PolDep{v[0], v[1]}; }
+static inline PolDep operator+(PolDep a, PolDep b) { return PolDep{a.par + b.par, a.perp + b.perp}; }
+static inline PolDep operator-(PolDep a, PolDep b) { return PolDep{a.par - b.par, a.perp - b.perp}; }
+static inline PolDep operator*(double s, PolDep a) { return PolDep{s * a.par, s * a.perp}; }
+static inline PolDep operator*(PolDep a, double s) { return PolDep{a.par * s, a.perp * s}; }
+static inline PolDep operator*(PolDep a, PolDep b) { return PolDep{a.par * b.par, a.perp * b.perp}; }
+static inline PolDep operator/(PolDep a, PolDep b) { return PolDep{a.par / b.par, a.perp / b.perp}; }
+static inline PolDep pd_div(PolDep a, double s) { return a * (1.0 / s); }  // Div<f64>: times the reciprocal
+static inline PolDep pd_exp(PolDep a) { return PolDep{std::exp(a.par), std::exp(a.perp)}; }
+static inline PolDep pd_ln(PolDep a) { return PolDep{std::log(a.par), std::log(a.perp)}; }
+static inline PolDep pd_powf(PolDep a, PolDep m) { return PolDep{std::pow(a.par, m.par), std::pow(a.perp, m.perp)}; }
+
+// pair_creation/lp/mod.rs:345-370
+static void lpp_sum_limits(double a, double eta, int* n_min_out, int* n_max_out) {
+    double n_min = std::ceil(2.0 * (1.0 + 0.5 * a * a) / eta);
+    double range = a < 1.0 ? 2.0 + (2.0 + 20.0 * a * a) * std::exp(-std::sqrt(0.5 * eta))
+                           : 3.0 + 2.8 * std::pow(a, 8.0 / 3.0) / std::cbrt(eta) + 0.25 * a * a * a * std::sqrt(eta);
+    double test = 0.25 - (1.0 + 0.5 * a * a) / (2.0 * n_min * eta);
+    if (test <= 2.220446049250313e-16) {
+        *n_min_out = rust_as_i32(n_min) + 1;
+        *n_max_out = rust_as_i32(n_min + 1.0 + range);
+    } else {
+        *n_min_out = rust_as_i32(n_min);
+        *n_max_out = rust_as_i32(n_min + range);
+    }
+}
+
+// pair_creation/lp/mod.rs:371-374
+static bool lpp_is_negligible(double a, double eta) {
+    return std::log10(eta) < -1.0 - std::pow(std::log10(a) + 2.0, 2) / 4.5;
+}
+
+// pair_creation/lp/tables/mod.rs:19-58
+static bool lpp_main_contains(double a, double eta) {
+    return std::log(a) >= PTG_BW_LP_LN_MIN_A && a < 25.0 && std::log(eta) >= PTG_BW_LP_LN_MIN_ETA && eta < 2.0;
+}
+
+static bool lpp_main_interpolate(double a, double eta, double f[2]) {
+    const double* T = g_lma.bw_lp_total;  // [61][25][2]
+    const double LMA = PTG_BW_LP_LN_MIN_A, LME = PTG_BW_LP_LN_MIN_ETA, SA = PTG_BW_LP_LN_A_STEP, SE = PTG_BW_LP_LN_ETA_STEP;
+    int ia = (int)((std::log(a) - LMA) / SA);
+    int ie = (int)((std::log(eta) - LME) / SE);
+    if (ia < 0 || ie < 0 || ia >= 25 - 1 || ie >= 61 - 1) return false;
+    auto at = [&](int e, int c) { return pd(T + ((size_t)e * 25 + c) * 2); };
+    PolDep r;
+    if (a * eta > 2.0) {
+        double da = (std::log(a) - LMA) / SA - ia;
+        double de = (std::log(eta) - LME) / SE - ie;
+        r = (1.0 - da) * (1.0 - de) * at(ie, ia) + da * (1.0 - de) * at(ie, ia + 1) + (1.0 - da) * de * at(ie + 1, ia) +
+            da * de * at(ie + 1, ia + 1);
+    } else {
+        double a_min = std::exp(LMA + ia * SA), a_max = std::exp(LMA + (ia + 1) * SA);
+        double e_min = std::exp(LME + ie * SE), e_max = std::exp(LME + (ie + 1) * SE);
+        double da = ((a_min * a_max / a) - a_min) / (a_max - a_min);
+        double de = ((e_min * e_max / eta) - e_min) / (e_max - e_min);
+        r = at(ie, ia) * da * de + at(ie, ia + 1) * (1.0 - da) * de + at(ie + 1, ia) * da * (1.0 - de) +
+            at(ie + 1, ia + 1) * (1.0 - da) * (1.0 - de);
+    }
+    PolDep e = pd_exp(r);
+    f[0] = e.par, f[1] = e.perp;
+    return true;
+}
+
+// pair_creation/lp/tables/mid_range/mod.rs:9-98
+static bool lpp_mid_contains(double a, double eta) {
+    double ln_a = std::log(a);
+    double lep = std::log(eta / (1.0 + 0.5 * a * a));
+    return ln_a > PTG_BW_LPM_LN_MIN_A && a < 2.0 && lep > PTG_BW_LPM_LN_MIN_ETA_PRIME && lep < PTG_BW_LPM_LN_MAX_ETA_PRIME;
+}
+
+static PolDep lpp_mid_interp_eta_prime(double ep, int ia) {
+    const double* T = g_lma.bw_lp_mid_total;  // [157][36][2]
+    const double D = PTG_BW_LPM_ETA_PRIME_DENSITY;
+    int ie = rust_as_i32(D * (std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / ep - 1.0));
+    if (ie % (int)D == (int)D - 1) ie -= 1;
+    auto at = [&](int e) { return pd(T + ((size_t)e * 36 + ia) * 2); };
+    double l0 = 2.0 / (1.0 + (double)(ie + 2) / D), m0 = 2.0 / (1.0 + (double)(ie + 1) / D), u0 = 2.0 / (1.0 + (double)ie / D);
+    PolDep l1 = at(ie + 2), m1 = at(ie + 1), u1 = at(ie);
+    PolDep m = pd_div(pd_ln((u1 - l1) / (m1 - l1)), std::log((u0 - l0) / (m0 - l0)));
+    PolDep alpha = (m1 - l1) / pd_powf(PolDep{m0 - l0, m0 - l0}, m);
+    PolDep r = alpha * pd_powf(PolDep{ep - l0, ep - l0}, m) + l1;
+    if (!std::isfinite(r.par)) {
+        if (ep < m0) {
+            double w = (std::log(ep) - std::log(l0)) / (std::log(m0) - std::log(l0));
+            r.par = (1.0 - w) * l1.par + w * m1.par;
+        } else {
+            double w = (std::log(ep) - std::log(m0)) / (std::log(u0) - std::log(m0));
+            r.par = (1.0 - w) * m1.par + w * u1.par;
+        }
+    }
+    if (!std::isfinite(r.perp)) {
+        if (ep < m0) {
+            double w = (std::log(ep) - std::log(l0)) / (std::log(m0) - std::log(l0));
+            r.perp = (1.0 - w) * l1.perp + w * m1.perp;
+        } else {
+            double w = (std::log(ep) - std::log(m0)) / (std::log(u0) - std::log(m0));
+            r.perp = (1.0 - w) * m1.perp + w * u1.perp;
+        }
+    }
+    return r;
+}
+
+static void lpp_mid_interpolate(double a, double eta, double f[2]) {
+    const double LMA = PTG_BW_LPM_LN_MIN_A, SA = PTG_BW_LPM_LN_A_STEP;
+    int ia = rust_as_i32((std::log(a) - LMA) / SA);
+    double ep = eta / (1.0 + 0.5 * a * a);
+    PolDep r;
+    if (a < 0.5) {
+        double da = (std::log(a) - LMA) / SA - ia;
+        r = (1.0 - da) * lpp_mid_interp_eta_prime(ep, ia) + da * lpp_mid_interp_eta_prime(ep, ia + 1);
+    } else {
+        double a_min = std::exp(LMA + ia * SA), a_max = std::exp(LMA + (ia + 1) * SA);
+        double da = (a - a_min) / (a_max - a_min);
+        r = pd_div((1.0 - da) * a_min * lpp_mid_interp_eta_prime(ep, ia) + da * a_max * lpp_mid_interp_eta_prime(ep, ia + 1), a);
+    }
+    PolDep e = pd_exp(r);
+    f[0] = e.par, f[1] = e.perp;
+}
+
+// pair_creation/lp/mod.rs:380-420: [f_par, f_perp]; false outside every table
+bool lp_pair_rates(double a, double eta, double f[2]) {
+    f[0] = f[1] = 0.0;
+    if (lpp_is_negligible(a, eta)) return true;
+    if (lpp_mid_contains(a, eta)) {
+        lpp_mid_interpolate(a, eta, f);
+        return true;
+    }
+    if (lpp_main_contains(a, eta)) return lpp_main_interpolate(a, eta, f);
+    return true;  // outside both tables the reference takes the rate as zero
+}
+
+// pair_creation/lp/mod.rs:385-420 (probability and Stokes update)
+static double lpp_probability(const double f[2], double eta, const Stokes& sv, double dphi, Stokes* out) {
+    double f0 = f[0], f1 = f[1];
+    double prob = ALPHA_FINE * (0.5 * ((f0 + f1) + sv.q * (f0 - f1))) * dphi / eta;
+    double prob_avg = ALPHA_FINE * (0.5 * (f0 + f1)) * dphi / eta;
+    double delta = ALPHA_FINE * (0.5 * (f0 - f1)) * dphi / eta;
+    *out = Stokes(sv.i, (sv.q * (1.0 - prob_avg) - delta) / (1.0 - prob), sv.u * (1.0 - prob_avg) / (1.0 - prob),
+                  sv.v * (1.0 - prob_avg) / (1.0 - prob));
+    return prob;
+}
+
+// pair_creation/lp/tables/mod.rs:60-113
+static int lpp_main_invert(double a, double eta, double sv1, double frac) {
+    const double* T = g_lma.bw_lp_cdf;  // [1525][16][3]
+    double fa = (std::log(a) - PTG_BW_LP_CDF_MIN_0) / PTG_BW_LP_CDF_STEP_0;
+    double fe = (std::log(eta) - PTG_BW_LP_CDF_MIN_1) / PTG_BW_LP_CDF_STEP_1;
+    int ia = (int)fa, ie = (int)fe;
+    double da = fa - std::trunc(fa), de = fe - std::trunc(fe);
+    int idx[4] = {25 * ie + ia, 25 * ie + ia + 1, 25 * (ie + 1) + ia, 25 * (ie + 1) + ia + 1};
+    double w[4] = {(1.0 - da) * (1.0 - de), da * (1.0 - de), (1.0 - da) * de, da * de};
+    double u = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        if (idx[k] < 0 || idx[k] >= 1525) return -1;
+        const double* src = T + (size_t)idx[k] * 48;
+        double n_min = src[0];
+        double f_max = PolDep{src[45 + 1], src[45 + 2]}.interp(sv1);
+        double tb[30];
+        for (int i = 0; i < 15; ++i) {
+            tb[2 * i] = std::log(src[3 * i] - n_min + 1.0);
+            double f = PolDep{src[3 * i + 1], src[3 * i + 2]}.interp(sv1);
+            tb[2 * i + 1] = std::log(-1.0 * std::log(1.0 - f / f_max));
+        }
+        bool ok;
+        double uk = Pwmci(tb, 15, true).invert(std::log(-1.0 * std::log(1.0 - frac)), &ok);
+        u += uk * w[k];
+    }
+    int n_min, n_max;
+    lpp_sum_limits(a, eta, &n_min, &n_max);
+    double n = (double)n_min + std::expm1(u);
+    return rust_as_i32(n) + 1;
+}
+
+// pair_creation/lp/tables/mid_range/mod.rs:100-270 (needs the regenerated
+// mid-range CDF)
+static int lpp_mid_corners(double a, double eta, int ie_out[1], int idx[4], double w[4], bool* next_to_bdy) {
+    const double LMA = PTG_BW_LPM_LN_MIN_A, SA = PTG_BW_LPM_LN_A_STEP, D = PTG_BW_LPM_ETA_PRIME_DENSITY;
+    int ia = rust_as_i32((std::log(a) - LMA) / SA);
+    double da = (std::log(a) - LMA) / SA - ia;
+    double ep = eta / (1.0 + 0.5 * a * a);
+    int ie = rust_as_i32(D * (std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / ep - 1.0));
+    *next_to_bdy = ie % (int)D == (int)D - 1;
+    if (*next_to_bdy) ie -= 1;
+    double lower = std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / (1.0 + (double)(ie + 1) / D);
+    double upper = std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / (1.0 + (double)ie / D);
+    double de = (std::log(ep) - std::log(lower)) / (std::log(upper) - std::log(lower));
+    idx[0] = 36 * ie + ia, idx[1] = 36 * ie + ia + 1, idx[2] = 36 * (ie + 1) + ia, idx[3] = 36 * (ie + 1) + ia + 1;
+    w[0] = (1.0 - da) * de, w[1] = da * de, w[2] = (1.0 - da) * (1.0 - de), w[3] = da * (1.0 - de);
+    ie_out[0] = ie;
+    for (int k = 0; k < 4; ++k)
+        if (idx[k] < 0 || idx[k] >= 5652) return -1;
+    return 0;
+}
+
+static int lpp_mid_invert(double a, double eta, double sv1, double frac) {
+    const double* T = g_lma.bw_lp_mid_cdf;  // [5652][16][3]
+    if (!T) return -2;
+    int ie, idx[4];
+    double w[4];
+    bool bdy;
+    if (lpp_mid_corners(a, eta, &ie, idx, w, &bdy) < 0) return -1;
+    int n_min, n_max;
+    lpp_sum_limits(a, eta, &n_min, &n_max);
+    double fr[2];
+    lpp_mid_interpolate(a, eta, fr);
+    double total_rate = 0.5 * ((fr[0] + fr[1]) + sv1 * (fr[0] - fr[1]));
+    double p_lowest = 0.0;
+    if (bdy) {
+        // interpolate_lowest_harmonic (mid_range/mod.rs:100-150), with the
+        // weights of that function's own (unshifted) eta' bracket
+        const double LMA = PTG_BW_LPM_LN_MIN_A, SA = PTG_BW_LPM_LN_A_STEP, D = PTG_BW_LPM_ETA_PRIME_DENSITY;
+        int ia = rust_as_i32((std::log(a) - LMA) / SA);
+        double da = (std::log(a) - LMA) / SA - ia;
+        double ep = eta / (1.0 + 0.5 * a * a);
+        int ie0 = rust_as_i32(D * (std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / ep - 1.0));
+        double lower = std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / (1.0 + (double)(ie0 + 1) / D);
+        double upper = std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / (1.0 + (double)ie0 / D);
+        double de = (std::log(ep) - std::log(lower)) / (std::log(upper) - std::log(lower));
+        int jx[4] = {36 * ie0 + ia, 36 * ie0 + ia + 1, 36 * (ie0 + 1) + ia, 36 * (ie0 + 1) + ia + 1};
+        double wx[4] = {(1.0 - da) * de, da * de, (1.0 - da) * (1.0 - de), da * (1.0 - de)};
+        double acc = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            if (jx[k] < 0 || jx[k] >= 5652) return -1;
+            const double* tb = T + (size_t)jx[k] * 48;
+            double fr0 = 0.0;
+            if (!(tb[0] > (double)n_min)) {
+                double f = PolDep{tb[1], tb[2]}.interp(sv1);
+                double f_max = PolDep{tb[46], tb[47]}.interp(sv1);
+                fr0 = f / f_max;
+            }
+            acc += wx[k] * std::pow(fr0 * total_rate, 3);
+        }
+        double rate_lowest = std::cbrt(acc);
+        p_lowest = rate_lowest / total_rate;
+        if (frac <= p_lowest) return n_min;
+    }
+    double n = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        const double* src = T + (size_t)idx[k] * 48;
+        double f_max = PolDep{src[46], src[47]}.interp(sv1);
+        double tb[32];
+        for (int i = 0; i < 16; ++i) {
+            tb[2 * i] = src[3 * i];
+            tb[2 * i + 1] = PolDep{src[3 * i + 1], src[3 * i + 2]}.interp(sv1) / f_max;
+        }
+        double nk;
+        bool ok = true;
+        if (bdy) {
+            if (tb[0] == (double)n_min) {
+                double t01 = tb[1];
+                for (int i = 0; i < 16; ++i) tb[2 * i + 1] = (t01 - tb[2 * i + 1] + p_lowest * (tb[2 * i + 1] - 1.0)) / (t01 - 1.0);
+            }
+            nk = Pwmci(tb, 16).invert(frac, &ok);
+        } else {
+            nk = frac <= tb[1] ? tb[0] - 0.1 : Pwmci(tb, 16).invert(frac, &ok);
+        }
+        if (!ok) return -1;  // the reference unwraps this inversion
+        n += nk * w[k];
+    }
+    return std::isfinite(n) ? rust_as_i32(std::ceil(n)) : -1;
+}
+
+// pair_creation/lp/theta_bound.rs:11-101
+struct LppThetaBound {
+    double s[16], f[16];
+    void init(int n, double a, double eta) {
+        double s_min = 0.5;
+        double s_max = 0.5 + std::sqrt(0.25 - (1.0 + 0.5 * a * a) / (2.0 * n * eta));
+        for (int i = 0; i < 16; ++i) {
+            double z = std::cos(PI * i / 15.0);
+            s[i] = s_min + 0.5 * (z + 1.0) * (s_max - s_min);
+            double r_n = std::sqrt(2.0 * n * eta * s[i] * (1.0 - s[i]) - (1.0 + 0.5 * a * a));
+            double x = a * r_n / (eta * s[i] * (1.0 - s[i]));
+            double y = a * a / (8.0 * eta * s[i] * (1.0 - s[i]));
+            double x_crit = y > n / 6.0 ? 4.0 * std::sqrt(y) * std::sqrt(n - 2.0 * y) : n + 2.0 * y;
+            double ln_j_crit = std::log(0.443) - std::log((double)n) / 3.0;
+            double ln_j_bdy = ThetaBound::ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y);
+            ln_j_bdy = std::fmin(ln_j_bdy, ln_j_crit);
+            double ct = std::fmax(1.0 - x_crit * std::log(0.01) / (x * (ln_j_bdy - ln_j_crit)), -1.0);
+            f[i] = std::acos(ct);
+            if (std::isnan(f[i])) f[i] = PI;
+        }
+        double f_min = f[0];
+        for (int i = 1; i < 16; ++i) {
+            if (f[i] < f_min)
+                f_min = f[i];
+            else
+                f[i] = f_min;
+        }
+    }
+    double at(double arg) const {
+        double val = f[15];
+        for (int i = 1; i < 16; ++i) {
+            if (arg > s[i]) {
+                double wt = (arg - s[i - 1]) / (s[i] - s[i - 1]);
+                val = wt * f[i] + (1.0 - wt) * f[i - 1];
+                break;
+            }
+        }
+        return std::fmin(val, FRAC_PI_2);
+    }
+};
+
+// pair_creation/lp/mod.rs:27-114: the double-differential partial rate
+struct LppRate {
+    int n;
+    double a, eta;
+    DoubleBessel dj;
+    LppThetaBound tb;
+    LppRate(int n_, double a_, double eta_) : n(n_), a(a_), eta(eta_), dj(n_, n_ * SQRT_2, n_ * 0.5) { tb.init(n, a, eta); }
+    void s_bounds(double* s_min, double* s_max) const {
+        *s_min = 0.5;
+        *s_max = std::fmax(0.5 + std::sqrt(0.25 - (1.0 + 0.5 * a * a) / (2.0 * n * eta)), 0.5);
+    }
+    void elements(double s, double theta, double* unpol, double* d1, double* d2) {
+        double r2 = 2.0 * n * eta * s * (1.0 - s) - (1.0 + 0.5 * a * a);
+        if (!(r2 > 0.0)) {
+            *unpol = *d1 = *d2 = 0.0;
+            return;
+        }
+        double rn = std::sqrt(r2);
+        double x = a * rn * std::cos(theta) / (eta * s * (1.0 - s));
+        double y = a * a / (8.0 * eta * s * (1.0 - s));
+        double j[5];
+        dj.evaluate(x, y, j);
+        double g0 = j[2], g1 = 0.5 * (j[1] + j[3]), g2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+        double h_s = 0.5 / (s * (1.0 - s)) - 1.0;
+        *unpol = powi(g0, 2) + a * a * h_s * (powi(g1, 2) - g0 * g2);
+        *d1 = powi(g0 * rn * std::cos(theta) - g1 * a, 2) - powi(g0 * std::sin(theta), 2) * r2;
+        *d2 = 2.0 * g0 * rn * std::sin(theta) * (g0 * rn * std::cos(theta) - g1 * a);
+    }
+    double fully_resolved(double s, double theta, double sv1, double sv2) {
+        double u, d1, d2;
+        elements(s, theta, &u, &d1, &d2);
+        return (u - sv1 * d1 - sv2 * d2) / (2.0 * PI);
+    }
+    // (unpol - delta, unpol + delta) / 2 pi: the two linear polarisations
+    void at(double s, double theta, double out[2]) {
+        double u, d1, d2;
+        elements(s, theta, &u, &d1, &d2);
+        out[0] = (u - d1) / (2.0 * PI);
+        out[1] = (u + d1) / (2.0 * PI);
+    }
+    double ceiling(double sv1, double sv2) {
+        double s_min, s_max;
+        s_bounds(&s_min, &s_max);
+        double centre = 0.5 + std::sqrt(0.25 - (1.0 + a * a) / (2.0 * n * eta));
+        double lower = s_min, upper = s_max;
+        if (std::isfinite(centre)) {
+            lower = std::fmax(centre - 0.2, s_min);
+            upper = 0.5 * (centre + s_max);
+        }
+        double mx = NAN;
+        for (int i = 0; i < 50; ++i) {
+            double v = fully_resolved(lower + (upper - lower) * (double)i / 50.0, 0.0, sv1, sv2);
+            mx = std::isnan(mx) ? v : (std::isnan(v) ? mx : std::max(mx, v));
+        }
+        return 1.2 * mx;
+    }
+    int sample(double sv1, double sv2, DrawStream& rng, double* s_out, double* theta_out, uint64_t* rej) {
+        double s_min, s_max;
+        s_bounds(&s_min, &s_max);
+        double mx = ceiling(sv1, sv2);
+        double s = 0.0, theta = 0.0;
+        int it;
+        for (it = 0; it < REJECTION_CAP; ++it) {
+            double ss = s_min + (s_max - s_min) * rng.next();
+            double th = FRAC_PI_2 * rng.next();
+            if (th > tb.at(ss)) continue;
+            double z = mx * rng.next();
+            if (z < fully_resolved(ss, th, sv1, sv2)) {
+                s = ss, theta = th;
+                break;
+            }
+        }
+        *rej += it;
+        if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+        if ((int)(2.0 * rng.next()) == 0) s = 1.0 - s;
+        int quadrant = (int)(4.0 * rng.next());
+        if (quadrant == 1)
+            theta = PI - theta;
+        else if (quadrant == 2)
+            theta = PI + theta;
+        else if (quadrant == 3)
+            theta = 2.0 * PI - theta;
+        *s_out = s;
+        *theta_out = theta;
+        return PTG_OK;
+    }
+};
+
+// pair_creation/lp/mod.rs:424-441
+int lp_pair_sample(double a, double eta, double sv1, double sv2, DrawStream& rng, int* n_out, double* s, double* theta,
+                   uint64_t* rej) {
+    double frac = rng.next();
+    int n;
+    if (lpp_mid_contains(a, eta))
+        n = lpp_mid_invert(a, eta, sv1, frac);
+    else if (lpp_main_contains(a, eta))
+        n = lpp_main_invert(a, eta, sv1, frac);
+    else
+        return PTG_ERR_OUT_OF_TABLE;
+    if (n == -2) return PTG_ERR_TABLES;
+    if (n < 1) return PTG_ERR_OUT_OF_TABLE;
+    LppRate r(n, a, eta);
+    *n_out = n;
+    return r.sample(sv1, sv2, rng, s, theta, rej);
+}
+
+
+// ------------------------------------- LP Breit-Wheeler table generator --
+// quadrature/adaptive.rs:1-370: adaptive 2-D Clenshaw-Curtis integration of
+// a complex integrand (here the two linear polarisations)
+struct C2 {
+    double re, im;
+};
+static inline C2 c2_add(C2 a, C2 b) { return C2{a.re + b.re, a.im + b.im}; }
+static inline C2 c2_sub(C2 a, C2 b) { return C2{a.re - b.re, a.im - b.im}; }
+static inline C2 c2_scale(double s, C2 a) { return C2{s * a.re, s * a.im}; }
+
+struct AdRegion {
+    C2 integral, error;
+    double x[2], y[2];
+    C2 cache[3][3];
+};
+
+static const double CC5[5][3] = {{0.0, 1.0 / 30.0, 1.0 / 6.0},
+                                 {0.1464466094067262, 4.0 / 15.0, 0.0},
+                                 {0.5, 2.0 / 5.0, 2.0 / 3.0},
+                                 {0.8535533905932738, 4.0 / 15.0, 0.0},
+                                 {1.0, 1.0 / 30.0, 1.0 / 6.0}};
+static const double CC5_EXT[9] = {0.0, 0.1464466094067262, 0.5, 0.8535533905932738, 1.0,
+                                  1.1464466094067262, 1.5, 1.8535533905932738, 2.0};
+static const double CC9[9][3] = {{0.0000000000000000, 0.0079365079365079, 1.0 / 30.0},
+                                 {0.0380602337443566, 0.0731093246080091, 0.0},
+                                 {0.1464466094067262, 0.1396825396825397, 4.0 / 15.0},
+                                 {0.3086582838174551, 0.1808589293602449, 0.0},
+                                 {0.5000000000000000, 0.1968253968253968, 2.0 / 5.0},
+                                 {0.6913417161825449, 0.1808589293602449, 0.0},
+                                 {0.8535533905932738, 0.1396825396825397, 4.0 / 15.0},
+                                 {0.9619397662556434, 0.0731093246080091, 0.0},
+                                 {1.0000000000000000, 0.0079365079365079, 1.0 / 30.0}};
+static const double CC9_EXT[17] = {0.0000000000000000, 0.0380602337443566, 0.1464466094067262, 0.3086582838174551,
+                                   0.5000000000000000, 0.6913417161825449, 0.8535533905932738, 0.9619397662556434,
+                                   1.0000000000000000, 1.0380602337443566, 1.1464466094067262, 1.3086582838174551,
+                                   1.5000000000000000, 1.6913417161825449, 1.8535533905932738, 1.9619397662556434,
+                                   2.0000000000000000};
+
+template <class F, class R>
+static AdRegion ad_new(F& f, R& inside, double x0, double x1, double y0, double y1) {
+    AdRegion g;
+    C2 result{0.0, 0.0}, error{0.0, 0.0};
+    for (int i = 0; i < 5; ++i) {
+        double y = y0 + CC5[i][0] * (y1 - y0);
+        for (int j = 0; j < 5; ++j) {
+            double x = x0 + CC5[j][0] * (x1 - x0);
+            C2 z = inside(x, y) ? f(x, y) : C2{0.0, 0.0};
+            result = c2_add(result, c2_scale(CC5[i][1] * CC5[j][1] * (y1 - y0) * (x1 - x0), z));
+            error = c2_add(error, c2_scale(CC5[i][2] * CC5[j][2] * (y1 - y0) * (x1 - x0), z));
+            if (i % 2 == 0 && j % 2 == 0) g.cache[i / 2][j / 2] = z;
+        }
+    }
+    g.integral = result;
+    g.error = c2_sub(result, error);
+    g.x[0] = x0, g.x[1] = x1, g.y[0] = y0, g.y[1] = y1;
+    return g;
+}
+
+static AdRegion ad_child(C2 res, C2 err, double xa, double xb, double ya, double yb, const C2 c[3][3]) {
+    AdRegion g;
+    g.integral = res;
+    g.error = c2_sub(res, err);
+    g.x[0] = xa, g.x[1] = xb, g.y[0] = ya, g.y[1] = yb;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) g.cache[i][j] = c[i][j];
+    return g;
+}
+
+// Region::custom_partition (adaptive.rs:33-152)
+template <class F, class R>
+static void ad_custom_partition(const AdRegion& r, F& f, R& inside, bool sx, double xs, bool sy, double ys,
+                                AdRegion out[4]) {
+    double x0 = r.x[0], x1 = r.x[1], y0 = r.y[0], y1 = r.y[1];
+    double x_mid = sx ? xs : 0.5 * (x0 + x1);
+    double y_mid = sy ? ys : 0.5 * (y0 + y1);
+    C2 z[9][9];
+    for (int i = 0; i < 9; ++i) {
+        double ty = CC5_EXT[i];
+        double y = i < 4 ? y0 + ty * (y_mid - y0) : y_mid + (ty - 1.0) * (y1 - y_mid);
+        for (int j = 0; j < 9; ++j) {
+            double tx = CC5_EXT[j];
+            double x = j < 4 ? x0 + tx * (x_mid - x0) : x_mid + (tx - 1.0) * (x1 - x_mid);
+            if (i % 8 == 0 && j % 8 == 0)
+                z[i][j] = r.cache[i / 4][j / 4];
+            else if (i % 4 == 0 && j % 4 == 0 && !sx && !sy)
+                z[i][j] = r.cache[i / 4][j / 4];
+            else
+                z[i][j] = inside(x, y) ? f(x, y) : C2{0.0, 0.0};
+        }
+    }
+    C2 res[4], err[4];
+    for (int q = 0; q < 4; ++q) res[q] = err[q] = C2{0.0, 0.0};
+    for (int rr = 0; rr < 2; ++rr)
+        for (int cc = 0; cc < 2; ++cc)
+            for (int i = 0; i < 5; ++i)
+                for (int j = 0; j < 5; ++j) {
+                    C2 val = z[i + 4 * rr][j + 4 * cc];
+                    double dy = rr < 1 ? y_mid - y0 : y1 - y_mid;
+                    double dx = cc < 1 ? x_mid - x0 : x1 - x_mid;
+                    res[2 * rr + cc] = c2_add(res[2 * rr + cc], c2_scale(CC5[j][1] * CC5[i][1] * dx * dy, val));
+                    err[2 * rr + cc] = c2_add(err[2 * rr + cc], c2_scale(CC5[j][2] * CC5[i][2] * dx * dy, val));
+                }
+    C2 cb[3][3] = {{z[0][0], z[0][2], z[0][4]}, {z[2][0], z[2][2], z[2][4]}, {z[4][0], z[4][2], z[4][4]}};
+    C2 cr[3][3] = {{z[0][4], z[0][6], z[0][8]}, {z[2][4], z[2][6], z[2][8]}, {z[4][4], z[4][6], z[4][8]}};
+    C2 ct[3][3] = {{z[4][0], z[4][2], z[4][4]}, {z[6][0], z[6][2], z[6][4]}, {z[8][0], z[8][2], z[8][4]}};
+    C2 cu[3][3] = {{z[4][4], z[4][6], z[4][8]}, {z[6][4], z[6][6], z[6][8]}, {z[8][4], z[8][6], z[8][8]}};
+    out[0] = ad_child(res[0], err[0], x0, x_mid, y0, y_mid, cb);
+    out[1] = ad_child(res[1], err[1], x_mid, x1, y0, y_mid, cr);
+    out[2] = ad_child(res[2], err[2], x0, x_mid, y_mid, y1, ct);
+    out[3] = ad_child(res[3], err[3], x_mid, x1, y_mid, y1, cu);
+}
+
+// Region::partition (adaptive.rs:180-300)
+template <class F, class R>
+static void ad_partition(const AdRegion& r, F& f, R& inside, AdRegion out[4]) {
+    double x0 = r.x[0], x1 = r.x[1], y0 = r.y[0], y1 = r.y[1];
+    double x_mid = 0.5 * (x0 + x1), y_mid = 0.5 * (y0 + y1);
+    static thread_local C2 z[17][17];
+    for (int i = 0; i < 17; ++i) {
+        double y = y0 + 0.5 * CC9_EXT[i] * (y1 - y0);
+        for (int j = 0; j < 17; ++j) {
+            double x = x0 + 0.5 * CC9_EXT[j] * (x1 - x0);
+            if (i % 8 == 0 && j % 8 == 0)
+                z[i][j] = r.cache[i / 8][j / 8];
+            else
+                z[i][j] = inside(x, y) ? f(x, y) : C2{0.0, 0.0};
+        }
+    }
+    C2 res[4], err[4];
+    for (int q = 0; q < 4; ++q) res[q] = err[q] = C2{0.0, 0.0};
+    for (int rr = 0; rr < 2; ++rr)
+        for (int cc = 0; cc < 2; ++cc)
+            for (int i = 0; i < 9; ++i)
+                for (int j = 0; j < 9; ++j) {
+                    C2 val = z[i + 8 * rr][j + 8 * cc];
+                    double dy = 0.5 * (y1 - y0), dx = 0.5 * (x1 - x0);
+                    res[2 * rr + cc] = c2_add(res[2 * rr + cc], c2_scale(CC9[j][1] * CC9[i][1] * dx * dy, val));
+                    err[2 * rr + cc] = c2_add(err[2 * rr + cc], c2_scale(CC9[j][2] * CC9[i][2] * dx * dy, val));
+                }
+    C2 cb[3][3] = {{z[0][0], z[0][4], z[0][8]}, {z[4][0], z[4][4], z[4][8]}, {z[8][0], z[8][4], z[8][8]}};
+    C2 cr[3][3] = {{z[0][8], z[0][12], z[0][16]}, {z[4][8], z[4][12], z[4][16]}, {z[8][8], z[8][12], z[8][16]}};
+    C2 ct[3][3] = {{z[8][0], z[8][4], z[8][8]}, {z[12][0], z[12][4], z[12][8]}, {z[16][0], z[16][4], z[16][8]}};
+    C2 cu[3][3] = {{z[8][8], z[8][12], z[8][16]}, {z[12][8], z[12][12], z[12][16]}, {z[16][8], z[16][12], z[16][16]}};
+    out[0] = ad_child(res[0], err[0], x0, x_mid, y0, y_mid, cb);
+    out[1] = ad_child(res[1], err[1], x_mid, x1, y0, y_mid, cr);
+    out[2] = ad_child(res[2], err[2], x0, x_mid, y_mid, y1, ct);
+    out[3] = ad_child(res[3], err[3], x_mid, x1, y_mid, y1, cu);
+}
+
+// integrate_2d (adaptive.rs:316-370)
+template <class F, class R>
+static C2 ad_integrate_2d(F f, double x0, bool has_xd, double xd, double x1, double y0, bool has_yd, double yd, double y1,
+                          R inside, double tol, int max_recursion) {
+    std::vector<AdRegion> regions;
+    regions.reserve(64);
+    AdRegion first = ad_new(f, inside, x0, x1, y0, y1);
+    if (!has_xd && !has_yd) {
+        regions.push_back(first);
+    } else {
+        AdRegion q[4];
+        ad_custom_partition(first, f, inside, has_xd, xd, has_yd, yd, q);
+        for (auto& g : q) regions.push_back(g);
+    }
+    C2 integral{0.0, 0.0};
+    for (int it = 0; it < max_recursion; ++it) {
+        C2 i_sum{0.0, 0.0}, e_sum{0.0, 0.0};
+        for (const auto& g : regions) {
+            i_sum = c2_add(i_sum, g.integral);
+            e_sum = c2_add(e_sum, g.error);
+        }
+        integral = i_sum;
+        if (std::fabs(e_sum.re) <= tol * std::fabs(i_sum.re) && std::fabs(e_sum.im) <= tol * std::fabs(i_sum.im)) break;
+        AdRegion worst = regions.back();
+        regions.pop_back();
+        AdRegion q[4];
+        ad_partition(worst, f, inside, q);
+        for (auto& g : q) regions.push_back(g);
+        std::stable_sort(regions.begin(), regions.end(), [](const AdRegion& a, const AdRegion& b) {
+            return a.error.re * a.error.re + a.error.im * a.error.im < b.error.re * b.error.re + b.error.im * b.error.im;
+        });
+    }
+    return integral;
+}
+
+// pair_creation/lp/mod.rs:115-227: DoubleDiffPartialRate::integrate, the
+// partial rate for the two linear polarisations (multiply by alpha/eta)
+static C2 lpp_integrate(int n, double a, double eta) {
+    LppRate r(n, a, eta);
+    double s_min, s_max;
+    r.s_bounds(&s_min, &s_max);
+    auto at = [&](double s, double th) {
+        double o[2];
+        r.at(s, th, o);
+        return C2{o[0], o[1]};
+    };
+    if (r.tb.at(0.5) < 0.75 * FRAC_PI_2) {
+        double s_peak = 0.5 + std::sqrt(0.25 - (1.0 + a * a) / (2.0 * n * eta));
+        bool has_peak = s_peak > s_min + 2.0 * (s_max - s_min) / 3.0;
+        double theta_split = r.tb.at(has_peak ? s_peak : 0.5);
+        LppThetaBound tb = r.tb;
+        C2 v = ad_integrate_2d(at, s_min, has_peak, s_peak, s_max, 0.0, true, theta_split, FRAC_PI_2,
+                               [&](double s, double th) { return th < tb.at(s); }, 1.0e-3, 16);
+        return c2_scale(4.0 * 2.0, v);
+    }
+    double s_peak = std::fmin(0.5 + std::sqrt(0.25 - (1.0 + a * a) / (2.0 * n * eta)), 0.5);
+    C2 integral{0.0, 0.0};
+    auto segment = [&](double s0, double s1, const double* nodes, const double* weights, int nn) {
+        C2 acc{0.0, 0.0};
+        for (int k = 0; k < nn; ++k) {
+            double s = s0 + 0.5 * (nodes[k] + 1.0) * (s1 - s0);
+            double mt = r.tb.at(s);
+            C2 sd{0.0, 0.0};
+            for (int q = 0; q < 32; ++q) {
+                double th = 0.5 * (PTG_GAUSS_32_NODES[q] + 1.0) * mt;
+                sd = c2_add(sd, c2_scale(0.5 * PTG_GAUSS_32_WEIGHTS[q] * mt, at(s, th)));
+            }
+            acc = c2_add(acc, c2_scale(0.5 * weights[k] * (s1 - s0), sd));
+        }
+        return acc;
+    };
+    if (s_peak < s_min + 2.0 * (s_max - s_min) / 3.0) {
+        s_peak = std::fmin(s_peak, s_min + (s_max - s_min) / 3.0);
+        integral = c2_add(segment(s_min, s_peak, PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32),
+                          segment(s_peak, s_max, PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32));
+    } else {
+        double delta = s_max - s_peak;
+        integral = c2_add(c2_add(segment(s_min, s_max - 2.0 * delta, PTG_GAUSS_16_NODES, PTG_GAUSS_16_WEIGHTS, 16),
+                                 segment(s_max - 2.0 * delta, s_peak, PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32)),
+                          segment(s_peak, s_max, PTG_GAUSS_32_NODES, PTG_GAUSS_32_WEIGHTS, 32));
+    }
+    return c2_scale(2.0 * 4.0, integral);
+}
+
+void lp_pair_partial_rate(int n, double a, double eta, double out[2]) {
+    C2 v = lpp_integrate(n, a, eta);
+    out[0] = v.re, out[1] = v.im;
+}
+
+// pair_creation/lp/mod.rs:443-507: TotalRate::by_summation, the 16 CDF
+// nodes [n, cumulative par, cumulative perp]
+void lp_pair_by_summation(double a, double eta, double cdf[48]) {
+    int n_min, n_max;
+    lpp_sum_limits(a, eta, &n_min, &n_max);
+    std::vector<C2> cum;
+    C2 total{0.0, 0.0};
+    for (int n = n_min; n <= n_max; ++n) {
+        total = c2_add(total, lpp_integrate(n, a, eta));
+        cum.push_back(total);
+    }
+    double delta = (double)(n_max - n_min);
+    double u_max = std::log(1.0 + delta);
+    for (int i = 0; i < 48; ++i) cdf[i] = 0.0;
+    cdf[0] = (double)n_min;
+    double u = 0.0, du = u_max / 15.0;
+    for (int i = 1; i <= 15; ++i) {
+        u = u + du;
+        double nn = (double)n_min + std::expm1(u);
+        if (std::round(nn) <= cdf[3 * (i - 1)]) {
+            nn = cdf[3 * (i - 1)] + 1.0;
+            u = std::log(nn - (double)n_min + 1.0);
+            du = (u_max - u) / (15.0 - (double)i);
+        } else {
+            nn = std::round(nn);
+        }
+        cdf[3 * i] = nn;
+    }
+    for (int i = 0; i < 16; ++i) {
+        size_t index = (size_t)rust_as_i32(cdf[3 * i]) - (size_t)n_min;
+        const C2& c = index < cum.size() ? cum[index] : cum.back();
+        cdf[3 * i + 1] = c.re;
+        cdf[3 * i + 2] = c.im;
+    }
+}
+
+// DoubleDiffPartialRate::at, for tests of the regenerated tables
+void lp_pair_dd_rate(int n, double a, double eta, double s, double theta, double out[2]) {
+    LppRate r(n, a, eta);
+    r.at(s, theta, out);
+}
+
+
 // pair_creation/mod.rs:21-42 (CP only: LP added with its sampler)
 bool bw_probability(const V4& ell, const Stokes& sv_in, const V4& k, double a, double dt, int pol, double pol_angle,
                     double* prob, Stokes* sv_out) {
     double eta = k * ell;
     Stokes sv = sv_in.in_lma_basis(ell).rotate_by(pol_angle);
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
-    if (pol != PTG_POL_CIRCULAR) return false;
     double f[2];
-    if (!cp_pair_rates(a, eta, f)) return false;
     Stokes out;
-    *prob = cpp_probability(f, eta, sv, dphi, &out);
+    if (pol == PTG_POL_CIRCULAR) {
+        if (!cp_pair_rates(a, eta, f)) return false;
+        *prob = cpp_probability(f, eta, sv, dphi, &out);
+    } else {
+        if (!lp_pair_rates(a * SQRT_2, eta, f)) return false;
+        *prob = lpp_probability(f, eta, sv, dphi, &out);
+    }
     *sv_out = out.rotate_by(-pol_angle).from_lma_basis(ell);
     return true;
 }
@@ -1335,8 +2048,8 @@ int bw_generate(const V4& ell, const Stokes& sv_in, const V4& k, double a, int p
     Stokes sv = sv_in.in_lma_basis(ell).rotate_by(pol_angle);
     int n;
     double s, cphi;
-    if (pol != PTG_POL_CIRCULAR) return PTG_ERR_UNSUPPORTED;
-    int st = cpp_sample(a, eta, sv.q, sv.u, sv.v, rng, &n, &s, &cphi, rej);
+    int st = pol == PTG_POL_CIRCULAR ? cpp_sample(a, eta, sv.q, sv.u, sv.v, rng, &n, &s, &cphi, rej)
+                                     : lp_pair_sample(a * SQRT_2, eta, sv.q, sv.u, rng, &n, &s, &cphi, rej);
     if (st != PTG_OK) return st;
     double j = n;
     double e_zmf = std::sqrt(0.5 * j * eta);
@@ -1374,7 +2087,7 @@ int lma_pair_create(const Laser& L, const V4& r, const V4& ell, const Stokes& po
     }
     V4 kappa = (SPEED_OF_LIGHT * COMPTON_TIME * chirp) * L.wavevector;
     if (!bw_probability(ell, pol, kappa, a, dt, L.d.polarization, L.d.pol_angle, prob, pol_new))
-        return L.d.polarization == PTG_POL_CIRCULAR ? PTG_ERR_OUT_OF_TABLE : PTG_ERR_UNSUPPORTED;
+        return PTG_ERR_OUT_OF_TABLE;
     double ri = (*prob * rate_increase > 0.1) ? 0.1 / *prob : rate_increase;
     if (rng.next() < *prob * ri) {
         int n;

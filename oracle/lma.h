@@ -72,6 +72,13 @@ bool cp_pair_by_lookup(double a, double eta, double f[2]);
 bool cp_pair_rates(double a, double eta, double f[2]);
 bool bw_probability(const V4& ell, const Stokes& sv, const V4& k, double a, double dt, int pol, double pol_angle,
                     double* prob, Stokes* sv_out);
+// pair_creation/lp
+bool lp_pair_rates(double a, double eta, double f[2]);
+int lp_pair_sample(double a, double eta, double sv1, double sv2, DrawStream& rng, int* n, double* s, double* theta,
+                   uint64_t* rej);
+void lp_pair_dd_rate(int n, double a, double eta, double s, double theta, double out[2]);
+void lp_pair_partial_rate(int n, double a, double eta, double out[2]);
+void lp_pair_by_summation(double a, double eta, double cdf[48]);
 int bw_generate(const V4& ell, const Stokes& sv, const V4& k, double a, int pol, double pol_angle, DrawStream& rng,
                 int* n, V4* q, uint64_t* rej);
 

@@ -107,6 +107,11 @@ def lib():
         "orc_lp_rate": (d, [d, d]),
         "orc_lp_harmonic_index": (i, [d, d, d]),
         "orc_lp_sample": (i, [d, d, u64, u64, u32, DP]),
+        "orc_lp_pair_rates": (None, [d, d, DP]),
+        "orc_lp_pair_dd_rate": (None, [i, d, d, d, d, DP]),
+        "orc_lp_pair_partial_rate": (None, [i, d, d, DP]),
+        "orc_lp_pair_by_summation": (None, [d, d, DP]),
+        "orc_lp_pair_sample": (i, [d, d, d, d, u64, u64, u32, DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -374,6 +379,36 @@ def lp_harmonic_index(a, eta, frac):
 def lp_sample(a, eta, seed, stream, step):
     out = np.zeros(7)
     rc = lib().orc_lp_sample(a, eta, seed, stream, step, _dp(out))
+    return rc, out
+
+
+def lp_pair_rates(a, eta):
+    out = np.zeros(2)
+    lib().orc_lp_pair_rates(a, eta, _dp(out))
+    return out
+
+
+def lp_pair_dd_rate(n, a, eta, s, theta):
+    out = np.zeros(2)
+    lib().orc_lp_pair_dd_rate(n, a, eta, s, theta, _dp(out))
+    return out
+
+
+def lp_pair_partial_rate(n, a, eta):
+    out = np.zeros(2)
+    lib().orc_lp_pair_partial_rate(n, a, eta, _dp(out))
+    return out
+
+
+def lp_pair_by_summation(a, eta):
+    out = np.zeros(48)
+    lib().orc_lp_pair_by_summation(a, eta, _dp(out))
+    return out.reshape(16, 3)
+
+
+def lp_pair_sample(a, eta, sv1, sv2, seed, stream, step):
+    out = np.zeros(3)
+    rc = lib().orc_lp_pair_sample(a, eta, sv1, sv2, seed, stream, step, _dp(out))
     return rc, out
 
 

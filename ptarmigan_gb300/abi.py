@@ -117,6 +117,30 @@ class RunStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 
+class Collision(C.Structure):
+    """ptg_collision: one collision of a multi-collision batch."""
+    _fields_ = [
+        ("laser", LaserDesc),
+        ("seed", C.c_uint64),
+        ("id_base", C.c_uint64),
+        ("first", C.c_uint64),
+        ("count", C.c_uint64),
+    ]
+
+
+class QueueCfg(C.Structure):
+    """ptg_queue_cfg: launch shape of the queue kernel."""
+    _fields_ = [
+        ("variant", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("chunk", C.c_int32),
+        ("use_graph", C.c_int32),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class DeviceCfg(C.Structure):
     _fields_ = [
         ("device", C.c_int32),

@@ -1,7 +1,8 @@
 """Builds the engine's shared library, in-tree, for sm_103a only.
 
-``build()`` runs nvcc on ``csrc/ptg_engine.cu`` (one translation unit that
-includes every kernel) into ``_build/libptarmigan_gb300.so``.  It rebuilds
+``build()`` compiles each translation unit of ``csrc/`` (the host engine and
+the kernel families: LCFA waves, LMA waves, the queue kernel variants) in
+parallel with nvcc, then links ``_build/libptarmigan_gb300.so``.  It rebuilds
 only when a source is newer than the library.
 """
 
@@ -9,16 +10,22 @@ import glob
 import os
 import shutil
 import subprocess
+from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libptarmigan_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "20091,550"]
+
+
+def _units():
+    return sorted(glob.glob(os.path.join(HERE, "csrc", "*.cu")))
 
 
 def _sources():
-    srcs = glob.glob(os.path.join(HERE, "csrc", "*.cu")) + glob.glob(os.path.join(HERE, "csrc", "*.cuh"))
+    srcs = _units() + glob.glob(os.path.join(HERE, "csrc", "*.cuh")) + glob.glob(os.path.join(HERE, "csrc", "*.h"))
     srcs += [os.path.join(HERE, "tables", "ptg_tables_small.h"), os.path.join(ROOT, "include", "ptarmigan_gb300.h")]
     return srcs
 
@@ -37,18 +44,29 @@ def needs_build():
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
+def _run(cmd):
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + out.stdout + out.stderr)
+    return out.stdout + out.stderr
+
+
 def build(force=False, verbose=False):
     """Compiles the library if needed and returns its path."""
     if not force and not needs_build():
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    objs, cmds = [], []
+    for src in _units():
+        obj = os.path.join(BUILD_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
+        objs.append(obj)
+        cmds.append([nvcc, *ARCH, *FLAGS, "-c", "-o", obj, src])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(cmds), os.cpu_count() or 1))) as ex:
+        logs = list(ex.map(_run, cmds))
     tmp = LIB_PATH + ".tmp"
-    cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-           "-diag-suppress", "20091", "-o", tmp, os.path.join(HERE, "csrc", "ptg_engine.cu")]
-    out = subprocess.run(cmd, capture_output=True, text=True)
-    if out.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + out.stdout + out.stderr)
+    logs.append(_run([nvcc, *ARCH, "-shared", "-o", tmp, *objs]))
     if verbose:
-        print(out.stdout + out.stderr)
+        print("".join(logs))
     os.replace(tmp, LIB_PATH)
     return LIB_PATH

@@ -58,7 +58,7 @@ __device__ __forceinline__ void bw_over_theta(int n, double a, double eta, doubl
 }
 
 // pair_creation/cp/mod.rs:92-186: integral over s and theta, both S3 parts
-__device__ __noinline__ void bw_integrate(int n, double a, double eta, double* out_re, double* out_im) {
+static __device__ __noinline__ void bw_integrate(int n, double a, double eta, double* out_re, double* out_im) {
     double ell = n;
     double sn = 2.0 * ell * eta / (1.0 + a * a);
     *out_re = 0.0, *out_im = 0.0;
@@ -122,7 +122,7 @@ __device__ __forceinline__ bool bw_is_too_small(double a, double eta) {
 }
 
 // pair_creation/cp/mod.rs:385-393
-__device__ __noinline__ void bw_by_summation(double a, double eta, double* f0, double* f1) {
+static __device__ __noinline__ void bw_by_summation(double a, double eta, double* f0, double* f1) {
     int n0, n1;
     bw_sum_limits(a, eta, &n0, &n1);
     double re = 0.0, im = 0.0;
@@ -135,7 +135,7 @@ __device__ __noinline__ void bw_by_summation(double a, double eta, double* f0, d
 }
 
 // pair_creation/cp/mod.rs:395-448; false where the reference panics
-__device__ __noinline__ bool bw_by_lookup(const double* T, double a, double eta, double* f0, double* f1) {
+static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, double eta, double* f0, double* f1) {
     const double LMA = PTG_BW_CP_LN_MIN_A, LME = PTG_BW_CP_LN_MIN_ETA, SA = PTG_BW_CP_LN_A_STEP, SE = PTG_BW_CP_LN_ETA_STEP;
     const int NC = 74, NR = 121;
     double x = log(a), y = log(eta);
@@ -181,7 +181,7 @@ __device__ __forceinline__ bool bw_rates(const double* T, double a, double eta, 
 
 // pair_creation/cp/mod.rs:191-243: s by rejection on the theta-integrated
 // spectrum, the side of s = 1/2, then theta by rejection.
-__device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3,
+static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3,
                                               Draws& rng, double* s_out, double* theta_out, uint32_t* rej) {
     double s_min, s_max;
     bw_s_bounds(n, a, eta, &s_min, &s_max);
@@ -229,7 +229,7 @@ __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, doubl
 }
 
 // pair_creation/cp/mod.rs:314-346: harmonic by explicit summation
-__device__ __noinline__ int bw_sample(const double* T, double a, double eta, double sv1, double sv2, double sv3,
+static __device__ __noinline__ int bw_sample(const double* T, double a, double eta, double sv1, double sv2, double sv3,
                                       Draws& rng, int* n_out, double* s, double* theta, uint32_t* rej) {
     int n0, n1;
     bw_sum_limits(a, eta, &n0, &n1);
@@ -270,7 +270,7 @@ __device__ __forceinline__ d4 stokes_rotate_by(d4 sv, double theta) {
 }
 
 // pair_creation/mod.rs:21-42 + cp/mod.rs:280-309 (CP).  Returns false out of table.
-__device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
+static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
                                             double pol_angle, double* prob, d4* sv_out) {
     double eta = dot4(k, ell);
     d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
@@ -290,7 +290,7 @@ __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 sv_in, d
 }
 
 // pair_creation/mod.rs:49-110 (CP): the positron momentum
-__device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
+static __device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
                                         int* n_out, d4* q_out, uint32_t* rej) {
     double eta = dot4(k, ell);
     d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);

@@ -19,7 +19,9 @@
 
 #include "../../include/ptarmigan_gb300.h"
 #include "ptg_collide.cuh"
+#include "ptg_launch.h"
 #include "ptg_nlc.cuh"
+#include "ptg_queue.cuh"
 
 using namespace ptg;
 
@@ -71,6 +73,22 @@ struct ptg_ctx {
     int grid_cap = 0;  // > 0: the wave grid is capped (workspace budget)
     std::vector<void*> table_bufs;
     bool tables_loaded = false;
+    // multi-collision queue: per-collision device arrays and pinned mirrors
+    size_t q_cap = 0;                      // collisions the arrays hold
+    CollParams* d_coll = nullptr;
+    CollStats* d_cstats = nullptr;
+    unsigned long long* d_qoff = nullptr;  // [q_cap + 1] loaded-index prefix of the counts
+    unsigned long long* d_qfirst = nullptr;
+    unsigned long long* d_qout = nullptr;  // [q_cap + 1] output offsets
+    unsigned long long* d_qcursor = nullptr;
+    CollParams* h_coll = nullptr;
+    CollStats* h_cstats = nullptr;
+    unsigned long long* h_qoff = nullptr;
+    unsigned long long* h_qfirst = nullptr;
+    unsigned long long* h_qout = nullptr;
+    ptg_queue_cfg qcfg{0, 0, 1, 1};
+    cudaGraphExec_t q_graph = nullptr;
+    std::string q_graph_key;
 };
 
 // ------------------------------------------------------------ helpers ---
@@ -150,31 +168,33 @@ static ptg_status check_laser(const ptg_laser_desc* d) {
 }
 
 // ------------------------------------------------------------ kernels ---
-__global__ void k_load_primaries(Store s, ptg_particles in, unsigned long long n, unsigned long long id_base,
-                                 double* init_u, unsigned long long* shower_count) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// Primary `row` of `in` into store slot i.
+__device__ __forceinline__ void load_primary(const Store& s, const ptg_particles& in, unsigned long long row,
+                                             unsigned long long i, unsigned long long default_id,
+                                             unsigned long long stream, double* init_u,
+                                             unsigned long long* shower_count) {
     unsigned long long cap = s.cap;
-    d4 r = d4{in.r[4 * i], in.r[4 * i + 1], in.r[4 * i + 2], in.r[4 * i + 3]};
-    d4 u = d4{in.u[4 * i], in.u[4 * i + 1], in.u[4 * i + 2], in.u[4 * i + 3]};
-    int sp = in.species[i];
+    unsigned long long k = row;
+    d4 r = d4{in.r[4 * k], in.r[4 * k + 1], in.r[4 * k + 2], in.r[4 * k + 3]};
+    d4 u = d4{in.u[4 * k], in.u[4 * k + 1], in.u[4 * k + 2], in.u[4 * k + 3]};
+    int sp = in.species[k];
     put4(s.r, cap, i, r);
     put4(s.u, cap, i, u);
-    put4(s.r0, cap, i, in.r0 ? d4{in.r0[4 * i], in.r0[4 * i + 1], in.r0[4 * i + 2], in.r0[4 * i + 3]} : r);
+    put4(s.r0, cap, i, in.r0 ? d4{in.r0[4 * k], in.r0[4 * k + 1], in.r0[4 * k + 2], in.r0[4 * k + 3]} : r);
     d4 u0 = sp == SP_PHOTON ? d4{0, 0, 0, 0} : d4{1, 0, 0, 0};
-    if (in.u0) u0 = d4{in.u0[4 * i], in.u0[4 * i + 1], in.u0[4 * i + 2], in.u0[4 * i + 3]};
+    if (in.u0) u0 = d4{in.u0[4 * k], in.u0[4 * k + 1], in.u0[4 * k + 2], in.u0[4 * k + 3]};
     put4(s.u0, cap, i, u0);
-    put4(s.pol, cap, i, in.pol ? d4{in.pol[4 * i], in.pol[4 * i + 1], in.pol[4 * i + 2], in.pol[4 * i + 3]} : d4{1, 0, 0, 0});
-    s.weight[i] = in.weight ? in.weight[i] : 1.0;
+    put4(s.pol, cap, i, in.pol ? d4{in.pol[4 * k], in.pol[4 * k + 1], in.pol[4 * k + 2], in.pol[4 * k + 3]} : d4{1, 0, 0, 0});
+    s.weight[i] = in.weight ? in.weight[k] : 1.0;
     s.payload[i] = 0.0;
     s.parent_chi[i] = 0.0;
     s.icount[i] = 0.0;
     s.work[i] = 0.0;
-    unsigned long long id = in.id ? in.id[i] : i;
+    unsigned long long id = in.id ? in.id[k] : default_id;
     s.id[i] = id;
-    s.parent_id[i] = in.parent_id ? in.parent_id[i] : id;
+    s.parent_id[i] = in.parent_id ? in.parent_id[k] : id;
     s.primary[i] = i;
-    s.stream[i] = primary_stream(id_base + i);
+    s.stream[i] = stream;
     s.species[i] = sp;
     s.generation[i] = 0;
     s.flags[i] = 0;
@@ -183,19 +203,30 @@ __global__ void k_load_primaries(Store s, ptg_particles in, unsigned long long n
     shower_count[i] = 0;
 }
 
+__global__ void k_load_primaries(Store s, ptg_particles in, unsigned long long n, unsigned long long id_base,
+                                 double* init_u, unsigned long long* shower_count) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    load_primary(s, in, i, i, i, primary_stream(id_base + i), init_u, shower_count);
+}
+
 struct FilterArgs {
     Store s;
     const double* init_u;
     unsigned long long* shower_count;
     unsigned long long n;
+    const unsigned long long* n_live;  // if set, slots at or past *n_live are skipped as well
     double min_energy, cos_max_angle;
     int discard_bg_e, discard_bg_ph, multiplicity;
 };
 
 __device__ __forceinline__ bool filter_keep(const FilterArgs& a, unsigned long long i, bool* counted) {
     const Store& s = a.s;
-    int fl = s.flags[i];
     *counted = false;
+    // a phantom (queue slot reserved by an append that overflowed the store)
+    // holds nothing but its status
+    if (s.status[i] == ST_PHANTOM) return false;
+    int fl = s.flags[i];
     if (fl & FLAG_DROP) return false;
     if (fl & FLAG_INTERMEDIATE) return true;
     int gen = s.generation[i], sp = s.species[i];
@@ -213,36 +244,21 @@ __device__ __forceinline__ bool filter_keep(const FilterArgs& a, unsigned long l
     return keep;
 }
 
+__device__ __forceinline__ bool in_range(const FilterArgs& a, unsigned long long i) {
+    return i < a.n && (!a.n_live || i < *a.n_live);
+}
+
 __global__ void k_filter_count(FilterArgs a) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+    if (!in_range(a, i)) return;
     bool counted;
     filter_keep(a, i, &counted);
     if (counted) atomicAdd(&a.shower_count[a.s.primary[i]], 1ull);
 }
 
-__global__ void k_compact(FilterArgs a, Counters* c, ptg_particles o, unsigned long long out_cap) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    bool keep = false;
-    if (i < a.n) {
-        bool counted;
-        keep = filter_keep(a, i, &counted);
-        // main.rs:278-283: multiplicity selection drops whole showers
-        if (keep && a.multiplicity >= 0 && !(a.s.flags[i] & FLAG_INTERMEDIATE) &&
-            a.shower_count[a.s.primary[i]] != (unsigned long long)a.multiplicity + 1)
-            keep = false;
-    }
-    unsigned ballot = __ballot_sync(0xffffffffu, keep);
-    if (ballot == 0) return;
-    unsigned lane = threadIdx.x & 31u;
-    unsigned leader = __ffs(ballot) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&c->n_out, (unsigned long long)__popc(ballot));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (!keep) return;
-    unsigned long long j = base + __popc(ballot & ((1u << lane) - 1u));
-    if (j >= out_cap) return;
-    const Store& s = a.s;
+// Store slot i into row j of a row-major output.
+__device__ __forceinline__ void write_row(const ptg_particles& o, unsigned long long j, const Store& s,
+                                          unsigned long long i) {
     unsigned long long cap = s.cap;
     for (int k = 0; k < 4; ++k) {
         o.r[4 * j + k] = s.r[k * cap + i];
@@ -264,6 +280,33 @@ __global__ void k_compact(FilterArgs a, Counters* c, ptg_particles o, unsigned l
     o.generation[j] = s.generation[i];
     o.flags[j] = s.flags[i];
     o.status[j] = s.status[i];
+}
+
+// filter_keep plus the multiplicity selection (main.rs:278-283), which
+// drops whole showers.
+__device__ __forceinline__ bool final_keep(const FilterArgs& a, unsigned long long i) {
+    bool counted;
+    bool keep = filter_keep(a, i, &counted);
+    if (keep && a.multiplicity >= 0 && !(a.s.flags[i] & FLAG_INTERMEDIATE) &&
+        a.shower_count[a.s.primary[i]] != (unsigned long long)a.multiplicity + 1)
+        keep = false;
+    return keep;
+}
+
+__global__ void k_compact(FilterArgs a, Counters* c, ptg_particles o, unsigned long long out_cap) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool keep = in_range(a, i) && final_keep(a, i);
+    unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (ballot == 0) return;
+    unsigned lane = threadIdx.x & 31u;
+    unsigned leader = __ffs(ballot) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&c->n_out, (unsigned long long)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!keep) return;
+    unsigned long long j = base + __popc(ballot & ((1u << lane) - 1u));
+    if (j >= out_cap) return;
+    write_row(o, j, a.s, i);
 }
 
 __global__ void k_sum_work(Store s, unsigned long long n, double* out) {
@@ -374,6 +417,12 @@ __global__ void k_lp_sample(unsigned long long m, int cap, const LmaTables* t, c
 }
 
 // ---------------------------------------------------------- storage -----
+// 5 four-vectors, 5 doubles, 4 u64 and 6 32-bit fields per particle, each
+// array padded to 256 B
+static constexpr size_t store_bytes(unsigned long long cap) {
+    return (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 6 * 4) * cap + 20 * 256;
+}
+
 static void carve_store(Store* s, void* mem, unsigned long long cap) {
     char* p = (char*)mem;
     auto take = [&](size_t bytes) {
@@ -400,6 +449,8 @@ static void carve_store(Store* s, void* mem, unsigned long long cap) {
     s->generation = (int*)take(4 * cap);
     s->flags = (int*)take(4 * cap);
     s->status = (int*)take(4 * cap);
+    s->coll = (int*)take(4 * cap);
+    s->ready = (unsigned int*)take(4 * cap);
 }
 
 static size_t particles_bytes(unsigned long long cap) {
@@ -440,7 +491,7 @@ static ptg_status ensure_store(ptg_ctx* c, unsigned long long cap) {
     if (c->store_mem) cudaFree(c->store_mem);
     c->store_mem = nullptr;
     c->cap = 0;
-    size_t bytes = (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 4 * 4) * cap + 18 * 256;
+    size_t bytes = store_bytes(cap);
     if (cudaMalloc(&c->store_mem, bytes) != cudaSuccess) {
         cudaGetLastError();
         return set_err(PTG_ERR_ALLOC, "could not allocate the shower store (" + std::to_string(bytes) + " bytes)");
@@ -531,6 +582,7 @@ const char* ptg_status_string(ptg_status s) {
         case PTG_ERR_TABLES: return "tables missing or malformed";
         case PTG_ERR_UNSUPPORTED: return "unsupported option combination";
         case PTG_ERR_ALLOC: return "device allocation failed";
+        case PTG_ERR_TIMEOUT: return "a bounded device wait ran out";
     }
     return "unknown status";
 }
@@ -555,7 +607,10 @@ ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out) {
     cudaDeviceProp prop;
     CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
     c->num_sms = prop.multiProcessorCount;
-    if (cfg && cfg->block_size > 0) c->block = cfg->block_size;
+    if (cfg && cfg->block_size > 0 && cfg->block_size != 128) {
+        delete c;
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "the collision kernels run 128 threads per block");
+    }
     if (cfg && cfg->blocks_per_sm > 0) c->blocks_per_sm = cfg->blocks_per_sm;
     CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&c->ev0));
@@ -603,6 +658,18 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     cudaFree(c->gl);
     cudaFree(c->lma_dev);
     cudaFree(c->dbw);
+    if (c->q_graph) cudaGraphExecDestroy(c->q_graph);
+    cudaFree(c->d_coll);
+    cudaFree(c->d_cstats);
+    cudaFree(c->d_qoff);
+    cudaFree(c->d_qfirst);
+    cudaFree(c->d_qout);
+    cudaFree(c->d_qcursor);
+    cudaFreeHost(c->h_coll);
+    cudaFreeHost(c->h_cstats);
+    cudaFreeHost(c->h_qoff);
+    cudaFreeHost(c->h_qfirst);
+    cudaFreeHost(c->h_qout);
     for (void* p : c->table_bufs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -683,25 +750,19 @@ static int grid_for(ptg_ctx* c, const void* kernel) {
     return per_sm * c->num_sms;
 }
 
-template <int MODEL>
-static cudaError_t launch_wave(ptg_ctx* c, const WaveArgs& a) {
-    int grid = grid_for(c, (const void*)collide_wave<MODEL>);
+static const void* wave_kernel(int model) {
+    return (model == M_PLANE_WAVE || model == M_FOCUSED_LASER) ? wave_kernel_lma(model) : wave_kernel_lcfa(model);
+}
+
+static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
+    int grid = grid_for(c, wave_kernel(a.f.model));
     if (c->grid_cap > 0 && grid > c->grid_cap) grid = c->grid_cap;
     unsigned long long n = a.hi - a.lo;
     unsigned long long need = (n + c->block - 1) / c->block;
     if ((unsigned long long)grid > need) grid = (int)need;
     if (grid < 1) grid = 1;
-    collide_wave<MODEL><<<grid, c->block, 0, c->stream>>>(a);
-    return cudaGetLastError();
-}
-
-static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
-    switch (a.f.model) {
-        case M_PLANE_WAVE: return launch_wave<M_PLANE_WAVE>(c, a);
-        case M_FAST_PLANE_WAVE: return launch_wave<M_FAST_PLANE_WAVE>(c, a);
-        case M_FOCUSED_LASER: return launch_wave<M_FOCUSED_LASER>(c, a);
-        default: return launch_wave<M_FAST_FOCUSED_LASER>(c, a);
-    }
+    if (a.f.model == M_PLANE_WAVE || a.f.model == M_FOCUSED_LASER) return launch_wave_lma(a.f.model, grid, c->stream, a);
+    return launch_wave_lcfa(a.f.model, grid, c->stream, a);
 }
 
 // Linearly polarised LMA emission evaluates J(n, x, y) by recurrence in a
@@ -709,23 +770,20 @@ static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
 // to 1.5x the reference's harmonic sum limit at 1.05 a0 (its eta -> 0 bound);
 // a sampled order beyond that retires the particle with PTG_ERR_UNSUPPORTED.
 // The workspace stays within min(8 GiB, free / 4), which may cap the grid.
-static ptg_status ensure_dbw(ptg_ctx* c, const ptg_laser_desc* laser, WaveArgs* a) {
-    double A = 1.05 * laser->a0;
+static ptg_status ensure_dbw(ptg_ctx* c, double a0, int grid_wanted, double** ws, int* cap_out, int* grid_out) {
+    double A = 1.05 * a0;
     int n_cap = (int)std::ceil(1.5 * (6.0 * (1.0 + A * A) + 2.0 * A * A * A)) + 16;
     int cap = db_len_for(n_cap);
-    size_t per_warp = (size_t)cap * 5 * 32 * sizeof(double);
-    size_t warps_per_block = (size_t)(c->block + 31) / 32;
-    const void* kern = laser->model == PTG_PLANE_WAVE ? (const void*)collide_wave<M_PLANE_WAVE>
-                                                      : (const void*)collide_wave<M_FOCUSED_LASER>;
-    int grid = grid_for(c, kern);
+    size_t per_block = (size_t)cap * 5 * 32 * sizeof(double) * (size_t)((c->block + 31) / 32);
     size_t free_b = 0, total_b = 0;
     CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    size_t budget = std::min<size_t>((size_t)8 << 30, free_b / 4);
-    size_t max_blocks = budget / (per_warp * warps_per_block);
+    size_t budget = std::min<size_t>((size_t)8 << 30, (free_b + c->dbw_bytes) / 4);
+    size_t max_blocks = budget / per_block;
     if (max_blocks < 1)
-        return set_err(PTG_ERR_ALLOC, "no room for one block of LP LMA workspaces at a0 = " + std::to_string(laser->a0));
+        return set_err(PTG_ERR_ALLOC, "no room for one block of LP LMA workspaces at a0 = " + std::to_string(a0));
+    int grid = grid_wanted;
     if ((size_t)grid > max_blocks) grid = (int)max_blocks;
-    size_t need = per_warp * warps_per_block * (size_t)grid;
+    size_t need = per_block * (size_t)grid;
     if (need > c->dbw_bytes) {
         cudaFree(c->dbw);
         c->dbw = nullptr;
@@ -736,20 +794,18 @@ static ptg_status ensure_dbw(ptg_ctx* c, const ptg_laser_desc* laser, WaveArgs* 
         }
         c->dbw_bytes = need;
     }
-    a->dbw = (double*)c->dbw;
-    a->db_cap = cap;
-    c->grid_cap = grid;
+    *ws = (double*)c->dbw;
+    *cap_out = cap;
+    *grid_out = grid;
     return PTG_OK;
 }
 
-// Runs a batch whose primaries are described by device pointers `d_in`.
-static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
-                            const ptg_particles* d_in, uint64_t seed, uint64_t id_base, ptg_run_stats* stats) {
+// The option checks of main.rs:339-400 for one laser; loads the LMA tables
+// when the model needs them.
+static ptg_status check_run(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o) {
     ptg_status st = check_laser(laser);
     if (st != PTG_OK) return st;
     if (!o) return set_err(PTG_ERR_INVALID_ARGUMENT, "options is NULL");
-    if (!d_in || !d_in->species || !d_in->r || !d_in->u)
-        return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
     bool lcfa = laser->model == PTG_FAST_PLANE_WAVE || laser->model == PTG_FAST_FOCUSED_LASER;
     if (o->gaunt_factor && !lcfa)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "Gaunt factor correction is only available under the LCFA");
@@ -760,33 +816,49 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
         st = ptg_load_tables(c, nullptr);
         if (st != PTG_OK) return st;
     }
+    return PTG_OK;
+}
+
+// StepOptions from the collision options (dt is set per laser).
+static void fill_step_options(const ptg_collide_options& o, StepOptions* so) {
+    so->t_stop = o.t_stop;
+    so->has_t_stop = std::isfinite(o.t_stop) ? 1 : 0;
+    so->rate_increase = o.rate_increase;
+    so->eqn = (o.classical && o.rr) ? (o.gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
+    so->classical_mode = o.classical && !o.gaunt_factor;
+    so->classical = o.classical;
+    so->electron_recoils = !o.classical && o.rr;
+    so->tracking_photons = o.tracking_photons;
+    so->pol_resolved = o.pol_resolved;
+    so->rotate_stokes = o.rotate_stokes_pars;
+    so->tracking_secondaries = o.tracking_secondaries;
+    so->max_generation = o.max_generation;
+    so->keep_decayed = o.keep_decayed_photons;
+}
+
+// Runs a batch whose primaries are described by device pointers `d_in`.
+static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
+                            const ptg_particles* d_in, uint64_t seed, uint64_t id_base, ptg_run_stats* stats) {
+    ptg_status st = check_run(c, laser, o);
+    if (st != PTG_OK) return st;
+    if (!d_in || !d_in->species || !d_in->r || !d_in->u)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
+    bool lcfa = laser->model == PTG_FAST_PLANE_WAVE || laser->model == PTG_FAST_FOCUSED_LASER;
     CUDA_TRY(cudaSetDevice(c->device));
     unsigned long long n = d_in->n;
     double dt_max;
     FieldParams f = make_field(*laser, &dt_max);
     WaveArgs a{};
     a.f = f;
+    fill_step_options(*o, &a.o);
     a.o.dt = dt_max * o->dt_multiplier;
-    a.o.t_stop = o->t_stop;
-    a.o.has_t_stop = std::isfinite(o->t_stop) ? 1 : 0;
-    a.o.rate_increase = o->rate_increase;
-    a.o.eqn = (o->classical && o->rr) ? (o->gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
-    a.o.classical_mode = o->classical && !o->gaunt_factor;
-    a.o.classical = o->classical;
-    a.o.electron_recoils = !o->classical && o->rr;
-    a.o.tracking_photons = o->tracking_photons;
-    a.o.pol_resolved = o->pol_resolved;
-    a.o.rotate_stokes = o->rotate_stokes_pars;
-    a.o.tracking_secondaries = o->tracking_secondaries;
-    a.o.max_generation = o->max_generation;
-    a.o.keep_decayed = o->keep_decayed_photons;
     a.gl = c->gl;
     a.lma = c->lma_dev;
     a.dbw = nullptr;
     a.db_cap = 0;
     c->grid_cap = 0;
     if (!lcfa && laser->polarization != PTG_POL_CIRCULAR) {
-        st = ensure_dbw(c, laser, &a);
+        st = ensure_dbw(c, laser->a0, grid_for(c, wave_kernel(laser->model)), &a.dbw, &a.db_cap, &c->grid_cap);
         if (st != PTG_OK) return st;
     }
     a.seed = seed;
@@ -836,7 +908,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
         unsigned long long total = hi;
         st = ensure_out(c, total > 0 ? total : 1);
         if (st != PTG_OK) return st;
-        FilterArgs fa;
+        FilterArgs fa{};
         fa.s = c->s;
         fa.init_u = c->init_u;
         fa.shower_count = c->shower_count;
@@ -918,18 +990,10 @@ static ptg_status stage_primaries(ptg_ctx* c, const ptg_particles* h) {
     return PTG_OK;
 }
 
-ptg_status ptg_collide_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
-                             const ptg_particles* primaries, uint64_t seed, uint64_t id_base, ptg_particles* out,
-                             ptg_run_stats* stats) {
-    if (!c || !primaries || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
-    CUDA_TRY(cudaSetDevice(c->device));
-    ptg_status st = stage_primaries(c, primaries);
-    if (st != PTG_OK) return st;
-    ptg_particles din = c->d_in;
-    // restore carved pointers for the next staging (optional fields may be NULL now)
-    carve_particles(&c->d_in, c->in_mem, c->in_cap);
-    st = run_batch(c, laser, o, &din, seed, id_base, stats);
-    if (st != PTG_OK) return st;
+// Copies the context's device output (c->d_out, c->d_out.n rows) into
+// newly allocated host arrays (freed by ptg_particles_free); the copies are
+// queued on the context's stream and not waited for.
+static ptg_status download_output(ptg_ctx* c, ptg_particles* out) {
     size_t m = c->d_out.n;
     std::memset(out, 0, sizeof(*out));
     out->n = m;
@@ -982,12 +1046,462 @@ ptg_status ptg_collide_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_
         CUDA_TRY(down(out->flags, d.flags, 4 * m));
         CUDA_TRY(down(out->status, d.status, 4 * m));
     }
+    return PTG_OK;
+}
+
+ptg_status ptg_collide_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
+                             const ptg_particles* primaries, uint64_t seed, uint64_t id_base, ptg_particles* out,
+                             ptg_run_stats* stats) {
+    if (!c || !primaries || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    ptg_status st = stage_primaries(c, primaries);
+    if (st != PTG_OK) return st;
+    ptg_particles din = c->d_in;
+    // restore carved pointers for the next staging (optional fields may be NULL now)
+    carve_particles(&c->d_in, c->in_mem, c->in_cap);
+    st = run_batch(c, laser, o, &din, seed, id_base, stats);
+    if (st != PTG_OK) return st;
+    st = download_output(c, out);
+    if (st != PTG_OK) return st;
+    size_t m = c->d_out.n;
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     if (stats) {
         double sum = 0.0;
         for (size_t i = 0; i < m; ++i) sum += out->work[i];
         stats->absorbed_energy = sum * ELECTRON_MASS_MEV;
     }
+    return PTG_OK;
+}
+
+
+// ------------------------------------------------ multi-collision queue ---
+// Slot i of a multi batch belongs to collision c with off[c] <= i < off[c+1];
+// its source row is first[c] + (i - off[c]).
+__device__ __forceinline__ int coll_of(const unsigned long long* off, int n_coll, unsigned long long i) {
+    int lo = 0, hi = n_coll;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_queue_reset(Counters* c, CollStats* st, int n_coll, unsigned long long n) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        *c = Counters{};
+        c->n_total = n;
+    }
+    if (t < n_coll) st[t] = CollStats{};
+}
+
+__global__ void k_load_multi(Store s, ptg_particles in, unsigned long long n, const unsigned long long* off,
+                             const unsigned long long* first, const CollParams* cp, int n_coll, double* init_u,
+                             unsigned long long* shower_count) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = coll_of(off, n_coll, i);
+    unsigned long long loc = i - off[c];
+    load_primary(s, in, first[c] + loc, i, loc, primary_stream(cp[c].id_base + loc), init_u, shower_count);
+    s.coll[i] = c;
+    s.ready[i] = 1u;
+}
+
+// Per-collision output counts and created secondaries; warp-aggregated over
+// lanes of the same collision.
+__global__ void k_multi_count(FilterArgs fa, CollStats* st, unsigned long long n_prim) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool in = in_range(fa, i);
+    int c = in ? fa.s.coll[i] : -1;
+    bool keep = in && final_keep(fa, i);
+    bool created = in && i >= n_prim;
+    unsigned peers = __match_any_sync(0xffffffffu, c);
+    unsigned nk = __popc(__ballot_sync(0xffffffffu, keep) & peers);
+    unsigned nc = __popc(__ballot_sync(0xffffffffu, created) & peers);
+    if (in && (threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1)) {
+        if (nk) atomicAdd(&st[c].n_out, (unsigned long long)nk);
+        if (nc) atomicAdd(&st[c].n_created, (unsigned long long)nc);
+    }
+}
+
+__global__ void k_multi_scan(CollStats* st, int n_coll, unsigned long long* out_off, unsigned long long* cursor,
+                             Counters* c) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long acc = 0;
+    for (int k = 0; k < n_coll; ++k) {
+        out_off[k] = acc;
+        cursor[k] = acc;
+        acc += st[k].n_out;
+    }
+    out_off[n_coll] = acc;
+    c->n_out = acc;
+}
+
+__global__ void k_multi_compact(FilterArgs fa, unsigned long long* cursor, ptg_particles o, unsigned long long out_cap) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    bool keep = in_range(fa, i) && final_keep(fa, i);
+    int c = keep ? fa.s.coll[i] : -1;
+    unsigned peers = __match_any_sync(0xffffffffu, c);
+    unsigned keepers = __ballot_sync(0xffffffffu, keep) & peers;
+    if (!keep) return;
+    unsigned lane = threadIdx.x & 31u;
+    unsigned leader = __ffs(keepers) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&cursor[c], (unsigned long long)__popc(keepers));
+    base = __shfl_sync(keepers, base, leader);
+    unsigned long long j = base + __popc(keepers & ((1u << lane) - 1u));
+    if (j < out_cap) write_row(o, j, fa.s, i);
+}
+
+static ptg_status ensure_queue_arrays(ptg_ctx* c, size_t n_coll) {
+    if (c->q_cap >= n_coll) return PTG_OK;
+    size_t k = std::max<size_t>(n_coll, 64);
+    cudaFree(c->d_coll), cudaFree(c->d_cstats), cudaFree(c->d_qoff), cudaFree(c->d_qfirst), cudaFree(c->d_qout),
+        cudaFree(c->d_qcursor);
+    cudaFreeHost(c->h_coll), cudaFreeHost(c->h_cstats), cudaFreeHost(c->h_qoff), cudaFreeHost(c->h_qfirst),
+        cudaFreeHost(c->h_qout);
+    c->q_cap = 0;
+    if (c->q_graph) {
+        cudaGraphExecDestroy(c->q_graph);
+        c->q_graph = nullptr;
+        c->q_graph_key.clear();
+    }
+    CUDA_TRY(cudaMalloc(&c->d_coll, sizeof(CollParams) * k));
+    CUDA_TRY(cudaMalloc(&c->d_cstats, sizeof(CollStats) * k));
+    CUDA_TRY(cudaMalloc(&c->d_qoff, 8 * (k + 1)));
+    CUDA_TRY(cudaMalloc(&c->d_qfirst, 8 * k));
+    CUDA_TRY(cudaMalloc(&c->d_qout, 8 * (k + 1)));
+    CUDA_TRY(cudaMalloc(&c->d_qcursor, 8 * k));
+    CUDA_TRY(cudaMallocHost(&c->h_coll, sizeof(CollParams) * k));
+    CUDA_TRY(cudaMallocHost(&c->h_cstats, sizeof(CollStats) * k));
+    CUDA_TRY(cudaMallocHost(&c->h_qoff, 8 * (k + 1)));
+    CUDA_TRY(cudaMallocHost(&c->h_qfirst, 8 * k));
+    CUDA_TRY(cudaMallocHost(&c->h_qout, 8 * (k + 1)));
+    c->q_cap = k;
+    return PTG_OK;
+}
+
+static const void* queue_kernel_of(int variant) { return variant == 1 ? queue_kernel_v1() : queue_kernel_v0(); }
+
+// Blocks of the queue kernel for a launch shape.
+static int queue_grid(ptg_ctx* c, const ptg_queue_cfg& q) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, queue_kernel_of(q.variant), 128, 0);
+    if (occ <= 0) occ = 1;
+    int per_sm = q.blocks_per_sm > 0 ? std::min(q.blocks_per_sm, occ) : occ;
+    return per_sm * c->num_sms;
+}
+
+// The device sequence of one multi batch, on c->stream: reset, load,
+// persistent queue kernel, per-collision counts, offsets and compaction,
+// and the read-back of the counters into pinned memory.  Captured once per
+// shape as a CUDA graph when cfg.use_graph is set.
+static cudaError_t enqueue_multi(ptg_ctx* c, const QueueArgs& q, const ptg_particles& d_in, unsigned long long n,
+                                 size_t n_coll, int grid, int variant, const FilterArgs& fa_proto, bool capturing) {
+    cudaStream_t s = c->stream;
+    cudaError_t e;
+    // under capture, external event records become graph nodes that record
+    // at replay
+    unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if ((e = cudaEventRecordWithFlags(c->ev0, s, evf)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c->d_coll, c->h_coll, sizeof(CollParams) * n_coll, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(c->d_qoff, c->h_qoff, 8 * (n_coll + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c->d_qfirst, c->h_qfirst, 8 * n_coll, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+    k_queue_reset<<<(unsigned)((n_coll + 255) / 256) + 1, 256, 0, s>>>(c->counters, c->d_cstats, (int)n_coll, n);
+    if ((e = cudaMemsetAsync(c->s.ready, 0, 4 * c->s.cap, s)) != cudaSuccess) return e;
+    if (n > 0)
+        k_load_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c->s, d_in, n, c->d_qoff, c->d_qfirst, c->d_coll,
+                                                                  (int)n_coll, c->init_u, c->shower_count);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = variant == 1 ? launch_queue_v1(grid, s, q) : launch_queue_v0(grid, s, q);
+    if (e != cudaSuccess) return e;
+    // compaction over every reserved slot that fits the store (an overflowed
+    // batch is rerun, so its output is never read)
+    FilterArgs fa = fa_proto;
+    fa.n = c->s.cap;
+    fa.n_live = &c->counters->n_total;
+    unsigned blocks = (unsigned)((c->s.cap + 255) / 256);
+    if (fa.multiplicity >= 0) k_filter_count<<<blocks, 256, 0, s>>>(fa);
+    k_multi_count<<<blocks, 256, 0, s>>>(fa, c->d_cstats, n);
+    k_multi_scan<<<1, 32, 0, s>>>(c->d_cstats, (int)n_coll, c->d_qout, c->d_qcursor, c->counters);
+    k_multi_compact<<<blocks, 256, 0, s>>>(fa, c->d_qcursor, c->d_out, c->out_cap);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaEventRecordWithFlags(c->ev1, s, evf)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c->h_counters, c->counters, sizeof(Counters), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(c->h_cstats, c->d_cstats, sizeof(CollStats) * n_coll, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return e;
+    return cudaMemcpyAsync(c->h_qout, c->d_qout, 8 * (n_coll + 1), cudaMemcpyDeviceToHost, s);
+}
+
+// Runs a multi batch with device primaries.  On return c->d_out holds the
+// output rows (grouped by collision) and c->h_qout their offsets.
+static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll, const ptg_collide_options* o,
+                            const ptg_particles* d_in, const ptg_queue_cfg& qc, ptg_run_stats* stats,
+                            ptg_run_stats* total) {
+    if (!c || !coll || !o || !d_in) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n_coll == 0 || n_coll > (1u << 20)) return set_err(PTG_ERR_INVALID_ARGUMENT, "number of collisions out of range");
+    if (!d_in->species || !d_in->r || !d_in->u)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
+    if (qc.variant < 0 || qc.variant > 1 || qc.chunk < 1 || qc.chunk > 64 || qc.blocks_per_sm < 0)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaGetLastError();  // no stale error may reach the capture below
+    double lp_lma_a0 = 0.0;
+    bool any_lp_lma = false;
+    unsigned long long n = 0;
+    for (size_t k = 0; k < n_coll; ++k) {
+        ptg_status st = check_run(c, &coll[k].laser, o);
+        if (st != PTG_OK) return set_err(st, "collision " + std::to_string(k) + ": " + g_last_error);
+        if (coll[k].first + coll[k].count > d_in->n || coll[k].first + coll[k].count < coll[k].first)
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "collision " + std::to_string(k) + " reads past the primaries");
+        bool lcfa = coll[k].laser.model == PTG_FAST_PLANE_WAVE || coll[k].laser.model == PTG_FAST_FOCUSED_LASER;
+        if (!lcfa && coll[k].laser.polarization != PTG_POL_CIRCULAR) {
+            any_lp_lma = true;
+            lp_lma_a0 = std::max(lp_lma_a0, coll[k].laser.a0);
+        }
+        n += coll[k].count;
+    }
+    ptg_status st = ensure_queue_arrays(c, n_coll);
+    if (st != PTG_OK) return st;
+    st = ensure_init(c, n > 0 ? n : 1);
+    if (st != PTG_OK) return st;
+    // per-collision parameters into the pinned mirrors (read by the copies
+    // at the head of the sequence)
+    c->h_qoff[0] = 0;
+    for (size_t k = 0; k < n_coll; ++k) {
+        double dt_max;
+        CollParams& cp = c->h_coll[k];
+        cp = CollParams{};
+        cp.f = make_field(coll[k].laser, &dt_max);
+        cp.dt = dt_max * o->dt_multiplier;
+        cp.seed = coll[k].seed;
+        cp.id_base = coll[k].id_base;
+        c->h_qfirst[k] = coll[k].first;
+        c->h_qoff[k + 1] = c->h_qoff[k] + coll[k].count;
+    }
+    int grid = queue_grid(c, qc);
+    QueueArgs q{};
+    fill_step_options(*o, &q.base.o);
+    q.base.gl = c->gl;
+    q.base.lma = c->lma_dev;
+    q.base.n_primaries = n;
+    q.coll = c->d_coll;
+    q.stats = c->d_cstats;
+    q.n_coll = (int)n_coll;
+    q.chunk = qc.chunk;
+    // longest wait any lane may legitimately see: the drain of the batch's
+    // last showers; generous, but bounded
+    q.wait_ns = (unsigned long long)(20.0e9 + 2.0e3 * (double)n);
+    if (any_lp_lma) {
+        st = ensure_dbw(c, lp_lma_a0, grid, &q.base.dbw, &q.base.db_cap, &grid);
+        if (st != PTG_OK) return st;
+    }
+    unsigned long long want = c->cap;
+    if (want < 4 * n + 1024) want = 4 * n + 1024;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        st = ensure_store(c, want);
+        if (st != PTG_OK) return st;
+        st = ensure_out(c, c->cap);
+        if (st != PTG_OK) return st;
+        q.base.s = c->s;
+        q.base.c = c->counters;
+        FilterArgs fa{};
+        fa.s = c->s;
+        fa.init_u = c->init_u;
+        fa.shower_count = c->shower_count;
+        fa.min_energy = o->min_energy;
+        fa.cos_max_angle = std::cos(o->max_angle);
+        fa.discard_bg_e = o->discard_bg_e;
+        fa.discard_bg_ph = o->discard_bg_ph;
+        fa.multiplicity = o->multiplicity;
+        if (qc.use_graph) {
+            char key[512];
+            std::snprintf(key, sizeof key, "%llu/%zu/%llu/%llu/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%d/%p/%d", n, n_coll,
+                          c->s.cap, c->out_cap, grid, qc.variant, qc.chunk, (void*)d_in->species, (void*)d_in->r,
+                          (void*)d_in->u, (void*)d_in->pol, (void*)d_in->weight, (void*)d_in->id, (void*)d_in->r0,
+                          (void*)d_in->u0, q.base.db_cap, (void*)q.base.dbw, (int)sizeof(StepOptions));
+            std::string k = key;
+            k.append((const char*)&q.base.o, sizeof(StepOptions));
+            k.append((const char*)&fa.min_energy, 2 * sizeof(double));
+            k.append((const char*)&fa.discard_bg_e, 3 * sizeof(int));
+            if (!c->q_graph || k != c->q_graph_key) {
+                if (c->q_graph) cudaGraphExecDestroy(c->q_graph);
+                c->q_graph = nullptr;
+                c->q_graph_key.clear();
+                cudaGraph_t g = nullptr;
+                CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = enqueue_multi(c, q, *d_in, n, n_coll, grid, qc.variant, fa, true);
+                cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+                if (e != cudaSuccess || e2 != cudaSuccess) {
+                    if (g) cudaGraphDestroy(g);
+                    cudaGetLastError();
+                    return set_err(PTG_ERR_CUDA, std::string("graph capture of the queue batch: ") +
+                                                     cudaGetErrorString(e != cudaSuccess ? e : e2));
+                }
+                cudaError_t e3 = cudaGraphInstantiate(&c->q_graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e3 != cudaSuccess) {
+                    c->q_graph = nullptr;
+                    return set_err(PTG_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(e3));
+                }
+                c->q_graph_key = k;
+            }
+            CUDA_TRY(cudaGraphLaunch(c->q_graph, c->stream));
+        } else {
+            CUDA_TRY(enqueue_multi(c, q, *d_in, n, n_coll, grid, qc.variant, fa, false));
+        }
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        const Counters& h = *c->h_counters;
+        if (h.overflow) {
+            want = 2 * (h.n_total > want ? h.n_total : want);
+            continue;
+        }
+        if (h.timeouts) return set_err(PTG_ERR_TIMEOUT, "queue kernel: a bounded wait ran out");
+        if (h.completed != h.n_total)
+            return set_err(PTG_ERR_TIMEOUT, "queue kernel finished with " + std::to_string(h.n_total - h.completed) +
+                                                " slots unprocessed");
+        c->d_out.n = h.n_out;
+        float ms = 0.0f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        if (total) std::memset(total, 0, sizeof(*total));
+        for (size_t k = 0; k < n_coll; ++k) {
+            const CollStats& cs = c->h_cstats[k];
+            ptg_run_stats r{};
+            r.n_primaries = coll[k].count;
+            r.n_out = cs.n_out;
+            r.n_created = coll[k].count + cs.n_created;
+            r.lepton_steps = cs.lepton_steps;
+            r.photon_steps = cs.photon_steps;
+            r.emissions = cs.emissions;
+            r.pair_events = cs.pair_events;
+            r.rejections = cs.rejections;
+            r.particle_errors = cs.errors;
+            r.waves = (uint32_t)(attempt + 1);  // queue launches, reruns after an overflow included
+            r.device_ms = ms;
+            if (stats) stats[k] = r;
+            if (total) {
+                total->n_primaries += r.n_primaries;
+                total->n_out += r.n_out;
+                total->n_created += r.n_created;
+                total->lepton_steps += r.lepton_steps;
+                total->photon_steps += r.photon_steps;
+                total->emissions += r.emissions;
+                total->pair_events += r.pair_events;
+                total->rejections += r.rejections;
+                total->particle_errors += r.particle_errors;
+            }
+        }
+        if (total) {
+            total->particle_errors += h.errors;
+            total->waves = (uint32_t)(attempt + 1);
+            total->device_ms = ms;
+        }
+        return PTG_OK;
+    }
+    return set_err(PTG_ERR_QUEUE_OVERFLOW, "shower store kept overflowing");
+}
+
+ptg_status ptg_collide_multi_device(ptg_ctx* c, size_t n_coll, const ptg_collision* coll,
+                                    const ptg_collide_options* o, const ptg_particles* d_primaries,
+                                    ptg_particles* d_out, uint64_t* out_offsets, ptg_run_stats* stats,
+                                    ptg_run_stats* total) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    ptg_status st = run_multi(c, n_coll, coll, o, d_primaries, c->qcfg, stats, total);
+    if (st != PTG_OK) return st;
+    if (d_out) *d_out = c->d_out;
+    if (out_offsets)
+        for (size_t k = 0; k <= n_coll; ++k) out_offsets[k] = c->h_qout[k];
+    return PTG_OK;
+}
+
+ptg_status ptg_collide_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll, const ptg_collide_options* o,
+                             const ptg_particles* primaries, ptg_particles* out, uint64_t* out_offsets,
+                             ptg_run_stats* stats, ptg_run_stats* total) {
+    if (!c || !primaries || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    ptg_status st = stage_primaries(c, primaries);
+    if (st != PTG_OK) return st;
+    ptg_particles din = c->d_in;
+    carve_particles(&c->d_in, c->in_mem, c->in_cap);
+    st = run_multi(c, n_coll, coll, o, &din, c->qcfg, stats, total);
+    if (st != PTG_OK) return st;
+    st = download_output(c, out);
+    if (st != PTG_OK) return st;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (out_offsets)
+        for (size_t k = 0; k <= n_coll; ++k) out_offsets[k] = c->h_qout[k];
+    // absorbed energy per collision, from the downloaded work column
+    for (size_t k = 0; k < n_coll; ++k) {
+        double sum = 0.0;
+        for (uint64_t i = c->h_qout[k]; i < c->h_qout[k + 1]; ++i) sum += out->work[i];
+        if (stats) stats[k].absorbed_energy = sum * ELECTRON_MASS_MEV;
+        if (total) total->absorbed_energy += sum * ELECTRON_MASS_MEV;
+    }
+    return PTG_OK;
+}
+
+ptg_status ptg_queue_config(ptg_ctx* c, const ptg_queue_cfg* cfg, ptg_queue_cfg* cfg_out) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (cfg) {
+        if (cfg->variant < 0 || cfg->variant > 1 || cfg->chunk < 1 || cfg->chunk > 64 || cfg->blocks_per_sm < 0)
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
+        c->qcfg = *cfg;
+    }
+    if (cfg_out) *cfg_out = c->qcfg;
+    return PTG_OK;
+}
+
+// The autotuner: every candidate shape runs the sample batch once to warm
+// up (and to size the store), then twice timed with the batch's device
+// events; the fastest mean is kept.
+ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* coll, const ptg_collide_options* o,
+                              const ptg_particles* d_primaries, double sample_fraction, ptg_queue_cfg* best,
+                              double* best_ms) {
+    if (!c || !coll || !o || !d_primaries) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!(sample_fraction > 0.0 && sample_fraction <= 1.0))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "sample_fraction must lie in (0, 1]");
+    std::vector<ptg_collision> sample(coll, coll + n_coll);
+    for (auto& s : sample) {
+        uint64_t m = (uint64_t)std::ceil(sample_fraction * (double)s.count);
+        s.count = std::min<uint64_t>(s.count, std::max<uint64_t>(m, 1));
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    int occ[2] = {0, 0};
+    for (int v = 0; v < 2; ++v) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], queue_kernel_of(v), 128, 0);
+        if (occ[v] < 1) occ[v] = 1;
+    }
+    std::vector<ptg_queue_cfg> cands;
+    for (int v = 0; v < 2; ++v)
+        for (int bps : {occ[v], occ[v] > 1 ? occ[v] - 1 : 0})
+            for (int chunk : {1, 2, 4})
+                if (bps > 0) cands.push_back(ptg_queue_cfg{v, bps, chunk, 1});
+    double best_t = 1e300;
+    ptg_queue_cfg best_c = c->qcfg;
+    for (const auto& cand : cands) {
+        ptg_status st = run_multi(c, n_coll, sample.data(), o, d_primaries, cand, nullptr, nullptr);
+        if (st != PTG_OK) return st;
+        double t = 0.0;
+        for (int rep = 0; rep < 2; ++rep) {
+            ptg_run_stats tot{};
+            st = run_multi(c, n_coll, sample.data(), o, d_primaries, cand, nullptr, &tot);
+            if (st != PTG_OK) return st;
+            t += tot.device_ms;
+        }
+        t *= 0.5;
+        if (t < best_t) {
+            best_t = t;
+            best_c = cand;
+        }
+    }
+    c->qcfg = best_c;
+    if (best) *best = best_c;
+    if (best_ms) *best_ms = best_t;
     return PTG_OK;
 }
 
@@ -1156,6 +1670,85 @@ ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_pa
 // lacks nonlinear_compton/cp/tables/cdf.rs; its generator is
 // nonlinear_compton/cp/mod.rs:472-612).  Grid: a = 0.02 * 10^(j/20),
 // j < 61; eta = 1e-3 * 10^(i/20), i < 70; n_max = 10 (1 + a^3).
+namespace ptg {
+
+// -------------------------------------------------- table regeneration --
+// The CP harmonic CDF table (nonlinear_compton/cp/tables/cdf.rs) is not in
+// the reference tree; its generator is nonlinear_compton/cp/mod.rs:472-612.
+// Pass 1: one thread per (grid point, harmonic) computes the partial rate.
+struct RegenChunk {
+    int point;     // grid point index (eta row * 61 + a column)
+    int n0;        // first harmonic of this block
+};
+
+__global__ void k_regen_cp_partial(const RegenChunk* chunks, const double* a_of, const double* eta_of,
+                                   const int* nmax_of, const unsigned long long* offset_of, double* rates) {
+    RegenChunk ch = chunks[blockIdx.x];
+    int n = ch.n0 + (int)threadIdx.x;
+    if (n > nmax_of[ch.point]) return;
+    double a = a_of[ch.point], eta = eta_of[ch.point];
+    rates[offset_of[ch.point] + (n - 1)] = cp_partial_rate(n, a, eta);
+}
+
+// Pass 2: one thread per grid point: the cumulative sum in harmonic order
+// and the 32 CDF nodes of the reference's generator.
+__global__ void k_regen_cp_cdf(int npoints, const int* nmax_of, const unsigned long long* offset_of, const double* rates,
+                               double* cum /* [sum nmax][2] */, double* cdf_out /* [npoints][32][2] */,
+                               double* total_out /* [npoints] */) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npoints) return;
+    int n_max = nmax_of[p];
+    const double* r = rates + offset_of[p];
+    double* c = cum + 2 * offset_of[p];
+    double cs = 0.0;
+    for (int n = 1; n <= n_max; ++n) {
+        cs = cs + r[n - 1];
+        c[2 * (n - 1)] = (double)n;
+        c[2 * (n - 1) + 1] = cs;
+    }
+    double rate = cs;
+    double* out = cdf_out + (size_t)p * 64;
+    out[0] = c[0];
+    out[1] = c[1] / rate;
+    double limit = c[2 * (n_max - 1)];
+    if (n_max <= 32) {
+        for (int i = 1; i <= 31; ++i) {
+            if (i < n_max) {
+                out[2 * i] = c[2 * i];
+                out[2 * i + 1] = c[2 * i + 1] / rate;
+            } else {
+                out[2 * i] = (double)(i + 1);
+                out[2 * i + 1] = 1.0;
+            }
+        }
+    } else if (n_max < 100) {
+        for (int i = 1; i <= 7; ++i) {
+            out[2 * i] = c[2 * i];
+            out[2 * i + 1] = c[2 * i + 1] / rate;
+        }
+        double delta = (log((double)n_max) - log(9.0)) / (31.0 - 8.0);
+        for (int i = 8; i <= 31; ++i) {
+            double n = fmin(exp(log(9.0) + (double)(i - 8) * delta), limit);
+            double v = 0.0;
+            pw_evaluate(c, n_max, false, n, &v);
+            out[2 * i] = n;
+            out[2 * i + 1] = v / rate;
+        }
+    } else {
+        double delta = log((double)n_max) / 31.0;
+        for (int i = 1; i <= 31; ++i) {
+            double n = fmin(exp((double)i * delta), limit);
+            double v = 0.0;
+            pw_evaluate(c, n_max, false, n, &v);
+            out[2 * i] = n;
+            out[2 * i + 1] = v / rate;
+        }
+    }
+    total_out[p] = rate;
+}
+
+}  // namespace ptg
+
 ptg_status ptg_regen_nlc_cp_cdf(ptg_ctx* c, double* cdf_out, double* total_out) {
     if (!c || !cdf_out || !total_out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     CUDA_TRY(cudaSetDevice(c->device));
@@ -1225,7 +1818,7 @@ namespace {
 constexpr unsigned long long NOALLOC_MAX_PRIMARIES = 4096;
 constexpr unsigned long long NOALLOC_MAX_PARTICLES = 32768;  // shower store, primaries included
 constexpr size_t noalloc_align(size_t b) { return (b + 255) & ~(size_t)255; }
-constexpr size_t NOALLOC_STORE_BYTES = (size_t)(5 * 32 + 5 * 8 + 4 * 8 + 4 * 4) * NOALLOC_MAX_PARTICLES + 18 * 256;
+constexpr size_t NOALLOC_STORE_BYTES = store_bytes(NOALLOC_MAX_PARTICLES);
 constexpr size_t NOALLOC_OFF_COUNTERS = NOALLOC_STORE_BYTES;
 constexpr size_t NOALLOC_OFF_INIT_U = NOALLOC_OFF_COUNTERS + noalloc_align(sizeof(Counters));
 constexpr size_t NOALLOC_OFF_COUNTS = NOALLOC_OFF_INIT_U + noalloc_align(32 * NOALLOC_MAX_PRIMARIES);
@@ -1277,14 +1870,12 @@ __global__ void k_noalloc_reset(Counters* c, unsigned long long n) {
     }
 }
 
-template <int MODEL>
 static cudaError_t noalloc_wave(const WaveArgs& a, int grid_max, cudaStream_t s) {
     unsigned long long n = a.hi - a.lo;
     unsigned long long need = (n + 127) / 128;
     int grid = (unsigned long long)grid_max > need ? (int)need : grid_max;
     if (grid < 1) grid = 1;
-    collide_wave<MODEL><<<grid, 128, 0, s>>>(a);
-    return cudaGetLastError();
+    return launch_wave_lcfa(a.f.model, grid, s, a);
 }
 
 ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* o,
@@ -1349,8 +1940,7 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
     a.seed = seed;
     a.n_primaries = n;
     a.id_base = id_base;
-    const void* kern = laser->model == PTG_FAST_PLANE_WAVE ? (const void*)collide_wave<M_FAST_PLANE_WAVE>
-                                                           : (const void*)collide_wave<M_FAST_FOCUSED_LASER>;
+    const void* kern = wave_kernel_lcfa(laser->model);
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0));
     int grid_max = (per_sm > 0 ? per_sm : 1) * sms;
 
@@ -1368,8 +1958,7 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
         a.lo = lo;
         a.hi = hi;
         CUDA_TRY(cudaMemsetAsync(&counters->next, 0, 8, s));
-        CUDA_TRY(laser->model == PTG_FAST_PLANE_WAVE ? noalloc_wave<M_FAST_PLANE_WAVE>(a, grid_max, s)
-                                                     : noalloc_wave<M_FAST_FOCUSED_LASER>(a, grid_max, s));
+        CUDA_TRY(noalloc_wave(a, grid_max, s));
         ++waves;
         CUDA_TRY(cudaMemcpyAsync(&h, counters, sizeof(Counters), cudaMemcpyDeviceToHost, s));
         CUDA_TRY(cudaStreamSynchronize(s));
@@ -1380,7 +1969,7 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
         hi = h.n_total;
     }
     unsigned long long total = hi;
-    FilterArgs fa;
+    FilterArgs fa{};
     fa.s = store;
     fa.init_u = init_u;
     fa.shower_count = shower_count;

@@ -25,7 +25,7 @@ __device__ __forceinline__ double series_up_to(const double (*s)[20], double x) 
 }
 
 // special_functions/airy.rs:41-78 (x >= 0)
-__device__ __noinline__ double airy_ai(double x) {
+static __device__ __noinline__ double airy_ai(double x) {
     if (x < 1.0) return series_up_to(PTG_AIRY_SMALL_X, x);
     double s = 2.0 * pow(x, 1.5) / 3.0;
     double a = 0.262183997088323 * pow(s, -1.0 / 6.0) * exp(-s);
@@ -44,7 +44,7 @@ __device__ __noinline__ double airy_ai(double x) {
 }
 
 // special_functions/airy.rs:80-118 (x >= 0)
-__device__ __noinline__ double airy_ai_prime(double x) {
+static __device__ __noinline__ double airy_ai_prime(double x) {
     if (x < 1.0) return series_up_to(PTG_AIRY_PRIME_SMALL_X, x);
     double s = 2.0 * pow(x, 1.5) / 3.0;
     double b = -0.2898380090915846 * pow(s, 1.0 / 6.0) * exp(-s);
@@ -125,7 +125,7 @@ __device__ __forceinline__ double from_linear_cdf_table(double global_zero, doub
 }
 
 // lcfa/photon_emission/classical.rs:24-61
-__device__ __noinline__ void lcfa_classical_sample(double chi, double gamma, double rand1, double rand2,
+static __device__ __noinline__ void lcfa_classical_sample(double chi, double gamma, double rand1, double rand2,
                                                    double rand3, double* omega_mc2, double* theta) {
     double delta = acos((-9.0 + 50.0 * rand2 - 25.0 * (rand2 * rand2)) / 16.0);
     double z = powi((2.0 + 4.0 * cos(delta / 3.0)) / (5.0 * (1.0 - rand2)), 3);
@@ -147,7 +147,7 @@ __device__ __noinline__ void lcfa_classical_sample(double chi, double gamma, dou
 
 // lcfa/photon_emission/mod.rs:80-231.  *theta < 0 encodes the reference's
 // `None` (polar angle would exceed pi).
-__device__ __noinline__ void lcfa_photon_sample(double chi, double gamma, double rand1, double rand2, double rand3,
+static __device__ __noinline__ void lcfa_photon_sample(double chi, double gamma, double rand1, double rand2, double rand3,
                                                 double* omega_mc2, double* theta) {
     double lnchi = log(chi);
     if (lnchi <= PTG_LCFA_PH_LN_CHI_MIN) {
@@ -249,7 +249,7 @@ __device__ __noinline__ void lcfa_photon_sample(double chi, double gamma, double
 
 // lcfa/photon_emission/mod.rs:239-298 (quantum) and classical.rs:70-118.
 // Returns [Q, U, V] with I = 1.
-__device__ __noinline__ d3 lcfa_stokes(d4 k, double chi, double gamma, d3 v, d3 w, bool classical) {
+static __device__ __noinline__ d3 lcfa_stokes(d4 k, double chi, double gamma, d3 v, d3 w, bool classical) {
     v = normalize(v);
     w = normalize(w);
     d3 n = normalize(mk3(k.x, k.y, k.z));
@@ -287,7 +287,7 @@ __device__ __noinline__ d3 lcfa_stokes(d4 k, double chi, double gamma, d3 v, d3 
 }
 
 // lcfa/photon_emission/mod.rs:330-346 (modified Landau-Lifshitz)
-__device__ __noinline__ double gaunt_factor(double chi) {
+static __device__ __noinline__ double gaunt_factor(double chi) {
     if (chi <= 1.0e-3) return 1.0 - 55.0 * SQRT_3 * chi / 16.0 + 48.0 * chi * chi;
     if (chi > 500.0) {
         double c = cbrt(chi);
@@ -416,7 +416,7 @@ __device__ __forceinline__ double lcfa_pair_angular_ceiling(double s, double chi
 
 // lcfa/pair_creation/mod.rs:180-217 with :141-173.  Returns false if a
 // rejection loop reached its cap.
-__device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double chi, d3 a_perp, Draws& rng, const PairGL& gl,
+static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double chi, d3 a_perp, Draws& rng, const PairGL& gl,
                                               double* gamma_p, double* cos_theta, double* phi, uint32_t* rejections) {
     double c2, s2;
     d4 sv = stokes_in_basis(sv_in, a_perp, mk3(ell.x, ell.y, ell.z), &c2, &s2);

@@ -39,7 +39,7 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
 // nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
 // `dbw` is this lane's DoubleBessel workspace (linear polarisation only).
 // Returns a ptg status (0 = ok).
-__device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw, d4 r, d4 u,
+static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw, d4 r, d4 u,
                                         double dt, Draws& rng, bool classical, bool* emitted, d4* k_out, d4* u_prime,
                                         d3* pol, double* a_eff, double* chi, double* absorption, uint32_t* rej) {
     *emitted = false;
@@ -92,7 +92,7 @@ __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t
 
 // plane_wave.rs:284-316 / focused_laser.rs:283-306 with
 // pair_creation::probability and generate (pair_creation/mod.rs:21-110).
-__device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTables& t, d4 r, d4 ell, d4 pol, double dt,
+static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTables& t, d4 r, d4 ell, d4 pol, double dt,
                                             Draws& rng, double rate_increase, double* prob, d4* pol_new,
                                             bool* created, d4* ue, d4* up, double* frac, double* a_eff, double* chi,
                                             double* absorption, uint32_t* rej) {

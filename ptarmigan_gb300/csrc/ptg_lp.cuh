@@ -98,7 +98,7 @@ struct Ssq {
 
 // double_bessel.rs:142-246: J(n-2..n+2, x, y) by recurrence.  Returns false
 // on a workspace too small for n.
-__host__ __device__ __noinline__ bool db_around(const DbGeom& g, const DbWork& w, double x, double y, double j[5]) {
+static __host__ __device__ __noinline__ bool db_around(const DbGeom& g, const DbWork& w, double x, double y, double j[5]) {
     const int len = g.len;
     double* W = w.base;
 #define DBW(e, c) W[((size_t)(e) * 5 + (c)) * 32]
@@ -192,7 +192,7 @@ __host__ __device__ __noinline__ bool db_around(const DbGeom& g, const DbWork& w
 }
 
 // double_bessel.rs:272-355: saddle-point approximation for large order.
-__host__ __device__ __noinline__ double db_spa(int ni, double x, double y) {
+static __host__ __device__ __noinline__ double db_spa(int ni, double x, double y) {
     double n = ni;
     if (n <= -2.0 * y + x) {
         double ct = y > 0.0 ? x / (8.0 * y) - sqrt(x * x / (64.0 * y * y) + 0.5 - n / (4.0 * y)) : n / x;
@@ -252,7 +252,7 @@ __host__ __device__ __forceinline__ bool db_evaluate(const DbGeom& g, const DbWo
 
 // ------------------------------------------------------ LP emission -----
 // nonlinear_compton/lp/mod.rs:21-50.  Returns NaN on a workspace failure.
-__device__ __noinline__ double lp_ddpr(double a, double eta, double s, double theta, const DbGeom& g, const DbWork& w) {
+static __device__ __noinline__ double lp_ddpr(double a, double eta, double s, double theta, const DbGeom& g, const DbWork& w) {
     int n = g.n;
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
     double wn = fmin(s / (sn * (1.0 - s)), 1.0);
@@ -279,7 +279,7 @@ __device__ __forceinline__ int lp_sum_limit(double a, double eta) {
 }
 
 // nonlinear_compton/lp/mod.rs:53-140
-__device__ __noinline__ double lp_ceiling(double a, double eta, const DbGeom& g, const DbWork& w) {
+static __device__ __noinline__ double lp_ceiling(double a, double eta, const DbGeom& g, const DbWork& w) {
     int n = g.n;
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
     double smax = sn / (1.0 + sn);
@@ -343,7 +343,7 @@ struct ThetaBound {
     }
 };
 
-__device__ __noinline__ double ln_double_bessel_x_zero(int ni, double y) {
+static __device__ __noinline__ double ln_double_bessel_x_zero(int ni, double y) {
     double n = ni;
     double z = sqrt(n / (4.0 * y) - 0.5);
     const cxd I{0.0, 1.0};
@@ -356,7 +356,7 @@ __device__ __noinline__ double ln_double_bessel_x_zero(int ni, double y) {
     return log(sqrt(2.0 / (PI * cx_norm(f2)))) + phase.re + log(fabs(cos(phase.im)));
 }
 
-__device__ __noinline__ void theta_bound(int n, double a, double eta, ThetaBound* tb) {
+static __device__ __noinline__ void theta_bound(int n, double a, double eta, ThetaBound* tb) {
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
     for (int i = 0; i < 16; ++i) {
         double z = cos(PI * i / 15.0);
@@ -433,7 +433,7 @@ __device__ __forceinline__ bool lp_rate(const NlcTables& t, double a, double eta
 
 // nonlinear_compton/lp/mod.rs:459-553: one grid corner of the harmonic CDF
 // (16 nodes of [n, cdf]); NaN where the reference's inversion would fail.
-__device__ __noinline__ double lp_cdf_corner(const double* table, double frac, double a) {
+static __device__ __noinline__ double lp_cdf_corner(const double* table, double frac, double a) {
     if (frac <= table[1]) return 0.9;
     double v = 0.0;
     if (a < 5.0) return pw_invert(table, 16, false, frac, &v) ? v : NAN;
@@ -447,7 +447,7 @@ __device__ __noinline__ double lp_cdf_corner(const double* table, double frac, d
 }
 
 // Returns the harmonic order, or -1 if the lookup failed.
-__device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double a, double eta, double frac) {
+static __device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double a, double eta, double frac) {
     const double MIN0 = PTG_NLC_LP_CDF_MIN_0, MIN1 = PTG_NLC_LP_CDF_MIN_1, S0 = PTG_NLC_LP_CDF_STEP_0,
                  S1 = PTG_NLC_LP_CDF_STEP_1;
     const double* T = t.lp_cdf;
@@ -475,7 +475,7 @@ __device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double a, doub
 // nonlinear_compton/lp/mod.rs:586-676: harmonic, s, azimuth theta in
 // [0, 2 pi) and the Stokes vector (in the LMA basis) of the emitted photon.
 // Returns a ptg status.
-__device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w, double a, double eta, Draws& rng,
+static __device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w, double a, double eta, Draws& rng,
                                       int* n_out, double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
     if (t.lp_cdf == nullptr || w.base == nullptr) return 8;  // PTG_ERR_TABLES
     int n = lp_harmonic_index(t, a, eta, rng.next());

@@ -203,7 +203,7 @@ __device__ __forceinline__ bool pw_between(double x, double mn, double mx) {
 
 // pwmci.rs:102-229: inverse quadratic interpolation with secant and
 // bisection fall-backs, at most 32 iterations, relative tolerance 1e-6.
-__device__ __noinline__ bool pw_invert(const double* tb, int len, bool ext, double f, double* out) {
+static __device__ __noinline__ bool pw_invert(const double* tb, int len, bool ext, double f, double* out) {
     int i;
     int loc = pw_locate(tb, len, 1, f, &i);
     if (loc != 0) {

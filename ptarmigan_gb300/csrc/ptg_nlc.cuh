@@ -17,7 +17,7 @@ constexpr double FRAC_PI_4 = 0.78539816339744830962;
 // ------------------------------------------------------------ Bessel ---
 // special_functions/bessel.rs:117-176: (J_{n-1}, J_n, J_{n+1})(x) by Miller's
 // backward recurrence normalised with J_0 + 2 sum J_2k = 1; O(n) work.
-__device__ __noinline__ void triple_j(int n, double x, double* a, double* b, double* c) {
+static __device__ __noinline__ void triple_j(int n, double x, double* a, double* b, double* c) {
     if (x == 0.0) {
         *a = (n == 1) ? 1.0 : 0.0;
         *b = (n == 0) ? 1.0 : 0.0;
@@ -64,7 +64,7 @@ __device__ __noinline__ void triple_j(int n, double x, double* a, double* b, dou
 }
 
 // special_functions/bessel.rs:178-199: uniform asymptotic expansion (n >= 1000)
-__device__ __noinline__ double j_asymptotic(int n, double x) {
+static __device__ __noinline__ double j_asymptotic(int n, double x) {
     double m = (double)n;
     double z = x / m;
     double zeta;
@@ -112,7 +112,7 @@ __device__ __forceinline__ double cp_diff_partial_rate(int n, double a, double e
 }
 
 // nonlinear_compton/cp/mod.rs:42-75
-__device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
+static __device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     int n_switch = (int)(32.3 * (1.0 + 0.476 * pow(a, 1.56)));
     double mx = -HUGE_VAL;
@@ -134,7 +134,7 @@ __device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
 }
 
 // nonlinear_compton/cp/mod.rs:92-136: integral of dW_n/dv over v (GL-32 x 2)
-__device__ __noinline__ double cp_partial_rate(int n, double a, double eta) {
+static __device__ __noinline__ double cp_partial_rate(int n, double a, double eta) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     int n_switch = (int)(32.3 * (1.0 + 0.476 * pow(a, 1.56)));
     double lower = 0.0, upper = 0.0;
@@ -213,7 +213,7 @@ __device__ __forceinline__ bool cp_rate(const NlcTables& t, double a, double eta
 
 // nonlinear_compton/cp/tables/mod.rs:37-121: harmonic index from the CDF
 // table (four grid corners, each inverted in [ln n, ln(-ln(1 - cdf))]).
-__device__ __noinline__ double cp_cdf_corner(const double* table, double frac) {
+static __device__ __noinline__ double cp_cdf_corner(const double* table, double frac) {
     if (frac <= table[1]) return 0.9;
     double rs[62];
     for (int i = 0; i < 31; ++i) {
@@ -226,7 +226,7 @@ __device__ __noinline__ double cp_cdf_corner(const double* table, double frac) {
     return exp(v);
 }
 
-__device__ __noinline__ int cp_invert(const NlcTables& t, double a, double eta, double frac) {
+static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, double eta, double frac) {
     const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
     double la = log(a), le = log(eta);
     if (la <= MIN0) return 1;
@@ -247,7 +247,7 @@ __device__ __noinline__ int cp_invert(const NlcTables& t, double a, double eta, 
 }
 
 // nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
-__device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
+static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
                                       double* theta_out, d3* sv_out, uint32_t* rej) {
     if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
     int n = cp_invert(t, a, eta, rng.next());
@@ -315,7 +315,7 @@ __device__ __forceinline__ d3 stokes_from_lma_basis(d3 sv, d4 k) {
 
 // nonlinear_compton/mod.rs:58-138 for a sampled (n, s, cphi, Stokes):
 // builds k' in the zero-momentum frame and boosts it to the lab.
-__device__ __noinline__ int nlc_kinematics(d4 k, d4 q, double a, double eta, int n, double s, double cphi, d3 sv,
+static __device__ __noinline__ int nlc_kinematics(d4 k, d4 q, double a, double eta, int n, double s, double cphi, d3 sv,
                                            double pol_angle, bool classical, d4* k_out, d3* sv_out) {
     double ell = n;
     double p_zmf = classical ? ell * eta / sqrt(1.0 + a * a) : ell * eta / sqrt(1.0 + a * a + 2.0 * ell * eta);
@@ -358,85 +358,6 @@ __device__ __noinline__ int nlc_kinematics(d4 k, d4 q, double a, double eta, int
     if (!(fabs(s - s_new) / s < 1.0e-2)) return 3;
     *k_out = kprime;
     return 0;
-}
-
-}  // namespace ptg
-
-namespace ptg {
-
-// -------------------------------------------------- table regeneration --
-// The CP harmonic CDF table (nonlinear_compton/cp/tables/cdf.rs) is not in
-// the reference tree; its generator is nonlinear_compton/cp/mod.rs:472-612.
-// Pass 1: one thread per (grid point, harmonic) computes the partial rate.
-struct RegenChunk {
-    int point;     // grid point index (eta row * 61 + a column)
-    int n0;        // first harmonic of this block
-};
-
-__global__ void k_regen_cp_partial(const RegenChunk* chunks, const double* a_of, const double* eta_of,
-                                   const int* nmax_of, const unsigned long long* offset_of, double* rates) {
-    RegenChunk ch = chunks[blockIdx.x];
-    int n = ch.n0 + (int)threadIdx.x;
-    if (n > nmax_of[ch.point]) return;
-    double a = a_of[ch.point], eta = eta_of[ch.point];
-    rates[offset_of[ch.point] + (n - 1)] = cp_partial_rate(n, a, eta);
-}
-
-// Pass 2: one thread per grid point: the cumulative sum in harmonic order
-// and the 32 CDF nodes of the reference's generator.
-__global__ void k_regen_cp_cdf(int npoints, const int* nmax_of, const unsigned long long* offset_of, const double* rates,
-                               double* cum /* [sum nmax][2] */, double* cdf_out /* [npoints][32][2] */,
-                               double* total_out /* [npoints] */) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npoints) return;
-    int n_max = nmax_of[p];
-    const double* r = rates + offset_of[p];
-    double* c = cum + 2 * offset_of[p];
-    double cs = 0.0;
-    for (int n = 1; n <= n_max; ++n) {
-        cs = cs + r[n - 1];
-        c[2 * (n - 1)] = (double)n;
-        c[2 * (n - 1) + 1] = cs;
-    }
-    double rate = cs;
-    double* out = cdf_out + (size_t)p * 64;
-    out[0] = c[0];
-    out[1] = c[1] / rate;
-    double limit = c[2 * (n_max - 1)];
-    if (n_max <= 32) {
-        for (int i = 1; i <= 31; ++i) {
-            if (i < n_max) {
-                out[2 * i] = c[2 * i];
-                out[2 * i + 1] = c[2 * i + 1] / rate;
-            } else {
-                out[2 * i] = (double)(i + 1);
-                out[2 * i + 1] = 1.0;
-            }
-        }
-    } else if (n_max < 100) {
-        for (int i = 1; i <= 7; ++i) {
-            out[2 * i] = c[2 * i];
-            out[2 * i + 1] = c[2 * i + 1] / rate;
-        }
-        double delta = (log((double)n_max) - log(9.0)) / (31.0 - 8.0);
-        for (int i = 8; i <= 31; ++i) {
-            double n = fmin(exp(log(9.0) + (double)(i - 8) * delta), limit);
-            double v = 0.0;
-            pw_evaluate(c, n_max, false, n, &v);
-            out[2 * i] = n;
-            out[2 * i + 1] = v / rate;
-        }
-    } else {
-        double delta = log((double)n_max) / 31.0;
-        for (int i = 1; i <= 31; ++i) {
-            double n = fmin(exp((double)i * delta), limit);
-            double v = 0.0;
-            pw_evaluate(c, n_max, false, n, &v);
-            out[2 * i] = n;
-            out[2 * i + 1] = v / rate;
-        }
-    }
-    total_out[p] = rate;
 }
 
 }  // namespace ptg

@@ -1,0 +1,215 @@
+// Persistent multi-collision work queue: the types shared by the engine and
+// the queue kernel (ptg_queue.cu).
+//
+// Many independent collisions (each with its own laser, time step, seed and
+// primaries) share one shower store.  One launch drains it: every lane takes
+// tickets from a global cursor; ticket t is store slot t.  A slot exists once
+// some lane has reserved it (n_total > t) and is readable once its producer
+// has published it (ready[t] set with release semantics after the data).
+// A lane whose ticket lies beyond n_total waits, bounded in time, until the
+// slot is created or the queue has drained (every reserved slot finished:
+// completed == n_total, read in that order).  Primaries and all generations
+// of secondaries flow through the same queue, so there are no waves and no
+// host round trips inside a batch.
+#pragma once
+#include "ptg_collide.cuh"
+
+namespace ptg {
+
+// Per-collision parameters, read by the lanes when they switch collision.
+struct CollParams {
+    FieldParams f;
+    double dt;                    // max_timestep * dt_multiplier for this laser
+    unsigned long long seed;
+    unsigned long long id_base;   // primary streams: primary_stream(id_base + i)
+};
+
+// Per-collision event counts.
+struct CollStats {
+    unsigned long long lepton_steps, photon_steps, emissions, pair_events, rejections, errors;
+    unsigned long long n_created, n_out;
+};
+
+struct QueueArgs {
+    WaveArgs base;             // store, counters, tables, shared step options
+    const CollParams* coll;    // [n_coll]
+    CollStats* stats;          // [n_coll]
+    int n_coll;
+    int chunk;                 // tickets taken per grab
+    unsigned long long wait_ns;  // bound on any single wait for a slot
+};
+
+
+// ------------------------------------------------------------ kernel ----
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Warp-aggregated grab of `k` consecutive tickets per calling lane.
+__device__ __forceinline__ unsigned long long grab_tickets(Counters* c, unsigned k) {
+    unsigned mask = __activemask();
+    unsigned leader = __ffs(mask) - 1;
+    unsigned rank = __popc(mask & ((1u << lane_id()) - 1u));
+    unsigned long long base = 0;
+    if (lane_id() == leader) base = atomicAdd(&c->next, (unsigned long long)(k * __popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + (unsigned long long)rank * k;
+}
+
+enum { WAIT_TIMEOUT = -1, WAIT_DRAINED = 0, WAIT_READY = 1, WAIT_SKIP = 2 };
+
+// Waits until slot t is published (READY), lies beyond the store (SKIP:
+// its producer retired it), or the queue has drained (DRAINED).  Bounded by
+// `wait_ns` of wall time and by an iteration cap.
+static __device__ __noinline__ int wait_slot(const WaveArgs& a, unsigned long long t, unsigned long long wait_ns) {
+    unsigned long long t0 = global_ns();
+    for (unsigned it = 0; it < (1u << 30); ++it) {
+        unsigned long long n = ld_acquire(&a.c->n_total);
+        if (t < n) {
+            if (t >= a.s.cap) return WAIT_SKIP;
+            for (unsigned jt = 0; jt < (1u << 30); ++jt) {
+                if (ld_acquire(a.s.ready + t)) return WAIT_READY;
+                if ((jt & 63u) == 63u && global_ns() - t0 > wait_ns) return WAIT_TIMEOUT;
+                __nanosleep(32);
+            }
+            return WAIT_TIMEOUT;
+        }
+        unsigned long long done = ld_acquire(&a.c->completed);
+        unsigned long long n2 = ld_acquire(&a.c->n_total);
+        if (done == n2 && t >= n2) return WAIT_DRAINED;
+        if ((it & 15u) == 15u && global_ns() - t0 > wait_ns) return WAIT_TIMEOUT;
+        __nanosleep(256);
+    }
+    return WAIT_TIMEOUT;
+}
+
+struct PartCounts {
+    uint32_t rej, nemit, npair;
+    unsigned long long lsteps, psteps;
+};
+
+// main.rs:134-289 for one particle: steps it until it leaves the field,
+// decays or fails.
+template <int MODEL>
+static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, PartCounts& pc) {
+    for (;;) {
+        bool done;
+        if (L.status != ST_OK || lane_untracked(a, L)) {
+            done = true;
+        } else if (L.species != SP_PHOTON) {
+            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
+            if (!done) {
+                lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
+                ++L.step;
+                ++pc.lsteps;
+                done = L.status != ST_OK;
+            }
+        } else {
+            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
+                     a.o.tracking_photons);
+            if (!done) {
+                photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair);
+                ++L.step;
+                ++pc.psteps;
+                done = L.status != ST_OK;
+            }
+        }
+        if (done) return;
+    }
+}
+
+__device__ __forceinline__ void queue_load(const WaveArgs& a, Lane& L, unsigned long long i) {
+    const Store& s = a.s;
+    L.slot = i;
+    L.r = get4(s.r, s.cap, i);
+    L.u = get4(s.u, s.cap, i);
+    L.pol = get4(s.pol, s.cap, i);
+    L.weight = s.weight[i];
+    L.icount = s.icount[i];
+    L.work = s.work[i];
+    L.stream = s.stream[i];
+    L.id = s.id[i];
+    L.species = s.species[i];
+    L.gen = s.generation[i];
+    L.status = s.status[i];
+    L.flags = s.flags[i];
+    L.coll = s.coll[i];
+    L.step = 0;
+    L.decayed = false;
+}
+
+// Kernel variants: MINB > 1 caps the registers so that MINB blocks of 128
+// threads fit on an SM (the LCFA paths need fewer registers than LMA's).
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
+    WaveArgs a = q.base;
+    int cur = -1;
+    unsigned long long t = 0, t_end = 0;
+    for (;;) {
+        if (t == t_end) {
+            t = grab_tickets(a.c, (unsigned)q.chunk);
+            t_end = t + (unsigned long long)q.chunk;
+        }
+        unsigned long long ticket = t++;
+        int w = wait_slot(a, ticket, q.wait_ns);
+        if (w == WAIT_DRAINED) break;
+        if (w == WAIT_TIMEOUT) {
+            atomicAdd(&a.c->timeouts, 1ull);
+            break;
+        }
+        if (w == WAIT_SKIP) continue;
+        Lane L;
+        queue_load(a, L, ticket);
+        if (L.status == ST_PHANTOM || L.coll < 0 || L.coll >= q.n_coll) {
+            if (L.status != ST_PHANTOM) atomicAdd(&a.c->errors, 1ull);
+            __threadfence();
+            atomicAdd(&a.c->completed, 1ull);
+            continue;
+        }
+        if (L.coll != cur) {
+            const CollParams& cp = q.coll[L.coll];
+            a.f = cp.f;
+            a.o.dt = cp.dt;
+            a.seed = cp.seed;
+            a.id_base = cp.id_base;
+            cur = L.coll;
+        }
+        L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
+        L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
+        PartCounts pc{0, 0, 0, 0, 0};
+        switch (a.f.model) {
+            case M_PLANE_WAVE: run_particle<M_PLANE_WAVE>(a, L, pc); break;
+            case M_FAST_PLANE_WAVE: run_particle<M_FAST_PLANE_WAVE>(a, L, pc); break;
+            case M_FOCUSED_LASER: run_particle<M_FOCUSED_LASER>(a, L, pc); break;
+            default: run_particle<M_FAST_FOCUSED_LASER>(a, L, pc); break;
+        }
+        if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
+        lane_store(a, L);
+        CollStats* cs = q.stats + L.coll;
+        if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
+        if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
+        if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
+        if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
+        if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
+        if (L.status != ST_OK) atomicAdd(&cs->errors, 1ull);
+        // the particle's children were appended and published before this
+        __threadfence();
+        atomicAdd(&a.c->completed, 1ull);
+    }
+}
+
+}  // namespace ptg

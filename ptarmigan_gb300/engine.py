@@ -22,6 +22,7 @@ _EXPORTS = [
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_eval_fields", "ptg_push_steps",
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
+    "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune",
 ]
 
 
@@ -82,6 +83,18 @@ def load(path=None):
     L.ptg_lp_sample.restype = st
     L.ptg_lp_sample.argtypes = [ctxp, C.c_size_t, DP, DP, C.c_uint64, C.POINTER(C.c_uint64), C.c_uint32, DP,
                                 C.POINTER(C.c_int32)]
+    U64P = C.POINTER(C.c_uint64)
+    L.ptg_collide_multi.restype = st
+    L.ptg_collide_multi.argtypes = [ctxp, C.c_size_t, C.POINTER(abi.Collision), C.POINTER(abi.CollideOptions),
+                                    C.POINTER(abi.Particles), C.POINTER(abi.Particles), U64P,
+                                    C.POINTER(abi.RunStats), C.POINTER(abi.RunStats)]
+    L.ptg_collide_multi_device.restype = st
+    L.ptg_collide_multi_device.argtypes = L.ptg_collide_multi.argtypes
+    L.ptg_queue_config.restype = st
+    L.ptg_queue_config.argtypes = [ctxp, C.POINTER(abi.QueueCfg), C.POINTER(abi.QueueCfg)]
+    L.ptg_queue_autotune.restype = st
+    L.ptg_queue_autotune.argtypes = [ctxp, C.c_size_t, C.POINTER(abi.Collision), C.POINTER(abi.CollideOptions),
+                                     C.POINTER(abi.Particles), C.c_double, C.POINTER(abi.QueueCfg), DP]
     _lib = L
     return L
 
@@ -173,6 +186,95 @@ class Engine:
         self._check(self.L.ptg_collide_batch_device(self._h, C.byref(laser), C.byref(options), C.byref(view), seed,
                                                     id_base, C.byref(out), C.byref(st)))
         return out, st.as_dict()
+
+    # -- multi-collision queue ---------------------------------------------
+    @staticmethod
+    def _collisions(collisions):
+        arr = (abi.Collision * len(collisions))()
+        for k, c in enumerate(collisions):
+            arr[k].laser = c["laser"]
+            arr[k].seed = c["seed"]
+            arr[k].id_base = c.get("id_base", 0)
+            arr[k].first = c["first"]
+            arr[k].count = c["count"]
+        return arr
+
+    @staticmethod
+    def _device_view(d_primaries):
+        view = abi.Particles()
+        view.n = int(d_primaries["species"].shape[0])
+        for name, dt, _cols in abi.PARTICLE_FIELDS:
+            t = d_primaries.get(name)
+            ct = {np.float64: C.POINTER(C.c_double), np.int32: C.POINTER(C.c_int32),
+                  np.uint64: C.POINTER(C.c_uint64)}[dt]
+            setattr(view, name, C.cast(C.c_void_p(t.data_ptr()) if t is not None else None, ct))
+        return view
+
+    def collide_multi(self, collisions, options, primaries):
+        """Many collisions in one persistent launch.  `collisions`: dicts with
+        laser, seed, id_base, first, count (rows of `primaries`).  Returns
+        (list of per-collision output dicts, list of per-collision stats,
+        total stats)."""
+        arr = self._collisions(collisions)
+        m = len(collisions)
+        view = abi.particles_view(primaries, len(primaries["species"]))
+        out = abi.Particles()
+        offs = (C.c_uint64 * (m + 1))()
+        stats = (abi.RunStats * m)()
+        total = abi.RunStats()
+        self._check(self.L.ptg_collide_multi(self._h, m, arr, C.byref(options), C.byref(view), C.byref(out), offs,
+                                             stats, C.byref(total)))
+        try:
+            n = out.n
+            whole = {}
+            for name, dt, cols in abi.PARTICLE_FIELDS:
+                shape = (n, cols) if cols > 1 else (n,)
+                if n == 0:
+                    whole[name] = np.zeros(shape, dtype=dt)
+                else:
+                    whole[name] = np.array(np.ctypeslib.as_array(getattr(out, name), shape=shape), dtype=dt, copy=True)
+        finally:
+            self.L.ptg_particles_free(C.byref(out))
+        parts = [{k: v[offs[i]:offs[i + 1]] for k, v in whole.items()} for i in range(m)]
+        return parts, [stats[i].as_dict() for i in range(m)], total.as_dict()
+
+    def collide_multi_device(self, collisions, options, d_primaries):
+        """Device-resident multi batch (primaries: dict of CUDA tensors).
+        Returns (Particles with device pointers, offsets, per-collision
+        stats, total stats)."""
+        arr = self._collisions(collisions)
+        m = len(collisions)
+        view = self._device_view(d_primaries)
+        out = abi.Particles()
+        offs = (C.c_uint64 * (m + 1))()
+        stats = (abi.RunStats * m)()
+        total = abi.RunStats()
+        self._check(self.L.ptg_collide_multi_device(self._h, m, arr, C.byref(options), C.byref(view), C.byref(out),
+                                                    offs, stats, C.byref(total)))
+        return out, list(offs), [stats[i].as_dict() for i in range(m)], total.as_dict()
+
+    def queue_config(self, variant=None, blocks_per_sm=None, chunk=None, use_graph=None):
+        """Reads, and optionally sets, the queue kernel's launch shape."""
+        cur = abi.QueueCfg()
+        self._check(self.L.ptg_queue_config(self._h, None, C.byref(cur)))
+        if any(v is not None for v in (variant, blocks_per_sm, chunk, use_graph)):
+            new = abi.QueueCfg(cur.variant if variant is None else variant,
+                               cur.blocks_per_sm if blocks_per_sm is None else blocks_per_sm,
+                               cur.chunk if chunk is None else chunk,
+                               cur.use_graph if use_graph is None else int(use_graph))
+            self._check(self.L.ptg_queue_config(self._h, C.byref(new), C.byref(cur)))
+        return cur.as_dict()
+
+    def queue_autotune(self, collisions, options, d_primaries, sample_fraction=0.1):
+        """Runs the autotuner on a sample of a device-resident batch; the
+        chosen launch shape stays set in the context."""
+        arr = self._collisions(collisions)
+        view = self._device_view(d_primaries)
+        best = abi.QueueCfg()
+        ms = C.c_double()
+        self._check(self.L.ptg_queue_autotune(self._h, len(collisions), arr, C.byref(options), C.byref(view),
+                                              sample_fraction, C.byref(best), C.byref(ms)))
+        return best.as_dict(), ms.value
 
     # -- diagnostics -----------------------------------------------------
     def fields(self, laser, r):

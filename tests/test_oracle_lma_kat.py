@@ -193,3 +193,59 @@ def test_lp_harmonic_index_distribution(orc, a, eta):
             continue
         got = np.mean((ns >= lo) & (ns <= hi))
         assert abs(got - expected) / expected < 5e-2, (lo, hi, got, expected)
+
+
+# pair_creation/lp/mod.rs:632-671: LP Breit-Wheeler rates from the main
+# table against the reference's integrated targets (relative 2e-2), as
+# (a, eta, par, perp)
+@pytest.mark.parametrize("a,eta,tpar,tperp", [
+    (5.0, 1.00, 1.887692e-1, 3.316904e-1), (5.0, 0.20, 3.710312e-3, 6.936493e-3),
+    (5.0, 0.10, 1.064405e-4, 2.038094e-4), (5.0, 0.05, 2.020565e-7, 3.954686e-7),
+    (5.0, 0.02, 6.585973e-15, 1.298047e-14), (7.0, 1.00, 3.059499e-1, 5.304186e-1),
+    (7.0, 0.20, 1.178253e-2, 2.192628e-2), (7.0, 0.10, 7.458782e-4, 1.420485e-3),
+    (7.0, 0.05, 6.611321e-6, 1.284355e-5), (7.0, 0.02, 2.035366e-11, 3.995504e-11),
+    (7.0, 0.005, 4.609079e-37, 9.102267e-37), (12.0, 1.00, 5.951957e-1, 9.947496e-1),
+    (12.0, 0.20, 4.881726e-2, 8.788478e-2), (12.0, 0.10, 7.119589e-3, 1.327181e-2),
+    (12.0, 0.05, 3.261287e-4, 6.137394e-4), (12.0, 0.02, 1.189212e-7, 2.307944e-7),
+    (12.0, 0.005, 5.473355e-23, 1.084261e-22), (15.0, 1.00, 7.563206e-1, 1.259821e0),
+    (15.0, 0.2, 7.828999e-2, 1.387037e-1), (15.0, 0.1, 1.455098e-2, 2.686104e-2),
+    (15.0, 0.05, 1.036607e-3, 1.975386e-3), (15.0, 0.02, 1.474648e-6, 2.884113e-6),
+    (15.0, 0.005, 5.380813e-19, 1.072893e-18)])
+def test_lp_pair_rate_lookup(orc, a, eta, tpar, tperp):
+    par, perp = orc.lp_pair_rates(a, eta)
+    assert abs(par - tpar) / tpar < 2e-2 and abs(perp - tperp) / tperp < 2e-2
+
+
+def _lpm_node(i, j):
+    from ptarmigan_gb300.tables import small_tables as st
+    a = math.exp(st.scalar("BW_LPM_LN_MIN_A")) * 10.0 ** (j / 20.0)
+    eta = (1.0 + 0.5 * a * a) * 2.0 / (1.0 + i / 4.0)
+    return a, eta
+
+
+# pair_creation/lp/mod.rs:1063-1163 generated the mid-range tables with
+# TotalRate::by_summation at eta' = 2 / (1 + i/4), a = 10^(-7/5 + j/20): the
+# restatement of that sum (DoubleDiffPartialRate::integrate, direct and
+# adaptive) reproduces the shipped totals at the nodes.
+@pytest.mark.parametrize("i,j", [(0, 20), (10, 30), (40, 25), (20, 5), (156, 12)])
+def test_lp_pair_by_summation_reproduces_mid_range_totals(orc, i, j):
+    import os
+    from ptarmigan_gb300.tables.extract import read_ptgt
+    shape, vals = read_ptgt(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                         "ptarmigan_gb300", "tables", "data", "bw_lp_mid_total.ptgt"))
+    table = np.array(vals).reshape(shape)
+    a, eta = _lpm_node(i, j)
+    cdf = orc.lp_pair_by_summation(a, eta)
+    expect = np.exp(table[i, j])
+    assert np.all(np.abs(cdf[15, 1:] / expect - 1.0) < 1e-9), (cdf[15, 1:], expect)
+    # the nodes are increasing integers and the cumulative sums monotone
+    assert np.all(np.diff(cdf[:, 0]) >= 1.0) and np.all(np.diff(cdf[:, 1]) >= 0.0)
+
+
+# pair_creation/lp/mod.rs:632-671: across both tables the photon polarised
+# perpendicular to the field (S_1 = -1) decays faster than the parallel one
+def test_lp_pair_rates_respect_the_polarisation_order(orc):
+    # perpendicular (S_1 = -1) photons decay faster than parallel ones
+    for a, eta in [(0.5, 0.3), (1.5, 0.2), (3.0, 0.1), (8.0, 0.05)]:
+        par, perp = orc.lp_pair_rates(a, eta)
+        assert perp > par > 0.0
