@@ -52,6 +52,15 @@ N_PRIMARIES = 1_000_000
 WORKLOAD = "focused LCFA shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; FastFocusedLaser a0=10 w0=4 um 0.8 um 30 fs LP; pairs on; generations<=2"
 
 
+# FP64 operations per step of collide_wave on this workload (2 x DFMA + DMUL
+# + DADD from ncu's SASS instruction counts over a 1e4-primary batch,
+# divided by that batch's step counts) and DRAM bytes per primary (ncu,
+# 1e6-primary batch).
+FP64_PER_LEPTON_STEP = 253.9
+FP64_PER_PHOTON_STEP = 34.2
+DRAM_BYTES_PER_PRIMARY = 2.05e6 / 1e4
+
+
 def workload(n, seed):
     from ptarmigan_gb300 import abi, beam
     laser = abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
@@ -419,28 +428,24 @@ def main():
         e2e_s = float(t.item())
     e2e = args.n * world * e2e_steps / e2e_s
 
-    # roofline of the dominant kernel (the LCFA wave): FP64 work per launch
-    # from the event counts, over the wave time measured above
+    # roofline of the dominant kernel (collide_wave, FP64-pipe bound): FP64
+    # operations per charged and per photon step, counted by ncu on a 1e4
+    # primary batch of this workload (profiles/collide_wave_fp64_counts_n1e4.md),
+    # times this run's step counts, over the waves' device time; peak = the
+    # device's measured FP64 FMA throughput (ptg_fp64_peak).
     pk, pk_kind = peaks()
     st0 = stats[-1]
-    fp64_model = json.load(open(os.path.join(ROOT, "profiles", "fp64_opcount.json"))) if os.path.exists(
-        os.path.join(ROOT, "profiles", "fp64_opcount.json")) else None
-    roofline = None
-    if fp64_model:
-        # FP64 operations of the wave kernels per batch (op-count model per
-        # lepton and photon step, from ncu instruction counts), over the
-        # batch's device time (the waves are ~100% of it)
-        flops = (st0["lepton_steps"] * fp64_model["per_lepton_step"]
-                 + st0["photon_steps"] * fp64_model["per_photon_step"])
-        achieved = flops / (np.mean(kern_ms) / 1e3) / 1e12
-        peak = fp64_peak_tflops(dev)
-        traffic = None
-        if fp64_model.get("dram_bytes_per_primary"):
-            traffic = fp64_model["dram_bytes_per_primary"] * args.n
-        roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak, "traffic": traffic,
-                    "peak_source": "measured here: cuBLAS DGEMM 8192^3 best of 5 (no FP64 figure in MEASURED_PEAKS.json)",
-                    "hbm_frac": None if traffic is None else (traffic / (np.mean(kern_ms) / 1e3) / 1e9) / pk.get("hbm_gbs", 6800.0)}
+    flops = st0["lepton_steps"] * FP64_PER_LEPTON_STEP + st0["photon_steps"] * FP64_PER_PHOTON_STEP
+    kern_s = float(np.mean(kern_ms)) / 1e3
+    achieved = flops / kern_s / 1e12
+    peak = eng.fp64_peak()
+    traffic = DRAM_BYTES_PER_PRIMARY * args.n
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic,
+                "peak_source": "measured in this run: FP64 FMA throughput kernel (ptg_fp64_peak); "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "fp64_flops_per_step": {"lepton": FP64_PER_LEPTON_STEP, "photon": FP64_PER_PHOTON_STEP},
+                "hbm_frac": (traffic / kern_s / 1e9) / pk.get("hbm_gbs", 6800.0)}
 
     launches = int(sum(2 + s["waves"] for s in stats))
     line = {

@@ -323,6 +323,57 @@ ptg_status ptg_double_bessel(ptg_ctx* ctx, int32_t n, size_t count, const double
 ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
                          const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
 
+/* --------------------------------------------------- learned proposal ---
+ * No reference counterpart: an MLP (inputs ln a, ln eta, ln n; 4 layers of
+ * width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the
+ * tensor cores) proposes v = s / s_max for CP nonlinear Compton emission in
+ * 16 bins, with an exact accept/reject against the spectrum
+ * (nonlinear_compton/cp/mod.rs:17-40) and the reference's sampler as the
+ * fallback wherever the learned envelope falls under the spectrum. */
+typedef struct {
+    uint64_t n_samples;      /* training samples drawn with the table sampler */
+    int32_t batch, epochs;
+    float lr, tau;           /* Adam learning rate (cosine decay); quantile of the pinball loss */
+    uint64_t seed;
+    double a_lo, a_hi, eta_lo, eta_hi;  /* log-uniform training domain */
+} ptg_mlp_train_cfg;
+
+typedef struct {
+    float loss_first, loss_last;
+    int32_t steps, reserved;
+    double data_ms, train_ms;
+} ptg_mlp_train_stats;
+
+typedef struct {
+    uint64_t n, seed;                   /* emissions; draws of (a, eta, n) shared by both samplers */
+    double a_lo, a_hi, eta_lo, eta_hi;
+    float margin, reserved;             /* ln of the envelope's safety factor */
+} ptg_sampler_bench_cfg;
+
+typedef struct {
+    double plain_ms, learned_ms, infer_ms;  /* device times (inference includes the features pass) */
+    double plain_evals, learned_evals;      /* spectrum evaluations per emission */
+    uint64_t fallbacks, errors;
+} ptg_sampler_bench_stats;
+
+/* Random initialisation; parameter access ([count] floats, get and/or
+ * set); the training loop; the loss gradient of a batch ([n][5] = x0, x1,
+ * x2, bin, target) for checks; batched inference ([n][3] -> [n][16]); the
+ * switch that makes the collision kernels use the network; and the sampler
+ * benchmark (v_plain, v_learned: [n], may be NULL). */
+ptg_status ptg_mlp_init(ptg_ctx* ctx, uint64_t seed);
+ptg_status ptg_mlp_params(ptg_ctx* ctx, float* get, const float* set, int32_t* count);
+ptg_status ptg_mlp_train(ptg_ctx* ctx, const ptg_mlp_train_cfg* cfg, ptg_mlp_train_stats* stats);
+ptg_status ptg_mlp_grad(ptg_ctx* ctx, const float* samples, size_t n, float tau, float* grad, float* loss);
+ptg_status ptg_mlp_infer(ptg_ctx* ctx, const float* x, size_t n, float* out);
+ptg_status ptg_mlp_use(ptg_ctx* ctx, int32_t enabled, float margin);
+ptg_status ptg_sampler_bench(ptg_ctx* ctx, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
+                             ptg_sampler_bench_stats* stats);
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
+ * FP64-pipe-bound collision kernels. */
+ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);
+
 /* Table maintenance: regenerates the CP nonlinear-Compton harmonic CDF
  * table on the device.  The reference ships it as
  * nonlinear_compton/cp/tables/cdf.rs, which is absent from its tree; this
@@ -330,6 +381,15 @@ ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const doub
  * cdf_out: [70*61][32][2] (eta-major grid, [n, cdf(n)] nodes);
  * total_out: [70*61] total rates, to check against the shipped totals. */
 ptg_status ptg_regen_nlc_cp_cdf(ptg_ctx* ctx, double* cdf_out, double* total_out);
+
+/* Table maintenance: regenerates the LP Breit-Wheeler mid-range harmonic
+ * CDF (pair_creation/lp/tables/mid_range/cdf.rs, absent from the reference
+ * tree) with its generator, pair_creation/lp/mod.rs:1063-1163
+ * (TotalRate::by_summation at eta' = 2/(1 + i/4), a = 10^(-7/5 + j/20)).
+ * cdf_out: [157*36][16][3] ([n, cumulative par, cumulative perp] nodes);
+ * total_out: [157*36][2] totals, to check against the shipped
+ * mid_range/total.rs. */
+ptg_status ptg_regen_bw_lp_mid_cdf(ptg_ctx* ctx, double* cdf_out, double* total_out);
 
 #ifdef __cplusplus
 }

@@ -164,6 +164,7 @@ int orc_load_tables(const char* dir) {
     std::string err;
     return load_lma_tables(dir, &err) ? 0 : 1;
 }
+int orc_has_lp_mid_cdf() { return g_lma.bw_lp_mid_cdf != nullptr; }
 int orc_has_cp_cdf(void) { return g_lma.nlc_cp_cdf != nullptr; }
 
 double orc_bessel_j(double x, int n) { return bessel_j(x, n); }
@@ -294,6 +295,29 @@ int orc_lp_pair_sample(double a, double eta, double sv1, double sv2, uint64_t se
     uint64_t rej = 0;
     int st = lp_pair_sample(a, eta, sv1, sv2, rng, &n, &s, &th, &rej);
     out3[0] = n, out3[1] = s, out3[2] = th;
+    return st;
+}
+
+double orc_cp_cl_integrated(int n, double a) { return cp_cl_integrated(n, a); }
+double orc_lp_cl_partial_rate(int n, double a) { return lp_cl_partial_rate(n, a); }
+double orc_nlc_classical_rate(double a, double eta, int pol) {
+    double r;
+    bool ok = pol == 1 ? cp_classical_rate(a, eta, &r) : lp_classical_rate(a, eta, &r);
+    return ok ? r : NAN;
+}
+int orc_nlc_classical_sample(double a, double eta, int pol, uint64_t seed, uint64_t stream, uint32_t step,
+                             double* out7) {
+    DrawStream rng;
+    rng.seed = seed;
+    rng.stream = stream;
+    rng.begin_step(step);
+    int n = 0;
+    double s = 0.0, th = 0.0;
+    Stokes sv;
+    uint64_t rej = 0;
+    int st = pol == 1 ? cp_classical_sample(a, eta, rng, &n, &s, &th, &sv, &rej)
+                      : lp_classical_sample(a, eta, rng, &n, &s, &th, &sv, &rej);
+    out7[0] = n, out7[1] = s, out7[2] = th, out7[3] = sv.i, out7[4] = sv.q, out7[5] = sv.u, out7[6] = sv.v;
     return st;
 }
 

@@ -25,6 +25,14 @@ static inline double powi(double a, int b) {
     }
     return recip ? 1.0 / r : r;
 }
+
+// Rust's `as i32` on f64: saturating, NaN -> 0.
+static int rust_as_i32(double x) {
+    if (std::isnan(x)) return 0;
+    if (x >= 2147483647.0) return 2147483647;
+    if (x <= -2147483648.0) return (-2147483647 - 1);
+    return (int)x;
+}
 static inline double sq(double x) { return x * x; }
 constexpr double FRAC_PI_2 = 1.57079632679489661923132169163975144;
 constexpr double FRAC_PI_4 = 0.785398163397448309615660845819875721;
@@ -763,6 +771,32 @@ struct ThetaBound {
         return tb;
     }
 
+    // nonlinear_compton/lp/mod.rs:209-268: the bound at fixed v = s / s_max
+    static ThetaBound for_harmonic_low_eta(int n, double a) {
+        ThetaBound tb;
+        for (int i = 0; i < 16; ++i) {
+            double z = std::cos(PI * i / 15.0);
+            double v = 0.5 * (z + 1.0);
+            tb.s[i] = v;
+            double x = 2.0 * n * a * std::sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+            double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+            double x_crit = y > n / 6.0 ? 4.0 * std::sqrt(y) * std::sqrt(n - 2.0 * y) : n + 2.0 * y;
+            double ln_j_crit = std::log(0.443) - std::log((double)n) / 3.0;
+            double ln_j_bdy = std::fmin(ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y), ln_j_crit);
+            double ct = std::fmax(1.0 - x_crit * std::log(0.01) / (x * (ln_j_bdy - ln_j_crit)), -1.0);
+            tb.f[i] = std::acos(ct);
+            if (std::isnan(tb.f[i])) tb.f[i] = PI;
+        }
+        double f_min = tb.f[0];
+        for (int i = 1; i < 16; ++i) {
+            if (tb.f[i] < f_min)
+                f_min = tb.f[i];
+            else
+                tb.f[i] = f_min;
+        }
+        return tb;
+    }
+
     double at(double arg) const {
         double val = f[15];
         for (int i = 1; i < 16; ++i) {
@@ -833,7 +867,9 @@ bool lp_classical_rate(double a, double eta, double* out) {
     int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
     if (ix >= 60) return false;
     double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
-    *out = eta * std::exp((1.0 - dx) * g_lma.nlc_lp_cl_rate[ix] + dx * g_lma.nlc_lp_cl_rate[ix + 1]);
+    double f = (1.0 - dx) * g_lma.nlc_lp_cl_rate[ix] + dx * g_lma.nlc_lp_cl_rate[ix + 1];
+    double prefactor = 2.0 * eta / (1.0 + 0.5 * a * a);
+    *out = prefactor * std::exp(f);
     return true;
 }
 
@@ -960,6 +996,248 @@ int lp_sample(double a, double eta, DrawStream& rng, int* n_out, double* s_out, 
 }
 
 // ------------------------------------------------- LMA NLC dispatch ----
+
+// ------------------------------------------------ classical LMA emission --
+// nonlinear_compton/cp/classical.rs:45-175
+static double cp_cl_ceiling(int n, double a) {
+    double n_switch = std::round(3.0 * (1.0 + 0.54 * std::pow(a, 2.75)));
+    double mx;
+    if (n == 1) {
+        mx = cp_spectrum_low_eta(n, a, 0.99);
+    } else if (a < 0.15 || n > (int)n_switch) {
+        mx = cp_spectrum_low_eta(n, a, 0.5);
+    } else {
+        double b = a < 0.5 ? 2.3 * a : 0.8 * std::exp(-(a - 0.5) / 3.5) + 0.35;
+        double v = 1.0 - 0.5 * std::pow(std::log((double)n), b) / std::pow(std::log(n_switch), b);
+        mx = NAN;
+        for (int i = -4; i < 4; ++i) {
+            double f = cp_spectrum_low_eta(n, a, std::fmin(v + 0.1 * (double)i / 4.0, 1.0));
+            mx = std::isnan(mx) ? f : (std::isnan(f) ? mx : std::max(mx, f));
+        }
+    }
+    return 1.1 * mx;
+}
+
+// cdf_table: [61][32][2] over ln a, two-point interpolation, inversion in
+// [ln n, ln(-ln(1 - cdf))]; -1 if the lookup fails
+static int cp_cl_harmonic_index(double a, double frac) {
+    const double* T = g_lma.nlc_cp_cl_cdf;
+    if (std::log(a) <= PTG_NLC_CL_MIN) return 1;
+    int ix = (int)((std::log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    double dx = (std::log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    if (ix >= 60) return -1;
+    double n = 0.0;
+    for (int k = 0; k < 2; ++k) {
+        const double* tb = T + (size_t)(ix + k) * 64;
+        double w = k == 0 ? 1.0 - dx : dx;
+        double nk;
+        if (frac <= tb[1]) {
+            nk = 0.9;
+        } else {
+            double rs[62];
+            for (int i = 0; i < 31; ++i) {
+                rs[2 * i] = std::log(tb[2 * i]);
+                rs[2 * i + 1] = std::log(-1.0 * std::log(1.0 - tb[2 * i + 1]));
+            }
+            bool ok;
+            nk = std::exp(Pwmci(rs, 31, true).invert(std::log(-1.0 * std::log(1.0 - frac)), &ok));
+        }
+        n += nk * w;
+    }
+    return std::isfinite(n) ? rust_as_i32(std::ceil(n)) : -1;
+}
+
+int cp_classical_sample(double a, double eta, DrawStream& rng, int* n_out, double* s_out, double* theta_out,
+                        Stokes* sv_out, uint64_t* rej) {
+    int n = cp_cl_harmonic_index(a, rng.next());
+    if (n < 1) return PTG_ERR_OUT_OF_TABLE;
+    double mx = cp_cl_ceiling(n, a);
+    double v = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next(), u = rng.next();
+        if (u <= cp_spectrum_low_eta(n, a, vv) / mx) {
+            v = vv;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double s = v * sn;
+    double theta = 2.0 * PI * rng.next();
+    double z = std::sqrt((double)(4 * n * n) * (a * a / (1.0 + a * a)) * v * (1.0 - v));
+    double jm, j, jp;
+    bessel_j_pm(z, n, &jm, &j, &jp);
+    double xi0 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) - powi(2.0 * j / a, 2);
+    double xi1 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) + 8.0 * j * j * (1.0 - powi((double)n / z, 2) - 0.5 / (a * a));
+    double xi3 = 2.0 * (1.0 - 2.0 * v) * (jm * jm - jp * jp);
+    Stokes sv(1.0, xi1 / xi0, 0.0 / xi0, xi3 / xi0);
+    *sv_out = sv.rotate_by(FRAC_PI_2 + theta);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return PTG_OK;
+}
+
+// nonlinear_compton/lp/classical.rs:19-120
+static double lp_cl_ddpr(double a, double v, double theta, DoubleBessel& dj) {
+    int n = dj.n;
+    double x = 2.0 * n * a * std::cos(theta) * std::sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+    double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+    double j[5];
+    dj.evaluate(x, y, j);
+    double g0, g1, g2;
+    if (n % 2 == 0) {
+        g0 = j[2], g1 = -0.5 * (j[1] + j[3]), g2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        g0 = -j[2], g1 = 0.5 * (j[1] + j[3]), g2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    return (-g0 * g0 - a * a * (g0 * g2 - g1 * g1)) / (2.0 * PI);
+}
+
+static double lp_cl_ceiling(double a, DoubleBessel& dj) {
+    int n = dj.n;
+    double mx = NAN;
+    auto upd = [&](double f) { mx = std::isnan(mx) ? f : (std::isnan(f) ? mx : std::max(mx, f)); };
+    if (n == 1) {
+        upd(lp_cl_ddpr(a, 0.01, FRAC_PI_2, dj));
+    } else if (a <= 1.5) {
+        double v_min = 0.1 + (9.0 / std::sqrt((double)n) - 1.0) / 10.0;
+        double v_max = std::fmin(v_min + 0.4, 1.0);
+        for (int i = 1; i <= 16; ++i) upd(lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / 16.0, 0.0, dj));
+    } else if (a < 5.0) {
+        int n_switch = rust_as_i32(3.0 * std::pow(a / 2.0, 4.0 / 3.0));
+        double theta = n > n_switch ? 0.0 : FRAC_PI_2 * (1.0 - std::log((double)n) / std::log((double)n_switch));
+        double v_min = std::fmin(0.35 + (7.0 / std::sqrt((double)n) - 1.0) / 9.0, 0.55);
+        double v_max = 0.55 + (7.0 / std::sqrt((double)n) - 1.0) / 9.0;
+        int num = a > 4.0 ? 32 : 16;
+        for (int i = 0; i < num; ++i) upd(lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / num, theta, dj));
+    } else {
+        double n_switch = 10.0 * powi(a / 5.0, 2);
+        double theta = 0.0;
+        if (!(n > rust_as_i32(n_switch))) {
+            double pw = 0.3 + (0.7 - 0.3) * (std::log(a) - std::log(5.0)) / (std::log(20.0) - std::log(5.0));
+            theta = FRAC_PI_2 * (std::pow((double)n, -pw) - std::pow(n_switch, -pw)) / (1.0 - std::pow(n_switch, -pw));
+        }
+        double v_min = 0.3 + 0.4 * std::log((double)n) * std::pow((double)n, -0.7);
+        double v_max = v_min + 0.2;
+        int num = a > 8.0 ? 64 : 32;
+        for (int i = 0; i < num; ++i) upd(lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / num, theta, dj));
+    }
+    return 1.1 * mx;
+}
+
+static int lp_cl_harmonic_index(double a, double frac) {
+    const double* T = g_lma.nlc_lp_cl_cdf;
+    if (std::log(a) <= PTG_NLC_CL_MIN) return 1;
+    int ix = (int)((std::log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    double dx = (std::log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    if (ix >= 60) return -1;
+    double n = 0.0;
+    for (int k = 0; k < 2; ++k) {
+        const double* tb = T + (size_t)(ix + k) * 32;
+        double w = k == 0 ? 1.0 - dx : dx;
+        double nk = 0.9;
+        if (!(frac <= tb[1])) {
+            bool ok;
+            nk = Pwmci(tb, 16).invert(frac, &ok);
+            if (!ok) return -1;  // the reference unwraps this inversion
+        }
+        n += nk * w;
+    }
+    return std::isfinite(n) ? rust_as_i32(std::ceil(n)) : -1;
+}
+
+
+// nonlinear_compton/cp/mod.rs:137-153
+double cp_cl_integrated(int n, double a) {
+    double lower = 0.0, upper = 0.0;
+    for (int k = 0; k < 32; ++k) lower += 0.25 * PTG_GAUSS_32_WEIGHTS[k] * cp_spectrum_low_eta(n, a, 0.25 * (PTG_GAUSS_32_NODES[k] + 1.0));
+    for (int k = 0; k < 32; ++k) upper += 0.25 * PTG_GAUSS_32_WEIGHTS[k] * cp_spectrum_low_eta(n, a, 0.25 * (PTG_GAUSS_32_NODES[k] + 3.0));
+    return lower + upper;
+}
+
+// nonlinear_compton/lp/classical.rs:113-180 (integral over v and theta)
+double lp_cl_partial_rate(int n, double a) {
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    ThetaBound tb = ThetaBound::for_harmonic_low_eta(n, a);
+    auto single = [&](double v, double tmax) {
+        double acc = 0.0;
+        for (int k = 0; k < 32; ++k) {
+            double th = 0.5 * (PTG_GAUSS_32_NODES[k] + 1.0) * tmax;
+            acc += 4.0 * (0.5 * tmax) * PTG_GAUSS_32_WEIGHTS[k] * lp_cl_ddpr(a, v, th, dj);
+        }
+        return acc;
+    };
+    double lower = 0.0, middle = 0.0, upper = 0.0;
+    for (int k = 0; k < 32; ++k) {
+        double v = 0.5 * (PTG_GAUSS_32_NODES[k] + 1.0) * 0.5;
+        lower += PTG_GAUSS_32_WEIGHTS[k] * (0.5 * 0.5) * single(v, tb.at(v));
+    }
+    for (int k = 0; k < 32; ++k) {
+        double v = 0.5 + 0.5 * (PTG_GAUSS_32_NODES[k] + 1.0) * 0.25;
+        middle += PTG_GAUSS_32_WEIGHTS[k] * (0.5 * 0.25) * single(v, tb.at(v));
+    }
+    for (int k = 0; k < 32; ++k) {
+        double v = 0.75 + 0.5 * (PTG_GAUSS_32_NODES[k] + 1.0) * 0.25;
+        upper += PTG_GAUSS_32_WEIGHTS[k] * (0.5 * 0.25) * single(v, tb.at(v));
+    }
+    return lower + middle + upper;
+}
+
+int lp_classical_sample(double a, double eta, DrawStream& rng, int* n_out, double* s_out, double* theta_out,
+                        Stokes* sv_out, uint64_t* rej) {
+    int n = lp_cl_harmonic_index(a, rng.next());
+    if (n < 1) return PTG_ERR_OUT_OF_TABLE;
+    DoubleBessel dj(n, n * SQRT_2, n * 0.5);
+    ThetaBound tb = ThetaBound::for_harmonic_low_eta(n, a);
+    double smax = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double mx = lp_cl_ceiling(a, dj);
+    double v = 0.0, s = 0.0, theta = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next();
+        double ss = vv * smax;
+        double th = FRAC_PI_2 * rng.next();
+        if (th > tb.at(vv)) continue;
+        double z = mx * rng.next();
+        if (z < lp_cl_ddpr(a, vv, th, dj)) {
+            v = vv, s = ss, theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return PTG_ERR_REJECTION_CAP;
+    int quadrant = (int)(4.0 * rng.next());
+    if (quadrant == 1)
+        theta = PI - theta;
+    else if (quadrant == 2)
+        theta = PI + theta;
+    else if (quadrant == 3)
+        theta = 2.0 * PI - theta;
+    double x = 2.0 * n * a * std::cos(theta) * std::sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+    double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+    double j[5];
+    dj.evaluate(x, y, j);
+    double A0, A1, A2;
+    if (n % 2 == 0) {
+        A0 = j[2], A1 = -0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        A0 = -j[2], A1 = 0.5 * (j[1] + j[3]), A2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    double u = std::sqrt((1.0 + 0.5 * a * a) * (1.0 - v) / v);
+    double xi0 = 2.0 * (powi(A1, 2) - A0 * A2) - 2.0 * powi(A0 / a, 2);
+    double xi1 = 2.0 * (powi(A1, 2) - A0 * A2) - 2.0 * (1.0 + 2.0 * u * u * powi(std::sin(theta), 2)) * powi(A0 / a, 2);
+    double xi2 = 2.0 * powi(u * A0 / a, 2) * std::sin(2.0 * theta) + 4.0 * u * A0 * A1 * std::sin(theta) / a;
+    *sv_out = Stokes(1.0, xi1 / xi0, xi2 / xi0, 0.0);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
+    return PTG_OK;
+}
+
+
 // nonlinear_compton/mod.rs:19-47
 bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classical, double* p) {
     double a_sqd = q * q - 1.0;
@@ -987,13 +1265,12 @@ int nlc_generate(const V4& k, const V4& q, int pol, double pol_angle, bool class
     double s, cphi;
     Stokes sv;
     int st;
-    if (pol == PTG_POL_CIRCULAR && !classical) {
-        st = cp_sample(a, eta, rng, &n, &s, &cphi, &sv, rej);
-    } else if (pol == PTG_POL_LINEAR && !classical) {
-        st = lp_sample(a * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
-    } else {
-        return PTG_ERR_UNSUPPORTED;
-    }
+    if (pol == PTG_POL_CIRCULAR)
+        st = classical ? cp_classical_sample(a, eta, rng, &n, &s, &cphi, &sv, rej)
+                       : cp_sample(a, eta, rng, &n, &s, &cphi, &sv, rej);
+    else
+        st = classical ? lp_classical_sample(a * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej)
+                       : lp_sample(a * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
     if (st != PTG_OK) return st;
     double ell = n;
     double p_zmf = classical ? ell * eta / std::sqrt(1.0 + a * a) : ell * eta / std::sqrt(1.0 + a * a + 2.0 * ell * eta);
@@ -1318,13 +1595,6 @@ static int cpp_sample(double a, double eta, double sv1, double sv2, double sv3, 
 // pair_creation/lp/**: rates from the shipped tables (main and mid-range),
 // harmonic index by CDF inversion, (s, theta) by rejection.
 
-// Rust's `as i32` on f64: saturating, NaN -> 0.
-static int rust_as_i32(double x) {
-    if (std::isnan(x)) return 0;
-    if (x >= 2147483647.0) return 2147483647;
-    if (x <= -2147483648.0) return (-2147483647 - 1);
-    return (int)x;
-}
 
 // pair_creation/lp/tables/pol_dep.rs: a pair (S_1 = +1, S_1 = -1)
 struct PolDep {

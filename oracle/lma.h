@@ -60,6 +60,14 @@ bool lp_classical_rate(double a, double eta, double* out);
 int lp_harmonic_index(double a, double eta, double frac);
 int lp_sample(double a, double eta, DrawStream& rng, int* n, double* s, double* theta, Stokes* sv, uint64_t* rej);
 
+// nonlinear_compton/{cp,lp}/classical.rs
+double cp_cl_integrated(int n, double a);
+double lp_cl_partial_rate(int n, double a);
+int cp_classical_sample(double a, double eta, DrawStream& rng, int* n, double* s, double* theta, Stokes* sv,
+                        uint64_t* rej);
+int lp_classical_sample(double a, double eta, DrawStream& rng, int* n, double* s, double* theta, Stokes* sv,
+                        uint64_t* rej);
+
 // nonlinear_compton/mod.rs
 bool nlc_probability(const V4& k, const V4& q, double dt, int pol, bool classical, double* p);
 int nlc_generate(const V4& k, const V4& q, int pol, double pol_angle, bool classical, DrawStream& rng, int* n,

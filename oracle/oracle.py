@@ -80,6 +80,7 @@ def lib():
         "orc_result_free": (None, [vp]),
         "orc_load_tables": (i, [C.c_char_p]),
         "orc_has_cp_cdf": (i, []),
+        "orc_has_lp_mid_cdf": (i, []),
         "orc_bessel_j": (d, [d, i]),
         "orc_bessel_triple_j": (d, [i, d]),
         "orc_bessel_j_asymptotic": (d, [i, d]),
@@ -108,6 +109,10 @@ def lib():
         "orc_lp_harmonic_index": (i, [d, d, d]),
         "orc_lp_sample": (i, [d, d, u64, u64, u32, DP]),
         "orc_lp_pair_rates": (None, [d, d, DP]),
+        "orc_cp_cl_integrated": (d, [i, d]),
+        "orc_lp_cl_partial_rate": (d, [i, d]),
+        "orc_nlc_classical_rate": (d, [d, d, i]),
+        "orc_nlc_classical_sample": (i, [d, d, i, u64, u64, u32, DP]),
         "orc_lp_pair_dd_rate": (None, [i, d, d, d, d, DP]),
         "orc_lp_pair_partial_rate": (None, [i, d, d, DP]),
         "orc_lp_pair_by_summation": (None, [d, d, DP]),
@@ -278,6 +283,10 @@ def cp_rate(a, eta):
     return lib().orc_cp_rate(a, eta)
 
 
+def has_lp_mid_cdf():
+    return bool(lib().orc_has_lp_mid_cdf())
+
+
 def has_cp_cdf():
     return bool(lib().orc_has_cp_cdf())
 
@@ -379,6 +388,24 @@ def lp_harmonic_index(a, eta, frac):
 def lp_sample(a, eta, seed, stream, step):
     out = np.zeros(7)
     rc = lib().orc_lp_sample(a, eta, seed, stream, step, _dp(out))
+    return rc, out
+
+
+def cp_cl_integrated(n, a):
+    return lib().orc_cp_cl_integrated(n, a)
+
+
+def lp_cl_partial_rate(n, a):
+    return lib().orc_lp_cl_partial_rate(n, a)
+
+
+def nlc_classical_rate(a, eta, pol):
+    return lib().orc_nlc_classical_rate(a, eta, pol)
+
+
+def nlc_classical_sample(a, eta, pol, seed, stream, step):
+    out = np.zeros(7)
+    rc = lib().orc_nlc_classical_sample(a, eta, pol, seed, stream, step, _dp(out))
     return rc, out
 
 

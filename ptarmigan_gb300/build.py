@@ -18,6 +18,10 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libptarmigan_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "20091,550"]
+# Table regeneration reproduces the reference's generators, whose adaptive
+# quadrature stops on a tolerance test: separate multiplies and adds (no FMA
+# contraction), as in the reference's own arithmetic, keep those decisions.
+UNIT_FLAGS = {"ptg_regen.cu": ["-fmad=false"]}
 
 
 def _units():
@@ -61,7 +65,7 @@ def build(force=False, verbose=False):
     for src in _units():
         obj = os.path.join(BUILD_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
-        cmds.append([nvcc, *ARCH, *FLAGS, "-c", "-o", obj, src])
+        cmds.append([nvcc, *ARCH, *FLAGS, *UNIT_FLAGS.get(os.path.basename(src), []), "-c", "-o", obj, src])
     with ThreadPoolExecutor(max_workers=max(1, min(len(cmds), os.cpu_count() or 1))) as ex:
         logs = list(ex.map(_run, cmds))
     tmp = LIB_PATH + ".tmp"

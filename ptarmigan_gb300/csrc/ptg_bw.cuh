@@ -289,15 +289,11 @@ static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 s
     return true;
 }
 
-// pair_creation/mod.rs:49-110 (CP): the positron momentum
-static __device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
-                                        int* n_out, d4* q_out, uint32_t* rej) {
+// pair_creation/mod.rs:62-110: the positron momentum for a sampled
+// harmonic n, s and azimuth (rms amplitude a).  Returns a ptg status.
+static __device__ __noinline__ int bw_kinematics(d4 ell, d4 k, double a, double pol_angle, int n, double s, double cphi,
+                                                 d4* q_out) {
     double eta = dot4(k, ell);
-    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
-    int n;
-    double s, cphi;
-    int st = bw_sample(T, a, eta, sv.x, sv.y, sv.z, rng, &n, &s, &cphi, rej);
-    if (st != 0) return st;
     double j = n;
     double e_zmf = sqrt(0.5 * j * eta);
     double p_zmf = sqrt(0.5 * j * eta - 1.0 - a * a);
@@ -321,9 +317,21 @@ static __device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in
     q = boost_by(q, d4{uz.t, -uz.x, -uz.y, -uz.z});
     double s_new = 1.0 - dot4(k, q) / dot4(k, ell);
     if (!(fabs(s - s_new) / s < 1.0e-3)) return 3;
-    *n_out = n;
     *q_out = q;
     return 0;
+}
+
+// pair_creation/mod.rs:49-110 (CP): the positron momentum
+static __device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
+                                        int* n_out, d4* q_out, uint32_t* rej) {
+    double eta = dot4(k, ell);
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    int n;
+    double s, cphi;
+    int st = bw_sample(T, a, eta, sv.x, sv.y, sv.z, rng, &n, &s, &cphi, rej);
+    if (st != 0) return st;
+    *n_out = n;
+    return bw_kinematics(ell, k, a, pol_angle, n, s, cphi, q_out);
 }
 
 }  // namespace ptg

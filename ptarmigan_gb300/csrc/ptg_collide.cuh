@@ -68,6 +68,8 @@ struct WaveArgs {
     const LmaTables* lma;
     double* dbw;                   // DoubleBessel workspaces (LP LMA), one slot per resident lane
     int db_cap;                    // orders per slot
+    DbPool dbpool;                 // shared larger slots (pair creation at small eta)
+    MlpParams mlp;                 // learned CP proposal (enabled = 0: the reference sampler)
     unsigned long long seed;
     unsigned long long lo, hi;     // wave = store slots [lo, hi)
     unsigned long long n_primaries, id_base;
@@ -249,13 +251,14 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         }
     } else {
         lma_push(f, L.r, L.u, rqm, dt, a.o.eqn, &r, &u, &dt_actual, &dwork);
-        DbWork dbw{nullptr, 0};
+        DbWork dbw{nullptr, 0, 32};
         if (a.dbw) {
             size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
             dbw.base = a.dbw + warp * (size_t)a.db_cap * 5 * 32 + lane_id();
             dbw.cap = a.db_cap;
+            dbw.pool = a.dbpool;
         }
-        int st = lma_radiate(f, *a.lma, dbw, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr,
+        int st = lma_radiate(f, *a.lma, dbw, a.mlp, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr,
                              &kpol, &a_eff, &chi, &absorption, rej);
         if (st != ST_OK) {
             L.status = st;
@@ -364,8 +367,15 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
             }
         }
     } else {
-        int st = lma_pair_create(f, *a.lma, r, ell, pol, dt, rng, a.o.rate_increase, &prob, &pol_new, &created, &ue,
-                                 &up, &frac, &a_eff, &chi, &absorption, rej);
+        DbWork dbw{nullptr, 0, 32};
+        if (a.dbw) {
+            size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+            dbw.base = a.dbw + warp * (size_t)a.db_cap * 5 * 32 + lane_id();
+            dbw.cap = a.db_cap;
+            dbw.pool = a.dbpool;
+        }
+        int st = lma_pair_create(f, *a.lma, dbw, r, ell, pol, dt, rng, a.o.rate_increase, &prob, &pol_new, &created,
+                                 &ue, &up, &frac, &a_eff, &chi, &absorption, rej);
         if (st != ST_OK) {
             L.status = st;
             L.r = r;

@@ -20,6 +20,7 @@
 #include "../../include/ptarmigan_gb300.h"
 #include "ptg_collide.cuh"
 #include "ptg_launch.h"
+#include "ptg_mlp.cuh"
 #include "ptg_nlc.cuh"
 #include "ptg_queue.cuh"
 
@@ -70,6 +71,8 @@ struct ptg_ctx {
     // DoubleBessel workspaces for linearly polarised LMA emission
     void* dbw = nullptr;
     size_t dbw_bytes = 0;
+    void* dbpool = nullptr;  // shared large J(n, x, y) slots, then their state words
+    size_t dbpool_bytes = 0;
     int grid_cap = 0;  // > 0: the wave grid is capped (workspace budget)
     std::vector<void*> table_bufs;
     bool tables_loaded = false;
@@ -87,11 +90,20 @@ struct ptg_ctx {
     unsigned long long* h_qfirst = nullptr;
     unsigned long long* h_qout = nullptr;
     ptg_queue_cfg qcfg{0, 0, 1, 1};
+    // learned CP proposal: FP32 master, Adam moments, per-block gradient
+    // partials, BF16 weights (w0 w1 w2 w3 t1 t2 t3)
+    float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_partial = nullptr, *mlp_loss = nullptr;
+    __nv_bfloat16* mlp_bf = nullptr;
+    int mlp_step = 0;
+    bool mlp_ready = false, mlp_enabled = false;
+    float mlp_margin = 0.25f;
     cudaGraphExec_t q_graph = nullptr;
     std::string q_graph_key;
 };
 
 // ------------------------------------------------------------ helpers ---
+static MlpParams mlp_params(ptg_ctx* c);
+
 static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     FieldParams f{};
     f.model = d.model;
@@ -389,7 +401,7 @@ __global__ void k_double_bessel(unsigned long long m, int n, int cap, const doub
                                 double* ws, double* j5, int* ok) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= m) return;
-    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap};
+    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap, 32};
     DbGeom g;
     double j[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     bool good = db_geom(n, cap, &g) && (mode ? db_evaluate(g, w, x[i], y[i], j) : db_around(g, w, x[i], y[i], j));
@@ -404,7 +416,7 @@ __global__ void k_lp_sample(unsigned long long m, int cap, const LmaTables* t, c
                             double* out7, int* status) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= m) return;
-    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap};
+    DbWork w{ws + (i >> 5) * (size_t)cap * 5 * 32 + (i & 31), cap, 32};
     Draws rng;
     rng.begin(seed, stream[i], step);
     int n = 0;
@@ -658,6 +670,9 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     cudaFree(c->gl);
     cudaFree(c->lma_dev);
     cudaFree(c->dbw);
+    cudaFree(c->dbpool);
+    cudaFree(c->mlp_p), cudaFree(c->mlp_m), cudaFree(c->mlp_v), cudaFree(c->mlp_partial), cudaFree(c->mlp_loss);
+    cudaFree(c->mlp_bf);
     if (c->q_graph) cudaGraphExecDestroy(c->q_graph);
     cudaFree(c->d_coll);
     cudaFree(c->d_cstats);
@@ -700,6 +715,8 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
         {"bw_lp_cdf", &c->lma_host.bw_lp_cdf, 1525 * 16 * 3, true},
         {"bw_lp_mid_total", &c->lma_host.bw_lp_mid_total, 157 * 36 * 2, true},
         {"bw_lp_mid_cdf", &c->lma_host.bw_lp_mid_cdf, 5652 * 16 * 3, false},
+        {"nlc_cp_classical_cdf", &c->lma_host.nlc_cp_cl_cdf, 61 * 32 * 2, true},
+        {"nlc_lp_classical_cdf", &c->lma_host.nlc_lp_cl_cdf, 61 * 16 * 2, true},
     };
     CUDA_TRY(cudaSetDevice(c->device));
     for (auto& w : wants) {
@@ -770,15 +787,26 @@ static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
 // to 1.5x the reference's harmonic sum limit at 1.05 a0 (its eta -> 0 bound);
 // a sampled order beyond that retires the particle with PTG_ERR_UNSUPPORTED.
 // The workspace stays within min(8 GiB, free / 4), which may cap the grid.
-static ptg_status ensure_dbw(ptg_ctx* c, double a0, int grid_wanted, double** ws, int* cap_out, int* grid_out) {
+static ptg_status ensure_dbw(ptg_ctx* c, double a0, int grid_wanted, WaveArgs* a, int* grid_out) {
     double A = 1.05 * a0;
     int n_cap = (int)std::ceil(1.5 * (6.0 * (1.0 + A * A) + 2.0 * A * A * A)) + 16;
     int cap = db_len_for(n_cap);
     size_t per_block = (size_t)cap * 5 * 32 * sizeof(double) * (size_t)((c->block + 31) / 32);
     size_t free_b = 0, total_b = 0;
     CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    size_t budget = std::min<size_t>((size_t)8 << 30, (free_b + c->dbw_bytes) / 4);
-    size_t max_blocks = budget / per_block;
+    size_t budget = std::min<size_t>((size_t)8 << 30, (free_b + c->dbw_bytes + c->dbpool_bytes) / 4);
+    // the shared pool: harmonics of pair creation down to the smallest eta
+    // where the LP rate is not negligible (pair_creation/lp/mod.rs:371-374),
+    // clipped to the tables' eta >= 0.002
+    double l = std::log10(A) + 2.0;
+    double eta_min = std::max(std::pow(10.0, -1.0 - l * l / 4.5), 0.002);
+    int p_min, p_max;
+    lpp_sum_limits(A, eta_min, &p_min, &p_max);
+    int pool_cap = db_len_for(std::max(p_max + 16, n_cap));
+    size_t slot_bytes = (size_t)pool_cap * 5 * sizeof(double);
+    int slots = (int)std::min<size_t>(64, (budget / 4) / slot_bytes);
+    size_t pool_bytes = slots > 0 ? slot_bytes * (size_t)slots + 256 + 4 * (size_t)slots : 0;
+    size_t max_blocks = (budget - std::min(budget, pool_bytes)) / per_block;
     if (max_blocks < 1)
         return set_err(PTG_ERR_ALLOC, "no room for one block of LP LMA workspaces at a0 = " + std::to_string(a0));
     int grid = grid_wanted;
@@ -794,8 +822,27 @@ static ptg_status ensure_dbw(ptg_ctx* c, double a0, int grid_wanted, double** ws
         }
         c->dbw_bytes = need;
     }
-    *ws = (double*)c->dbw;
-    *cap_out = cap;
+    if (pool_bytes > c->dbpool_bytes) {
+        cudaFree(c->dbpool);
+        c->dbpool = nullptr;
+        c->dbpool_bytes = 0;
+        if (cudaMalloc(&c->dbpool, pool_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(PTG_ERR_ALLOC, "cannot allocate the shared J(n, x, y) pool");
+        }
+        c->dbpool_bytes = pool_bytes;
+    }
+    a->dbw = (double*)c->dbw;
+    a->db_cap = cap;
+    a->dbpool = DbPool{};
+    if (slots > 0) {
+        size_t state_off = (slot_bytes * (size_t)slots + 255) & ~(size_t)255;
+        a->dbpool.base = (double*)c->dbpool;
+        a->dbpool.state = (unsigned*)((char*)c->dbpool + state_off);
+        a->dbpool.cap = pool_cap;
+        a->dbpool.slots = slots;
+        CUDA_TRY(cudaMemsetAsync(a->dbpool.state, 0, 4 * (size_t)slots, c->stream));
+    }
     *grid_out = grid;
     return PTG_OK;
 }
@@ -854,11 +901,12 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
     a.o.dt = dt_max * o->dt_multiplier;
     a.gl = c->gl;
     a.lma = c->lma_dev;
+    a.mlp = mlp_params(c);
     a.dbw = nullptr;
     a.db_cap = 0;
     c->grid_cap = 0;
     if (!lcfa && laser->polarization != PTG_POL_CIRCULAR) {
-        st = ensure_dbw(c, laser->a0, grid_for(c, wave_kernel(laser->model)), &a.dbw, &a.db_cap, &c->grid_cap);
+        st = ensure_dbw(c, laser->a0, grid_for(c, wave_kernel(laser->model)), &a, &c->grid_cap);
         if (st != PTG_OK) return st;
     }
     a.seed = seed;
@@ -1289,6 +1337,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     fill_step_options(*o, &q.base.o);
     q.base.gl = c->gl;
     q.base.lma = c->lma_dev;
+    q.base.mlp = mlp_params(c);
     q.base.n_primaries = n;
     q.coll = c->d_coll;
     q.stats = c->d_cstats;
@@ -1298,7 +1347,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     // last showers; generous, but bounded
     q.wait_ns = (unsigned long long)(20.0e9 + 2.0e3 * (double)n);
     if (any_lp_lma) {
-        st = ensure_dbw(c, lp_lma_a0, grid, &q.base.dbw, &q.base.db_cap, &grid);
+        st = ensure_dbw(c, lp_lma_a0, grid, &q.base, &grid);
         if (st != PTG_OK) return st;
     }
     unsigned long long want = c->cap;
@@ -1804,6 +1853,437 @@ ptg_status ptg_regen_nlc_cp_cdf(ptg_ctx* c, double* cdf_out, double* total_out) 
     }
     cleanup();
     if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    return PTG_OK;
+}
+
+
+ptg_status ptg_regen_bw_lp_mid_cdf(ptg_ctx* c, double* cdf_out, double* total_out) {
+    if (!c || !cdf_out || !total_out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    const int NC = 36, NR = 157, NP = NC * NR;
+    std::vector<int> nmin(NP), nmax(NP);
+    std::vector<unsigned long long> off(NP);
+    std::vector<int> n_of;
+    std::vector<double> a_of, eta_of;
+    int n_top = 1;
+    for (int i = 0; i < NR; ++i) {
+        double ep = std::exp(PTG_BW_LPM_LN_MAX_ETA_PRIME) / (1.0 + (double)i / PTG_BW_LPM_ETA_PRIME_DENSITY);
+        for (int j = 0; j < NC; ++j) {
+            double a = std::exp(PTG_BW_LPM_LN_MIN_A) * std::pow(10.0, (double)j / 20.0);
+            double eta = (1.0 + 0.5 * a * a) * ep;
+            int p = i * NC + j;
+            lpp_sum_limits(a, eta, &nmin[p], &nmax[p]);
+            if (nmax[p] < nmin[p]) nmax[p] = nmin[p];
+            off[p] = n_of.size();
+            for (int n = nmin[p]; n <= nmax[p]; ++n) {
+                n_of.push_back(n);
+                a_of.push_back(a);
+                eta_of.push_back(eta);
+                n_top = std::max(n_top, n);
+            }
+        }
+    }
+    size_t jobs = n_of.size();
+    int cap = db_len_for(n_top);
+    const size_t chunk = 32768;
+    int *d_n = nullptr, *d_nmin = nullptr, *d_nmax = nullptr, *d_bad = nullptr;
+    double *d_a = nullptr, *d_eta = nullptr, *d_rates = nullptr, *d_ws = nullptr, *d_cdf = nullptr, *d_tot = nullptr;
+    unsigned long long* d_off = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_n), cudaFree(d_nmin), cudaFree(d_nmax), cudaFree(d_bad), cudaFree(d_a), cudaFree(d_eta);
+        cudaFree(d_rates), cudaFree(d_ws), cudaFree(d_cdf), cudaFree(d_tot), cudaFree(d_off);
+    };
+    bool ok = cudaMalloc(&d_n, 4 * jobs) == cudaSuccess && cudaMalloc(&d_a, 8 * jobs) == cudaSuccess &&
+              cudaMalloc(&d_eta, 8 * jobs) == cudaSuccess && cudaMalloc(&d_rates, 16 * jobs) == cudaSuccess &&
+              cudaMalloc(&d_ws, (size_t)cap * 40 * chunk) == cudaSuccess && cudaMalloc(&d_nmin, 4 * NP) == cudaSuccess &&
+              cudaMalloc(&d_nmax, 4 * NP) == cudaSuccess && cudaMalloc(&d_off, 8 * NP) == cudaSuccess &&
+              cudaMalloc(&d_cdf, 8 * 48 * NP) == cudaSuccess && cudaMalloc(&d_tot, 16 * NP) == cudaSuccess &&
+              cudaMalloc(&d_bad, 4) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cleanup();
+        return set_err(PTG_ERR_ALLOC, "table regeneration buffers");
+    }
+    cudaMemcpy(d_n, n_of.data(), 4 * jobs, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_a, a_of.data(), 8 * jobs, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_eta, eta_of.data(), 8 * jobs, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_nmin, nmin.data(), 4 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_nmax, nmax.data(), 4 * NP, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_off, off.data(), 8 * NP, cudaMemcpyHostToDevice);
+    cudaMemset(d_bad, 0, 4);
+    cudaError_t e = cudaSuccess;
+    for (size_t first = 0; first < jobs && e == cudaSuccess; first += chunk) {
+        size_t count = std::min(chunk, jobs - first);
+        e = launch_regen_lpm_partial(first, count, d_n, d_a, d_eta, d_ws, cap, d_rates, d_bad, c->stream);
+    }
+    if (e == cudaSuccess) e = launch_regen_lpm_cdf(NP, d_nmin, d_nmax, d_off, d_rates, d_cdf, d_tot, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    int bad = 0;
+    if (e == cudaSuccess) {
+        cudaMemcpy(&bad, d_bad, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(cdf_out, d_cdf, 8 * 48 * NP, cudaMemcpyDeviceToHost);
+        cudaMemcpy(total_out, d_tot, 16 * NP, cudaMemcpyDeviceToHost);
+    }
+    cleanup();
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    if (bad) return set_err(PTG_ERR_UNSUPPORTED, "harmonic beyond the J(n, x, y) workspace during regeneration");
+    return PTG_OK;
+}
+
+
+// FP64 FMA throughput: eight independent chains per thread, so that the
+// pipe, not the dependency latency, bounds it.
+__global__ void k_fp64_fma(int iters, double a, double b, double* sink) {
+    double x[8];
+    for (int k = 0; k < 8; ++k) x[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i)
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    double acc = 0.0;
+    for (int k = 0; k < 8; ++k) acc += x[k];
+    if (acc == 12345.678) sink[0] = acc;  // keeps the chains live
+}
+
+ptg_status ptg_fp64_peak(ptg_ctx* c, double* tflops) {
+    if (!c || !tflops) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    CUDA_TRY(cudaSetDevice(c->device));
+    double* sink = nullptr;
+    CUDA_TRY(cudaMalloc(&sink, 8));
+    const int iters = 4096, block = 256, grid = 8 * c->num_sms;
+    k_fp64_fma<<<grid, block, 0, c->stream>>>(iters, 0.999999, 1e-9, sink);
+    CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+    for (int r = 0; r < 5; ++r) k_fp64_fma<<<grid, block, 0, c->stream>>>(iters, 0.999999, 1e-9, sink);
+    CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+    CUDA_TRY(cudaEventSynchronize(c->ev1));
+    float ms = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    cudaFree(sink);
+    *tflops = 5.0 * 2.0 * 8.0 * iters * (double)grid * block / (ms * 1e-3) / 1e12;
+    return PTG_OK;
+}
+
+
+// ---------------------------------------------------- learned proposal ---
+static const int MLP_GRAD_BLOCKS = 64;
+
+static MlpDev mlp_dev(ptg_ctx* c) {
+    MlpDev m{};
+    __nv_bfloat16* b = c->mlp_bf;
+    m.w0 = b;
+    m.w1 = m.w0 + MLP_H * MLP_IN_PAD;
+    m.w2 = m.w1 + MLP_H * MLP_H;
+    m.w3 = m.w2 + MLP_H * MLP_H;
+    m.t1 = m.w3 + MLP_OUT * MLP_H;
+    m.t2 = m.t1 + MLP_H * MLP_H;
+    m.t3 = m.t2 + MLP_H * MLP_H;
+    m.p = c->mlp_p;
+    return m;
+}
+
+// The collision kernels' view (disabled unless a trained network is in use).
+static MlpParams mlp_params(ptg_ctx* c) {
+    MlpParams p{};
+    if (!c->mlp_ready || !c->mlp_enabled) return p;
+    MlpDev m = mlp_dev(c);
+    p.w0 = m.w0, p.w1 = m.w1, p.w2 = m.w2, p.w3 = m.w3;
+    p.b0 = c->mlp_p + P_B0, p.b1 = c->mlp_p + P_B1, p.b2 = c->mlp_p + P_B2, p.b3 = c->mlp_p + P_B3;
+    p.margin = c->mlp_margin;
+    p.enabled = 1;
+    return p;
+}
+
+static ptg_status mlp_alloc(ptg_ctx* c) {
+    if (c->mlp_p) return PTG_OK;
+    size_t np = P_TOTAL;
+    size_t nbf = (size_t)MLP_H * MLP_IN_PAD + 3 * (size_t)MLP_H * MLP_H + 2 * (size_t)MLP_OUT * MLP_H + 2 * 64;
+    if (cudaMalloc(&c->mlp_p, 4 * np) != cudaSuccess || cudaMalloc(&c->mlp_m, 4 * np) != cudaSuccess ||
+        cudaMalloc(&c->mlp_v, 4 * np) != cudaSuccess ||
+        cudaMalloc(&c->mlp_partial, 4 * np * MLP_GRAD_BLOCKS) != cudaSuccess ||
+        cudaMalloc(&c->mlp_loss, 4 * MLP_GRAD_BLOCKS) != cudaSuccess || cudaMalloc(&c->mlp_bf, 2 * nbf) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "learned-proposal buffers");
+    }
+    CUDA_TRY(cudaMemset(c->mlp_bf, 0, 2 * nbf));
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_init(ptg_ctx* c, uint64_t seed) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    CUDA_TRY(cudaSetDevice(c->device));
+    ptg_status st = mlp_alloc(c);
+    if (st != PTG_OK) return st;
+    // uniform He initialisation from a splitmix sequence; biases zero
+    std::vector<float> p(P_TOTAL, 0.0f);
+    uint64_t z = seed;
+    auto uni = [&]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](int off, int rows, int cols, int used_cols, int fan_in) {
+        double lim = std::sqrt(6.0 / fan_in);
+        for (int r = 0; r < rows; ++r)
+            for (int k = 0; k < cols; ++k)
+                p[off + r * cols + k] = k < used_cols ? (float)((2.0 * uni() - 1.0) * lim) : 0.0f;
+    };
+    fill(P_W0, MLP_H, MLP_IN_PAD, MLP_IN, MLP_IN);
+    fill(P_W1, MLP_H, MLP_H, MLP_H, MLP_H);
+    fill(P_W2, MLP_H, MLP_H, MLP_H, MLP_H);
+    fill(P_W3, MLP_OUT, MLP_H, MLP_H, MLP_H);
+    CUDA_TRY(cudaMemcpy(c->mlp_p, p.data(), 4 * P_TOTAL, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(c->mlp_m, 0, 4 * P_TOTAL));
+    CUDA_TRY(cudaMemset(c->mlp_v, 0, 4 * P_TOTAL));
+    c->mlp_step = 0;
+    CUDA_TRY(launch_mlp_sync(c->mlp_p, mlp_dev(c), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->mlp_ready = true;
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_params(ptg_ctx* c, float* get, const float* set, int32_t* count) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (count) *count = P_TOTAL;
+    if (!get && !set) return PTG_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    ptg_status st = mlp_alloc(c);
+    if (st != PTG_OK) return st;
+    if (set) {
+        std::vector<float> p(set, set + P_TOTAL);
+        for (int r = 0; r < MLP_H; ++r)
+            for (int k = MLP_IN; k < MLP_IN_PAD; ++k) p[P_W0 + r * MLP_IN_PAD + k] = 0.0f;
+        CUDA_TRY(cudaMemcpy(c->mlp_p, p.data(), 4 * P_TOTAL, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemset(c->mlp_m, 0, 4 * P_TOTAL));
+        CUDA_TRY(cudaMemset(c->mlp_v, 0, 4 * P_TOTAL));
+        c->mlp_step = 0;
+        CUDA_TRY(launch_mlp_sync(c->mlp_p, mlp_dev(c), c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        c->mlp_ready = true;
+    }
+    if (get) {
+        if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: call ptg_mlp_init or set parameters");
+        CUDA_TRY(cudaMemcpy(get, c->mlp_p, 4 * P_TOTAL, cudaMemcpyDeviceToHost));
+    }
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_grad(ptg_ctx* c, const float* samples, size_t n, float tau, float* grad, float* loss) {
+    if (!c || !samples || !grad) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: call ptg_mlp_init first");
+    if (n == 0 || n > (1u << 24)) return set_err(PTG_ERR_INVALID_ARGUMENT, "sample count out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    std::vector<char> buf(mlp_sample_bytes() * n);
+    for (size_t i = 0; i < n; ++i) {
+        float v[5] = {samples[5 * i], samples[5 * i + 1], samples[5 * i + 2], 0.0f, samples[5 * i + 4]};
+        int bin = (int)samples[5 * i + 3];
+        std::memcpy(&buf[i * 20], v, 12);
+        std::memcpy(&buf[i * 20 + 12], &bin, 4);
+        std::memcpy(&buf[i * 20 + 16], &v[4], 4);
+    }
+    void* d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, buf.size()));
+    cudaMemcpy(d, buf.data(), buf.size(), cudaMemcpyHostToDevice);
+    cudaError_t e = launch_mlp_grad(mlp_dev(c), d, 0, (int)n, tau, c->mlp_partial, c->mlp_loss, MLP_GRAD_BLOCKS, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    std::vector<float> part((size_t)P_TOTAL * MLP_GRAD_BLOCKS), ls(MLP_GRAD_BLOCKS);
+    if (e == cudaSuccess) {
+        cudaMemcpy(part.data(), c->mlp_partial, 4 * part.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(ls.data(), c->mlp_loss, 4 * ls.size(), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d);
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    for (int i = 0; i < P_TOTAL; ++i) {
+        double g = 0.0;
+        for (int b = 0; b < MLP_GRAD_BLOCKS; ++b) g += part[(size_t)b * P_TOTAL + i];
+        grad[i] = (float)g;
+    }
+    if (loss) {
+        double l = 0.0;
+        for (float v : ls) l += v;
+        *loss = (float)(l / (double)n);
+    }
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_infer(ptg_ctx* c, const float* x, size_t n, float* out) {
+    if (!c || !x || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: call ptg_mlp_init first");
+    if (n == 0) return PTG_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    float *dx = nullptr, *dout = nullptr;
+    CUDA_TRY(cudaMalloc(&dx, 12 * n));
+    if (cudaMalloc(&dout, 64 * n) != cudaSuccess) {
+        cudaFree(dx);
+        return set_err(PTG_ERR_ALLOC, "inference buffers");
+    }
+    cudaMemcpy(dx, x, 12 * n, cudaMemcpyHostToDevice);
+    cudaError_t e = launch_mlp_infer(mlp_dev(c), dx, n, dout, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) cudaMemcpy(out, dout, 64 * n, cudaMemcpyDeviceToHost);
+    cudaFree(dx), cudaFree(dout);
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_train(ptg_ctx* c, const ptg_mlp_train_cfg* cfg, ptg_mlp_train_stats* stats) {
+    if (!c || !cfg) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cfg->n_samples < 1024 || cfg->batch < 64 || cfg->epochs < 1 || !(cfg->lr > 0.0f) ||
+        !(cfg->tau > 0.0f && cfg->tau < 1.0f))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "training configuration out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->tables_loaded) {
+        ptg_status st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    if (!c->lma_host.nlc_cp_cdf) return set_err(PTG_ERR_TABLES, "the CP harmonic CDF table is needed");
+    if (!c->mlp_ready) {
+        ptg_status st = ptg_mlp_init(c, cfg->seed ^ 0x5DEECE66Dull);
+        if (st != PTG_OK) return st;
+    }
+    void* data = nullptr;
+    size_t bytes = mlp_sample_bytes() * cfg->n_samples;
+    if (cudaMalloc(&data, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "training data (" + std::to_string(bytes) + " bytes)");
+    }
+    CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+    cudaError_t e = launch_mlp_data(c->lma_dev, cfg->n_samples, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo,
+                                    cfg->eta_hi, data, c->stream);
+    cudaEvent_t ev_mid = nullptr;
+    cudaEventCreate(&ev_mid);
+    cudaEventRecord(ev_mid, c->stream);
+    unsigned long long steps_per_epoch = cfg->n_samples / (unsigned long long)cfg->batch;
+    long long total = (long long)steps_per_epoch * cfg->epochs;
+    float loss_first = NAN, loss_last = NAN;
+    std::vector<float> ls(MLP_GRAD_BLOCKS);
+    for (long long k = 0; k < total && e == cudaSuccess; ++k) {
+        unsigned long long first = (unsigned long long)(k % (long long)steps_per_epoch) * cfg->batch;
+        // cosine decay of the learning rate
+        float lr = cfg->lr * 0.5f * (1.0f + std::cos(3.14159265f * (float)k / (float)total));
+        e = launch_mlp_grad(mlp_dev(c), data, first, cfg->batch, cfg->tau, c->mlp_partial, c->mlp_loss,
+                            MLP_GRAD_BLOCKS, c->stream);
+        if (e == cudaSuccess)
+            e = launch_mlp_adam(c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_partial, MLP_GRAD_BLOCKS, lr, ++c->mlp_step,
+                                mlp_dev(c), c->stream);
+        if (e == cudaSuccess && (k == 0 || k == total - 1)) {
+            e = cudaMemcpyAsync(ls.data(), c->mlp_loss, 4 * MLP_GRAD_BLOCKS, cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            double l = 0.0;
+            for (float v : ls) l += v;
+            (k == 0 ? loss_first : loss_last) = (float)(l / cfg->batch);
+        }
+    }
+    cudaEventRecord(c->ev1, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    float ms_data = 0.0f, ms_all = 0.0f;
+    cudaEventElapsedTime(&ms_data, c->ev0, ev_mid);
+    cudaEventElapsedTime(&ms_all, c->ev0, c->ev1);
+    cudaEventDestroy(ev_mid);
+    cudaFree(data);
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    if (stats) {
+        stats->loss_first = loss_first;
+        stats->loss_last = loss_last;
+        stats->steps = (int32_t)total;
+        stats->data_ms = ms_data;
+        stats->train_ms = ms_all - ms_data;
+    }
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_use(ptg_ctx* c, int32_t enabled, float margin) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (enabled && !c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: train or load one first");
+    if (!(margin >= 0.0f && margin < 10.0f)) return set_err(PTG_ERR_INVALID_ARGUMENT, "margin out of range");
+    c->mlp_enabled = enabled != 0;
+    c->mlp_margin = margin;
+    return PTG_OK;
+}
+
+ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
+                             ptg_sampler_bench_stats* stats) {
+    if (!c || !cfg) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: train or load one first");
+    if (cfg->n == 0 || cfg->n > (1ull << 28)) return set_err(PTG_ERR_INVALID_ARGUMENT, "sample count out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->tables_loaded) {
+        ptg_status st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    unsigned long long n = cfg->n;
+    float *dx = nullptr, *denv = nullptr;
+    double *dv0 = nullptr, *dv1 = nullptr;
+    unsigned *de0 = nullptr, *de1 = nullptr, *df = nullptr;
+    int* dst = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dx), cudaFree(denv), cudaFree(dv0), cudaFree(dv1), cudaFree(de0), cudaFree(de1), cudaFree(df);
+        cudaFree(dst);
+    };
+    bool ok = cudaMalloc(&dx, 12 * n) == cudaSuccess && cudaMalloc(&denv, 64 * n) == cudaSuccess &&
+              cudaMalloc(&dv0, 8 * n) == cudaSuccess && cudaMalloc(&dv1, 8 * n) == cudaSuccess &&
+              cudaMalloc(&de0, 4 * n) == cudaSuccess && cudaMalloc(&de1, 4 * n) == cudaSuccess &&
+              cudaMalloc(&df, 4 * n) == cudaSuccess && cudaMalloc(&dst, 4 * n) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cleanup();
+        return set_err(PTG_ERR_ALLOC, "sampler benchmark buffers");
+    }
+    cudaEvent_t e[6];
+    for (auto& ev : e) cudaEventCreate(&ev);
+    cudaStream_t s = c->stream;
+    cudaError_t err = cudaSuccess;
+    // plain: the reference's ceiling and rejection
+    cudaEventRecord(e[0], s);
+    err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
+                               cfg->margin, nullptr, dv0, de0, df, dst, s);
+    cudaEventRecord(e[1], s);
+    // learned: features, batched tensor-core inference, then sampling
+    if (err == cudaSuccess)
+        err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1,
+                                   nullptr, cfg->margin, dx, nullptr, nullptr, nullptr, nullptr, s);
+    cudaEventRecord(e[2], s);
+    if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), dx, n, denv, s);
+    cudaEventRecord(e[3], s);
+    if (err == cudaSuccess)
+        err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1, denv,
+                                   cfg->margin, nullptr, dv1, de1, df, dst, s);
+    cudaEventRecord(e[4], s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    std::vector<unsigned> ev0(n), ev1(n), fb(n);
+    std::vector<int> status(n);
+    if (err == cudaSuccess) {
+        if (v_plain) cudaMemcpy(v_plain, dv0, 8 * n, cudaMemcpyDeviceToHost);
+        if (v_learned) cudaMemcpy(v_learned, dv1, 8 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(ev0.data(), de0, 4 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(ev1.data(), de1, 4 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(fb.data(), df, 4 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(status.data(), dst, 4 * n, cudaMemcpyDeviceToHost);
+    }
+    float t_plain = 0, t_feat = 0, t_inf = 0, t_learn = 0;
+    cudaEventElapsedTime(&t_plain, e[0], e[1]);
+    cudaEventElapsedTime(&t_feat, e[1], e[2]);
+    cudaEventElapsedTime(&t_inf, e[2], e[3]);
+    cudaEventElapsedTime(&t_learn, e[3], e[4]);
+    for (auto& ev : e) cudaEventDestroy(ev);
+    cleanup();
+    if (err != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(err));
+    if (stats) {
+        double s0 = 0, s1 = 0;
+        unsigned long long nf = 0, ne = 0;
+        for (unsigned long long i = 0; i < n; ++i) {
+            s0 += ev0[i], s1 += ev1[i];
+            nf += fb[i] ? 1 : 0;
+            ne += status[i] != 0 ? 1 : 0;
+        }
+        stats->plain_ms = t_plain;
+        stats->learned_ms = t_learn;
+        stats->infer_ms = t_inf + t_feat;
+        stats->plain_evals = s0 / (double)n;
+        stats->learned_evals = s1 / (double)n;
+        stats->fallbacks = nf;
+        stats->errors = ne;
+    }
     return PTG_OK;
 }
 

@@ -21,4 +21,29 @@ cudaError_t launch_queue_v0(int grid, cudaStream_t s, const QueueArgs& q);
 cudaError_t launch_queue_v1(int grid, cudaStream_t s, const QueueArgs& q);
 const void* queue_kernel_v0();
 const void* queue_kernel_v1();
+
+// Regeneration of the LP Breit-Wheeler mid-range CDF (ptg_regen.cu).
+cudaError_t launch_regen_lpm_partial(unsigned long long first, unsigned long long count, const int* n_of,
+                                     const double* a_of, const double* eta_of, double* ws, int cap, double* rates,
+                                     int* bad, cudaStream_t s);
+cudaError_t launch_regen_lpm_cdf(int npoints, const int* nmin_of, const int* nmax_of, const unsigned long long* off_of,
+                                 const double* rates, double* cdf_out, double* total_out, cudaStream_t s);
+
+// The learned CP proposal (ptg_mlp.cu).
+struct MlpDev;
+struct LmaTables;
+cudaError_t launch_mlp_infer(const MlpDev& m, const float* x, unsigned long long n, float* out, cudaStream_t s);
+cudaError_t launch_mlp_grad(const MlpDev& m, const void* data, unsigned long long first, int rows, float tau,
+                            float* partial, float* loss, int blocks, cudaStream_t s);
+cudaError_t launch_mlp_adam(float* p, float* mom, float* vel, const float* partial, int nblocks, float lr, int step,
+                            const MlpDev& m, cudaStream_t s);
+cudaError_t launch_mlp_sync(const float* p, const MlpDev& m, cudaStream_t s);
+cudaError_t launch_mlp_data(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                            double a_hi, double e_lo, double e_hi, void* out, cudaStream_t s);
+cudaError_t launch_sampler_bench(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                                 double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
+                                 float* x_out, double* v_out, unsigned* evals, unsigned* fallbacks, int* status,
+                                 cudaStream_t s);
+int mlp_param_count();
+size_t mlp_sample_bytes();
 }  // namespace ptg

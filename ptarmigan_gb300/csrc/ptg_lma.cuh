@@ -5,7 +5,9 @@
 #include "ptg_fields.cuh"
 #include "ptg_math.cuh"
 #include "ptg_bw.cuh"
+#include "ptg_bw_lp.cuh"
 #include "ptg_lp.cuh"
+#include "ptg_mlp.cuh"
 #include "ptg_nlc.cuh"
 
 namespace ptg {
@@ -23,10 +25,13 @@ struct LmaTables {
     const double* bw_lp_cdf;        // [1525][16][3]
     const double* bw_lp_mid_total;  // [157][36][2]
     const double* bw_lp_mid_cdf;    // [5652][16][3] (regenerated)
+    const double* nlc_cp_cl_cdf;    // [61][32][2]
+    const double* nlc_lp_cl_cdf;    // [61][16][2]
 };
 
 __device__ __forceinline__ NlcTables nlc_view(const LmaTables& t) {
-    return NlcTables{t.nlc_lp_rate, t.nlc_lp_cdf, t.nlc_cp_rate, t.nlc_cp_cdf, t.nlc_cp_cl_rate, t.nlc_lp_cl_rate};
+    return NlcTables{t.nlc_lp_rate,    t.nlc_lp_cdf,     t.nlc_cp_rate,   t.nlc_cp_cdf,
+                     t.nlc_cp_cl_rate, t.nlc_lp_cl_rate, t.nlc_cp_cl_cdf, t.nlc_lp_cl_cdf};
 }
 
 // Standard normal from two uniforms (Box-Muller), for the finite bandwidth.
@@ -39,9 +44,10 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
 // nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
 // `dbw` is this lane's DoubleBessel workspace (linear polarisation only).
 // Returns a ptg status (0 = ok).
-static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw, d4 r, d4 u,
-                                        double dt, Draws& rng, bool classical, bool* emitted, d4* k_out, d4* u_prime,
-                                        d3* pol, double* a_eff, double* chi, double* absorption, uint32_t* rej) {
+static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw,
+                                               const MlpParams& mlp, d4 r, d4 u, double dt, Draws& rng, bool classical,
+                                               bool* emitted, d4* k_out, d4* u_prime, d3* pol, double* a_eff,
+                                               double* chi, double* absorption, uint32_t* rej) {
     *emitted = false;
     double a = sqrt(lma_a_sqd(f, r));
     double chirp = 1.0;
@@ -70,12 +76,28 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
     if (!ok) return 2;  // PTG_ERR_OUT_OF_TABLE
     double prob = ALPHA_FINE * rate * dphi / eta;
     if (rng.next() < prob) {
-        if (classical) return 9;  // PTG_ERR_UNSUPPORTED: classical LMA samplers not built
         int n;
         double s, cphi;
         d3 sv;
-        int st = f.circular ? cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
-                            : lp_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
+        int st;
+        if (f.circular && !classical && mlp.enabled) {
+            // the learned proposal for v (ptg_mlp.cuh): same harmonic
+            // draw, exact accept/reject against the spectrum
+            n = cp_invert(nt, aq, eta, rng.next());
+            if (n < 1) n = 1;
+            float x[3], o[MLP_OUT];
+            mlp_features(aq, eta, n, x);
+            mlp_forward_lane(mlp, x, o);
+            LearnedCounts lc{0, 0, 0};
+            double v = 0.0;
+            st = cp_sample_v_learned(o, mlp.margin, n, aq, eta, rng, &v, rej, &lc);
+            if (st == 0) cp_finish(n, aq, eta, v, rng, &s, &cphi, &sv);
+        } else if (f.circular)
+            st = classical ? cp_classical_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
+                           : cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
+        else
+            st = classical ? lp_classical_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej)
+                           : lp_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
         if (st != 0) return st;
         d4 k;
         st = nlc_kinematics(kappa, u, aq, eta, n, s, cphi, sv, f.pol_angle, classical, &k, pol);
@@ -90,12 +112,50 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
     return 0;
 }
 
+// pair_creation/mod.rs:21-42 (LP): probability and Stokes update, peak
+// amplitude a sqrt 2 for the tables
+static __device__ __noinline__ bool lp_bw_probability(const LmaTables& t, d4 ell, d4 sv_in, d4 k, double a, double dt,
+                                                      double pol_angle, double* prob, d4* sv_out) {
+    double eta = dot4(k, ell);
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    double dphi = eta * dt / (COMPTON_TIME * ell.t);
+    double f[2];
+    if (!lpp_rates(t.bw_lp_total, t.bw_lp_mid_total, a * SQRT_2, eta, f)) return false;
+    double f0 = f[0], f1 = f[1];
+    double c = ALPHA_FINE * dphi / eta;
+    double p = c * (0.5 * ((f0 + f1) + sv.x * (f0 - f1)));
+    double p_avg = c * (0.5 * (f0 + f1));
+    double delta = c * (0.5 * (f0 - f1));
+    d4 o = d4{sv.t, (sv.x * (1.0 - p_avg) - delta) / (1.0 - p), sv.y * (1.0 - p_avg) / (1.0 - p),
+              sv.z * (1.0 - p_avg) / (1.0 - p)};
+    o = stokes_rotate_by(o, -pol_angle);
+    d3 g = stokes_from_lma_basis(mk3(o.x, o.y, o.z), ell);
+    *sv_out = d4{o.t, g.x, g.y, g.z};
+    *prob = p;
+    return true;
+}
+
+// pair_creation/mod.rs:49-110 (LP)
+static __device__ __noinline__ int lp_bw_generate(const LmaTables& t, const DbWork& w, d4 ell, d4 sv_in, d4 k, double a,
+                                                  double pol_angle, Draws& rng, int* n_out, d4* q_out, uint32_t* rej) {
+    double eta = dot4(k, ell);
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    int n;
+    double s, cphi;
+    int st = lpp_sample(t.bw_lp_cdf, t.bw_lp_mid_cdf, t.bw_lp_mid_total, w, a * SQRT_2, eta, sv.x, sv.y, rng, &n, &s,
+                        &cphi, rej);
+    if (st != 0) return st;
+    *n_out = n;
+    return bw_kinematics(ell, k, a, pol_angle, n, s, cphi, q_out);
+}
+
 // plane_wave.rs:284-316 / focused_laser.rs:283-306 with
 // pair_creation::probability and generate (pair_creation/mod.rs:21-110).
-static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTables& t, d4 r, d4 ell, d4 pol, double dt,
-                                            Draws& rng, double rate_increase, double* prob, d4* pol_new,
-                                            bool* created, d4* ue, d4* up, double* frac, double* a_eff, double* chi,
-                                            double* absorption, uint32_t* rej) {
+static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const LmaTables& t, const DbWork& dbw, d4 r,
+                                                   d4 ell, d4 pol, double dt, Draws& rng, double rate_increase,
+                                                   double* prob, d4* pol_new, bool* created, d4* ue, d4* up,
+                                                   double* frac, double* a_eff, double* chi, double* absorption,
+                                                   uint32_t* rej) {
     *prob = 0.0;
     *pol_new = pol;
     *created = false;
@@ -107,13 +167,15 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
     }
     double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp;
     d4 kappa = d4{kk, 0.0, 0.0, kk};
-    if (!f.circular) return 9;  // PTG_ERR_UNSUPPORTED: LP pair sampler not built
-    if (!bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)) return 2;
+    bool ok = f.circular ? bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)
+                         : lp_bw_probability(t, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new);
+    if (!ok) return 2;
     double ri = (*prob * rate_increase > 0.1) ? 0.1 / *prob : rate_increase;
     if (rng.next() < *prob * ri) {
         int n;
         d4 q;
-        int st = bw_generate(t.bw_cp_total, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej);
+        int st = f.circular ? bw_generate(t.bw_cp_total, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej)
+                            : lp_bw_generate(t, dbw, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej);
         if (st != 0) return st;
         *ue = d4{ell.t + n * kappa.t - q.t, ell.x + n * kappa.x - q.x, ell.y + n * kappa.y - q.y, ell.z + n * kappa.z - q.z};
         *up = q;

@@ -54,10 +54,43 @@ __host__ __device__ __forceinline__ cxd cx_acos(cxd z) {
 }
 
 // ----------------------------------------------------- DoubleBessel -----
-struct DbWork {
-    double* base;  // this lane's slot: coefficient c of order e at base[(5 e + c) * 32]
-    int cap;       // orders the slot holds
+// A pool of large workspaces shared by all lanes, for harmonic orders
+// beyond a lane's own slot (pair creation at small eta).  Slot k holds
+// `cap` orders at base + k * cap * 5; state[k] is 0 (free) or 1 (taken).
+struct DbPool {
+    double* base;
+    unsigned* state;
+    int cap, slots;
 };
+
+struct DbWork {
+    double* base;  // coefficient c of order e at base[(5 e + c) * stride]
+    int cap;       // orders the slot holds
+    int stride;    // 32 for a lane-interleaved warp slot, 1 for a pooled slot
+    DbPool pool;   // larger slots for orders beyond `cap` (may be empty)
+};
+
+// Takes a free pool slot (bounded wait: slots are held only for the
+// duration of one sample).  Returns -1 if none freed up in time.
+__device__ __forceinline__ int db_pool_acquire(const DbPool& p, unsigned hint) {
+    if (!p.base || p.slots <= 0) return -1;
+    for (int it = 0; it < (1 << 16); ++it) {
+        for (int q = 0; q < p.slots; ++q) {
+            int k = (int)((hint + (unsigned)q) % (unsigned)p.slots);
+            if (atomicCAS(p.state + k, 0u, 1u) == 0u) {
+                __threadfence();
+                return k;
+            }
+        }
+        __nanosleep(2000);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void db_pool_release(const DbPool& p, int k) {
+    __threadfence();
+    atomicExch(p.state + k, 0u);
+}
 
 struct DbGeom {
     int n, k_min, len;
@@ -101,7 +134,8 @@ struct Ssq {
 static __host__ __device__ __noinline__ bool db_around(const DbGeom& g, const DbWork& w, double x, double y, double j[5]) {
     const int len = g.len;
     double* W = w.base;
-#define DBW(e, c) W[((size_t)(e) * 5 + (c)) * 32]
+    const size_t stride = (size_t)w.stride;
+#define DBW(e, c) W[((size_t)(e) * 5 + (c)) * stride]
     // forward recurrence from the default element (all coefficients 1)
     {
         double p0 = 1.0, p1 = 1.0, p2 = 1.0, q0 = 1.0, q1 = 1.0;
@@ -402,7 +436,9 @@ __device__ __forceinline__ bool lp_classical_rate(const NlcTables& t, double a, 
     int ix = (int)((x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
     if (ix >= 60) return false;
     double dx = (x - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
-    *out = eta * exp((1.0 - dx) * t.lp_cl_rate[ix] + dx * t.lp_cl_rate[ix + 1]);
+    double f = (1.0 - dx) * t.lp_cl_rate[ix] + dx * t.lp_cl_rate[ix + 1];
+    double prefactor = 2.0 * eta / (1.0 + 0.5 * a * a);
+    *out = prefactor * exp(f);
     return true;
 }
 
@@ -472,6 +508,29 @@ static __device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double 
     return isfinite(n) ? (int)ceil(n) : -1;
 }
 
+static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork& w, const DbGeom& g, double a,
+                                               double eta, Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                               d3* sv_out, uint32_t* rej);
+
+// The workspace for harmonic n: the lane's own slot, or a pooled one
+// (returned in *slot, to release) when n needs more orders.
+__device__ __forceinline__ int db_take(const DbWork& w, int n, DbWork* wk, DbGeom* g, int* slot) {
+    *slot = -1;
+    if (db_geom(n, w.cap, g)) {
+        *wk = w;
+        return 0;
+    }
+    int k = db_pool_acquire(w.pool, (unsigned)(blockIdx.x * 131u + threadIdx.x));
+    if (k < 0) return w.pool.slots > 0 ? 11 : 9;  // PTG_ERR_TIMEOUT / PTG_ERR_UNSUPPORTED
+    *wk = DbWork{w.pool.base + (size_t)k * w.pool.cap * 5, w.pool.cap, 1, w.pool};
+    if (!db_geom(n, w.pool.cap, g)) {
+        db_pool_release(w.pool, k);
+        return 9;
+    }
+    *slot = k;
+    return 0;
+}
+
 // nonlinear_compton/lp/mod.rs:586-676: harmonic, s, azimuth theta in
 // [0, 2 pi) and the Stokes vector (in the LMA basis) of the emitted photon.
 // Returns a ptg status.
@@ -480,8 +539,21 @@ static __device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w
     if (t.lp_cdf == nullptr || w.base == nullptr) return 8;  // PTG_ERR_TABLES
     int n = lp_harmonic_index(t, a, eta, rng.next());
     if (n < 1) return 2;  // PTG_ERR_OUT_OF_TABLE
+    DbWork wk;
+    int slot = -1;
     DbGeom g;
-    if (!db_geom(n, w.cap, &g)) return 9;  // PTG_ERR_UNSUPPORTED: order beyond the workspace
+    int st = db_take(w, n, &wk, &g, &slot);
+    if (st != 0) return st;
+    st = lp_sample_n(t, wk, g, a, eta, rng, n_out, s_out, theta_out, sv_out, rej);
+    if (slot >= 0) db_pool_release(w.pool, slot);
+    return st;
+}
+
+// lp_sample for a harmonic whose J(n, x, y) workspace is ready.
+static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork& w, const DbGeom& g, double a,
+                                               double eta, Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                               d3* sv_out, uint32_t* rej) {
+    int n = g.n;
     ThetaBound tb;
     theta_bound(n, a, eta, &tb);
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
@@ -531,6 +603,168 @@ static __device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w
     *s_out = s;
     *theta_out = theta;
     return 0;
+}
+
+
+// ---------------------------------------------- classical LP emission ----
+// nonlinear_compton/lp/classical.rs:19-40 (v = s / s_max)
+static __device__ __noinline__ double lp_cl_ddpr(double a, double v, double theta, const DbGeom& g, const DbWork& w) {
+    int n = g.n;
+    double x = 2.0 * n * a * cos(theta) * sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+    double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+    double j[5];
+    if (!db_evaluate(g, w, x, y, j)) return NAN;
+    double g0, g1, g2;
+    if (n % 2 == 0) {
+        g0 = j[2], g1 = -0.5 * (j[1] + j[3]), g2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        g0 = -j[2], g1 = 0.5 * (j[1] + j[3]), g2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    return (-g0 * g0 - a * a * (g0 * g2 - g1 * g1)) / (2.0 * PI);
+}
+
+// nonlinear_compton/lp/classical.rs:43-108
+static __device__ __noinline__ double lp_cl_ceiling(double a, const DbGeom& g, const DbWork& w) {
+    int n = g.n;
+    double mx = NAN;
+    if (n == 1) {
+        mx = lp_cl_ddpr(a, 0.01, PI / 2.0, g, w);
+    } else if (a <= 1.5) {
+        double v_min = 0.1 + (9.0 / sqrt((double)n) - 1.0) / 10.0;
+        double v_max = fmin(v_min + 0.4, 1.0);
+        for (int i = 1; i <= 16; ++i) mx = rmax(mx, lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / 16.0, 0.0, g, w));
+    } else if (a < 5.0) {
+        double nsw = 3.0 * pow(a / 2.0, 4.0 / 3.0);
+        int n_switch = nsw >= 2147483647.0 ? 2147483647 : (int)nsw;
+        double theta = n > n_switch ? 0.0 : (PI / 2.0) * (1.0 - log((double)n) / log((double)n_switch));
+        double v_min = fmin(0.35 + (7.0 / sqrt((double)n) - 1.0) / 9.0, 0.55);
+        double v_max = 0.55 + (7.0 / sqrt((double)n) - 1.0) / 9.0;
+        int num = a > 4.0 ? 32 : 16;
+        for (int i = 0; i < num; ++i) mx = rmax(mx, lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / num, theta, g, w));
+    } else {
+        double n_switch = 10.0 * (a / 5.0) * (a / 5.0);
+        double theta = 0.0;
+        if (!(n > (int)n_switch)) {
+            double pw = 0.3 + (0.7 - 0.3) * (log(a) - log(5.0)) / (log(20.0) - log(5.0));
+            theta = (PI / 2.0) * (pow((double)n, -pw) - pow(n_switch, -pw)) / (1.0 - pow(n_switch, -pw));
+        }
+        double v_min = 0.3 + 0.4 * log((double)n) * pow((double)n, -0.7);
+        double v_max = v_min + 0.2;
+        int num = a > 8.0 ? 64 : 32;
+        for (int i = 0; i < num; ++i) mx = rmax(mx, lp_cl_ddpr(a, v_min + (v_max - v_min) * (double)i / num, theta, g, w));
+    }
+    return 1.1 * mx;
+}
+
+// nonlinear_compton/lp/mod.rs:209-268 (ThetaBound at fixed v)
+static __device__ __noinline__ void theta_bound_low_eta(int n, double a, ThetaBound* tb) {
+    for (int i = 0; i < 16; ++i) {
+        double z = cos(PI * i / 15.0);
+        double v = 0.5 * (z + 1.0);
+        tb->s[i] = v;
+        double x = 2.0 * n * a * sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+        double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+        double x_crit = y > n / 6.0 ? 4.0 * sqrt(y) * sqrt(n - 2.0 * y) : n + 2.0 * y;
+        double ln_j_crit = log(0.443) - log((double)n) / 3.0;
+        double ln_j_bdy = fmin(ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y), ln_j_crit);
+        double ct = fmax(1.0 - x_crit * log(0.01) / (x * (ln_j_bdy - ln_j_crit)), -1.0);
+        double fi = acos(ct);
+        tb->f[i] = isnan(fi) ? PI : fi;
+    }
+    double f_min = tb->f[0];
+    for (int i = 1; i < 16; ++i) {
+        if (tb->f[i] < f_min)
+            f_min = tb->f[i];
+        else
+            tb->f[i] = f_min;
+    }
+}
+
+// nonlinear_compton/lp/classical.rs:213-252 (cdf_table [61][16][2])
+static __device__ __noinline__ int lp_cl_harmonic_index(const NlcTables& t, double a, double frac) {
+    if (log(a) <= PTG_NLC_CL_MIN) return 1;
+    int ix = (int)((log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    double dx = (log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    if (ix >= 60) return -1;
+    double n = 0.0;
+    for (int k = 0; k < 2; ++k) {
+        const double* tb = t.lp_cl_cdf + (size_t)(ix + k) * 32;
+        double nk = 0.9;
+        if (!(frac <= tb[1]) && !pw_invert(tb, 16, false, frac, &nk)) return -1;
+        n += nk * (k == 0 ? 1.0 - dx : dx);
+    }
+    if (!isfinite(n)) return -1;
+    double c = ceil(n);
+    return c >= 2147483647.0 ? 2147483647 : (int)c;
+}
+
+static __device__ __noinline__ int lp_classical_sample_n(const DbGeom& g, const DbWork& w, double a, double eta,
+                                                         Draws& rng, double* s_out, double* theta_out, d3* sv_out,
+                                                         uint32_t* rej) {
+    int n = g.n;
+    ThetaBound tb;
+    theta_bound_low_eta(n, a, &tb);
+    double smax = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double mx = lp_cl_ceiling(a, g, w);
+    double v = 0.0, s = 0.0, theta = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next();
+        double ss = vv * smax;
+        double th = (PI / 2.0) * rng.next();
+        if (th > tb.at(vv)) continue;
+        double z = mx * rng.next();
+        if (z < lp_cl_ddpr(a, vv, th, g, w)) {
+            v = vv, s = ss, theta = th;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;
+    int quadrant = (int)(4.0 * rng.next());
+    if (quadrant == 1)
+        theta = PI - theta;
+    else if (quadrant == 2)
+        theta = PI + theta;
+    else if (quadrant == 3)
+        theta = 2.0 * PI - theta;
+    double x = 2.0 * n * a * cos(theta) * sqrt(v * (1.0 - v) / (1.0 + 0.5 * a * a));
+    double y = 0.25 * n * a * a * v / (1.0 + 0.5 * a * a);
+    double j[5];
+    if (!db_evaluate(g, w, x, y, j)) return 9;
+    double A0, A1, A2;
+    if (n % 2 == 0) {
+        A0 = j[2], A1 = -0.5 * (j[1] + j[3]), A2 = 0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    } else {
+        A0 = -j[2], A1 = 0.5 * (j[1] + j[3]), A2 = -0.25 * (j[0] + 2.0 * j[2] + j[4]);
+    }
+    double u = sqrt((1.0 + 0.5 * a * a) * (1.0 - v) / v);
+    double st = sin(theta);
+    double xi0 = 2.0 * (A1 * A1 - A0 * A2) - 2.0 * (A0 / a) * (A0 / a);
+    double xi1 = 2.0 * (A1 * A1 - A0 * A2) - 2.0 * (1.0 + 2.0 * u * u * st * st) * (A0 / a) * (A0 / a);
+    double xi2 = 2.0 * (u * A0 / a) * (u * A0 / a) * sin(2.0 * theta) + 4.0 * u * A0 * A1 * st / a;
+    *sv_out = mk3(xi1 / xi0, xi2 / xi0, 0.0);
+    *s_out = s;
+    *theta_out = theta;
+    return 0;
+}
+
+// nonlinear_compton/lp/classical.rs:257-330.  Returns a ptg status.
+static __device__ __noinline__ int lp_classical_sample(const NlcTables& t, const DbWork& w, double a, double eta,
+                                                       Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                                       d3* sv_out, uint32_t* rej) {
+    if (t.lp_cl_cdf == nullptr || w.base == nullptr) return 8;
+    int n = lp_cl_harmonic_index(t, a, rng.next());
+    if (n < 1) return 2;
+    DbWork wk;
+    DbGeom g;
+    int slot = -1;
+    int st = db_take(w, n, &wk, &g, &slot);
+    if (st != 0) return st;
+    *n_out = n;
+    st = lp_classical_sample_n(g, wk, a, eta, rng, s_out, theta_out, sv_out, rej);
+    if (slot >= 0) db_pool_release(w.pool, slot);
+    return st;
 }
 
 // Orders a DoubleBessel workspace must hold for harmonics up to n.

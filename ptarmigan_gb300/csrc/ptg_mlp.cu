@@ -1,0 +1,536 @@
+// Training and batched inference of the learned CP proposal (ptg_mlp.cuh)
+// on the tensor cores: BF16 operands, FP32 accumulation, warp-level
+// mma.sync m16n8k16.  A warp carries 16 rows through the network; the
+// accumulator fragments of one layer are, two n-tiles at a time, exactly
+// the A fragments of the next layer, so activations never leave registers
+// in the forward pass.  Weight gradients (dW = dZ^T H) take their
+// transposed operands from shared memory.
+//
+// Also here: the training-data generator (table sampler draws of a, eta,
+// n, one exact spectrum value per sample) and the sampler benchmark
+// (plain reference sampler vs learned proposal, same a, eta, n).
+#include <cuda_bf16.h>
+
+#include "ptg_launch.h"
+#include "ptg_lma.cuh"
+#include "ptg_mlp.cuh"
+
+namespace ptg {
+
+// One training sample: normalised inputs, the bin of v, ln f(v) - ln f(v*).
+struct MlpSample {
+    float x0, x1, x2;
+    int bin;
+    float t;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float d[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// B fragment (k = 2t..2t+1 and 2t+8..2t+9, n = g) of a K x N operand whose
+// element (k, n) is W[n * ld + k] (row-major [N][K], consecutive k).
+__device__ __forceinline__ void load_b(const __nv_bfloat16* W, int ld, int kb, int nb, uint32_t b[2]) {
+    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16* p = W + (size_t)(nb + g) * ld + kb + 2 * t;
+    b[0] = *reinterpret_cast<const uint32_t*>(p);
+    b[1] = *reinterpret_cast<const uint32_t*>(p + 8);
+}
+
+// Dense layer on a warp's 16 rows: z[ntile][4] = A . W^T + bias, A given as
+// ktiles x 4 fragments.
+template <int KT, int NT>
+__device__ __forceinline__ void dense(const uint32_t a[KT][4], const __nv_bfloat16* W, int ld, const float* bias,
+                                      float z[NT][4]) {
+    int lane = threadIdx.x & 31, t = lane & 3;
+    for (int nt = 0; nt < NT; ++nt) {
+        float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
+        z[nt][0] = b0, z[nt][1] = b1, z[nt][2] = b0, z[nt][3] = b1;
+        for (int kt = 0; kt < KT; ++kt) {
+            uint32_t b[2];
+            load_b(W, ld, kt * 16, nt * 8, b);
+            mma_bf16(z[nt], a[kt], b);
+        }
+    }
+}
+
+// Accumulator tiles (pairs of n-tiles) as the next layer's A fragments.
+template <int NT>
+__device__ __forceinline__ void to_a(const float h[NT][4], uint32_t a[NT / 2][4]) {
+    for (int k = 0; k < NT / 2; ++k) {
+        a[k][0] = pack_bf16(h[2 * k][0], h[2 * k][1]);
+        a[k][1] = pack_bf16(h[2 * k][2], h[2 * k][3]);
+        a[k][2] = pack_bf16(h[2 * k + 1][0], h[2 * k + 1][1]);
+        a[k][3] = pack_bf16(h[2 * k + 1][2], h[2 * k + 1][3]);
+    }
+}
+
+__device__ __forceinline__ void input_a(const float x[2][3], uint32_t a[1][4]) {
+    // 16 x 16 input tile, columns 0..2 used: rows g (x[0]) and g + 8 (x[1])
+    int t = threadIdx.x & 3;
+    float c0 = t == 0 ? x[0][0] : (t == 1 ? x[0][2] : 0.0f);
+    float c1 = t == 0 ? x[0][1] : 0.0f;
+    float d0 = t == 0 ? x[1][0] : (t == 1 ? x[1][2] : 0.0f);
+    float d1 = t == 0 ? x[1][1] : 0.0f;
+    a[0][0] = pack_bf16(c0, c1);
+    a[0][1] = pack_bf16(d0, d1);
+    a[0][2] = 0u;
+    a[0][3] = 0u;
+}
+
+template <int NT>
+__device__ __forceinline__ void silu_tiles(const float z[NT][4], float h[NT][4]) {
+    for (int n = 0; n < NT; ++n)
+        for (int q = 0; q < 4; ++q) h[n][q] = silu(z[n][q]);
+}
+
+__device__ __forceinline__ float dsilu(float z) {
+    float s = 1.0f / (1.0f + __expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+// Forward pass of a warp's 16 rows; keeps the pre-activations for backward.
+struct WarpFwd {
+    float z0[8][4], z1[8][4], z2[8][4], o[2][4];
+};
+
+__device__ __forceinline__ void warp_forward(const MlpDev& m, const float x[2][3], WarpFwd& f) {
+    uint32_t a0[1][4], a1[4][4];
+    input_a(x, a0);
+    dense<1, 8>(a0, m.w0, MLP_IN_PAD, m.p + P_B0, f.z0);
+    float h[8][4];
+    silu_tiles<8>(f.z0, h);
+    to_a<8>(h, a1);
+    dense<4, 8>(a1, m.w1, MLP_H, m.p + P_B1, f.z1);
+    silu_tiles<8>(f.z1, h);
+    to_a<8>(h, a1);
+    dense<4, 8>(a1, m.w2, MLP_H, m.p + P_B2, f.z2);
+    silu_tiles<8>(f.z2, h);
+    to_a<8>(h, a1);
+    dense<4, 2>(a1, m.w3, MLP_H, m.p + P_B3, f.o);
+}
+
+// Batched inference: out[row][16].
+__global__ void __launch_bounds__(128) k_mlp_infer(MlpDev m, const float* x_in /* [n][3] */, unsigned long long n,
+                                                   float* out) {
+    unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    unsigned long long r0 = warp * 16;
+    if (r0 >= n) return;
+    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float x[2][3];
+    for (int h = 0; h < 2; ++h) {
+        unsigned long long r = r0 + g + 8 * h;
+        for (int i = 0; i < 3; ++i) x[h][i] = r < n ? x_in[3 * r + i] : 0.0f;
+    }
+    WarpFwd f;
+    warp_forward(m, x, f);
+    for (int nt = 0; nt < 2; ++nt)
+        for (int h = 0; h < 2; ++h) {
+            unsigned long long r = r0 + g + 8 * h;
+            if (r < n) {
+                out[r * 16 + nt * 8 + 2 * t] = f.o[nt][2 * h];
+                out[r * 16 + nt * 8 + 2 * t + 1] = f.o[nt][2 * h + 1];
+            }
+        }
+}
+
+// Shared-memory staging for the weight gradients of one warp.
+struct WarpStage {
+    __nv_bfloat16 d[16][72];  // dZ (or dO) rows x out, padded
+    __nv_bfloat16 h[16][72];  // the layer's input rows x in, padded
+};
+
+// dW[out][in] += sum over the warp's 16 rows of d[row][out] * h[row][in],
+// M = out (mt tiles of 16), N = in (nt tiles of 8), K = 16 rows; added
+// into the block's shared accumulator.
+__device__ __forceinline__ void grad_w(const WarpStage& s, int m_tiles, int n_tiles, float* acc, int ld) {
+    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int mt = 0; mt < m_tiles; ++mt) {
+        uint32_t a[4];
+        // A[m = out][k = row] = d[row][out]
+        auto A = [&](int m, int k) { return s.d[k][mt * 16 + m]; };
+        __nv_bfloat162 p;
+        p.x = A(g, 2 * t), p.y = A(g, 2 * t + 1);
+        a[0] = *reinterpret_cast<uint32_t*>(&p);
+        p.x = A(g + 8, 2 * t), p.y = A(g + 8, 2 * t + 1);
+        a[1] = *reinterpret_cast<uint32_t*>(&p);
+        p.x = A(g, 2 * t + 8), p.y = A(g, 2 * t + 9);
+        a[2] = *reinterpret_cast<uint32_t*>(&p);
+        p.x = A(g + 8, 2 * t + 8), p.y = A(g + 8, 2 * t + 9);
+        a[3] = *reinterpret_cast<uint32_t*>(&p);
+        for (int nt = 0; nt < n_tiles; ++nt) {
+            uint32_t b[2];
+            // B[k = row][n = in] = h[row][in]
+            p.x = s.h[2 * t][nt * 8 + g], p.y = s.h[2 * t + 1][nt * 8 + g];
+            b[0] = *reinterpret_cast<uint32_t*>(&p);
+            p.x = s.h[2 * t + 8][nt * 8 + g], p.y = s.h[2 * t + 9][nt * 8 + g];
+            b[1] = *reinterpret_cast<uint32_t*>(&p);
+            float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            mma_bf16(c, a, b);
+            int row = mt * 16 + g, col = nt * 8 + 2 * t;
+            atomicAdd(&acc[row * ld + col], c[0]);
+            atomicAdd(&acc[row * ld + col + 1], c[1]);
+            atomicAdd(&acc[(row + 8) * ld + col], c[2]);
+            atomicAdd(&acc[(row + 8) * ld + col + 1], c[3]);
+        }
+    }
+}
+
+// Accumulator-layout tiles (rows g, g + 8) into the stage's row matrix.
+template <int NT>
+__device__ __forceinline__ void stage_rows(const float v[NT][4], __nv_bfloat16 (*dst)[72]) {
+    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int nt = 0; nt < NT; ++nt) {
+        dst[g][nt * 8 + 2 * t] = __float2bfloat16(v[nt][0]);
+        dst[g][nt * 8 + 2 * t + 1] = __float2bfloat16(v[nt][1]);
+        dst[g + 8][nt * 8 + 2 * t] = __float2bfloat16(v[nt][2]);
+        dst[g + 8][nt * 8 + 2 * t + 1] = __float2bfloat16(v[nt][3]);
+    }
+}
+
+// Bias gradient: column sums of accumulator tiles over the warp's rows.
+template <int NT>
+__device__ __forceinline__ void grad_b(const float d[NT][4], float* acc) {
+    int lane = threadIdx.x & 31, t = lane & 3;
+    for (int nt = 0; nt < NT; ++nt)
+        for (int q = 0; q < 2; ++q) {
+            float v = d[nt][q] + d[nt][q + 2];
+            for (int off = 4; off < 32; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane < 4) atomicAdd(&acc[nt * 8 + 2 * t + q], v);
+        }
+}
+
+// One optimisation step's gradients over `rows` samples starting at `first`
+// (pinball loss at quantile tau on ln f - ln f(v*), averaged): each block
+// covers a contiguous share and writes its partial gradient to
+// partial[block][P_TOTAL]; loss_out[block] gets its loss sum.
+__global__ void __launch_bounds__(128) k_mlp_grad(MlpDev m, const MlpSample* data, unsigned long long first,
+                                                  int rows, float tau, float* partial, float* loss_out) {
+    extern __shared__ float smem[];  // P_TOTAL gradient accumulators, then 4 warp stages
+    float* acc = smem;
+    WarpStage* stage = reinterpret_cast<WarpStage*>(smem + ((P_TOTAL + 3) / 4) * 4);
+    __shared__ float loss_s;
+    for (int i = threadIdx.x; i < P_TOTAL; i += blockDim.x) acc[i] = 0.0f;
+    if (threadIdx.x == 0) loss_s = 0.0f;
+    __syncthreads();
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    int per_block = (rows + gridDim.x - 1) / gridDim.x;
+    per_block = (per_block + 63) / 64 * 64;
+    int b0r = blockIdx.x * per_block;
+    int b1r = min(rows, b0r + per_block);
+    WarpStage& s = stage[warp];
+    float inv_rows = 1.0f / (float)rows;
+    float loss = 0.0f;
+    for (int r0 = b0r + warp * 16; r0 < b1r; r0 += 64) {
+        float x[2][3];
+        int bin[2];
+        float tgt[2];
+        bool ok[2];
+        for (int h = 0; h < 2; ++h) {
+            int r = r0 + g + 8 * h;
+            ok[h] = r < b1r;
+            MlpSample smp = ok[h] ? data[first + r] : MlpSample{0.0f, 0.0f, 0.0f, -1, 0.0f};
+            x[h][0] = smp.x0, x[h][1] = smp.x1, x[h][2] = smp.x2;
+            bin[h] = smp.bin;
+            tgt[h] = smp.t;
+            if (smp.bin < 0 || !(smp.t == smp.t)) ok[h] = false;
+        }
+        WarpFwd f;
+        warp_forward(m, x, f);
+        // pinball loss on the sampled bin only
+        float d_o[2][4];
+        for (int nt = 0; nt < 2; ++nt)
+            for (int q = 0; q < 4; ++q) {
+                int h = q >> 1, col = nt * 8 + 2 * t + (q & 1);
+                float d = 0.0f;
+                if (ok[h] && col == bin[h]) {
+                    float res = tgt[h] - f.o[nt][q];
+                    loss += res > 0.0f ? tau * res : (tau - 1.0f) * res;
+                    d = (res > 0.0f ? -tau : 1.0f - tau) * inv_rows;
+                }
+                d_o[nt][q] = d;
+            }
+        // layer 3: dW3 = dO^T h2, db3, dH2 = dO W3
+        float h2[8][4];
+        silu_tiles<8>(f.z2, h2);
+        __syncwarp();
+        stage_rows<2>(d_o, s.d);
+        stage_rows<8>(h2, s.h);
+        __syncwarp();
+        grad_w(s, 1, 8, acc + P_W3, MLP_H);
+        grad_b<2>(d_o, acc + P_B3);
+        uint32_t ad[4][4];
+        {
+            uint32_t a_o[1][4];
+            to_a<2>(d_o, a_o);
+            float dh[8][4];
+            for (int nt = 0; nt < 8; ++nt) {
+                dh[nt][0] = dh[nt][1] = dh[nt][2] = dh[nt][3] = 0.0f;
+                uint32_t b[2];
+                load_b(m.t3, MLP_OUT, 0, nt * 8, b);
+                mma_bf16(dh[nt], a_o[0], b);
+                for (int q = 0; q < 4; ++q) dh[nt][q] *= dsilu(f.z2[nt][q]);
+            }
+            // dZ2 in dh: layer 2 gradients, then dH1 = dZ2 W2
+            float h1[8][4];
+            silu_tiles<8>(f.z1, h1);
+            __syncwarp();
+            stage_rows<8>(dh, s.d);
+            stage_rows<8>(h1, s.h);
+            __syncwarp();
+            grad_w(s, 4, 8, acc + P_W2, MLP_H);
+            grad_b<8>(dh, acc + P_B2);
+            to_a<8>(dh, ad);
+        }
+        {
+            float dh[8][4];
+            for (int nt = 0; nt < 8; ++nt) {
+                dh[nt][0] = dh[nt][1] = dh[nt][2] = dh[nt][3] = 0.0f;
+                for (int kt = 0; kt < 4; ++kt) {
+                    uint32_t b[2];
+                    load_b(m.t2, MLP_H, kt * 16, nt * 8, b);
+                    mma_bf16(dh[nt], ad[kt], b);
+                }
+                for (int q = 0; q < 4; ++q) dh[nt][q] *= dsilu(f.z1[nt][q]);
+            }
+            float h0[8][4];
+            silu_tiles<8>(f.z0, h0);
+            __syncwarp();
+            stage_rows<8>(dh, s.d);
+            stage_rows<8>(h0, s.h);
+            __syncwarp();
+            grad_w(s, 4, 8, acc + P_W1, MLP_H);
+            grad_b<8>(dh, acc + P_B1);
+            to_a<8>(dh, ad);
+        }
+        {
+            float dh[8][4];
+            for (int nt = 0; nt < 8; ++nt) {
+                dh[nt][0] = dh[nt][1] = dh[nt][2] = dh[nt][3] = 0.0f;
+                for (int kt = 0; kt < 4; ++kt) {
+                    uint32_t b[2];
+                    load_b(m.t1, MLP_H, kt * 16, nt * 8, b);
+                    mma_bf16(dh[nt], ad[kt], b);
+                }
+                for (int q = 0; q < 4; ++q) dh[nt][q] *= dsilu(f.z0[nt][q]);
+            }
+            // layer 0: input x padded to 16 columns
+            float xin[2][4];
+            for (int h = 0; h < 2; ++h) xin[h][0] = xin[h][1] = xin[h][2] = xin[h][3] = 0.0f;
+            __syncwarp();
+            stage_rows<8>(dh, s.d);
+            for (int h = 0; h < 2; ++h)
+                for (int c = 0; c < 16; c += 4) {
+                    // lanes write the 16 x 16 input tile of their rows
+                    int col = c + t;
+                    s.h[g + 8 * h][col] = __float2bfloat16(col < 3 ? x[h][col] : 0.0f);
+                }
+            __syncwarp();
+            grad_w(s, 4, 2, acc + P_W0, MLP_IN_PAD);
+            grad_b<8>(dh, acc + P_B0);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (lane == 0) atomicAdd(&loss_s, loss);
+    __syncthreads();
+    float* out = partial + (size_t)blockIdx.x * P_TOTAL;
+    for (int i = threadIdx.x; i < P_TOTAL; i += blockDim.x) out[i] = acc[i];
+    if (threadIdx.x == 0) loss_out[blockIdx.x] = loss_s;
+}
+
+// Sum of the blocks' partial gradients, Adam step on the FP32 master, and
+// the BF16 copies (row-major and transposed) the other kernels read.
+__global__ void k_mlp_adam(float* p, float* mom, float* vel, const float* partial, int nblocks, float lr, float b1,
+                           float b2, float eps, int step, MlpDev m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P_TOTAL) return;
+    // padding columns of layer 0 stay zero
+    if (i < P_W1 && (i % MLP_IN_PAD) >= MLP_IN) return;
+    float g = 0.0f;
+    for (int b = 0; b < nblocks; ++b) g += partial[(size_t)b * P_TOTAL + i];
+    float mo = b1 * mom[i] + (1.0f - b1) * g;
+    float ve = b2 * vel[i] + (1.0f - b2) * g * g;
+    mom[i] = mo;
+    vel[i] = ve;
+    float mh = mo / (1.0f - powf(b1, (float)step)), vh = ve / (1.0f - powf(b2, (float)step));
+    float w = p[i] - lr * mh / (sqrtf(vh) + eps);
+    p[i] = w;
+    __nv_bfloat16 wb = __float2bfloat16(w);
+    if (i < P_W1) {
+        m.w0[i] = wb;
+    } else if (i < P_W2) {
+        int k = i - P_W1, o = k / MLP_H, c = k % MLP_H;
+        m.w1[k] = wb;
+        m.t1[c * MLP_H + o] = wb;
+    } else if (i < P_W3) {
+        int k = i - P_W2, o = k / MLP_H, c = k % MLP_H;
+        m.w2[k] = wb;
+        m.t2[c * MLP_H + o] = wb;
+    } else if (i < P_B0) {
+        int k = i - P_W3, o = k / MLP_H, c = k % MLP_H;
+        m.w3[k] = wb;
+        m.t3[c * MLP_OUT + o] = wb;
+    }
+}
+
+// BF16 copies from the FP32 master (after initialisation or a load).
+__global__ void k_mlp_sync(const float* p, MlpDev m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P_B0) return;
+    __nv_bfloat16 wb = __float2bfloat16(p[i]);
+    if (i < P_W1) {
+        m.w0[i] = wb;
+    } else if (i < P_W2) {
+        int k = i - P_W1, o = k / MLP_H, c = k % MLP_H;
+        m.w1[k] = wb;
+        m.t1[c * MLP_H + o] = wb;
+    } else if (i < P_W3) {
+        int k = i - P_W2, o = k / MLP_H, c = k % MLP_H;
+        m.w2[k] = wb;
+        m.t2[c * MLP_H + o] = wb;
+    } else {
+        int k = i - P_W3, o = k / MLP_H, c = k % MLP_H;
+        m.w3[k] = wb;
+        m.t3[c * MLP_OUT + o] = wb;
+    }
+}
+
+// Draws of the table sampler for training and benchmarking: (a, eta)
+// log-uniform over [a_lo, a_hi] x [eta_lo, eta_hi], n by the CP harmonic
+// CDF; one uniform v and the exact spectrum f(v) per sample.
+__device__ __forceinline__ void draw_point(Draws& rng, double a_lo, double a_hi, double e_lo, double e_hi, double* a,
+                                           double* eta) {
+    *a = exp(log(a_lo) + (log(a_hi) - log(a_lo)) * rng.next());
+    *eta = exp(log(e_lo) + (log(e_hi) - log(e_lo)) * rng.next());
+}
+
+__global__ void k_mlp_data(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo, double a_hi,
+                           double e_lo, double e_hi, MlpSample* out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Draws rng;
+    rng.begin(seed, mix64(i + 0x5851F42D4C957F2Dull), 0);
+    double a, eta;
+    draw_point(rng, a_lo, a_hi, e_lo, e_hi, &a, &eta);
+    NlcTables nt = nlc_view(*t);
+    int nh = cp_invert(nt, a, eta, rng.next());
+    if (nh < 1) nh = 1;
+    double sn = 2.0 * nh * eta / (1.0 + a * a);
+    double v_star = (1.0 + sn) / (2.0 + sn);
+    double base = log(cp_diff_partial_rate(nh, a, eta, v_star));
+    double v = rng.next();
+    double f = cp_diff_partial_rate(nh, a, eta, v);
+    MlpSample s;
+    float x[3];
+    mlp_features(a, eta, nh, x);
+    s.x0 = x[0], s.x1 = x[1], s.x2 = x[2];
+    s.bin = min((int)(v * MLP_OUT), MLP_OUT - 1);
+    double tv = log(f) - base;
+    s.t = (f > 0.0 && isfinite(tv) && isfinite(base)) ? (float)tv : __int_as_float(0x7fc00000);
+    out[i] = s;
+}
+
+// Sampler benchmark: the same (a, eta, n) per index for both methods; the
+// plain method runs the reference's ceiling and rejection, the learned one
+// takes the envelope from `env` (batched inference, [n][16]).  Writes v and
+// per-sample counters (spectrum evaluations, fallbacks).
+__global__ void k_sampler_bench(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                                double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
+                                float* x_out, double* v_out, unsigned* evals_out, unsigned* fallback_out,
+                                int* status_out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Draws pt;
+    pt.begin(seed, mix64(i + 0x2545F4914F6CDD1Dull), 0);
+    double a, eta;
+    draw_point(pt, a_lo, a_hi, e_lo, e_hi, &a, &eta);
+    NlcTables nt = nlc_view(*t);
+    int nh = cp_invert(nt, a, eta, pt.next());
+    if (nh < 1) nh = 1;
+    if (x_out) {
+        float x[3];
+        mlp_features(a, eta, nh, x);
+        x_out[3 * i] = x[0], x_out[3 * i + 1] = x[1], x_out[3 * i + 2] = x[2];
+    }
+    if (!v_out) return;  // features only
+    Draws rng;
+    rng.begin(seed ^ 0x9E3779B97F4A7C15ull, mix64(i), learned ? 2 : 1);
+    double v = -1.0;
+    uint32_t rej = 0;
+    int st;
+    unsigned evals;
+    unsigned fb = 0;
+    if (learned) {
+        LearnedCounts c{0, 0, 0};
+        st = cp_sample_v_learned(env + 16 * i, margin, nh, a, eta, rng, &v, &rej, &c);
+        evals = c.evals + (c.fallbacks ? 32u + rej + 1u : 0u);
+        fb = c.fallbacks;
+    } else {
+        st = cp_sample_v(nh, a, eta, rng, &v, &rej);
+        evals = 32u + rej + 1u;
+    }
+    v_out[i] = v;
+    evals_out[i] = evals;
+    fallback_out[i] = fb;
+    status_out[i] = st;
+}
+
+// ------------------------------------------------------------ launchers --
+cudaError_t launch_mlp_infer(const MlpDev& m, const float* x, unsigned long long n, float* out, cudaStream_t s) {
+    unsigned long long warps = (n + 15) / 16;
+    k_mlp_infer<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(m, x, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(const MlpDev& m, const void* data, unsigned long long first, int rows, float tau,
+                            float* partial, float* loss, int blocks, cudaStream_t s) {
+    size_t smem = sizeof(float) * ((P_TOTAL + 3) / 4) * 4 + 4 * sizeof(WarpStage);
+    static bool configured = false;  // one device per process uses this path
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    k_mlp_grad<<<blocks, 128, smem, s>>>(m, (const MlpSample*)data, first, rows, tau, partial, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_adam(float* p, float* mom, float* vel, const float* partial, int nblocks, float lr, int step,
+                            const MlpDev& m, cudaStream_t s) {
+    k_mlp_adam<<<(P_TOTAL + 255) / 256, 256, 0, s>>>(p, mom, vel, partial, nblocks, lr, 0.9f, 0.999f, 1e-8f, step, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_sync(const float* p, const MlpDev& m, cudaStream_t s) {
+    k_mlp_sync<<<(P_B0 + 255) / 256, 256, 0, s>>>(p, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_data(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                            double a_hi, double e_lo, double e_hi, void* out, cudaStream_t s) {
+    k_mlp_data<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, (MlpSample*)out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sampler_bench(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                                 double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
+                                 float* x_out, double* v_out, unsigned* evals, unsigned* fallbacks, int* status,
+                                 cudaStream_t s) {
+    k_sampler_bench<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, learned, env,
+                                                                margin, x_out, v_out, evals, fallbacks, status);
+    return cudaGetLastError();
+}
+
+int mlp_param_count() { return P_TOTAL; }
+size_t mlp_sample_bytes() { return sizeof(MlpSample); }
+
+}  // namespace ptg

@@ -171,6 +171,8 @@ struct NlcTables {
     const double* cp_cdf;    // [4270][32][2]
     const double* cp_cl_rate;  // [61]
     const double* lp_cl_rate;  // [61]
+    const double* cp_cl_cdf;   // [61][32][2]
+    const double* lp_cl_cdf;   // [61][16][2]
 };
 
 // nonlinear_compton/cp/classical.rs:22-43
@@ -247,23 +249,26 @@ static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, doubl
 }
 
 // nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
-static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
-                                      double* theta_out, d3* sv_out, uint32_t* rej) {
-    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
-    int n = cp_invert(t, a, eta, rng.next());
-    if (n < 1) n = 1;
+// nonlinear_compton/cp/mod.rs:181-200: v = s / s_max by rejection under
+// the ceiling.  Returns a ptg status.
+static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draws& rng, double* v_out, uint32_t* rej) {
     double mx = cp_ceiling(n, a, eta);
-    double v = 0.0;
     int it;
     for (it = 0; it < REJECTION_CAP; ++it) {
         double vv = rng.next(), u = rng.next();
         if (u <= cp_diff_partial_rate(n, a, eta, vv) / mx) {
-            v = vv;
+            *v_out = vv;
             break;
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;  // PTG_ERR_REJECTION_CAP
+    return it == REJECTION_CAP ? 4 : 0;  // PTG_ERR_REJECTION_CAP
+}
+
+// nonlinear_compton/cp/mod.rs:200-234: s, the azimuth and the Stokes
+// parameters once v is sampled.
+static __device__ __noinline__ void cp_finish(int n, double a, double eta, double v, Draws& rng, double* s_out,
+                                              double* theta_out, d3* sv_out) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     double s = v * (sn / (1.0 + sn));
     double theta = 2.0 * PI * rng.next();
@@ -281,9 +286,21 @@ static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, doubl
     double s2, c2;
     sincos(2.0 * (FRAC_PI_2 + theta), &s2, &c2);
     *sv_out = mk3(c2 * q + s2 * u, -s2 * q + c2 * u, vv);
-    *n_out = n;
     *s_out = s;
     *theta_out = theta;
+}
+
+// nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
+static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
+                                      double* theta_out, d3* sv_out, uint32_t* rej) {
+    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    double v = 0.0;
+    int st = cp_sample_v(n, a, eta, rng, &v, rej);
+    if (st != 0) return st;
+    cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    *n_out = n;
     return 0;
 }
 
@@ -357,6 +374,86 @@ static __device__ __noinline__ int nlc_kinematics(d4 k, d4 q, double a, double e
     double s_new = dot4(k, kprime) / dot4(k, q);
     if (!(fabs(s - s_new) / s < 1.0e-2)) return 3;
     *k_out = kprime;
+    return 0;
+}
+
+
+// ---------------------------------------------- classical CP emission ----
+// nonlinear_compton/cp/mod.rs:78-86
+__device__ __forceinline__ double cp_spectrum_low_eta(int n, double a, double v) {
+    if (v < 0.0 || v >= 1.0) return 0.0;
+    double z = sqrt(4.0 * a * a * ((double)n * n) * v * (1.0 - v) / (1.0 + a * a));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    return n * (a * a * jm * jm - 2.0 * (1.0 + a * a) * j * j + a * a * jp * jp) / (1.0 + a * a);
+}
+
+// nonlinear_compton/cp/classical.rs:45-75
+static __device__ __noinline__ double cp_cl_ceiling(int n, double a) {
+    double n_switch = round(3.0 * (1.0 + 0.54 * pow(a, 2.75)));
+    double mx = NAN;
+    if (n == 1) {
+        mx = cp_spectrum_low_eta(n, a, 0.99);
+    } else if (a < 0.15 || n > (int)n_switch) {
+        mx = cp_spectrum_low_eta(n, a, 0.5);
+    } else {
+        double b = a < 0.5 ? 2.3 * a : 0.8 * exp(-(a - 0.5) / 3.5) + 0.35;
+        double v = 1.0 - 0.5 * pow(log((double)n), b) / pow(log(n_switch), b);
+        for (int i = -4; i < 4; ++i) {
+            double f = cp_spectrum_low_eta(n, a, fmin(v + 0.1 * (double)i / 4.0, 1.0));
+            mx = isnan(mx) ? f : (isnan(f) ? mx : fmax(mx, f));
+        }
+    }
+    return 1.1 * mx;
+}
+
+// nonlinear_compton/cp/classical.rs:87-130 (cdf_table [61][32][2])
+static __device__ __noinline__ int cp_cl_harmonic_index(const NlcTables& t, double a, double frac) {
+    if (log(a) <= PTG_NLC_CL_MIN) return 1;
+    int ix = (int)((log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
+    double dx = (log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
+    if (ix >= 60) return -1;
+    double n = cp_cdf_corner(t.cp_cl_cdf + (size_t)ix * 64, frac) * (1.0 - dx) +
+               cp_cdf_corner(t.cp_cl_cdf + (size_t)(ix + 1) * 64, frac) * dx;
+    if (!isfinite(n)) return -1;
+    double c = ceil(n);
+    return c >= 2147483647.0 ? 2147483647 : (int)c;
+}
+
+// nonlinear_compton/cp/classical.rs:132-175.  Returns a ptg status.
+static __device__ __noinline__ int cp_classical_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out,
+                                                       double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
+    if (t.cp_cl_cdf == nullptr) return 8;
+    int n = cp_cl_harmonic_index(t, a, rng.next());
+    if (n < 1) return 2;
+    double mx = cp_cl_ceiling(n, a);
+    double v = 0.0;
+    int it;
+    for (it = 0; it < REJECTION_CAP; ++it) {
+        double vv = rng.next(), u = rng.next();
+        if (u <= cp_spectrum_low_eta(n, a, vv) / mx) {
+            v = vv;
+            break;
+        }
+    }
+    *rej += it;
+    if (it == REJECTION_CAP) return 4;
+    double s = v * (2.0 * n * eta / (1.0 + a * a));
+    double theta = 2.0 * PI * rng.next();
+    double z = sqrt((double)(4 * n * n) * (a * a / (1.0 + a * a)) * v * (1.0 - v));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    double xi0 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) - (2.0 * j / a) * (2.0 * j / a);
+    double xi1 = 2.0 * (jm * jm + jp * jp - 2.0 * j * j) + 8.0 * j * j * (1.0 - ((double)n / z) * ((double)n / z) - 0.5 / (a * a));
+    double xi3 = 2.0 * (1.0 - 2.0 * v) * (jm * jm - jp * jp);
+    double q = xi1 / xi0, u2 = 0.0 / xi0, v3 = xi3 / xi0;
+    // rotate_by(pi/2 + theta)
+    double s2, c2;
+    sincos(2.0 * (PI / 2.0 + theta), &s2, &c2);
+    *sv_out = mk3(c2 * q + s2 * u2, -s2 * q + c2 * u2, v3);
+    *n_out = n;
+    *s_out = s;
+    *theta_out = theta;
     return 0;
 }
 

@@ -22,7 +22,7 @@ _EXPORTS = [
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_eval_fields", "ptg_push_steps",
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
-    "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune",
+    "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
 ]
 
 
@@ -95,6 +95,8 @@ def load(path=None):
     L.ptg_queue_autotune.restype = st
     L.ptg_queue_autotune.argtypes = [ctxp, C.c_size_t, C.POINTER(abi.Collision), C.POINTER(abi.CollideOptions),
                                      C.POINTER(abi.Particles), C.c_double, C.POINTER(abi.QueueCfg), DP]
+    L.ptg_fp64_peak.restype = st
+    L.ptg_fp64_peak.argtypes = [ctxp, DP]
     _lib = L
     return L
 
@@ -275,6 +277,12 @@ class Engine:
         self._check(self.L.ptg_queue_autotune(self._h, len(collisions), arr, C.byref(options), C.byref(view),
                                               sample_fraction, C.byref(best), C.byref(ms)))
         return best.as_dict(), ms.value
+
+    def fp64_peak(self):
+        """Measured FP64 FMA throughput, TFLOP/s."""
+        v = C.c_double()
+        self._check(self.L.ptg_fp64_peak(self._h, C.byref(v)))
+        return v.value
 
     # -- diagnostics -----------------------------------------------------
     def fields(self, laser, r):

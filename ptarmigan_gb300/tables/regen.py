@@ -6,7 +6,12 @@ the reference; this runs its generator on the GPU
 rates it computed (``nlc_cp_cdf_totals.ptgt``), which must reproduce the
 shipped total-rate table ``nlc_cp_rate.ptgt``.
 
-    python ptarmigan_gb300/tables/regen.py --out DIR
+``pair_creation/lp/tables/mid_range/cdf.rs`` (the LP Breit-Wheeler
+mid-range CDF) is absent as well: ``ptg_regen_bw_lp_mid_cdf`` runs its
+generator and writes ``bw_lp_mid_cdf.ptgt``; its totals must reproduce the
+shipped ``bw_lp_mid_total.ptgt``.
+
+    python ptarmigan_gb300/tables/regen.py --out DIR [--which cp,lpm]
 """
 
 import argparse
@@ -45,9 +50,38 @@ def regen_cp(out_dir):
     return rel
 
 
+def regen_lp_mid(out_dir):
+    build.build()
+    L = engine.load()
+    L.ptg_regen_bw_lp_mid_cdf.restype = C.c_int
+    L.ptg_regen_bw_lp_mid_cdf.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    eng = engine.Engine()
+    cdf = np.zeros(5652 * 48)
+    tot = np.zeros(5652 * 2)
+    st = L.ptg_regen_bw_lp_mid_cdf(eng._h, cdf.ctypes.data_as(C.POINTER(C.c_double)),
+                                    tot.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise RuntimeError(L.ptg_last_error().decode())
+    eng.close()
+    write_ptgt(os.path.join(out_dir, "bw_lp_mid_cdf.ptgt"), (5652, 16, 3), cdf.tolist())
+    _, shipped = read_ptgt(os.path.join(HERE, "data", "bw_lp_mid_total.ptgt"))
+    shipped = np.exp(np.array(shipped))
+    ok = shipped > 0.0
+    rel = np.abs(tot[ok] - shipped[ok]) / shipped[ok]
+    zero_ok = np.all(tot[~ok] == 0.0)
+    print("LP BW mid-range CDF regenerated: max |total - shipped| / shipped = %.3e (median %.3e), "
+          "zero totals reproduced: %s" % (rel.max(), np.median(rel), zero_ok))
+    return rel
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(HERE, "data"))
+    ap.add_argument("--which", default="cp,lpm")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
-    regen_cp(args.out)
+    which = args.which.split(",")
+    if "cp" in which:
+        regen_cp(args.out)
+    if "lpm" in which:
+        regen_lp_mid(args.out)

@@ -403,3 +403,40 @@ def test_lma_lp_focused_matches_oracle(eng, orc):
     assert ost["emissions"] > 20
     _compare_showers(gout, oout, tol=LMA_TOL)
     assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)
+
+
+def test_lma_lp_focused_pairs_match_oracle(eng, orc):
+    """Photon beam on a linearly polarised focused laser (LMA): LP
+    Breit-Wheeler rates (main and mid-range tables), Stokes update, harmonic
+    inversion (regenerated mid-range CDF) and the (s, theta) sampler."""
+    if not orc.has_lp_mid_cdf():
+        pytest.skip("LP Breit-Wheeler mid-range CDF missing")
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 3.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=3e-6,
+                           fwhm_duration=30e-15, pol_angle=0.2)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(120, g, sigma=0.001 * g, radius=1e-6, length=2e-6, rms_div=8e-6, laser=laser, seed=19,
+                      species=abi.PHOTON, stokes=(0.4, -0.3, 0.2))
+    opts = abi.collide_options(pol_resolved=1, rate_increase=300.0)
+    gout, gst = eng.collide(laser, opts, prim, seed=29)
+    oout, ost = orc.collide(laser, opts, prim, seed=29, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["pair_events"] >= 10
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["pair_events"] == pytest.approx(ost["pair_events"], rel=0.05, abs=2)
+
+
+@pytest.mark.parametrize("pol", [abi.CIRCULAR, abi.LINEAR])
+def test_lma_classical_matches_oracle(eng, orc, pol):
+    """Classical radiation mode under the LMA (nonlinear_compton/{cp,lp}/
+    classical.rs): table rates, harmonic CDFs, low-eta spectra and the
+    Landau-Lifshitz push."""
+    laser = abi.laser_desc(abi.PLANE_WAVE, 2.0, 0.8e-6, pol, abi.COS2, n_cycles=12.0)
+    g = beam.gamma_from_energy(5.0)
+    prim = beam.build(160, g, sigma=0.001 * g, radius=1e-6, length=4e-6, rms_div=0.0, laser=laser, seed=14)
+    opts = abi.collide_options(classical=1, rr=1, tracking_photons=0)
+    gout, gst = eng.collide(laser, opts, prim, seed=31)
+    oout, ost = orc.collide(laser, opts, prim, seed=31, threads=8)
+    assert ost["particle_errors"] == 0 and gst["particle_errors"] == 0
+    assert ost["emissions"] > 30
+    _compare_showers(gout, oout, tol=LMA_TOL)
+    assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)

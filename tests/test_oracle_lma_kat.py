@@ -249,3 +249,39 @@ def test_lp_pair_rates_respect_the_polarisation_order(orc):
     for a, eta in [(0.5, 0.3), (1.5, 0.2), (3.0, 0.1), (8.0, 0.05)]:
         par, perp = orc.lp_pair_rates(a, eta)
         assert perp > par > 0.0
+
+
+# nonlinear_compton/cp/classical.rs:14-20 and lp/classical.rs:180-186: the
+# classical rate tables hold the sums over harmonics of the integrated
+# low-eta spectra; at the table's nodes (ln a = MIN + ix STEP) the sums
+# reproduce them.
+@pytest.mark.parametrize("ix", [10, 30, 45])
+def test_cp_classical_rate_at_nodes(orc, ix):
+    a = math.exp(-3.912023005428 + ix * 0.1151292546497)
+    nmax = int(10.0 * (1.0 + a ** 3))
+    total = sum(orc.cp_cl_integrated(n, a) for n in range(1, nmax + 1))
+    assert abs(total / orc.nlc_classical_rate(a, 1.0, 1) - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("ix", [5, 10, 20])
+def test_lp_classical_rate_at_nodes(orc, ix):
+    a = math.exp(-3.912023005428 + ix * 0.1151292546497)
+    nmax = int(math.ceil(6.0 * (1.0 + a * a) + 2.0 * a ** 3))
+    total = sum(n * orc.lp_cl_partial_rate(n, a) for n in range(1, nmax + 1))
+    expect = orc.nlc_classical_rate(a, 1.0, 0) / (2.0 / (1.0 + 0.5 * a * a))
+    assert abs(total / expect - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("pol", [0, 1])
+def test_classical_samplers_run_and_stay_in_range(orc, pol):
+    """classical.rs samplers: harmonic >= 1, 0 <= s <= s_max, finite Stokes
+    parameters (the reference does not bound their degree of polarisation:
+    its assert on it is commented out)."""
+    for k, (a, eta) in enumerate([(0.3, 0.01), (1.0, 0.05), (3.0, 0.02), (7.0, 0.01)]):
+        for stream in range(20):
+            rc, out = orc.nlc_classical_sample(a, eta, pol, 5, 100 * k + stream, 3)
+            assert rc == 0
+            n, s = out[0], out[1]
+            smax = 2.0 * n * eta / ((1.0 + a * a) if pol == 1 else (1.0 + 0.5 * a * a))
+            assert n >= 1 and 0.0 <= s <= smax * (1.0 + 1e-12)
+            assert np.all(np.isfinite(out[3:7])) and out[3] == 1.0

@@ -52,3 +52,40 @@ def test_regenerated_cdf_nodes_match_oracle(orc, i, j):
         nn, ff = node[k]
         if nn == math.floor(nn) and nn <= n_max:
             assert abs(ff - rates[int(nn) - 1] / total) < 1e-9, (k, nn, ff)
+
+
+def _load_table(name):
+    import os
+    from ptarmigan_gb300.tables.extract import read_ptgt
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    shape, vals = read_ptgt(os.path.join(here, "ptarmigan_gb300", "tables", "data", name))
+    return np.array(vals).reshape(shape)
+
+
+def test_lp_mid_cdf_totals_reproduce_shipped_table():
+    """The regenerated LP Breit-Wheeler mid-range CDF (generated on the GPU
+    by ptg_regen_bw_lp_mid_cdf) ends at the shipped totals: most nodes to
+    1e-9; the rest within the adaptive quadrature's tolerance (1e-3), where
+    a last-bit difference of a device transcendental flipped a refinement."""
+    cdf = _load_table("bw_lp_mid_cdf.ptgt")
+    tot = np.exp(_load_table("bw_lp_mid_total.ptgt").reshape(-1, 2))
+    last = cdf[:, 15, 1:]
+    pos = tot > 0.0
+    rel = np.where(pos, np.abs(last - tot) / np.where(pos, tot, 1.0), 0.0).max(axis=1)
+    assert np.all(last[~pos] == 0.0)
+    assert np.all(rel < 1e-3)
+    assert np.mean(rel < 1e-9) > 0.9
+
+
+@pytest.mark.parametrize("i,j", [(0, 3), (37, 17), (80, 30), (120, 8), (156, 33)])
+def test_lp_mid_cdf_nodes_match_oracle(orc, i, j):
+    import math
+    from ptarmigan_gb300.tables import small_tables as st
+    cdf = _load_table("bw_lp_mid_cdf.ptgt")[i * 36 + j]
+    a = math.exp(st.scalar("BW_LPM_LN_MIN_A")) * 10.0 ** (j / 20.0)
+    eta = (1.0 + 0.5 * a * a) * math.exp(st.scalar("BW_LPM_LN_MAX_ETA_PRIME")) / (1.0 + i / 4.0)
+    ref = orc.lp_pair_by_summation(a, eta)
+    assert np.array_equal(cdf[:, 0], ref[:, 0])
+    pos = ref[:, 1:] > 0.0
+    rel = np.abs(cdf[:, 1:][pos] / ref[:, 1:][pos] - 1.0)
+    assert np.all(rel < 1e-3)
