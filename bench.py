@@ -29,7 +29,18 @@ Other workloads (--workload), each one JSON line of the same metric:
   cp_shower       electrons at 16.5 GeV, 0.1% spread, 5 x 5 x 24 um, 8 urad,
                   on a circularly polarised focused laser (LMA) a0 = 5, w0 =
                   3 um, 0.8 um, 30 fs; Stokes parameters tracked, pairs on,
-                  all generations (--n primaries, default 1e6).
+                  all generations (--n primaries, default 1e6).  `value` is
+                  the learned proposal inside the persistent queue kernel,
+                  `plain_value` the reference's sampler through the wave
+                  kernels, with the photon spectra of both compared by KS.
+  learned_sampler the CP photon-energy sampler alone: the network is trained
+                  on the GPU on 5e7 table-sampler draws (a log-uniform in
+                  [0.05, 20], eta log-uniform in [1e-3, 2]), then each step
+                  samples 1e7 emissions of the same (a, eta) distribution
+                  with the learned proposal (`value`, inputs and inference
+                  included) and with the reference's sampler
+                  (`plain_value`); acceptance rate and the KS distance
+                  between the two are reported.
 """
 
 import argparse
@@ -237,6 +248,63 @@ def cp_shower_workload(n, seed):
     return laser, opts, prim
 
 
+MLP_MARGIN = 0.25  # ln of the learned envelope's safety factor
+MLP_TRAIN = dict(n_samples=50_000_000, batch=16384, epochs=3, lr=2e-3, tau=0.98, seed=7)
+
+
+def ks_distance(a, b):
+    """Two-sample Kolmogorov-Smirnov statistic."""
+    a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
+    grid = np.concatenate([a, b])
+    return float(np.max(np.abs(np.searchsorted(a, grid, side="right") / len(a) -
+                               np.searchsorted(b, grid, side="right") / len(b))))
+
+
+def ks_critical(n, m, alpha=1e-3):
+    """Two-sample KS critical value at significance alpha."""
+    c = math.sqrt(-0.5 * math.log(alpha / 2.0))
+    return c * math.sqrt((n + m) / (n * m))
+
+
+def train_network(eng):
+    eng.mlp_init(3)
+    return eng.mlp_train(**MLP_TRAIN)
+
+
+def run_learned_sampler(args, eng, sampler, line):
+    n = args.n or 10_000_000
+    tr = train_network(eng)
+    for w in range(args.warmup):
+        eng.sampler_bench(min(n, 1_000_000), seed=500 + w, margin=MLP_MARGIN, want_v=False)
+    runs, ks = [], None
+    with sampler:
+        for k in range(args.steps):
+            v0, v1, st = eng.sampler_bench(n, seed=1000 + k, margin=MLP_MARGIN, want_v=(k == 0))
+            runs.append(st)
+            if k == 0:
+                ks = ks_distance(v0[v0 > 0], v1[v1 > 0])
+    learned_ms = float(np.mean([r["learned_ms"] + r["features_ms"] + r["infer_ms"] for r in runs]))
+    plain_ms = float(np.mean([r["plain_ms"] for r in runs]))
+    last = runs[-1]
+    line.update({
+        "metric": "CP photon emissions sampled/s: learned proposal vs table sampler at KS <= 1e-3",
+        "unit": "emissions/s", "value": n / (learned_ms / 1e3), "ms_per_step": learned_ms,
+        "plain_value": n / (plain_ms / 1e3), "plain_ms": plain_ms,
+        "dtype": "f64 spectrum and accept/reject; bf16 weights, f32 accumulation in the network",
+        "ks_vs_plain": ks, "ks_critical_1e-3": ks_critical(n, n),
+        "acceptance": last["acceptance"], "learned_evals_per_emission": last["learned_evals"],
+        "plain_evals_per_emission": last["plain_evals"],
+        "envelope_violations": last["fallbacks"], "trial_cap_handovers": last["exhausted"],
+        "errors": last["errors_plain"] + last["errors_learned"],
+        "ms_split": {"features": last["features_ms"], "inference": last["infer_ms"], "sampling": last["learned_ms"]},
+        "training": dict(tr, **{k: v for k, v in MLP_TRAIN.items()}),
+        "config": {"workload": "learned_sampler: CP NLC v-sampler, a log-uniform [0.05, 20], eta log-uniform "
+                               "[1e-3, 2], n from the CP harmonic table; %d emissions per step; network 6-64-64-64-16 "
+                               "SiLU trained on the GPU on 5e7 table-sampler draws" % n,
+                   "emissions_per_step": n, "margin": MLP_MARGIN},
+        "gpu_launches": 4 * args.steps})
+
+
 def run_extra(args):
     """The non-default workloads: device time with CUDA events on the
     engine's stream, inputs resident in HBM."""
@@ -260,7 +328,9 @@ def run_extra(args):
 
     line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic"}
-    if args.workload == "a0_scan":
+    if args.workload == "learned_sampler":
+        run_learned_sampler(args, eng, sampler, line)
+    elif args.workload == "a0_scan":
         colls, opts, prim = a0_scan_workload(1, scale=args.scale)
         n = int(sum(c["count"] for c in colls))
         d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
@@ -289,14 +359,9 @@ def run_extra(args):
                                                                           "emissions", "pair_events", "n_created",
                                                                           "n_out", "particle_errors")}},
                      "gpu_launches": 7 * args.steps})
-    else:
-        if args.workload == "plane_wave_lma":
-            laser, opts, prim = plane_wave_lma_workload(args.n or 10_000, 1)
-            desc = "plane_wave_lma: 1e4 e- 5 GeV 0.1%, LP PlaneWave (LMA) a0=1 cos2 30.9 cycles, emission only"
-        else:
-            laser, opts, prim = cp_shower_workload(args.n or 1_000_000, 1)
-            desc = ("cp_shower: e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 30 fs; "
-                    "Stokes tracked, pairs on, all generations")
+    elif args.workload == "plane_wave_lma":
+        laser, opts, prim = plane_wave_lma_workload(args.n or 10_000, 1)
+        desc = "plane_wave_lma: 1e4 e- 5 GeV 0.1%, LP PlaneWave (LMA) a0=1 cos2 30.9 cycles, emission only"
         n = len(prim["species"])
         d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
         for w in range(args.warmup):
@@ -307,21 +372,83 @@ def run_extra(args):
                 t, r = timed(lambda: eng.collide_device(laser, opts, d_prim, seed=1000 + k))
                 ms.append(t)
                 st = r[1]
-        # the same batch through the persistent queue (one collision)
-        coll = [{"laser": laser, "seed": 1000, "id_base": n, "first": 0, "count": n}]
-        eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
-        eng.collide_multi_device(coll, opts, d_prim)
-        tq, rq = timed(lambda: eng.collide_multi_device(coll, opts, d_prim))
         line.update({"value": n / (np.mean(ms) / 1e3), "ms_per_step": float(np.mean(ms)),
-                     "queue_value": n / (tq / 1e3),
                      "config": {"workload": desc, "n_primaries": n,
                                 "events_per_step": {k: st[k] for k in ("lepton_steps", "photon_steps", "emissions",
-                                                                       "pair_events", "n_created", "n_out", "waves",
-                                                                       "particle_errors")}},
-                     "gpu_launches": int(sum([2 + st["waves"]]) * args.steps)})
+                                                                       "n_out", "waves", "particle_errors")}},
+                     "gpu_launches": int((2 + st["waves"]) * args.steps)})
+    else:
+        run_cp_shower(args, eng, timed, sampler, line, dev)
     line["clocks"] = sampler.summary()
     print(json.dumps(line), flush=True)
     eng.close()
+
+
+def run_cp_shower(args, eng, timed, sampler, line, dev):
+    """The CP LMA shower: the learned proposal inside the persistent queue
+    kernel (value) against the reference's sampler through the wave kernels
+    (plain_value), same primaries and seeds; the photon spectra, Stokes
+    parameters and pair yields of the two are compared."""
+    import torch
+    from ptarmigan_gb300 import abi
+    laser, opts, prim = cp_shower_workload(args.n or 1_000_000, 1)
+    desc = ("cp_shower: e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 30 fs; "
+            "Stokes tracked, pairs on, all generations")
+    n = len(prim["species"])
+    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    tr = train_network(eng)
+
+    def plain(seed):
+        eng.mlp_use(False)
+        return eng.collide_device(laser, opts, d_prim, seed=seed)
+
+    def learned(seed):
+        eng.mlp_use(True, margin=MLP_MARGIN)
+        return eng.collide_multi_device([{"laser": laser, "seed": seed, "id_base": n, "first": 0, "count": n}],
+                                        opts, d_prim)
+
+    eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
+    for w in range(args.warmup):
+        plain(100 + w)
+        learned(100 + w)
+    ms_l, ms_p, st_l, st_p = [], [], None, None
+    with sampler:
+        for k in range(args.steps):
+            t, r = timed(lambda: learned(1000 + k))
+            ms_l.append(t)
+            st_l = r[3]
+            t, r = timed(lambda: plain(1000 + k))
+            ms_p.append(t)
+            st_p = r[1]
+    # statistics of one step of each, through the host entry points (same seeds)
+    eng.mlp_use(False)
+    out_p, _ = eng.collide(laser, opts, prim, seed=1000)
+    eng.mlp_use(True, margin=MLP_MARGIN)
+    parts, _, _ = eng.collide_multi([{"laser": laser, "seed": 1000, "id_base": n, "first": 0, "count": n}],
+                                    opts, prim)
+    out_l = parts[0]
+    eng.mlp_use(False)
+
+    def summary(out):
+        ph = out["species"] == abi.PHOTON
+        return {"photons": int(ph.sum()), "positrons": int((out["species"] == abi.POSITRON).sum()),
+                "stokes_mean": [float(x) for x in out["pol"][ph].mean(axis=0)],
+                "mean_electron_energy_mev": float(out["u"][out["species"] == abi.ELECTRON, 0].mean() * 0.51099895)}
+    e_p = out_p["u"][out_p["species"] == abi.PHOTON, 0]
+    e_l = out_l["u"][out_l["species"] == abi.PHOTON, 0]
+    keys = ("lepton_steps", "photon_steps", "emissions", "pair_events", "n_created", "n_out", "particle_errors")
+    line.update({"value": n / (np.mean(ms_l) / 1e3), "ms_per_step": float(np.mean(ms_l)),
+                 "plain_value": n / (np.mean(ms_p) / 1e3), "plain_ms": float(np.mean(ms_p)),
+                 "ks_photon_energy_vs_plain": ks_distance(e_p, e_l),
+                 "ks_critical_1e-3": ks_critical(len(e_p), len(e_l)),
+                 "learned": summary(out_l), "plain": summary(out_p),
+                 "training": dict(tr, **MLP_TRAIN),
+                 "config": {"workload": desc, "n_primaries": n, "margin": MLP_MARGIN,
+                            "value_path": "learned proposal + persistent queue kernel (CUDA graph)",
+                            "plain_path": "reference sampler + wave kernels",
+                            "events_per_step_learned": {k: st_l[k] for k in keys},
+                            "events_per_step_plain": {k: st_p[k] for k in keys}},
+                 "gpu_launches": int((7 + 2 + st_p["waves"]) * args.steps)})
 
 
 def nbytes(d):
@@ -338,7 +465,7 @@ def main():
     ap.add_argument("--cpu-sample-per-core", type=int, default=1500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="lcfa_shower", choices=["lcfa_shower", "plane_wave_lma", "a0_scan",
-                                                                    "cp_shower"])
+                                                                    "cp_shower", "learned_sampler"])
     ap.add_argument("--scale", type=float, default=1.0, help="a0_scan: beam-size scale")
     ap.add_argument("--tune-fraction", type=float, default=0.02, help="a0_scan: autotuner sample fraction")
     args = ap.parse_args()

@@ -324,8 +324,8 @@ ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const doub
                          const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
 
 /* --------------------------------------------------- learned proposal ---
- * No reference counterpart: an MLP (inputs ln a, ln eta, ln n; 4 layers of
- * width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the
+ * No reference counterpart: an MLP (six features of a, eta and n; 4 layers
+ * of width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the
  * tensor cores) proposes v = s / s_max for CP nonlinear Compton emission in
  * 16 bins, with an exact accept/reject against the spectrum
  * (nonlinear_compton/cp/mod.rs:17-40) and the reference's sampler as the
@@ -351,16 +351,31 @@ typedef struct {
 } ptg_sampler_bench_cfg;
 
 typedef struct {
-    double plain_ms, learned_ms, infer_ms;  /* device times (inference includes the features pass) */
+    double plain_ms, learned_ms;            /* device times of the two samplers */
+    double features_ms, infer_ms;           /* the learned path's inputs and batched inference */
     double plain_evals, learned_evals;      /* spectrum evaluations per emission */
-    uint64_t fallbacks, errors;
+    double acceptance;                      /* accepted / proposed under the learned envelope */
+    uint64_t fallbacks;                     /* envelope under the spectrum: the reference's sampler took over */
+    uint64_t exhausted;                     /* no acceptance within the learned trial cap: the envelope
+                                               capped at the reference's ceiling took over */
+    uint64_t errors_plain, errors_learned;  /* emissions that ended with a nonzero status */
 } ptg_sampler_bench_stats;
 
+/* Per-emission detail of the sampler benchmark (each array [n] or, for x
+ * and env, [n][6] and [n][16]; any may be NULL). */
+typedef struct {
+    float* x;                   /* the network's inputs, [n][6] */
+    float* env;                 /* its outputs */
+    int32_t *status_plain, *status_learned;
+    uint32_t *evals_plain, *evals_learned;
+    uint32_t* fallback;         /* 0; 1 = envelope violation; 2 = trial cap; 3 = both */
+} ptg_sampler_bench_detail;
+
 /* Random initialisation; parameter access ([count] floats, get and/or
- * set); the training loop; the loss gradient of a batch ([n][5] = x0, x1,
- * x2, bin, target) for checks; batched inference ([n][3] -> [n][16]); the
+ * set); the training loop; the loss gradient of a batch ([n][8] = the six
+ * inputs, bin, target) for checks; batched inference ([n][6] -> [n][16]); the
  * switch that makes the collision kernels use the network; and the sampler
- * benchmark (v_plain, v_learned: [n], may be NULL). */
+ * benchmark (v_plain, v_learned: [n], may be NULL; detail may be NULL). */
 ptg_status ptg_mlp_init(ptg_ctx* ctx, uint64_t seed);
 ptg_status ptg_mlp_params(ptg_ctx* ctx, float* get, const float* set, int32_t* count);
 ptg_status ptg_mlp_train(ptg_ctx* ctx, const ptg_mlp_train_cfg* cfg, ptg_mlp_train_stats* stats);
@@ -368,7 +383,7 @@ ptg_status ptg_mlp_grad(ptg_ctx* ctx, const float* samples, size_t n, float tau,
 ptg_status ptg_mlp_infer(ptg_ctx* ctx, const float* x, size_t n, float* out);
 ptg_status ptg_mlp_use(ptg_ctx* ctx, int32_t enabled, float margin);
 ptg_status ptg_sampler_bench(ptg_ctx* ctx, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
-                             ptg_sampler_bench_stats* stats);
+                             const ptg_sampler_bench_detail* detail, ptg_sampler_bench_stats* stats);
 
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */

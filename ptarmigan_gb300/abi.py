@@ -141,6 +141,83 @@ class QueueCfg(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class MlpTrainCfg(C.Structure):
+    _fields_ = [
+        ("n_samples", C.c_uint64),
+        ("batch", C.c_int32),
+        ("epochs", C.c_int32),
+        ("lr", C.c_float),
+        ("tau", C.c_float),
+        ("seed", C.c_uint64),
+        ("a_lo", C.c_double),
+        ("a_hi", C.c_double),
+        ("eta_lo", C.c_double),
+        ("eta_hi", C.c_double),
+    ]
+
+
+class MlpTrainStats(C.Structure):
+    _fields_ = [
+        ("loss_first", C.c_float),
+        ("loss_last", C.c_float),
+        ("steps", C.c_int32),
+        ("reserved", C.c_int32),
+        ("data_ms", C.c_double),
+        ("train_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
+class SamplerBenchCfg(C.Structure):
+    _fields_ = [
+        ("n", C.c_uint64),
+        ("seed", C.c_uint64),
+        ("a_lo", C.c_double),
+        ("a_hi", C.c_double),
+        ("eta_lo", C.c_double),
+        ("eta_hi", C.c_double),
+        ("margin", C.c_float),
+        ("reserved", C.c_float),
+    ]
+
+
+# Inputs of the learned proposal's network (features of a, eta, n).
+MLP_INPUTS = 6
+
+
+class SamplerBenchDetail(C.Structure):
+    _fields_ = [
+        ("x", C.POINTER(C.c_float)),
+        ("env", C.POINTER(C.c_float)),
+        ("status_plain", C.POINTER(C.c_int32)),
+        ("status_learned", C.POINTER(C.c_int32)),
+        ("evals_plain", C.POINTER(C.c_uint32)),
+        ("evals_learned", C.POINTER(C.c_uint32)),
+        ("fallback", C.POINTER(C.c_uint32)),
+    ]
+
+
+class SamplerBenchStats(C.Structure):
+    _fields_ = [
+        ("plain_ms", C.c_double),
+        ("learned_ms", C.c_double),
+        ("features_ms", C.c_double),
+        ("infer_ms", C.c_double),
+        ("plain_evals", C.c_double),
+        ("learned_evals", C.c_double),
+        ("acceptance", C.c_double),
+        ("fallbacks", C.c_uint64),
+        ("exhausted", C.c_uint64),
+        ("errors_plain", C.c_uint64),
+        ("errors_learned", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class DeviceCfg(C.Structure):
     _fields_ = [
         ("device", C.c_int32),

@@ -1994,12 +1994,17 @@ static MlpParams mlp_params(ptg_ctx* c) {
 static ptg_status mlp_alloc(ptg_ctx* c) {
     if (c->mlp_p) return PTG_OK;
     size_t np = P_TOTAL;
-    size_t nbf = (size_t)MLP_H * MLP_IN_PAD + 3 * (size_t)MLP_H * MLP_H + 2 * (size_t)MLP_OUT * MLP_H + 2 * 64;
+    // w0, w1, w2, w3 and the transposes t1, t2, t3 (mlp_dev's layout)
+    size_t nbf = (size_t)MLP_H * MLP_IN_PAD + 4 * (size_t)MLP_H * MLP_H + 2 * (size_t)MLP_OUT * MLP_H;
     if (cudaMalloc(&c->mlp_p, 4 * np) != cudaSuccess || cudaMalloc(&c->mlp_m, 4 * np) != cudaSuccess ||
         cudaMalloc(&c->mlp_v, 4 * np) != cudaSuccess ||
         cudaMalloc(&c->mlp_partial, 4 * np * MLP_GRAD_BLOCKS) != cudaSuccess ||
         cudaMalloc(&c->mlp_loss, 4 * MLP_GRAD_BLOCKS) != cudaSuccess || cudaMalloc(&c->mlp_bf, 2 * nbf) != cudaSuccess) {
         cudaGetLastError();
+        cudaFree(c->mlp_p), cudaFree(c->mlp_m), cudaFree(c->mlp_v), cudaFree(c->mlp_partial), cudaFree(c->mlp_loss);
+        cudaFree(c->mlp_bf);
+        c->mlp_p = c->mlp_m = c->mlp_v = c->mlp_partial = c->mlp_loss = nullptr;
+        c->mlp_bf = nullptr;
         return set_err(PTG_ERR_ALLOC, "learned-proposal buffers");
     }
     CUDA_TRY(cudaMemset(c->mlp_bf, 0, 2 * nbf));
@@ -2073,13 +2078,15 @@ ptg_status ptg_mlp_grad(ptg_ctx* c, const float* samples, size_t n, float tau, f
     if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: call ptg_mlp_init first");
     if (n == 0 || n > (1u << 24)) return set_err(PTG_ERR_INVALID_ARGUMENT, "sample count out of range");
     CUDA_TRY(cudaSetDevice(c->device));
-    std::vector<char> buf(mlp_sample_bytes() * n);
+    // rows of MLP_IN inputs, the bin (as a float) and the target
+    const size_t row = MLP_IN + 2, sb = mlp_sample_bytes();
+    std::vector<char> buf(sb * n);
     for (size_t i = 0; i < n; ++i) {
-        float v[5] = {samples[5 * i], samples[5 * i + 1], samples[5 * i + 2], 0.0f, samples[5 * i + 4]};
-        int bin = (int)samples[5 * i + 3];
-        std::memcpy(&buf[i * 20], v, 12);
-        std::memcpy(&buf[i * 20 + 12], &bin, 4);
-        std::memcpy(&buf[i * 20 + 16], &v[4], 4);
+        const float* r = samples + row * i;
+        int bin = (int)r[MLP_IN];
+        std::memcpy(&buf[i * sb], r, 4 * MLP_IN);
+        std::memcpy(&buf[i * sb + 4 * MLP_IN], &bin, 4);
+        std::memcpy(&buf[i * sb + 4 * MLP_IN + 4], &r[MLP_IN + 1], 4);
     }
     void* d = nullptr;
     CUDA_TRY(cudaMalloc(&d, buf.size()));
@@ -2112,12 +2119,12 @@ ptg_status ptg_mlp_infer(ptg_ctx* c, const float* x, size_t n, float* out) {
     if (n == 0) return PTG_OK;
     CUDA_TRY(cudaSetDevice(c->device));
     float *dx = nullptr, *dout = nullptr;
-    CUDA_TRY(cudaMalloc(&dx, 12 * n));
+    CUDA_TRY(cudaMalloc(&dx, 4 * MLP_IN * n));
     if (cudaMalloc(&dout, 64 * n) != cudaSuccess) {
         cudaFree(dx);
         return set_err(PTG_ERR_ALLOC, "inference buffers");
     }
-    cudaMemcpy(dx, x, 12 * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(dx, x, 4 * MLP_IN * n, cudaMemcpyHostToDevice);
     cudaError_t e = launch_mlp_infer(mlp_dev(c), dx, n, dout, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) cudaMemcpy(out, dout, 64 * n, cudaMemcpyDeviceToHost);
@@ -2202,10 +2209,11 @@ ptg_status ptg_mlp_use(ptg_ctx* c, int32_t enabled, float margin) {
 }
 
 ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
-                             ptg_sampler_bench_stats* stats) {
+                             const ptg_sampler_bench_detail* detail, ptg_sampler_bench_stats* stats) {
     if (!c || !cfg) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!c->mlp_ready) return set_err(PTG_ERR_INVALID_ARGUMENT, "no network: train or load one first");
     if (cfg->n == 0 || cfg->n > (1ull << 28)) return set_err(PTG_ERR_INVALID_ARGUMENT, "sample count out of range");
+    if (!(cfg->margin >= 0.0f && cfg->margin < 10.0f)) return set_err(PTG_ERR_INVALID_ARGUMENT, "margin out of range");
     CUDA_TRY(cudaSetDevice(c->device));
     if (!c->tables_loaded) {
         ptg_status st = ptg_load_tables(c, nullptr);
@@ -2215,50 +2223,63 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
     float *dx = nullptr, *denv = nullptr;
     double *dv0 = nullptr, *dv1 = nullptr;
     unsigned *de0 = nullptr, *de1 = nullptr, *df = nullptr;
-    int* dst = nullptr;
+    int *ds0 = nullptr, *ds1 = nullptr;
+    unsigned long long* ctr = nullptr;
     auto cleanup = [&]() {
         cudaFree(dx), cudaFree(denv), cudaFree(dv0), cudaFree(dv1), cudaFree(de0), cudaFree(de1), cudaFree(df);
-        cudaFree(dst);
+        cudaFree(ds0), cudaFree(ds1), cudaFree(ctr);
     };
-    bool ok = cudaMalloc(&dx, 12 * n) == cudaSuccess && cudaMalloc(&denv, 64 * n) == cudaSuccess &&
+    bool ok = cudaMalloc(&dx, 4 * MLP_IN * n) == cudaSuccess && cudaMalloc(&denv, 64 * n) == cudaSuccess &&
               cudaMalloc(&dv0, 8 * n) == cudaSuccess && cudaMalloc(&dv1, 8 * n) == cudaSuccess &&
               cudaMalloc(&de0, 4 * n) == cudaSuccess && cudaMalloc(&de1, 4 * n) == cudaSuccess &&
-              cudaMalloc(&df, 4 * n) == cudaSuccess && cudaMalloc(&dst, 4 * n) == cudaSuccess;
+              cudaMalloc(&df, 4 * n) == cudaSuccess && cudaMalloc(&ds0, 4 * n) == cudaSuccess &&
+              cudaMalloc(&ds1, 4 * n) == cudaSuccess && cudaMalloc(&ctr, 8) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         cleanup();
         return set_err(PTG_ERR_ALLOC, "sampler benchmark buffers");
     }
-    cudaEvent_t e[6];
+    cudaEvent_t e[5];
     for (auto& ev : e) cudaEventCreate(&ev);
     cudaStream_t s = c->stream;
     cudaError_t err = cudaSuccess;
     // plain: the reference's ceiling and rejection
     cudaEventRecord(e[0], s);
-    err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
-                               cfg->margin, nullptr, dv0, de0, df, dst, s);
+    err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
+                             cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
     cudaEventRecord(e[1], s);
     // learned: features, batched tensor-core inference, then sampling
     if (err == cudaSuccess)
-        err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1,
-                                   nullptr, cfg->margin, dx, nullptr, nullptr, nullptr, nullptr, s);
+        err = launch_sampler_features(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, dx, s);
     cudaEventRecord(e[2], s);
     if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), dx, n, denv, s);
     cudaEventRecord(e[3], s);
     if (err == cudaSuccess)
-        err = launch_sampler_bench(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1, denv,
-                                   cfg->margin, nullptr, dv1, de1, df, dst, s);
+        err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1, denv,
+                                 cfg->margin, ctr, dv1, de1, df, ds1, s);
     cudaEventRecord(e[4], s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     std::vector<unsigned> ev0(n), ev1(n), fb(n);
-    std::vector<int> status(n);
+    std::vector<int> st0(n), st1(n);
     if (err == cudaSuccess) {
         if (v_plain) cudaMemcpy(v_plain, dv0, 8 * n, cudaMemcpyDeviceToHost);
         if (v_learned) cudaMemcpy(v_learned, dv1, 8 * n, cudaMemcpyDeviceToHost);
         cudaMemcpy(ev0.data(), de0, 4 * n, cudaMemcpyDeviceToHost);
         cudaMemcpy(ev1.data(), de1, 4 * n, cudaMemcpyDeviceToHost);
         cudaMemcpy(fb.data(), df, 4 * n, cudaMemcpyDeviceToHost);
-        cudaMemcpy(status.data(), dst, 4 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(st0.data(), ds0, 4 * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(st1.data(), ds1, 4 * n, cudaMemcpyDeviceToHost);
+        if (detail) {
+            if (detail->x) cudaMemcpy(detail->x, dx, 4 * MLP_IN * n, cudaMemcpyDeviceToHost);
+            if (detail->env) cudaMemcpy(detail->env, denv, 64 * n, cudaMemcpyDeviceToHost);
+            if (detail->status_plain) std::memcpy(detail->status_plain, st0.data(), 4 * n);
+            if (detail->status_learned) std::memcpy(detail->status_learned, st1.data(), 4 * n);
+            if (detail->evals_plain) std::memcpy(detail->evals_plain, ev0.data(), 4 * n);
+            if (detail->evals_learned) std::memcpy(detail->evals_learned, ev1.data(), 4 * n);
+            if (detail->fallback)
+                for (unsigned long long q = 0; q < n; ++q) detail->fallback[q] = fb[q] & 3u;
+        }
+        err = cudaGetLastError();
     }
     float t_plain = 0, t_feat = 0, t_inf = 0, t_learn = 0;
     cudaEventElapsedTime(&t_plain, e[0], e[1]);
@@ -2269,20 +2290,29 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
     cleanup();
     if (err != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(err));
     if (stats) {
-        double s0 = 0, s1 = 0;
-        unsigned long long nf = 0, ne = 0;
+        double s0 = 0, s1 = 0, proposals = 0, accepted = 0;
+        unsigned long long nf = 0, nx = 0, ne0 = 0, ne1 = 0;
         for (unsigned long long i = 0; i < n; ++i) {
+            unsigned kind = fb[i] & 3u;
             s0 += ev0[i], s1 += ev1[i];
-            nf += fb[i] ? 1 : 0;
-            ne += status[i] != 0 ? 1 : 0;
+            nf += (kind == 1u || kind == 3u) ? 1 : 0;
+            nx += (kind == 2u || kind == 3u) ? 1 : 0;
+            ne0 += st0[i] != 0 ? 1 : 0;
+            ne1 += st1[i] != 0 ? 1 : 0;
+            proposals += (double)(fb[i] >> 2);
+            accepted += (st1[i] == 0 && (kind == 0u || kind == 2u)) ? 1.0 : 0.0;
         }
         stats->plain_ms = t_plain;
         stats->learned_ms = t_learn;
-        stats->infer_ms = t_inf + t_feat;
+        stats->infer_ms = t_inf;
+        stats->features_ms = t_feat;
+        stats->acceptance = proposals > 0 ? accepted / proposals : 0.0;
         stats->plain_evals = s0 / (double)n;
         stats->learned_evals = s1 / (double)n;
         stats->fallbacks = nf;
-        stats->errors = ne;
+        stats->exhausted = nx;
+        stats->errors_plain = ne0;
+        stats->errors_learned = ne1;
     }
     return PTG_OK;
 }

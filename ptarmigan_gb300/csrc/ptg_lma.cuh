@@ -88,7 +88,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
             float x[3], o[MLP_OUT];
             mlp_features(aq, eta, n, x);
             mlp_forward_lane(mlp, x, o);
-            LearnedCounts lc{0, 0, 0};
+            LearnedCounts lc{0, 0, 0, 0};
             double v = 0.0;
             st = cp_sample_v_learned(o, mlp.margin, n, aq, eta, rng, &v, rej, &lc);
             if (st == 0) cp_finish(n, aq, eta, v, rng, &s, &cphi, &sv);

@@ -11,15 +11,18 @@
 // (plain reference sampler vs learned proposal, same a, eta, n).
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "ptg_launch.h"
 #include "ptg_lma.cuh"
 #include "ptg_mlp.cuh"
 
 namespace ptg {
 
-// One training sample: normalised inputs, the bin of v, ln f(v) - ln f(v*).
+// One training sample: the network's inputs, the bin of v, the target
+// (largest sampled ln f in the bin, relative to ln f(v*)).
 struct MlpSample {
-    float x0, x1, x2;
+    float x[MLP_IN];
     int bin;
     float t;
 };
@@ -74,15 +77,20 @@ __device__ __forceinline__ void to_a(const float h[NT][4], uint32_t a[NT / 2][4]
     }
 }
 
-__device__ __forceinline__ void input_a(const float x[2][3], uint32_t a[1][4]) {
-    // 16 x 16 input tile, columns 0..2 used: rows g (x[0]) and g + 8 (x[1])
+__device__ __forceinline__ void input_a(const float x[2][MLP_IN], uint32_t a[1][4]) {
+    // 16 x 16 input tile, columns 0..MLP_IN-1 used (all below 8): this
+    // lane holds columns 2t, 2t+1 of rows g (x[0]) and g + 8 (x[1])
+    static_assert(MLP_IN <= 8, "the inputs fill the first half of the K tile");
     int t = threadIdx.x & 3;
-    float c0 = t == 0 ? x[0][0] : (t == 1 ? x[0][2] : 0.0f);
-    float c1 = t == 0 ? x[0][1] : 0.0f;
-    float d0 = t == 0 ? x[1][0] : (t == 1 ? x[1][2] : 0.0f);
-    float d1 = t == 0 ? x[1][1] : 0.0f;
-    a[0][0] = pack_bf16(c0, c1);
-    a[0][1] = pack_bf16(d0, d1);
+    float c[2][2];
+    for (int h = 0; h < 2; ++h)
+        for (int q = 0; q < 2; ++q) {
+            float v = 0.0f;
+            for (int i = 0; i < MLP_IN; ++i) v = (2 * t + q == i) ? x[h][i] : v;
+            c[h][q] = v;
+        }
+    a[0][0] = pack_bf16(c[0][0], c[0][1]);
+    a[0][1] = pack_bf16(c[1][0], c[1][1]);
     a[0][2] = 0u;
     a[0][3] = 0u;
 }
@@ -103,7 +111,7 @@ struct WarpFwd {
     float z0[8][4], z1[8][4], z2[8][4], o[2][4];
 };
 
-__device__ __forceinline__ void warp_forward(const MlpDev& m, const float x[2][3], WarpFwd& f) {
+__device__ __forceinline__ void warp_forward(const MlpDev& m, const float x[2][MLP_IN], WarpFwd& f) {
     uint32_t a0[1][4], a1[4][4];
     input_a(x, a0);
     dense<1, 8>(a0, m.w0, MLP_IN_PAD, m.p + P_B0, f.z0);
@@ -120,16 +128,16 @@ __device__ __forceinline__ void warp_forward(const MlpDev& m, const float x[2][3
 }
 
 // Batched inference: out[row][16].
-__global__ void __launch_bounds__(128) k_mlp_infer(MlpDev m, const float* x_in /* [n][3] */, unsigned long long n,
-                                                   float* out) {
+__global__ void __launch_bounds__(128) k_mlp_infer(MlpDev m, const float* x_in /* [n][MLP_IN] */,
+                                                   unsigned long long n, float* out) {
     unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
     unsigned long long r0 = warp * 16;
     if (r0 >= n) return;
     int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float x[2][3];
+    float x[2][MLP_IN];
     for (int h = 0; h < 2; ++h) {
         unsigned long long r = r0 + g + 8 * h;
-        for (int i = 0; i < 3; ++i) x[h][i] = r < n ? x_in[3 * r + i] : 0.0f;
+        for (int i = 0; i < MLP_IN; ++i) x[h][i] = r < n ? x_in[MLP_IN * r + i] : 0.0f;
     }
     WarpFwd f;
     warp_forward(m, x, f);
@@ -231,15 +239,17 @@ __global__ void __launch_bounds__(128) k_mlp_grad(MlpDev m, const MlpSample* dat
     float inv_rows = 1.0f / (float)rows;
     float loss = 0.0f;
     for (int r0 = b0r + warp * 16; r0 < b1r; r0 += 64) {
-        float x[2][3];
+        float x[2][MLP_IN];
         int bin[2];
         float tgt[2];
         bool ok[2];
         for (int h = 0; h < 2; ++h) {
             int r = r0 + g + 8 * h;
             ok[h] = r < b1r;
-            MlpSample smp = ok[h] ? data[first + r] : MlpSample{0.0f, 0.0f, 0.0f, -1, 0.0f};
-            x[h][0] = smp.x0, x[h][1] = smp.x1, x[h][2] = smp.x2;
+            MlpSample smp{};
+            smp.bin = -1;
+            if (ok[h]) smp = data[first + r];
+            for (int i = 0; i < MLP_IN; ++i) x[h][i] = smp.x[i];
             bin[h] = smp.bin;
             tgt[h] = smp.t;
             if (smp.bin < 0 || !(smp.t == smp.t)) ok[h] = false;
@@ -324,15 +334,15 @@ __global__ void __launch_bounds__(128) k_mlp_grad(MlpDev m, const MlpSample* dat
                 for (int q = 0; q < 4; ++q) dh[nt][q] *= dsilu(f.z0[nt][q]);
             }
             // layer 0: input x padded to 16 columns
-            float xin[2][4];
-            for (int h = 0; h < 2; ++h) xin[h][0] = xin[h][1] = xin[h][2] = xin[h][3] = 0.0f;
             __syncwarp();
             stage_rows<8>(dh, s.d);
             for (int h = 0; h < 2; ++h)
                 for (int c = 0; c < 16; c += 4) {
                     // lanes write the 16 x 16 input tile of their rows
                     int col = c + t;
-                    s.h[g + 8 * h][col] = __float2bfloat16(col < 3 ? x[h][col] : 0.0f);
+                    float v = 0.0f;
+                    for (int i = 0; i < MLP_IN; ++i) v = col == i ? x[h][i] : v;
+                    s.h[g + 8 * h][col] = __float2bfloat16(v);
                 }
             __syncwarp();
             grad_w(s, 4, 2, acc + P_W0, MLP_IN_PAD);
@@ -406,7 +416,8 @@ __global__ void k_mlp_sync(const float* p, MlpDev m) {
 
 // Draws of the table sampler for training and benchmarking: (a, eta)
 // log-uniform over [a_lo, a_hi] x [eta_lo, eta_hi], n by the CP harmonic
-// CDF; one uniform v and the exact spectrum f(v) per sample.
+// CDF; one bin of v and the exact spectrum's largest sampled value in it
+// per sample.
 __device__ __forceinline__ void draw_point(Draws& rng, double a_lo, double a_hi, double e_lo, double e_hi, double* a,
                                            double* eta) {
     *a = exp(log(a_lo) + (log(a_hi) - log(a_lo)) * rng.next());
@@ -427,61 +438,182 @@ __global__ void k_mlp_data(const LmaTables* t, unsigned long long n, unsigned lo
     double sn = 2.0 * nh * eta / (1.0 + a * a);
     double v_star = (1.0 + sn) / (2.0 + sn);
     double base = log(cp_diff_partial_rate(nh, a, eta, v_star));
-    double v = rng.next();
-    double f = cp_diff_partial_rate(nh, a, eta, v);
+    // the target is the largest of f at the bin's two edges and at two
+    // uniform interior points, so that a high quantile of it tracks the
+    // bin's maximum
+    int bin = min((int)(rng.next() * MLP_OUT), MLP_OUT - 1);
+    double lo = fmax((double)bin / MLP_OUT, 1e-9), hi = fmin((double)(bin + 1) / MLP_OUT, 1.0 - 1e-9);
+    double f = fmax(cp_diff_partial_rate(nh, a, eta, lo), cp_diff_partial_rate(nh, a, eta, hi));
+    for (int q = 0; q < 2; ++q) f = fmax(f, cp_diff_partial_rate(nh, a, eta, lo + (hi - lo) * rng.next()));
     MlpSample s;
-    float x[3];
-    mlp_features(a, eta, nh, x);
-    s.x0 = x[0], s.x1 = x[1], s.x2 = x[2];
-    s.bin = min((int)(v * MLP_OUT), MLP_OUT - 1);
-    double tv = log(f) - base;
-    s.t = (f > 0.0 && isfinite(tv) && isfinite(base)) ? (float)tv : __int_as_float(0x7fc00000);
+    mlp_features(a, eta, nh, s.x);
+    s.bin = bin;
+    // bins far under the peak carry no proposals: their targets are
+    // floored, which keeps the envelope above the spectrum there and the
+    // regression's range to the part of the spectrum that matters
+    double tv = fmax(log(f) - base, (double)MLP_TARGET_FLOOR);
+    s.t = (f > 0.0 && isfinite(base)) ? (float)tv : (isfinite(base) ? MLP_TARGET_FLOOR : __int_as_float(0x7fc00000));
     out[i] = s;
 }
 
-// Sampler benchmark: the same (a, eta, n) per index for both methods; the
-// plain method runs the reference's ceiling and rejection, the learned one
-// takes the envelope from `env` (batched inference, [n][16]).  Writes v and
-// per-sample counters (spectrum evaluations, fallbacks).
-__global__ void k_sampler_bench(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                                double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
-                                float* x_out, double* v_out, unsigned* evals_out, unsigned* fallback_out,
-                                int* status_out) {
-    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// ---------------------------------------------------- sampler benchmark --
+// Emission i draws (a, eta) and the harmonic n from its own stream, so both
+// methods see the same (a, eta, n) per index.
+__device__ __forceinline__ void bench_point(const NlcTables& nt, unsigned long long i, unsigned long long seed,
+                                            double a_lo, double a_hi, double e_lo, double e_hi, double* a, double* eta,
+                                            int* nh) {
     Draws pt;
     pt.begin(seed, mix64(i + 0x2545F4914F6CDD1Dull), 0);
-    double a, eta;
-    draw_point(pt, a_lo, a_hi, e_lo, e_hi, &a, &eta);
+    draw_point(pt, a_lo, a_hi, e_lo, e_hi, a, eta);
+    *nh = max(cp_invert(nt, *a, *eta, pt.next()), 1);
+}
+
+__global__ void k_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                                   double a_hi, double e_lo, double e_hi, float* x_out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
     NlcTables nt = nlc_view(*t);
-    int nh = cp_invert(nt, a, eta, pt.next());
-    if (nh < 1) nh = 1;
-    if (x_out) {
-        float x[3];
-        mlp_features(a, eta, nh, x);
-        x_out[3 * i] = x[0], x_out[3 * i + 1] = x[1], x_out[3 * i + 2] = x[2];
-    }
-    if (!v_out) return;  // features only
+    double a, eta;
+    int nh;
+    bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
+    mlp_features(a, eta, nh, x_out + MLP_IN * i);
+}
+
+// Both samplers as one state machine per lane, so that every lane of a warp
+// evaluates the spectrum at the same instruction on every pass of a single
+// loop: a lane that finishes an emission takes the next one from a global
+// counter (warp-aggregated) instead of idling while the other lanes of its
+// warp finish theirs.  The cost per emission is heavy-tailed (from two to
+// thousands of spectrum evaluations); without this the slowest lane sets
+// every warp's time.  Per emission and method the draws and decisions are
+// those of cp_sample_v (plain) and cp_sample_v_learned (learned, with the
+// capped continuation of cp_sample_v_capped).  fallback_out: bits 0-1 =
+// 0; 1 = the learned envelope under the spectrum, the reference's sampler
+// took over; 2 = no acceptance within LEARNED_TRIALS, the capped envelope
+// took over; 3 = 2 and then 1.  Bits 2-31: proposals drawn from the
+// learned (or capped) envelope.
+enum : int { SB_IDLE, SB_DONE, SB_CEIL, SB_TRIAL, SB_STAR, SB_LTRIAL, SB_MTRIAL };
+
+template <bool LEARNED>
+__global__ void __launch_bounds__(128) k_sampler_run(const LmaTables* t, unsigned long long n, unsigned long long seed,
+                                                     double a_lo, double a_hi, double e_lo, double e_hi,
+                                                     const float* env, float margin, unsigned long long* counter,
+                                                     double* v_out, unsigned* evals_out, unsigned* fallback_out,
+                                                     int* status_out) {
+    NlcTables nt = nlc_view(*t);
+    const unsigned FULL = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    int phase = SB_IDLE;
+    unsigned long long i = 0;
+    double a = 0.0, eta = 0.0, mx = 0.0, v = 0.0, u = 0.0;
+    int nh = 1, k = 0, bin = 0;
+    unsigned evals = 0, fb = 0, trials = 0, capped = 0;
+    Envelope e{};
     Draws rng;
-    rng.begin(seed ^ 0x9E3779B97F4A7C15ull, mix64(i), learned ? 2 : 1);
-    double v = -1.0;
-    uint32_t rej = 0;
-    int st;
-    unsigned evals;
-    unsigned fb = 0;
-    if (learned) {
-        LearnedCounts c{0, 0, 0};
-        st = cp_sample_v_learned(env + 16 * i, margin, nh, a, eta, rng, &v, &rej, &c);
-        evals = c.evals + (c.fallbacks ? 32u + rej + 1u : 0u);
-        fb = c.fallbacks;
-    } else {
-        st = cp_sample_v(nh, a, eta, rng, &v, &rej);
-        evals = 32u + rej + 1u;
+    for (;;) {
+        // new emissions for idle lanes
+        unsigned idle = __ballot_sync(FULL, phase == SB_IDLE);
+        if (idle) {
+            int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (phase == SB_IDLE) {
+                i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i >= n) {
+                    phase = SB_DONE;
+                } else {
+                    bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
+                    rng.begin(seed ^ 0x9E3779B97F4A7C15ull, mix64(i), LEARNED ? 2 : 1);
+                    evals = fb = trials = 0;
+                    k = 0;
+                    mx = -HUGE_VAL;
+                    phase = LEARNED ? SB_STAR : SB_CEIL;
+                }
+            }
+        }
+        if (__all_sync(FULL, phase == SB_DONE)) break;
+        // the point this lane evaluates on this pass
+        if (phase == SB_CEIL) {
+            v = cp_ceiling_point(nh, a, eta, k);
+        } else if (phase == SB_TRIAL) {
+            v = rng.next();
+            u = rng.next();
+        } else if (phase == SB_STAR) {
+            double sn = 2.0 * nh * eta / (1.0 + a * a);
+            v = (1.0 + sn) / (2.0 + sn);
+        } else if (phase == SB_LTRIAL || phase == SB_MTRIAL) {
+            v = envelope_draw(e, rng, &bin);
+        }
+        double f = 0.0;
+        if (phase != SB_DONE) {
+            f = cp_diff_partial_rate(nh, a, eta, v);
+            evals += 1;
+        }
+        // transitions
+        int st = -1;  // >= 0: the emission ends with this status
+        if (phase == SB_CEIL) {
+            mx = fmax(mx, f);
+            if (++k == 32) {
+                mx *= 1.2;
+                k = 0;
+                if (fb == 2) {
+                    capped = envelope_cap(&e, mx);
+                    phase = SB_MTRIAL;
+                } else {
+                    phase = SB_TRIAL;
+                }
+            }
+        } else if (phase == SB_TRIAL) {
+            if (u <= f / mx) {
+                st = 0;
+            } else if (++k == REJECTION_CAP) {
+                st = 4;  // PTG_ERR_REJECTION_CAP
+            }
+        } else if (phase == SB_STAR) {
+            if (envelope_from(env + MLP_OUT * i, margin, f, &e)) {
+                phase = SB_LTRIAL;
+            } else {
+                fb = 1;
+                phase = SB_CEIL;
+            }
+        } else if (phase == SB_LTRIAL) {
+            double g = e.scale * (double)e.w[bin];
+            trials += 1;
+            if (f > g) {
+                fb = 1;  // the envelope is under the spectrum: hand over
+                phase = SB_CEIL;
+            } else if (rng.next() * g < f) {
+                st = 0;
+            } else if (trials == LEARNED_TRIALS) {
+                fb = 2;
+                phase = SB_CEIL;
+            }
+        } else if (phase == SB_MTRIAL) {
+            double g = e.scale * (double)e.w[bin];
+            trials += 1;
+            if (f > g) {
+                if (capped & (1u << bin)) {
+                    st = 0;  // over the reference's own ceiling: its rule accepts
+                } else {
+                    fb = 3;
+                    k = 0;
+                    phase = SB_TRIAL;
+                }
+            } else if (rng.next() * g < f) {
+                st = 0;
+            } else if (++k == REJECTION_CAP) {
+                st = 4;
+            }
+        }
+        if (st >= 0) {
+            v_out[i] = st == 0 ? v : -1.0;
+            evals_out[i] = evals;
+            if (fallback_out) fallback_out[i] = fb | (min(trials, 0x3FFFFFFFu) << 2);
+            status_out[i] = st;
+            phase = SB_IDLE;
+        }
     }
-    v_out[i] = v;
-    evals_out[i] = evals;
-    fallback_out[i] = fb;
-    status_out[i] = st;
 }
 
 // ------------------------------------------------------------ launchers --
@@ -521,12 +653,33 @@ cudaError_t launch_mlp_data(const LmaTables* t, unsigned long long n, unsigned l
     return cudaGetLastError();
 }
 
-cudaError_t launch_sampler_bench(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                                 double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
-                                 float* x_out, double* v_out, unsigned* evals, unsigned* fallbacks, int* status,
-                                 cudaStream_t s) {
-    k_sampler_bench<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, learned, env,
-                                                                margin, x_out, v_out, evals, fallbacks, status);
+cudaError_t launch_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                                    double a_hi, double e_lo, double e_hi, float* x_out, cudaStream_t s) {
+    k_sampler_features<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, x_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
+                               double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
+                               unsigned long long* counter, double* v_out, unsigned* evals, unsigned* fallbacks,
+                               int* status, cudaStream_t s) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = learned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sampler_run<true>, 128, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sampler_run<false>, 128, 0);
+    if (e != cudaSuccess) return e;
+    // persistent grid: one wave of resident blocks, no more lanes than work
+    unsigned long long blocks = (unsigned long long)max(sms, 1) * (unsigned long long)max(per_sm, 1);
+    blocks = std::min(blocks, (n + 127) / 128);
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    if (learned)
+        k_sampler_run<true><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, margin, counter,
+                                                             v_out, evals, fallbacks, status);
+    else
+        k_sampler_run<false><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, margin,
+                                                              counter, v_out, evals, fallbacks, status);
     return cudaGetLastError();
 }
 

@@ -3,14 +3,15 @@
 // The reference samples v = s / s_max at harmonic n by rejection under a
 // flat ceiling that costs 32 evaluations of the spectrum
 // (nonlinear_compton/cp/mod.rs:42-70) before the first trial.  Here a small
-// MLP (inputs ln a, ln eta, ln n; 4 layers of width 64, SiLU; BF16 weights,
-// FP32 accumulation) predicts, for 16 equal bins of v, an upper envelope of
-// ln f(v) relative to ln f at v* = (1 + s_n) / (2 + s_n).  The sampler draws
-// a bin in proportion to the envelope, v uniformly inside it, and accepts
-// with probability f(v) / g(v) against the exact spectrum f, so accepted v
-// follow f exactly wherever g >= f.  A proposal with f > g (the envelope
-// under the spectrum) is detected and the emission falls back to the
-// reference's own sampler, so the distribution stays the reference's.
+// MLP (six features of a, eta and n; 4 layers of width 64, SiLU; BF16
+// weights, FP32 accumulation) predicts, for 16 equal bins of v, an upper
+// envelope of ln f(v) relative to ln f at v* = (1 + s_n) / (2 + s_n).  The
+// sampler draws a bin in proportion to the envelope, v uniformly inside it,
+// and accepts with probability f(v) / g(v) against the exact spectrum f,
+// so accepted v follow f exactly wherever g >= f.  A proposal with f > g
+// (the envelope under the spectrum) is detected and the emission is handed
+// to the reference's own sampler, as is one that finds no acceptance within
+// a fixed number of trials.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -18,7 +19,10 @@
 
 namespace ptg {
 
-enum { MLP_IN = 3, MLP_H = 64, MLP_OUT = 16, MLP_IN_PAD = 16 };
+enum { MLP_IN = 6, MLP_H = 64, MLP_OUT = 16, MLP_IN_PAD = 16 };
+
+// Lowest training target (ln of the envelope relative to f(v*)).
+constexpr float MLP_TARGET_FLOOR = -24.0f;
 
 // Device view of the network: row-major [out][in] BF16 weights (input of
 // layer 0 padded to 16), FP32 biases.
@@ -29,19 +33,26 @@ struct MlpParams {
     int enabled;
 };
 
-// Normalised inputs: ln a in [ln 0.05, ln 20], ln eta in [ln 1e-3, ln 2],
-// ln n in [0, ~12].
-__host__ __device__ __forceinline__ void mlp_features(double a, double eta, int n, float x[3]) {
-    x[0] = (float)(log(a) / 3.0);
+// Inputs, each scaled to about [-1, 1] over a in [0.05, 20], eta in
+// [1e-3, 2], n in [1, ~5e4]: ln a, ln eta, ln n, ln s_n (s_n = 2 n eta /
+// (1 + a^2), which maps v to the Bessel argument), v*, and
+// ln(n / (1 + a^2)^{3/2}), which sets how sharply J_n peaks in v.
+__host__ __device__ __forceinline__ void mlp_features(double a, double eta, int n, float x[MLP_IN]) {
+    double ln_a = log(a), ln_n = log((double)n), ln_1a2 = log1p(a * a);
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    x[0] = (float)(ln_a / 3.0);
     x[1] = (float)((log(eta) + 3.1) / 3.8);
-    x[2] = (float)(log((double)n) / 6.0 - 1.0);
+    x[2] = (float)(ln_n / 6.0 - 1.0);
+    x[3] = (float)(log(sn) / 6.0);
+    x[4] = (float)(2.0 * (1.0 + sn) / (2.0 + sn) - 2.0);
+    x[5] = (float)((ln_n - 1.5 * ln_1a2) / 6.0);
 }
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 
 // One lane's forward pass in FP32 (CUDA cores); used inside the collision
 // kernels, where emissions arrive one lane at a time.
-static __device__ __noinline__ void mlp_forward_lane(const MlpParams& m, const float x[3], float out[MLP_OUT]) {
+static __device__ __noinline__ void mlp_forward_lane(const MlpParams& m, const float x[MLP_IN], float out[MLP_OUT]) {
     float h0[MLP_H], h1[MLP_H];
     for (int o = 0; o < MLP_H; ++o) {
         float z = m.b0[o];
@@ -90,44 +101,109 @@ struct MlpDev {
 struct LearnedCounts {
     uint32_t evals;      // spectrum evaluations
     uint32_t trials;     // proposals
-    uint32_t fallbacks;  // envelope violations (fell back to the reference sampler)
+    uint32_t fallbacks;  // envelope violations (the reference's sampler took over)
+    uint32_t exhausted;  // no acceptance within LEARNED_TRIALS (the capped envelope took over)
 };
 
-// v at harmonic n from the learned envelope `o` (16 log-heights relative
-// to ln f(v*)).  Falls back to cp_sample_v on a violation.  Returns a ptg
-// status.
-static __device__ __noinline__ int cp_sample_v_learned(const float o[MLP_OUT], float margin, int n, double a, double eta,
-                                                       Draws& rng, double* v_out, uint32_t* rej, LearnedCounts* c) {
-    double sn = 2.0 * n * eta / (1.0 + a * a);
-    double v_star = (1.0 + sn) / (2.0 + sn);
-    double f_star = cp_diff_partial_rate(n, a, eta, v_star);
-    c->evals += 1;
-    double base = log(f_star);
-    if (!(f_star > 0.0) || !isfinite(base)) {
-        c->fallbacks += 1;
-        return cp_sample_v(n, a, eta, rng, v_out, rej);
+// Proposals under the learned envelope alone before the sampler also
+// computes the reference's ceiling C and continues under min(envelope, C).
+// A capped run of independent trials followed by a valid sampler still
+// returns v distributed as f, so the cap costs nothing in exactness; it
+// bounds the work where the learned envelope is loose.
+constexpr int LEARNED_TRIALS = 16;
+
+// The learned envelope of one emission: bin heights scale * w[k], w <= 1.
+struct Envelope {
+    double scale;
+    float w[MLP_OUT];
+    float total;
+};
+
+// From the network's outputs o (ln heights relative to f(v*)) and f(v*).
+// Returns false when the envelope is unusable.
+__device__ __forceinline__ bool envelope_from(const float* o, float margin, double f_star, Envelope* e) {
+    float o_max = -HUGE_VALF;
+    for (int q = 0; q < MLP_OUT; ++q) o_max = fmaxf(o_max, o[q]);
+    e->total = 0.0f;
+    for (int q = 0; q < MLP_OUT; ++q) {
+        e->w[q] = __expf(o[q] - o_max);
+        e->total += e->w[q];
     }
-    double w[MLP_OUT], cum[MLP_OUT];
-    double acc = 0.0;
-    for (int k = 0; k < MLP_OUT; ++k) {
-        w[k] = exp((double)o[k] + (double)margin);
-        acc += w[k];
-        cum[k] = acc;
+    e->scale = f_star * exp((double)o_max + (double)margin);
+    return f_star > 0.0 && isfinite(e->scale) && e->total > 0.0f;
+}
+
+// The envelope capped at the flat ceiling c: heights min(scale * w, c);
+// bit k of the result is set where the cap applies.
+__device__ __forceinline__ unsigned envelope_cap(Envelope* e, double c) {
+    double h[MLP_OUT], h_max = 0.0;
+    unsigned capped = 0;
+    for (int q = 0; q < MLP_OUT; ++q) {
+        double v = e->scale * (double)e->w[q];
+        if (v >= c) {
+            v = c;
+            capped |= 1u << q;
+        }
+        h[q] = v;
+        h_max = fmax(h_max, v);
     }
+    e->total = 0.0f;
+    for (int q = 0; q < MLP_OUT; ++q) {
+        e->w[q] = (float)(h[q] / h_max);
+        e->total += e->w[q];
+    }
+    e->scale = h_max;
+    return capped;
+}
+
+// A bin in proportion to the envelope's heights, and v uniformly in it.
+__device__ __forceinline__ double envelope_draw(const Envelope& e, Draws& rng, int* bin) {
+    float r = (float)rng.next() * e.total;
+    int k = 0;
+    float c = e.w[0];
+    while (k < MLP_OUT - 1 && c <= r) c += e.w[++k];
+    *bin = k;
+    return ((double)k + rng.next()) * (1.0 / MLP_OUT);
+}
+
+// The reference's sampler taking over one emission; counts its spectrum
+// evaluations (the 32-point ceiling and one per trial).
+static __device__ __noinline__ int cp_hand_over(int n, double a, double eta, Draws& rng, double* v_out,
+                                                uint32_t* rej, LearnedCounts* c) {
+    uint32_t before = *rej;
+    int st = cp_sample_v(n, a, eta, rng, v_out, rej);
+    c->evals += 32u + (*rej - before) + 1u;
+    return st;
+}
+
+// After LEARNED_TRIALS rejections: the reference's ceiling c, then
+// rejection under min(envelope, c).  Where the cap applies and f exceeds
+// it, the reference's own rule (accept when u <= f / c) accepts; where the
+// learned height applies and f exceeds it, the envelope is under the
+// spectrum and the reference's sampler takes over with the same c.
+static __device__ __noinline__ int cp_sample_v_capped(Envelope e, int n, double a, double eta, Draws& rng,
+                                                      double* v_out, uint32_t* rej, LearnedCounts* c) {
+    double ceil = cp_ceiling(n, a, eta);
+    c->evals += 32u;
+    unsigned capped = envelope_cap(&e, ceil);
     for (int it = 0; it < REJECTION_CAP; ++it) {
-        double u1 = rng.next() * acc;
-        int k = 0;
-        while (k < MLP_OUT - 1 && cum[k] <= u1) ++k;
-        double v = ((double)k + rng.next()) * (1.0 / MLP_OUT);
+        int k;
+        double v = envelope_draw(e, rng, &k);
         double f = cp_diff_partial_rate(n, a, eta, v);
         c->evals += 1;
-        c->trials += 1;
-        double g = exp(base) * w[k];
+        double g = e.scale * (double)e.w[k];
         if (f > g) {
-            // the envelope is under the spectrum here: use the reference's sampler
+            if (capped & (1u << k)) {
+                *v_out = v;
+                *rej += it;
+                return 0;
+            }
             c->fallbacks += 1;
             *rej += it;
-            return cp_sample_v(n, a, eta, rng, v_out, rej);
+            uint32_t before = *rej;
+            int st = cp_sample_v_under(n, a, eta, ceil, rng, v_out, rej);
+            c->evals += (*rej - before) + 1u;
+            return st;
         }
         if (rng.next() * g < f) {
             *v_out = v;
@@ -136,7 +212,44 @@ static __device__ __noinline__ int cp_sample_v_learned(const float o[MLP_OUT], f
         }
     }
     *rej += REJECTION_CAP;
-    return 4;
+    return 4;  // PTG_ERR_REJECTION_CAP
+}
+
+// v at harmonic n from the learned envelope `o` (16 log-heights relative
+// to ln f(v*)).  Returns a ptg status.
+static __device__ __noinline__ int cp_sample_v_learned(const float o[MLP_OUT], float margin, int n, double a, double eta,
+                                                       Draws& rng, double* v_out, uint32_t* rej, LearnedCounts* c) {
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double v_star = (1.0 + sn) / (2.0 + sn);
+    double f_star = cp_diff_partial_rate(n, a, eta, v_star);
+    c->evals += 1;
+    Envelope e;
+    if (!envelope_from(o, margin, f_star, &e)) {
+        c->fallbacks += 1;
+        return cp_hand_over(n, a, eta, rng, v_out, rej, c);
+    }
+    for (int it = 0; it < LEARNED_TRIALS; ++it) {
+        int k;
+        double v = envelope_draw(e, rng, &k);
+        double f = cp_diff_partial_rate(n, a, eta, v);
+        c->evals += 1;
+        c->trials += 1;
+        double g = e.scale * (double)e.w[k];
+        if (f > g) {
+            // the envelope is under the spectrum here
+            c->fallbacks += 1;
+            *rej += it;
+            return cp_hand_over(n, a, eta, rng, v_out, rej, c);
+        }
+        if (rng.next() * g < f) {
+            *v_out = v;
+            *rej += it;
+            return 0;
+        }
+    }
+    *rej += LEARNED_TRIALS;
+    c->exhausted += 1;
+    return cp_sample_v_capped(e, n, a, eta, rng, v_out, rej, c);
 }
 
 }  // namespace ptg

@@ -111,25 +111,24 @@ __device__ __forceinline__ double cp_diff_partial_rate(int n, double a, double e
     return -smax * (j * j + 0.5 * a * a * (1.0 + 0.5 * vs * vs / (1.0 - vs)) * (2.0 * j * j - jp * jp - jm * jm));
 }
 
-// nonlinear_compton/cp/mod.rs:42-75
-static __device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
+// nonlinear_compton/cp/mod.rs:42-75: the k-th of the 32 points (k in
+// [0, 32)) at which the ceiling takes the spectrum's maximum.
+__device__ __forceinline__ double cp_ceiling_point(int n, double a, double eta, int k) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     int n_switch = (int)(32.3 * (1.0 + 0.476 * pow(a, 1.56)));
-    double mx = -HUGE_VAL;
     if (sn < 2.0 || n < n_switch) {
         double v_opt = (1.0 + sn) / (2.0 + sn);
-        for (int i = 0; i < 16; ++i) mx = fmax(mx, cp_diff_partial_rate(n, a, eta, i * v_opt / 16.0));
-        for (int i = 0; i < 16; ++i) mx = fmax(mx, cp_diff_partial_rate(n, a, eta, v_opt + i * (1.0 - v_opt) / 16.0));
-    } else {
-        for (int k = 0; k < 16; ++k) {
-            double u = 0.5 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
-            mx = fmax(mx, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
-        }
-        for (int k = 0; k < 16; ++k) {
-            double u = (1.0 + sn) + 0.5 * 2.0 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0);
-            mx = fmax(mx, cp_diff_partial_rate(n, a, eta, u / (1.0 + u)));
-        }
+        return k < 16 ? k * v_opt / 16.0 : v_opt + (k - 16) * (1.0 - v_opt) / 16.0;
     }
+    double u = k < 16 ? 0.5 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k] + 1.0)
+                      : (1.0 + sn) + 0.5 * 2.0 * (1.0 + sn) * (PTG_GAUSS_16_NODES[k - 16] + 1.0);
+    return u / (1.0 + u);
+}
+
+// nonlinear_compton/cp/mod.rs:42-75: 1.2 x the largest of those values
+static __device__ __noinline__ double cp_ceiling(int n, double a, double eta) {
+    double mx = -HUGE_VAL;
+    for (int k = 0; k < 32; ++k) mx = fmax(mx, cp_diff_partial_rate(n, a, eta, cp_ceiling_point(n, a, eta, k)));
     return 1.2 * mx;
 }
 
@@ -250,9 +249,9 @@ static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, doubl
 
 // nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
 // nonlinear_compton/cp/mod.rs:181-200: v = s / s_max by rejection under
-// the ceiling.  Returns a ptg status.
-static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draws& rng, double* v_out, uint32_t* rej) {
-    double mx = cp_ceiling(n, a, eta);
+// the flat ceiling mx.  Returns a ptg status.
+static __device__ __noinline__ int cp_sample_v_under(int n, double a, double eta, double mx, Draws& rng,
+                                                     double* v_out, uint32_t* rej) {
     int it;
     for (it = 0; it < REJECTION_CAP; ++it) {
         double vv = rng.next(), u = rng.next();
@@ -263,6 +262,11 @@ static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draw
     }
     *rej += it;
     return it == REJECTION_CAP ? 4 : 0;  // PTG_ERR_REJECTION_CAP
+}
+
+// The same under the reference's ceiling.
+static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draws& rng, double* v_out, uint32_t* rej) {
+    return cp_sample_v_under(n, a, eta, cp_ceiling(n, a, eta), rng, v_out, rej);
 }
 
 // nonlinear_compton/cp/mod.rs:200-234: s, the azimuth and the Stokes

@@ -13,6 +13,7 @@ import os
 import numpy as np
 
 from . import abi
+from .abi import MLP_INPUTS
 from .build import LIB_PATH
 
 _lib = None
@@ -23,6 +24,8 @@ _EXPORTS = [
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_eval_fields", "ptg_push_steps",
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
+    "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
+    "ptg_sampler_bench",
 ]
 
 
@@ -97,6 +100,22 @@ def load(path=None):
                                      C.POINTER(abi.Particles), C.c_double, C.POINTER(abi.QueueCfg), DP]
     L.ptg_fp64_peak.restype = st
     L.ptg_fp64_peak.argtypes = [ctxp, DP]
+    FP = C.POINTER(C.c_float)
+    L.ptg_mlp_init.restype = st
+    L.ptg_mlp_init.argtypes = [ctxp, C.c_uint64]
+    L.ptg_mlp_params.restype = st
+    L.ptg_mlp_params.argtypes = [ctxp, FP, FP, C.POINTER(C.c_int32)]
+    L.ptg_mlp_train.restype = st
+    L.ptg_mlp_train.argtypes = [ctxp, C.POINTER(abi.MlpTrainCfg), C.POINTER(abi.MlpTrainStats)]
+    L.ptg_mlp_grad.restype = st
+    L.ptg_mlp_grad.argtypes = [ctxp, FP, C.c_size_t, C.c_float, FP, FP]
+    L.ptg_mlp_infer.restype = st
+    L.ptg_mlp_infer.argtypes = [ctxp, FP, C.c_size_t, FP]
+    L.ptg_mlp_use.restype = st
+    L.ptg_mlp_use.argtypes = [ctxp, C.c_int32, C.c_float]
+    L.ptg_sampler_bench.restype = st
+    L.ptg_sampler_bench.argtypes = [ctxp, C.POINTER(abi.SamplerBenchCfg), DP, DP, C.POINTER(abi.SamplerBenchDetail),
+                                     C.POINTER(abi.SamplerBenchStats)]
     _lib = L
     return L
 
@@ -277,6 +296,77 @@ class Engine:
         self._check(self.L.ptg_queue_autotune(self._h, len(collisions), arr, C.byref(options), C.byref(view),
                                               sample_fraction, C.byref(best), C.byref(ms)))
         return best.as_dict(), ms.value
+
+    # -- learned proposal --------------------------------------------------
+    def mlp_init(self, seed=1):
+        self._check(self.L.ptg_mlp_init(self._h, seed))
+
+    def mlp_params(self, set_to=None):
+        """Returns the FP32 parameter vector (after setting it, if given)."""
+        cnt = C.c_int32()
+        self._check(self.L.ptg_mlp_params(self._h, None, None, C.byref(cnt)))
+        if set_to is not None:
+            v = np.ascontiguousarray(set_to, dtype=np.float32)
+            self._check(self.L.ptg_mlp_params(self._h, None, v.ctypes.data_as(C.POINTER(C.c_float)), None))
+        out = np.zeros(cnt.value, dtype=np.float32)
+        self._check(self.L.ptg_mlp_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), None, None))
+        return out
+
+    def mlp_grad(self, samples, tau):
+        """Loss gradient of a batch: samples [n][MLP_INPUTS + 2] = the inputs,
+        bin, target."""
+        smp = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, MLP_INPUTS + 2)
+        cnt = C.c_int32()
+        self._check(self.L.ptg_mlp_params(self._h, None, None, C.byref(cnt)))
+        g = np.zeros(cnt.value, dtype=np.float32)
+        loss = C.c_float()
+        FP = C.POINTER(C.c_float)
+        self._check(self.L.ptg_mlp_grad(self._h, smp.ctypes.data_as(FP), len(smp), tau, g.ctypes.data_as(FP),
+                                        C.byref(loss)))
+        return g, loss.value
+
+    def mlp_infer(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_INPUTS)
+        out = np.zeros((len(x), 16), dtype=np.float32)
+        FP = C.POINTER(C.c_float)
+        self._check(self.L.ptg_mlp_infer(self._h, x.ctypes.data_as(FP), len(x), out.ctypes.data_as(FP)))
+        return out
+
+    def mlp_train(self, n_samples=2_000_000, batch=4096, epochs=1, lr=2e-3, tau=0.98, seed=7,
+                  a_range=(0.05, 20.0), eta_range=(1e-3, 2.0)):
+        cfg = abi.MlpTrainCfg(n_samples, batch, epochs, lr, tau, seed, a_range[0], a_range[1], eta_range[0],
+                              eta_range[1])
+        st = abi.MlpTrainStats()
+        self._check(self.L.ptg_mlp_train(self._h, C.byref(cfg), C.byref(st)))
+        return st.as_dict()
+
+    def mlp_use(self, enabled=True, margin=0.25):
+        self._check(self.L.ptg_mlp_use(self._h, int(enabled), margin))
+
+    def sampler_bench(self, n, seed=3, a_range=(0.05, 20.0), eta_range=(1e-3, 2.0), margin=0.25, want_v=True,
+                      detail=False):
+        """Plain vs learned v sampler on the same (a, eta, n) draws.  Returns
+        (v_plain, v_learned, stats[, per-emission detail dict])."""
+        cfg = abi.SamplerBenchCfg(n, seed, a_range[0], a_range[1], eta_range[0], eta_range[1], margin, 0.0)
+        st = abi.SamplerBenchStats()
+        v0 = np.zeros(n) if want_v else None
+        v1 = np.zeros(n) if want_v else None
+        det = None
+        dv = None
+        if detail:
+            det = {"x": np.zeros((n, MLP_INPUTS), np.float32), "env": np.zeros((n, 16), np.float32),
+                   "status_plain": np.zeros(n, np.int32), "status_learned": np.zeros(n, np.int32),
+                   "evals_plain": np.zeros(n, np.uint32), "evals_learned": np.zeros(n, np.uint32),
+                   "fallback": np.zeros(n, np.uint32)}
+            dv = abi.SamplerBenchDetail()
+            for name, _ in abi.SamplerBenchDetail._fields_:
+                setattr(dv, name, det[name].ctypes.data_as(dict(abi.SamplerBenchDetail._fields_)[name]))
+        self._check(self.L.ptg_sampler_bench(self._h, C.byref(cfg), _dp(v0) if want_v else None,
+                                             _dp(v1) if want_v else None, C.byref(dv) if dv is not None else None,
+                                             C.byref(st)))
+        if detail:
+            return v0, v1, st.as_dict(), det
+        return v0, v1, st.as_dict()
 
     def fp64_peak(self):
         """Measured FP64 FMA throughput, TFLOP/s."""

@@ -3,6 +3,7 @@ exports every entry point the public header declares; host-only entry
 points agree with the oracle; without a GPU the context reports
 PTG_ERR_NO_DEVICE instead of falling back to anything."""
 
+import ctypes as C
 import math
 import os
 import re
@@ -83,3 +84,42 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     with pytest.raises(engine.PtgError) as e:
         engine.Engine()
     assert e.value.status == abi.PTG_ERR_NO_DEVICE
+
+
+# ctypes mirror -> C struct of the header
+_LAYOUTS = {
+    "LaserDesc": "ptg_laser_desc", "CollideOptions": "ptg_collide_options", "Particles": "ptg_particles",
+    "RunStats": "ptg_run_stats", "DeviceCfg": "ptg_device_cfg", "Collision": "ptg_collision",
+    "QueueCfg": "ptg_queue_cfg", "MlpTrainCfg": "ptg_mlp_train_cfg", "MlpTrainStats": "ptg_mlp_train_stats",
+    "SamplerBenchCfg": "ptg_sampler_bench_cfg", "SamplerBenchStats": "ptg_sampler_bench_stats",
+    "SamplerBenchDetail": "ptg_sampler_bench_detail",
+}
+
+
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """Every ctypes mirror has the size and field offsets that a C compiler
+    gives the header's struct."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ptarmigan_gb300.h"', "int main(void) {"]
+    for py, cname in _LAYOUTS.items():
+        cls = getattr(abi, py)
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (py, cname))
+        for field in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (py, field[0], cname, field[0]))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([gcc, "-std=c99", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = dict(line.rsplit(" ", 1) for line in out if line)
+    for py in _LAYOUTS:
+        cls = getattr(abi, py)
+        assert int(got["%s size" % py]) == C.sizeof(cls), py
+        for field in cls._fields_:
+            assert int(got["%s.%s" % (py, field[0])]) == getattr(cls, field[0]).offset, (py, field[0])
