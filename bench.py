@@ -65,11 +65,13 @@ WORKLOAD = "focused LCFA shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; Fa
 
 # FP64 operations per step of collide_wave on this workload (2 x DFMA + DMUL
 # + DADD from ncu's SASS instruction counts over a 1e4-primary batch,
-# divided by that batch's step counts) and DRAM bytes per primary (ncu,
-# 1e6-primary batch).
+# divided by that batch's step counts) and DRAM bytes per primary
+# (dram__bytes_read.sum + dram__bytes_write.sum over the lepton and photon
+# waves of a 1e6-primary batch: 1.460e9 + 1.100e9 bytes; the pair waves add
+# nothing measurable).
 FP64_PER_LEPTON_STEP = 253.9
 FP64_PER_PHOTON_STEP = 34.2
-DRAM_BYTES_PER_PRIMARY = 2.05e6 / 1e4
+DRAM_BYTES_PER_PRIMARY = 2.5605e9 / 1e6
 
 
 def workload(n, seed):
@@ -266,14 +268,19 @@ def ks_critical(n, m, alpha=1e-3):
     return c * math.sqrt((n + m) / (n * m))
 
 
-def train_network(eng):
+def train_network(eng, args=None):
+    cfg = dict(MLP_TRAIN)
+    if args is not None and args.train_samples:
+        cfg["n_samples"] = args.train_samples
+    if args is not None and args.train_epochs:
+        cfg["epochs"] = args.train_epochs
     eng.mlp_init(3)
-    return eng.mlp_train(**MLP_TRAIN)
+    return dict(eng.mlp_train(**cfg), **cfg)
 
 
 def run_learned_sampler(args, eng, sampler, line):
     n = args.n or 10_000_000
-    tr = train_network(eng)
+    tr = train_network(eng, args)
     for w in range(args.warmup):
         eng.sampler_bench(min(n, 1_000_000), seed=500 + w, margin=MLP_MARGIN, want_v=False)
     runs, ks = [], None
@@ -297,10 +304,11 @@ def run_learned_sampler(args, eng, sampler, line):
         "envelope_violations": last["fallbacks"], "trial_cap_handovers": last["exhausted"],
         "errors": last["errors_plain"] + last["errors_learned"],
         "ms_split": {"features": last["features_ms"], "inference": last["infer_ms"], "sampling": last["learned_ms"]},
-        "training": dict(tr, **{k: v for k, v in MLP_TRAIN.items()}),
+        "training": tr,
         "config": {"workload": "learned_sampler: CP NLC v-sampler, a log-uniform [0.05, 20], eta log-uniform "
                                "[1e-3, 2], n from the CP harmonic table; %d emissions per step; network 6-64-64-64-16 "
-                               "SiLU trained on the GPU on 5e7 table-sampler draws" % n,
+                               "SiLU trained on the GPU on %.3g table-sampler draws x %d epochs"
+                               % (n, tr["n_samples"], tr["epochs"]),
                    "emissions_per_step": n, "margin": MLP_MARGIN},
         "gpu_launches": 4 * args.steps})
 
@@ -396,7 +404,7 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
             "Stokes tracked, pairs on, all generations")
     n = len(prim["species"])
     d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-    tr = train_network(eng)
+    tr = train_network(eng, args)
 
     def plain(seed):
         eng.mlp_use(False)
@@ -442,7 +450,7 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
                  "ks_photon_energy_vs_plain": ks_distance(e_p, e_l),
                  "ks_critical_1e-3": ks_critical(len(e_p), len(e_l)),
                  "learned": summary(out_l), "plain": summary(out_p),
-                 "training": dict(tr, **MLP_TRAIN),
+                 "training": tr,
                  "config": {"workload": desc, "n_primaries": n, "margin": MLP_MARGIN,
                             "value_path": "learned proposal + persistent queue kernel (CUDA graph)",
                             "plain_path": "reference sampler + wave kernels",
@@ -461,19 +469,23 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=N_PRIMARIES)
+    ap.add_argument("--n", type=int, default=None, help="primaries (emissions for learned_sampler)")
     ap.add_argument("--cpu-sample-per-core", type=int, default=1500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="lcfa_shower", choices=["lcfa_shower", "plane_wave_lma", "a0_scan",
                                                                     "cp_shower", "learned_sampler"])
     ap.add_argument("--scale", type=float, default=1.0, help="a0_scan: beam-size scale")
     ap.add_argument("--tune-fraction", type=float, default=0.02, help="a0_scan: autotuner sample fraction")
+    ap.add_argument("--train-samples", type=int, default=0,
+                    help="learned_sampler, cp_shower: training samples (default 5e7)")
+    ap.add_argument("--train-epochs", type=int, default=0, help="learned_sampler, cp_shower: epochs (default 3)")
     args = ap.parse_args()
     if args.workload != "lcfa_shower" and args.impl == "gb300":
-        if args.n == N_PRIMARIES:
-            args.n = 0
+        args.n = args.n or 0
         run_extra(args)
         return
+    if args.n is None:
+        args.n = N_PRIMARIES
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

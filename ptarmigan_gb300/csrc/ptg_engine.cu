@@ -1963,7 +1963,7 @@ ptg_status ptg_fp64_peak(ptg_ctx* c, double* tflops) {
 
 
 // ---------------------------------------------------- learned proposal ---
-static const int MLP_GRAD_BLOCKS = 64;
+static const int MLP_GRAD_BLOCKS = 304;  // two per SM on 152 SMs (shared memory allows two)
 
 static MlpDev mlp_dev(ptg_ctx* c) {
     MlpDev m{};
@@ -2225,15 +2225,17 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
     unsigned *de0 = nullptr, *de1 = nullptr, *df = nullptr;
     int *ds0 = nullptr, *ds1 = nullptr;
     unsigned long long* ctr = nullptr;
+    void* dpts = nullptr;
     auto cleanup = [&]() {
         cudaFree(dx), cudaFree(denv), cudaFree(dv0), cudaFree(dv1), cudaFree(de0), cudaFree(de1), cudaFree(df);
-        cudaFree(ds0), cudaFree(ds1), cudaFree(ctr);
+        cudaFree(ds0), cudaFree(ds1), cudaFree(ctr), cudaFree(dpts);
     };
     bool ok = cudaMalloc(&dx, 4 * MLP_IN * n) == cudaSuccess && cudaMalloc(&denv, 64 * n) == cudaSuccess &&
               cudaMalloc(&dv0, 8 * n) == cudaSuccess && cudaMalloc(&dv1, 8 * n) == cudaSuccess &&
               cudaMalloc(&de0, 4 * n) == cudaSuccess && cudaMalloc(&de1, 4 * n) == cudaSuccess &&
               cudaMalloc(&df, 4 * n) == cudaSuccess && cudaMalloc(&ds0, 4 * n) == cudaSuccess &&
-              cudaMalloc(&ds1, 4 * n) == cudaSuccess && cudaMalloc(&ctr, 8) == cudaSuccess;
+              cudaMalloc(&ds1, 4 * n) == cudaSuccess && cudaMalloc(&ctr, 8) == cudaSuccess &&
+              cudaMalloc(&dpts, sampler_point_bytes() * n) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         cleanup();
@@ -2246,17 +2248,18 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
     // plain: the reference's ceiling and rejection
     cudaEventRecord(e[0], s);
     err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
-                             cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
+                             nullptr, cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
     cudaEventRecord(e[1], s);
     // learned: features, batched tensor-core inference, then sampling
     if (err == cudaSuccess)
-        err = launch_sampler_features(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, dx, s);
+        err = launch_sampler_features(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, dx,
+                                      dpts, s);
     cudaEventRecord(e[2], s);
     if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), dx, n, denv, s);
     cudaEventRecord(e[3], s);
     if (err == cudaSuccess)
         err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1, denv,
-                                 cfg->margin, ctr, dv1, de1, df, ds1, s);
+                                 dpts, cfg->margin, ctr, dv1, de1, df, ds1, s);
     cudaEventRecord(e[4], s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     std::vector<unsigned> ev0(n), ev1(n), fb(n);

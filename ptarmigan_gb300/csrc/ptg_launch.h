@@ -40,12 +40,13 @@ cudaError_t launch_mlp_adam(float* p, float* mom, float* vel, const float* parti
 cudaError_t launch_mlp_sync(const float* p, const MlpDev& m, cudaStream_t s);
 cudaError_t launch_mlp_data(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
                             double a_hi, double e_lo, double e_hi, void* out, cudaStream_t s);
+size_t sampler_point_bytes();
 cudaError_t launch_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                                    double a_hi, double e_lo, double e_hi, float* x_out, cudaStream_t s);
+                                    double a_hi, double e_lo, double e_hi, float* x_out, void* pts, cudaStream_t s);
 cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                               double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
-                               unsigned long long* counter, double* v_out, unsigned* evals, unsigned* fallbacks,
-                               int* status, cudaStream_t s);
+                               double a_hi, double e_lo, double e_hi, int learned, const float* env, const void* pts,
+                               float margin, unsigned long long* counter, double* v_out, unsigned* evals,
+                               unsigned* fallbacks, int* status, cudaStream_t s);
 int mlp_param_count();
 size_t mlp_sample_bytes();
 }  // namespace ptg

@@ -468,8 +468,16 @@ __device__ __forceinline__ void bench_point(const NlcTables& nt, unsigned long l
     *nh = max(cp_invert(nt, *a, *eta, pt.next()), 1);
 }
 
+// One emission's point, kept between the learned path's passes.
+struct BenchPoint {
+    double a, eta;
+    int n, pad;
+};
+
+// The learned path's first pass: the point of every emission and the
+// network's inputs for it.
 __global__ void k_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                                   double a_hi, double e_lo, double e_hi, float* x_out) {
+                                   double a_hi, double e_lo, double e_hi, float* x_out, BenchPoint* pts) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     NlcTables nt = nlc_view(*t);
@@ -477,6 +485,7 @@ __global__ void k_sampler_features(const LmaTables* t, unsigned long long n, uns
     int nh;
     bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
     mlp_features(a, eta, nh, x_out + MLP_IN * i);
+    pts[i] = BenchPoint{a, eta, nh, 0};
 }
 
 // Both samplers as one state machine per lane, so that every lane of a warp
@@ -497,9 +506,9 @@ enum : int { SB_IDLE, SB_DONE, SB_CEIL, SB_TRIAL, SB_STAR, SB_LTRIAL, SB_MTRIAL 
 template <bool LEARNED>
 __global__ void __launch_bounds__(128) k_sampler_run(const LmaTables* t, unsigned long long n, unsigned long long seed,
                                                      double a_lo, double a_hi, double e_lo, double e_hi,
-                                                     const float* env, float margin, unsigned long long* counter,
-                                                     double* v_out, unsigned* evals_out, unsigned* fallback_out,
-                                                     int* status_out) {
+                                                     const float* env, const BenchPoint* pts, float margin,
+                                                     unsigned long long* counter, double* v_out, unsigned* evals_out,
+                                                     unsigned* fallback_out, int* status_out) {
     NlcTables nt = nlc_view(*t);
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
@@ -523,7 +532,12 @@ __global__ void __launch_bounds__(128) k_sampler_run(const LmaTables* t, unsigne
                 if (i >= n) {
                     phase = SB_DONE;
                 } else {
-                    bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
+                    if (LEARNED) {
+                        BenchPoint p = pts[i];
+                        a = p.a, eta = p.eta, nh = p.n;
+                    } else {
+                        bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
+                    }
                     rng.begin(seed ^ 0x9E3779B97F4A7C15ull, mix64(i), LEARNED ? 2 : 1);
                     evals = fb = trials = 0;
                     k = 0;
@@ -653,16 +667,20 @@ cudaError_t launch_mlp_data(const LmaTables* t, unsigned long long n, unsigned l
     return cudaGetLastError();
 }
 
+size_t sampler_point_bytes() { return sizeof(BenchPoint); }
+
 cudaError_t launch_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                                    double a_hi, double e_lo, double e_hi, float* x_out, cudaStream_t s) {
-    k_sampler_features<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, x_out);
+                                    double a_hi, double e_lo, double e_hi, float* x_out, void* pts, cudaStream_t s) {
+    k_sampler_features<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, x_out,
+                                                                   (BenchPoint*)pts);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
-                               double a_hi, double e_lo, double e_hi, int learned, const float* env, float margin,
-                               unsigned long long* counter, double* v_out, unsigned* evals, unsigned* fallbacks,
-                               int* status, cudaStream_t s) {
+                               double a_hi, double e_lo, double e_hi, int learned, const float* env, const void* pts,
+                               float margin, unsigned long long* counter, double* v_out, unsigned* evals,
+                               unsigned* fallbacks, int* status, cudaStream_t s) {
+    if (learned && (!env || !pts)) return cudaErrorInvalidValue;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -674,11 +692,12 @@ cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigne
     blocks = std::min(blocks, (n + 127) / 128);
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
+    const BenchPoint* p = (const BenchPoint*)pts;
     if (learned)
-        k_sampler_run<true><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, margin, counter,
-                                                             v_out, evals, fallbacks, status);
+        k_sampler_run<true><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, p, margin,
+                                                             counter, v_out, evals, fallbacks, status);
     else
-        k_sampler_run<false><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, margin,
+        k_sampler_run<false><<<(unsigned)blocks, 128, 0, s>>>(t, n, seed, a_lo, a_hi, e_lo, e_hi, env, p, margin,
                                                               counter, v_out, evals, fallbacks, status);
     return cudaGetLastError();
 }
