@@ -415,7 +415,9 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
         return eng.collide_multi_device([{"laser": laser, "seed": seed, "id_base": n, "first": 0, "count": n}],
                                         opts, d_prim)
 
-    eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
+    coll = [{"laser": laser, "seed": 100, "id_base": n, "first": 0, "count": n}]
+    eng.mlp_use(True, margin=MLP_MARGIN)
+    tune, tune_ms = eng.queue_autotune(coll, opts, d_prim, sample_fraction=args.tune_fraction)
     for w in range(args.warmup):
         plain(100 + w)
         learned(100 + w)
@@ -452,7 +454,8 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
                  "learned": summary(out_l), "plain": summary(out_p),
                  "training": tr,
                  "config": {"workload": desc, "n_primaries": n, "margin": MLP_MARGIN,
-                            "value_path": "learned proposal + persistent queue kernel (CUDA graph)",
+                            "value_path": "learned proposal + persistent queue kernel (CUDA graph, autotuned)",
+                            "autotuned": tune, "autotune_sample_ms": tune_ms,
                             "plain_path": "reference sampler + wave kernels",
                             "events_per_step_learned": {k: st_l[k] for k in keys},
                             "events_per_step_plain": {k: st_p[k] for k in keys}},

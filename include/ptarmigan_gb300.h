@@ -249,7 +249,9 @@ typedef struct {
 
 /* Launch shape of the queue kernel. */
 typedef struct {
-    int32_t variant;        /* 0: registers as needed; 1: capped for 3 blocks of 128 threads per SM */
+    int32_t variant;        /* 0: registers as needed; 1: capped for 3 blocks of 128 threads per SM;
+                               2: the single-collision kernel, for a batch of one collision
+                               (larger batches run variant 0) */
     int32_t blocks_per_sm;  /* 0 = occupancy maximum of the variant */
     int32_t chunk;          /* tickets (store slots) a lane takes per grab: 1..64 */
     int32_t use_graph;      /* replay the batch as a captured CUDA graph */

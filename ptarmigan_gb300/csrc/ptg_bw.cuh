@@ -166,6 +166,39 @@ static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, doub
     return true;
 }
 
+// A bound on each component of bw_by_summation's result.  For x >= 0 and
+// m >= 0, |J_m(x)| <= (x/2)^m / m!.  The integrand of bw_integrate is at
+// most J_n^2 (1 + k) + k (J_{n-1}^2 + J_{n+1}^2) with k = a^2 q / 2, where q
+// is at most its value at s_min (q falls on (0, 1/2]) and the Bessel
+// argument is at most n a / sqrt(1 + a^2); the quadrature weights of a
+// harmonic sum to s_max - s_min <= 1/2 and bw_integrate doubles the sum.
+// Harmonics below threshold (s_n <= 4) contribute nothing, as there.
+__device__ __forceinline__ double bw_summation_bound(double a, double eta) {
+    int n0, n1;
+    bw_sum_limits(a, eta, &n0, &n1);
+    double a2 = a * a, c = a / sqrt(1.0 + a2);
+    double total = 0.0;
+    for (int n = n0; n <= n1; ++n) {
+        double sn = 2.0 * n * eta / (1.0 + a2);
+        if (sn <= 4.0) continue;
+        double s_min = fmin(0.5 * (1.0 - sqrt(1.0 - 4.0 / sn)), 0.5);
+        double q = (1.0 - s_min) / s_min + s_min / (1.0 - s_min);
+        double x = 0.5 * n * c;
+        double bm = exp((n - 1) * log(x) - lgamma((double)n));  // bound on J_{n-1}
+        double b = bm * x / n, bp = b * x / (n + 1);             // J_n, J_{n+1}
+        double k = 0.5 * a2 * q;
+        total += b * b * (1.0 + k) + k * (bm * bm + bp * bp);
+    }
+    return total;
+}
+
+// Per-step pair probabilities below this are taken as zero where the rate
+// would otherwise be summed harmonic by harmonic.  No uniform draw is that
+// small but an exact zero (draws are multiples of 2^-53), the Stokes
+// factors (1 - p_avg) / (1 - p) of bw_probability round to exactly 1, and
+// the interaction count differs by less than this per step.
+constexpr double PAIR_PROB_NEGLIGIBLE = 1e-25;
+
 // TotalRate::value / probability dispatch (pair_creation/cp/mod.rs:265-287)
 __device__ __forceinline__ bool bw_rates(const double* T, double a, double eta, double* f0, double* f1) {
     if (a < 0.02 || bw_is_too_small(a, eta)) {
@@ -276,8 +309,14 @@ static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 s
     d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
     double f0, f1;
-    if (!bw_rates(T, a, eta, &f0, &f1)) return false;
     double c = ALPHA_FINE * dphi / eta;
+    if (a >= 0.02 && a < exp(PTG_BW_CP_LN_MIN_A) && !bw_is_too_small(a, eta) &&
+        c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE) {
+        // the summed rate cannot give a probability that matters: skip it
+        f0 = f1 = 0.0;
+    } else if (!bw_rates(T, a, eta, &f0, &f1)) {
+        return false;
+    }
     double p = c * (0.5 * ((f0 + f1) + sv.z * (f0 - f1)));
     double p_avg = c * (0.5 * (f0 + f1));
     double delta = c * (0.5 * (f0 - f1));

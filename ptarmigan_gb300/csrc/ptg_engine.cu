@@ -1232,12 +1232,25 @@ static ptg_status ensure_queue_arrays(ptg_ctx* c, size_t n_coll) {
     return PTG_OK;
 }
 
-static const void* queue_kernel_of(int variant) { return variant == 1 ? queue_kernel_v1() : queue_kernel_v0(); }
+static bool lma_model(int model) { return model == M_PLANE_WAVE || model == M_FOCUSED_LASER; }
+
+// The queue kernel of a variant; `model` (an M_* value) selects the
+// single-collision kernel's instantiation for variant 2.
+static const void* queue_kernel_of(int variant, int model) {
+    if (variant == 2) return lma_model(model) ? queue_kernel_single_lma(model) : queue_kernel_single_lcfa(model);
+    return variant == 1 ? queue_kernel_v1() : queue_kernel_v0();
+}
+
+static cudaError_t launch_queue(int variant, int model, int grid, cudaStream_t s, const QueueArgs& q) {
+    if (variant == 2)
+        return lma_model(model) ? launch_queue_single_lma(model, grid, s, q) : launch_queue_single_lcfa(model, grid, s, q);
+    return variant == 1 ? launch_queue_v1(grid, s, q) : launch_queue_v0(grid, s, q);
+}
 
 // Blocks of the queue kernel for a launch shape.
-static int queue_grid(ptg_ctx* c, const ptg_queue_cfg& q) {
+static int queue_grid(ptg_ctx* c, const ptg_queue_cfg& q, int model) {
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, queue_kernel_of(q.variant), 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, queue_kernel_of(q.variant, model), 128, 0);
     if (occ <= 0) occ = 1;
     int per_sm = q.blocks_per_sm > 0 ? std::min(q.blocks_per_sm, occ) : occ;
     return per_sm * c->num_sms;
@@ -1248,7 +1261,8 @@ static int queue_grid(ptg_ctx* c, const ptg_queue_cfg& q) {
 // and the read-back of the counters into pinned memory.  Captured once per
 // shape as a CUDA graph when cfg.use_graph is set.
 static cudaError_t enqueue_multi(ptg_ctx* c, const QueueArgs& q, const ptg_particles& d_in, unsigned long long n,
-                                 size_t n_coll, int grid, int variant, const FilterArgs& fa_proto, bool capturing) {
+                                 size_t n_coll, int grid, int variant, int model, const FilterArgs& fa_proto,
+                                 bool capturing) {
     cudaStream_t s = c->stream;
     cudaError_t e;
     // under capture, external event records become graph nodes that record
@@ -1265,7 +1279,7 @@ static cudaError_t enqueue_multi(ptg_ctx* c, const QueueArgs& q, const ptg_parti
         k_load_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c->s, d_in, n, c->d_qoff, c->d_qfirst, c->d_coll,
                                                                   (int)n_coll, c->init_u, c->shower_count);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    e = variant == 1 ? launch_queue_v1(grid, s, q) : launch_queue_v0(grid, s, q);
+    e = launch_queue(variant, model, grid, s, q);
     if (e != cudaSuccess) return e;
     // compaction over every reserved slot that fits the store (an overflowed
     // batch is rerun, so its output is never read)
@@ -1295,7 +1309,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     if (n_coll == 0 || n_coll > (1u << 20)) return set_err(PTG_ERR_INVALID_ARGUMENT, "number of collisions out of range");
     if (!d_in->species || !d_in->r || !d_in->u)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
-    if (qc.variant < 0 || qc.variant > 1 || qc.chunk < 1 || qc.chunk > 64 || qc.blocks_per_sm < 0)
+    if (qc.variant < 0 || qc.variant > 2 || qc.chunk < 1 || qc.chunk > 64 || qc.blocks_per_sm < 0)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
     CUDA_TRY(cudaSetDevice(c->device));
     cudaGetLastError();  // no stale error may reach the capture below
@@ -1332,9 +1346,22 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         c->h_qfirst[k] = coll[k].first;
         c->h_qoff[k + 1] = c->h_qoff[k] + coll[k].count;
     }
-    int grid = queue_grid(c, qc);
+    // the single-collision kernel runs batches of one collision, with that
+    // collision's parameters in its launch arguments; larger batches run
+    // variant 0 instead
+    int model = c->h_coll[0].f.model;
+    int variant = (qc.variant == 2 && n_coll != 1) ? 0 : qc.variant;
+    ptg_queue_cfg qe = qc;
+    qe.variant = variant;
+    int grid = queue_grid(c, qe, model);
     QueueArgs q{};
+    if (variant == 2) {
+        q.base.f = c->h_coll[0].f;
+        q.base.seed = c->h_coll[0].seed;
+        q.base.id_base = c->h_coll[0].id_base;
+    }
     fill_step_options(*o, &q.base.o);
+    if (variant == 2) q.base.o.dt = c->h_coll[0].dt;
     q.base.gl = c->gl;
     q.base.lma = c->lma_dev;
     q.base.mlp = mlp_params(c);
@@ -1371,7 +1398,8 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         if (qc.use_graph) {
             char key[512];
             std::snprintf(key, sizeof key, "%llu/%zu/%llu/%llu/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%d/%p/%d", n, n_coll,
-                          c->s.cap, c->out_cap, grid, qc.variant, qc.chunk, (void*)d_in->species, (void*)d_in->r,
+                          c->s.cap, c->out_cap, grid, variant * 8 + (model + 1), qc.chunk, (void*)d_in->species,
+                          (void*)d_in->r,
                           (void*)d_in->u, (void*)d_in->pol, (void*)d_in->weight, (void*)d_in->id, (void*)d_in->r0,
                           (void*)d_in->u0, q.base.db_cap, (void*)q.base.dbw, (int)sizeof(StepOptions));
             std::string k = key;
@@ -1384,7 +1412,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
                 c->q_graph_key.clear();
                 cudaGraph_t g = nullptr;
                 CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                cudaError_t e = enqueue_multi(c, q, *d_in, n, n_coll, grid, qc.variant, fa, true);
+                cudaError_t e = enqueue_multi(c, q, *d_in, n, n_coll, grid, variant, model, fa, true);
                 cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess || e2 != cudaSuccess) {
                     if (g) cudaGraphDestroy(g);
@@ -1402,7 +1430,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
             }
             CUDA_TRY(cudaGraphLaunch(c->q_graph, c->stream));
         } else {
-            CUDA_TRY(enqueue_multi(c, q, *d_in, n, n_coll, grid, qc.variant, fa, false));
+            CUDA_TRY(enqueue_multi(c, q, *d_in, n, n_coll, grid, variant, model, fa, false));
         }
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         const Counters& h = *c->h_counters;
@@ -1497,7 +1525,7 @@ ptg_status ptg_collide_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* col
 ptg_status ptg_queue_config(ptg_ctx* c, const ptg_queue_cfg* cfg, ptg_queue_cfg* cfg_out) {
     if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
     if (cfg) {
-        if (cfg->variant < 0 || cfg->variant > 1 || cfg->chunk < 1 || cfg->chunk > 64 || cfg->blocks_per_sm < 0)
+        if (cfg->variant < 0 || cfg->variant > 2 || cfg->chunk < 1 || cfg->chunk > 64 || cfg->blocks_per_sm < 0)
             return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
         c->qcfg = *cfg;
     }
@@ -1520,13 +1548,17 @@ ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* co
         s.count = std::min<uint64_t>(s.count, std::max<uint64_t>(m, 1));
     }
     CUDA_TRY(cudaSetDevice(c->device));
-    int occ[2] = {0, 0};
-    for (int v = 0; v < 2; ++v) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], queue_kernel_of(v), 128, 0);
+    // the single-collision variant is a candidate for a batch of one
+    double dt_max;
+    int model = make_field(coll[0].laser, &dt_max).model;
+    int n_var = n_coll == 1 ? 3 : 2;
+    int occ[3] = {0, 0, 0};
+    for (int v = 0; v < n_var; ++v) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], queue_kernel_of(v, model), 128, 0);
         if (occ[v] < 1) occ[v] = 1;
     }
     std::vector<ptg_queue_cfg> cands;
-    for (int v = 0; v < 2; ++v)
+    for (int v = 0; v < n_var; ++v)
         for (int bps : {occ[v], occ[v] > 1 ? occ[v] - 1 : 0})
             for (int chunk : {1, 2, 4})
                 if (bps > 0) cands.push_back(ptg_queue_cfg{v, bps, chunk, 1});

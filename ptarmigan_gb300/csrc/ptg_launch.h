@@ -16,11 +16,17 @@ const void* wave_kernel_lcfa(int model);
 const void* wave_kernel_lma(int model);
 
 // The persistent multi-collision queue kernel (128 threads per block):
-// variant 0 with the registers it needs, variant 1 capped for 3 blocks/SM.
+// variant 0 with the registers it needs, variant 1 capped for 3 blocks/SM,
+// variant 2 the single-collision kernel (one instantiation per field model,
+// M_* values).
 cudaError_t launch_queue_v0(int grid, cudaStream_t s, const QueueArgs& q);
 cudaError_t launch_queue_v1(int grid, cudaStream_t s, const QueueArgs& q);
 const void* queue_kernel_v0();
 const void* queue_kernel_v1();
+cudaError_t launch_queue_single_lma(int model, int grid, cudaStream_t s, const QueueArgs& q);
+cudaError_t launch_queue_single_lcfa(int model, int grid, cudaStream_t s, const QueueArgs& q);
+const void* queue_kernel_single_lma(int model);
+const void* queue_kernel_single_lcfa(int model);
 
 // Regeneration of the LP Breit-Wheeler mid-range CDF (ptg_regen.cu).
 cudaError_t launch_regen_lpm_partial(unsigned long long first, unsigned long long count, const int* n_of,

@@ -97,6 +97,19 @@ static __device__ __noinline__ int wait_slot(const WaveArgs& a, unsigned long lo
     return WAIT_TIMEOUT;
 }
 
+// One look at slot t, without waiting: READY, SKIP, DRAINED or NOT_YET.
+enum { POLL_NOT_YET = 3 };
+__device__ __forceinline__ int poll_slot(const WaveArgs& a, unsigned long long t) {
+    unsigned long long n = ld_acquire(&a.c->n_total);
+    if (t < n) {
+        if (t >= a.s.cap) return WAIT_SKIP;
+        return ld_acquire(a.s.ready + t) ? WAIT_READY : POLL_NOT_YET;
+    }
+    unsigned long long done = ld_acquire(&a.c->completed);
+    unsigned long long n2 = ld_acquire(&a.c->n_total);
+    return (done == n2 && t >= n2) ? WAIT_DRAINED : POLL_NOT_YET;
+}
+
 struct PartCounts {
     uint32_t rej, nemit, npair;
     unsigned long long lsteps, psteps;
@@ -152,6 +165,67 @@ __device__ __forceinline__ void queue_load(const WaveArgs& a, Lane& L, unsigned 
     L.decayed = false;
 }
 
+// A loaded ticket: false if it holds no particle to run (a phantom slot or
+// a bad collision index), which then counts as completed.  Otherwise
+// switches the lane's collision parameters if needed.
+__device__ __forceinline__ bool queue_begin(const QueueArgs& q, WaveArgs& a, Lane& L, int& cur) {
+    if (L.status == ST_PHANTOM || L.coll < 0 || L.coll >= q.n_coll) {
+        if (L.status != ST_PHANTOM) atomicAdd(&a.c->errors, 1ull);
+        __threadfence();
+        atomicAdd(&a.c->completed, 1ull);
+        return false;
+    }
+    if (L.coll != cur) {
+        const CollParams& cp = q.coll[L.coll];
+        a.f = cp.f;
+        a.o.dt = cp.dt;
+        a.seed = cp.seed;
+        a.id_base = cp.id_base;
+        cur = L.coll;
+    }
+    L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
+    L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
+    return true;
+}
+
+// A particle that has left the field, decayed or failed: its record back to
+// the store, its counts to its collision, then `completed` (after its
+// children, which were appended and published while it ran).
+__device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs& a, Lane& L, const PartCounts& pc) {
+    if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
+    lane_store(a, L);
+    CollStats* cs = q.stats + L.coll;
+    if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
+    if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
+    if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
+    if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
+    if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
+    if (L.status != ST_OK) atomicAdd(&cs->errors, 1ull);
+    __threadfence();
+    atomicAdd(&a.c->completed, 1ull);
+}
+
+// One step of the lane's particle (main.rs:134-289's loop body); true when
+// the particle is done.
+template <int MODEL>
+__device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCounts& pc) {
+    if (L.status != ST_OK || lane_untracked(a, L)) return true;
+    if (L.species != SP_PHOTON) {
+        if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop))) return true;
+        lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
+        ++L.step;
+        ++pc.lsteps;
+        return L.status != ST_OK;
+    }
+    if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
+          a.o.tracking_photons))
+        return true;
+    photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair);
+    ++L.step;
+    ++pc.psteps;
+    return L.status != ST_OK;
+}
+
 // Kernel variants: MINB > 1 caps the registers so that MINB blocks of 128
 // threads fit on an SM (the LCFA paths need fewer registers than LMA's).
 template <int MINB>
@@ -174,22 +248,7 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
         if (w == WAIT_SKIP) continue;
         Lane L;
         queue_load(a, L, ticket);
-        if (L.status == ST_PHANTOM || L.coll < 0 || L.coll >= q.n_coll) {
-            if (L.status != ST_PHANTOM) atomicAdd(&a.c->errors, 1ull);
-            __threadfence();
-            atomicAdd(&a.c->completed, 1ull);
-            continue;
-        }
-        if (L.coll != cur) {
-            const CollParams& cp = q.coll[L.coll];
-            a.f = cp.f;
-            a.o.dt = cp.dt;
-            a.seed = cp.seed;
-            a.id_base = cp.id_base;
-            cur = L.coll;
-        }
-        L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
-        L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
+        if (!queue_begin(q, a, L, cur)) continue;
         PartCounts pc{0, 0, 0, 0, 0};
         switch (a.f.model) {
             case M_PLANE_WAVE: run_particle<M_PLANE_WAVE>(a, L, pc); break;
@@ -197,18 +256,79 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
             case M_FOCUSED_LASER: run_particle<M_FOCUSED_LASER>(a, L, pc); break;
             default: run_particle<M_FAST_FOCUSED_LASER>(a, L, pc); break;
         }
-        if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
-        lane_store(a, L);
-        CollStats* cs = q.stats + L.coll;
-        if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
-        if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
-        if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
-        if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
-        if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
-        if (L.status != ST_OK) atomicAdd(&cs->errors, 1ull);
-        // the particle's children were appended and published before this
-        __threadfence();
-        atomicAdd(&a.c->completed, 1ull);
+        queue_finish(q, a, L, pc);
+    }
+}
+
+// The single-collision variant (a batch of one collision): one pass of a
+// single loop is one step of every lane's particle, as in collide_wave, so
+// a lane whose particle ends takes its next ticket at once, and the step
+// code reads the collision's parameters from the kernel's parameter space
+// (as collide_wave does) rather than from a per-lane copy that follows the
+// lane's current collision.  A lane whose ticket is not yet published looks
+// again on the next pass; the warp sleeps only when none of its lanes has a
+// particle.  Every wait is bounded by q.wait_ns of wall time.
+//
+// Tickets past the primaries are secondaries, mostly photons, whose steps
+// are a different code path from a lepton's: a lane holding such a ticket
+// starts it only once no lane of its warp is stepping a lepton, so that the
+// warps that carry the last primaries (the critical path) run undivided,
+// as in a wave, while warps that are free take the secondaries without a
+// device-wide barrier.
+template <int MODEL>
+__global__ void __launch_bounds__(128) collide_queue_single(const __grid_constant__ QueueArgs q) {
+    const unsigned FULL = 0xffffffffu;
+    const WaveArgs& a = q.base;
+    Lane L;
+    PartCounts pc{0, 0, 0, 0, 0};
+    bool have = false, holding = false, finished = false;
+    unsigned long long t = 0, t_end = 0, ticket = 0, wait_from = 0;
+    for (;;) {
+        if (__all_sync(FULL, finished)) break;
+        bool leptons = __any_sync(FULL, have && L.species != SP_PHOTON);
+        if (!have && !finished) {
+            if (!holding) {
+                if (t == t_end) {
+                    t = grab_tickets(a.c, (unsigned)q.chunk);
+                    t_end = t + (unsigned long long)q.chunk;
+                }
+                ticket = t++;
+                holding = true;
+                wait_from = global_ns();
+            }
+            int w = (leptons && ticket >= a.n_primaries) ? POLL_NOT_YET : poll_slot(a, ticket);
+            if (w == WAIT_DRAINED) {
+                finished = true;
+            } else if (w == WAIT_SKIP) {
+                holding = false;
+            } else if (w == POLL_NOT_YET) {
+                if (global_ns() - wait_from > q.wait_ns) {
+                    atomicAdd(&a.c->timeouts, 1ull);
+                    finished = true;
+                }
+            } else {
+                holding = false;
+                queue_load(a, L, ticket);
+                if (L.status == ST_PHANTOM || L.coll != 0) {
+                    if (L.status != ST_PHANTOM) atomicAdd(&a.c->errors, 1ull);
+                    __threadfence();
+                    atomicAdd(&a.c->completed, 1ull);
+                } else {
+                    L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
+                    L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
+                    pc = PartCounts{0, 0, 0, 0, 0};
+                    have = true;
+                }
+            }
+        }
+        if (__all_sync(FULL, !have)) {
+            __nanosleep(256);
+            continue;
+        }
+        if (have && queue_step<MODEL>(a, L, pc)) {
+            queue_finish(q, a, L, pc);
+            have = false;
+        }
     }
 }
 

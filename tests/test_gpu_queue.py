@@ -155,8 +155,38 @@ def test_queue_autotune_picks_a_valid_shape(eng):
     dev = torch.device("cuda", 0)
     d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
     best, ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=0.5)
+    # a mixed batch: the flat variant is not a candidate
     assert best["variant"] in (0, 1) and 1 <= best["chunk"] <= 64 and best["blocks_per_sm"] >= 1
     assert ms > 0.0 and math.isfinite(ms)
     assert eng.queue_config() == best
     out, offs, stats, total = eng.collide_multi_device(colls, opts, d_prim)
     assert offs[-1] == total["n_out"] and total["particle_errors"] == 0
+
+
+@pytest.mark.parametrize("model", [abi.FAST_FOCUSED_LASER, abi.FOCUSED_LASER])
+def test_single_collision_queue_matches_wave_path(eng, model):
+    """The single-collision queue kernel (variant 2: one step per pass with
+    lane refill, parameters in the launch arguments), pairs and every
+    generation on, matches the wave path particle for particle; a batch of
+    several collisions asked for variant 2 runs variant 0."""
+    if model == abi.FAST_FOCUSED_LASER:
+        laser = abi.laser_desc(model, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=3e-6, fwhm_duration=30e-15)
+    else:
+        laser = abi.laser_desc(model, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6, fwhm_duration=30e-15)
+    colls, prim = _batch([(laser, 120, 16.5, 21)])
+    opts = abi.collide_options(pol_resolved=1)
+    eng.queue_config(variant=2, blocks_per_sm=0, chunk=1, use_graph=1)
+    try:
+        parts, stats, total = eng.collide_multi(colls, opts, prim)
+        assert total["particle_errors"] == 0
+        c = colls[0]
+        single, sst = eng.collide(c["laser"], opts, prim, seed=c["seed"], id_base=c["id_base"])
+        _compare(parts[0], single, TOL[model], 0.02)
+        assert stats[0]["emissions"] == pytest.approx(sst["emissions"], rel=0.03, abs=2)
+        assert stats[0]["lepton_steps"] == pytest.approx(sst["lepton_steps"], rel=0.01)
+        colls_m, prim_m = _batch(_mixed_specs())
+        parts_m, _, total_m = eng.collide_multi(colls_m, abi.collide_options(max_generation=2, tracking_photons=0),
+                                                prim_m)
+        assert total_m["particle_errors"] == 0 and len(parts_m) == len(colls_m)
+    finally:
+        eng.queue_config(variant=0)
