@@ -342,7 +342,7 @@ def run_extra(args):
         colls, opts, prim = a0_scan_workload(1, scale=args.scale)
         n = int(sum(c["count"] for c in colls))
         d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-        tune, tune_ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=args.tune_fraction)
+        tune, tune_ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=args.tune_fraction or 0.02)
         for _ in range(args.warmup):
             eng.collide_multi_device(colls, opts, d_prim)
         ms, stats = [], None
@@ -417,7 +417,7 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
 
     coll = [{"laser": laser, "seed": 100, "id_base": n, "first": 0, "count": n}]
     eng.mlp_use(True, margin=MLP_MARGIN)
-    tune, tune_ms = eng.queue_autotune(coll, opts, d_prim, sample_fraction=args.tune_fraction)
+    tune, tune_ms = eng.queue_autotune(coll, opts, d_prim, sample_fraction=args.tune_fraction or 0.1)
     for w in range(args.warmup):
         plain(100 + w)
         learned(100 + w)
@@ -449,6 +449,7 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
     keys = ("lepton_steps", "photon_steps", "emissions", "pair_events", "n_created", "n_out", "particle_errors")
     line.update({"value": n / (np.mean(ms_l) / 1e3), "ms_per_step": float(np.mean(ms_l)),
                  "plain_value": n / (np.mean(ms_p) / 1e3), "plain_ms": float(np.mean(ms_p)),
+                 "ms_each_step": {"value_path": [float(x) for x in ms_l], "plain_path": [float(x) for x in ms_p]},
                  "ks_photon_energy_vs_plain": ks_distance(e_p, e_l),
                  "ks_critical_1e-3": ks_critical(len(e_p), len(e_l)),
                  "learned": summary(out_l), "plain": summary(out_p),
@@ -478,7 +479,8 @@ def main():
     ap.add_argument("--workload", default="lcfa_shower", choices=["lcfa_shower", "plane_wave_lma", "a0_scan",
                                                                     "cp_shower", "learned_sampler"])
     ap.add_argument("--scale", type=float, default=1.0, help="a0_scan: beam-size scale")
-    ap.add_argument("--tune-fraction", type=float, default=0.02, help="a0_scan: autotuner sample fraction")
+    ap.add_argument("--tune-fraction", type=float, default=None,
+                    help="autotuner sample fraction (a0_scan 0.02, cp_shower 0.1)")
     ap.add_argument("--train-samples", type=int, default=0,
                     help="learned_sampler, cp_shower: training samples (default 5e7)")
     ap.add_argument("--train-epochs", type=int, default=0, help="learned_sampler, cp_shower: epochs (default 3)")
