@@ -399,11 +399,21 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
     parameters and pair yields of the two are compared."""
     import torch
     from ptarmigan_gb300 import abi
+    t_host = time.time()
     laser, opts, prim = cp_shower_workload(args.n or 1_000_000, 1)
+    host_beam_ms = (time.time() - t_host) * 1e3
     desc = ("cp_shower: e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 30 fs; "
             "Stokes tracked, pairs on, all generations")
     n = len(prim["species"])
     d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    # the same beam generated on the device (ptg_build_beam), timed apart:
+    # beam generation is not part of the metric
+    from ptarmigan_gb300 import beam as beam_mod
+    g = beam_mod.gamma_from_energy(16.5)
+    bd = abi.beam_desc(gamma_mean=g, gamma_sigma=0.001 * g, sigma_x=5e-6, sigma_z=24e-6, rms_div=8e-6,
+                       initial_z=beam_mod.initial_z(laser, 24e-6))
+    eng.build_beam(bd, n, seed=1)
+    device_beam_ms, _ = timed(lambda: eng.build_beam(bd, n, seed=2))
     tr = train_network(eng, args)
 
     def plain(seed):
@@ -453,6 +463,7 @@ def run_cp_shower(args, eng, timed, sampler, line, dev):
                  "ks_photon_energy_vs_plain": ks_distance(e_p, e_l),
                  "ks_critical_1e-3": ks_critical(len(e_p), len(e_l)),
                  "learned": summary(out_l), "plain": summary(out_p),
+                 "beam_generation_ms": {"device_ptg_build_beam": device_beam_ms, "host_numpy": host_beam_ms},
                  "training": tr,
                  "config": {"workload": desc, "n_primaries": n, "margin": MLP_MARGIN,
                             "value_path": "learned proposal + persistent queue kernel (CUDA graph, autotuned)",

@@ -387,6 +387,48 @@ ptg_status ptg_mlp_use(ptg_ctx* ctx, int32_t enabled, float margin);
 ptg_status ptg_sampler_bench(ptg_ctx* ctx, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
                              const ptg_sampler_bench_detail* detail, ptg_sampler_bench_stats* stats);
 
+/* ------------------------------------------------------ beam builder ---
+ * Primary beams generated on the device: BeamBuilder::build
+ * (particle/builder.rs:173-219) with GammaDistribution::sample and
+ * RadialDistribution::sample (particle/dstr.rs:27-225).  Same
+ * distributions; a counter-based stream per particle instead of the
+ * reference's sequential RNG, so beams are statistically, not bitwise,
+ * the reference's. */
+typedef enum { PTG_GAMMA_NORMAL = 0, PTG_GAMMA_BREM = 1, PTG_GAMMA_CUSTOM = 2 } ptg_gamma_dstr;
+typedef enum { PTG_RADIAL_NORMAL = 0, PTG_RADIAL_TRUNC_NORMAL = 1, PTG_RADIAL_UNIFORM = 2 } ptg_radial_dstr;
+
+typedef struct {
+    int32_t species;            /* ptg_species */
+    int32_t gamma_dstr;         /* ptg_gamma_dstr */
+    double gamma_mean;          /* Normal: mean Lorentz factor */
+    double gamma_sigma;         /* Normal: rms */
+    double gamma_min;           /* Brem: minimum; Custom: unused (the CDF's first node) */
+    double gamma_max;           /* Brem: maximum */
+    double energy_chirp;        /* Normal, Custom: gamma-z correlation (rho = -energy_chirp) */
+    const double* custom_cdf;   /* Custom: host array of [len][2] (gamma, CDF) nodes, CDF from 0 to 1 */
+    int32_t custom_len;         /* Custom: nodes (2..4096) */
+    int32_t radial_dstr;        /* ptg_radial_dstr */
+    double sigma_x, sigma_y;    /* Normal, TruncNormal: rms transverse sizes (m) */
+    double x_max, y_max;        /* TruncNormal: semi-axes of the cut (m) */
+    double r_max;               /* Uniform: disk radius (m) */
+    double sigma_z;             /* rms length (m) */
+    double rms_div;             /* rms divergence (rad) */
+    double collision_angle;     /* rad */
+    double collision_plane;     /* rad */
+    double offset[3];           /* m */
+    double initial_z;           /* Field::ideal_initial_z() + 3 sigma_z (main.rs:1064) */
+    double pol[4];              /* Stokes vector of every primary */
+    double weight;
+} ptg_beam_desc;
+
+/* Writes n primaries into device arrays (species, r, u, pol, weight, id,
+ * parent_id of `out`, rows of 4 for four-vectors; other fields may be
+ * NULL).  Particle i draws from stream (seed, first_id + i) and gets id and
+ * parent id first_id + i.  Runs on the context's stream and returns after
+ * the kernel has finished. */
+ptg_status ptg_build_beam(ptg_ctx* ctx, const ptg_beam_desc* beam, uint64_t n, uint64_t seed, uint64_t first_id,
+                          const ptg_particles* out);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */
 ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);

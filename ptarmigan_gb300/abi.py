@@ -183,6 +183,65 @@ class SamplerBenchCfg(C.Structure):
     ]
 
 
+GAMMA_NORMAL, GAMMA_BREM, GAMMA_CUSTOM = 0, 1, 2
+RADIAL_NORMAL, RADIAL_TRUNC_NORMAL, RADIAL_UNIFORM = 0, 1, 2
+
+
+class BeamDesc(C.Structure):
+    _fields_ = [
+        ("species", C.c_int32),
+        ("gamma_dstr", C.c_int32),
+        ("gamma_mean", C.c_double),
+        ("gamma_sigma", C.c_double),
+        ("gamma_min", C.c_double),
+        ("gamma_max", C.c_double),
+        ("energy_chirp", C.c_double),
+        ("custom_cdf", C.POINTER(C.c_double)),
+        ("custom_len", C.c_int32),
+        ("radial_dstr", C.c_int32),
+        ("sigma_x", C.c_double),
+        ("sigma_y", C.c_double),
+        ("x_max", C.c_double),
+        ("y_max", C.c_double),
+        ("r_max", C.c_double),
+        ("sigma_z", C.c_double),
+        ("rms_div", C.c_double),
+        ("collision_angle", C.c_double),
+        ("collision_plane", C.c_double),
+        ("offset", C.c_double * 3),
+        ("initial_z", C.c_double),
+        ("pol", C.c_double * 4),
+        ("weight", C.c_double),
+    ]
+
+
+def beam_desc(gamma_mean=None, gamma_sigma=0.0, species=ELECTRON, gamma_dstr=GAMMA_NORMAL, gamma_min=0.0,
+              gamma_max=0.0, energy_chirp=0.0, custom_cdf=None, radial_dstr=RADIAL_NORMAL, sigma_x=0.0,
+              sigma_y=None, x_max=0.0, y_max=0.0, r_max=0.0, sigma_z=0.0, rms_div=0.0, collision_angle=0.0,
+              collision_plane=0.0, offset=(0.0, 0.0, 0.0), initial_z=0.0, stokes=(0.0, 0.0, 0.0), weight=1.0):
+    """A BeamDesc (the YAML beam section's keys).  `custom_cdf`: [len][2]
+    (gamma, CDF) nodes; the array must outlive the call that uses it."""
+    d = BeamDesc()
+    d.species, d.gamma_dstr, d.radial_dstr = species, gamma_dstr, radial_dstr
+    d.gamma_mean = gamma_mean if gamma_mean is not None else 0.0
+    d.gamma_sigma, d.gamma_min, d.gamma_max, d.energy_chirp = gamma_sigma, gamma_min, gamma_max, energy_chirp
+    if custom_cdf is not None:
+        d.custom_cdf = custom_cdf.ctypes.data_as(C.POINTER(C.c_double))
+        d.custom_len = len(custom_cdf)
+    d.sigma_x = sigma_x
+    d.sigma_y = sigma_x if sigma_y is None else sigma_y
+    d.x_max, d.y_max, d.r_max, d.sigma_z, d.rms_div = x_max, y_max, r_max, sigma_z, rms_div
+    d.collision_angle, d.collision_plane = collision_angle, collision_plane
+    for k in range(3):
+        d.offset[k] = offset[k]
+    d.initial_z = initial_z
+    d.pol[0] = 1.0
+    for k in range(3):
+        d.pol[k + 1] = stokes[k]
+    d.weight = weight
+    return d
+
+
 # Inputs of the learned proposal's network (features of a, eta, n).
 MLP_INPUTS = 6
 

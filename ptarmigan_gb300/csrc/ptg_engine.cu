@@ -1975,6 +1975,80 @@ __global__ void k_fp64_fma(int iters, double a, double b, double* sink) {
     if (acc == 12345.678) sink[0] = acc;  // keeps the chains live
 }
 
+// ------------------------------------------------------ beam builder ---
+ptg_status ptg_build_beam(ptg_ctx* c, const ptg_beam_desc* d, uint64_t n, uint64_t seed, uint64_t first_id,
+                          const ptg_particles* out) {
+    if (!c || !d || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n == 0) return PTG_OK;
+    if (d->species < PTG_ELECTRON || d->species > PTG_PHOTON)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "beam species out of range");
+    if (d->gamma_dstr < PTG_GAMMA_NORMAL || d->gamma_dstr > PTG_GAMMA_CUSTOM || d->radial_dstr < PTG_RADIAL_NORMAL ||
+        d->radial_dstr > PTG_RADIAL_UNIFORM)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "beam distribution out of range");
+    if (!(std::fabs(d->energy_chirp) < 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "energy chirp must lie in (-1, 1)");
+    if (d->gamma_dstr == PTG_GAMMA_NORMAL && !(d->gamma_mean > 1.0 && d->gamma_sigma >= 0.0))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "normal spectrum needs gamma > 1 and sigma >= 0");
+    if (d->gamma_dstr == PTG_GAMMA_BREM && !(d->gamma_min > 0.0 && d->gamma_max > d->gamma_min))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "bremsstrahlung spectrum needs 0 < gamma_min < gamma_max");
+    if (d->gamma_dstr == PTG_GAMMA_CUSTOM) {
+        if (!d->custom_cdf || d->custom_len < 2 || d->custom_len > 4096)
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "custom spectrum needs 2..4096 CDF nodes");
+        for (int k = 0; k < d->custom_len; ++k) {
+            const double* p = d->custom_cdf + 2 * k;
+            if (!std::isfinite(p[0]) || !std::isfinite(p[1]) ||
+                (k > 0 && (p[0] <= p[-2] || p[1] < p[-1])))
+                return set_err(PTG_ERR_INVALID_ARGUMENT, "custom CDF nodes must be finite and increasing");
+        }
+    }
+    if (d->radial_dstr == PTG_RADIAL_TRUNC_NORMAL && !(d->x_max > 0.0 && d->y_max > 0.0))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "truncated normal needs x_max, y_max > 0");
+    CUDA_TRY(cudaSetDevice(c->device));
+    BeamArgs b{};
+    b.species = d->species;
+    b.gamma_dstr = d->gamma_dstr;
+    b.radial_dstr = d->radial_dstr;
+    b.gamma_mean = d->gamma_mean, b.gamma_sigma = d->gamma_sigma;
+    b.gamma_min = d->gamma_min, b.gamma_max = d->gamma_max;
+    b.rho = -d->energy_chirp;  // builder.rs:120-124 flips the sign
+    b.sigma_x = d->sigma_x, b.sigma_y = d->sigma_y, b.x_max = d->x_max, b.y_max = d->y_max, b.r_max = d->r_max;
+    b.sigma_z = d->sigma_z, b.rms_div = d->rms_div;
+    b.angle = d->collision_angle;
+    b.cos_a = std::cos(d->collision_angle), b.sin_a = std::sin(d->collision_angle);
+    b.cos_p = std::cos(d->collision_plane), b.sin_p = std::sin(d->collision_plane);
+    b.off_x = d->offset[0], b.off_y = d->offset[1], b.off_z = d->offset[2];
+    b.initial_z = d->initial_z;
+    for (int k = 0; k < 4; ++k) b.pol[k] = d->pol[k];
+    b.weight = d->weight;
+    double* dcdf = nullptr;
+    unsigned long long* derr = nullptr;
+    auto cleanup = [&]() { cudaFree(dcdf), cudaFree(derr); };
+    if (cudaMalloc(&derr, 8) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "beam builder counter");
+    }
+    if (d->gamma_dstr == PTG_GAMMA_CUSTOM) {
+        if (cudaMalloc(&dcdf, 16 * (size_t)d->custom_len) != cudaSuccess) {
+            cudaGetLastError();
+            cleanup();
+            return set_err(PTG_ERR_ALLOC, "custom spectrum table");
+        }
+        cudaMemcpyAsync(dcdf, d->custom_cdf, 16 * (size_t)d->custom_len, cudaMemcpyHostToDevice, c->stream);
+        b.custom_cdf = dcdf;
+        b.custom_len = d->custom_len;
+    }
+    cudaMemsetAsync(derr, 0, 8, c->stream);
+    cudaError_t e = launch_build_beam(b, n, seed, first_id, out->species, out->r, out->u, out->pol, out->weight,
+                                      (unsigned long long*)out->id, (unsigned long long*)out->parent_id, derr,
+                                      c->stream);
+    unsigned long long nerr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nerr, derr, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cleanup();
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    if (nerr) return set_err(PTG_ERR_REJECTION_CAP, std::to_string(nerr) + " primaries could not be sampled");
+    return PTG_OK;
+}
+
 ptg_status ptg_fp64_peak(ptg_ctx* c, double* tflops) {
     if (!c || !tflops) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     CUDA_TRY(cudaSetDevice(c->device));

@@ -53,6 +53,20 @@ cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigne
                                double a_hi, double e_lo, double e_hi, int learned, const float* env, const void* pts,
                                float margin, unsigned long long* counter, double* v_out, unsigned* evals,
                                unsigned* fallbacks, int* status, cudaStream_t s);
+// Primary beams on the device (ptg_beam.cu).
+struct BeamArgs {
+    int species, gamma_dstr, radial_dstr, custom_len;
+    double gamma_mean, gamma_sigma, gamma_min, gamma_max, rho;
+    const double* custom_cdf;  // device [len][2]
+    double sigma_x, sigma_y, x_max, y_max, r_max, sigma_z, rms_div;
+    double angle, cos_a, sin_a, cos_p, sin_p;  // collision angle and plane
+    double off_x, off_y, off_z, initial_z;
+    double pol[4], weight;
+};
+cudaError_t launch_build_beam(const BeamArgs& b, unsigned long long n, unsigned long long seed,
+                              unsigned long long first_id, int* species, double* r, double* u, double* pol,
+                              double* weight, unsigned long long* id, unsigned long long* parent_id,
+                              unsigned long long* errors, cudaStream_t s);
 int mlp_param_count();
 size_t mlp_sample_bytes();
 }  // namespace ptg

@@ -25,7 +25,7 @@ _EXPORTS = [
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
-    "ptg_sampler_bench",
+    "ptg_sampler_bench", "ptg_build_beam",
 ]
 
 
@@ -113,6 +113,9 @@ def load(path=None):
     L.ptg_mlp_infer.argtypes = [ctxp, FP, C.c_size_t, FP]
     L.ptg_mlp_use.restype = st
     L.ptg_mlp_use.argtypes = [ctxp, C.c_int32, C.c_float]
+    L.ptg_build_beam.restype = st
+    L.ptg_build_beam.argtypes = [ctxp, C.POINTER(abi.BeamDesc), C.c_uint64, C.c_uint64, C.c_uint64,
+                                 C.POINTER(abi.Particles)]
     L.ptg_sampler_bench.restype = st
     L.ptg_sampler_bench.argtypes = [ctxp, C.POINTER(abi.SamplerBenchCfg), DP, DP, C.POINTER(abi.SamplerBenchDetail),
                                      C.POINTER(abi.SamplerBenchStats)]
@@ -137,6 +140,7 @@ class Engine:
         h = C.c_void_p()
         self._check(L.ptg_context_create(C.byref(cfg), C.byref(h)))
         self._h = h
+        self.device = device
         self.L = L
 
     def _check(self, status):
@@ -296,6 +300,25 @@ class Engine:
         self._check(self.L.ptg_queue_autotune(self._h, len(collisions), arr, C.byref(options), C.byref(view),
                                               sample_fraction, C.byref(best), C.byref(ms)))
         return best.as_dict(), ms.value
+
+    # -- beam builder ------------------------------------------------------
+    def build_beam(self, desc, n, seed, first_id=0, device=None):
+        """Generates n primaries on the device (ptg_build_beam).  Returns a
+        dict of CUDA tensors (species, r, u, pol, weight, id, parent_id) that
+        collide_device and collide_multi_device accept."""
+        import torch
+        dev = device if device is not None else torch.device("cuda", self.device)
+        out = {"species": torch.empty(n, dtype=torch.int32, device=dev),
+               "r": torch.empty((n, 4), dtype=torch.float64, device=dev),
+               "u": torch.empty((n, 4), dtype=torch.float64, device=dev),
+               "pol": torch.empty((n, 4), dtype=torch.float64, device=dev),
+               "weight": torch.empty(n, dtype=torch.float64, device=dev),
+               "id": torch.empty(n, dtype=torch.uint64, device=dev),
+               "parent_id": torch.empty(n, dtype=torch.uint64, device=dev)}
+        view = self._device_view(out)
+        torch.cuda.synchronize(dev)
+        self._check(self.L.ptg_build_beam(self._h, C.byref(desc), n, seed, first_id, C.byref(view)))
+        return out
 
     # -- learned proposal --------------------------------------------------
     def mlp_init(self, seed=1):
