@@ -429,6 +429,56 @@ typedef struct {
 ptg_status ptg_build_beam(ptg_ctx* ctx, const ptg_beam_desc* beam, uint64_t n, uint64_t seed, uint64_t first_id,
                           const ptg_particles* out);
 
+/* -------------------------------------------------- distribution output ---
+ * Histograms of a particle set on the device: Histogram::generate_1d and
+ * generate_2d (output/hgram.rs:209-448) over the particle functions of
+ * output/functions.rs, with the weights, range filter and bin and height
+ * specifications of DistributionFunction (output/mod.rs:173-343). */
+typedef enum {
+    PTG_OUT_ANGLE_X = 0, PTG_OUT_ANGLE_Y, PTG_OUT_THETA, PTG_OUT_POLAR_ANGLE, PTG_OUT_PX, PTG_OUT_PY, PTG_OUT_PZ,
+    PTG_OUT_P_PERP, PTG_OUT_R_PERP, PTG_OUT_R_X, PTG_OUT_R_Y, PTG_OUT_P_MINUS, PTG_OUT_P_PLUS, PTG_OUT_GAMMA,
+    PTG_OUT_ENERGY, PTG_OUT_UNIT, PTG_OUT_X, PTG_OUT_Y, PTG_OUT_Z, PTG_OUT_RADIUS, PTG_OUT_PAYLOAD,
+    PTG_OUT_PARENT_CHI, PTG_OUT_N_INTER, PTG_OUT_ABSORPTION, PTG_OUT_S1, PTG_OUT_S2, PTG_OUT_S3, PTG_OUT_POL_X,
+    PTG_OUT_POL_Y, PTG_OUT_WEIGHT, PTG_OUT_HELICITY
+} ptg_output_func;                                   /* output/functions.rs:10-105 */
+typedef enum { PTG_WEIGHT_NUMBER = 0, PTG_WEIGHT_ENERGY, PTG_WEIGHT_POL_X, PTG_WEIGHT_POL_Y,
+               PTG_WEIGHT_HELICITY } ptg_weight_func; /* output/functions.rs:244-263 */
+typedef enum { PTG_BINS_AUTO = 0, PTG_BINS_LOG, PTG_BINS_FIXED_NUMBER, PTG_BINS_FIXED_SIZE } ptg_bin_spec;
+typedef enum { PTG_HEIGHT_COUNT = 0, PTG_HEIGHT_DENSITY, PTG_HEIGHT_PDF } ptg_height_spec;
+
+typedef struct {
+    int32_t dim;                 /* 1 or 2 */
+    int32_t species;             /* ptg_species: the particle set is the particles of this species */
+    int32_t func[2];             /* ptg_output_func of each axis */
+    double scale[2];             /* unit conversion of each axis: value * scale */
+    int32_t weight;              /* ptg_weight_func */
+    int32_t bin_spec;            /* ptg_bin_spec, both axes */
+    int32_t height;              /* ptg_height_spec */
+    int32_t n_bins;              /* PTG_BINS_FIXED_NUMBER */
+    double bin_size;             /* PTG_BINS_FIXED_SIZE */
+    int32_t filter_func;         /* ptg_output_func, or -1: no filter */
+    int32_t reserved;
+    double filter_min, filter_max;  /* accepted when filter_min <= func(pt) < filter_max (default units) */
+} ptg_hgram_spec;
+
+typedef struct {
+    int32_t dim;
+    int32_t empty;               /* 1: the set is empty (the reference writes no histogram) */
+    uint64_t bins[2];
+    double min[2], max[2];       /* of the (log of the, for PTG_BINS_LOG) scaled values */
+    double bin_size[2];          /* 0 on an axis with a single bin */
+    double bin_volume, total, unweighted_total;
+    uint64_t n_counts;           /* bins[0] * bins[1] */
+} ptg_hgram_info;
+
+/* `particles` holds device arrays (rows of 4 for four-vectors); the
+ * function, weight and filter read species, u, r, pol, weight, payload,
+ * parent_chi, interaction_count and work as they need.  Fills `info`;
+ * writes the n_counts heights (row-major as the reference's) into `counts`
+ * when it is not NULL and counts_capacity >= n_counts. */
+ptg_status ptg_histogram(ptg_ctx* ctx, const ptg_particles* particles, const ptg_hgram_spec* spec,
+                         ptg_hgram_info* info, double* counts, uint64_t counts_capacity);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */
 ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);

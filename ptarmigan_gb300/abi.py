@@ -183,6 +183,44 @@ class SamplerBenchCfg(C.Structure):
     ]
 
 
+BINS_AUTO, BINS_LOG, BINS_FIXED_NUMBER, BINS_FIXED_SIZE = 0, 1, 2, 3
+HEIGHT_COUNT, HEIGHT_DENSITY, HEIGHT_PDF = 0, 1, 2
+WEIGHT_NUMBER, WEIGHT_ENERGY, WEIGHT_POL_X, WEIGHT_POL_Y, WEIGHT_HELICITY = 0, 1, 2, 3, 4
+
+
+class HgramSpec(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("species", C.c_int32),
+        ("func", C.c_int32 * 2),
+        ("scale", C.c_double * 2),
+        ("weight", C.c_int32),
+        ("bin_spec", C.c_int32),
+        ("height", C.c_int32),
+        ("n_bins", C.c_int32),
+        ("bin_size", C.c_double),
+        ("filter_func", C.c_int32),
+        ("reserved", C.c_int32),
+        ("filter_min", C.c_double),
+        ("filter_max", C.c_double),
+    ]
+
+
+class HgramInfo(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("empty", C.c_int32),
+        ("bins", C.c_uint64 * 2),
+        ("min", C.c_double * 2),
+        ("max", C.c_double * 2),
+        ("bin_size", C.c_double * 2),
+        ("bin_volume", C.c_double),
+        ("total", C.c_double),
+        ("unweighted_total", C.c_double),
+        ("n_counts", C.c_uint64),
+    ]
+
+
 GAMMA_NORMAL, GAMMA_BREM, GAMMA_CUSTOM = 0, 1, 2
 RADIAL_NORMAL, RADIAL_TRUNC_NORMAL, RADIAL_UNIFORM = 0, 1, 2
 

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1973,6 +1974,154 @@ __global__ void k_fp64_fma(int iters, double a, double b, double* sink) {
     double acc = 0.0;
     for (int k = 0; k < 8; ++k) acc += x[k];
     if (acc == 12345.678) sink[0] = acc;  // keeps the chains live
+}
+
+// ------------------------------------------------- distribution output ---
+// hgram.rs:171-184
+static uint64_t hgram_number_of_bins(double mn, double mx, uint64_t n, const ptg_hgram_spec& sp) {
+    if (mn == mx) return 1;
+    switch (sp.bin_spec) {
+        case PTG_BINS_FIXED_NUMBER: return (uint64_t)std::max(sp.n_bins, 0);
+        case PTG_BINS_FIXED_SIZE: {
+            double b = std::ceil((mx - mn) / sp.bin_size);
+            return b > 0.0 ? (b < 1.8e19 ? (uint64_t)b : ~0ull) : 0;
+        }
+        default: {
+            double b = std::ceil(2.0 * std::cbrt((double)n));
+            return b > 0.0 ? (uint64_t)b : 0;
+        }
+    }
+}
+
+// the width of a bin along an axis (hgram.rs:186-205, 241-251)
+static double hgram_bin_width(double mn, double mx, uint64_t nbins, const ptg_hgram_spec& sp) {
+    return sp.bin_spec == PTG_BINS_FIXED_SIZE ? sp.bin_size : (mx - mn) / (double)nbins;
+}
+
+ptg_status ptg_histogram(ptg_ctx* c, const ptg_particles* d, const ptg_hgram_spec* sp, ptg_hgram_info* info,
+                         double* counts, uint64_t counts_capacity) {
+    if (!c || !d || !sp || !info) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (sp->dim != 1 && sp->dim != 2) return set_err(PTG_ERR_INVALID_ARGUMENT, "histograms are 1- or 2-dimensional");
+    for (int k = 0; k < sp->dim; ++k)
+        if (sp->func[k] < PTG_OUT_ANGLE_X || sp->func[k] > PTG_OUT_HELICITY)
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "output function out of range");
+    if (sp->filter_func < -1 || sp->filter_func > PTG_OUT_HELICITY || sp->weight < PTG_WEIGHT_NUMBER ||
+        sp->weight > PTG_WEIGHT_HELICITY || sp->bin_spec < PTG_BINS_AUTO || sp->bin_spec > PTG_BINS_FIXED_SIZE ||
+        sp->height < PTG_HEIGHT_COUNT || sp->height > PTG_HEIGHT_PDF)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "histogram specification out of range");
+    if (sp->bin_spec == PTG_BINS_FIXED_NUMBER && sp->n_bins < 1)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "a fixed number of bins must be >= 1");
+    if (sp->bin_spec == PTG_BINS_FIXED_SIZE && !(sp->bin_size > 0.0))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "a fixed bin size must be > 0");
+    if (!d->species || !d->u || !d->r || !d->pol || !d->weight)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "particles need species, u, r, pol and weight");
+    auto uses = [&](int f) {
+        if (sp->filter_func == f) return true;
+        for (int k = 0; k < sp->dim; ++k)
+            if (sp->func[k] == f) return true;
+        return false;
+    };
+    if ((uses(PTG_OUT_PAYLOAD) && !d->payload) || (uses(PTG_OUT_PARENT_CHI) && !d->parent_chi) ||
+        (uses(PTG_OUT_N_INTER) && !d->interaction_count) || (uses(PTG_OUT_ABSORPTION) && !d->work))
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "an output function reads a field that is NULL");
+    std::memset(info, 0, sizeof(*info));
+    info->dim = sp->dim;
+    CUDA_TRY(cudaSetDevice(c->device));
+    HgramArgs h{};
+    h.species = d->species, h.u = d->u, h.r = d->r, h.pol = d->pol, h.weight = d->weight;
+    h.payload = d->payload, h.parent_chi = d->parent_chi, h.icount = d->interaction_count, h.work = d->work;
+    h.n = d->n;
+    h.want_species = sp->species;
+    h.dim = sp->dim;
+    h.func[0] = sp->func[0], h.func[1] = sp->dim == 2 ? sp->func[1] : sp->func[0];
+    h.scale[0] = sp->scale[0], h.scale[1] = sp->dim == 2 ? sp->scale[1] : sp->scale[0];
+    h.wfunc = sp->weight;
+    h.log_bins = sp->bin_spec == PTG_BINS_LOG;
+    h.filter_func = sp->filter_func;
+    h.fmin = sp->filter_min, h.fmax = sp->filter_max;
+    int blocks = (int)std::min<unsigned long long>((d->n + 255) / 256, 4ull * (unsigned long long)c->num_sms);
+    if (blocks < 1) blocks = 1;
+    double* dpart = nullptr;
+    double* dcts = nullptr;
+    auto cleanup = [&]() { cudaFree(dpart), cudaFree(dcts); };
+    if (cudaMalloc(&dpart, 48 * (size_t)blocks) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "histogram partials");
+    }
+    std::vector<double> part(6 * (size_t)blocks);
+    cudaError_t e = launch_hgram_stats(h, blocks, dpart, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, 48 * (size_t)blocks, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cleanup();
+        return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    double mn[2] = {DBL_MAX, DBL_MAX}, mx[2] = {-DBL_MAX, -DBL_MAX}, total = 0.0, num = 0.0;
+    for (int b = 0; b < blocks; ++b) {
+        const double* p = &part[6 * (size_t)b];
+        mn[0] = std::min(mn[0], p[0]), mx[0] = std::max(mx[0], p[1]);
+        mn[1] = std::min(mn[1], p[2]), mx[1] = std::max(mx[1], p[3]);
+        total += p[4], num += p[5];
+    }
+    uint64_t gnum = (uint64_t)num;
+    if (gnum == 0) {
+        info->empty = 1;
+        cleanup();
+        return PTG_OK;
+    }
+    // bins, sizes and the bin volume (hgram.rs:240-251 in 1d, 186-205 in 2d)
+    double vol = 1.0;
+    for (int k = 0; k < sp->dim; ++k) {
+        uint64_t nb = hgram_number_of_bins(mn[k], mx[k], gnum, *sp);
+        info->bins[k] = nb;
+        info->min[k] = mn[k], info->max[k] = mx[k];
+        double w = mn[k] == mx[k] ? (sp->dim == 1 ? 1.0 : 0.0) : hgram_bin_width(mn[k], mx[k], nb, *sp);
+        if (sp->dim == 1) {
+            vol = w;
+            h.bin_sz[0] = w;
+            info->bin_size[0] = nb <= 1 ? 0.0 : w;
+        } else {
+            vol *= mn[k] == mx[k] ? 1.0 : w;
+            h.bin_sz[k] = w;
+            info->bin_size[k] = w;
+        }
+        h.gmin[k] = mn[k];
+        h.nbins[k] = nb;
+    }
+    if (sp->dim == 1) info->bins[1] = 1, h.nbins[1] = 1;
+    unsigned long long ncts = h.nbins[0] * h.nbins[1];
+    if (h.nbins[0] == 0 || h.nbins[1] == 0 || h.nbins[0] > (1ull << 31) || h.nbins[1] > (1ull << 31) ||
+        ncts > (1ull << 31)) {
+        cleanup();
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "histogram would have " + std::to_string(h.nbins[0]) + " x " +
+                                                     std::to_string(h.nbins[1]) + " bins");
+    }
+    info->n_counts = ncts;
+    info->bin_volume = vol;
+    info->total = total;
+    info->unweighted_total = (double)gnum;
+    if (!counts || counts_capacity < ncts) {
+        cleanup();
+        return PTG_OK;
+    }
+    h.density_log = h.log_bins && (sp->height == PTG_HEIGHT_DENSITY || sp->height == PTG_HEIGHT_PDF);
+    if (cudaMalloc(&dcts, 8 * ncts) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return set_err(PTG_ERR_ALLOC, "histogram counts");
+    }
+    e = cudaMemsetAsync(dcts, 0, 8 * ncts, c->stream);
+    if (e == cudaSuccess) e = launch_hgram_fill(h, blocks, dcts, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts, dcts, 8 * ncts, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cleanup();
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    // heights (hgram.rs:297-301)
+    if (sp->height == PTG_HEIGHT_DENSITY)
+        for (unsigned long long k = 0; k < ncts; ++k) counts[k] = counts[k] / vol;
+    else if (sp->height == PTG_HEIGHT_PDF)
+        for (unsigned long long k = 0; k < ncts; ++k) counts[k] = counts[k] / (vol * total);
+    return PTG_OK;
 }
 
 // ------------------------------------------------------ beam builder ---

@@ -67,6 +67,21 @@ cudaError_t launch_build_beam(const BeamArgs& b, unsigned long long n, unsigned 
                               unsigned long long first_id, int* species, double* r, double* u, double* pol,
                               double* weight, unsigned long long* id, unsigned long long* parent_id,
                               unsigned long long* errors, cudaStream_t s);
+// Distribution output (ptg_hgram.cu): the particle set, its functions and
+// the binning of one histogram.
+struct HgramArgs {
+    const int* species;
+    const double *u, *r, *pol, *weight, *payload, *parent_chi, *icount, *work;
+    unsigned long long n;
+    int want_species, dim, func[2], wfunc, log_bins, filter_func;
+    double scale[2], fmin, fmax;
+    // binning (fill pass)
+    double gmin[2], bin_sz[2];
+    unsigned long long nbins[2];
+    int density_log;  // scale log-binned weights by the bin's linear width
+};
+cudaError_t launch_hgram_stats(const HgramArgs& h, int blocks, double* partials, cudaStream_t s);
+cudaError_t launch_hgram_fill(const HgramArgs& h, int blocks, double* counts, cudaStream_t s);
 int mlp_param_count();
 size_t mlp_sample_bytes();
 }  // namespace ptg

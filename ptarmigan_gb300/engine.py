@@ -25,8 +25,16 @@ _EXPORTS = [
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
-    "ptg_sampler_bench", "ptg_build_beam",
+    "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram",
 ]
+
+
+def _hgram_info(info):
+    d = info.dim
+    return {"dim": d, "empty": bool(info.empty), "bins": [int(info.bins[k]) for k in range(d)],
+            "min": [info.min[k] for k in range(d)], "max": [info.max[k] for k in range(d)],
+            "bin_size": [info.bin_size[k] for k in range(d)], "bin_volume": info.bin_volume, "total": info.total,
+            "unweighted_total": info.unweighted_total, "n_counts": int(info.n_counts)}
 
 
 class PtgError(RuntimeError):
@@ -113,6 +121,9 @@ def load(path=None):
     L.ptg_mlp_infer.argtypes = [ctxp, FP, C.c_size_t, FP]
     L.ptg_mlp_use.restype = st
     L.ptg_mlp_use.argtypes = [ctxp, C.c_int32, C.c_float]
+    L.ptg_histogram.restype = st
+    L.ptg_histogram.argtypes = [ctxp, C.POINTER(abi.Particles), C.POINTER(abi.HgramSpec), C.POINTER(abi.HgramInfo),
+                                DP, C.c_uint64]
     L.ptg_build_beam.restype = st
     L.ptg_build_beam.argtypes = [ctxp, C.POINTER(abi.BeamDesc), C.c_uint64, C.c_uint64, C.c_uint64,
                                  C.POINTER(abi.Particles)]
@@ -300,6 +311,23 @@ class Engine:
         self._check(self.L.ptg_queue_autotune(self._h, len(collisions), arr, C.byref(options), C.byref(view),
                                               sample_fraction, C.byref(best), C.byref(ms)))
         return best.as_dict(), ms.value
+
+    # -- distribution output -----------------------------------------------
+    def histogram(self, particles, spec):
+        """Histogram of a particle set on the device (ptg_histogram).
+        `particles`: a Particles struct with device pointers (as
+        collide_device returns) or a dict of CUDA tensors.  Returns (info
+        dict, heights array shaped [bins[1]][bins[0]] in 2d), or (info, None)
+        for an empty set."""
+        view = particles if isinstance(particles, abi.Particles) else self._device_view(particles)
+        info = abi.HgramInfo()
+        self._check(self.L.ptg_histogram(self._h, C.byref(view), C.byref(spec), C.byref(info), None, 0))
+        if info.empty:
+            return _hgram_info(info), None
+        counts = np.zeros(info.n_counts)
+        self._check(self.L.ptg_histogram(self._h, C.byref(view), C.byref(spec), C.byref(info), _dp(counts),
+                                         info.n_counts))
+        return _hgram_info(info), counts
 
     # -- beam builder ------------------------------------------------------
     def build_beam(self, desc, n, seed, first_id=0, device=None):

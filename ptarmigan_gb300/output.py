@@ -1,0 +1,251 @@
+"""Distribution output: the reference's DistributionFunction (output/mod.rs:
+173-343) over histograms generated on the device (ptg_histogram), with its
+unit systems (output/units.rs) and its plain-text file format
+(output/hgram.rs:530-562).
+
+    dstr = DistributionFunction.load("energy:(log;energy)")
+    dstr.write(engine, particles, abi.PHOTON, UnitSystem.default(), "out/photon")
+
+Filter bounds are numbers or "auto" (the reference's own expression
+evaluator is not part of this package).
+"""
+
+import math
+
+from . import abi
+
+# constants.rs
+ELEMENTARY_CHARGE = 1.602177e-19
+SPEED_OF_LIGHT = 2.997925e8
+
+# output/functions.rs:10-105: name -> (device function, output type)
+_DIMLESS, _ANGLE, _LENGTH, _ENERGY, _MOMENTUM = range(5)
+FUNCTIONS = {}
+for _names, _f, _t in (
+        (("angle_x",), 0, _ANGLE), (("angle_y",), 1, _ANGLE), (("theta", "pi_minus_angle"), 2, _ANGLE),
+        (("angle", "polar_angle"), 3, _ANGLE), (("px", "p_x"), 4, _MOMENTUM), (("py", "p_y"), 5, _MOMENTUM),
+        (("pz", "p_z"), 6, _MOMENTUM), (("p_perp",), 7, _MOMENTUM), (("r_perp",), 8, _DIMLESS),
+        (("r_x", "rx"), 9, _DIMLESS), (("r_y", "ry"), 10, _DIMLESS), (("p^-", "p-", "p_minus"), 11, _MOMENTUM),
+        (("p^+", "p+", "p_plus"), 12, _MOMENTUM), (("gamma",), 13, _DIMLESS), (("energy",), 14, _ENERGY),
+        (("unit",), 15, _DIMLESS), (("x",), 16, _LENGTH), (("y",), 17, _LENGTH), (("z",), 18, _LENGTH),
+        (("radius", "rho"), 19, _LENGTH), (("birth_a",), 20, _DIMLESS), (("parent_chi",), 21, _DIMLESS),
+        (("n_inter", "n_gamma", "n_pos"), 22, _DIMLESS), (("absorption", "energy_abs"), 23, _ENERGY),
+        (("weight", "number"), 29, _DIMLESS), (("S_1", "S1"), 24, _DIMLESS), (("S_2", "S2"), 25, _DIMLESS),
+        (("S_3", "S3"), 26, _DIMLESS), (("pol_x", "pol_sigma"), 27, _DIMLESS), (("pol_y", "pol_pi"), 28, _DIMLESS),
+        (("helicity",), 30, _DIMLESS)):
+    for _n in _names:
+        FUNCTIONS[_n] = (_f, _t)
+
+# output/mod.rs:226-233
+WEIGHTS = {"energy": abi.WEIGHT_ENERGY, "weight": abi.WEIGHT_NUMBER, "auto": abi.WEIGHT_NUMBER,
+           "pol_x": abi.WEIGHT_POL_X, "pol_y": abi.WEIGHT_POL_Y, "helicity": abi.WEIGHT_HELICITY}
+
+
+class Unit:
+    """A unit: `scale` converts from the default MeV-m system."""
+
+    def __init__(self, scale, name):
+        self.scale, self.name = scale, name
+
+
+class UnitSystem:
+    """output/units.rs:39-80."""
+
+    def __init__(self, length, energy, momentum):
+        self.length, self.energy, self.momentum = length, energy, momentum
+
+    @staticmethod
+    def default():
+        return UnitSystem(Unit(1.0, "m"), Unit(1.0, "MeV"), Unit(1.0, "MeV/c"))
+
+    @staticmethod
+    def hep():
+        return UnitSystem(Unit(1.0e3, "mm"), Unit(1.0e-3, "GeV"), Unit(1.0e-3, "GeV/c"))
+
+    @staticmethod
+    def si():
+        return UnitSystem(Unit(1.0, "m"), Unit(1.0e6 * ELEMENTARY_CHARGE, "J"),
+                          Unit(1.0e6 * ELEMENTARY_CHARGE / SPEED_OF_LIGHT, "kg/m/s"))
+
+    @staticmethod
+    def named(s):
+        """The output:units key: auto, hep or si (main.rs:925-945)."""
+        table = {"auto": UnitSystem.default, "hep": UnitSystem.hep, "HEP": UnitSystem.hep, "si": UnitSystem.si,
+                 "SI": UnitSystem.si}
+        if s not in table:
+            raise ValueError('unit system requested, "%s", is not one of "auto", "hep", or "si"' % s)
+        return table[s]()
+
+    def unit_of(self, otype):
+        """ParticleOutputType::into_unit (output/mod.rs:43-53)."""
+        return {_DIMLESS: Unit(1.0, "1"), _ANGLE: Unit(1.0, "rad"), _LENGTH: self.length, _ENERGY: self.energy,
+                _MOMENTUM: self.momentum}[otype]
+
+
+def _canonical(name):
+    return {"p^-": "p_minus", "p-": "p_minus", "p^+": "p_plus", "p+": "p_plus", "rho": "radius"}.get(name, name)
+
+
+def _bin_spec(s):
+    """BinSpec::from (output/hgram.rs:73-88): (kind, n_bins, bin_size)."""
+    try:
+        n = int(s)
+        if n >= 0 and str(n) == s.strip():
+            return abi.BINS_FIXED_NUMBER, n, 0.0
+    except ValueError:
+        pass
+    try:
+        return abi.BINS_FIXED_SIZE, 0, float(s)
+    except ValueError:
+        pass
+    return (abi.BINS_LOG if s == "log" else abi.BINS_AUTO), 0, 0.0
+
+
+class DistributionFunction:
+    """A distribution output spec such as "angle_x:angle_y:(100;energy)" or
+    "energy:(log;weight;energy in 1e3, auto)"."""
+
+    def __init__(self, names, funcs, types, bin_spec, weight, filter_):
+        self.names, self.funcs, self.types = names, funcs, types
+        self.dim = len(funcs)
+        self.bin_spec = bin_spec
+        self.weight = weight
+        self.filter = filter_  # None or (name, func, min, max) in default units
+
+    @staticmethod
+    def load(spec):
+        ss = spec.split(":")
+        bspec, weight, filt = (abi.BINS_AUTO, 0, 0.0), "weight", None
+        if len(ss) >= 2 and ss[-1].startswith("(") and ss[-1].endswith(")"):
+            last = ss.pop()[1:-1].split(";")
+            if len(last) == 1:
+                weight = last[0].strip()
+            elif len(last) == 2:
+                bspec, weight = _bin_spec(last[0].strip()), last[1].strip()
+            elif len(last) == 3:
+                bspec, weight, filt = _bin_spec(last[0].strip()), last[1].strip(), last[2]
+        if weight not in WEIGHTS or any(n not in FUNCTIONS for n in ss) or len(ss) not in (1, 2):
+            raise ValueError("cannot convert %r to a distribution function" % spec)
+        names = [_canonical(n) for n in ss]
+        funcs = [FUNCTIONS[n][0] for n in ss]
+        types = [FUNCTIONS[n][1] for n in ss]
+        return DistributionFunction(names, funcs, types, bspec, weight, DistributionFunction._filter(filt, spec))
+
+    @staticmethod
+    def _filter(s, spec):
+        """Filter::from_str (output/mod.rs:69-124), bounds given in SI."""
+        if s is None:
+            return None
+        err = ValueError("cannot convert %r to a filter" % spec)
+        if "," not in s:
+            raise err
+        prefix, suffix = s.split(",", 1)
+        words = prefix.split()
+        if len(words) < 3 or words[1] != "in":
+            raise err
+        name = _canonical(words[0])
+        if name not in FUNCTIONS:
+            raise err
+        func, otype = FUNCTIONS[name]
+
+        def num(t, auto):
+            t = t.strip()
+            if t == "auto":
+                return auto
+            try:
+                return float(t)
+            except ValueError:
+                raise err
+        lo = num("".join(words[2:]), -math.inf)
+        hi = num(suffix, math.inf)
+        # from_si multiplies by the reciprocal of the scale (output/units.rs:33-35)
+        r = 1.0 / UnitSystem.si().unit_of(otype).scale
+        return name, func, lo * r, hi * r
+
+    def spec(self, species, units):
+        h = abi.HgramSpec()
+        h.dim = self.dim
+        h.species = species
+        for k in range(self.dim):
+            h.func[k] = self.funcs[k]
+            h.scale[k] = units.unit_of(self.types[k]).scale
+        h.weight = WEIGHTS[self.weight]
+        h.bin_spec, h.n_bins, h.bin_size = self.bin_spec
+        h.height = abi.HEIGHT_DENSITY  # DistributionFunction::load always asks for densities
+        if self.filter is None:
+            h.filter_func, h.filter_min, h.filter_max = -1, -math.inf, math.inf
+        else:
+            h.filter_func, h.filter_min, h.filter_max = self.filter[1], self.filter[2], self.filter[3]
+        return h
+
+    def suffix(self):
+        """output/mod.rs:268-318."""
+        s = "_" + "-".join(self.names)
+        if self.weight not in ("weight", "auto"):
+            s += "_%s-weight" % self.weight
+        if self.bin_spec[0] == abi.BINS_LOG:
+            s += "_log"
+        if self.filter is not None:
+            s += "_%s-cut" % self.filter[0]
+        return s
+
+    def histogram(self, engine, particles, species, units):
+        """(Histogram, or None for an empty set)."""
+        info, counts = engine.histogram(particles, self.spec(species, units))
+        if counts is None:
+            return None
+        unit_names = [units.unit_of(t).name for t in self.types]
+        return Histogram(info, counts, self.names, unit_names)
+
+    def write(self, engine, particles, species, units, prefix):
+        """Writes prefix + suffix + ".dat"; returns the file name or None."""
+        h = self.histogram(engine, particles, species, units)
+        if h is None:
+            return None
+        return h.write_plain_text(prefix + self.suffix())
+
+
+def rust_exp(x):
+    """Rust's `{:.9e}` for an f64: 9 digits after the point, exponent with
+    no sign for positive powers and no padding."""
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "inf" if x > 0 else "-inf"
+    m, e = ("%.9e" % x).split("e")
+    return "%se%d" % (m, int(e))
+
+
+class Histogram:
+    """A histogram with the reference's metadata (output/hgram.rs:119-133)."""
+
+    def __init__(self, info, counts, names, units):
+        self.dim = info["dim"]
+        self.bins = info["bins"]
+        self.min, self.max, self.bin_size = info["min"], info["max"], info["bin_size"]
+        self.total, self.unweighted_total = info["total"], info["unweighted_total"]
+        self.counts = counts
+        if self.dim == 1:
+            self.name = "hgram/density/%s" % names[0]
+            self.bunit = "1/%s" % units[0]
+        else:
+            self.name = "hgram/density/%s_%s" % (names[0], names[1])
+            self.bunit = "1/(%s.%s)" % (units[0], units[1])
+        self.axis, self.unit = list(names), list(units)
+
+    def write_plain_text(self, filename):
+        """output/hgram.rs:530-562."""
+        filename = filename + ".dat"
+        lines = ["\t".join(self.axis) + "\t" + self.name, "\t".join(self.unit) + "\t" + self.bunit]
+        index = [0] * self.dim
+        for ct in self.counts:
+            for j in range(self.dim - 1):
+                if index[j] >= self.bins[j]:
+                    index[j] -= self.bins[j]
+                    index[j + 1] += 1
+            coord = [self.min[j] + (0.5 + index[j]) * self.bin_size[j] for j in range(self.dim)]
+            lines.append("".join(rust_exp(c) + "\t" for c in coord) + rust_exp(float(ct)))
+            index[0] += 1
+        with open(filename, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        return filename

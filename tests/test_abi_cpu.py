@@ -92,7 +92,8 @@ _LAYOUTS = {
     "RunStats": "ptg_run_stats", "DeviceCfg": "ptg_device_cfg", "Collision": "ptg_collision",
     "QueueCfg": "ptg_queue_cfg", "MlpTrainCfg": "ptg_mlp_train_cfg", "MlpTrainStats": "ptg_mlp_train_stats",
     "SamplerBenchCfg": "ptg_sampler_bench_cfg", "SamplerBenchStats": "ptg_sampler_bench_stats",
-    "SamplerBenchDetail": "ptg_sampler_bench_detail", "BeamDesc": "ptg_beam_desc",
+    "SamplerBenchDetail": "ptg_sampler_bench_detail", "BeamDesc": "ptg_beam_desc", "HgramSpec": "ptg_hgram_spec",
+    "HgramInfo": "ptg_hgram_info",
 }
 
 
