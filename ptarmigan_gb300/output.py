@@ -12,6 +12,8 @@ evaluator is not part of this package).
 
 import math
 
+import numpy as np
+
 from . import abi
 
 # constants.rs
@@ -197,12 +199,23 @@ class DistributionFunction:
         unit_names = [units.unit_of(t).name for t in self.types]
         return Histogram(info, counts, self.names, unit_names)
 
-    def write(self, engine, particles, species, units, prefix):
-        """Writes prefix + suffix + ".dat"; returns the file name or None."""
+    def write(self, engine, particles, species, units, prefix, file_format="plain_text"):
+        """Writes prefix + suffix + ".dat" (or ".fits"); returns the file name,
+        or None for an empty set."""
         h = self.histogram(engine, particles, species, units)
         if h is None:
             return None
+        if file_format == "fits":
+            return h.write_fits(prefix + self.suffix())
         return h.write_plain_text(prefix + self.suffix())
+
+
+VERSION = "0.1.0"
+
+
+def rust_exp_upper(x, width=20):
+    """Rust's `{:>20.9E}`."""
+    return rust_exp(x).replace("e", "E").rjust(width)
 
 
 def rust_exp(x):
@@ -232,6 +245,50 @@ class Histogram:
             self.name = "hgram/density/%s_%s" % (names[0], names[1])
             self.bunit = "1/(%s.%s)" % (units[0], units[1])
         self.axis, self.unit = list(names), list(units)
+
+    def write_fits(self, filename):
+        """output/hgram.rs:450-528: a primary HDU of 80-character cards
+        padded to 2880 bytes, then the heights as big-endian f64, padded to
+        a whole block."""
+        cards = ["SIMPLE  = %20s / %-47s" % ("T", "file conforms to FITS standard"),
+                 "BITPIX  = %20d / %-47s" % (-64, "number of bits per data pixel"),
+                 "NAXIS   = %20d / %-47s" % (self.dim, "number of data axes")]
+        for n in range(1, self.dim + 1):
+            cards.append("NAXIS%-3d= %20d / %-47s" % (n, self.bins[n - 1], "number of pixels along this axis"))
+        cards.append("EXTEND  = %20s / %-47s" % ("T", "dataset may contain extensions"))
+        for n in range(1, self.dim + 1):
+            cards.append("CRPIX%-3d= %s%-50s" % (n, rust_exp_upper(0.5), ""))
+            cards.append("CRVAL%-3d= %s%-50s" % (n, rust_exp_upper(self.min[n - 1]), ""))
+            cards.append("CDELT%-3d= %s%-50s" % (n, rust_exp_upper(self.bin_size[n - 1]), ""))
+            cards.append("CNAME%-3d= '%s'%s" % (n, self.axis[n - 1], " " * (80 - 12 - len(self.axis[n - 1]))))
+            cards.append("CUNIT%-3d= '%s'%s" % (n, self.unit[n - 1], " " * (80 - 12 - len(self.unit[n - 1]))))
+        cards.append("BUNIT   = '%s'%s" % (self.bunit, " " * (80 - 12 - len(self.bunit))))
+        cards.append("TOTAL   = %s%-50s" % (rust_exp_upper(self.total), ""))
+        cards.append("UWTOTAL = %s%-50s" % (rust_exp_upper(self.unweighted_total), ""))
+        cards.append("OBJECT  = '%s'%s" % (self.name, " " * (80 - 12 - len(self.name))))
+        if len(self.counts):
+            lo = hi = float(self.counts[0])
+            for c in self.counts:  # the reference's scan (else-if: a new minimum is not tested as a maximum)
+                c = float(c)
+                if c < lo:
+                    lo = c
+                elif c > hi:
+                    hi = c
+            cards.append("DATAMIN = %s%-50s" % (rust_exp_upper(lo), ""))
+            cards.append("DATAMAX = %s%-50s" % (rust_exp_upper(hi), ""))
+        comment = "COMMENT   Generated by ptarmigan-gb300 v%s" % VERSION
+        cards.append(comment.ljust(80))
+        cards.append("END".ljust(80))
+        header = "".join(cards).encode("ascii")
+        if any(len(c) != 80 for c in cards):
+            raise ValueError("a FITS card is not 80 characters long")
+        header += b" " * ((2880 - len(header) % 2880) % 2880)
+        data = np.asarray(self.counts, dtype=">f8").tobytes()
+        data += b"\0" * ((2880 - len(data) % 2880) % 2880)
+        filename = filename + ".fits"
+        with open(filename, "wb") as f:
+            f.write(header + data)
+        return filename
 
     def write_plain_text(self, filename):
         """output/hgram.rs:530-562."""

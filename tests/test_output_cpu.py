@@ -74,3 +74,27 @@ def test_oracle_histogram_on_known_points():
     assert info["bins"] == [4] and info["min"] == [0.0] and info["max"] == [7.0]
     assert list(cts) == [2.0, 2.0, 2.0, 1.0]  # the maximum lands past the last bin
     assert info["total"] == 8.0
+
+
+def test_fits_layout(tmp_path):
+    info = {"dim": 2, "bins": [3, 2], "min": [-1.0, 0.25], "max": [2.0, 1.0], "bin_size": [1.0, 0.375],
+            "total": 12.5, "unweighted_total": 7.0}
+    cts = np.array([0.5, -1.0, 2.0, 3.0, 0.0, 4.5])
+    h = Histogram(info, cts, ["angle_x", "angle_y"], ["rad", "rad"])
+    path = h.write_fits(str(tmp_path / "h"))
+    raw = open(path, "rb").read()
+    assert len(raw) % 2880 == 0 and len(raw) == 2 * 2880
+    cards = [raw[i:i + 80].decode() for i in range(0, 2880, 80)]
+    assert cards[0].startswith("SIMPLE  =                    T / file conforms to FITS standard")
+    assert cards[1].startswith("BITPIX  =                  -64 /")
+    assert cards[2].startswith("NAXIS   =                    2 /")
+    assert cards[3].startswith("NAXIS1  =                    3 /") and cards[4].startswith("NAXIS2  =                    2 /")
+    assert cards[6] == "CRPIX1  = " + "5.000000000E-1".rjust(20) + " " * 50
+    assert cards[7] == "CRVAL1  = " + "-1.000000000E0".rjust(20) + " " * 50
+    assert cards[9] == "CNAME1  = 'angle_x'" + " " * 61
+    names = [c[:8] for c in cards]
+    i = names.index("DATAMIN ")
+    assert cards[i].split("=")[1].strip() == "-1.000000000E0" and cards[i + 1].split("=")[1].strip() == "4.500000000E0"
+    assert "END" + " " * 77 in cards
+    data = np.frombuffer(raw[2880:2880 + 48], dtype=">f8")
+    assert np.array_equal(data, cts) and raw[2880 + 48:] == b"\0" * (2880 - 48)
