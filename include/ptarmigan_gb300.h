@@ -479,6 +479,30 @@ typedef struct {
 ptg_status ptg_histogram(ptg_ctx* ctx, const ptg_particles* particles, const ptg_hgram_spec* spec,
                          ptg_hgram_info* info, double* counts, uint64_t counts_capacity);
 
+/* Sums behind the summary statistics (SummaryStatistic, output/stats.rs:
+ * 265-483) over the particles of one species: with v = var_func(pt) and
+ * w = weight_func(pt) (PTG_OUT_UNIT for an unweighted statistic), and
+ * "within" meaning min < filter_func(pt) < max (always, without a filter),
+ *   total = sum over all of v w, subtotal = sum within of v w,
+ *   count = sum within of w, minimum / maximum within of v w,
+ *   sum_diffs = sum within of w (v - shift), sum_sq_diffs = sum within of
+ *   w (v - shift)^2, sum_cos / sum_sin = sum within of w cos v, w sin v. */
+typedef struct {
+    int32_t species;             /* ptg_species */
+    int32_t var_func;            /* ptg_output_func */
+    int32_t weight_func;         /* ptg_output_func */
+    int32_t filter_func;         /* ptg_output_func, or -1 */
+    double min, max;             /* filter bounds, default units, exclusive */
+    double shift;
+} ptg_stats_spec;
+
+typedef struct {
+    double total, subtotal, count, minimum, maximum, sum_diffs, sum_sq_diffs, sum_cos, sum_sin;
+} ptg_stats_sums;
+
+ptg_status ptg_particle_sums(ptg_ctx* ctx, const ptg_particles* particles, const ptg_stats_spec* spec,
+                             ptg_stats_sums* out);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */
 ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);

@@ -155,3 +155,36 @@ def generate(p, species, funcs, scales, wfunc, bin_spec, n_bins=0, bin_size=0.0,
     info = {"dim": dim, "bins": bins, "min": mn, "max": mx, "bin_size": shown, "bin_volume": vol, "total": total,
             "unweighted_total": float(n)}
     return info, cts
+
+
+def summary(p, species, op, var_func, weight_func, filter_func, lo, hi):
+    """SummaryStatistic::evaluate (output/stats.rs:265-483), sequentially
+    over the particles of one species in array order."""
+    sel = p["species"] == species
+    q = {k: v[sel] for k, v in p.items()}
+    v, w = value(q, var_func), value(q, weight_func)
+    within = np.ones(len(v), dtype=bool) if filter_func < 0 else (lambda f: (f > lo) & (f < hi))(value(q, filter_func))
+    vw = v * w
+    if op == "total":
+        return float(np.sum(vw[within]))
+    if op == "fraction":
+        return float(np.sum(vw[within]) / np.sum(vw))
+    if op == "mean":
+        return float(np.sum(vw[within]) / np.sum(w[within]))
+    if op == "minimum":
+        return float(np.min(vw[within])) if within.any() else math.inf
+    if op == "maximum":
+        return float(np.max(vw[within])) if within.any() else -math.inf
+    if op == "variance":
+        first = np.nonzero(within[:10])[0]
+        m = float(np.sum(vw[first]) / np.sum(w[first]))
+        d = v[within] - m
+        s2, s1, c = np.sum(w[within] * d ** 2), np.sum(w[within] * d), np.sum(w[within])
+        return float((s2 - s1 ** 2 / c) / c)
+    xb = np.sum(w[within] * np.cos(v[within])) / np.sum(w[within])
+    yb = np.sum(w[within] * np.sin(v[within])) / np.sum(w[within])
+    if op == "circmean":
+        return math.atan2(yb, xb)
+    if op == "circvar":
+        return 1.0 - math.hypot(xb, yb)
+    return math.sqrt(-2.0 * math.log(math.hypot(xb, yb)))

@@ -221,6 +221,26 @@ class HgramInfo(C.Structure):
     ]
 
 
+class StatsSpec(C.Structure):
+    _fields_ = [
+        ("species", C.c_int32),
+        ("var_func", C.c_int32),
+        ("weight_func", C.c_int32),
+        ("filter_func", C.c_int32),
+        ("min", C.c_double),
+        ("max", C.c_double),
+        ("shift", C.c_double),
+    ]
+
+
+class StatsSums(C.Structure):
+    _fields_ = [(name, C.c_double) for name in ("total", "subtotal", "count", "minimum", "maximum", "sum_diffs",
+                                                 "sum_sq_diffs", "sum_cos", "sum_sin")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 GAMMA_NORMAL, GAMMA_BREM, GAMMA_CUSTOM = 0, 1, 2
 RADIAL_NORMAL, RADIAL_TRUNC_NORMAL, RADIAL_UNIFORM = 0, 1, 2
 

@@ -2124,6 +2124,52 @@ ptg_status ptg_histogram(ptg_ctx* c, const ptg_particles* d, const ptg_hgram_spe
     return PTG_OK;
 }
 
+ptg_status ptg_particle_sums(ptg_ctx* c, const ptg_particles* d, const ptg_stats_spec* sp, ptg_stats_sums* out) {
+    if (!c || !d || !sp || !out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int f : {sp->var_func, sp->weight_func})
+        if (f < PTG_OUT_ANGLE_X || f > PTG_OUT_HELICITY)
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "output function out of range");
+    if (sp->filter_func < -1 || sp->filter_func > PTG_OUT_HELICITY)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "filter function out of range");
+    if (!d->species || !d->u || !d->r || !d->pol || !d->weight)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "particles need species, u, r, pol and weight");
+    for (int f : {sp->var_func, sp->weight_func, sp->filter_func})
+        if ((f == PTG_OUT_PAYLOAD && !d->payload) || (f == PTG_OUT_PARENT_CHI && !d->parent_chi) ||
+            (f == PTG_OUT_N_INTER && !d->interaction_count) || (f == PTG_OUT_ABSORPTION && !d->work))
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "an output function reads a field that is NULL");
+    CUDA_TRY(cudaSetDevice(c->device));
+    HgramArgs h{};
+    h.species = d->species, h.u = d->u, h.r = d->r, h.pol = d->pol, h.weight = d->weight;
+    h.payload = d->payload, h.parent_chi = d->parent_chi, h.icount = d->interaction_count, h.work = d->work;
+    h.n = d->n;
+    h.want_species = sp->species;
+    h.func[0] = sp->var_func, h.func[1] = sp->weight_func;
+    h.filter_func = sp->filter_func;
+    h.fmin = sp->min, h.fmax = sp->max;
+    int blocks = (int)std::min<unsigned long long>((d->n + 255) / 256, 4ull * (unsigned long long)c->num_sms);
+    if (blocks < 1) blocks = 1;
+    double* dpart = nullptr;
+    if (cudaMalloc(&dpart, 72 * (size_t)blocks) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(PTG_ERR_ALLOC, "statistic partials");
+    }
+    std::vector<double> part(9 * (size_t)blocks);
+    cudaError_t e = launch_particle_sums(h, sp->shift, blocks, dpart, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dpart, 72 * (size_t)blocks, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(dpart);
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
+    double a[9] = {0.0, 0.0, 0.0, HUGE_VAL, -HUGE_VAL, 0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < blocks; ++b)
+        for (int k = 0; k < 9; ++k) {
+            double v = part[9 * (size_t)b + k];
+            a[k] = k == 3 ? std::min(a[k], v) : (k == 4 ? std::max(a[k], v) : a[k] + v);
+        }
+    out->total = a[0], out->subtotal = a[1], out->count = a[2], out->minimum = a[3], out->maximum = a[4];
+    out->sum_diffs = a[5], out->sum_sq_diffs = a[6], out->sum_cos = a[7], out->sum_sin = a[8];
+    return PTG_OK;
+}
+
 // ------------------------------------------------------ beam builder ---
 ptg_status ptg_build_beam(ptg_ctx* c, const ptg_beam_desc* d, uint64_t n, uint64_t seed, uint64_t first_id,
                           const ptg_particles* out) {

@@ -217,6 +217,59 @@ __global__ void __launch_bounds__(256) k_hgram_fill(HgramArgs h, double* counts)
     }
 }
 
+// Summary-statistic sums (output/stats.rs:265-410): per block, [total,
+// subtotal, count, min, max, sum of w (v - shift), sum of w (v - shift)^2,
+// sum of w cos v, sum of w sin v].
+__global__ void __launch_bounds__(256) k_particle_sums(HgramArgs h, double shift, double* partials) {
+    __shared__ double sh[9][8];
+    double a[9] = {0.0, 0.0, 0.0, HUGE_VAL, -HUGE_VAL, 0.0, 0.0, 0.0, 0.0};
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < h.n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (h.species[i] != h.want_species) continue;
+        double v = out_value(h, i, h.func[0]), w = out_value(h, i, h.func[1]);
+        double vw = v * w;
+        a[0] += vw;
+        bool within = true;
+        if (h.filter_func >= 0) {
+            double f = out_value(h, i, h.filter_func);
+            within = f > h.fmin && f < h.fmax;
+        }
+        if (!within) continue;
+        a[1] += vw;
+        a[2] += w;
+        if (vw < a[3]) a[3] = vw;
+        if (vw > a[4]) a[4] = vw;
+        double d = v - shift;
+        a[5] += w * d;
+        a[6] += w * (d * d);
+        a[7] += w * cos(v);
+        a[8] += w * sin(v);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int k = 0; k < 9; ++k) {
+            double o = __shfl_down_sync(0xffffffffu, a[k], off);
+            a[k] = k == 3 ? fmin(a[k], o) : (k == 4 ? fmax(a[k], o) : a[k] + o);
+        }
+    }
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int k = 0; k < 9; ++k) sh[k][warp] = a[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 9; ++k) {
+            double o = sh[k][0];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                o = k == 3 ? fmin(o, sh[k][w]) : (k == 4 ? fmax(o, sh[k][w]) : o + sh[k][w]);
+            partials[9 * blockIdx.x + k] = o;
+        }
+    }
+}
+
+cudaError_t launch_particle_sums(const HgramArgs& h, double shift, int blocks, double* partials, cudaStream_t s) {
+    k_particle_sums<<<blocks, 256, 0, s>>>(h, shift, partials);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_hgram_stats(const HgramArgs& h, int blocks, double* partials, cudaStream_t s) {
     k_hgram_stats<<<blocks, 256, 0, s>>>(h, partials);
     return cudaGetLastError();

@@ -82,6 +82,10 @@ struct HgramArgs {
 };
 cudaError_t launch_hgram_stats(const HgramArgs& h, int blocks, double* partials, cudaStream_t s);
 cudaError_t launch_hgram_fill(const HgramArgs& h, int blocks, double* counts, cudaStream_t s);
+// Summary-statistic sums: h.func[0] is the variable, h.func[1] the weight
+// function, h.filter_func / fmin / fmax the exclusive filter; 9 doubles per
+// block.
+cudaError_t launch_particle_sums(const HgramArgs& h, double shift, int blocks, double* partials, cudaStream_t s);
 int mlp_param_count();
 size_t mlp_sample_bytes();
 }  // namespace ptg

@@ -25,7 +25,7 @@ _EXPORTS = [
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
-    "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram",
+    "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram", "ptg_particle_sums",
 ]
 
 
@@ -121,6 +121,9 @@ def load(path=None):
     L.ptg_mlp_infer.argtypes = [ctxp, FP, C.c_size_t, FP]
     L.ptg_mlp_use.restype = st
     L.ptg_mlp_use.argtypes = [ctxp, C.c_int32, C.c_float]
+    L.ptg_particle_sums.restype = st
+    L.ptg_particle_sums.argtypes = [ctxp, C.POINTER(abi.Particles), C.POINTER(abi.StatsSpec),
+                                    C.POINTER(abi.StatsSums)]
     L.ptg_histogram.restype = st
     L.ptg_histogram.argtypes = [ctxp, C.POINTER(abi.Particles), C.POINTER(abi.HgramSpec), C.POINTER(abi.HgramInfo),
                                 DP, C.c_uint64]
@@ -328,6 +331,13 @@ class Engine:
         self._check(self.L.ptg_histogram(self._h, C.byref(view), C.byref(spec), C.byref(info), _dp(counts),
                                          info.n_counts))
         return _hgram_info(info), counts
+
+    def particle_sums(self, particles, spec):
+        """The sums behind a summary statistic (ptg_particle_sums)."""
+        view = particles if isinstance(particles, abi.Particles) else self._device_view(particles)
+        out = abi.StatsSums()
+        self._check(self.L.ptg_particle_sums(self._h, C.byref(view), C.byref(spec), C.byref(out)))
+        return out.as_dict()
 
     # -- beam builder ------------------------------------------------------
     def build_beam(self, desc, n, seed, first_id=0, device=None):

@@ -218,14 +218,14 @@ def rust_exp_upper(x, width=20):
     return rust_exp(x).replace("e", "E").rjust(width)
 
 
-def rust_exp(x):
-    """Rust's `{:.9e}` for an f64: 9 digits after the point, exponent with
-    no sign for positive powers and no padding."""
+def rust_exp(x, digits=9):
+    """Rust's `{:.9e}` (or another precision) for an f64: the digits after
+    the point, an exponent with no sign for positive powers and no padding."""
     if math.isnan(x):
         return "NaN"
     if math.isinf(x):
         return "inf" if x > 0 else "-inf"
-    m, e = ("%.9e" % x).split("e")
+    m, e = ("%.*e" % (digits, x)).split("e")
     return "%se%d" % (m, int(e))
 
 
@@ -306,3 +306,131 @@ class Histogram:
         with open(filename, "w") as f:
             f.write("\n".join(lines) + "\n")
         return filename
+
+
+# output/stats.rs:19-55
+_REDUCTIONS = {"total": "total", "fraction": "fraction", "frac": "fraction", "mean": "mean", "variance": "variance",
+               "var": "variance", "minimum": "minimum", "min": "minimum", "maximum": "maximum", "max": "maximum",
+               "circmean": "circmean", "cmean": "circmean", "circvariance": "circvar", "cvariance": "circvar",
+               "circvar": "circvar", "cvar": "circvar", "circstd": "circstd", "cstd": "circstd"}
+
+
+class SummaryStatistic:
+    """A summary statistic such as "mean energy", "fraction energy in (1e-13;
+    auto)" or "variance angle_x`weight for energy in (auto; 1e-12)"
+    (SummaryStatistic::load, output/stats.rs:85-262), evaluated on the
+    device (ptg_particle_sums).  Bounds are numbers or "auto"."""
+
+    def __init__(self, spec):
+        err = ValueError("cannot convert %r to a summary statistic" % spec)
+        start, end = spec.find("("), spec.rfind(")")
+        rng = spec[start:end + 1] if start >= 0 and end >= 0 else None
+        words = (spec.replace(rng, "") if rng else spec).split()
+        self.filter = None
+        if len(words) == 5:
+            if words[2] != "for" or words[3] not in FUNCTIONS:
+                raise err
+            self.filter = (words[3],) + FUNCTIONS[words[3]]
+        lo, hi = -math.inf, math.inf
+        if len(words) in (3, 5):
+            if rng is None or words[-1] != "in":
+                raise err
+            parts = ["".join(p.split()) for p in rng[1:-1].split(";")]
+            if len(parts) != 2:
+                raise err
+
+            def num(t, auto):
+                if t == "auto":
+                    return auto
+                try:
+                    return float(t)
+                except ValueError:
+                    raise err
+            lo, hi = num(parts[0], -math.inf), num(parts[1], math.inf)
+        if len(words) not in (2, 3, 5) or words[0] not in _REDUCTIONS:
+            raise err
+        self.op = _REDUCTIONS[words[0]]
+        vw = words[1].split("`")
+        if len(vw) > 2 or vw[0] not in FUNCTIONS or (len(vw) == 2 and vw[1] not in FUNCTIONS):
+            raise err
+        self.var_name, self.weight_name = vw[0], (vw[1] if len(vw) == 2 else "unit")
+        self.var_func, vtype = FUNCTIONS[self.var_name]
+        self.weight_func = FUNCTIONS[self.weight_name][0]
+        if self.op in ("circmean", "circvar", "circstd") and vtype != _ANGLE:
+            raise err
+        unit = UnitSystem.default().unit_of(vtype).name
+        if self.op in ("fraction", "circvar"):
+            unit = "1"
+        elif self.op == "variance":
+            unit = "1" if unit == "1" else "(%s)^2" % unit
+        self.unit = unit
+        if (math.isfinite(lo) or math.isfinite(hi)) and self.filter is None:
+            self.filter = (self.var_name, self.var_func, vtype)
+        ftype = self.filter[2] if self.filter is not None else vtype
+        r = 1.0 / UnitSystem.si().unit_of(ftype).scale  # from_si
+        self.min, self.max = lo * r, hi * r
+        self.filter_unit = UnitSystem.default().unit_of(self.filter[2]).name if self.filter else None
+        self.name, self.value = "", 0.0
+
+    def _spec(self, species, shift=0.0):
+        s = abi.StatsSpec()
+        s.species, s.var_func, s.weight_func = species, self.var_func, self.weight_func
+        s.filter_func = self.filter[1] if self.filter is not None else -1
+        s.min, s.max, s.shift = self.min, self.max, shift
+        return s
+
+    def evaluate(self, engine, particles, species, name):
+        """SummaryStatistic::evaluate (output/stats.rs:412-483)."""
+        self.name = name
+        a = engine.particle_sums(particles, self._spec(species))
+        op = self.op
+        if op == "total":
+            v = a["subtotal"]
+        elif op == "fraction":
+            v = a["subtotal"] / a["total"]
+        elif op == "mean":
+            v = a["subtotal"] / a["count"]
+        elif op == "variance":
+            # shifted by the mean (the reference shifts by the mean of its
+            # first ten particles): the same variance up to rounding
+            m = a["subtotal"] / a["count"] if a["count"] else 0.0
+            b = engine.particle_sums(particles, self._spec(species, m))
+            v = (b["sum_sq_diffs"] - b["sum_diffs"] ** 2 / b["count"]) / b["count"]
+        elif op == "minimum":
+            v = a["minimum"]
+        elif op == "maximum":
+            v = a["maximum"]
+        else:
+            mx, my = a["sum_cos"] / a["count"], a["sum_sin"] / a["count"]
+            if op == "circmean":
+                v = math.atan2(my, mx)
+            elif op == "circvar":
+                v = 1.0 - math.hypot(mx, my)
+            else:
+                v = math.sqrt(-2.0 * math.log(math.hypot(mx, my)))
+        self.value = v
+        return v
+
+    def __str__(self):
+        """impl Display (output/stats.rs:493-516)."""
+        bounds = ""
+        if self.filter is not None:
+            fn, fu = self.filter[0], self.filter_unit
+            if math.isfinite(self.min) and math.isinf(self.max):
+                bounds = " (%s [%s] > %s)" % (fn, fu, rust_exp(self.min, 6))
+            elif math.isinf(self.min) and math.isfinite(self.max):
+                bounds = " (%s [%s] < %s)" % (fn, fu, rust_exp(self.max, 6))
+            else:
+                bounds = " (%s < %s [%s] < %s)" % (rust_exp(self.min, 6), fn, fu, rust_exp(self.max, 6))
+        wstr = " (%s-weighted)" % self.weight_name if self.weight_name != "unit" else ""
+        return "%s: %s %s%s%s = %s [%s]" % (self.name, self.op, self.var_name, wstr, bounds, rust_exp(self.value, 6),
+                                          self.unit)
+
+
+def write_stats(filename, electron=(), positron=(), photon=()):
+    """The stats file of main.rs:1268-1285: electron, then positron, then
+    photon statistics, one per line."""
+    with open(filename, "w") as f:
+        for st in list(electron) + list(positron) + list(photon):
+            f.write(str(st) + "\n")
+    return filename

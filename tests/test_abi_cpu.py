@@ -93,7 +93,7 @@ _LAYOUTS = {
     "QueueCfg": "ptg_queue_cfg", "MlpTrainCfg": "ptg_mlp_train_cfg", "MlpTrainStats": "ptg_mlp_train_stats",
     "SamplerBenchCfg": "ptg_sampler_bench_cfg", "SamplerBenchStats": "ptg_sampler_bench_stats",
     "SamplerBenchDetail": "ptg_sampler_bench_detail", "BeamDesc": "ptg_beam_desc", "HgramSpec": "ptg_hgram_spec",
-    "HgramInfo": "ptg_hgram_info",
+    "HgramInfo": "ptg_hgram_info", "StatsSpec": "ptg_stats_spec", "StatsSums": "ptg_stats_sums",
 }
 
 

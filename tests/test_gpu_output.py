@@ -109,3 +109,32 @@ def test_empty_species_gives_no_histogram(eng, shower):
         if not np.any(shower["species"] == abi.POSITRON) else (None, None)
     if info is not None:
         assert info["empty"] and cts is None
+
+
+STATS = [
+    ("mean energy", abi.PHOTON), ("total energy`weight", abi.PHOTON), ("fraction energy in (1.602177e-11; auto)", abi.PHOTON),
+    ("variance angle_x", abi.ELECTRON), ("variance energy`weight for theta in (auto; 1e-3)", abi.PHOTON),
+    ("min gamma", abi.ELECTRON), ("max gamma", abi.ELECTRON), ("circmean angle_y", abi.PHOTON),
+    ("circvar theta", abi.PHOTON), ("cstd angle_x", abi.ELECTRON), ("mean S1`weight", abi.PHOTON),
+    ("mean pol_x", abi.PHOTON),
+]
+
+
+@pytest.mark.parametrize("spec,species", STATS)
+def test_device_statistics_match_restatement(eng, shower, spec, species):
+    from oracle import hgram
+    from ptarmigan_gb300.output import SummaryStatistic
+    st = SummaryStatistic(spec)
+    got = st.evaluate(eng, _device(shower), species, "photon" if species == abi.PHOTON else "electron")
+    ff = st.filter[1] if st.filter else -1
+    want = hgram.summary(shower, species, st.op, st.var_func, st.weight_func, ff, st.min, st.max)
+    if st.op == "circvar":
+        # 1 - R with R near 1: an absolute comparison of the resultant length
+        assert abs(got - want) < 1e-13, (spec, got, want)
+    elif st.op == "circstd":
+        # sqrt(-2 ln R): compare -2 ln R, which the rounding of R moves by ~1e-16
+        assert abs(got ** 2 - want ** 2) < 2e-13, (spec, got, want)
+    else:
+        assert got == pytest.approx(want, rel=1e-9, abs=1e-15), (spec, got, want)
+    line = str(st)
+    assert line.startswith(st.name + ": " + st.op + " ") and line.endswith("[%s]" % st.unit)

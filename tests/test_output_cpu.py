@@ -98,3 +98,22 @@ def test_fits_layout(tmp_path):
     assert "END" + " " * 77 in cards
     data = np.frombuffer(raw[2880:2880 + 48], dtype=">f8")
     assert np.array_equal(data, cts) and raw[2880 + 48:] == b"\0" * (2880 - 48)
+
+
+def test_summary_statistic_display(tmp_path):
+    from ptarmigan_gb300.output import SummaryStatistic, write_stats
+    st = SummaryStatistic("fraction energy in (1.602177e-13; auto)")
+    st.name, st.value = "electron", 0.561
+    assert str(st) == "electron: fraction energy (energy [MeV] > 1.000000e0) = 5.610000e-1 [1]"
+    st = SummaryStatistic("mean energy`weight for r_perp in (1e-3; 2e-3)")
+    st.name, st.value = "photon", 1000.0
+    assert str(st) == ("photon: mean energy (weight-weighted) (1.000000e-3 < r_perp [1] < 2.000000e-3) "
+                       "= 1.000000e3 [MeV]")
+    st2 = SummaryStatistic("variance x")
+    st2.name, st2.value = "positron", 2.5e-12
+    assert str(st2) == "positron: variance x = 2.500000e-12 [(m)^2]"
+    path = write_stats(str(tmp_path / "stats.txt"), electron=[], positron=[st2], photon=[st])
+    assert open(path).read().splitlines()[0].startswith("positron: variance x")
+    for bad in ("median energy", "mean nonsense", "circmean energy", "mean energy in 1, 2"):
+        with pytest.raises(ValueError):
+            SummaryStatistic(bad)
