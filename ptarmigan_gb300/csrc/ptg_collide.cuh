@@ -73,6 +73,10 @@ struct WaveArgs {
     unsigned long long seed;
     unsigned long long lo, hi;     // wave = store slots [lo, hi)
     unsigned long long n_primaries, id_base;
+    // processing order of the wave's slots (offsets from lo), or NULL for
+    // slot order; the results do not depend on it (streams are fixed per
+    // particle), only how coherently the lanes of a warp step
+    const unsigned long long* order;
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -412,8 +416,10 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
 }
 
 __device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
-    unsigned long long i = a.lo + atomicAdd(&a.c->next, 1ull);
+    unsigned long long k = atomicAdd(&a.c->next, 1ull);
+    unsigned long long i = a.lo + k;
     if (i >= a.hi) return false;
+    if (a.order) i = a.lo + a.order[k];
     const Store& s = a.s;
     L.slot = i;
     L.r = get4(s.r, s.cap, i);

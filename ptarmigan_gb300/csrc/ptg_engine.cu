@@ -85,6 +85,13 @@ struct ptg_ctx {
     unsigned long long* d_qfirst = nullptr;
     unsigned long long* d_qout = nullptr;  // [q_cap + 1] output offsets
     unsigned long long* d_qcursor = nullptr;
+    // wave ordering by laser phase: slot permutation and bucket counters
+    unsigned long long* d_order = nullptr;
+    unsigned long long order_cap = 0;
+    unsigned* d_buckets = nullptr;   // counts, then offsets
+    unsigned* h_buckets = nullptr;   // pinned
+    double* d_phase_mm = nullptr;    // per-block min/max
+    double* h_phase_mm = nullptr;    // pinned
     CollParams* h_coll = nullptr;
     CollStats* h_cstats = nullptr;
     unsigned long long* h_qoff = nullptr;
@@ -674,6 +681,8 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     cudaFree(c->dbpool);
     cudaFree(c->mlp_p), cudaFree(c->mlp_m), cudaFree(c->mlp_v), cudaFree(c->mlp_partial), cudaFree(c->mlp_loss);
     cudaFree(c->mlp_bf);
+    cudaFree(c->d_order), cudaFree(c->d_buckets), cudaFree(c->d_phase_mm);
+    cudaFreeHost(c->h_buckets), cudaFreeHost(c->h_phase_mm);
     if (c->q_graph) cudaGraphExecDestroy(c->q_graph);
     cudaFree(c->d_coll);
     cudaFree(c->d_cstats);
@@ -884,6 +893,116 @@ static void fill_step_options(const ptg_collide_options& o, StepOptions* so) {
     so->keep_decayed = o.keep_decayed_photons;
 }
 
+// ----------------------------------------------------- wave ordering ---
+// A wave's lanes take particles in order of their laser phase k (t - z)
+// (furthest from the pulse first): the lanes of a warp then enter and leave
+// the pulse together, so the field evaluations and emission steps run with
+// full warps, and the longest trajectories start first.  A counting sort
+// over WAVE_BUCKETS phase buckets.
+constexpr int WAVE_BUCKETS = 4096;
+constexpr int WAVE_ORDER_BLOCKS = 256;
+constexpr unsigned long long WAVE_ORDER_MIN = 2048;  // smaller waves run in slot order
+
+// t - z of particle k of the range: store slots lo + k (component-major),
+// or, with rows != NULL, row-major input rows lo + k.
+struct WaveKeys {
+    Store s;
+    const double* rows;
+    __device__ __forceinline__ double key(unsigned long long i) const {
+        return rows ? rows[4 * i] - rows[4 * i + 3] : s.r[0 * s.cap + i] - s.r[3 * s.cap + i];
+    }
+};
+
+__global__ void k_wave_key_range(WaveKeys s, unsigned long long lo, unsigned long long n, double* mm) {
+    __shared__ double smin[256], smax[256];
+    double mn = HUGE_VAL, mx = -HUGE_VAL;
+    for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+         k += (unsigned long long)gridDim.x * blockDim.x) {
+        double v = s.key(lo + k);
+        mn = fmin(mn, v), mx = fmax(mx, v);
+    }
+    smin[threadIdx.x] = mn, smax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) mm[2 * blockIdx.x] = smin[0], mm[2 * blockIdx.x + 1] = smax[0];
+}
+
+__device__ __forceinline__ int wave_bucket(double v, double mn, double inv_width) {
+    double b = (v - mn) * inv_width;  // NaN keys go to bucket 0
+    return b > 0.0 ? (b < (double)(WAVE_BUCKETS - 1) ? (int)b : WAVE_BUCKETS - 1) : 0;
+}
+
+__global__ void k_wave_bucket_count(WaveKeys s, unsigned long long lo, unsigned long long n, double mn,
+                                    double inv_width, unsigned* counts) {
+    unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(&counts[wave_bucket(s.key(lo + k), mn, inv_width)], 1u);
+}
+
+__global__ void k_wave_bucket_scatter(WaveKeys s, unsigned long long lo, unsigned long long n, double mn,
+                                      double inv_width, unsigned* offsets, unsigned long long* order) {
+    unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned pos = atomicAdd(&offsets[wave_bucket(s.key(lo + k), mn, inv_width)], 1u);
+    order[pos] = k;
+}
+
+// Fills c->d_order for slots [lo, hi) (synchronises the stream).  Returns
+// false if the wave keeps slot order.
+static bool order_wave(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, unsigned long long hi) {
+    unsigned long long n = hi - lo;
+    if (n < WAVE_ORDER_MIN || n > 0xffffffffull) return false;
+    if (!c->d_buckets) {
+        if (cudaMalloc(&c->d_buckets, 4 * WAVE_BUCKETS) != cudaSuccess ||
+            cudaMallocHost(&c->h_buckets, 4 * WAVE_BUCKETS) != cudaSuccess ||
+            cudaMalloc(&c->d_phase_mm, 16 * WAVE_ORDER_BLOCKS) != cudaSuccess ||
+            cudaMallocHost(&c->h_phase_mm, 16 * WAVE_ORDER_BLOCKS) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    if (c->order_cap < n) {
+        cudaFree(c->d_order);
+        c->d_order = nullptr;
+        c->order_cap = 0;
+        if (cudaMalloc(&c->d_order, 8 * n) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        c->order_cap = n;
+    }
+    cudaStream_t st = c->stream;
+    k_wave_key_range<<<WAVE_ORDER_BLOCKS, 256, 0, st>>>(s, lo, n, c->d_phase_mm);
+    if (cudaMemcpyAsync(c->h_phase_mm, c->d_phase_mm, 16 * WAVE_ORDER_BLOCKS, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return false;
+    double mn = HUGE_VAL, mx = -HUGE_VAL;
+    for (int b = 0; b < WAVE_ORDER_BLOCKS; ++b) mn = std::min(mn, c->h_phase_mm[2 * b]), mx = std::max(mx, c->h_phase_mm[2 * b + 1]);
+    if (!(mx > mn) || !std::isfinite(mx - mn)) return false;
+    double inv_width = (double)WAVE_BUCKETS / (mx - mn);
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    cudaMemsetAsync(c->d_buckets, 0, 4 * WAVE_BUCKETS, st);
+    k_wave_bucket_count<<<blocks, 256, 0, st>>>(s, lo, n, mn, inv_width, c->d_buckets);
+    if (cudaMemcpyAsync(c->h_buckets, c->d_buckets, 4 * WAVE_BUCKETS, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return false;
+    unsigned acc = 0;
+    for (int b = 0; b < WAVE_BUCKETS; ++b) {
+        unsigned v = c->h_buckets[b];
+        c->h_buckets[b] = acc;
+        acc += v;
+    }
+    cudaMemcpyAsync(c->d_buckets, c->h_buckets, 4 * WAVE_BUCKETS, cudaMemcpyHostToDevice, st);
+    k_wave_bucket_scatter<<<blocks, 256, 0, st>>>(s, lo, n, mn, inv_width, c->d_buckets, c->d_order);
+    return cudaGetLastError() == cudaSuccess;
+}
+
 // Runs a batch whose primaries are described by device pointers `d_in`.
 static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_collide_options* o,
                             const ptg_particles* d_in, uint64_t seed, uint64_t id_base, ptg_run_stats* stats) {
@@ -937,6 +1056,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
         while (lo < hi) {
             a.lo = lo;
             a.hi = hi;
+            a.order = order_wave(c, WaveKeys{c->s, nullptr}, lo, hi) ? c->d_order : nullptr;
             CUDA_TRY(cudaMemsetAsync(&c->counters->next, 0, 8, c->stream));
             CUDA_TRY(launch_wave_model(c, a));
             ++waves;
@@ -1360,6 +1480,11 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         q.base.f = c->h_coll[0].f;
         q.base.seed = c->h_coll[0].seed;
         q.base.id_base = c->h_coll[0].id_base;
+        // primaries in order of laser phase, from the input rows (before the
+        // captured sequence loads them)
+        q.base.order = order_wave(c, WaveKeys{Store{}, d_in->r}, coll[0].first, coll[0].first + coll[0].count)
+                           ? c->d_order
+                           : nullptr;
     }
     fill_step_options(*o, &q.base.o);
     if (variant == 2) q.base.o.dt = c->h_coll[0].dt;
@@ -1399,11 +1524,12 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         if (qc.use_graph) {
             char key[512];
             std::snprintf(key, sizeof key, "%llu/%zu/%llu/%llu/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%d/%p/%d", n, n_coll,
-                          c->s.cap, c->out_cap, grid, variant * 8 + (model + 1), qc.chunk, (void*)d_in->species,
-                          (void*)d_in->r,
+                          c->s.cap, c->out_cap, grid, variant * 8 + (model + 1) + (q.base.order ? 64 : 0), qc.chunk,
+                          (void*)d_in->species, (void*)d_in->r,
                           (void*)d_in->u, (void*)d_in->pol, (void*)d_in->weight, (void*)d_in->id, (void*)d_in->r0,
                           (void*)d_in->u0, q.base.db_cap, (void*)q.base.dbw, (int)sizeof(StepOptions));
             std::string k = key;
+            k.append((const char*)&q.base.order, sizeof(q.base.order));  // captured by value in the launch
             k.append((const char*)&q.base.o, sizeof(StepOptions));
             k.append((const char*)&fa.min_energy, 2 * sizeof(double));
             k.append((const char*)&fa.discard_bg_e, 3 * sizeof(int));
@@ -1543,12 +1669,16 @@ ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* co
     if (!c || !coll || !o || !d_primaries) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!(sample_fraction > 0.0 && sample_fraction <= 1.0))
         return set_err(PTG_ERR_INVALID_ARGUMENT, "sample_fraction must lie in (0, 1]");
+    CUDA_TRY(cudaSetDevice(c->device));
+    // a single collision's sample fills every lane the kernel can hold twice
+    // over, so that the shapes are compared at the occupancy they will run
+    // at; several collisions run side by side and fill the device together
+    uint64_t floor_count = n_coll == 1 ? 2ull * (uint64_t)c->num_sms * 3ull * 128ull : 1ull;
     std::vector<ptg_collision> sample(coll, coll + n_coll);
     for (auto& s : sample) {
         uint64_t m = (uint64_t)std::ceil(sample_fraction * (double)s.count);
-        s.count = std::min<uint64_t>(s.count, std::max<uint64_t>(m, 1));
+        s.count = std::min<uint64_t>(s.count, std::max<uint64_t>(m, floor_count));
     }
-    CUDA_TRY(cudaSetDevice(c->device));
     // the single-collision variant is a candidate for a batch of one
     double dt_max;
     int model = make_field(coll[0].laser, &dt_max).model;
@@ -1561,7 +1691,7 @@ ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* co
     std::vector<ptg_queue_cfg> cands;
     for (int v = 0; v < n_var; ++v)
         for (int bps : {occ[v], occ[v] > 1 ? occ[v] - 1 : 0})
-            for (int chunk : {1, 2, 4})
+            for (int chunk : {1, 2})
                 if (bps > 0) cands.push_back(ptg_queue_cfg{v, bps, chunk, 1});
     double best_t = 1e300;
     ptg_queue_cfg best_c = c->qcfg;

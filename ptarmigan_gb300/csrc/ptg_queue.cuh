@@ -296,7 +296,10 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
                 holding = true;
                 wait_from = global_ns();
             }
-            int w = (leptons && ticket >= a.n_primaries) ? POLL_NOT_YET : poll_slot(a, ticket);
+            // primaries in the batch's order of laser phase (a.order), the
+            // rest in ticket order
+            unsigned long long slot = (a.order && ticket < a.n_primaries) ? a.order[ticket] : ticket;
+            int w = (leptons && ticket >= a.n_primaries) ? POLL_NOT_YET : poll_slot(a, slot);
             if (w == WAIT_DRAINED) {
                 finished = true;
             } else if (w == WAIT_SKIP) {
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
                 }
             } else {
                 holding = false;
-                queue_load(a, L, ticket);
+                queue_load(a, L, slot);
                 if (L.status == ST_PHANTOM || L.coll != 0) {
                     if (L.status != ST_PHANTOM) atomicAdd(&a.c->errors, 1ull);
                     __threadfence();
