@@ -945,18 +945,70 @@ __global__ void k_wave_bucket_count(WaveKeys s, unsigned long long lo, unsigned 
 }
 
 __global__ void k_wave_bucket_scatter(WaveKeys s, unsigned long long lo, unsigned long long n, double mn,
-                                      double inv_width, unsigned* offsets, unsigned long long* order) {
+                                      double inv_width, unsigned* offsets, unsigned long long* order,
+                                      unsigned long long base) {
     unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned pos = atomicAdd(&offsets[wave_bucket(s.key(lo + k), mn, inv_width)], 1u);
-    order[pos] = k;
+    order[pos] = base + k;
 }
 
-// Fills c->d_order for slots [lo, hi) (synchronises the stream).  Returns
-// false if the wave keeps slot order.
+__global__ void k_iota(unsigned long long* out, unsigned long long n) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = i;
+}
+
+static bool order_range(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, unsigned long long hi,
+                        unsigned long long* out, unsigned long long base);
+
+static bool ensure_order(ptg_ctx* c, unsigned long long n) {
+    if (c->order_cap >= n) return true;
+    cudaFree(c->d_order);
+    c->d_order = nullptr;
+    c->order_cap = 0;
+    if (cudaMalloc(&c->d_order, 8 * n) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    c->order_cap = n;
+    return true;
+}
+
+// Fills c->d_order for slots [lo, hi) with offsets from lo (synchronises
+// the stream).  Returns false if the wave keeps slot order.
 static bool order_wave(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, unsigned long long hi) {
     unsigned long long n = hi - lo;
     if (n < WAVE_ORDER_MIN || n > 0xffffffffull) return false;
+    if (!ensure_order(c, n)) return false;
+    return order_range(c, s, lo, hi, c->d_order, 0);
+}
+
+// A batch of collisions whose primaries fill slots [off_k, off_k + count_k)
+// from input rows [first_k, ...): c->d_order maps ticket t < n to a slot,
+// each collision's primaries in order of laser phase (collisions too small
+// to sort keep slot order).  Returns false if the batch keeps slot order.
+static bool order_collisions(ptg_ctx* c, const double* rows, size_t n_coll, const ptg_collision* coll,
+                             const unsigned long long* off, unsigned long long n) {
+    bool any = false;
+    for (size_t k = 0; k < n_coll; ++k) any = any || coll[k].count >= WAVE_ORDER_MIN;
+    if (!any || n > 0xffffffffull || !ensure_order(c, n)) return false;
+    k_iota<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_order, n);
+    for (size_t k = 0; k < n_coll; ++k) {
+        if (coll[k].count < WAVE_ORDER_MIN) continue;
+        if (!order_range(c, WaveKeys{Store{}, rows}, coll[k].first, coll[k].first + coll[k].count,
+                         c->d_order + off[k], off[k])) {
+            // that collision keeps slot order
+            k_iota<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_order, n);
+            return false;
+        }
+    }
+    return cudaGetLastError() == cudaSuccess;
+}
+
+// The counting sort of [lo, hi) into out[0, hi - lo) = base + offset.
+static bool order_range(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, unsigned long long hi,
+                        unsigned long long* out, unsigned long long base) {
+    unsigned long long n = hi - lo;
     if (!c->d_buckets) {
         if (cudaMalloc(&c->d_buckets, 4 * WAVE_BUCKETS) != cudaSuccess ||
             cudaMallocHost(&c->h_buckets, 4 * WAVE_BUCKETS) != cudaSuccess ||
@@ -965,16 +1017,6 @@ static bool order_wave(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, uns
             cudaGetLastError();
             return false;
         }
-    }
-    if (c->order_cap < n) {
-        cudaFree(c->d_order);
-        c->d_order = nullptr;
-        c->order_cap = 0;
-        if (cudaMalloc(&c->d_order, 8 * n) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        c->order_cap = n;
     }
     cudaStream_t st = c->stream;
     k_wave_key_range<<<WAVE_ORDER_BLOCKS, 256, 0, st>>>(s, lo, n, c->d_phase_mm);
@@ -999,7 +1041,7 @@ static bool order_wave(ptg_ctx* c, const WaveKeys& s, unsigned long long lo, uns
         acc += v;
     }
     cudaMemcpyAsync(c->d_buckets, c->h_buckets, 4 * WAVE_BUCKETS, cudaMemcpyHostToDevice, st);
-    k_wave_bucket_scatter<<<blocks, 256, 0, st>>>(s, lo, n, mn, inv_width, c->d_buckets, c->d_order);
+    k_wave_bucket_scatter<<<blocks, 256, 0, st>>>(s, lo, n, mn, inv_width, c->d_buckets, out, base);
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -1482,10 +1524,10 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         q.base.id_base = c->h_coll[0].id_base;
         // primaries in order of laser phase, from the input rows (before the
         // captured sequence loads them)
-        q.base.order = order_wave(c, WaveKeys{Store{}, d_in->r}, coll[0].first, coll[0].first + coll[0].count)
-                           ? c->d_order
-                           : nullptr;
     }
+    // primaries in order of laser phase within each collision, from the
+    // input rows (before the captured sequence loads them)
+    q.base.order = order_collisions(c, d_in->r, n_coll, coll, c->h_qoff, n) ? c->d_order : nullptr;
     fill_step_options(*o, &q.base.o);
     if (variant == 2) q.base.o.dt = c->h_coll[0].dt;
     q.base.gl = c->gl;

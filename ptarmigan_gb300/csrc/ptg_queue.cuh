@@ -239,7 +239,9 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
             t_end = t + (unsigned long long)q.chunk;
         }
         unsigned long long ticket = t++;
-        int w = wait_slot(a, ticket, q.wait_ns);
+        // primaries in each collision's order of laser phase (a.order)
+        unsigned long long slot = (a.order && ticket < a.n_primaries) ? a.order[ticket] : ticket;
+        int w = wait_slot(a, slot, q.wait_ns);
         if (w == WAIT_DRAINED) break;
         if (w == WAIT_TIMEOUT) {
             atomicAdd(&a.c->timeouts, 1ull);
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
         }
         if (w == WAIT_SKIP) continue;
         Lane L;
-        queue_load(a, L, ticket);
+        queue_load(a, L, slot);
         if (!queue_begin(q, a, L, cur)) continue;
         PartCounts pc{0, 0, 0, 0, 0};
         switch (a.f.model) {
