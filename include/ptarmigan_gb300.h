@@ -354,7 +354,8 @@ typedef struct {
 
 typedef struct {
     double plain_ms, learned_ms;            /* device times of the two samplers */
-    double features_ms, infer_ms;           /* the learned path's inputs and batched inference */
+    double features_ms;                     /* the emissions' (a, eta, n) and the network's inputs: shared */
+    double infer_ms;                        /* the learned path's batched inference */
     double plain_evals, learned_evals;      /* spectrum evaluations per emission */
     double acceptance;                      /* accepted / proposed under the learned envelope */
     uint64_t fallbacks;                     /* envelope under the spectrum: the reference's sampler took over */

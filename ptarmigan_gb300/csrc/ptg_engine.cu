@@ -2718,16 +2718,17 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
     for (auto& ev : e) cudaEventCreate(&ev);
     cudaStream_t s = c->stream;
     cudaError_t err = cudaSuccess;
-    // plain: the reference's ceiling and rejection
+    // the emissions' points (a, eta, n) and the network's inputs: shared
     cudaEventRecord(e[0], s);
-    err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
-                             nullptr, cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
+    err = launch_sampler_features(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, dx, dpts,
+                                  s);
     cudaEventRecord(e[1], s);
-    // learned: features, batched tensor-core inference, then sampling
+    // plain: the reference's ceiling and rejection
     if (err == cudaSuccess)
-        err = launch_sampler_features(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, dx,
-                                      dpts, s);
+        err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 0, nullptr,
+                                 dpts, cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
     cudaEventRecord(e[2], s);
+    // learned: batched tensor-core inference, then sampling
     if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), dx, n, denv, s);
     cudaEventRecord(e[3], s);
     if (err == cudaSuccess)
@@ -2758,8 +2759,8 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
         err = cudaGetLastError();
     }
     float t_plain = 0, t_feat = 0, t_inf = 0, t_learn = 0;
-    cudaEventElapsedTime(&t_plain, e[0], e[1]);
-    cudaEventElapsedTime(&t_feat, e[1], e[2]);
+    cudaEventElapsedTime(&t_feat, e[0], e[1]);
+    cudaEventElapsedTime(&t_plain, e[1], e[2]);
     cudaEventElapsedTime(&t_inf, e[2], e[3]);
     cudaEventElapsedTime(&t_learn, e[3], e[4]);
     for (auto& ev : e) cudaEventDestroy(ev);

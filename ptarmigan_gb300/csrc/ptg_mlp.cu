@@ -474,8 +474,8 @@ struct BenchPoint {
     int n, pad;
 };
 
-// The learned path's first pass: the point of every emission and the
-// network's inputs for it.
+// The first pass, shared by both samplers: the point of every emission, and
+// the network's inputs for it.
 __global__ void k_sampler_features(const LmaTables* t, unsigned long long n, unsigned long long seed, double a_lo,
                                    double a_hi, double e_lo, double e_hi, float* x_out, BenchPoint* pts) {
     unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
@@ -532,12 +532,8 @@ __global__ void __launch_bounds__(128) k_sampler_run(const LmaTables* t, unsigne
                 if (i >= n) {
                     phase = SB_DONE;
                 } else {
-                    if (LEARNED) {
-                        BenchPoint p = pts[i];
-                        a = p.a, eta = p.eta, nh = p.n;
-                    } else {
-                        bench_point(nt, i, seed, a_lo, a_hi, e_lo, e_hi, &a, &eta, &nh);
-                    }
+                    BenchPoint p = pts[i];
+                    a = p.a, eta = p.eta, nh = p.n;
                     rng.begin(seed ^ 0x9E3779B97F4A7C15ull, mix64(i), LEARNED ? 2 : 1);
                     evals = fb = trials = 0;
                     k = 0;
@@ -680,7 +676,7 @@ cudaError_t launch_sampler_run(const LmaTables* t, unsigned long long n, unsigne
                                double a_hi, double e_lo, double e_hi, int learned, const float* env, const void* pts,
                                float margin, unsigned long long* counter, double* v_out, unsigned* evals,
                                unsigned* fallbacks, int* status, cudaStream_t s) {
-    if (learned && (!env || !pts)) return cudaErrorInvalidValue;
+    if (!pts || (learned && !env)) return cudaErrorInvalidValue;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
