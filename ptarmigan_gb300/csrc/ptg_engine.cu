@@ -102,6 +102,7 @@ struct ptg_ctx {
     // partials, BF16 weights (w0 w1 w2 w3 t1 t2 t3)
     float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_partial = nullptr, *mlp_loss = nullptr;
     __nv_bfloat16* mlp_bf = nullptr;
+    void* mlp_packed = nullptr;  // weights in fragment order for inference
     int mlp_step = 0;
     bool mlp_ready = false, mlp_enabled = false;
     float mlp_margin = 0.25f;
@@ -681,6 +682,7 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     cudaFree(c->dbpool);
     cudaFree(c->mlp_p), cudaFree(c->mlp_m), cudaFree(c->mlp_v), cudaFree(c->mlp_partial), cudaFree(c->mlp_loss);
     cudaFree(c->mlp_bf);
+    cudaFree(c->mlp_packed);
     cudaFree(c->d_order), cudaFree(c->d_buckets), cudaFree(c->d_phase_mm);
     cudaFreeHost(c->h_buckets), cudaFreeHost(c->h_phase_mm);
     if (c->q_graph) cudaGraphExecDestroy(c->q_graph);
@@ -2472,12 +2474,14 @@ static ptg_status mlp_alloc(ptg_ctx* c) {
     if (cudaMalloc(&c->mlp_p, 4 * np) != cudaSuccess || cudaMalloc(&c->mlp_m, 4 * np) != cudaSuccess ||
         cudaMalloc(&c->mlp_v, 4 * np) != cudaSuccess ||
         cudaMalloc(&c->mlp_partial, 4 * np * MLP_GRAD_BLOCKS) != cudaSuccess ||
-        cudaMalloc(&c->mlp_loss, 4 * MLP_GRAD_BLOCKS) != cudaSuccess || cudaMalloc(&c->mlp_bf, 2 * nbf) != cudaSuccess) {
+        cudaMalloc(&c->mlp_loss, 4 * MLP_GRAD_BLOCKS) != cudaSuccess || cudaMalloc(&c->mlp_bf, 2 * nbf) != cudaSuccess ||
+        cudaMalloc(&c->mlp_packed, mlp_packed_bytes()) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(c->mlp_p), cudaFree(c->mlp_m), cudaFree(c->mlp_v), cudaFree(c->mlp_partial), cudaFree(c->mlp_loss);
-        cudaFree(c->mlp_bf);
+        cudaFree(c->mlp_bf), cudaFree(c->mlp_packed);
         c->mlp_p = c->mlp_m = c->mlp_v = c->mlp_partial = c->mlp_loss = nullptr;
         c->mlp_bf = nullptr;
+        c->mlp_packed = nullptr;
         return set_err(PTG_ERR_ALLOC, "learned-proposal buffers");
     }
     CUDA_TRY(cudaMemset(c->mlp_bf, 0, 2 * nbf));
@@ -2598,7 +2602,7 @@ ptg_status ptg_mlp_infer(ptg_ctx* c, const float* x, size_t n, float* out) {
         return set_err(PTG_ERR_ALLOC, "inference buffers");
     }
     cudaMemcpy(dx, x, 4 * MLP_IN * n, cudaMemcpyHostToDevice);
-    cudaError_t e = launch_mlp_infer(mlp_dev(c), dx, n, dout, c->stream);
+    cudaError_t e = launch_mlp_infer(mlp_dev(c), c->mlp_packed, dx, n, dout, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) cudaMemcpy(out, dout, 64 * n, cudaMemcpyDeviceToHost);
     cudaFree(dx), cudaFree(dout);
@@ -2729,7 +2733,7 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
                                  dpts, cfg->margin, ctr, dv0, de0, nullptr, ds0, s);
     cudaEventRecord(e[2], s);
     // learned: batched tensor-core inference, then sampling
-    if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), dx, n, denv, s);
+    if (err == cudaSuccess) err = launch_mlp_infer(mlp_dev(c), c->mlp_packed, dx, n, denv, s);
     cudaEventRecord(e[3], s);
     if (err == cudaSuccess)
         err = launch_sampler_run(c->lma_dev, n, cfg->seed, cfg->a_lo, cfg->a_hi, cfg->eta_lo, cfg->eta_hi, 1, denv,

@@ -38,7 +38,10 @@ cudaError_t launch_regen_lpm_cdf(int npoints, const int* nmin_of, const int* nma
 // The learned CP proposal (ptg_mlp.cu).
 struct MlpDev;
 struct LmaTables;
-cudaError_t launch_mlp_infer(const MlpDev& m, const float* x, unsigned long long n, float* out, cudaStream_t s);
+// Packs the weights into `packed` (mlp_packed_bytes()) and runs the batch.
+cudaError_t launch_mlp_infer(const MlpDev& m, void* packed, const float* x, unsigned long long n, float* out,
+                             cudaStream_t s);
+size_t mlp_packed_bytes();
 cudaError_t launch_mlp_grad(const MlpDev& m, const void* data, unsigned long long first, int rows, float tau,
                             float* partial, float* loss, int blocks, cudaStream_t s);
 cudaError_t launch_mlp_adam(float* p, float* mom, float* vel, const float* partial, int nblocks, float lr, int step,

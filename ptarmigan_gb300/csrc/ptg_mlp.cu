@@ -102,7 +102,7 @@ __device__ __forceinline__ void silu_tiles(const float z[NT][4], float h[NT][4])
 }
 
 __device__ __forceinline__ float dsilu(float z) {
-    float s = 1.0f / (1.0f + __expf(-z));
+    float s = __frcp_rn(1.0f + __expf(-z));
     return s * (1.0f + z * (1.0f - s));
 }
 
@@ -127,28 +127,98 @@ __device__ __forceinline__ void warp_forward(const MlpDev& m, const float x[2][M
     dense<4, 2>(a1, m.w3, MLP_H, m.p + P_B3, f.o);
 }
 
-// Batched inference: out[row][16].
-__global__ void __launch_bounds__(128) k_mlp_infer(MlpDev m, const float* x_in /* [n][MLP_IN] */,
-                                                   unsigned long long n, float* out) {
-    unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
-    unsigned long long r0 = warp * 16;
-    if (r0 >= n) return;
-    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float x[2][MLP_IN];
-    for (int h = 0; h < 2; ++h) {
-        unsigned long long r = r0 + g + 8 * h;
-        for (int i = 0; i < MLP_IN; ++i) x[h][i] = r < n ? x_in[MLP_IN * r + i] : 0.0f;
+// Batched inference.  The weights are first packed in fragment order
+// (k_mlp_pack): for every (k tile, n tile) of a layer, each lane's two
+// 32-bit B fragments side by side, so that a warp reads a tile with one
+// 8-byte load per lane, all 256 bytes contiguous.  Each block stages the
+// packed weights (20 KB) and the biases in shared memory once and its warps
+// then run 16-row tiles in a grid-stride loop.  The products and their
+// order are those of warp_forward, so the outputs are the same bit for bit.
+enum : int {
+    PK_L0 = 0,                   // 1 x 8 tiles
+    PK_L1 = PK_L0 + 1 * 8 * 32,  // 4 x 8 tiles
+    PK_L2 = PK_L1 + 4 * 8 * 32,  // 4 x 8 tiles
+    PK_L3 = PK_L2 + 4 * 8 * 32,  // 4 x 2 tiles
+    PK_TOTAL = PK_L3 + 4 * 2 * 32
+};
+
+__global__ void k_mlp_pack(MlpDev m, uint2* packed) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= PK_TOTAL) return;
+    int lane = idx & 31, tile = idx >> 5;
+    const __nv_bfloat16* W;
+    int ld, nt_count, local;
+    if (idx < PK_L1) {
+        W = m.w0, ld = MLP_IN_PAD, nt_count = 8, local = tile;
+    } else if (idx < PK_L2) {
+        W = m.w1, ld = MLP_H, nt_count = 8, local = tile - PK_L1 / 32;
+    } else if (idx < PK_L3) {
+        W = m.w2, ld = MLP_H, nt_count = 8, local = tile - PK_L2 / 32;
+    } else {
+        W = m.w3, ld = MLP_H, nt_count = 2, local = tile - PK_L3 / 32;
     }
-    WarpFwd f;
-    warp_forward(m, x, f);
-    for (int nt = 0; nt < 2; ++nt)
+    int kt = local / nt_count, nt = local % nt_count;
+    int g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16* p = W + (size_t)(nt * 8 + g) * ld + kt * 16 + 2 * t;
+    packed[idx] = make_uint2(*reinterpret_cast<const uint32_t*>(p), *reinterpret_cast<const uint32_t*>(p + 8));
+}
+
+template <int KT, int NT>
+__device__ __forceinline__ void dense_packed(const uint32_t a[KT][4], const uint2* w, const float* bias,
+                                             float z[NT][4]) {
+    int lane = threadIdx.x & 31, t = lane & 3;
+    for (int nt = 0; nt < NT; ++nt) {
+        float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
+        z[nt][0] = b0, z[nt][1] = b1, z[nt][2] = b0, z[nt][3] = b1;
+        for (int kt = 0; kt < KT; ++kt) {
+            uint2 f = w[(kt * NT + nt) * 32 + lane];
+            uint32_t b[2] = {f.x, f.y};
+            mma_bf16(z[nt], a[kt], b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mlp_infer(const uint2* packed, const float* params,
+                                                   const float* x_in /* [n][MLP_IN] */, unsigned long long n,
+                                                   float* out) {
+    __shared__ uint2 w[PK_TOTAL];
+    __shared__ float bias[3 * MLP_H + MLP_OUT];  // b0, b1, b2, b3 (contiguous in the master vector)
+    for (int k = threadIdx.x; k < PK_TOTAL; k += blockDim.x) w[k] = packed[k];
+    for (int k = threadIdx.x; k < 3 * MLP_H + MLP_OUT; k += blockDim.x) bias[k] = params[P_B0 + k];
+    __syncthreads();
+    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    unsigned long long tiles = (n + 15) / 16;
+    for (unsigned long long tile = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+         tile < tiles; tile += warps) {
+        unsigned long long r0 = tile * 16;
+        float x[2][MLP_IN];
         for (int h = 0; h < 2; ++h) {
             unsigned long long r = r0 + g + 8 * h;
-            if (r < n) {
-                out[r * 16 + nt * 8 + 2 * t] = f.o[nt][2 * h];
-                out[r * 16 + nt * 8 + 2 * t + 1] = f.o[nt][2 * h + 1];
-            }
+            for (int i = 0; i < MLP_IN; ++i) x[h][i] = r < n ? x_in[MLP_IN * r + i] : 0.0f;
         }
+        uint32_t a0[1][4], a1[4][4];
+        float z[8][4], h8[8][4], o[2][4];
+        input_a(x, a0);
+        dense_packed<1, 8>(a0, w + PK_L0, bias, z);
+        silu_tiles<8>(z, h8);
+        to_a<8>(h8, a1);
+        dense_packed<4, 8>(a1, w + PK_L1, bias + MLP_H, z);
+        silu_tiles<8>(z, h8);
+        to_a<8>(h8, a1);
+        dense_packed<4, 8>(a1, w + PK_L2, bias + 2 * MLP_H, z);
+        silu_tiles<8>(z, h8);
+        to_a<8>(h8, a1);
+        dense_packed<4, 2>(a1, w + PK_L3, bias + 3 * MLP_H, o);
+        for (int nt = 0; nt < 2; ++nt)
+            for (int h = 0; h < 2; ++h) {
+                unsigned long long r = r0 + g + 8 * h;
+                if (r < n) {
+                    out[r * 16 + nt * 8 + 2 * t] = o[nt][2 * h];
+                    out[r * 16 + nt * 8 + 2 * t + 1] = o[nt][2 * h + 1];
+                }
+            }
+    }
 }
 
 // Shared-memory staging for the weight gradients of one warp.
@@ -627,9 +697,17 @@ __global__ void __launch_bounds__(128) k_sampler_run(const LmaTables* t, unsigne
 }
 
 // ------------------------------------------------------------ launchers --
-cudaError_t launch_mlp_infer(const MlpDev& m, const float* x, unsigned long long n, float* out, cudaStream_t s) {
-    unsigned long long warps = (n + 15) / 16;
-    k_mlp_infer<<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(m, x, n, out);
+size_t mlp_packed_bytes() { return sizeof(uint2) * PK_TOTAL; }
+
+cudaError_t launch_mlp_infer(const MlpDev& m, void* packed, const float* x, unsigned long long n, float* out,
+                             cudaStream_t s) {
+    k_mlp_pack<<<(PK_TOTAL + 255) / 256, 256, 0, s>>>(m, (uint2*)packed);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned long long tiles = (n + 15) / 16;
+    unsigned long long blocks = std::min<unsigned long long>((tiles + 7) / 8, 4ull * (unsigned long long)std::max(sms, 1));
+    k_mlp_infer<<<(unsigned)std::max<unsigned long long>(blocks, 1), 256, 0, s>>>((const uint2*)packed, m.p, x, n, out);
     return cudaGetLastError();
 }
 

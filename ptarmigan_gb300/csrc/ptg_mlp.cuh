@@ -48,7 +48,9 @@ __host__ __device__ __forceinline__ void mlp_features(double a, double eta, int 
     x[5] = (float)((ln_n - 1.5 * ln_1a2) / 6.0);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU with the fast FP32 exponential and division (the network only
+// shapes a proposal; both are within a few ulp)
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
 // One lane's forward pass in FP32 (CUDA cores); used inside the collision
 // kernels, where emissions arrive one lane at a time.
