@@ -145,7 +145,7 @@ typedef struct {
     uint64_t rejections;       /* rejection-loop iterations */
     uint64_t particle_errors;  /* particles retired with status != PTG_OK */
     uint32_t waves;            /* generations launched */
-    uint32_t reserved;
+    uint32_t ordered_waves;    /* of which put in order of laser phase first (three small kernels each) */
     double absorbed_energy;    /* sum of work over all particles, MeV */
     double device_ms;          /* kernel time of the batch */
 } ptg_run_stats;

@@ -108,7 +108,7 @@ class RunStats(C.Structure):
         ("rejections", C.c_uint64),
         ("particle_errors", C.c_uint64),
         ("waves", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("ordered_waves", C.c_uint32),
         ("absorbed_energy", C.c_double),
         ("device_ms", C.c_double),
     ]

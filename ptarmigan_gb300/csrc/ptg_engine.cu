@@ -1095,12 +1095,13 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
             CUDA_TRY(cudaGetLastError());
         }
         unsigned long long lo = 0, hi = n;
-        uint32_t waves = 0;
+        uint32_t waves = 0, ordered = 0;
         bool overflow = false;
         while (lo < hi) {
             a.lo = lo;
             a.hi = hi;
             a.order = order_wave(c, WaveKeys{c->s, nullptr}, lo, hi) ? c->d_order : nullptr;
+            ordered += a.order ? 1u : 0u;
             CUDA_TRY(cudaMemsetAsync(&c->counters->next, 0, 8, c->stream));
             CUDA_TRY(launch_wave_model(c, a));
             ++waves;
@@ -1155,6 +1156,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
             stats->rejections = c->h_counters->rejections;
             stats->particle_errors = c->h_counters->errors;
             stats->waves = waves;
+            stats->ordered_waves = ordered;
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             stats->device_ms = ms;
