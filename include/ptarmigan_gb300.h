@@ -325,6 +325,12 @@ ptg_status ptg_double_bessel(ptg_ctx* ctx, int32_t n, size_t count, const double
 ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
                          const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
 
+/* The same samples drawn by the warp-cooperative sampler the wave kernel
+ * uses for LP emissions (each warp samples its 32 points in turn, all lanes
+ * together); the results equal ptg_lp_sample's. */
+ptg_status ptg_lp_sample_warp(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
+                              const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
+
 /* --------------------------------------------------- learned proposal ---
  * No reference counterpart: an MLP (six features of a, eta and n; 4 layers
  * of width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the

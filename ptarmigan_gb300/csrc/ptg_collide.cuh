@@ -171,7 +171,8 @@ __device__ __forceinline__ void retire_overflow(const WaveArgs& a, unsigned long
 // One charged-particle step: main.rs:170-206.  Returns false when the
 // particle is finished.
 template <int MODEL, bool QUEUE = false>
-__device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit) {
+__device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit,
+                                            LpDefer* dfr = nullptr) {
     const FieldParams& f = a.f;
     double rqm = (L.species == SP_ELECTRON ? ELECTRON_CHARGE : -ELECTRON_CHARGE) / ELECTRON_MASS;
     double dt = a.o.dt;
@@ -263,7 +264,8 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             dbw.pool = a.dbpool;
         }
         int st = lma_radiate(f, *a.lma, dbw, a.mlp, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr,
-                             &kpol, &a_eff, &chi, &absorption, rej);
+                             &kpol, &a_eff, &chi, &absorption, rej, dfr);
+        if (st == LMA_DEFERRED) return;  // the step repeats once the warp has sampled
         if (st != ST_OK) {
             L.status = st;
             L.r = r;
@@ -454,40 +456,102 @@ __device__ __forceinline__ void lane_store(const WaveArgs& a, Lane& L) {
     s.flags[i] = L.flags;
 }
 
+// This lane's DoubleBessel workspace: slot `lane` of its warp's block of
+// lane-interleaved slots.
+__device__ __forceinline__ DbWork lane_dbw(const WaveArgs& a) {
+    DbWork w{nullptr, 0, 32};
+    if (a.dbw) {
+        size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        w.base = a.dbw + warp * (size_t)a.db_cap * 5 * 32 + lane_id();
+        w.cap = a.db_cap;
+        w.pool = a.dbpool;
+    }
+    return w;
+}
+
+// The LP emission deferred by lane `src` of this warp (`warp_dfr` is the
+// warp's array), sampled by all 32 lanes.
+static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* warp_dfr, int src) {
+    __syncwarp();
+    LpDefer& d = warp_dfr[src];
+    Draws rng = d.rng;
+    int n = 0;
+    double s = 0.0, theta = 0.0;
+    d3 sv = mk3(0.0, 0.0, 0.0);
+    uint32_t rej = 0;
+    int st = lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
+    __syncwarp();
+    if ((int)lane_id() == src) {
+        d.rng = rng;
+        d.n = n, d.s = s, d.theta = theta, d.sv = sv, d.status = st, d.rej = rej;
+        d.pend = 2;
+    }
+    __syncwarp();
+}
+
+// Wave kernel.  With the LMA models in linear polarisation, emissions are
+// sampled by the whole warp (LpDefer): the lanes then loop together, and
+// after every round of steps the warp serves the emissions its lanes left.
 template <int MODEL>
 __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
+    constexpr bool LMA = MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER;
     Lane L;
     uint32_t rej = 0, nemit = 0, npair = 0;
     unsigned long long lsteps = 0, psteps = 0, nerr = 0;
+    LpDefer* dfr = nullptr;
+    if constexpr (LMA) {
+        __shared__ LpDefer s_dfr[128];
+        // uniform over the grid: the kernel's arguments decide
+        if (!a.f.circular && a.dbw != nullptr && !a.o.classical_mode) {
+            dfr = &s_dfr[threadIdx.x];
+            dfr->pend = 0;
+        }
+    }
     bool have = lane_load(a, L);
-    while (have) {
-        bool done;
-        if (L.status != ST_OK || lane_untracked(a, L)) {
-            done = true;
-        } else if (L.species != SP_PHOTON) {
-            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
-            if (!done) {
-                lepton_step<MODEL>(a, L, &rej, &nemit);
-                ++L.step;
-                ++lsteps;
-                done = L.status != ST_OK;
+    for (;;) {
+        if (have) {
+            bool done;
+            if (L.status != ST_OK || lane_untracked(a, L)) {
+                done = true;
+            } else if (L.species != SP_PHOTON) {
+                done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
+                if (!done) {
+                    lepton_step<MODEL>(a, L, &rej, &nemit, dfr);
+                    if (dfr == nullptr || dfr->pend != 1) {
+                        ++L.step;
+                        ++lsteps;
+                        done = L.status != ST_OK;
+                    }
+                }
+            } else {
+                done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) &&
+                         !L.decayed && a.o.tracking_photons);
+                if (!done) {
+                    photon_step<MODEL>(a, L, &rej, &npair);
+                    ++L.step;
+                    ++psteps;
+                    done = L.status != ST_OK;
+                }
             }
-        } else {
-            done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
-                     a.o.tracking_photons);
-            if (!done) {
-                photon_step<MODEL>(a, L, &rej, &npair);
-                ++L.step;
-                ++psteps;
-                done = L.status != ST_OK;
+            if (done) {
+                if (L.status != ST_OK) ++nerr;
+                // a decayed photon leaves the output, or becomes an intermediate
+                if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
+                lane_store(a, L);
+                have = lane_load(a, L);
             }
         }
-        if (done) {
-            if (L.status != ST_OK) ++nerr;
-            // a decayed photon leaves the output, or becomes an intermediate
-            if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
-            lane_store(a, L);
-            have = lane_load(a, L);
+        if (LMA && dfr != nullptr) {
+            __syncwarp();
+            unsigned pending = __ballot_sync(0xffffffffu, have && dfr->pend == 1);
+            while (pending != 0u) {
+                int src = __ffs(pending) - 1;
+                pending &= pending - 1u;
+                lp_defer_serve(a, dfr - lane_id(), src);
+            }
+            if (!__any_sync(0xffffffffu, have)) break;
+        } else if (!have) {
+            break;
         }
     }
     // warp reduction of the counters: one atomic per warp

@@ -437,6 +437,32 @@ __global__ void k_lp_sample(unsigned long long m, int cap, const LmaTables* t, c
     o[0] = n, o[1] = s, o[2] = th, o[3] = 1.0, o[4] = sv.x, o[5] = sv.y, o[6] = sv.z;
 }
 
+// The same samples with lp_sample_warp: each warp samples its 32 points
+// one after another, all lanes together.
+__global__ void k_lp_sample_warp(unsigned long long m, int cap, const LmaTables* t, const double* a,
+                                 const double* eta, unsigned long long seed, const unsigned long long* stream,
+                                 unsigned step, double* ws, double* out7, int* status) {
+    unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+    const unsigned lane = threadIdx.x & 31u;
+    for (unsigned q = 0; q < 32u; ++q) {
+        unsigned long long i = base + q;
+        if (i >= m) break;  // the same for every lane of the warp
+        DbWork w{ws + (base >> 5) * (size_t)cap * 5 * 32 + lane, cap, 32};
+        Draws rng;
+        rng.begin(seed, stream[i], step);
+        int n = 0;
+        double s = 0.0, th = 0.0;
+        d3 sv = mk3(0.0, 0.0, 0.0);
+        uint32_t rej = 0;
+        int st = lp_sample_warp(nlc_view(*t), w, a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
+        if (lane == q) {
+            status[i] = st;
+            double* o = out7 + 7 * i;
+            o[0] = n, o[1] = s, o[2] = th, o[3] = 1.0, o[4] = sv.x, o[5] = sv.y, o[6] = sv.z;
+        }
+    }
+}
+
 // ---------------------------------------------------------- storage -----
 // 5 four-vectors, 5 doubles, 4 u64 and 6 32-bit fields per particle, each
 // array padded to 256 B
@@ -1887,8 +1913,8 @@ ptg_status ptg_double_bessel(ptg_ctx* c, int32_t n, size_t count, const double* 
     return PTG_OK;
 }
 
-ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
-                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+static ptg_status lp_sample_points(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                                   const uint64_t* stream, uint32_t step, double* out7, int32_t* status, bool warp) {
     if (!c || !a || !eta || !stream || !out7 || !status) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     if (count == 0) return PTG_OK;
     if (!c->tables_loaded) {
@@ -1907,10 +1933,24 @@ ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double
         c, {{va.data(), 8 * count}, {ve.data(), 8 * count}, {vs.data(), 8 * count}, {nullptr, lanes * (size_t)cap * 40},
             {out7, 56 * count}, {status, 4 * count}},
         [&](std::vector<void*>& d) {
-            k_lp_sample<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
+            // the workspace holds one slot per lane of ceil(count / 32)
+            // warps; k_lp_sample_warp's warps past the last point stop
+            // before they touch it
+            auto kern = warp ? k_lp_sample_warp : k_lp_sample;
+            kern<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
                 count, cap, c->lma_dev, (double*)d[0], (double*)d[1], seed, (unsigned long long*)d[2], step,
                 (double*)d[3], (double*)d[4], (int*)d[5]);
         });
+}
+
+ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+    return lp_sample_points(c, count, a, eta, seed, stream, step, out7, status, false);
+}
+
+ptg_status ptg_lp_sample_warp(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                              const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+    return lp_sample_points(c, count, a, eta, seed, stream, step, out7, status, true);
 }
 
 ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_par, double* t_perp) {

@@ -40,6 +40,24 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
     return sqrt(-2.0 * log(1.0 - u1)) * cos(2.0 * PI * u2);
 }
 
+// An LP emission sampled by its whole warp (the wave kernel): the lane
+// records the emission's a, eta and draws and abandons the step; the warp
+// samples it with lp_sample_warp; the lane then repeats the step, which
+// reproduces everything up to the sample (same inputs, same draws), and
+// takes the stored sample with the draws as they stood after it.
+struct LpDefer {
+    Draws rng;      // the draws at the sample; after it, once served
+    double a, eta;  // peak amplitude (a sqrt 2) and eta of the emission
+    double s, theta;
+    d3 sv;
+    int n, status;
+    int pend;  // 0: none; 1: waiting for the warp; 2: served
+    uint32_t rej;
+};
+
+// lma_radiate's status for an emission left to the warp
+constexpr int LMA_DEFERRED = 101;
+
 // plane_wave.rs:251-282 / focused_laser.rs:260-281 with
 // nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
 // `dbw` is this lane's DoubleBessel workspace (linear polarisation only).
@@ -47,7 +65,8 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
 static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTables& t, const DbWork& dbw,
                                                const MlpParams& mlp, d4 r, d4 u, double dt, Draws& rng, bool classical,
                                                bool* emitted, d4* k_out, d4* u_prime, d3* pol, double* a_eff,
-                                               double* chi, double* absorption, uint32_t* rej) {
+                                               double* chi, double* absorption, uint32_t* rej,
+                                               LpDefer* dfr = nullptr) {
     *emitted = false;
     double a = sqrt(lma_a_sqd(f, r));
     double chirp = 1.0;
@@ -95,9 +114,22 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
         } else if (f.circular)
             st = classical ? cp_classical_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
                            : cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
-        else
-            st = classical ? lp_classical_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej)
-                           : lp_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
+        else if (classical)
+            st = lp_classical_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
+        else if (dfr == nullptr)
+            st = lp_sample(nt, dbw, aq * SQRT_2, eta, rng, &n, &s, &cphi, &sv, rej);
+        else if (dfr->pend == 2) {
+            n = dfr->n, s = dfr->s, cphi = dfr->theta, sv = dfr->sv, st = dfr->status;
+            *rej += dfr->rej;
+            rng = dfr->rng;
+            dfr->pend = 0;
+        } else {
+            dfr->rng = rng;
+            dfr->a = aq * SQRT_2;
+            dfr->eta = eta;
+            dfr->pend = 1;
+            return LMA_DEFERRED;
+        }
         if (st != 0) return st;
         d4 k;
         st = nlc_kinematics(kappa, u, aq, eta, n, s, cphi, sv, f.pol_angle, classical, &k, pol);

@@ -312,50 +312,79 @@ __device__ __forceinline__ int lp_sum_limit(double a, double eta) {
     return (int)ceil(6.0 * (1.0 + a * a) + 2.0 * pow(a, m));
 }
 
-// nonlinear_compton/lp/mod.rs:53-140
-static __device__ __noinline__ double lp_ceiling(double a, double eta, const DbGeom& g, const DbWork& w) {
-    int n = g.n;
+// nonlinear_compton/lp/mod.rs:53-140: the points (s, theta) at which the
+// ceiling scans the rate, as a plan the scan walks point by point (a lane
+// each in the cooperative sampler).
+struct LpCeilPlan {
+    double smax, theta, x0, x1;
+    int i0, cnt, mode;  // mode 4: n = 1 (two points)
+};
+
+__device__ __forceinline__ void lp_ceiling_plan(double a, double eta, int n, LpCeilPlan* p) {
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
-    double smax = sn / (1.0 + sn);
-    double mx = NAN;
-    double theta = 0.0, x0 = 0.0, x1 = 1.0;  // s = smax * (x0 + (x1 - x0) i / cnt), i = i0..cnt
-    int i0 = 1, cnt = 32;
+    p->smax = sn / (1.0 + sn);
+    p->theta = 0.0, p->x0 = 0.0, p->x1 = 1.0;
+    p->i0 = 1, p->cnt = 32;
     if (n == 1) {
-        mx = rmax(lp_ddpr(a, eta, 0.01 * smax, PI / 2.0, g, w), lp_ddpr(a, eta, 0.99 * smax, PI / 2.0, g, w));
-        return 1.15 * mx;
+        p->mode = 4;
     } else if (a <= 2.0) {
-        x0 = 0.4;
+        p->mode = 0;
     } else if (a <= 5.0) {
         int n_switch = (int)ceil(1.3 * pow(a, 1.2));
         if (n < n_switch) {
-            theta = (PI / 2.0) * (1.0 - log((double)n) / log((double)n_switch));
-            i0 = 0, x0 = 0.0;
+            p->theta = (PI / 2.0) * (1.0 - log((double)n) / log((double)n_switch));
+            p->i0 = 0;
+            p->mode = 2;
         } else {
-            x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.4);
-            cnt = n < lp_sum_limit(a, eta) / 2 ? 32 : 64;
+            p->x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.4);
+            p->cnt = n < lp_sum_limit(a, eta) / 2 ? 32 : 64;
+            p->mode = 3;
         }
     } else {
         int n_switch = (int)ceil(a * a);
         if (n < n_switch) {
             double ns = n_switch;
-            theta = (PI / 2.0) * (pow((double)n, -0.7) - pow(ns, -0.7)) / (1.0 - pow(ns, -0.7));
-            x0 = 0.3, cnt = 64;
+            p->theta = (PI / 2.0) * (pow((double)n, -0.7) - pow(ns, -0.7)) / (1.0 - pow(ns, -0.7));
+            p->cnt = 64;
+            p->mode = 1;
         } else {
-            x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.3);
-            x1 = (1.0 + sn) / (2.0 + sn);
-            cnt = n > 10 * n_switch ? 64 : (n > 3 * n_switch ? 42 : 32);
+            p->x0 = fmax(4.0 * n * eta / (3.0 * a * a + 4.0 * n * eta), 0.3);
+            p->x1 = (1.0 + sn) / (2.0 + sn);
+            p->cnt = n > 10 * n_switch ? 64 : (n > 3 * n_switch ? 42 : 32);
+            p->mode = 3;
         }
     }
-    for (int i = i0; i <= cnt; ++i) {
-        double s;
-        if (a <= 2.0)
-            s = smax * (0.4 + 0.6 * (double)i / 32.0);
-        else if (a > 5.0 && n < (int)ceil(a * a))
-            s = smax * (0.3 + 0.7 * (double)i / 64.0);
-        else if (i0 == 0)
-            s = smax * (double)i / 32.0;
-        else
-            s = smax * (x0 + (x1 - x0) * (double)i / (double)cnt);
+}
+
+__device__ __forceinline__ int lp_ceiling_points(const LpCeilPlan& p) { return p.mode == 4 ? 2 : p.cnt - p.i0 + 1; }
+
+// Point k of the scan (k < lp_ceiling_points).
+__device__ __forceinline__ void lp_ceiling_point(const LpCeilPlan& p, int k, double* s, double* theta) {
+    if (p.mode == 4) {
+        *s = (k == 0 ? 0.01 : 0.99) * p.smax;
+        *theta = PI / 2.0;
+        return;
+    }
+    int i = p.i0 + k;
+    *theta = p.theta;
+    if (p.mode == 0)
+        *s = p.smax * (0.4 + 0.6 * (double)i / 32.0);
+    else if (p.mode == 1)
+        *s = p.smax * (0.3 + 0.7 * (double)i / 64.0);
+    else if (p.mode == 2)
+        *s = p.smax * (double)i / 32.0;
+    else
+        *s = p.smax * (p.x0 + (p.x1 - p.x0) * (double)i / (double)p.cnt);
+}
+
+// The ceiling: 1.15 x the largest rate over the plan's points (NaN-ignoring).
+static __device__ __noinline__ double lp_ceiling(double a, double eta, const DbGeom& g, const DbWork& w) {
+    LpCeilPlan p;
+    lp_ceiling_plan(a, eta, g.n, &p);
+    double mx = NAN;
+    for (int k = 0, np = lp_ceiling_points(p); k < np; ++k) {
+        double s, theta;
+        lp_ceiling_point(p, k, &s, &theta);
         mx = rmax(mx, lp_ddpr(a, eta, s, theta, g, w));
     }
     return 1.15 * mx;
@@ -390,24 +419,27 @@ static __device__ __noinline__ double ln_double_bessel_x_zero(int ni, double y) 
     return log(sqrt(2.0 / (PI * cx_norm(f2)))) + phase.re + log(fabs(cos(phase.im)));
 }
 
-static __device__ __noinline__ void theta_bound(int n, double a, double eta, ThetaBound* tb) {
+// Point i of the 16-point bound on theta as a function of s.
+__device__ __forceinline__ void theta_bound_point(int n, double a, double eta, int i, double* s_i, double* f_i) {
     double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
-    for (int i = 0; i < 16; ++i) {
-        double z = cos(PI * i / 15.0);
-        double si = 0.5 * (z + 1.0) * sn / (1.0 + sn);
-        tb->s[i] = si;
-        double wn = fmin(si / (sn * (1.0 - si)), 1.0);
-        double x = 2.0 * n * a * sqrt(wn * (1.0 - wn)) / sqrt(1.0 + 0.5 * a * a);
-        double y = a * a * si / (8.0 * eta * (1.0 - si));
-        double x_crit = y > n / 6.0 ? 4.0 * sqrt(y) * sqrt(n - 2.0 * y) : n + 2.0 * y;
-        double ln_j_crit = log(0.443) - log((double)n) / 3.0;
-        double ln_j_bdy = ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y);
-        ln_j_bdy = fmin(ln_j_bdy, ln_j_crit);
-        double ct = 1.0 - x_crit * log(0.01) / (x * (ln_j_bdy - ln_j_crit));
-        ct = fmax(ct, -1.0);
-        double fi = acos(ct);
-        tb->f[i] = isnan(fi) ? PI : fi;
-    }
+    double z = cos(PI * i / 15.0);
+    double si = 0.5 * (z + 1.0) * sn / (1.0 + sn);
+    *s_i = si;
+    double wn = fmin(si / (sn * (1.0 - si)), 1.0);
+    double x = 2.0 * n * a * sqrt(wn * (1.0 - wn)) / sqrt(1.0 + 0.5 * a * a);
+    double y = a * a * si / (8.0 * eta * (1.0 - si));
+    double x_crit = y > n / 6.0 ? 4.0 * sqrt(y) * sqrt(n - 2.0 * y) : n + 2.0 * y;
+    double ln_j_crit = log(0.443) - log((double)n) / 3.0;
+    double ln_j_bdy = ln_double_bessel_x_zero(n % 2 == 0 ? n : n + 1, y);
+    ln_j_bdy = fmin(ln_j_bdy, ln_j_crit);
+    double ct = 1.0 - x_crit * log(0.01) / (x * (ln_j_bdy - ln_j_crit));
+    ct = fmax(ct, -1.0);
+    double fi = acos(ct);
+    *f_i = isnan(fi) ? PI : fi;
+}
+
+// The bound made non-increasing in s (the points run from s_max down).
+__device__ __forceinline__ void theta_bound_finish(ThetaBound* tb) {
     double f_min = tb->f[0];
     for (int i = 1; i < 16; ++i) {
         if (tb->f[i] < f_min)
@@ -415,6 +447,11 @@ static __device__ __noinline__ void theta_bound(int n, double a, double eta, The
         else
             tb->f[i] = f_min;
     }
+}
+
+static __device__ __noinline__ void theta_bound(int n, double a, double eta, ThetaBound* tb) {
+    for (int i = 0; i < 16; ++i) theta_bound_point(n, a, eta, i, &tb->s[i], &tb->f[i]);
+    theta_bound_finish(tb);
 }
 
 // nonlinear_compton/lp/linear.rs
@@ -549,6 +586,10 @@ static __device__ __noinline__ int lp_sample(const NlcTables& t, const DbWork& w
     return st;
 }
 
+static __device__ __noinline__ int lp_finish(int n, double a, double eta, double s, double theta, const DbGeom& g,
+                                             const DbWork& w, Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                             d3* sv_out);
+
 // lp_sample for a harmonic whose J(n, x, y) workspace is ready.
 static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork& w, const DbGeom& g, double a,
                                                double eta, Draws& rng, int* n_out, double* s_out, double* theta_out,
@@ -573,6 +614,15 @@ static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork&
     }
     *rej += it;
     if (it == REJECTION_CAP) return 4;  // PTG_ERR_REJECTION_CAP
+    return lp_finish(n, a, eta, s, theta, g, w, rng, n_out, s_out, theta_out, sv_out);
+}
+
+// The accepted (s, theta in [0, pi/2]): the quadrant of the azimuth and the
+// photon's Stokes parameters.
+static __device__ __noinline__ int lp_finish(int n, double a, double eta, double s, double theta, const DbGeom& g,
+                                             const DbWork& w, Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                             d3* sv_out) {
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
     int quadrant = (int)(4.0 * rng.next());
     if (quadrant == 1)
         theta = PI - theta;
@@ -605,6 +655,121 @@ static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork&
     return 0;
 }
 
+
+// Draws held by lane `src`, for every lane of the warp.
+__device__ __forceinline__ Draws shfl_draws(const Draws& d, int src) {
+    const unsigned all = 0xffffffffu;
+    Draws o;
+    o.k0 = __shfl_sync(all, d.k0, src);
+    o.k1 = __shfl_sync(all, d.k1, src);
+    o.s_lo = __shfl_sync(all, d.s_lo, src);
+    o.s_hi = __shfl_sync(all, d.s_hi, src);
+    o.step = __shfl_sync(all, d.step, src);
+    o.block = __shfl_sync(all, d.block, src);
+    for (int q = 0; q < 4; ++q) o.w[q] = __shfl_sync(all, d.w[q], src);
+    o.pos = __shfl_sync(all, d.pos, src);
+    return o;
+}
+
+// lp_sample carried out by all 32 lanes of a converged warp, each with its
+// own DoubleBessel workspace `w`, for one emission whose a, eta and draws
+// every lane holds.  Every lane returns the same result, and it is
+// lp_sample's on the same draws: the ceiling's points are spread over the
+// lanes (the NaN-ignoring max does not depend on the order), and the
+// rejection trials are dealt out in the order the serial sampler draws them
+// (every lane replays the draws, which are cheap next to the rate), so
+// that lane k evaluates the k-th trial that passes the theta bound; the
+// first accepted trial in draw order is taken, with the draws as they stood
+// after it.
+static __device__ __noinline__ int lp_sample_warp(const NlcTables& t, const DbWork& w, double a, double eta,
+                                                  Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                                  d3* sv_out, uint32_t* rej) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
+    if (t.lp_cdf == nullptr || w.base == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = lp_harmonic_index(t, a, eta, rng.next());
+    if (n < 1) return 2;  // PTG_ERR_OUT_OF_TABLE
+    DbGeom g;
+    if (!db_geom(n, w.cap, &g)) {
+        // the harmonic needs a pooled workspace: lane 0 samples alone
+        int st = 0, nn = 0;
+        double s = 0.0, th = 0.0;
+        d3 sv = mk3(0.0, 0.0, 0.0);
+        uint32_t r0 = 0;
+        if (lane == 0) {
+            DbWork wk;
+            int slot = -1;
+            st = db_take(w, n, &wk, &g, &slot);
+            if (st == 0) {
+                st = lp_sample_n(t, wk, g, a, eta, rng, &nn, &s, &th, &sv, &r0);
+                if (slot >= 0) db_pool_release(w.pool, slot);
+            }
+        }
+        __syncwarp();
+        st = __shfl_sync(all, st, 0);
+        *n_out = __shfl_sync(all, nn, 0);
+        *s_out = __shfl_sync(all, s, 0);
+        *theta_out = __shfl_sync(all, th, 0);
+        *sv_out = mk3(__shfl_sync(all, sv.x, 0), __shfl_sync(all, sv.y, 0), __shfl_sync(all, sv.z, 0));
+        *rej += __shfl_sync(all, r0, 0);
+        rng = shfl_draws(rng, 0);
+        return st;
+    }
+    // the bound on theta: point i on lane i
+    ThetaBound tb;
+    {
+        double si = 0.0, fi = 0.0;
+        if (lane < 16) theta_bound_point(n, a, eta, lane, &si, &fi);
+        for (int i = 0; i < 16; ++i) {
+            tb.s[i] = __shfl_sync(all, si, i);
+            tb.f[i] = __shfl_sync(all, fi, i);
+        }
+        theta_bound_finish(&tb);
+    }
+    // the ceiling: its points spread over the lanes
+    LpCeilPlan p;
+    lp_ceiling_plan(a, eta, n, &p);
+    double mx = NAN;
+    for (int k = lane, np = lp_ceiling_points(p); k < np; k += 32) {
+        double s, theta;
+        lp_ceiling_point(p, k, &s, &theta);
+        mx = rmax(mx, lp_ddpr(a, eta, s, theta, g, w));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = rmax(mx, __shfl_xor_sync(all, mx, o));
+    mx = 1.15 * mx;
+    // rejection, 32 trials that pass the theta bound at a time
+    double sn = 2.0 * n * eta / (1.0 + 0.5 * a * a);
+    double smax = sn / (1.0 + sn);
+    Draws r = rng;
+    int it = 0;
+    while (it < REJECTION_CAP) {
+        int my_it = -1;
+        double my_s = 0.0, my_th = 0.0, my_z = 0.0;
+        Draws my_r = r;
+        for (int k = 0; k < 32 && it < REJECTION_CAP; ++it) {
+            double ss = smax * r.next();
+            double th = (PI / 2.0) * r.next();
+            if (th > tb.at(ss)) continue;
+            double z = mx * r.next();
+            if (k == lane) my_it = it, my_s = ss, my_th = th, my_z = z, my_r = r;
+            ++k;
+        }
+        bool acc = my_it >= 0 && my_z < lp_ddpr(a, eta, my_s, my_th, g, w);
+        unsigned m = __ballot_sync(all, acc);
+        if (m != 0u) {
+            int win = __ffs(m) - 1;
+            int acc_it = __shfl_sync(all, my_it, win);
+            double s = __shfl_sync(all, my_s, win);
+            double theta = __shfl_sync(all, my_th, win);
+            rng = shfl_draws(my_r, win);
+            *rej += acc_it;
+            return lp_finish(n, a, eta, s, theta, g, w, rng, n_out, s_out, theta_out, sv_out);
+        }
+    }
+    rng = r;
+    *rej += REJECTION_CAP;
+    return 4;  // PTG_ERR_REJECTION_CAP
+}
 
 // ---------------------------------------------- classical LP emission ----
 // nonlinear_compton/lp/classical.rs:19-40 (v = s / s_max)

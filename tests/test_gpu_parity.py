@@ -374,6 +374,29 @@ def test_lp_sampler_matches_oracle(eng, orc):
     assert mism <= 0.01 * len(a)
 
 
+def test_lp_warp_sampler_equals_serial_sampler(eng):
+    """The warp-cooperative LP sampler returns lp_sample's results bit for
+    bit: same harmonic, (s, theta), Stokes parameters and status, over a
+    range of a (including a > 5, where the ceiling scans 64 points) and
+    eta."""
+    a_vals = [0.3, 0.8, 1.414, 2.5, 4.0, 6.0, 9.0]
+    eta_vals = [2e-3, 0.03, 0.3, 1.0]
+    a, eta, streams = [], [], []
+    for ai in a_vals:
+        for ei in eta_vals:
+            for k in range(40):
+                a.append(ai)
+                eta.append(ei)
+                streams.append(7919 * len(a) + k)
+    a, eta = np.array(a), np.array(eta)
+    streams = np.array(streams, dtype=np.uint64)
+    out_s, st_s = eng.lp_sample(a, eta, 5, streams, 3)
+    out_w, st_w = eng.lp_sample(a, eta, 5, streams, 3, warp=True)
+    assert np.array_equal(st_s, st_w)
+    assert np.count_nonzero(st_s == 0) >= 0.95 * len(a)
+    assert np.array_equal(out_s, out_w)
+
+
 def test_lma_lp_plane_wave_matches_oracle(eng, orc):
     """Linearly polarised plane wave (LMA), emission only, as in the
     plane-wave benchmark: electrons at 5 GeV, a0 = 1."""

@@ -190,3 +190,24 @@ def test_single_collision_queue_matches_wave_path(eng, model):
         assert total_m["particle_errors"] == 0 and len(parts_m) == len(colls_m)
     finally:
         eng.queue_config(variant=0)
+
+
+def test_lp_emissions_warp_sampled_match_serial_sampler(eng):
+    """Linear polarisation, LMA: the wave kernel samples emissions with the
+    whole warp (lp_sample_warp), the queue kernel lane by lane
+    (lp_sample); both give the same particles."""
+    laser = abi.laser_desc(abi.PLANE_WAVE, 1.0, 0.8e-6, abi.LINEAR, abi.COS2, n_cycles=30.0)
+    colls, prim = _batch([(laser, 800, 5.0, 31)])
+    opts = abi.collide_options(tracking_photons=0)
+    eng.queue_config(variant=2, blocks_per_sm=0, chunk=1, use_graph=0)
+    try:
+        parts, stats, total = eng.collide_multi(colls, opts, prim)
+    finally:
+        eng.queue_config(variant=0)
+    c = colls[0]
+    single, sst = eng.collide(c["laser"], opts, prim, seed=c["seed"], id_base=c["id_base"])
+    assert total["particle_errors"] == 0 and sst["particle_errors"] == 0
+    assert sst["emissions"] > 50
+    _compare(parts[0], single, TOL[abi.PLANE_WAVE], 0.02)
+    assert stats[0]["emissions"] == pytest.approx(sst["emissions"], rel=0.03, abs=2)
+    assert stats[0]["lepton_steps"] == pytest.approx(sst["lepton_steps"], rel=0.01)
