@@ -813,11 +813,18 @@ static cudaError_t launch_wave_model(ptg_ctx* c, const WaveArgs& a) {
     int grid = grid_for(c, wave_kernel(a.f.model));
     if (c->grid_cap > 0 && grid > c->grid_cap) grid = c->grid_cap;
     unsigned long long n = a.hi - a.lo;
-    unsigned long long need = (n + c->block - 1) / c->block;
-    if ((unsigned long long)grid > need) grid = (int)need;
+    int threads = 128;
+    if (n < (unsigned long long)grid * 128ull) {
+        // a wave smaller than the resident grid: one-warp blocks, so that
+        // its warps spread over every SM instead of filling the first few
+        // (the same lanes: the workspaces cover grid x 4 warps)
+        threads = 32;
+        grid = (int)std::min<unsigned long long>((n + 31) / 32, (unsigned long long)grid * 4ull);
+    }
     if (grid < 1) grid = 1;
-    if (a.f.model == M_PLANE_WAVE || a.f.model == M_FOCUSED_LASER) return launch_wave_lma(a.f.model, grid, c->stream, a);
-    return launch_wave_lcfa(a.f.model, grid, c->stream, a);
+    if (a.f.model == M_PLANE_WAVE || a.f.model == M_FOCUSED_LASER)
+        return launch_wave_lma(a.f.model, grid, threads, c->stream, a);
+    return launch_wave_lcfa(a.f.model, grid, threads, c->stream, a);
 }
 
 // Linearly polarised LMA emission evaluates J(n, x, y) by recurrence in a
@@ -2908,7 +2915,7 @@ static cudaError_t noalloc_wave(const WaveArgs& a, int grid_max, cudaStream_t s)
     unsigned long long need = (n + 127) / 128;
     int grid = (unsigned long long)grid_max > need ? (int)need : grid_max;
     if (grid < 1) grid = 1;
-    return launch_wave_lcfa(a.f.model, grid, s, a);
+    return launch_wave_lcfa(a.f.model, grid, 128, s, a);
 }
 
 ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* o,

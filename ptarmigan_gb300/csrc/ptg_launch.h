@@ -10,8 +10,10 @@ struct WaveArgs;
 struct QueueArgs;
 
 // One wave of collide_wave<model> (block size 128).
-cudaError_t launch_wave_lcfa(int model, int grid, cudaStream_t s, const WaveArgs& a);
-cudaError_t launch_wave_lma(int model, int grid, cudaStream_t s, const WaveArgs& a);
+// threads: 128, or 32 for a wave smaller than the resident grid (at most
+// 4 x grid blocks of 32 then, the same lanes)
+cudaError_t launch_wave_lcfa(int model, int grid, int threads, cudaStream_t s, const WaveArgs& a);
+cudaError_t launch_wave_lma(int model, int grid, int threads, cudaStream_t s, const WaveArgs& a);
 const void* wave_kernel_lcfa(int model);
 const void* wave_kernel_lma(int model);
 

@@ -5,11 +5,11 @@
 
 namespace ptg {
 
-cudaError_t launch_wave_lma(int model, int grid, cudaStream_t s, const WaveArgs& a) {
+cudaError_t launch_wave_lma(int model, int grid, int threads, cudaStream_t s, const WaveArgs& a) {
     if (model == M_PLANE_WAVE)
-        collide_wave<M_PLANE_WAVE><<<grid, 128, 0, s>>>(a);
+        collide_wave<M_PLANE_WAVE><<<grid, threads, 0, s>>>(a);
     else if (model == M_FOCUSED_LASER)
-        collide_wave<M_FOCUSED_LASER><<<grid, 128, 0, s>>>(a);
+        collide_wave<M_FOCUSED_LASER><<<grid, threads, 0, s>>>(a);
     else
         return cudaErrorInvalidValue;
     return cudaGetLastError();
