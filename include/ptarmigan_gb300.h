@@ -175,8 +175,9 @@ ptg_status ptg_context_destroy(ptg_ctx* ctx);
 ptg_status ptg_load_tables(ptg_ctx* ctx, const char* dir);
 
 /* main.rs:1118-1135 for one batch: collide() over every primary, host
- * buffers in and out.  `out` arrays are allocated by the library and must
- * be released with ptg_particles_free().  `seed` keys the random streams
+ * buffers in and out.  `out` arrays are allocated by the library (one
+ * page-locked block, reused by the context's later outputs once released)
+ * and must be released with ptg_particles_free().  `seed` keys the random streams
  * (the role of control:rng_seed); `id_base` is the first id handed to
  * secondaries (the reference starts current_id at the number of primaries,
  * main.rs:1070). */
@@ -193,7 +194,8 @@ ptg_status ptg_collide_batch_device(ptg_ctx* ctx, const ptg_laser_desc* laser, c
                                     const ptg_particles* d_primaries, uint64_t seed, uint64_t id_base,
                                     ptg_particles* d_out, ptg_run_stats* stats);
 
-/* Frees arrays allocated by ptg_collide_batch. */
+/* Releases arrays allocated by ptg_collide_batch or ptg_collide_multi (the
+ * block goes back to its context, or is freed if the context is gone). */
 void ptg_particles_free(ptg_particles* p);
 
 /* Allocation-free variant of ptg_collide_batch_device.  It has no

@@ -16,6 +16,7 @@
 #include <dlfcn.h>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/ptarmigan_gb300.h"
@@ -691,10 +692,13 @@ ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out) {
     return PTG_OK;
 }
 
+static void host_blocks_release(ptg_ctx* c);
+
 ptg_status ptg_context_destroy(ptg_ctx* c) {
     if (!c) return PTG_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    host_blocks_release(c);
     cudaFree(c->store_mem);
     cudaFree(c->out_mem);
     cudaFree(c->in_mem);
@@ -1238,38 +1242,130 @@ static ptg_status stage_primaries(ptg_ctx* c, const ptg_particles* h) {
     return PTG_OK;
 }
 
-// Copies the context's device output (c->d_out, c->d_out.n rows) into
-// newly allocated host arrays (freed by ptg_particles_free); the copies are
-// queued on the context's stream and not waited for.
+// ------------------------------------------------ host output blocks ---
+// The host arrays of an output live in one page-locked block, so that the
+// device-to-host copies run at the link's speed and the pages are not
+// faulted in on every call.  A block lent to the caller is recorded here by
+// its base (the `r` array) and comes back through ptg_particles_free; the
+// context keeps up to two returned blocks for its next outputs and frees
+// them when it is destroyed.  A block returned after its context is gone is
+// freed at once.
+struct HostBlock {
+    void* base;
+    size_t bytes;
+    ptg_ctx* owner;
+};
+static std::mutex g_host_mu;
+static std::unordered_map<void*, HostBlock>& host_lent() {
+    static auto* m = new std::unordered_map<void*, HostBlock>();
+    return *m;
+}
+static std::unordered_map<ptg_ctx*, std::vector<HostBlock>>& host_idle() {
+    static auto* m = new std::unordered_map<ptg_ctx*, std::vector<HostBlock>>();
+    return *m;
+}
+constexpr size_t HOST_IDLE_MAX = 2;
+
+// A block of at least `bytes` for context c: a returned one if it is large
+// enough, else a new one.
+static void* host_block_take(ptg_ctx* c, size_t bytes) {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    auto& idle = host_idle()[c];
+    for (size_t k = 0; k < idle.size(); ++k) {
+        if (idle[k].bytes >= bytes) {
+            HostBlock b = idle[k];
+            idle.erase(idle.begin() + (long)k);
+            host_lent()[b.base] = b;
+            return b.base;
+        }
+    }
+    // room for 12.5 % more particles next time
+    size_t want = bytes + bytes / 8;
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    host_lent()[p] = HostBlock{p, want, c};
+    return p;
+}
+
+// Returns true if `base` was a lent block (now given back).
+static bool host_block_return(void* base) {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    auto it = host_lent().find(base);
+    if (it == host_lent().end()) return false;
+    HostBlock b = it->second;
+    host_lent().erase(it);
+    if (b.owner == nullptr) {
+        cudaFreeHost(b.base);
+        return true;
+    }
+    auto& idle = host_idle()[b.owner];
+    idle.push_back(b);
+    if (idle.size() > HOST_IDLE_MAX) {
+        // drop the smallest
+        size_t k_min = 0;
+        for (size_t k = 1; k < idle.size(); ++k)
+            if (idle[k].bytes < idle[k_min].bytes) k_min = k;
+        cudaFreeHost(idle[k_min].base);
+        idle.erase(idle.begin() + (long)k_min);
+    }
+    return true;
+}
+
+// The context's returned blocks are freed; its lent ones are freed when
+// they come back.
+static void host_blocks_release(ptg_ctx* c) {
+    std::lock_guard<std::mutex> g(g_host_mu);
+    auto it = host_idle().find(c);
+    if (it != host_idle().end()) {
+        for (auto& b : it->second) cudaFreeHost(b.base);
+        host_idle().erase(it);
+    }
+    for (auto& kv : host_lent())
+        if (kv.second.owner == c) kv.second.owner = nullptr;
+}
+
+// Copies the context's device output (c->d_out, c->d_out.n rows) into host
+// arrays carved from one page-locked block (returned by
+// ptg_particles_free); the copies are queued on the context's stream and
+// not waited for.
 static ptg_status download_output(ptg_ctx* c, ptg_particles* out) {
     size_t m = c->d_out.n;
     std::memset(out, 0, sizeof(*out));
-    out->n = m;
     size_t sz = m ? m : 1;
-    out->species = (int32_t*)std::malloc(4 * sz);
-    out->r = (double*)std::malloc(32 * sz);
-    out->u = (double*)std::malloc(32 * sz);
-    out->r0 = (double*)std::malloc(32 * sz);
-    out->u0 = (double*)std::malloc(32 * sz);
-    out->pol = (double*)std::malloc(32 * sz);
-    out->weight = (double*)std::malloc(8 * sz);
-    out->payload = (double*)std::malloc(8 * sz);
-    out->parent_chi = (double*)std::malloc(8 * sz);
-    out->interaction_count = (double*)std::malloc(8 * sz);
-    out->work = (double*)std::malloc(8 * sz);
-    out->id = (uint64_t*)std::malloc(8 * sz);
-    out->parent_id = (uint64_t*)std::malloc(8 * sz);
-    out->primary = (uint64_t*)std::malloc(8 * sz);
-    out->stream = (uint64_t*)std::malloc(8 * sz);
-    out->generation = (int32_t*)std::malloc(4 * sz);
-    out->flags = (int32_t*)std::malloc(4 * sz);
-    out->status = (int32_t*)std::malloc(4 * sz);
-    if (!out->species || !out->r || !out->u || !out->r0 || !out->u0 || !out->pol || !out->weight || !out->payload ||
-        !out->parent_chi || !out->interaction_count || !out->work || !out->id || !out->parent_id || !out->primary ||
-        !out->stream || !out->generation || !out->flags || !out->status) {
-        ptg_particles_free(out);
-        return set_err(PTG_ERR_ALLOC, "host allocation of the output failed");
-    }
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    // 8-byte fields first; r is the block's base
+    size_t w32 = up(32 * sz), w8 = up(8 * sz), w4 = up(4 * sz);
+    size_t bytes = 5 * w32 + 9 * w8 + 4 * w4;
+    char* base = (char*)host_block_take(c, bytes);
+    if (!base) return set_err(PTG_ERR_ALLOC, "host allocation of the output failed");
+    char* q = base;
+    auto take = [&](size_t w) {
+        char* r = q;
+        q += w;
+        return r;
+    };
+    out->r = (double*)take(w32);
+    out->u = (double*)take(w32);
+    out->r0 = (double*)take(w32);
+    out->u0 = (double*)take(w32);
+    out->pol = (double*)take(w32);
+    out->weight = (double*)take(w8);
+    out->payload = (double*)take(w8);
+    out->parent_chi = (double*)take(w8);
+    out->interaction_count = (double*)take(w8);
+    out->work = (double*)take(w8);
+    out->id = (uint64_t*)take(w8);
+    out->parent_id = (uint64_t*)take(w8);
+    out->primary = (uint64_t*)take(w8);
+    out->stream = (uint64_t*)take(w8);
+    out->species = (int32_t*)take(w4);
+    out->generation = (int32_t*)take(w4);
+    out->flags = (int32_t*)take(w4);
+    out->status = (int32_t*)take(w4);
+    out->n = m;
     const ptg_particles& d = c->d_out;
     auto down = [&](void* dst, const void* src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
@@ -1798,6 +1894,10 @@ ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* co
 
 void ptg_particles_free(ptg_particles* p) {
     if (!p) return;
+    if (p->r && host_block_return(p->r)) {
+        std::memset(p, 0, sizeof(*p));
+        return;
+    }
     std::free(p->species);
     std::free(p->r);
     std::free(p->u);

@@ -146,6 +146,39 @@ def _f64(a, shape):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(shape))
 
 
+class _HostOutput:
+    """Owns a library-allocated output (ptg_particles); released with
+    ptg_particles_free when the last array viewing it is gone."""
+
+    def __init__(self, lib, out):
+        self.lib, self.out = lib, out
+
+    def __del__(self):
+        try:
+            self.lib.ptg_particles_free(C.byref(self.out))
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def _host_arrays(lib, out):
+    """numpy views of a library output's host arrays (no copy); the block
+    goes back to the library when every view has been dropped."""
+    owner = _HostOutput(lib, out)
+    n = out.n
+    arrays = {}
+    ctype_of = {np.float64: C.c_double, np.int32: C.c_int32, np.uint64: C.c_uint64}
+    for name, dt, cols in abi.PARTICLE_FIELDS:
+        shape = (n, cols) if cols > 1 else (n,)
+        if n == 0:
+            arrays[name] = np.zeros(shape, dtype=dt)
+            continue
+        addr = C.cast(getattr(out, name), C.c_void_p).value
+        buf = (ctype_of[dt] * (n * cols)).from_address(addr)
+        buf._owner = owner
+        arrays[name] = np.frombuffer(buf, dtype=dt).reshape(shape)
+    return arrays
+
+
 class Engine:
     """One device context (stream, shower store, tables)."""
 
@@ -192,20 +225,7 @@ class Engine:
         st = abi.RunStats()
         self._check(self.L.ptg_collide_batch(self._h, C.byref(laser), C.byref(options), C.byref(view), seed, id_base,
                                              C.byref(out), C.byref(st)))
-        try:
-            m = out.n
-            arrays = {}
-            for name, dt, cols in abi.PARTICLE_FIELDS:
-                ptr = getattr(out, name)
-                shape = (m, cols) if cols > 1 else (m,)
-                if m == 0:
-                    arrays[name] = np.zeros(shape, dtype=dt)
-                    continue
-                buf = np.ctypeslib.as_array(ptr, shape=shape)
-                arrays[name] = np.array(buf, dtype=dt, copy=True)
-        finally:
-            self.L.ptg_particles_free(C.byref(out))
-        return arrays, st.as_dict()
+        return _host_arrays(self.L, out), st.as_dict()
 
     def collide_device(self, laser, options, d_primaries, seed, id_base=None):
         """Device-resident variant: `d_primaries` maps field names to CUDA
@@ -264,17 +284,7 @@ class Engine:
         total = abi.RunStats()
         self._check(self.L.ptg_collide_multi(self._h, m, arr, C.byref(options), C.byref(view), C.byref(out), offs,
                                              stats, C.byref(total)))
-        try:
-            n = out.n
-            whole = {}
-            for name, dt, cols in abi.PARTICLE_FIELDS:
-                shape = (n, cols) if cols > 1 else (n,)
-                if n == 0:
-                    whole[name] = np.zeros(shape, dtype=dt)
-                else:
-                    whole[name] = np.array(np.ctypeslib.as_array(getattr(out, name), shape=shape), dtype=dt, copy=True)
-        finally:
-            self.L.ptg_particles_free(C.byref(out))
+        whole = _host_arrays(self.L, out)
         parts = [{k: v[offs[i]:offs[i + 1]] for k, v in whole.items()} for i in range(m)]
         return parts, [stats[i].as_dict() for i in range(m)], total.as_dict()
 
