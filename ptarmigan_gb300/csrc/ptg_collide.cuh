@@ -218,10 +218,10 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
                 f3 t = f3add(e, f3cross(bt, b));
                 float eb = f3dot(e, bt);
                 float q = f3dot(t, t) - eb * eb;
-                float chi32 = q > 0.0f ? ((float)u.t * (float)f.chi_scale) * sqrtf(q) : 0.0f;
+                float chi32 = q > 0.0f ? ((float)u.t * f.chi_scale32) * sqrtf(q) : 0.0f;
                 float gam = (float)u.t;
                 prob = (float)dt_actual * (a.o.classical_mode ? (float)(SQRT_3 * ALPHA_FINE * 5.0 * FRAC_PI_3 / (2.0 * PI * COMPTON_TIME)) * chi32 / gam
-                                                             : lcfa_photon_rate32(chi32, gam));
+                                                             : lcfa_photon_rate32(chi32, gam, a.gl->ln_h32));
             }
         }
         if (prob > 0.0f && rng.next() < (double)prob) {
@@ -320,13 +320,14 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
         if (!a.o.pol_resolved) {
             f3 e, b;
             if (lcfa_fields32(f, r, &e, &b)) {
-                float inv = rsqrtf((float)(ell.x * ell.x + ell.y * ell.y + ell.z * ell.z));
-                f3 n = f3{(float)ell.x * inv, (float)ell.y * inv, (float)ell.z * inv};
+                f3 l3 = f3{(float)ell.x, (float)ell.y, (float)ell.z};
+                f3 n = f3scale(rsqrtf(f3dot(l3, l3)), l3);
                 f3 ap = f3add(f3add(e, f3scale(-f3dot(e, n), n)), f3cross(n, b));
                 float q = f3dot(ap, ap);
                 if (q > 0.0f) {
-                    float chi32 = ((float)ell.t * (float)f.chi_scale) * sqrtf(q);
-                    prob_step = (double)((float)(ALPHA_FINE / COMPTON_TIME) * ((float)dt / (float)ell.t) * chi32 * lcfa_t_mean32(chi32));
+                    float chi32 = ((float)ell.t * f.chi_scale32) * sqrtf(q);
+                    prob_step = (double)((float)(ALPHA_FINE / COMPTON_TIME) * ((float)dt / (float)ell.t) * chi32 *
+                                         lcfa_t_mean32(chi32, a.gl->ln_t32));
                 }
             }
         }

@@ -114,6 +114,32 @@ struct ptg_ctx {
 // ------------------------------------------------------------ helpers ---
 static MlpParams mlp_params(ptg_ctx* c);
 
+// Gauss-Laguerre node constants of the pair spectrum, and FP32 copies of the
+// per-step rate tables.
+static cudaError_t fill_pair_gl(PairGL* gl) {
+    double nodes[32], weights[32];
+    cudaError_t e = cudaMemcpyFromSymbol(nodes, PTG_GL_NODES, sizeof(nodes));
+    if (e == cudaSuccess) e = cudaMemcpyFromSymbol(weights, PTG_GL_WEIGHTS, sizeof(weights));
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < 32; ++k) {
+        double t = nodes[k];
+        gl->w[k] = weights[k];
+        gl->t[k] = t;
+        gl->c23[k] = std::cosh(2.0 * t / 3.0);
+        gl->c13_over_c1[k] = std::cosh(t / 3.0) / std::cosh(t);
+        gl->c1[k] = std::cosh(t);
+    }
+    double ln_h[41][2], ln_t[81][3];
+    e = cudaMemcpyFromSymbol(ln_h, PTG_LCFA_LN_H_CHI_TABLE, sizeof(ln_h));
+    if (e == cudaSuccess) e = cudaMemcpyFromSymbol(ln_t, PTG_LCFA_LN_T_CHI_TABLE, sizeof(ln_t));
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < 41; ++i)
+        for (int j = 0; j < 2; ++j) gl->ln_h32[i][j] = (float)ln_h[i][j];
+    for (int i = 0; i < 81; ++i)
+        for (int j = 0; j < 3; ++j) gl->ln_t32[i][j] = (float)ln_t[i][j];
+    return cudaSuccess;
+}
+
 static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     FieldParams f{};
     f.model = d.model;
@@ -141,6 +167,11 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     f.B0 = f.E0 / SPEED_OF_LIGHT;
     f.amp = (ELECTRON_MASS * SPEED_OF_LIGHT_SQD * f.k * d.a0) / ELEMENTARY_CHARGE;
     f.chi_scale = (d.model == PTG_FAST_PLANE_WAVE ? f.amp : f.E0) / CRITICAL_FIELD;
+    f.eps32 = (float)f.eps;
+    f.cos_pa32 = (float)f.cos_pa;
+    f.sin_pa32 = (float)f.sin_pa;
+    f.inv_tau32 = (float)f.inv_tau;
+    f.chi_scale32 = (float)f.chi_scale;
     double nc = f.n_cycles;
     f.max_phase = d.envelope == PTG_ENV_COS2 ? PI * nc : (d.envelope == PTG_ENV_FLATTOP ? PI * (nc + 1.0) : 6.0 * PI * nc);
     f.bandwidth = 0.0;
@@ -665,19 +696,8 @@ ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out) {
     CUDA_TRY(cudaEventCreate(&c->ev1));
     CUDA_TRY(cudaMalloc(&c->counters, sizeof(Counters)));
     CUDA_TRY(cudaMallocHost(&c->h_counters, sizeof(Counters)));
-    // Gauss-Laguerre node constants of the pair spectrum
     PairGL gl;
-    double nodes[32], weights[32];
-    CUDA_TRY(cudaMemcpyFromSymbol(nodes, PTG_GL_NODES, sizeof(nodes)));
-    CUDA_TRY(cudaMemcpyFromSymbol(weights, PTG_GL_WEIGHTS, sizeof(weights)));
-    for (int k = 0; k < 32; ++k) {
-        double t = nodes[k];
-        gl.w[k] = weights[k];
-        gl.t[k] = t;
-        gl.c23[k] = std::cosh(2.0 * t / 3.0);
-        gl.c13_over_c1[k] = std::cosh(t / 3.0) / std::cosh(t);
-        gl.c1[k] = std::cosh(t);
-    }
+    CUDA_TRY(fill_pair_gl(&gl));
     CUDA_TRY(cudaMalloc(&c->gl, sizeof(PairGL)));
     CUDA_TRY(cudaMemcpy(c->gl, &gl, sizeof(PairGL), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&c->lma_dev, sizeof(LmaTables)));
@@ -2985,18 +3005,8 @@ static ptg_status noalloc_setup(int dev, char** base) {
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || ptr == nullptr)
         return set_err(PTG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    double nodes[32], weights[32];
-    CUDA_TRY(cudaMemcpyFromSymbol(nodes, PTG_GL_NODES, sizeof(nodes)));
-    CUDA_TRY(cudaMemcpyFromSymbol(weights, PTG_GL_WEIGHTS, sizeof(weights)));
     PairGL gl;
-    for (int k = 0; k < 32; ++k) {
-        double t = nodes[k];
-        gl.w[k] = weights[k];
-        gl.t[k] = t;
-        gl.c23[k] = std::cosh(2.0 * t / 3.0);
-        gl.c13_over_c1[k] = std::cosh(t / 3.0) / std::cosh(t);
-        gl.c1[k] = std::cosh(t);
-    }
+    CUDA_TRY(fill_pair_gl(&gl));
     CUDA_TRY(cudaMemcpy((char*)ptr + NOALLOC_OFF_GL, &gl, sizeof(gl), cudaMemcpyHostToDevice));
     g_noalloc_base[dev] = (char*)ptr;
     *base = (char*)ptr;

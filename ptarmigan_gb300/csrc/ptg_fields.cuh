@@ -28,6 +28,9 @@ struct FieldParams {
     double inv_waist, inv_zr;  // reciprocals, so the per-step field needs no division
     double inv_tau;            // 1 / (omega * duration)
     double chi_scale;          // field scale of lcfa_fields32 over the critical field
+    // FP32 copies for the per-step FP32 path (converted once on the host,
+    // the same rounding as a conversion on the device)
+    float eps32, cos_pa32, sin_pa32, inv_tau32, chi_scale32;
 };
 
 __device__ __forceinline__ double phase_of(const FieldParams& f, d4 r) { return f.k * r.t - f.k * r.z; }

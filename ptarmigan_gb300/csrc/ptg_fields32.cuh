@@ -38,13 +38,13 @@ __device__ __forceinline__ float reduced_phase(double ph) {
 
 // Salamin beam (fast_focused_laser.rs:59-111) in FP32, normalised to E0.
 // (cr, sr) rotate by the polarisation angle.
-__device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr, double sr, f3* reE, f3* imE, f3* reB,
-                                           f3* imB) {
+__device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr, double sr, float c, float s,
+                                           f3* reE, f3* imE, f3* reB, f3* imB) {
     double rx = cr * r.x + sr * r.y;
     double ry = cr * r.y - sr * r.x;
     float x = (float)(rx * f.inv_waist), y = (float)(ry * f.inv_waist), z = (float)(r.z * f.inv_zr);
     float rho2 = x * x + y * y;
-    float e = (float)f.eps, e2 = e * e, e3 = e2 * e, e4 = e2 * e2;
+    float e = f.eps32, e2 = e * e, e3 = e2 * e, e4 = e2 * e2;
     float den = 1.0f / (1.0f + z * z);
     cf fc = cf{den, z * den};
     float ex = expf(-fc.re * rho2);
@@ -77,7 +77,6 @@ __device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr
     By = cf{By.im, -By.re};
     cf bz = cfadds(1.0f, cfadd(cfs(rho2, fc), cfs(-rho4 * 0.5f, f2)));
     cf Bz = cfmul(pre, cfadd(cfs(e * y, fc), cfs(e3 * y * 0.5f, cfmul(f2, bz))));
-    float c = (float)cr, s = (float)sr;
     *reE = f3{c * Ex.re - s * Ey.re, c * Ey.re + s * Ex.re, Ez.re};
     *imE = f3{c * Ex.im - s * Ey.im, c * Ey.im + s * Ex.im, Ez.im};
     *reB = f3{-s * By.re, c * By.re, Bz.re};
@@ -141,19 +140,19 @@ __device__ __forceinline__ bool lcfa_fields32(const FieldParams& f, d4 r, f3* e,
     if (f.envelope == ENV_GAUSSIAN) {
         float q = (float)(phase * f.inv_tau);
         env = expf(-2.0f * (float)LN_2 * q * q);
-        denv = (-4.0f * (float)LN_2 * (float)f.inv_tau) * q * env;
+        denv = (-4.0f * (float)LN_2 * f.inv_tau32) * q * env;
     } else {
         double de, dd;
         ffl_envelope(f, phase, &de, &dd);
         env = (float)de, denv = (float)dd;
     }
     f3 reE, imE, reB, imB;
-    ffl_beam32(f, r, f.cos_pa, f.sin_pa, &reE, &imE, &reB, &imB);
+    ffl_beam32(f, r, f.cos_pa, f.sin_pa, f.cos_pa32, f.sin_pa32, &reE, &imE, &reB, &imB);
     f3 ee = f3add(f3scale(env, reE), f3scale(denv, imE));
     f3 bb = f3add(f3scale(env, reB), f3scale(denv, imB));
     if (f.circular) {
         d4 rp = d4{r.t, r.y, -r.x, r.z};
-        ffl_beam32(f, rp, 1.0, 0.0, &reE, &imE, &reB, &imB);
+        ffl_beam32(f, rp, 1.0, 0.0, 1.0f, 0.0f, &reE, &imE, &reB, &imB);
         f3 ey = f3add(f3scale(env, imE), f3scale(-denv, reE));
         f3 by = f3add(f3scale(env, imB), f3scale(-denv, reB));
         ee = f3add(ee, f3{-ey.y, ey.x, ey.z});
@@ -171,7 +170,8 @@ __device__ __forceinline__ double field_scale(const FieldParams& f) {
 }
 
 // FP32 quantum synchrotron rate (lcfa/photon_emission/mod.rs:13-33), per second.
-__device__ __forceinline__ float lcfa_photon_rate32(float chi, float gamma) {
+// `lnh`: PTG_LCFA_LN_H_CHI_TABLE in FP32.
+__device__ __forceinline__ float lcfa_photon_rate32(float chi, float gamma, const float (*lnh)[2]) {
     float h;
     if (chi < 0.01f) {
         h = 5.0f * (float)FRAC_PI_3 * (1.0f - 8.0f * chi / (5.0f * (float)SQRT_3));
@@ -182,11 +182,11 @@ __device__ __forceinline__ float lcfa_photon_rate32(float chi, float gamma) {
         h = -2260.1819695887225f + c * h;
         h = 0.00296527643253334f * h / (chi * chi);
     } else {
-        float index = (logf(chi) - (float)PTG_LCFA_LN_H_CHI_TABLE[0][0]) / (float)PTG_LCFA_PH_DELTA_LN_CHI;
+        float index = (logf(chi) - lnh[0][0]) / (float)PTG_LCFA_PH_DELTA_LN_CHI;
         int i = (int)floorf(index);
         i = i < 0 ? 0 : (i > 39 ? 39 : i);
         float w = index - (float)i;
-        float ln_h = (1.0f - w) * (float)PTG_LCFA_LN_H_CHI_TABLE[i][1] + w * (float)PTG_LCFA_LN_H_CHI_TABLE[i + 1][1];
+        float ln_h = (1.0f - w) * lnh[i][1] + w * lnh[i + 1][1];
         h = expf(ln_h);
     }
     return (float)(SQRT_3 * ALPHA_FINE / (2.0 * PI * COMPTON_TIME)) * chi * h / gamma;
@@ -194,27 +194,27 @@ __device__ __forceinline__ float lcfa_photon_rate32(float chi, float gamma) {
 
 // FP32 mean of T_par and T_perp (lcfa/pair_creation/mod.rs:13-40): the
 // unpolarised Breit-Wheeler auxiliary function.
-__device__ __forceinline__ float lcfa_t_mean32(float chi) {
-    const double(*T)[3] = PTG_LCFA_LN_T_CHI_TABLE;
+// `T`: PTG_LCFA_LN_T_CHI_TABLE in FP32.
+__device__ __forceinline__ float lcfa_t_mean32(float chi, const float (*T)[3]) {
     const float D = (float)PTG_LCFA_PAIR_DELTA_LN_CHI;
     if (chi <= 0.01f) return 0.0f;
     if (chi < 1.0f) {
         float lc = logf(chi);
-        int i = (int)((lc - (float)T[0][0]) / D);
+        int i = (int)((lc - T[0][0]) / D);
         i = i < 0 ? 0 : (i > 79 ? 79 : i);
-        float e0 = expf((float)T[i][0]), e1 = expf((float)T[i + 1][0]);
+        float e0 = expf(T[i][0]), e1 = expf(T[i + 1][0]);
         float dx = (chi - e0) / (e1 - e0);
-        float par = (1.0f - dx) / (float)T[i][1] + dx / (float)T[i + 1][1];
-        float perp = (1.0f - dx) / (float)T[i][2] + dx / (float)T[i + 1][2];
+        float par = (1.0f - dx) / T[i][1] + dx / T[i + 1][1];
+        float perp = (1.0f - dx) / T[i][2] + dx / T[i + 1][2];
         return 0.5f * (expf(1.0f / par) + expf(1.0f / perp));
     }
     if (chi < 100.0f) {
         float lc = logf(chi);
-        int i = (int)((lc - (float)T[0][0]) / D);
+        int i = (int)((lc - T[0][0]) / D);
         i = i < 0 ? 0 : (i > 79 ? 79 : i);
-        float dx = (lc - (float)T[i][0]) / D;
-        return 0.5f * (expf((1.0f - dx) * (float)T[i][1] + dx * (float)T[i + 1][1]) +
-                       expf((1.0f - dx) * (float)T[i][2] + dx * (float)T[i + 1][2]));
+        float dx = (lc - T[i][0]) / D;
+        return 0.5f * (expf((1.0f - dx) * T[i][1] + dx * T[i + 1][1]) +
+                       expf((1.0f - dx) * T[i][2] + dx * T[i + 1][2]));
     }
     float c = cbrtf(chi);
     return 0.5f * ((0.3036898468348568f + 0.4555347702522852f) / c - 4.0f / (3.0f * chi));

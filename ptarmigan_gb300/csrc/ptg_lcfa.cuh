@@ -367,6 +367,9 @@ __device__ __forceinline__ double lcfa_pair_probability(d4 ell, d4 sv_in, double
 // cosh(t).  Filled once by the host.
 struct PairGL {
     double w[32], t[32], c23[32], c13_over_c1[32], c1[32];
+    // FP32 copies of the per-step rate tables (ln h(chi) and ln T(chi))
+    float ln_h32[41][2];
+    float ln_t32[81][3];
 };
 
 // lcfa/pair_creation/mod.rs:80-89
