@@ -69,8 +69,8 @@ WORKLOAD = "focused LCFA shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; Fa
 # (dram__bytes_read.sum + dram__bytes_write.sum over the lepton and photon
 # waves of a 1e6-primary batch: 1.460e9 + 1.100e9 bytes; the pair waves add
 # nothing measurable).
-FP64_PER_LEPTON_STEP = 253.9
-FP64_PER_PHOTON_STEP = 34.2
+FP64_PER_LEPTON_STEP = 213.8
+FP64_PER_PHOTON_STEP = 29.2
 DRAM_BYTES_PER_PRIMARY = 2.5605e9 / 1e6
 
 

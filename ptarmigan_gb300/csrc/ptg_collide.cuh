@@ -194,9 +194,10 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             // bit (every field term is an exact zero), recomputes gamma and
             // drifts the second half step; no work is done.
             u = L.u;
-            double g = sqrt(1.0 + (u.x * u.x + u.y * u.y + u.z * u.z));
-            u.t = g;
-            double h2 = 0.5 * SPEED_OF_LIGHT * dt / g;
+            double g2 = 1.0 + (u.x * u.x + u.y * u.y + u.z * u.z);
+            double ig = rsqrt(g2);
+            u.t = g2 * ig;  // gamma, as vay_push forms it
+            double h2 = (0.5 * SPEED_OF_LIGHT * dt) * ig;
             r = d4{rh.t + h2 * u.t, rh.x + h2 * u.x, rh.y + h2 * u.y, rh.z + h2 * u.z};
             dwork = 0.0;
             L.hh = h2;
