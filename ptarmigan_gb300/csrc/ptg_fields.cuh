@@ -124,7 +124,7 @@ __device__ __forceinline__ void ffl_beam(const FieldParams& f, d4 r, double cr, 
     cplx pre = cmul(cplx{fre, fim}, cplx{ex * cs, ex * sn});
     // corrections in FP32
     float xf = (float)x, yf = (float)y, r2 = (float)rho2;
-    float ef = (float)f.eps, e2 = ef * ef, e3 = e2 * ef, e4 = e2 * e2;
+    float ef = f.eps32, e2 = ef * ef, e3 = e2 * ef, e4 = e2 * e2;
     float fr = (float)fre, fi = (float)fim;
     float f2r = fr * fr - fi * fi, f2i = 2.0f * fr * fi;
     float f3r = f2r * fr - f2i * fi, f3i = f2r * fi + f2i * fr;
