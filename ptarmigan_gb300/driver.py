@@ -15,10 +15,11 @@ radius with its distribution and cutoff, length, collision_angle,
 collision_plane, rms_divergence, energy_chirp, offset, stokes_pars),
 output (ident, electron / photon / positron distributions, file_format,
 units, coordinate_system, discard_background(_e), min_energy, max_angle),
-stats (electron / photon / positron, and expressions) and constants.
-Not supported: beam:spectrum, beam:from_hdf5, output:dump_all_particles,
-intermediate-particle output, increase_pair_rate_by: auto and
-stop_at_time: auto.
+stats (electron / photon / positron, and expressions), constants, and
+output:dump_all_particles: hdf5 (the final-state file of main.rs:1289-1715,
+written by ptarmigan_gb300.hdf5).
+Not supported: beam:spectrum, beam:from_hdf5, intermediate-particle
+output, increase_pair_rate_by: auto and stop_at_time: auto.
 """
 
 import math
@@ -26,7 +27,7 @@ import os
 
 import numpy as np
 
-from . import abi, engine as engine_mod
+from . import abi, engine as engine_mod, hdf5
 from .input import COMPTON_TIME, ELECTRON_MASS, ELEMENTARY_CHARGE, SPEED_OF_LIGHT, Input, InputError
 from .output import DistributionFunction, SummaryStatistic, UnitSystem, rust_exp
 
@@ -195,8 +196,9 @@ def run(path, output_dir="", engine=None, log=print):
     ident = inp.str("output:ident", "")
     if ident == "auto":
         ident = os.path.splitext(os.path.basename(path))[0]
-    if inp.contains("output:dump_all_particles"):
-        raise InputError("output:dump_all_particles is not supported by this driver")
+    dump = inp.str("output:dump_all_particles", "") if inp.contains("output:dump_all_particles") else None
+    if dump is not None and dump != "hdf5":
+        raise InputError("output:dump_all_particles: the only format is hdf5")
     if inp.list("output:intermediate") or inp.list("stats:intermediate"):
         raise InputError("intermediate-particle output is not supported by this driver")
     units = UnitSystem.named(inp.str("output:units", "auto"))
@@ -228,6 +230,12 @@ def run(path, output_dir="", engine=None, log=print):
                 % (a0, n, st["n_out"], st["emissions"], st["pair_events"], st["device_ms"]))
             if beam_frame:
                 to_beam_basis(out, angle, plane)
+            if dump is not None:
+                cur0 = ident if len(a0s) == 1 else "%s%sa0_%.3f" % (ident, "_" if ident else "", a0)
+                fname = os.path.join(output_dir, cur0 + ("_" if cur0 else "") + "particles.h5")
+                write_particles_hdf5(fname, inp, path, laser, a0, desc, n, species, angle, plane, opts, out, units,
+                                     not beam_frame, seed)
+                written.append(fname)
             import torch
             dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to("cuda:%d" % eng.device) for k, v in out.items()}
             cur = ident if len(a0s) == 1 else "%s%sa0_%.3f" % (ident, "_" if ident else "", a0)
@@ -269,3 +277,198 @@ def _expression_line(inp, spec):
     if formula is not None:
         return "expr: %s (%s) = %s [%s]" % (name, formula, rust_exp(value, 6), unit)
     return "expr: %s = %s [%s]" % (name, rust_exp(value, 6), unit)
+
+
+# ------------------------------------------------------------ HDF5 dump ---
+VACUUM_PERMITTIVITY = 8.854188e-12
+ELECTRON_MASS_MEV = 0.510999
+
+
+def laser_energy(laser):
+    """(energy, unit) of the pulse: field/fast_focused_laser.rs:220-262 (J)
+    and field/fast_plane_wave.rs:197-236 (J/m^2, per unit area), shared by
+    the LMA models; None for a chirped plane wave, whose energy the
+    reference integrates numerically."""
+    if laser.model in (abi.PLANE_WAVE, abi.FAST_PLANE_WAVE) and laser.chirp_b != 0.0:
+        return None
+    omega = 2.0 * math.pi * SPEED_OF_LIGHT / laser.wavelength
+    amplitude = ELECTRON_MASS * SPEED_OF_LIGHT * omega * laser.a0 / ELEMENTARY_CHARGE
+    intensity = SPEED_OF_LIGHT * VACUUM_PERMITTIVITY * amplitude ** 2
+    delta = 1.0 if laser.polarization == abi.CIRCULAR else 0.0
+    nc = laser.n_cycles
+    if laser.envelope == abi.COS2:
+        duration = (1.0 + delta) * (1.0 + 3.0 * nc ** 2) * math.pi / (8.0 * nc) / omega
+    elif laser.envelope == abi.GAUSSIAN:
+        arg = -(math.pi * nc) ** 2 / math.log(2.0)
+        large = 0.5 * nc * math.sqrt(math.pi ** 3 / math.log(2.0))
+        px = large - math.expm1(arg) * math.sqrt(math.log(2.0) / math.pi) / (4.0 * nc)
+        py = large + (1.0 + math.exp(arg)) * math.sqrt(math.log(2.0) / math.pi) / (4.0 * nc)
+        duration = (px + delta * py) / omega
+    else:
+        duration = (1.0 + delta) * (nc - 3.0 / 16.0) * math.pi / omega
+    if laser.model in (abi.FOCUSED_LASER, abi.FAST_FOCUSED_LASER):
+        zr = math.pi * laser.waist ** 2 / laser.wavelength
+        e = laser.waist / zr
+        power = 0.5 * math.pi * intensity * laser.waist ** 2 * (1.0 + e * e / 4.0 + e ** 4 / 8.0)
+        return power * duration, "J"
+    return intensity * duration, "J/m^2"
+
+
+_POL = [("linear", 0), ("circular", 1)]
+_ENV = [("cos^2", 0), ("flattop", 1), ("gaussian", 2)]
+_ENV_NAME = {abi.COS2: "cos^2", abi.FLATTOP: "flattop", abi.GAUSSIAN: "gaussian"}
+_SPECIES_NAME = {abi.ELECTRON: "electron", abi.POSITRON: "positron", abi.PHOTON: "photon"}
+
+
+def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, angle, plane, opts, out, units,
+                         laser_defines_z, seed):
+    """The final-state file of main.rs:1289-1715: build information, the
+    parsed configuration, and every final-state particle by species, in the
+    output unit system, each dataset with its `unit` and `desc`
+    attributes and the reference's aliases."""
+    root = hdf5.Group()
+    b = root.group("build")
+    b.dataset("version", "ptarmigan-gb300")
+    b.dataset("branch", "")
+    b.dataset("commit-hash", "")
+    b.dataset("features", "gb300")
+    conf = root.group("config")
+    conf.dataset("mpi-tasks", 1)
+    with open(input_path, "r") as fh:
+        conf.dataset("input-file", fh.read())
+    u = conf.group("unit")
+    u.dataset("position", units.length.name)
+    u.dataset("momentum", units.momentum.name)
+    c = conf.group("control")
+    c.dataset("dt_multiplier", float(opts.dt_multiplier))
+    c.dataset("radiation_reaction", bool(opts.rr))
+    c.dataset("classical", bool(opts.classical))
+    c.dataset("pair_creation", bool(opts.tracking_photons))
+    c.dataset("pair_creation_is_pol_resolved", bool(opts.pol_resolved))
+    c.dataset("lcfa", laser.model in (abi.FAST_PLANE_WAVE, abi.FAST_FOCUSED_LASER))
+    c.dataset("rng_seed", inp.int("control:rng_seed", 0))
+    c.dataset("increase_pair_rate_by", float(opts.rate_increase))
+    c.dataset("bandwidth_correction", bool(laser.finite_bandwidth))
+    if math.isfinite(opts.t_stop):
+        c.dataset("stop_at_time", float(opts.t_stop), unit="s",
+                  desc="tracking has continued until all particles have this time coordinate")
+    c.dataset("select_multiplicity", int(opts.multiplicity) if opts.multiplicity >= 0 else False)
+    focusing = laser.model in (abi.FOCUSED_LASER, abi.FAST_FOCUSED_LASER)
+    lz = conf.group("laser")
+    L = units.length
+    lz.dataset("a0", float(a0), unit="1", desc="peak value of the laser normalized amplitude")
+    lz.dataset("wavelength", laser.wavelength * L.scale, unit=L.name, desc="wavelength of the carrier")
+    lz.dataset("polarization", hdf5.Enum(_POL, "circular" if laser.polarization == abi.CIRCULAR else "linear"),
+               desc="linear/circular")
+    if laser.polarization == abi.LINEAR:
+        lz.dataset("polarization_angle", float(laser.pol_angle), unit="rad",
+                   desc="angle between x-axis and electric field")
+    lz.dataset("focusing", focusing, desc="true/false => pulse is modelled in 3d/1d")
+    lz.dataset("envelope", hdf5.Enum(_ENV, _ENV_NAME[laser.envelope]),
+               desc="pulse envelope of the laser vector potential")
+    lz.dataset("chirp_b", float(laser.chirp_b), unit="1", desc="parameter that appears in carrier phase = phi + b phi^2")
+    if focusing:
+        lz.dataset("waist", laser.waist * L.scale, unit=L.name,
+                   desc="radius in the focal plane at which intensity is 1/e^2 of its peak value")
+    if laser.envelope == abi.GAUSSIAN:
+        lz.dataset("fwhm_duration", laser.n_cycles * laser.wavelength / SPEED_OF_LIGHT, unit="s",
+                   desc="full width at half maximum of the temporal intensity profile")
+    else:
+        lz.dataset("n_cycles", float(laser.n_cycles), unit="1",
+                   desc="number of wavelengths corresponding to the total pulse duration")
+    bm = conf.group("beam")
+    bm.dataset("n", int(n), unit="1", desc="number of primary macroparticles")
+    bm.dataset("species", _SPECIES_NAME[species])
+    bm.dataset("collision_angle", float(angle), unit="rad",
+               desc="polar angle between beam momentum and laser wavevector, zero if counterpropagating")
+    bm.dataset("collision_plane_angle", float(plane), unit="rad",
+               desc="azimuthal angle between beam momentum and laser wavevector, zero if p in E, k plane")
+    bm.dataset("offset", hdf5.Vector(np.asarray(list(desc.offset)) * L.scale), unit=L.name)
+    bm.dataset("imported_from_file", False)
+    bm.dataset("n_real", n * desc.weight, unit="1",
+               desc="total number of real particles represented by the primary macroparticles")
+    charge = {abi.ELECTRON: 1.0, abi.POSITRON: -1.0, abi.PHOTON: 0.0}[species] * n * desc.weight * -ELEMENTARY_CHARGE
+    bm.dataset("charge", charge, unit="C")
+    brem = desc.gamma_dstr == abi.GAMMA_BREM
+    bm.dataset("gamma", float(desc.gamma_max if brem else desc.gamma_mean), unit="1")
+    bm.dataset("sigma", float(desc.gamma_sigma), unit="1")
+    bm.dataset("bremsstrahlung_source", bool(brem))
+    if brem:
+        bm.dataset("gamma_min", float(desc.gamma_min), unit="1")
+    if desc.radial_dstr == abi.RADIAL_UNIFORM:
+        radius, r_max = desc.r_max, desc.r_max
+    elif desc.radial_dstr == abi.RADIAL_TRUNC_NORMAL:
+        radius, r_max = desc.sigma_x, desc.x_max
+    else:
+        radius, r_max = desc.sigma_x, math.inf
+    bm.dataset("radius", radius * L.scale, unit=L.name)
+    bm.dataset("radius_max", r_max * L.scale, unit=L.name,
+               desc="density distribution is cut off at this perpendicular distance from the beam axis")
+    bm.dataset("length", desc.sigma_z * L.scale, unit=L.name)
+    bm.dataset("rms_divergence", float(desc.rms_div), unit="rad")
+    bm.dataset("polarization", hdf5.Vector(list(desc.pol)), unit="1",
+               desc="Stokes parameters of the primary particles: I, Q, U, V", alias="polarisation")
+    bm.dataset("transverse_distribution_is_normal", desc.radial_dstr != abi.RADIAL_UNIFORM)
+    bm.dataset("longitudinal_distribution_is_normal", True)
+    E = units.energy
+    op = conf.group("output")
+    op.dataset("laser_defines_positive_z", bool(laser_defines_z))
+    op.dataset("beam_defines_positive_z", not laser_defines_z)
+    op.dataset("discard_background_e", bool(opts.discard_bg_e))
+    op.dataset("discard_background_ph", bool(opts.discard_bg_ph))
+    op.dataset("min_energy", opts.min_energy * ELECTRON_MASS_MEV * E.scale, unit=E.name)
+
+    P = units.momentum
+    fs = root.group("final-state")
+
+    def pick(code):
+        sel = out["species"] == code
+        return {k: v[sel] for k, v in out.items()}
+
+    ph = pick(abi.PHOTON)
+    g = fs.group("photon")
+    g.dataset("weight", ph["weight"], unit="1", desc="number of real photons each macrophoton represents")
+    g.dataset("a0_at_creation", ph["payload"], unit="1",
+              desc="normalized amplitude (RMS under LMA) at point of emission", alias="xi")
+    g.dataset("parent_chi", ph["parent_chi"], unit="1",
+              desc="quantum parameter (RMS under LMA) of parent at point of emission")
+    g.dataset("n_pos", ph["interaction_count"], unit="1", desc="total probability of pair creation for the photon")
+    g.dataset("id", ph["id"], desc="unique ID of the photon")
+    g.dataset("parent_id", ph["parent_id"],
+              desc="ID of the particle that created the photon (for primary particles, parent_id = id")
+    g.dataset("polarization", ph["pol"], unit="1", desc="Stokes parameters of the photon: I, Q, U, V",
+              alias="polarisation")
+    g.dataset("position", ph["r"] * L.scale, unit=L.name, desc="four-position of the photon")
+    g.dataset("momentum", ph["u"] * (ELECTRON_MASS_MEV * P.scale), unit=P.name, desc="four-momentum of the photon")
+    for code, name in ((abi.ELECTRON, "electron"), (abi.POSITRON, "positron")):
+        q = pick(code)
+        g = fs.group(name)
+        g.dataset("weight", q["weight"], unit="1", desc="number of real %ss each macro%s represents" % (name, name))
+        if code == abi.POSITRON:
+            g.dataset("a0_at_creation", q["payload"], unit="1",
+                      desc="normalized amplitude (RMS under LMA) at point of creation", alias="xi")
+            g.dataset("parent_chi", q["parent_chi"], unit="1",
+                      desc="quantum parameter (RMS under LMA) of parent at point of creation")
+        g.dataset("n_gamma", q["interaction_count"], unit="1",
+                  desc="total number of photons emitted by the %s" % name)
+        g.dataset("id", q["id"], desc="unique ID of the %s" % name)
+        g.dataset("parent_id", q["parent_id"],
+                  desc="ID of the particle that created the %s (for primary particles, parent_id = id)" % name)
+        g.dataset("absorption", q["work"] * (ELECTRON_MASS_MEV * E.scale), unit=E.name,
+                  desc="energy absorbed from the laser")
+        g.dataset("position", q["r"] * L.scale, unit=L.name, desc="four-position of the %s" % name)
+        if code == abi.POSITRON:
+            g.dataset("position_at_creation", q["r0"] * L.scale, unit=L.name,
+                      desc="four-position at which the positron was created")
+        g.dataset("momentum", q["u"] * (ELECTRON_MASS_MEV * P.scale), unit=P.name,
+                  desc="four-momentum of the %s" % name)
+    lg = fs.group("laser")
+    en = laser_energy(laser)
+    if en is not None:
+        if focusing:
+            lg.dataset("energy", en[0], unit=en[1], desc="total energy of the laser pulse")
+        else:
+            lg.dataset("energy_flux", en[0], unit=en[1], desc="total energy of the laser pulse, per unit area")
+    absorption = float(np.sum(out["weight"] * out["work"])) * ELECTRON_MASS_MEV * 1.0e6 * ELEMENTARY_CHARGE
+    lg.dataset("absorption", absorption, unit="J", desc="energy absorbed from the laser")
+    hdf5.write(fname, root)

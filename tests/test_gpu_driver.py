@@ -87,3 +87,29 @@ def test_a0_loop_names_each_run(tmp_path):
     files = run(str(src), str(tmp_path), log=lambda *a: None)
     names = {os.path.basename(f) for f in files}
     assert "scan_a0_1.000_photon_energy.dat" in names and "scan_a0_2.000_stats.txt" in names
+
+
+def test_final_state_hdf5_dump(tmp_path):
+    """output:dump_all_particles: hdf5 writes <ident>_particles.h5 with
+    every final-state particle: its photon count and total weight match
+    the statistics written from the same run."""
+    from ptarmigan_gb300 import hdf5
+    from ptarmigan_gb300.driver import run
+    src = tmp_path / "dump.yml"
+    text = INPUT.format(a0="2.0").replace("output:\n  ident: auto\n", "output:\n  ident: auto\n  dump_all_particles: hdf5\n")
+    src.write_text(text)
+    files = run(str(src), str(tmp_path / "out"), log=lambda *a: None)
+    h5 = [f for f in files if f.endswith("_particles.h5")]
+    assert [os.path.basename(f) for f in h5] == ["dump_particles.h5"]
+    f = hdf5.read(h5[0])["members"]
+    ph = f["final-state"]["members"]["photon"]["members"]
+    el = f["final-state"]["members"]["electron"]["members"]
+    assert el["weight"]["value"].size == 3000
+    stats = open(str(tmp_path / "out" / "dump_stats.txt")).read().splitlines()
+    total = float(stats[1].split("=")[1].split("[")[0])
+    assert np.sum(ph["weight"]["value"]) == pytest.approx(total, rel=1e-9)
+    assert ph["position"]["value"].shape == (ph["weight"]["value"].size, 4)
+    assert f["config"]["members"]["input-file"]["value"] == text
+    # momenta in GeV/c (units: hep): the photons are on shell
+    p = ph["momentum"]["value"]
+    assert np.allclose(p[:, 0] ** 2, np.sum(p[:, 1:] ** 2, axis=1), rtol=1e-9)
