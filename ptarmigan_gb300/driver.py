@@ -221,10 +221,16 @@ def run(path, output_dir="", engine=None, log=print):
         seed &= (1 << 64) - 1
         for a0 in a0s:
             laser = laser_from_input(inp, a0)
-            desc, n, species, angle, plane = beam_from_input(inp, laser)
             opts = options_from_input(inp, keep_decayed=False)
-            prim = eng.build_beam(desc, n, seed=seed)
-            host = {k: v.cpu().numpy() for k, v in prim.items()}
+            if inp.contains("beam:from_hdf5"):
+                host, loaded = beam_from_hdf5_input(inp, laser, path)
+                desc, n, species, angle, plane = None, len(host["species"]), loaded["species"], loaded["angle"], \
+                    loaded["plane"]
+            else:
+                desc, n, species, angle, plane = beam_from_input(inp, laser)
+                prim = eng.build_beam(desc, n, seed=seed)
+                host = {k: v.cpu().numpy() for k, v in prim.items()}
+                loaded = None
             out, st = eng.collide(laser, opts, host, seed=seed)
             log("a0 = %g: %d primaries -> %d particles (%d photons emitted, %d pairs), %.1f ms on the device"
                 % (a0, n, st["n_out"], st["emissions"], st["pair_events"], st["device_ms"]))
@@ -234,7 +240,7 @@ def run(path, output_dir="", engine=None, log=print):
                 cur0 = ident if len(a0s) == 1 else "%s%sa0_%.3f" % (ident, "_" if ident else "", a0)
                 fname = os.path.join(output_dir, cur0 + ("_" if cur0 else "") + "particles.h5")
                 write_particles_hdf5(fname, inp, path, laser, a0, desc, n, species, angle, plane, opts, out, units,
-                                     not beam_frame, seed)
+                                     not beam_frame, seed, loaded)
                 written.append(fname)
             import torch
             dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to("cuda:%d" % eng.device) for k, v in out.items()}
@@ -321,7 +327,7 @@ _SPECIES_NAME = {abi.ELECTRON: "electron", abi.POSITRON: "positron", abi.PHOTON:
 
 
 def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, angle, plane, opts, out, units,
-                         laser_defines_z, seed):
+                         laser_defines_z, seed, loaded=None):
     """The final-state file of main.rs:1289-1715: build information, the
     parsed configuration, and every final-state particle by species, in the
     output unit system, each dataset with its `unit` and `desc`
@@ -383,6 +389,20 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
                desc="polar angle between beam momentum and laser wavevector, zero if counterpropagating")
     bm.dataset("collision_plane_angle", float(plane), unit="rad",
                desc="azimuthal angle between beam momentum and laser wavevector, zero if p in E, k plane")
+    if desc is None:
+        # a beam loaded from file (main.rs:1446-1462)
+        bm.dataset("offset", hdf5.Vector(np.asarray(loaded["offset"]) * L.scale), unit=L.name)
+        bm.dataset("imported_from_file", True)
+        bm.dataset("distance_bt_ips", loaded["distance"] * L.scale, unit=L.name,
+                   desc="distance between particle beam source and focal spot")
+        bm.dataset("min_energy", loaded["min_energy"] * units.energy.scale, unit=units.energy.name,
+                   desc="primaries with energies below this threshold are discarded")
+        bm.dataset("max_angle", float(loaded["max_angle"]), unit="rad",
+                   desc="primaries propagating at angles larger than this are discarded")
+        _write_output_config(conf, opts, units, laser_defines_z)
+        _write_final_state(root, laser, out, units, focusing)
+        hdf5.write(fname, root)
+        return
     bm.dataset("offset", hdf5.Vector(np.asarray(list(desc.offset)) * L.scale), unit=L.name)
     bm.dataset("imported_from_file", False)
     bm.dataset("n_real", n * desc.weight, unit="1",
@@ -410,14 +430,23 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
                desc="Stokes parameters of the primary particles: I, Q, U, V", alias="polarisation")
     bm.dataset("transverse_distribution_is_normal", desc.radial_dstr != abi.RADIAL_UNIFORM)
     bm.dataset("longitudinal_distribution_is_normal", True)
+    _write_output_config(conf, opts, units, laser_defines_z)
+    _write_final_state(root, laser, out, units, focusing)
+    hdf5.write(fname, root)
+
+
+def _write_output_config(conf, opts, units, laser_defines_z):
     E = units.energy
     op = conf.group("output")
     op.dataset("laser_defines_positive_z", bool(laser_defines_z))
     op.dataset("beam_defines_positive_z", not laser_defines_z)
     op.dataset("discard_background_e", bool(opts.discard_bg_e))
     op.dataset("discard_background_ph", bool(opts.discard_bg_ph))
-    op.dataset("min_energy", opts.min_energy * ELECTRON_MASS_MEV * E.scale, unit=E.name)
+    op.dataset("min_energy", opts.min_energy * E.scale, unit=E.name)  # opts.min_energy is in MeV
 
+
+def _write_final_state(root, laser, out, units, focusing):
+    L, E = units.length, units.energy
     P = units.momentum
     fs = root.group("final-state")
 
@@ -471,4 +500,128 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
             lg.dataset("energy_flux", en[0], unit=en[1], desc="total energy of the laser pulse, per unit area")
     absorption = float(np.sum(out["weight"] * out["work"])) * ELECTRON_MASS_MEV * 1.0e6 * ELEMENTARY_CHARGE
     lg.dataset("absorption", absorption, unit="J", desc="energy absorbed from the laser")
-    hdf5.write(fname, root)
+
+
+# ------------------------------------------------------------ HDF5 load ---
+_LENGTH_UNITS = {"um": 1.0e6, "micron": 1.0e6, "mm": 1.0e3, "m": 1.0}
+_MOMENTUM_UNITS = {"MeV/c": 1.0, "MeV": 1.0, "GeV/c": 1.0e-3, "GeV": 1.0e-3,
+                   "kg/m/s": 1.0 / (1.0e6 * ELEMENTARY_CHARGE / SPEED_OF_LIGHT)}
+
+
+def _h5_get(tree, path):
+    node = tree
+    for part in path.split("/"):
+        if node.get("kind") != "group" or part not in node["members"]:
+            return None
+        node = node["members"][part]
+    return node
+
+
+def load_beam_hdf5(fname, species, distance, collision_angle, offset, auto_timing, min_energy, max_angle,
+                   initial_z):
+    """BeamLoader::build (particle/loader.rs:142-284) for files this
+    package's HDF5 module can read (its own final-state files, or files of
+    the same structures): the species' weight, position, momentum and
+    optional polarization in the file's units, rotated from the file's
+    beam axis onto the collision axis, shifted by the offset, propagated
+    between the interaction points (auto timing), and filtered by energy
+    (MeV) and angle.  Returns primaries for Engine.collide."""
+    tree = hdf5.read(fname)
+    sp = _SPECIES_NAME[species]
+
+    def need(path):
+        node = _h5_get(tree, path)
+        if node is None or node["kind"] != "dataset":
+            raise InputError("%s has no dataset %s" % (fname, path))
+        return node["value"]
+
+    x_unit = _LENGTH_UNITS.get(need("config/unit/position"))
+    p_unit = _MOMENTUM_UNITS.get(need("config/unit/momentum"))
+    if x_unit is None or p_unit is None:
+        raise InputError("%s: unrecognised position or momentum unit" % fname)
+
+    def flag(path):
+        node = _h5_get(tree, path)
+        return node is not None and node["kind"] == "dataset" and node["value"] is True
+
+    ca = _h5_get(tree, "config/beam/collision_angle")
+    ax = _h5_get(tree, "beam_axis")
+    if flag("config/output/beam_defines_positive_z"):
+        beam_axis = np.array([0.0, 0.0, 1.0])
+    elif flag("config/output/laser_defines_positive_z") and ca is not None:
+        beam_axis = np.array([-math.sin(ca["value"]), 0.0, -math.cos(ca["value"])])
+    elif ax is not None and ax["value"] in ("+x", "-x", "+z", "-z"):
+        beam_axis = {"+x": (1.0, 0.0, 0.0), "-x": (-1.0, 0.0, 0.0), "+z": (0.0, 0.0, 1.0),
+                     "-z": (0.0, 0.0, -1.0)}[ax["value"]]
+        beam_axis = np.array(beam_axis)
+    else:
+        beam_axis = np.array([0.0, 0.0, 1.0])  # the reference warns and assumes this
+    new_axis = np.array([-math.sin(collision_angle), 0.0, -math.cos(collision_angle)])
+    cross_y = beam_axis[2] * new_axis[0] - beam_axis[0] * new_axis[2]
+    theta = math.copysign(abs(math.acos(float(np.dot(new_axis, beam_axis)))), cross_y)
+
+    w = np.asarray(need("final-state/%s/weight" % sp), dtype=np.float64)
+    r = np.asarray(need("final-state/%s/position" % sp), dtype=np.float64).reshape(-1, 4) / x_unit
+    p = np.asarray(need("final-state/%s/momentum" % sp), dtype=np.float64).reshape(-1, 4) / p_unit
+    pol_node = _h5_get(tree, "final-state/%s/polarization" % sp)
+    m = min(len(w), len(r), len(p))
+    w, r, p = w[:m], r[:m], p[:m]
+    pol = (np.asarray(pol_node["value"], dtype=np.float64).reshape(-1, 4)[:m] if pol_node is not None
+           else np.tile([1.0, 0.0, 0.0, 0.0], (m, 1)))
+    u = p / ELECTRON_MASS_MEV
+
+    def rot_y(v):  # FourVector::rotate_around_y
+        sn, cs = math.sin(theta), math.cos(theta)
+        o = v.copy()
+        o[:, 1] = cs * v[:, 1] + sn * v[:, 3]
+        o[:, 3] = cs * v[:, 3] - sn * v[:, 1]
+        return o
+
+    u, r = rot_y(u), rot_y(r)
+    sa, ca_ = math.sin(collision_angle), math.cos(collision_angle)
+    ox, oy, oz = offset
+    r[:, 1] += ca_ * ox + sa * oz  # ThreeVector::rotate_around_y(angle) of the offset
+    r[:, 2] += oy
+    r[:, 3] += ca_ * oz - sa * ox
+    if auto_timing:
+        beta = u / u[:, :1]
+        den = (beta[:, 0] - beta[:, 3])[:, None]
+        lead = np.array([-1.0, sa, 0.0, ca_])
+        shift = distance * (lead[None, :] + (1.0 + ca_) * beta / den)
+        shift = shift - (2.0 * initial_z + r[:, :1] - r[:, 3:4]) * beta / den
+        r = r + shift
+    e = ELECTRON_MASS_MEV * u[:, 0]
+    n3 = u[:, 1:] / np.linalg.norm(u[:, 1:], axis=1, keepdims=True)
+    keep = (e > min_energy) & (n3 @ new_axis > math.cos(max_angle))
+    idx = np.nonzero(keep)[0].astype(np.uint64)
+    k = len(idx)
+    return {"species": np.full(k, species, dtype=np.int32), "r": np.ascontiguousarray(r[keep]),
+            "u": np.ascontiguousarray(u[keep]), "pol": np.ascontiguousarray(pol[keep]),
+            "weight": np.ascontiguousarray(w[keep]), "id": idx.copy(), "parent_id": idx.copy()}
+
+
+def beam_from_hdf5_input(inp, laser, input_path):
+    """main.rs:533-560: beam:from_hdf5 (file relative to the input file,
+    distance_bt_ips, auto_timing, min_energy in J, max_angle) with
+    beam:species, collision_angle and offset."""
+    species = SPECIES.get(inp.str("beam:species", "electron"))
+    if species is None:
+        raise InputError("beam:species must be electron, positron or photon")
+    fname = inp.str("beam:from_hdf5:file")
+    if not os.path.isabs(fname):
+        fname = os.path.join(os.path.dirname(os.path.abspath(input_path)), fname)
+    distance = inp.float("beam:from_hdf5:distance_bt_ips")
+    auto_timing = inp.bool("beam:from_hdf5:auto_timing", True)
+    min_energy = 1.0e-6 * inp.float("beam:from_hdf5:min_energy") / ELEMENTARY_CHARGE \
+        if inp.contains("beam:from_hdf5:min_energy") else 0.0
+    max_angle = inp.float("beam:from_hdf5:max_angle", math.pi)
+    angle = inp.float("beam:collision_angle", 0.0)
+    plane_s = inp.str("beam:collision_plane", "horizontal")
+    plane = {"horizontal": 0.0, "vertical": math.pi / 2}.get(plane_s)
+    if plane is None:
+        plane = inp.evaluate(plane_s)
+    offset = inp.floats("beam:offset", [0.0, 0.0, 0.0])
+    prim = load_beam_hdf5(fname, species, distance, angle, offset, auto_timing, min_energy, max_angle,
+                          engine_mod.laser_initial_z(laser))
+    return prim, {"species": species, "angle": angle, "plane": plane, "offset": offset, "distance": distance,
+                  "min_energy": min_energy, "max_angle": max_angle}

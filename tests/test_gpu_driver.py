@@ -113,3 +113,48 @@ def test_final_state_hdf5_dump(tmp_path):
     # momenta in GeV/c (units: hep): the photons are on shell
     p = ph["momentum"]["value"]
     assert np.allclose(p[:, 0] ** 2, np.sum(p[:, 1:] ** 2, axis=1), rtol=1e-9)
+
+
+STAGE2 = """---
+control:
+  lcfa: true
+  pair_creation: true
+  rng_seed: 3
+laser:
+  a0: 5.0
+  wavelength: 0.8 * micro
+  n_cycles: 8.0
+  polarization: linear
+beam:
+  species: photon
+  from_hdf5:
+    file: out/dump_particles.h5
+    distance_bt_ips: 0.0
+output:
+  ident: stage2
+  dump_all_particles: hdf5
+"""
+
+
+def test_staged_run_loads_the_dump(tmp_path):
+    """beam:from_hdf5 (particle/loader.rs): the photons of one run's
+    final-state file are the primaries of the next."""
+    from ptarmigan_gb300 import hdf5
+    from ptarmigan_gb300.driver import run
+    src = tmp_path / "dump.yml"
+    text = INPUT.format(a0="2.0").replace("output:\n  ident: auto\n", "output:\n  ident: auto\n  dump_all_particles: hdf5\n")
+    src.write_text(text)
+    run(str(src), str(tmp_path / "out"), log=lambda *a: None)
+    first = hdf5.read(str(tmp_path / "out" / "dump_particles.h5"))["members"]["final-state"]["members"]
+    n_photons = first["photon"]["members"]["weight"]["value"].size
+    assert n_photons > 100
+    src2 = tmp_path / "stage2.yml"
+    src2.write_text(STAGE2)
+    files = run(str(src2), str(tmp_path / "out2"), log=lambda *a: None)
+    second = hdf5.read([f for f in files if f.endswith("_particles.h5")][0])["members"]
+    assert second["config"]["members"]["beam"]["members"]["imported_from_file"]["value"] is True
+    fs = second["final-state"]["members"]
+    # photons leave as photons or as pairs; every primary is accounted for
+    n2 = fs["photon"]["members"]["id"]["value"]
+    assert n2.size + fs["electron"]["members"]["id"]["value"].size > 0
+    assert n2.size <= n_photons

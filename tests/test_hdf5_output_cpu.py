@@ -122,3 +122,55 @@ def test_laser_energy_matches_reference_test():
     assert driver.laser_energy(pw)[1] == "J/m^2"
     chirped = abi.laser_desc(abi.PLANE_WAVE, a0, wl, abi.LINEAR, abi.COS2, n_cycles=10.0, chirp_b=1e-3)
     assert driver.laser_energy(chirped) is None
+
+
+def _write_dump(tmp_path, laser_defines_z):
+    path = tmp_path / "run.yml"
+    path.write_text(INPUT)
+    inp = Input.from_file(str(path))
+    laser = driver.laser_from_input(inp, 5.0)
+    desc, n, species, angle, plane = driver.beam_from_input(inp, laser)
+    opts = driver.options_from_input(inp, keep_decayed=False)
+    out = _particles(np.random.default_rng(3))
+    out["u"][:, 0] = np.sqrt(1.0 + np.sum(out["u"][:, 1:] ** 2, axis=1)) + 1.0  # positive energies
+    fname = str(tmp_path / "dump.h5")
+    driver.write_particles_hdf5(fname, inp, str(path), laser, 5.0, desc, n, species, angle, plane, opts, out,
+                                UnitSystem.named("hep"), laser_defines_z, 1)
+    return fname, out
+
+
+def test_loader_reads_the_final_state_back(tmp_path):
+    """BeamLoader (particle/loader.rs:142-284) on this package's own file:
+    no rotation when the file's beam axis is the collision axis, no
+    timing shift without auto timing; ids are row indices."""
+    fname, out = _write_dump(tmp_path, laser_defines_z=True)
+    prim = driver.load_beam_hdf5(fname, abi.PHOTON, 0.0, 0.0, (0.0, 0.0, 0.0), False, 0.0, math.pi, 0.0)
+    sel = out["species"] == abi.PHOTON
+    assert np.allclose(prim["r"], out["r"][sel], rtol=1e-14, atol=1e-20)
+    assert np.allclose(prim["u"], out["u"][sel], rtol=1e-14)
+    assert np.array_equal(prim["pol"], out["pol"][sel])
+    assert np.array_equal(prim["id"], np.arange(sel.sum(), dtype=np.uint64))
+    # energy filter (MeV) and the offset
+    e = 0.510999 * out["u"][sel][:, 0]
+    es = np.sort(e)
+    cut = float(0.5 * (es[7] + es[8]))  # between two energies, clear of rounding
+    prim = driver.load_beam_hdf5(fname, abi.PHOTON, 0.0, 0.0, (1e-6, 0.0, 2e-6), False, cut, math.pi, 0.0)
+    assert len(prim["weight"]) == int(np.sum(e > cut))
+    keep = e > cut
+    assert np.allclose(prim["r"][:, 1], out["r"][sel][keep][:, 1] + 1e-6)
+    assert np.allclose(prim["r"][:, 3], out["r"][sel][keep][:, 3] + 2e-6)
+
+
+def test_loader_rotates_a_beam_defined_axis(tmp_path):
+    """A file whose beam defines +z is turned onto the collision axis -z (a
+    rotation by pi about y); auto timing moves particles along their
+    velocity, to a fixed light-cone coordinate t - z = -2 initial_z."""
+    fname, out = _write_dump(tmp_path, laser_defines_z=False)
+    sel = out["species"] == abi.ELECTRON
+    prim = driver.load_beam_hdf5(fname, abi.ELECTRON, 0.0, 0.0, (0.0, 0.0, 0.0), False, 0.0, math.pi, 0.0)
+    assert np.allclose(prim["u"][:, 1], -out["u"][sel][:, 1]) and np.allclose(prim["u"][:, 3], -out["u"][sel][:, 3])
+    assert np.allclose(prim["u"][:, 2], out["u"][sel][:, 2])
+    z0 = 5e-6
+    prim = driver.load_beam_hdf5(fname, abi.ELECTRON, 0.0, 0.0, (0.0, 0.0, 0.0), True, 0.0, math.pi, z0)
+    r = prim["r"]
+    assert np.allclose(r[:, 0] - r[:, 3], -2.0 * z0, atol=1e-18)
