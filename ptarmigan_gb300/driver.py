@@ -15,11 +15,12 @@ radius with its distribution and cutoff, length, collision_angle,
 collision_plane, rms_divergence, energy_chirp, offset, stokes_pars),
 output (ident, electron / photon / positron distributions, file_format,
 units, coordinate_system, discard_background(_e), min_energy, max_angle),
-stats (electron / photon / positron, and expressions), constants, and
+stats (electron / photon / positron, and expressions), constants,
 output:dump_all_particles: hdf5 (the final-state file of main.rs:1289-1715,
-written by ptarmigan_gb300.hdf5).
-Not supported: beam:spectrum, beam:from_hdf5, intermediate-particle
-output, increase_pair_rate_by: auto and stop_at_time: auto.
+written by ptarmigan_gb300.hdf5) and beam:from_hdf5 (particle/loader.rs,
+for files with the structures ptarmigan_gb300.hdf5 reads).
+Not supported: beam:spectrum, intermediate-particle output,
+increase_pair_rate_by: auto and stop_at_time: auto.
 """
 
 import math
