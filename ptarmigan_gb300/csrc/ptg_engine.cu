@@ -1109,6 +1109,12 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
                             const ptg_particles* d_in, uint64_t seed, uint64_t id_base, ptg_run_stats* stats) {
     ptg_status st = check_run(c, laser, o);
     if (st != PTG_OK) return st;
+    if (d_in && d_in->n == 0) {
+        // no primaries: an empty shower, as collide() mapped over none
+        c->d_out.n = 0;
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return PTG_OK;
+    }
     if (!d_in || !d_in->species || !d_in->r || !d_in->u)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
     bool lcfa = laser->model == PTG_FAST_PLANE_WAVE || laser->model == PTG_FAST_FOCUSED_LASER;
@@ -1248,6 +1254,10 @@ static ptg_status stage_primaries(ptg_ctx* c, const ptg_particles* h) {
     auto up = [&](void* dst, const void* src, size_t bytes) -> bool {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream) == cudaSuccess;
     };
+    if (n == 0) {
+        c->d_in.n = 0;
+        return PTG_OK;
+    }
     if (!h->species || !h->r || !h->u) return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
     bool ok = up(d.species, h->species, 4 * n) && up(d.r, h->r, 32 * n) && up(d.u, h->u, 32 * n);
     if (h->r0) ok = ok && up(d.r0, h->r0, 32 * n); else d.r0 = nullptr;

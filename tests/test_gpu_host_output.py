@@ -75,3 +75,34 @@ def test_empty_output_is_well_formed():
         assert st["n_out"] == 0
     finally:
         eng.close()
+
+
+def test_edge_batches():
+    """Zero primaries give an empty output; one primary runs alone; a
+    primary already past the pulse (phase beyond the field's extent) takes
+    no step and leaves unchanged; a batch of collisions may hold an empty
+    one."""
+    from ptarmigan_gb300 import build, engine
+    build.build()
+    eng = engine.Engine()
+    try:
+        laser, opts, prim = _batch(8, 6)
+        empty = {k: v[:0] for k, v in prim.items()}
+        out, st = eng.collide(laser, opts, empty, seed=1)
+        assert st["n_out"] == 0 and st["lepton_steps"] == 0 and out["u"].shape == (0, 4)
+        one = {k: v[:1] for k, v in prim.items()}
+        out, st = eng.collide(laser, opts, one, seed=1)
+        assert st["lepton_steps"] > 100 and st["particle_errors"] == 0 and out["u"].shape[0] >= 1
+        past = {k: v[:1].copy() for k, v in prim.items()}
+        past["r"][0] = [0.0, 0.0, 0.0, -1.0]  # k (t - z) far beyond the pulse
+        out, st = eng.collide(laser, opts, past, seed=1)
+        assert st["lepton_steps"] == 0 and out["u"].shape[0] == 1
+        assert np.array_equal(out["u"][0], past["u"][0]) and np.array_equal(out["r"][0], past["r"][0])
+        colls = [{"laser": laser, "seed": 3, "id_base": 100, "first": 0, "count": 4},
+                 {"laser": laser, "seed": 4, "id_base": 200, "first": 4, "count": 0},
+                 {"laser": laser, "seed": 5, "id_base": 300, "first": 4, "count": 4}]
+        parts, stats, total = eng.collide_multi(colls, opts, prim)
+        assert len(parts) == 3 and parts[1]["u"].shape[0] == 0 and stats[1]["lepton_steps"] == 0
+        assert total["particle_errors"] == 0 and parts[0]["u"].shape[0] >= 4 and parts[2]["u"].shape[0] >= 4
+    finally:
+        eng.close()
