@@ -37,8 +37,12 @@ __device__ __forceinline__ float reduced_phase(double ph) {
 }
 
 // Salamin beam (fast_focused_laser.rs:59-111) in FP32, normalised to E0.
-// (cr, sr) rotate by the polarisation angle.
-__device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr, double sr, float c, float s,
+// (cr, sr) rotate by the polarisation angle.  Returns false, with zero
+// fields, where the transverse Gaussian exp(-rho^2 / (1 + z^2)) is below
+// e^-110: there the FP32 factor is an exact zero and so would every field
+// component be (a particle far off axis, e.g. a photon emitted at a large
+// angle, then steps without evaluating the beam).
+__device__ __forceinline__ bool ffl_beam32(const FieldParams& f, d4 r, double cr, double sr, float c, float s,
                                            f3* reE, f3* imE, f3* reB, f3* imB) {
     double rx = cr * r.x + sr * r.y;
     double ry = cr * r.y - sr * r.x;
@@ -47,6 +51,10 @@ __device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr
     float e = f.eps32, e2 = e * e, e3 = e2 * e, e4 = e2 * e2;
     float den = 1.0f / (1.0f + z * z);
     cf fc = cf{den, z * den};
+    if (fc.re * rho2 > 110.0f) {
+        *reE = *imE = *reB = *imB = f3{0.0f, 0.0f, 0.0f};
+        return false;
+    }
     float ex = expf(-fc.re * rho2);
     float ph = reduced_phase(f.k * r.t - f.k * r.z);
     float sn, cs;
@@ -81,6 +89,7 @@ __device__ __forceinline__ void ffl_beam32(const FieldParams& f, d4 r, double cr
     *imE = f3{c * Ex.im - s * Ey.im, c * Ey.im + s * Ex.im, Ez.im};
     *reB = f3{-s * By.re, c * By.re, Bz.re};
     *imB = f3{-s * By.im, c * By.im, Bz.im};
+    return true;
 }
 
 // Normalised fields at r (e = E/E0, b = cB/E0).  Returns false where the
@@ -147,7 +156,11 @@ __device__ __forceinline__ bool lcfa_fields32(const FieldParams& f, d4 r, f3* e,
         env = (float)de, denv = (float)dd;
     }
     f3 reE, imE, reB, imB;
-    ffl_beam32(f, r, f.cos_pa, f.sin_pa, f.cos_pa32, f.sin_pa32, &reE, &imE, &reB, &imB);
+    if (!ffl_beam32(f, r, f.cos_pa, f.sin_pa, f.cos_pa32, f.sin_pa32, &reE, &imE, &reB, &imB)) {
+        *e = f3{0.f, 0.f, 0.f};
+        *b = f3{0.f, 0.f, 0.f};
+        return false;
+    }
     f3 ee = f3add(f3scale(env, reE), f3scale(denv, imE));
     f3 bb = f3add(f3scale(env, reB), f3scale(denv, imB));
     if (f.circular) {
