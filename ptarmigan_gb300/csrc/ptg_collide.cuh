@@ -119,6 +119,20 @@ __device__ __forceinline__ bool lane_untracked(const WaveArgs& a, const Lane& L)
     return (!a.o.tracking_secondaries && L.gen > 0) || (a.o.max_generation >= 0 && L.gen > a.o.max_generation);
 }
 
+// Steps after which a particle that is still inside the field is retired
+// with PTG_ERR_REJECTION_CAP (an iteration cap).  The reference steps until
+// the particle leaves the field, which a particle co-moving with the laser
+// (its phase k(t - z) advancing by ever less) may never do; every
+// configuration measured here stays below 1e6 steps per particle.
+constexpr uint32_t STEP_CAP = 1u << 26;
+
+// True when the lane's particle is finished before its next step: failed,
+// untracked, or at the step cap (which marks it failed).
+__device__ __forceinline__ bool lane_stops(const WaveArgs& a, Lane& L) {
+    if (L.status == ST_OK && L.step >= STEP_CAP) L.status = ST_REJECTION_CAP;
+    return L.status != ST_OK || lane_untracked(a, L);
+}
+
 __device__ __forceinline__ void spawn(const WaveArgs& a, unsigned long long slot, int species, d4 r, d4 u, d4 u0,
                                       d4 pol, double weight, double payload, double parent_chi, double work,
                                       unsigned long long parent_id, unsigned long long primary,
@@ -513,7 +527,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
     for (;;) {
         if (have) {
             bool done;
-            if (L.status != ST_OK || lane_untracked(a, L)) {
+            if (lane_stops(a, L)) {
                 done = true;
             } else if (L.species != SP_PHOTON) {
                 done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));

@@ -121,7 +121,7 @@ template <int MODEL>
 static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, PartCounts& pc) {
     for (;;) {
         bool done;
-        if (L.status != ST_OK || lane_untracked(a, L)) {
+        if (lane_stops(a, L)) {
             done = true;
         } else if (L.species != SP_PHOTON) {
             done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
@@ -209,7 +209,7 @@ __device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs&
 // the particle is done.
 template <int MODEL>
 __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCounts& pc) {
-    if (L.status != ST_OK || lane_untracked(a, L)) return true;
+    if (lane_stops(a, L)) return true;
     if (L.species != SP_PHOTON) {
         if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop))) return true;
         lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
