@@ -160,6 +160,11 @@ class Dataset:
         return self
 
 
+def _check_name(name):
+    if not name or "/" in name or "\0" in name or name in (".", ".."):
+        raise ValueError("invalid link name %r" % name)
+
+
 class Group:
     def __init__(self):
         self.children = {}
@@ -168,6 +173,7 @@ class Group:
         self.addr = None
 
     def group(self, name):
+        _check_name(name)
         g = self.children.get(name)
         if g is None:
             g = self.children[name] = Group()
@@ -177,6 +183,11 @@ class Group:
         return g
 
     def dataset(self, name, value, unit=None, desc=None, alias=None):
+        _check_name(name)
+        if alias is not None:
+            _check_name(alias)
+            if alias in self.children or alias == name:
+                raise ValueError("%r exists" % alias)
         if name in self.children:
             raise ValueError("%r exists" % name)
         d = Dataset(value)
@@ -263,8 +274,9 @@ class _Writer:
         seg_addr = self.alloc(bytes(seg))
         heap = b"HEAP" + bytes([0, 0, 0, 0]) + struct.pack("<QQQ", len(seg), HEAP_FREE_NULL, seg_addr)
         heap_addr = self.alloc(heap)
-        # symbol-table nodes of at most 2 * LEAF_K entries
-        chunks = [names[i:i + 2 * LEAF_K] for i in range(0, len(names), 2 * LEAF_K)] or [[]]
+        # symbol-table nodes of at most 2 * LEAF_K entries (none for an empty
+        # group, whose B-tree node then has no children)
+        chunks = [names[i:i + 2 * LEAF_K] for i in range(0, len(names), 2 * LEAF_K)]
         if len(chunks) > 2 * INTERNAL_K:
             raise ValueError("group with more than %d members" % (4 * LEAF_K * INTERNAL_K))
         snods = []
@@ -277,8 +289,7 @@ class _Writer:
         tree = bytearray(b"TREE" + bytes([0, 0]) + struct.pack("<HQQ", len(chunks), UNDEF, UNDEF))
         tree += struct.pack("<Q", 0)
         for chunk, addr in zip(chunks, snods):
-            last = off[chunk[-1]] if chunk else 0
-            tree += struct.pack("<QQ", addr, last)
+            tree += struct.pack("<QQ", addr, off[chunk[-1]])
         tree += b"\0" * (TREE_SIZE - len(tree))
         tree_addr = self.alloc(bytes(tree))
         msgs = [_message(MSG_STAB, struct.pack("<QQ", tree_addr, heap_addr))]

@@ -125,3 +125,27 @@ def test_rejects_unsupported(tmp_path):
         root.dataset("x", 2.0)
     with pytest.raises(ValueError):
         root.group("x")
+
+
+def test_names_and_text(tmp_path):
+    """Link names are checked; UTF-8 text and names that sort by byte
+    (upper case before lower) round-trip; an empty group is readable."""
+    root = hdf5.Group()
+    for bad in ("", "a/b", ".", ".."):
+        with pytest.raises(ValueError):
+            root.dataset(bad, 1.0)
+    root.dataset("x", 1.0)
+    with pytest.raises(ValueError):
+        root.dataset("y", 2.0, alias="x")
+    g = root.group("names")
+    for name in ("b", "B", "a", "A", "_", "Z9", "z"):
+        g.dataset(name, name)
+    root.group("empty")
+    root.dataset("text", "µm, γ and χ")
+    path = tmp_path / "n.h5"
+    hdf5.write(str(path), root)
+    r = hdf5.read(str(path))["members"]
+    assert list(r["names"]["members"]) == sorted(["b", "B", "a", "A", "_", "Z9", "z"], key=lambda s: s.encode())
+    assert all(v["value"] == k for k, v in r["names"]["members"].items())
+    assert r["empty"]["kind"] == "group" and r["empty"]["members"] == {}
+    assert r["text"]["value"] == "µm, γ and χ"
