@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define PTG_ABI_VERSION 1
+#define PTG_ABI_VERSION 2
 
 typedef enum {
     PTG_OK = 0,
@@ -148,6 +148,12 @@ typedef struct {
     uint32_t ordered_waves;    /* of which put in order of laser phase first (three small kernels each) */
     double absorbed_energy;    /* sum of work over all particles, MeV */
     double device_ms;          /* kernel time of the batch */
+    uint64_t max_steps;        /* most steps any one particle took */
+    uint64_t free_steps;       /* of lepton_steps + photon_steps, those that only drifted: outside the pulse
+                                  (where the field or <a^2> is below every bit the step could change), or a
+                                  photon whose pair probability is zero wherever it goes */
+    double wave_ms[8];         /* device time of each wave kernel (waves past the eighth add to the last
+                                  entry); zero for the queue, which runs no waves */
 } ptg_run_stats;
 
 typedef struct ptg_ctx ptg_ctx;
@@ -218,12 +224,16 @@ void ptg_particles_free(ptg_particles* p);
  * PTG_ERR_INVALID_ARGUMENT) and at most 32768 particles in a batch's
  * showers, primaries included (more is PTG_ERR_QUEUE_OVERFLOW); a result
  * longer than out_capacity is PTG_ERR_QUEUE_OVERFLOW with the needed row
- * count in stats->n_out.
+ * count in stats->n_out.  An empty batch (n = 0) gives an empty result.
  *
- * The first call on each device sets that device up (it looks up the
- * array's device address and uploads constants, with the device current);
- * make that first call before any stream capture.  All calls share the
- * array, and each call clears what must start at zero, so calls that
+ * Every call looks up the array's device address in the current context
+ * (cudaGetSymbolAddress, with the caller's device current) and uploads
+ * 2.6 KB of constants into it on `stream`.  It waits for `stream` after
+ * every wave, reading the wave's counters back to the host, so it returns
+ * when its work is done.  Waves run in slot order, not in order of laser
+ * phase as ptg_collide_batch_device runs its large waves; the results are
+ * the same, since each particle's random stream is fixed.  All calls share
+ * the array, and each call clears what must start at zero, so calls that
  * overlap on the GPU (concurrent streams or host threads) race: serialise
  * them. */
 ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_collide_options* opts,
@@ -295,6 +305,32 @@ ptg_status ptg_laser_initial_z(const ptg_laser_desc* laser, double* z0);
 
 /* The CUDA stream the context launches on (a cudaStream_t). */
 void* ptg_context_stream(ptg_ctx* ctx);
+
+/* Bounds on the work any one particle, sample or wait may take.  The
+ * reference has none: it steps a particle until it leaves the field and
+ * repeats a rejection loop until it accepts (its samplers panic on the rare
+ * inputs where they cannot), so a run there may not end; here every loop is
+ * bounded and a particle that reaches a bound is retired with a
+ * per-particle status, counted in ptg_run_stats.particle_errors.  Zero
+ * selects the default; lower values are for exercising those exits.
+ *   queue_wait_ns  any single wait of the queue kernel for a slot (default
+ *                  20 s + 2 us per primary): a wait that runs out ends the
+ *                  batch with PTG_ERR_TIMEOUT and leaves the context usable;
+ *   step_cap       steps after which a particle still in the field is
+ *                  retired with PTG_ERR_REJECTION_CAP (default 2^26; a
+ *                  photon whose pair probability is zero wherever it goes
+ *                  is moved to its exit in closed form and not capped);
+ *   rejection_cap  iterations of any rejection loop of the collision
+ *                  kernels' samplers, after which the particle is retired
+ *                  with PTG_ERR_REJECTION_CAP (default 65536, at most 2^30).
+ * `current` (may be NULL) receives the limits in force. */
+typedef struct {
+    uint64_t queue_wait_ns;
+    uint32_t step_cap;
+    uint32_t rejection_cap;
+    uint64_t reserved;
+} ptg_limits;
+ptg_status ptg_context_set_limits(ptg_ctx* ctx, const ptg_limits* limits, ptg_limits* current);
 
 /* Diagnostics entry points used by the parity tests: evaluate one field
  * model's E, B, a at n positions, and push n particles one step

@@ -507,6 +507,13 @@ static double rqm_of(int species) {
 }
 
 // main.rs:134-289
+// A bound on any one particle's steps, so that a run of the oracle always
+// ends: the reference steps a particle until it leaves the field, which a
+// photon moving almost with the laser (its phase k(t - z) advancing by ever
+// less) may take without limit to do.  A particle at the bound is retired
+// with PTG_ERR_REJECTION_CAP, as the device's own step cap does.
+constexpr uint32_t ORACLE_STEP_CAP = 1u << 26;
+
 void collide(const Laser& laser, const ptg_collide_options& o, const OracleParticle& incident, uint64_t seed,
              uint64_t* current_id, std::vector<OracleParticle>& out, OracleStats& st) {
     std::vector<OracleParticle> stack;
@@ -536,6 +543,10 @@ void collide(const Laser& laser, const ptg_collide_options& o, const OracleParti
         if (pt.species != PTG_PHOTON) {
             double rqm = rqm_of(pt.species);
             while (laser.contains(pt.r) && pt.r.t / SPEED_OF_LIGHT < t_stop) {
+                if (step >= ORACLE_STEP_CAP) {
+                    pt.status = PTG_ERR_REJECTION_CAP;
+                    break;
+                }
                 rng.begin_step(step);
                 V4 r, u;
                 double dt_actual, work;
@@ -582,6 +593,10 @@ void collide(const Laser& laser, const ptg_collide_options& o, const OracleParti
         } else {
             bool decayed = false;
             while (laser.contains(pt.r) && pt.r.t / SPEED_OF_LIGHT < t_stop && !decayed && o.tracking_photons) {
+                if (step >= ORACLE_STEP_CAP) {
+                    pt.status = PTG_ERR_REJECTION_CAP;
+                    break;
+                }
                 rng.begin_step(step);
                 V4 ell = pt.u;
                 V4 r = pt.r + SPEED_OF_LIGHT * ell * dt / ell.t;

@@ -20,6 +20,7 @@ PTG_ERR_NO_DEVICE = 7
 PTG_ERR_TABLES = 8
 PTG_ERR_UNSUPPORTED = 9
 PTG_ERR_ALLOC = 10
+PTG_ERR_TIMEOUT = 11
 
 PLANE_WAVE, FAST_PLANE_WAVE, FOCUSED_LASER, FAST_FOCUSED_LASER = 0, 1, 2, 3
 LINEAR, CIRCULAR = 0, 1
@@ -111,10 +112,15 @@ class RunStats(C.Structure):
         ("ordered_waves", C.c_uint32),
         ("absorbed_energy", C.c_double),
         ("device_ms", C.c_double),
+        ("max_steps", C.c_uint64),
+        ("free_steps", C.c_uint64),
+        ("wave_ms", C.c_double * 8),
     ]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name not in ("reserved", "wave_ms")}
+        d["wave_ms"] = [float(x) for x in self.wave_ms]
+        return d
 
 
 class Collision(C.Structure):
@@ -139,6 +145,20 @@ class QueueCfg(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Limits(C.Structure):
+    """ptg_limits: bounds on a particle's steps, a rejection loop and a
+    queue wait (0 = the default)."""
+    _fields_ = [
+        ("queue_wait_ns", C.c_uint64),
+        ("step_cap", C.c_uint32),
+        ("rejection_cap", C.c_uint32),
+        ("reserved", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 
 class MlpTrainCfg(C.Structure):

@@ -228,7 +228,7 @@ static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta
     mx *= 1.5;
     double s = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double ss = s_min + (s_max - s_min) * rng.next();
         double z = mx * rng.next();
         double re, im;
@@ -239,14 +239,14 @@ static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;
+    if (it == rng.cap) return 4;
     if (rng.next() < 0.5) s = 1.0 - s;
     double theta_opt = 0.5 * atan2(sv2, sv1);
     double tm = -HUGE_VAL;
     for (int i = 0; i < 4; ++i) tm = fmax(tm, bw_fully_resolved(n, a, eta, s, theta_opt + i * FRAC_PI_2, sv1, sv2, sv3));
     tm *= 1.01;
     double theta = 0.0;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double th = 2.0 * PI * rng.next();
         double z = tm * rng.next();
         if (z < bw_fully_resolved(n, a, eta, s, th, sv1, sv2, sv3)) {
@@ -255,7 +255,7 @@ static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;
+    if (it == rng.cap) return 4;
     *s_out = s;
     *theta_out = theta;
     return 0;

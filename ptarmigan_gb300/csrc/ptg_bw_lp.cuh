@@ -346,7 +346,7 @@ static __device__ __noinline__ int lpp_sample_s_theta(const DbGeom& g, const DbW
     mx *= 1.2;
     double s = 0.0, theta = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double ss = s_min + (s_max - s_min) * rng.next();
         double th = (PI / 2.0) * rng.next();
         if (th > tb.at(ss)) continue;
@@ -357,7 +357,7 @@ static __device__ __noinline__ int lpp_sample_s_theta(const DbGeom& g, const DbW
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;
+    if (it == rng.cap) return 4;
     if ((int)(2.0 * rng.next()) == 0) s = 1.0 - s;
     int quadrant = (int)(4.0 * rng.next());
     if (quadrant == 1)

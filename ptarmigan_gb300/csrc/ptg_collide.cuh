@@ -40,6 +40,8 @@ struct Counters {
     unsigned long long n_out;    // compaction cursor
     unsigned long long completed; // queue: slots finished (children appended)
     unsigned long long timeouts;  // queue: bounded waits that ran out
+    unsigned long long max_steps; // most steps any one particle took
+    unsigned long long free_steps; // steps that only drifted (outside the pulse, drifting photons)
 };
 
 struct StepOptions {
@@ -57,6 +59,8 @@ struct StepOptions {
     int max_generation;       // -1: no limit
     int keep_decayed;
     int has_t_stop;           // t_stop is finite
+    uint32_t step_cap;        // steps after which a particle still in the field is retired
+    int rej_cap;              // iterations any rejection loop may take
 };
 
 struct WaveArgs {
@@ -119,17 +123,18 @@ __device__ __forceinline__ bool lane_untracked(const WaveArgs& a, const Lane& L)
     return (!a.o.tracking_secondaries && L.gen > 0) || (a.o.max_generation >= 0 && L.gen > a.o.max_generation);
 }
 
-// Steps after which a particle that is still inside the field is retired
-// with PTG_ERR_REJECTION_CAP (an iteration cap).  The reference steps until
-// the particle leaves the field, which a particle co-moving with the laser
-// (its phase k(t - z) advancing by ever less) may never do; every
-// configuration measured here stays below 1e6 steps per particle.
+// Default number of steps after which a particle that is still inside the
+// field is retired with PTG_ERR_REJECTION_CAP (an iteration cap; the
+// context's limits may lower it).  The reference steps until the particle
+// leaves the field, which a particle co-moving with the laser (its phase
+// k(t - z) advancing by ever less) may never do; every configuration
+// measured here stays below 1e6 steps per particle.
 constexpr uint32_t STEP_CAP = 1u << 26;
 
 // True when the lane's particle is finished before its next step: failed,
 // untracked, or at the step cap (which marks it failed).
 __device__ __forceinline__ bool lane_stops(const WaveArgs& a, Lane& L) {
-    if (L.status == ST_OK && L.step >= STEP_CAP) L.status = ST_REJECTION_CAP;
+    if (L.status == ST_OK && L.step >= a.o.step_cap) L.status = ST_REJECTION_CAP;
     return L.status != ST_OK || lane_untracked(a, L);
 }
 
@@ -182,10 +187,10 @@ __device__ __forceinline__ void retire_overflow(const WaveArgs& a, unsigned long
     }
 }
 
-// One charged-particle step: main.rs:170-206.  Returns false when the
-// particle is finished.
+// One charged-particle step: main.rs:170-206.  Returns true when the step
+// only drifted (outside the pulse).
 template <int MODEL, bool QUEUE = false>
-__device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit,
+__device__ __forceinline__ bool lepton_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* nemit,
                                             LpDefer* dfr = nullptr) {
     const FieldParams& f = a.f;
     double rqm = (L.species == SP_ELECTRON ? ELECTRON_CHARGE : -ELECTRON_CHARGE) / ELECTRON_MASS;
@@ -193,11 +198,12 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
     d4 r, u;
     double dt_actual, dwork;
     Draws rng;
-    rng.begin(a.seed, L.stream, L.step);
+    rng.begin(a.seed, L.stream, L.step, a.o.rej_cap);
     bool emitted = false;
     d4 k = d4{0, 0, 0, 0}, upr = d4{0, 0, 0, 0};
     d3 kpol = mk3(0, 0, 0);
     double a_eff = 0.0, chi = 0.0, absorption = 0.0;
+    bool free_step = false;
     if (MODEL == M_FAST_PLANE_WAVE || MODEL == M_FAST_FOCUSED_LASER) {
         // Field::push default (field/mod.rs:147-152); h = c dt / (2 u^0) was
         // computed by the previous step (or at load)
@@ -215,6 +221,7 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             r = d4{rh.t + h2 * u.t, rh.x + h2 * u.x, rh.y + h2 * u.y, rh.z + h2 * u.z};
             dwork = 0.0;
             L.hh = h2;
+            free_step = true;
         } else {
             d3 E, B;
             double aa;
@@ -270,6 +277,13 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
             }
         }
     } else {
+        if (lma_step_field_free(f, L.r, dt)) {
+            // outside the pulse: the step only drifts, and its emission
+            // probability (proportional to <a^2> < 2^-60) is below every
+            // nonzero uniform, so it draws nothing
+            lma_push_field_free(L.r, L.u, dt, &L.r, &L.u, &dt_actual);
+            return true;
+        }
         lma_push(f, L.r, L.u, rqm, dt, a.o.eqn, &r, &u, &dt_actual, &dwork);
         DbWork dbw{nullptr, 0, 32};
         if (a.dbw) {
@@ -280,12 +294,12 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
         }
         int st = lma_radiate(f, *a.lma, dbw, a.mlp, r, u, dt_actual, rng, a.o.classical_mode != 0, &emitted, &k, &upr,
                              &kpol, &a_eff, &chi, &absorption, rej, dfr);
-        if (st == LMA_DEFERRED) return;  // the step repeats once the warp has sampled
+        if (st == LMA_DEFERRED) return false;  // the step repeats once the warp has sampled
         if (st != ST_OK) {
             L.status = st;
             L.r = r;
             L.u = u;
-            return;
+            return false;
         }
     }
     if (emitted) {
@@ -309,6 +323,66 @@ __device__ __forceinline__ void lepton_step(const WaveArgs& a, Lane& L, uint32_t
     L.r = r;
     L.u = u;
     L.work += dwork;
+    return free_step;
+}
+
+// Steps of a drifting photon taken one by one before the rest of its path
+// is found in closed form.
+constexpr uint32_t DRIFT_EXACT = 1u << 18;
+
+// True for a photon whose pair probability is zero on every step it has
+// left: an LCFA photon below the field's drift threshold, unpolarised as the
+// step sees it (pol_resolved off).
+__device__ __forceinline__ bool photon_drifts(const WaveArgs& a, const Lane& L) {
+    return L.species == SP_PHOTON && !a.o.pol_resolved && L.u.t < a.f.drift_ell_max;
+}
+
+// The rest of a drifting photon's path (main.rs:212-264 with a pair
+// probability of exactly zero): the step then leaves ell, the weight, the
+// Stokes vector and the interaction count as they are and draws nothing, so
+// it is r += (c dt / ell^0) ell until the photon leaves the field
+// (Field::contains) or reaches t_stop.  The first DRIFT_EXACT steps repeat
+// photon_step's additions, so r is bit for bit what stepping gives; a
+// photon still inside after them (one moving nearly with the laser, whose
+// phase k(t - z) advances by ever less) jumps to a few steps short of its
+// exit in closed form, r += (m h) ell, with a relative error of a few
+// ulps times the steps it jumps, and takes the last steps one by one.
+// Returns the steps taken; a photon whose phase cannot advance is retired
+// at the step cap.
+static __device__ __noinline__ unsigned long long photon_drift(const WaveArgs& a, Lane& L) {
+    const FieldParams& f = a.f;
+    const double h = L.hph;
+    const d4 ell = L.u;
+    d4 r = L.r;
+    unsigned long long steps = 0;
+    auto inside = [&](const d4& p) {
+        return contains(f, p) && (!a.o.has_t_stop || p.t / SPEED_OF_LIGHT < a.o.t_stop);
+    };
+    for (int jump = 0; jump < 4; ++jump) {
+        for (uint32_t k = 0; k < DRIFT_EXACT; ++k) {
+            if (!inside(r)) {
+                L.r = r;
+                return steps;
+            }
+            r = d4{r.t + h * ell.t, r.x + h * ell.x, r.y + h * ell.y, r.z + h * ell.z};
+            ++steps;
+        }
+        // steps left to the exit: the phase advances by k h (ell^0 - ell_z)
+        // per step, the time by h ell^0
+        double dphase = f.k * h * (ell.t - ell.z);
+        double left = dphase > 0.0 ? (f.max_phase - phase_of(f, r)) / dphase : HUGE_VAL;
+        if (a.o.has_t_stop) left = fmin(left, (a.o.t_stop * SPEED_OF_LIGHT - r.t) / (h * ell.t));
+        if (!(left < 4503599627370496.0)) break;  // 2^52: the photon cannot leave
+        double m = floor(left) - 4.0;
+        if (m > 0.0) {
+            double hm = h * m;
+            r = d4{r.t + hm * ell.t, r.x + hm * ell.x, r.y + hm * ell.y, r.z + hm * ell.z};
+            steps += (unsigned long long)m;
+        }
+    }
+    L.r = r;
+    L.status = ST_REJECTION_CAP;
+    return steps;
 }
 
 // One photon step: main.rs:214-256.
@@ -317,7 +391,7 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
     const FieldParams& f = a.f;
     double dt = a.o.dt;
     Draws rng;
-    rng.begin(a.seed, L.stream, L.step);
+    rng.begin(a.seed, L.stream, L.step, a.o.rej_cap);
     d4 ell = L.u;
     double h = L.hph;  // c dt / ell^0, fixed for a photon
     d4 r = d4{L.r.t + h * ell.t, L.r.x + h * ell.x, L.r.y + h * ell.y, L.r.z + h * ell.z};
@@ -512,8 +586,8 @@ template <int MODEL>
 __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
     constexpr bool LMA = MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER;
     Lane L;
-    uint32_t rej = 0, nemit = 0, npair = 0;
-    unsigned long long lsteps = 0, psteps = 0, nerr = 0;
+    uint32_t rej = 0, nemit = 0, npair = 0, maxst = 0;
+    unsigned long long lsteps = 0, psteps = 0, fsteps = 0, nerr = 0;
     LpDefer* dfr = nullptr;
     if constexpr (LMA) {
         __shared__ LpDefer s_dfr[128];
@@ -532,17 +606,25 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
             } else if (L.species != SP_PHOTON) {
                 done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
                 if (!done) {
-                    lepton_step<MODEL>(a, L, &rej, &nemit, dfr);
+                    bool fr = lepton_step<MODEL>(a, L, &rej, &nemit, dfr);
                     if (dfr == nullptr || dfr->pend != 1) {
                         ++L.step;
                         ++lsteps;
+                        fsteps += fr ? 1ull : 0ull;
                         done = L.status != ST_OK;
                     }
                 }
             } else {
                 done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) &&
                          !L.decayed && a.o.tracking_photons);
-                if (!done) {
+                if (!done && photon_drifts(a, L)) {
+                    unsigned long long ds = photon_drift(a, L);
+                    psteps += ds;
+                    fsteps += ds;
+                    ds += L.step;
+                    L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
+                    done = true;
+                } else if (!done) {
                     photon_step<MODEL>(a, L, &rej, &npair);
                     ++L.step;
                     ++psteps;
@@ -551,6 +633,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
             }
             if (done) {
                 if (L.status != ST_OK) ++nerr;
+                maxst = L.step > maxst ? L.step : maxst;
                 // a decayed photon leaves the output, or becomes an intermediate
                 if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
                 lane_store(a, L);
@@ -576,14 +659,18 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
     for (int o = 16; o > 0; o >>= 1) {
         lsteps += __shfl_down_sync(m, lsteps, o);
         psteps += __shfl_down_sync(m, psteps, o);
+        fsteps += __shfl_down_sync(m, fsteps, o);
         nerr += __shfl_down_sync(m, nerr, o);
         rej += __shfl_down_sync(m, rej, o);
         nemit += __shfl_down_sync(m, nemit, o);
         npair += __shfl_down_sync(m, npair, o);
     }
+    maxst = __reduce_max_sync(m, maxst);
     if (lane_id() == 0) {
+        if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
         atomicAdd(&a.c->lepton_steps, lsteps);
         atomicAdd(&a.c->photon_steps, psteps);
+        atomicAdd(&a.c->free_steps, fsteps);
         atomicAdd(&a.c->errors, nerr);
         atomicAdd(&a.c->rejections, (unsigned long long)rej);
         atomicAdd(&a.c->emissions, (unsigned long long)nemit);

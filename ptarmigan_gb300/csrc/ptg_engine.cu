@@ -49,6 +49,7 @@ struct ptg_ctx {
     int blocks_per_sm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_wa = nullptr, ev_wb = nullptr;  // around each wave launch
     // shower store
     Store s{};
     void* store_mem = nullptr;
@@ -109,6 +110,7 @@ struct ptg_ctx {
     float mlp_margin = 0.25f;
     cudaGraphExec_t q_graph = nullptr;
     std::string q_graph_key;
+    ptg_limits limits{0, 0, 0, 0};
 };
 
 // ------------------------------------------------------------ helpers ---
@@ -189,6 +191,36 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     if (d.model == PTG_FAST_FOCUSED_LASER && d.envelope == PTG_ENV_GAUSSIAN) {
         double tau = f.omega * f.duration;
         f.env_cut = tau * std::sqrt(18.0 * std::log(10.0) / (2.0 * LN_2));
+    }
+    // Photons that only drift.  In the LCFA models the transverse field a
+    // photon sees, |E - (E.n) n + n x cB|, is at most 8 times the field
+    // scale: E and cB are each below 2.2 times it (the two beams of
+    // circular polarisation, the envelope's derivative and the Gaussian
+    // beam's corrections of order eps^2 and beyond included).  So chi <= 8
+    // ell^0 chi_scale, and a photon with ell^0 < drift_ell_max has chi <
+    // 0.01 on every step, where T(chi) = 0 (lcfa/pair_creation/mod.rs:13-18):
+    // its pair probability is exactly zero wherever it goes.  Chirped plane
+    // waves are left out (their carrier frequency grows along the pulse).
+    f.drift_ell_max = 0.0;
+    if (lcfa && f.chirp_b == 0.0) f.drift_ell_max = 0.01 / (8.0 * f.chi_scale);
+    // LMA models: the phase beyond which <a^2> < 2^-60 everywhere (the
+    // beam factor of the focused model is at most 1).  cos^2 and flattop
+    // envelopes vanish exactly beyond pi nc and pi (nc + 1); the Gaussian
+    // ones fall below 2^-60 / max(1, norm a0^2).  Chirped plane waves and
+    // the finite-bandwidth option (which draws a width on every step) are
+    // left out.
+    f.lma_cut = 0.0;
+    if (!lcfa && f.chirp_b == 0.0 && !d.finite_bandwidth) {
+        double norm = f.circular ? 1.0 : 0.5;
+        double lnk = 60.0 * LN_2 + std::log(std::fmax(1.0, norm * d.a0 * d.a0));
+        if (d.envelope == PTG_ENV_COS2)
+            f.lma_cut = PI * nc;
+        else if (d.envelope == PTG_ENV_FLATTOP)
+            f.lma_cut = PI * (nc + 1.0);
+        else if (d.model == PTG_PLANE_WAVE)
+            f.lma_cut = PI * nc * std::sqrt(lnk / LN_2);  // exp2(-(phase / (pi nc))^2)
+        else
+            f.lma_cut = f.omega * f.duration * std::sqrt(lnk / (4.0 * LN_2));  // exp(-4 ln2 phase^2 / tau^2)
     }
     // Field::max_timestep
     double dt;
@@ -694,6 +726,8 @@ ptg_status ptg_context_create(const ptg_device_cfg* cfg, ptg_ctx** out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&c->ev0));
     CUDA_TRY(cudaEventCreate(&c->ev1));
+    CUDA_TRY(cudaEventCreate(&c->ev_wa));
+    CUDA_TRY(cudaEventCreate(&c->ev_wb));
     CUDA_TRY(cudaMalloc(&c->counters, sizeof(Counters)));
     CUDA_TRY(cudaMallocHost(&c->h_counters, sizeof(Counters)));
     PairGL gl;
@@ -750,12 +784,24 @@ ptg_status ptg_context_destroy(ptg_ctx* c) {
     for (void* p : c->table_bufs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_wa) cudaEventDestroy(c->ev_wa);
+    if (c->ev_wb) cudaEventDestroy(c->ev_wb);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return PTG_OK;
 }
 
 void* ptg_context_stream(ptg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+ptg_status ptg_context_set_limits(ptg_ctx* c, const ptg_limits* limits, ptg_limits* current) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (limits) {
+        if (limits->rejection_cap > (1u << 30)) return set_err(PTG_ERR_INVALID_ARGUMENT, "rejection cap above 2^30");
+        c->limits = *limits;
+    }
+    if (current) *current = c->limits;
+    return PTG_OK;
+}
 
 ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
     if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
@@ -781,23 +827,37 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
         {"nlc_lp_classical_cdf", &c->lma_host.nlc_lp_cl_cdf, 61 * 16 * 2, true},
     };
     CUDA_TRY(cudaSetDevice(c->device));
+    // all or nothing: the context keeps its tables unless every file reads
+    LmaTables host = c->lma_host;
+    std::vector<void*> bufs;
+    auto fail = [&](ptg_status st, const std::string& msg) {
+        for (void* p : bufs) cudaFree(p);
+        return set_err(st, msg);
+    };
     for (auto& w : wants) {
         std::vector<double> data;
         std::vector<uint32_t> shape;
         std::string path = d + "/" + w.name + ".ptgt";
+        const double** slot = (const double**)((char*)&host + ((char*)w.slot - (char*)&c->lma_host));
         if (!read_ptgt(path, &data, &shape)) {
-            if (w.required) return set_err(PTG_ERR_TABLES, "cannot read table " + path);
-            *w.slot = nullptr;
+            if (w.required) return fail(PTG_ERR_TABLES, "cannot read table " + path);
+            *slot = nullptr;
             continue;
         }
-        if (data.size() != w.count) return set_err(PTG_ERR_TABLES, "table " + path + " has the wrong size");
+        if (data.size() != w.count) return fail(PTG_ERR_TABLES, "table " + path + " has the wrong size");
+        for (double v : data)
+            if (std::isnan(v)) return fail(PTG_ERR_TABLES, "table " + path + " holds a NaN");
         void* p = nullptr;
-        CUDA_TRY(cudaMalloc(&p, 8 * data.size()));
-        CUDA_TRY(cudaMemcpy(p, data.data(), 8 * data.size(), cudaMemcpyHostToDevice));
-        c->table_bufs.push_back(p);
-        *w.slot = (const double*)p;
+        cudaError_t e = cudaMalloc(&p, 8 * data.size());
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        bufs.push_back(p);
+        e = cudaMemcpy(p, data.data(), 8 * data.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        *slot = (const double*)p;
     }
-    CUDA_TRY(cudaMemcpy(c->lma_dev, &c->lma_host, sizeof(LmaTables), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(c->lma_dev, &host, sizeof(LmaTables), cudaMemcpyHostToDevice));
+    c->lma_host = host;
+    for (void* p : bufs) c->table_bufs.push_back(p);
     c->tables_loaded = true;
     return PTG_OK;
 }
@@ -950,6 +1010,14 @@ static void fill_step_options(const ptg_collide_options& o, StepOptions* so) {
     so->tracking_secondaries = o.tracking_secondaries;
     so->max_generation = o.max_generation;
     so->keep_decayed = o.keep_decayed_photons;
+    so->step_cap = STEP_CAP;
+    so->rej_cap = REJECTION_CAP;
+}
+
+// The context's limits (ptg_context_set_limits) over the defaults.
+static void apply_limits(const ptg_ctx* c, StepOptions* so) {
+    if (c->limits.step_cap) so->step_cap = c->limits.step_cap;
+    if (c->limits.rejection_cap) so->rej_cap = (int)c->limits.rejection_cap;
 }
 
 // ----------------------------------------------------- wave ordering ---
@@ -1125,6 +1193,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
     WaveArgs a{};
     a.f = f;
     fill_step_options(*o, &a.o);
+    apply_limits(c, &a.o);
     a.o.dt = dt_max * o->dt_multiplier;
     a.gl = c->gl;
     a.lma = c->lma_dev;
@@ -1160,16 +1229,22 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
         unsigned long long lo = 0, hi = n;
         uint32_t waves = 0, ordered = 0;
         bool overflow = false;
+        double wave_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         while (lo < hi) {
             a.lo = lo;
             a.hi = hi;
             a.order = order_wave(c, WaveKeys{c->s, nullptr}, lo, hi) ? c->d_order : nullptr;
             ordered += a.order ? 1u : 0u;
             CUDA_TRY(cudaMemsetAsync(&c->counters->next, 0, 8, c->stream));
+            CUDA_TRY(cudaEventRecord(c->ev_wa, c->stream));
             CUDA_TRY(launch_wave_model(c, a));
-            ++waves;
+            CUDA_TRY(cudaEventRecord(c->ev_wb, c->stream));
             CUDA_TRY(cudaMemcpyAsync(c->h_counters, c->counters, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
             CUDA_TRY(cudaStreamSynchronize(c->stream));
+            float wms = 0.0f;
+            CUDA_TRY(cudaEventElapsedTime(&wms, c->ev_wa, c->ev_wb));
+            wave_ms[waves < 8 ? waves : 7] += wms;
+            ++waves;
             if (c->h_counters->overflow) {
                 overflow = true;
                 break;
@@ -1220,6 +1295,9 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
             stats->particle_errors = c->h_counters->errors;
             stats->waves = waves;
             stats->ordered_waves = ordered;
+            stats->max_steps = c->h_counters->max_steps;
+            stats->free_steps = c->h_counters->free_steps;
+            for (int w = 0; w < 8; ++w) stats->wave_ms[w] = wave_ms[w];
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             stats->device_ms = ms;
@@ -1692,6 +1770,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     // input rows (before the captured sequence loads them)
     q.base.order = order_collisions(c, d_in->r, n_coll, coll, c->h_qoff, n) ? c->d_order : nullptr;
     fill_step_options(*o, &q.base.o);
+    apply_limits(c, &q.base.o);
     if (variant == 2) q.base.o.dt = c->h_coll[0].dt;
     q.base.gl = c->gl;
     q.base.lma = c->lma_dev;
@@ -1704,6 +1783,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     // longest wait any lane may legitimately see: the drain of the batch's
     // last showers; generous, but bounded
     q.wait_ns = (unsigned long long)(20.0e9 + 2.0e3 * (double)n);
+    if (c->limits.queue_wait_ns) q.wait_ns = c->limits.queue_wait_ns;
     if (any_lp_lma) {
         st = ensure_dbw(c, lp_lma_a0, grid, &q.base, &grid);
         if (st != PTG_OK) return st;
@@ -1734,8 +1814,11 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
                           (void*)d_in->u, (void*)d_in->pol, (void*)d_in->weight, (void*)d_in->id, (void*)d_in->r0,
                           (void*)d_in->u0, q.base.db_cap, (void*)q.base.dbw, (int)sizeof(StepOptions));
             std::string k = key;
-            k.append((const char*)&q.base.order, sizeof(q.base.order));  // captured by value in the launch
-            k.append((const char*)&q.base.o, sizeof(StepOptions));
+            // the kernel's arguments are captured by value: every byte of them
+            // (the single-collision kernel's laser, seed and id base, the
+            // learned proposal's switch and margin, the step options, the
+            // phase order) must match for a replay
+            k.append((const char*)&q, sizeof(q));
             k.append((const char*)&fa.min_energy, 2 * sizeof(double));
             k.append((const char*)&fa.discard_bg_e, 3 * sizeof(int));
             if (!c->q_graph || k != c->q_graph_key) {
@@ -1786,6 +1869,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
             r.n_created = coll[k].count + cs.n_created;
             r.lepton_steps = cs.lepton_steps;
             r.photon_steps = cs.photon_steps;
+            r.free_steps = cs.free_steps;
             r.emissions = cs.emissions;
             r.pair_events = cs.pair_events;
             r.rejections = cs.rejections;
@@ -1799,6 +1883,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
                 total->n_created += r.n_created;
                 total->lepton_steps += r.lepton_steps;
                 total->photon_steps += r.photon_steps;
+                total->free_steps += r.free_steps;
                 total->emissions += r.emissions;
                 total->pair_events += r.pair_events;
                 total->rejections += r.rejections;
@@ -1808,6 +1893,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         if (total) {
             total->particle_errors += h.errors;
             total->waves = (uint32_t)(attempt + 1);
+            total->max_steps = h.max_steps;
             total->device_ms = ms;
         }
         return PTG_OK;
@@ -2983,7 +3069,12 @@ ptg_status ptg_sampler_bench(ptg_ctx* c, const ptg_sampler_bench_cfg* cfg, doubl
 // primaries' initial momenta, per-shower counts, the pair-spectrum node
 // constants and a fixed-size shower store) lives in one file-scope device
 // array.  Host code never dereferences that array's name: the device
-// address comes from cudaGetSymbolAddress() once per device.
+// address comes from cudaGetSymbolAddress() on every call.  Its waves run
+// in slot order: putting a wave in order of laser phase needs sort buffers,
+// and a batch of at most 4096 primaries gains little from it (the allocating
+// path orders only waves of 2048 particles or more).  The results are the
+// same either way, because each particle's random stream is fixed when it is
+// created.
 namespace {
 constexpr unsigned long long NOALLOC_MAX_PRIMARIES = 4096;
 constexpr unsigned long long NOALLOC_MAX_PARTICLES = 32768;  // shower store, primaries included
@@ -2994,31 +3085,34 @@ constexpr size_t NOALLOC_OFF_INIT_U = NOALLOC_OFF_COUNTERS + noalloc_align(sizeo
 constexpr size_t NOALLOC_OFF_COUNTS = NOALLOC_OFF_INIT_U + noalloc_align(32 * NOALLOC_MAX_PRIMARIES);
 constexpr size_t NOALLOC_OFF_GL = NOALLOC_OFF_COUNTS + noalloc_align(8 * NOALLOC_MAX_PRIMARIES);
 constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_GL + noalloc_align(sizeof(PairGL));
-constexpr int NOALLOC_MAX_DEVICES = 64;
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
+// The pair-spectrum node constants, computed once per process on the host
+// (they are the same on every device) and uploaded into the array by every
+// call.
 static std::mutex g_noalloc_mutex;
-static char* g_noalloc_base[NOALLOC_MAX_DEVICES];
+static PairGL g_noalloc_gl;
+static bool g_noalloc_gl_ready = false;
 
-// Once per device, with that device current: look up the array's device
-// address and upload the pair-spectrum node constants into it.
-static ptg_status noalloc_setup(int dev, char** base) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return set_err(PTG_ERR_INVALID_ARGUMENT, "device ordinal out of range");
-    if (g_noalloc_base[dev]) {
-        *base = g_noalloc_base[dev];
-        return PTG_OK;
-    }
+// Every call, with the caller's device current: the array's device address
+// in the current context (so that a context created after cudaDeviceReset,
+// or another context made current on the same device, gets its own), and
+// the constants uploaded on the call's stream ahead of its kernels.
+static ptg_status noalloc_setup(cudaStream_t s, char** base) {
     void* ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || ptr == nullptr)
         return set_err(PTG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    PairGL gl;
-    CUDA_TRY(fill_pair_gl(&gl));
-    CUDA_TRY(cudaMemcpy((char*)ptr + NOALLOC_OFF_GL, &gl, sizeof(gl), cudaMemcpyHostToDevice));
-    g_noalloc_base[dev] = (char*)ptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_gl_ready) {
+            CUDA_TRY(fill_pair_gl(&g_noalloc_gl));
+            g_noalloc_gl_ready = true;
+        }
+    }
+    CUDA_TRY(cudaMemcpyAsync((char*)ptr + NOALLOC_OFF_GL, &g_noalloc_gl, sizeof(PairGL), cudaMemcpyHostToDevice, s));
     *base = (char*)ptr;
     return PTG_OK;
 }
@@ -3046,6 +3140,15 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
     if (!o || !d_primaries || !d_out) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     if (laser->model != PTG_FAST_PLANE_WAVE && laser->model != PTG_FAST_FOCUSED_LASER)
         return set_err(PTG_ERR_UNSUPPORTED, "the allocation-free entry point covers the LCFA field models only");
+    if (!(o->rate_increase >= 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "increase in pair creation rate must be >= 1.0");
+    if (o->rate_increase > 1.0 && o->multiplicity >= 0)
+        return set_err(PTG_ERR_INVALID_ARGUMENT, "event biasing is incompatible with multiplicity selection");
+    if (d_primaries->n == 0) {
+        // no primaries: an empty shower, as ptg_collide_batch_device gives
+        d_out->n = 0;
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return PTG_OK;
+    }
     if (!d_primaries->species || !d_primaries->r || !d_primaries->u)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
     if (d_primaries->n > NOALLOC_MAX_PRIMARIES)
@@ -3056,15 +3159,12 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
         !d_out->payload || !d_out->parent_chi || !d_out->interaction_count || !d_out->work || !d_out->id ||
         !d_out->parent_id || !d_out->primary || !d_out->stream || !d_out->generation || !d_out->flags || !d_out->status)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "every output array must be a device buffer of out_capacity rows");
-    if (!(o->rate_increase >= 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "increase in pair creation rate must be >= 1.0");
-    if (o->rate_increase > 1.0 && o->multiplicity >= 0)
-        return set_err(PTG_ERR_INVALID_ARGUMENT, "event biasing is incompatible with multiplicity selection");
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
-    char* base = nullptr;
-    st = noalloc_setup(dev, &base);
-    if (st != PTG_OK) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    char* base = nullptr;
+    st = noalloc_setup(s, &base);
+    if (st != PTG_OK) return st;
     int sms = 0, per_sm = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 
@@ -3079,20 +3179,8 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
     double dt_max;
     WaveArgs a{};
     a.f = make_field(*laser, &dt_max);
+    fill_step_options(*o, &a.o);
     a.o.dt = dt_max * o->dt_multiplier;
-    a.o.t_stop = o->t_stop;
-    a.o.has_t_stop = std::isfinite(o->t_stop) ? 1 : 0;
-    a.o.rate_increase = o->rate_increase;
-    a.o.eqn = (o->classical && o->rr) ? (o->gaunt_factor ? EQN_MODIFIED_LL : EQN_LL) : EQN_LORENTZ;
-    a.o.classical_mode = o->classical && !o->gaunt_factor;
-    a.o.classical = o->classical;
-    a.o.electron_recoils = !o->classical && o->rr;
-    a.o.tracking_photons = o->tracking_photons;
-    a.o.pol_resolved = o->pol_resolved;
-    a.o.rotate_stokes = o->rotate_stokes_pars;
-    a.o.tracking_secondaries = o->tracking_secondaries;
-    a.o.max_generation = o->max_generation;
-    a.o.keep_decayed = o->keep_decayed_photons;
     a.s = store;
     a.c = counters;
     a.gl = gl;
@@ -3161,6 +3249,8 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
         stats->rejections = h.rejections;
         stats->particle_errors = h.errors;
         stats->waves = waves;
+        stats->max_steps = h.max_steps;
+        stats->free_steps = h.free_steps;
     }
     if (h.n_out > out_capacity)
         return set_err(PTG_ERR_QUEUE_OVERFLOW, "the output needs " + std::to_string(h.n_out) + " rows, out_capacity is " +

@@ -28,6 +28,8 @@ struct FieldParams {
     double inv_waist, inv_zr;  // reciprocals, so the per-step field needs no division
     double inv_tau;            // 1 / (omega * duration)
     double chi_scale;          // field scale of lcfa_fields32 over the critical field
+    double drift_ell_max;      // LCFA photons with ell^0 below this never create pairs (0 = off)
+    double lma_cut;            // LMA: |phase| beyond which <a^2> < 2^-60 (0 = off)
     // FP32 copies for the per-step FP32 path (converted once on the host,
     // the same rounding as a conversion on the device)
     float eps32, cos_pa32, sin_pa32, inv_tau32, chi_scale32;
@@ -400,6 +402,36 @@ __device__ __forceinline__ d4 lma_grad_a_sqd(const FieldParams& f, d4 r) {
     }
     double t = beam * genv + gb2 * env;
     return d4{-t, -(gb0 * env), -(gb1 * env), -t};
+}
+
+// A whole LMA step lies where <a^2> < 2^-60 (f.lma_cut): either it ends
+// before the pulse (the phase k(t - z) of a massive particle only grows, by
+// at most 2 k c dt per step) or it starts after it.
+__device__ __forceinline__ bool lma_step_field_free(const FieldParams& f, d4 r, double dt) {
+    if (f.lma_cut <= 0.0) return false;
+    double phase = phase_of(f, r);
+    return phase + 2.0 * f.omega * dt + 1.0 < -f.lma_cut || phase > f.lma_cut;
+}
+
+// lma_push where <a^2> and its gradient are below 2^-60: the ponderomotive
+// kick and the radiation-reaction terms (all proportional to them) are
+// below an ulp of u, and 1 + <a^2> rounds to 1, so u keeps its spatial part,
+// gamma is recomputed from it and the particle drifts two half steps, with
+// lma_push's own arithmetic.  The work done, also proportional to <a^2>, is
+// taken as zero.
+__device__ __forceinline__ void lma_push_field_free(d4 r0, d4 u0, double dt, d4* r_out, d4* u_out, double* dt_out) {
+    double dtau = dt / u0.t;
+    double h = 0.5 * SPEED_OF_LIGHT * dtau;
+    d4 r = d4{r0.t + h * u0.t, r0.x + h * u0.x, r0.y + h * u0.y, r0.z + h * u0.z};
+    double dt_actual = 0.5 * u0.t * dtau;
+    d4 u = u0;
+    r = d4{r.t + h * u.t, r.x + h * u.x, r.y + h * u.y, r.z + h * u.z};
+    dt_actual = dt_actual + 0.5 * u.t * dtau;
+    double b = 1.0;
+    u.t = sqrt(b + u.x * u.x + u.y * u.y + u.z * u.z);
+    *r_out = r;
+    *u_out = u;
+    *dt_out = dt_actual;
 }
 
 // plane_wave.rs:196-249 == focused_laser.rs:205-258: proper-time leapfrog

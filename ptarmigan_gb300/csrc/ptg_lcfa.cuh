@@ -426,7 +426,7 @@ static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double ch
     double mx = lcfa_pair_spectrum_ceiling(chi, sv.x, gl);
     double s = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double ss = rng.next(), u = rng.next();
         if (u <= lcfa_pair_spectrum(ss, chi, sv.x, gl) / mx) {
             s = ss;
@@ -434,10 +434,10 @@ static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double ch
         }
     }
     *rejections += it;
-    if (it == REJECTION_CAP) return false;
+    if (it == rng.cap) return false;
     double amx = lcfa_pair_angular_ceiling(s, chi, sv.x);
     double z = 1.0;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double y = rng.next(), u = rng.next();
         if (u <= lcfa_pair_angular_spectrum(y, s, chi, sv.x) / amx) {
             z = 1.0 + 4.0 * chi * y * y;
@@ -445,7 +445,7 @@ static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double ch
         }
     }
     *rejections += it;
-    if (it == REJECTION_CAP) return false;
+    if (it == rng.cap) return false;
     // azimuth (lcfa/pair_creation/mod.rs:141-173)
     double arg = 2.0 * z / (3.0 * chi * s * (1.0 - s));
     double k_ratio = (arg < 1.0e-4) ? 0.6368498843179743 / cbrt(arg)
@@ -463,7 +463,7 @@ static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double ch
     }
     amax *= 1.1;
     double ph = 0.0;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double p = 2.0 * PI * rng.next();
         double u = rng.next();
         double f = A + (cos(2.0 * p) * (1.0 - Cc) - Cc) * sv.x - Dd * sin(2.0 * p) * sv.y + Ee * sin(p) * sv.z;
@@ -473,7 +473,7 @@ static __device__ __noinline__ bool lcfa_pair_sample(d4 ell, d4 sv_in, double ch
         }
     }
     *rejections += it;
-    if (it == REJECTION_CAP) return false;
+    if (it == rng.cap) return false;
     double gp = s * ell.t;
     double ct = (2.0 * gp * gp - z23) / (2.0 * gp * gp - 1.0);
     *gamma_p = gp;

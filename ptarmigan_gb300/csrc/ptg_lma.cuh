@@ -68,11 +68,10 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
                                                double* chi, double* absorption, uint32_t* rej,
                                                LpDefer* dfr = nullptr) {
     *emitted = false;
-    double a = sqrt(lma_a_sqd(f, r));
     double chirp = 1.0;
-    if (f.model == M_PLANE_WAVE) {
+    if (f.model == M_PLANE_WAVE && f.chirp_b != 0.0) {
         chirp = 1.0 + 2.0 * f.chirp_b * phase_of(f, r);
-        if (chirp < 0.0 && a > 0.0) return 3;  // PTG_ERR_SANITY
+        if (chirp < 0.0 && lma_a_sqd(f, r) > 0.0) return 3;  // PTG_ERR_SANITY
     }
     double width = 1.0;
     if (f.bandwidth != 0.0) {
@@ -136,6 +135,8 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
         if (st != 0) return st;
         *k_out = k;
         *u_prime = d4{u.t + n * kappa.t - k.t, u.x + n * kappa.x - k.x, u.y + n * kappa.y - k.y, u.z + n * kappa.z - k.z};
+        // the local amplitude, needed only for the photon's record
+        double a = sqrt(lma_a_sqd(f, r));
         *a_eff = a;
         *chi = a * dot4(u, kappa);
         *absorption = n * kappa.t;

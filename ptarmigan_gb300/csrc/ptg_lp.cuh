@@ -602,7 +602,7 @@ static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork&
     double mx = lp_ceiling(a, eta, g, w);
     double s = 0.0, theta = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double ss = smax * rng.next();
         double th = (PI / 2.0) * rng.next();
         if (th > tb.at(ss)) continue;
@@ -613,7 +613,7 @@ static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork&
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;  // PTG_ERR_REJECTION_CAP
+    if (it == rng.cap) return 4;  // PTG_ERR_REJECTION_CAP
     return lp_finish(n, a, eta, s, theta, g, w, rng, n_out, s_out, theta_out, sv_out);
 }
 
@@ -668,6 +668,7 @@ __device__ __forceinline__ Draws shfl_draws(const Draws& d, int src) {
     o.block = __shfl_sync(all, d.block, src);
     for (int q = 0; q < 4; ++q) o.w[q] = __shfl_sync(all, d.w[q], src);
     o.pos = __shfl_sync(all, d.pos, src);
+    o.cap = __shfl_sync(all, d.cap, src);
     return o;
 }
 
@@ -742,11 +743,11 @@ static __device__ __noinline__ int lp_sample_warp(const NlcTables& t, const DbWo
     double smax = sn / (1.0 + sn);
     Draws r = rng;
     int it = 0;
-    while (it < REJECTION_CAP) {
+    while (it < r.cap) {
         int my_it = -1;
         double my_s = 0.0, my_th = 0.0, my_z = 0.0;
         Draws my_r = r;
-        for (int k = 0; k < 32 && it < REJECTION_CAP; ++it) {
+        for (int k = 0; k < 32 && it < r.cap; ++it) {
             double ss = smax * r.next();
             double th = (PI / 2.0) * r.next();
             if (th > tb.at(ss)) continue;
@@ -767,7 +768,7 @@ static __device__ __noinline__ int lp_sample_warp(const NlcTables& t, const DbWo
         }
     }
     rng = r;
-    *rej += REJECTION_CAP;
+    *rej += r.cap;
     return 4;  // PTG_ERR_REJECTION_CAP
 }
 
@@ -873,7 +874,7 @@ static __device__ __noinline__ int lp_classical_sample_n(const DbGeom& g, const 
     double mx = lp_cl_ceiling(a, g, w);
     double v = 0.0, s = 0.0, theta = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double vv = rng.next();
         double ss = vv * smax;
         double th = (PI / 2.0) * rng.next();
@@ -885,7 +886,7 @@ static __device__ __noinline__ int lp_classical_sample_n(const DbGeom& g, const 
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;
+    if (it == rng.cap) return 4;
     int quadrant = (int)(4.0 * rng.next());
     if (quadrant == 1)
         theta = PI - theta;

@@ -110,7 +110,8 @@ struct Draws {
     uint32_t k0, k1, s_lo, s_hi, step, block;
     uint32_t w[4];
     int pos;
-    __device__ __forceinline__ void begin(uint64_t seed, uint64_t stream, uint32_t st) {
+    int cap;  // iterations any rejection loop drawing from this stream may take
+    __device__ __forceinline__ void begin(uint64_t seed, uint64_t stream, uint32_t st, int rej_cap = REJECTION_CAP) {
         k0 = (uint32_t)seed;
         k1 = (uint32_t)(seed >> 32);
         s_lo = (uint32_t)stream;
@@ -118,6 +119,7 @@ struct Draws {
         step = st;
         block = 0;
         pos = 4;
+        cap = rej_cap;
     }
     __device__ __forceinline__ double next() {
         if (pos >= 4) {

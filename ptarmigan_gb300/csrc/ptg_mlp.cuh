@@ -188,7 +188,7 @@ static __device__ __noinline__ int cp_sample_v_capped(Envelope e, int n, double 
     double ceil = cp_ceiling(n, a, eta);
     c->evals += 32u;
     unsigned capped = envelope_cap(&e, ceil);
-    for (int it = 0; it < REJECTION_CAP; ++it) {
+    for (int it = 0; it < rng.cap; ++it) {
         int k;
         double v = envelope_draw(e, rng, &k);
         double f = cp_diff_partial_rate(n, a, eta, v);
@@ -213,7 +213,7 @@ static __device__ __noinline__ int cp_sample_v_capped(Envelope e, int n, double 
             return 0;
         }
     }
-    *rej += REJECTION_CAP;
+    *rej += rng.cap;
     return 4;  // PTG_ERR_REJECTION_CAP
 }
 

@@ -253,7 +253,7 @@ static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, doubl
 static __device__ __noinline__ int cp_sample_v_under(int n, double a, double eta, double mx, Draws& rng,
                                                      double* v_out, uint32_t* rej) {
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double vv = rng.next(), u = rng.next();
         if (u <= cp_diff_partial_rate(n, a, eta, vv) / mx) {
             *v_out = vv;
@@ -261,7 +261,7 @@ static __device__ __noinline__ int cp_sample_v_under(int n, double a, double eta
         }
     }
     *rej += it;
-    return it == REJECTION_CAP ? 4 : 0;  // PTG_ERR_REJECTION_CAP
+    return it == rng.cap ? 4 : 0;  // PTG_ERR_REJECTION_CAP
 }
 
 // The same under the reference's ceiling.
@@ -433,7 +433,7 @@ static __device__ __noinline__ int cp_classical_sample(const NlcTables& t, doubl
     double mx = cp_cl_ceiling(n, a);
     double v = 0.0;
     int it;
-    for (it = 0; it < REJECTION_CAP; ++it) {
+    for (it = 0; it < rng.cap; ++it) {
         double vv = rng.next(), u = rng.next();
         if (u <= cp_spectrum_low_eta(n, a, vv) / mx) {
             v = vv;
@@ -441,7 +441,7 @@ static __device__ __noinline__ int cp_classical_sample(const NlcTables& t, doubl
         }
     }
     *rej += it;
-    if (it == REJECTION_CAP) return 4;
+    if (it == rng.cap) return 4;
     double s = v * (2.0 * n * eta / (1.0 + a * a));
     double theta = 2.0 * PI * rng.next();
     double z = sqrt((double)(4 * n * n) * (a * a / (1.0 + a * a)) * v * (1.0 - v));

@@ -28,6 +28,7 @@ struct CollParams {
 struct CollStats {
     unsigned long long lepton_steps, photon_steps, emissions, pair_events, rejections, errors;
     unsigned long long n_created, n_out;
+    unsigned long long free_steps;
 };
 
 struct QueueArgs {
@@ -112,7 +113,7 @@ __device__ __forceinline__ int poll_slot(const WaveArgs& a, unsigned long long t
 
 struct PartCounts {
     uint32_t rej, nemit, npair;
-    unsigned long long lsteps, psteps;
+    unsigned long long lsteps, psteps, fsteps;
 };
 
 // main.rs:134-289 for one particle: steps it until it leaves the field,
@@ -126,7 +127,7 @@ static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, Par
         } else if (L.species != SP_PHOTON) {
             done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
             if (!done) {
-                lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
+                pc.fsteps += lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit) ? 1ull : 0ull;
                 ++L.step;
                 ++pc.lsteps;
                 done = L.status != ST_OK;
@@ -134,6 +135,14 @@ static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, Par
         } else {
             done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
                      a.o.tracking_photons);
+            if (!done && photon_drifts(a, L)) {
+                unsigned long long ds = photon_drift(a, L);
+                pc.psteps += ds;
+                pc.fsteps += ds;
+                ds += L.step;
+                L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
+                return;
+            }
             if (!done) {
                 photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair);
                 ++L.step;
@@ -197,6 +206,7 @@ __device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs&
     CollStats* cs = q.stats + L.coll;
     if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
     if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
+    if (pc.fsteps) atomicAdd(&cs->free_steps, pc.fsteps);
     if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
     if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
     if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
@@ -212,7 +222,7 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
     if (lane_stops(a, L)) return true;
     if (L.species != SP_PHOTON) {
         if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop))) return true;
-        lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
+        pc.fsteps += lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit) ? 1ull : 0ull;
         ++L.step;
         ++pc.lsteps;
         return L.status != ST_OK;
@@ -220,6 +230,14 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
     if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
           a.o.tracking_photons))
         return true;
+    if (photon_drifts(a, L)) {
+        unsigned long long ds = photon_drift(a, L);
+        pc.psteps += ds;
+        pc.fsteps += ds;
+        ds += L.step;
+        L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
+        return true;
+    }
     photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair);
     ++L.step;
     ++pc.psteps;
@@ -232,6 +250,7 @@ template <int MINB>
 __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
     WaveArgs a = q.base;
     int cur = -1;
+    uint32_t maxst = 0;
     unsigned long long t = 0, t_end = 0;
     for (;;) {
         if (t == t_end) {
@@ -251,15 +270,17 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
         Lane L;
         queue_load(a, L, slot);
         if (!queue_begin(q, a, L, cur)) continue;
-        PartCounts pc{0, 0, 0, 0, 0};
+        PartCounts pc{0, 0, 0, 0, 0, 0};
         switch (a.f.model) {
             case M_PLANE_WAVE: run_particle<M_PLANE_WAVE>(a, L, pc); break;
             case M_FAST_PLANE_WAVE: run_particle<M_FAST_PLANE_WAVE>(a, L, pc); break;
             case M_FOCUSED_LASER: run_particle<M_FOCUSED_LASER>(a, L, pc); break;
             default: run_particle<M_FAST_FOCUSED_LASER>(a, L, pc); break;
         }
+        maxst = L.step > maxst ? L.step : maxst;
         queue_finish(q, a, L, pc);
     }
+    if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }
 
 // The single-collision variant (a batch of one collision): one pass of a
@@ -282,7 +303,8 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
     const unsigned FULL = 0xffffffffu;
     const WaveArgs& a = q.base;
     Lane L;
-    PartCounts pc{0, 0, 0, 0, 0};
+    PartCounts pc{0, 0, 0, 0, 0, 0};
+    uint32_t maxst = 0;
     bool have = false, holding = false, finished = false;
     unsigned long long t = 0, t_end = 0, ticket = 0, wait_from = 0;
     for (;;) {
@@ -321,7 +343,7 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
                 } else {
                     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
                     L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
-                    pc = PartCounts{0, 0, 0, 0, 0};
+                    pc = PartCounts{0, 0, 0, 0, 0, 0};
                     have = true;
                 }
             }
@@ -331,10 +353,12 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             continue;
         }
         if (have && queue_step<MODEL>(a, L, pc)) {
+            maxst = L.step > maxst ? L.step : maxst;
             queue_finish(q, a, L, pc);
             have = false;
         }
     }
+    if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }
 
 }  // namespace ptg

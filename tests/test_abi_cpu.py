@@ -45,7 +45,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ptg_abi_version() == 1
+    assert lib.ptg_abi_version() == 2
 
 
 def test_struct_sizes_match_header():
@@ -94,6 +94,7 @@ _LAYOUTS = {
     "SamplerBenchCfg": "ptg_sampler_bench_cfg", "SamplerBenchStats": "ptg_sampler_bench_stats",
     "SamplerBenchDetail": "ptg_sampler_bench_detail", "BeamDesc": "ptg_beam_desc", "HgramSpec": "ptg_hgram_spec",
     "HgramInfo": "ptg_hgram_info", "StatsSpec": "ptg_stats_spec", "StatsSums": "ptg_stats_sums",
+    "Limits": "ptg_limits",
 }
 
 

@@ -211,3 +211,31 @@ def test_lp_emissions_warp_sampled_match_serial_sampler(eng):
     _compare(parts[0], single, TOL[abi.PLANE_WAVE], 0.02)
     assert stats[0]["emissions"] == pytest.approx(sst["emissions"], rel=0.03, abs=2)
     assert stats[0]["lepton_steps"] == pytest.approx(sst["lepton_steps"], rel=0.01)
+
+
+def test_graph_replay_follows_seed_and_sampler(eng):
+    """A replayed graph must run with the call's own kernel arguments: the
+    single-collision kernel takes the laser, seed and id base by value, and
+    every variant takes the learned proposal's switch.  Each graph-replayed
+    queue call must equal the wave path with the same seed and sampler, event
+    count for event count."""
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(16.5)
+    n = 3000
+    prim = beam.build(n, g, sigma=0.001 * g, radius=2e-6, length=10e-6, rms_div=8e-6, laser=laser, seed=8)
+    opts = abi.collide_options(pol_resolved=1, max_generation=-1)
+    eng.mlp_init(3)
+    eng.mlp_train(n_samples=200_000, batch=4096, epochs=1)
+    keys = ("lepton_steps", "photon_steps", "emissions", "pair_events", "rejections", "n_out")
+    for variant in (2, 0):
+        eng.queue_config(variant=variant, blocks_per_sm=0, chunk=1, use_graph=1)
+        for learned in (False, True, False):
+            eng.mlp_use(learned)
+            for seed in (31, 32):
+                _, ref = eng.collide(laser, opts, prim, seed=seed, id_base=n)
+                coll = [{"laser": laser, "seed": seed, "id_base": n, "first": 0, "count": n}]
+                _, _, total = eng.collide_multi(coll, opts, prim)
+                assert all(total[k] == ref[k] for k in keys), (variant, learned, seed, total, ref)
+    eng.mlp_use(False)
+    eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
