@@ -1,21 +1,45 @@
-"""Benchmark of the collision loop: collided primaries/s (showers included).
+"""Benchmark of the collision loop: collided primaries/s (showers included),
+the learned proposal in the persistent queue against the reference's table
+sampler, at a fixed KS distance on the photon spectrum.
 
-Workload (one "step" = one batch through the collision loop): the focused
-LCFA shower — 1e6 electrons at 10 GeV, 1% rms energy spread, 2 x 2 x 20 um
-rms, 50 urad divergence, head-on with a linearly polarised focused Gaussian
-laser (FastFocusedLaser) a0 = 10, w0 = 4 um, 0.8 um, 30 fs FWHM; LCFA
-emission and pair creation on, secondaries tracked to generation 2; FP64
-push.  Inputs are seeded synthetic beams with those distributions.
+Default workload, the polarisation-resolved CP shower (one "step" = one
+batch of 1e7 primaries through the collision loop): electrons at 16.5 GeV,
+0.1% rms energy spread, 5 x 5 x 24 um rms, 8 urad divergence, head-on with
+a circularly polarised focused Gaussian laser (FocusedLaser, LMA) a0 = 5,
+w0 = 3 um, 0.8 um, 30 fs FWHM; photon Stokes parameters tracked
+(pol_resolved), pair creation on, all secondaries tracked.  Inputs are
+seeded synthetic beams with those distributions (the reference has no
+public dataset); the input and the shower store are far larger than L2.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload cp_shower|lcfa_shower|plane_wave_lma|a0_scan|learned_sampler]
 
-Prints one JSON line.  `value` times ptg_collide_batch_device with the
-primaries resident in HBM; `e2e` times ptg_collide_batch (host buffers in
-and out, host<->device copies inside the timed region).  --impl reference
-times the CPU restatement of the reference's collision loop (the reference
-is Rust and no Rust toolchain is available) on all host cores.
+Prints one JSON line.  For cp_shower:
+  value         the learned proposal inside the persistent single-collision
+                queue kernel (CUDA graph, autotuned launch shape), primaries
+                resident in HBM, seeds 1000 .. 1000+K-1;
+  plain_value   the reference's table sampler through the wave kernels;
+  cross_terms   learned proposal + waves and table sampler + queue, so that
+                the gain splits into sampler and scheduler (all four arms
+                run the same K seeds);
+  e2e           the value path through ptg_collide_multi with host buffers
+                (page-locked primaries in, the shower out), same K seeds;
+  ks_*          photon-energy KS distance between the value path and the
+                plain path (seed 1000), against its 1e-3 critical value;
+  parity        the oracle (C++ FP64 restatement of the reference) against
+                the GPU on the cpu_baseline sample (same primaries, seed and
+                id base): particles matched by random stream, momenta within
+                tolerance, KS and chi-square on the photon spectra, pair
+                yield, Stokes parameters and electron energy loss;
+  roofline      the value path's dominant kernel on the FP64 pipe.
+--impl reference times the oracle on all host cores (the Rust reference
+cannot be built: no cargo or rustc).
 
 Other workloads (--workload), each one JSON line of the same metric:
+  lcfa_shower     1e6 electrons at 10 GeV, 1% spread, 2 x 2 x 20 um, 50 urad,
+                  on a linearly polarised focused Gaussian laser (LCFA,
+                  FastFocusedLaser) a0 = 10, w0 = 4 um, 0.8 um, 30 fs; pairs
+                  on, secondaries tracked to generation 2.
   plane_wave_lma  1e4 electrons at 5 GeV, 0.1% spread, 1 x 1 x 10 um, on a
                   linearly polarised plane wave (LMA), a0 = 1, 0.8 um, cos^2
                   envelope of 30 fs intensity FWHM (30.9 cycles), emission
@@ -26,21 +50,8 @@ Other workloads (--workload), each one JSON line of the same metric:
                   a circularly polarised focused Gaussian laser, w0 = 5 um,
                   0.8 um, 25 fs; LMA below a0 = 5, LCFA above; pairs on.
                   `plain_value` runs the same collisions one call each.
-  cp_shower       electrons at 16.5 GeV, 0.1% spread, 5 x 5 x 24 um, 8 urad,
-                  on a circularly polarised focused laser (LMA) a0 = 5, w0 =
-                  3 um, 0.8 um, 30 fs; Stokes parameters tracked, pairs on,
-                  all generations (--n primaries, default 1e6).  `value` is
-                  the learned proposal inside the persistent queue kernel,
-                  `plain_value` the reference's sampler through the wave
-                  kernels, with the photon spectra of both compared by KS.
-  learned_sampler the CP photon-energy sampler alone: the network is trained
-                  on the GPU on 5e7 table-sampler draws (a log-uniform in
-                  [0.05, 20], eta log-uniform in [1e-3, 2]), then each step
-                  samples 1e7 emissions of the same (a, eta) distribution
-                  with the learned proposal (`value`, inputs and inference
-                  included) and with the reference's sampler
-                  (`plain_value`); acceptance rate and the KS distance
-                  between the two are reported.
+  learned_sampler the CP photon-energy sampler alone, learned proposal
+                  against the table sampler on 1e7 emissions per step.
 """
 
 import argparse
@@ -57,31 +68,36 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "collided primaries/s incl. showers"
+METRIC = "collided primaries/s incl. showers: learned vs table sampler at fixed KS error"
 UNIT = "primaries/s"
-N_PRIMARIES = 1_000_000
-WORKLOAD = "focused LCFA shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; FastFocusedLaser a0=10 w0=4 um 0.8 um 30 fs LP; pairs on; generations<=2"
+SEED0 = 1000
+
+# Algorithmic FP64 operations per event of the collision loop, counted by
+# hand from the reference's formulas (roofline/opcounts.md: +, -, *, /,
+# sqrt and compare count 1, a fused multiply-add 2, exp/log/sin/cos 20;
+# cross-checked against ncu's executed FP64 instruction counts).
+OPS = {
+    # FocusedLaser (LMA, CP): lma_push (gradient at the midpoint, <a^2> at the
+    # end) + the emission probability (rate-table lookup); a field-free step
+    # is two half drifts and gamma
+    "lma_lepton_step": 303.0,
+    "free_lepton_step": 16.0,
+    # photon step in the LMA field with the Breit-Wheeler lookup and the
+    # Stokes update into and out of the LMA basis
+    "lma_photon_step": 260.0,
+    # FastFocusedLaser (LCFA): Salamin fields at the half step, Vay push,
+    # chi and the rate; the drift of a photon step; the photon's pair step
+    "lcfa_lepton_step": 780.0,
+    "lcfa_photon_step": 420.0,
+    "free_photon_step": 8.0,
+}
 
 
-# FP64 operations per step of collide_wave on this workload (2 x DFMA + DMUL
-# + DADD from ncu's SASS instruction counts over a 1e4-primary batch,
-# divided by that batch's step counts) and DRAM bytes per primary
-# (dram__bytes_read.sum + dram__bytes_write.sum over the lepton and photon
-# waves of a 1e6-primary batch: 1.460e9 + 1.100e9 bytes; the pair waves add
-# nothing measurable).
-FP64_PER_LEPTON_STEP = 213.8
-FP64_PER_PHOTON_STEP = 29.2
-DRAM_BYTES_PER_PRIMARY = 2.5605e9 / 1e6
-
-
-def workload(n, seed):
-    from ptarmigan_gb300 import abi, beam
-    laser = abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
-                           fwhm_duration=30e-15)
-    g = beam.gamma_from_energy(10.0)
-    prim = beam.build(n, g, sigma=0.01 * g, radius=2e-6, length=20e-6, rms_div=50e-6, laser=laser, seed=seed)
-    opts = abi.collide_options(max_generation=2)
-    return laser, opts, prim
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
 
 
 class ClockSampler:
@@ -141,71 +157,30 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def fp64_peak_tflops(dev):
-    """Measured FP64 peak: cuBLAS DGEMM 8192^3 (2 N^3 flops), best of 5."""
-    import torch
-    n = 8192
-    a = torch.randn(n, n, dtype=torch.float64, device=dev)
-    b = torch.randn(n, n, dtype=torch.float64, device=dev)
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = float("inf")
-    for _ in range(5):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        e1.synchronize()
-        best = min(best, e0.elapsed_time(e1) / 1e3)
-    del a, b
-    torch.cuda.empty_cache()
-    return 2.0 * n ** 3 / best / 1e12
+# ------------------------------------------------------------- workloads --
+def cp_shower_workload(n, seed):
+    """The polarisation-resolved CP LMA shower (see the module docstring)."""
+    from ptarmigan_gb300 import abi, beam
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6, fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(16.5)
+    prim = beam.build(n, g, sigma=0.001 * g, radius=5e-6, length=24e-6, rms_div=8e-6, laser=laser, seed=seed)
+    opts = abi.collide_options(pol_resolved=1, max_generation=-1)
+    return laser, opts, prim
 
 
-def cpu_threads():
-    try:
-        return len(os.sched_getaffinity(0))
-    except Exception:
-        return os.cpu_count() or 1
+def lcfa_workload(n, seed):
+    """The focused LCFA shower (see the module docstring)."""
+    from ptarmigan_gb300 import abi, beam
+    laser = abi.laser_desc(abi.FAST_FOCUSED_LASER, 10.0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=4e-6,
+                           fwhm_duration=30e-15)
+    g = beam.gamma_from_energy(10.0)
+    prim = beam.build(n, g, sigma=0.01 * g, radius=2e-6, length=20e-6, rms_div=50e-6, laser=laser, seed=seed)
+    opts = abi.collide_options(max_generation=2)
+    return laser, opts, prim
 
 
-def cpu_run(n_sample, seed, threads):
-    """The oracle (CPU restatement of the reference) on a sample."""
-    from oracle import oracle
-    oracle.build()
-    laser, opts, prim = workload(n_sample, seed)
-    t0 = time.perf_counter()
-    _, st = oracle.collide(laser, opts, prim, seed=seed, threads=threads)
-    dt = time.perf_counter() - t0
-    return n_sample / dt, st, dt
-
-
-def run_reference(args, rank, world):
-    if rank != 0:
-        return
-    threads = cpu_threads()
-    n_sample = max(64, args.cpu_sample_per_core * threads)
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_run(min(n_sample, 16 * threads), 99, threads)
-    vals = []
-    t_all = 0.0
-    for k in range(args.steps):
-        v, st, dt = cpu_run(n_sample, 1000 + k, threads)
-        vals.append(v)
-        t_all += dt
-    value = float(np.mean(vals))
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_primaries_per_step": n_sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d primaries per step of the same workload, oracle C++ FP64 restatement of "
-                                   "src/main.rs:134-289 (the Rust reference cannot be built: no cargo/rustc)" % n_sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+# the focused LCFA shower, kept under its earlier name for callers
+workload = lcfa_workload
 
 
 def plane_wave_lma_workload(n, seed):
@@ -228,7 +203,7 @@ def a0_scan_workload(seed, scale=1.0):
     colls, prims, first = [], [], 0
     for k, a0 in enumerate(np.geomspace(0.5, 20.0, 64)):
         model = abi.FOCUSED_LASER if a0 < 5.0 else abi.FAST_FOCUSED_LASER
-        laser = abi.laser_desc(model, float(a0), 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=5e-6, fwhm_duration=25e-15)
+        laser = abi.laser_desc(model, float(a0), 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=5e-6, fwhm_duration=25e-15)
         n = max(1, int(round(sizes[k] * scale)))
         g = beam.gamma_from_energy(16.5)
         p = beam.build(n, g, sigma=0.001 * g, radius=2e-6, length=20e-6, rms_div=8e-6, laser=laser,
@@ -241,43 +216,427 @@ def a0_scan_workload(seed, scale=1.0):
     return colls, abi.collide_options(), prim
 
 
-def cp_shower_workload(n, seed):
-    from ptarmigan_gb300 import abi, beam
-    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6, fwhm_duration=30e-15)
-    g = beam.gamma_from_energy(16.5)
-    prim = beam.build(n, g, sigma=0.001 * g, radius=5e-6, length=24e-6, rms_div=8e-6, laser=laser, seed=seed)
-    opts = abi.collide_options(pol_resolved=1, max_generation=-1)
-    return laser, opts, prim
-
+WORKLOADS = {
+    "cp_shower": ("cp_shower: 1e7 e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 0.8 um "
+                  "30 fs; Stokes tracked (pol_resolved), pairs on, all generations", cp_shower_workload, 10_000_000),
+    "lcfa_shower": ("lcfa_shower: 1e6 e- 10 GeV 1% spread, 2x2x20 um, 50 urad; FastFocusedLaser (LCFA) a0=10 w0=4 um "
+                    "0.8 um 30 fs LP; pairs on; generations<=2", lcfa_workload, 1_000_000),
+}
 
 MLP_MARGIN = 0.25  # ln of the learned envelope's safety factor
 MLP_TRAIN = dict(n_samples=50_000_000, batch=16384, epochs=3, lr=2e-3, tau=0.98, seed=7)
 
 
-def ks_distance(a, b):
-    """Two-sample Kolmogorov-Smirnov statistic."""
-    a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
-    grid = np.concatenate([a, b])
-    return float(np.max(np.abs(np.searchsorted(a, grid, side="right") / len(a) -
-                               np.searchsorted(b, grid, side="right") / len(b))))
-
-
-def ks_critical(n, m, alpha=1e-3):
-    """Two-sample KS critical value at significance alpha."""
-    c = math.sqrt(-0.5 * math.log(alpha / 2.0))
-    return c * math.sqrt((n + m) / (n * m))
-
-
 def train_network(eng, args=None):
     cfg = dict(MLP_TRAIN)
-    if args is not None and args.train_samples:
+    if args is not None and getattr(args, "train_samples", 0):
         cfg["n_samples"] = args.train_samples
-    if args is not None and args.train_epochs:
+    if args is not None and getattr(args, "train_epochs", 0):
         cfg["epochs"] = args.train_epochs
     eng.mlp_init(3)
     return dict(eng.mlp_train(**cfg), **cfg)
 
 
+def ks_distance(a, b):
+    from ptarmigan_gb300 import equivalence
+    return equivalence.ks_distance(a, b)
+
+
+def ks_critical(n, m, alpha=1e-3):
+    from ptarmigan_gb300 import equivalence
+    return equivalence.ks_critical(n, m, alpha)
+
+
+def nbytes(d):
+    return int(sum(v.nbytes for v in d.values()))
+
+
+def step_summary(ms):
+    a = np.asarray(ms, dtype=float)
+    return {"ms": [round(float(x), 3) for x in a], "mean": float(a.mean()), "p50": float(np.percentile(a, 50)),
+            "p90": float(np.percentile(a, 90)), "max": float(a.max()), "min": float(a.min())}
+
+
+def pinned_copy(prim):
+    """The primaries in page-locked host memory, as a caller streaming
+    batches to the device would hold them."""
+    import torch
+    out = {}
+    for key, v in prim.items():
+        buf = torch.empty(max(1, v.nbytes), dtype=torch.uint8, pin_memory=True).numpy()
+        a = buf[:v.nbytes].view(v.dtype).reshape(v.shape)
+        a[...] = v
+        out[key] = a
+    return out
+
+
+# ------------------------------------------------------------- CPU legs --
+def oracle_run(laser, opts, prim, seed, threads, id_base=None):
+    """The oracle (CPU restatement of the reference) on a batch, timed."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    out, st = oracle.collide(laser, opts, prim, seed=seed, id_base=id_base, threads=threads)
+    return out, st, time.perf_counter() - t0
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle on all host cores, a bounded sample of
+    the workload per step, seeds 1000 .. 1000+K-1."""
+    if rank != 0:
+        return
+    threads = cpu_threads()
+    desc, make, _n = WORKLOADS[args.workload if args.workload in WORKLOADS else "cp_shower"]
+    per_core = args.cpu_sample_per_core or (2500 if make is cp_shower_workload else 400)
+    n_sample = max(64, per_core * threads)
+    laser, opts, prim = make(n_sample, 7)
+    for w in range(max(1, min(args.warmup, 1))):
+        small = {k: v[:min(n_sample, 16 * threads)] for k, v in prim.items()}
+        oracle_run(laser, opts, small, 99, threads)
+    vals, t_all = [], 0.0
+    for k in range(args.steps):
+        _, _, dt = oracle_run(laser, opts, prim, SEED0 + k, threads, id_base=n_sample)
+        vals.append(n_sample / dt)
+        t_all += dt
+    value = args.steps * n_sample / t_all
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "n_primaries_per_step": n_sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d primaries per step of the same workload, oracle C++ FP64 restatement of "
+                                   "src/main.rs:134-289 (the Rust reference cannot be built: no cargo/rustc)" % n_sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- timing --
+class Timer:
+    """CUDA events on the engine's stream around each call and around a
+    whole run of calls."""
+
+    def __init__(self, stream):
+        import torch
+        self.torch = torch
+        self.stream = stream
+
+    def event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+    def run(self, fn, seeds):
+        """Calls fn(seed) for each seed; returns (total ms, per-call ms,
+        per-call results)."""
+        torch = self.torch
+        torch.cuda.synchronize()
+        e_all0 = self.event()
+        per, res = [], []
+        for s in seeds:
+            e0 = self.event()
+            r = fn(s)
+            e1 = self.event()
+            per.append((e0, e1))
+            res.append(r)
+        e_all1 = self.event()
+        e_all1.synchronize()
+        torch.cuda.synchronize()
+        return e_all0.elapsed_time(e_all1), [a.elapsed_time(b) for a, b in per], res
+
+
+def roofline_fp64(stats, kern_ms, peak_tflops, kind):
+    """The dominant kernel's algorithmic FP64 work per launch over its
+    duration, against the device's measured FP64 FMA throughput."""
+    lep, pho, free = stats["lepton_steps"], stats["photon_steps"], stats.get("free_steps", 0)
+    if kind == "lma":
+        # free steps are lepton steps outside the pulse here
+        flops = (lep - free) * OPS["lma_lepton_step"] + free * OPS["free_lepton_step"] + pho * OPS["lma_photon_step"]
+        model = {k: OPS[k] for k in ("lma_lepton_step", "free_lepton_step", "lma_photon_step")}
+    else:
+        flops = lep * OPS["lcfa_lepton_step"] + pho * OPS["lcfa_photon_step"]
+        # drifting photons' steps cost a drift, not a pair step
+        flops -= free * (OPS["lcfa_photon_step"] - OPS["free_photon_step"]) if free <= pho else 0.0
+        model = {k: OPS[k] for k in ("lcfa_lepton_step", "lcfa_photon_step", "free_photon_step")}
+    achieved = flops / (kern_ms / 1e3) / 1e12
+    return {"bound": "fp64", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+            "frac": achieved / peak_tflops, "algorithmic_flops_per_launch": flops, "flops_per_event": model,
+            "peak_source": "measured in this run: FP64 FMA throughput kernel (ptg_fp64_peak); MEASURED_PEAKS.json "
+                           "has no FP64 figure"}
+
+
+# ------------------------------------------------------------ cp_shower --
+def run_cp_shower(args, eng, stream, sampler, dev):
+    """configs[4]: the learned proposal + persistent queue (value) against
+    the reference's table sampler through the wave kernels (plain_value),
+    with both cross terms, all over the same seeds."""
+    import torch
+    from ptarmigan_gb300 import abi, equivalence
+    desc, make, n_default = WORKLOADS["cp_shower"]
+    n = args.n or n_default
+    t_host = time.time()
+    laser, opts, prim = make(n, 1)
+    host_beam_ms = (time.time() - t_host) * 1e3
+    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    timer = Timer(stream)
+    # the same beam generated on the device (ptg_build_beam), timed apart:
+    # beam generation is not part of the metric
+    from ptarmigan_gb300 import beam as beam_mod
+    g = beam_mod.gamma_from_energy(16.5)
+    bd = abi.beam_desc(gamma_mean=g, gamma_sigma=0.001 * g, sigma_x=5e-6, sigma_z=24e-6, rms_div=8e-6,
+                       initial_z=beam_mod.initial_z(laser, 24e-6))
+    eng.build_beam(bd, n, seed=1)
+    device_beam_ms, _, _ = timer.run(lambda s: eng.build_beam(bd, n, seed=s), [2])
+    t0 = time.time()
+    tr = train_network(eng, args)
+    tr["wall_s"] = time.time() - t0
+
+    def coll(seed):
+        return [{"laser": laser, "seed": seed, "id_base": n, "first": 0, "count": n}]
+
+    def learned_queue(seed):
+        eng.mlp_use(True, margin=MLP_MARGIN)
+        return eng.collide_multi_device(coll(seed), opts, d_prim)[3]
+
+    def table_queue(seed):
+        eng.mlp_use(False)
+        return eng.collide_multi_device(coll(seed), opts, d_prim)[3]
+
+    def table_waves(seed):
+        eng.mlp_use(False)
+        return eng.collide_device(laser, opts, d_prim, seed=seed, id_base=n)[1]
+
+    def learned_waves(seed):
+        eng.mlp_use(True, margin=MLP_MARGIN)
+        return eng.collide_device(laser, opts, d_prim, seed=seed, id_base=n)[1]
+
+    eng.mlp_use(True, margin=MLP_MARGIN)
+    t0 = time.time()
+    tune, tune_ms = eng.queue_autotune(coll(100), opts, d_prim, sample_fraction=args.tune_fraction or 0.01)
+    tune_wall = time.time() - t0
+    seeds = [SEED0 + k for k in range(args.steps)]
+    keys = ("lepton_steps", "photon_steps", "free_steps", "emissions", "pair_events", "rejections", "n_created",
+            "n_out", "particle_errors", "max_steps")
+
+    def arm(fn, warm):
+        for w in range(warm):
+            fn(100 + w)
+        total, per, res = timer.run(fn, seeds)
+        agg = {k: (max(r[k] for r in res) if k == "max_steps" else int(sum(r[k] for r in res))) for k in keys}
+        return {"value": n * len(seeds) / (total / 1e3), "ms_total": total, "steps": step_summary(per),
+                "events_sum": agg, "device_ms": [r["device_ms"] for r in res], "last": res[-1]}
+
+    with sampler:
+        value_arm = arm(learned_queue, args.warmup)
+    plain_arm = arm(table_waves, min(args.warmup, 2))
+    lw_arm = arm(learned_waves, 1)
+    tq_arm = arm(table_queue, 1)
+
+    # end to end through the host API, the value path, the same seeds
+    prim_h = pinned_copy(prim)
+    eng.mlp_use(True, margin=MLP_MARGIN)
+    parts, _, _ = eng.collide_multi(coll(1999), opts, prim_h)  # untimed warm-up
+    del parts
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    out_value_seed0 = None
+    for s in seeds:
+        parts, _, tot = eng.collide_multi(coll(s), opts, prim_h)
+        d2h = nbytes(parts[0])
+        if s == SEED0:
+            out_value_seed0 = parts[0]
+        del parts
+    e2e_s = time.perf_counter() - t0
+    e2e = n * len(seeds) / e2e_s
+
+    # the plain path's shower for seed 1000, for the spectra
+    eng.mlp_use(False)
+    out_plain_seed0, _ = eng.collide(laser, opts, prim, seed=SEED0, id_base=n)
+    cmp_value_plain = equivalence.compare(out_value_seed0, prim, out_plain_seed0, prim)
+
+    peak = eng.fp64_peak()
+    kern_ms = float(np.mean(value_arm["device_ms"]))
+    roof = roofline_fp64(value_arm["last"], kern_ms, peak, "lma")
+    roof["kernel"] = "collide_queue_single<FOCUSED_LASER> (value path); graph device time per batch"
+    roof["traffic"] = None
+    pk, pk_kind = peaks()
+
+    line = {
+        "metric": METRIC, "value": value_arm["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": value_arm["ms_total"] / len(seeds), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "n_primaries": n, "seeds": [seeds[0], seeds[-1]],
+                   "value_path": "learned proposal + persistent single-collision queue kernel (CUDA graph, autotuned)",
+                   "plain_path": "reference table sampler + wave kernels",
+                   "autotuned": tune, "autotune_sample_ms": tune_ms, "autotune_wall_s": tune_wall,
+                   "l2": "inputs (1.2 GB) and shower store larger than L2 (no flush needed)", "margin": MLP_MARGIN},
+        "step_ms": value_arm["steps"],
+        "particle_errors": value_arm["events_sum"]["particle_errors"],
+        "max_steps_per_particle": value_arm["events_sum"]["max_steps"],
+        "events_per_step": {k: v for k, v in value_arm["last"].items() if k in keys},
+        "plain_value": plain_arm["value"], "plain_step_ms": plain_arm["steps"],
+        "plain_particle_errors": plain_arm["events_sum"]["particle_errors"],
+        "cross_terms": {
+            "learned_waves": {"value": lw_arm["value"], "step_ms": lw_arm["steps"]},
+            "table_queue": {"value": tq_arm["value"], "step_ms": tq_arm["steps"]},
+        },
+        "attribution": {
+            "sampler_gain_on_waves": lw_arm["value"] / plain_arm["value"],
+            "sampler_gain_on_queue": value_arm["value"] / tq_arm["value"],
+            "scheduler_gain_with_table": tq_arm["value"] / plain_arm["value"],
+            "scheduler_gain_with_learned": value_arm["value"] / lw_arm["value"],
+            "total": value_arm["value"] / plain_arm["value"],
+        },
+        "ks_photon_energy_vs_plain": cmp_value_plain["ks_photon_energy"],
+        "ks_critical_1e-3": cmp_value_plain["ks_photon_energy_critical"],
+        "value_vs_plain": {k: cmp_value_plain[k] for k in ("photons", "ks_photon_polar_angle", "chi2_log_energy_200",
+                                                          "chi2_dof", "chi2_p", "sigma")},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes(prim), "d2h_bytes_per_step": d2h,
+                "steps": len(seeds), "seeds": "same as value"},
+        # value path per step: the graph's 7 kernels and 4 that put the primaries in phase order
+        "gpu_launches": int(11 * len(seeds)),
+        "roofline": roof,
+        "peaks": {"source": pk_kind, "hbm_gbs": pk.get("hbm_gbs")},
+        "beam_generation_ms": {"device_ptg_build_beam": device_beam_ms, "host_numpy": host_beam_ms},
+        "training": tr,
+    }
+    if not args.no_cpu_baseline:
+        line.update(cpu_and_parity(eng, make, laser, opts, args, per_core=2500, out_value=out_value_seed0,
+                                   prim_value=prim))
+    line["clocks"] = sampler.summary()
+    return line
+
+
+def cpu_and_parity(eng, make, laser, opts, args, per_core, out_value=None, prim_value=None):
+    """The oracle on a bounded sample of the workload (the CPU baseline),
+    and the GPU's table-sampler path on exactly that batch (same primaries,
+    seed and id base): particles matched by stream, and the statistics of
+    both; plus, when given, the value path's large output against the
+    oracle's sample (independent primaries), since the value path samples
+    differently."""
+    from ptarmigan_gb300 import equivalence
+    threads = cpu_threads()
+    n_s = max(64, (args.cpu_sample_per_core or per_core) * threads)
+    _l, _o, prim_s = make(n_s, 7)
+    ref, rst, dt = oracle_run(laser, opts, prim_s, 7, threads, id_base=n_s)
+    eng.mlp_use(False)
+    out, st = eng.collide(laser, opts, prim_s, seed=7, id_base=n_s)
+    tol = 5e-7 if laser.model in (0, 2) else 1e-8
+    par = equivalence.match(out, ref, tol)
+    cmp_same = equivalence.compare(out, prim_s, ref, prim_s)
+    par.update({"sample": "%d primaries (beam seed 7), collision seed 7: the GPU's table-sampler path and the oracle"
+                          % n_s,
+                "ks_photon_energy": cmp_same["ks_photon_energy"],
+                "ks_photon_polar_angle": cmp_same["ks_photon_polar_angle"],
+                "chi2_log_energy_200": cmp_same["chi2_log_energy_200"], "chi2_dof": cmp_same["chi2_dof"],
+                "gpu": cmp_same["a"], "oracle": cmp_same["b"],
+                "events": {"gpu": {k: st[k] for k in ("lepton_steps", "photon_steps", "emissions", "pair_events")},
+                           "oracle": {k: rst[k] for k in ("lepton_steps", "photon_steps", "emissions",
+                                                          "pair_events")}}})
+    if out_value is None:
+        return {"cpu_baseline": {"value": n_s / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "%d primaries of the same workload (%.1f s), oracle C++ FP64 restatement "
+                                           "of the collision loop on %d host threads" % (n_s, dt, threads)},
+                "parity": par}
+    cmp_val = equivalence.compare(out_value, prim_value, ref, prim_s)
+    par["value_path_vs_oracle"] = {
+        "what": "the value path's seed-1000 batch against the oracle's sample (independent primaries)",
+        "ks_photon_energy": cmp_val["ks_photon_energy"], "ks_critical_1e-3": cmp_val["ks_photon_energy_critical"],
+        "ks_photon_polar_angle": cmp_val["ks_photon_polar_angle"],
+        "ks_photon_polar_angle_critical": cmp_val["ks_photon_polar_angle_critical"],
+        "chi2_log_energy_200": cmp_val["chi2_log_energy_200"], "chi2_dof": cmp_val["chi2_dof"],
+        "chi2_p": cmp_val["chi2_p"], "sigma": cmp_val["sigma"], "passes": equivalence.passes(cmp_val)}
+    return {"cpu_baseline": {"value": n_s / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d primaries of the same workload (%.1f s), oracle C++ FP64 restatement of the "
+                                       "collision loop on %d host threads" % (n_s, dt, threads)},
+            "parity": par}
+
+
+# ---------------------------------------------------------- lcfa_shower --
+def run_lcfa_shower(args, eng, stream, sampler, dev, rank, world, dist_on):
+    """configs[1]: the focused LCFA shower through the wave kernels."""
+    import torch
+    import torch.distributed as dist
+    desc, make, n_default = WORKLOADS["lcfa_shower"]
+    n = args.n or n_default
+    laser, opts, prim = make(n, 1 + rank)
+    id_base = n * world + rank * (1 << 40)
+    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    timer = Timer(stream)
+    seeds = [SEED0 + k for k in range(args.steps)]
+    keys = ("lepton_steps", "photon_steps", "free_steps", "emissions", "pair_events", "rejections", "n_created",
+            "n_out", "particle_errors", "max_steps", "waves")
+
+    def barrier():
+        if dist_on:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for w in range(args.warmup):
+        eng.collide_device(laser, opts, d_prim, seed=100 + w, id_base=id_base)
+    barrier()
+    with sampler:
+        total, per, res = timer.run(lambda s: eng.collide_device(laser, opts, d_prim, seed=s, id_base=id_base)[1],
+                                    seeds)
+    barrier()
+    if dist_on:
+        t = torch.tensor([total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = n * world * len(seeds) / (total / 1e3)
+
+    prim_h = pinned_copy(prim)
+    out, _ = eng.collide(laser, opts, prim_h, seed=1999, id_base=id_base)  # untimed warm-up
+    del out
+    barrier()
+    t0 = time.perf_counter()
+    d2h = 0
+    for s in seeds:
+        out, _ = eng.collide(laser, opts, prim_h, seed=s, id_base=id_base)
+        d2h = nbytes(out)
+        del out
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist_on:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = n * world * len(seeds) / e2e_s
+
+    peak = eng.fp64_peak()
+    kern_ms = float(np.mean([r["device_ms"] for r in res]))
+    roof = roofline_fp64(res[-1], kern_ms, peak, "lcfa")
+    roof["kernel"] = "collide_wave<FAST_FOCUSED_LASER>: the batch's device time"
+    # DRAM bytes per primary from ncu over the waves of a 1e6 batch
+    roof["traffic"] = 2.5605e9 / 1e6 * n
+    pk, pk_kind = peaks()
+    roof["hbm_frac"] = (roof["traffic"] / (kern_ms / 1e3) / 1e9) / pk.get("hbm_gbs", 6800.0)
+    agg = {k: (max(r[k] for r in res) if k == "max_steps" else int(sum(r[k] for r in res))) for k in keys}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total / len(seeds), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "n_primaries_per_gpu": n, "parallelism": "replicas x%d" % world,
+                   "seeds": [seeds[0], seeds[-1]], "l2": "inputs and shower store larger than L2 (no flush needed)"},
+        "step_ms": step_summary(per),
+        "wave_ms_per_step": [[round(x, 2) for x in r["wave_ms"][:max(1, r["waves"])]] for r in res],
+        "particle_errors": agg["particle_errors"], "max_steps_per_particle": agg["max_steps"],
+        "events_per_step": {k: res[-1][k] for k in keys},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes(prim), "d2h_bytes_per_step": d2h,
+                "steps": len(seeds), "seeds": "same as value"},
+        "gpu_launches": int(sum(2 + r["waves"] + 3 * r["ordered_waves"] for r in res)),
+        "roofline": roof,
+        "peaks": {"source": pk_kind, "hbm_gbs": pk.get("hbm_gbs")},
+        "clocks": sampler.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line.update(cpu_and_parity(eng, make, laser, opts, args, per_core=400))
+    return line
+
+
+# ------------------------------------------------------ other workloads --
 def run_learned_sampler(args, eng, sampler, line):
     n = args.n or 10_000_000
     tr = train_network(eng, args)
@@ -286,7 +645,7 @@ def run_learned_sampler(args, eng, sampler, line):
     runs, ks = [], None
     with sampler:
         for k in range(args.steps):
-            v0, v1, st = eng.sampler_bench(n, seed=1000 + k, margin=MLP_MARGIN, want_v=(k == 0))
+            v0, v1, st = eng.sampler_bench(n, seed=SEED0 + k, margin=MLP_MARGIN, want_v=(k == 0))
             runs.append(st)
             if k == 0:
                 ks = ks_distance(v0[v0 > 0], v1[v1 > 0])
@@ -316,185 +675,77 @@ def run_learned_sampler(args, eng, sampler, line):
         "gpu_launches": 5 * args.steps})
 
 
-def run_extra(args):
-    """The non-default workloads: device time with CUDA events on the
-    engine's stream, inputs resident in HBM."""
+def run_a0_scan(args, eng, timer, sampler, line, dev):
     import torch
-    from ptarmigan_gb300 import build, engine
-    build.build()
-    eng = engine.Engine(device=0)
-    stream = torch.cuda.ExternalStream(eng.stream_ptr, device=0)
-    dev = torch.device("cuda", 0)
-    sampler = ClockSampler(0)
-
-    def timed(fn):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-        r = fn()
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        e1.synchronize()
-        return e0.elapsed_time(e1), r
-
-    line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic"}
-    if args.workload == "learned_sampler":
-        run_learned_sampler(args, eng, sampler, line)
-    elif args.workload == "a0_scan":
-        colls, opts, prim = a0_scan_workload(1, scale=args.scale)
-        n = int(sum(c["count"] for c in colls))
-        d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-        tune, tune_ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=args.tune_fraction or 0.02)
-        for _ in range(args.warmup):
-            eng.collide_multi_device(colls, opts, d_prim)
-        ms, stats = [], None
-        with sampler:
-            for _ in range(args.steps):
-                t, r = timed(lambda: eng.collide_multi_device(colls, opts, d_prim))
-                ms.append(t)
-                stats = r[3]
-        # the same collisions through the single-collision entry point
-        plain_ms = 0.0
-        for c in colls:
-            sub = {k: v[c["first"]:c["first"] + c["count"]] for k, v in d_prim.items()}
-            t, _ = timed(lambda: eng.collide_device(c["laser"], opts, sub, seed=c["seed"], id_base=c["id_base"]))
-            plain_ms += t
-        line.update({"value": n / (np.mean(ms) / 1e3), "ms_per_step": float(np.mean(ms)),
-                     "plain_value": n / (plain_ms / 1e3), "plain_ms": plain_ms,
-                     "config": {"workload": "a0_scan: 64 collisions, a0 0.5..20 log, beams log-uniform 1e3..1e6 "
-                                            "e- x%g, 16.5 GeV, CP focused w0=5 um 25 fs, LMA a0<5 / LCFA a0>=5, "
-                                            "pairs on, one persistent queue launch (graph)" % args.scale,
-                                "n_primaries": n, "autotuned": tune, "autotune_sample_ms": tune_ms,
-                                "events_per_step": {k: stats[k] for k in ("lepton_steps", "photon_steps",
-                                                                          "emissions", "pair_events", "n_created",
-                                                                          "n_out", "particle_errors")}},
-                     # the graph's 7 kernels, plus the phase ordering before
-                     # it: one kernel, and three per collision of >= 2048
-                     # primaries
-                     "gpu_launches": (7 + 1 + 3 * sum(1 for c in colls if c["count"] >= 2048)) * args.steps})
-    elif args.workload == "plane_wave_lma":
-        laser, opts, prim = plane_wave_lma_workload(args.n or 10_000, 1)
-        desc = "plane_wave_lma: 1e4 e- 5 GeV 0.1%, LP PlaneWave (LMA) a0=1 cos2 30.9 cycles, emission only"
-        n = len(prim["species"])
-        d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-        for w in range(args.warmup):
-            eng.collide_device(laser, opts, d_prim, seed=100 + w)
-        ms, st = [], None
-        with sampler:
-            for k in range(args.steps):
-                t, r = timed(lambda: eng.collide_device(laser, opts, d_prim, seed=1000 + k))
-                ms.append(t)
-                st = r[1]
-        line.update({"value": n / (np.mean(ms) / 1e3), "ms_per_step": float(np.mean(ms)),
-                     "config": {"workload": desc, "n_primaries": n,
-                                "events_per_step": {k: st[k] for k in ("lepton_steps", "photon_steps", "emissions",
-                                                                       "n_out", "waves", "particle_errors")}},
-                     "gpu_launches": int((2 + st["waves"] + 3 * st["ordered_waves"]) * args.steps)})
-        if not args.no_cpu_baseline:
-            # the oracle on the same 1e4 primaries (well under a second)
-            from oracle import oracle
-            oracle.build()
-            threads = cpu_threads()
-            t0 = time.perf_counter()
-            oracle.collide(laser, opts, prim, seed=1000, threads=threads)
-            dt = time.perf_counter() - t0
-            line["cpu_baseline"] = {"value": n / dt, "unit": "primaries/s", "cores": threads, "kind": "port",
-                                    "sample": "the same %d primaries (%.2f s), oracle C++ FP64 restatement of the "
-                                              "collision loop on %d host threads" % (n, dt, threads)}
-    else:
-        run_cp_shower(args, eng, timed, sampler, line, dev)
-    line["clocks"] = sampler.summary()
-    print(json.dumps(line), flush=True)
-    eng.close()
+    colls, opts, prim = a0_scan_workload(1, scale=args.scale)
+    n = int(sum(c["count"] for c in colls))
+    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    tune, tune_ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=args.tune_fraction or 0.02)
+    for _ in range(args.warmup):
+        eng.collide_multi_device(colls, opts, d_prim)
+    with sampler:
+        total, per, res = timer.run(lambda s: eng.collide_multi_device(colls, opts, d_prim)[3], range(args.steps))
+    stats = res[-1]
+    # the same collisions through the single-collision entry point
+    plain_ms = 0.0
+    for c in colls:
+        sub = {k: v[c["first"]:c["first"] + c["count"]] for k, v in d_prim.items()}
+        t, _, _ = timer.run(lambda s: eng.collide_device(c["laser"], opts, sub, seed=c["seed"], id_base=c["id_base"]),
+                            [0])
+        plain_ms += t
+    line.update({"value": n * args.steps / (total / 1e3), "ms_per_step": total / args.steps,
+                 "step_ms": step_summary(per),
+                 "plain_value": n / (plain_ms / 1e3), "plain_ms": plain_ms,
+                 "particle_errors": int(sum(r["particle_errors"] for r in res)),
+                 "max_steps_per_particle": int(max(r["max_steps"] for r in res)),
+                 "config": {"workload": "a0_scan: 64 collisions, a0 0.5..20 log, beams log-uniform 1e3..1e6 "
+                                        "e- x%g, 16.5 GeV, LP focused w0=5 um 25 fs, LMA a0<5 / LCFA a0>=5, "
+                                        "pairs on, one persistent queue launch (graph)" % args.scale,
+                            "n_primaries": n, "autotuned": tune, "autotune_sample_ms": tune_ms,
+                            "events_per_step": {k: stats[k] for k in ("lepton_steps", "photon_steps", "free_steps",
+                                                                      "emissions", "pair_events", "n_created",
+                                                                      "n_out", "particle_errors")}},
+                 # the graph's 7 kernels, plus the phase ordering before
+                 # it: one kernel, and three per collision of >= 2048
+                 # primaries
+                 "gpu_launches": (7 + 1 + 3 * sum(1 for c in colls if c["count"] >= 2048)) * args.steps})
 
 
-def run_cp_shower(args, eng, timed, sampler, line, dev):
-    """The CP LMA shower: the learned proposal inside the persistent queue
-    kernel (value) against the reference's sampler through the wave kernels
-    (plain_value), same primaries and seeds; the photon spectra, Stokes
-    parameters and pair yields of the two are compared."""
+def run_plane_wave(args, eng, timer, sampler, line, dev):
     import torch
-    from ptarmigan_gb300 import abi
-    t_host = time.time()
-    laser, opts, prim = cp_shower_workload(args.n or 1_000_000, 1)
-    host_beam_ms = (time.time() - t_host) * 1e3
-    desc = ("cp_shower: e- 16.5 GeV 0.1%, 5x5x24 um, 8 urad; CP FocusedLaser (LMA) a0=5 w0=3 um 30 fs; "
-            "Stokes tracked, pairs on, all generations")
+    from ptarmigan_gb300 import equivalence
+    laser, opts, prim = plane_wave_lma_workload(args.n or 10_000, 1)
+    desc = "plane_wave_lma: 1e4 e- 5 GeV 0.1%, LP PlaneWave (LMA) a0=1 cos2 30.9 cycles, emission only"
     n = len(prim["species"])
     d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-    # the same beam generated on the device (ptg_build_beam), timed apart:
-    # beam generation is not part of the metric
-    from ptarmigan_gb300 import beam as beam_mod
-    g = beam_mod.gamma_from_energy(16.5)
-    bd = abi.beam_desc(gamma_mean=g, gamma_sigma=0.001 * g, sigma_x=5e-6, sigma_z=24e-6, rms_div=8e-6,
-                       initial_z=beam_mod.initial_z(laser, 24e-6))
-    eng.build_beam(bd, n, seed=1)
-    device_beam_ms, _ = timed(lambda: eng.build_beam(bd, n, seed=2))
-    tr = train_network(eng, args)
-
-    def plain(seed):
-        eng.mlp_use(False)
-        return eng.collide_device(laser, opts, d_prim, seed=seed)
-
-    def learned(seed):
-        eng.mlp_use(True, margin=MLP_MARGIN)
-        return eng.collide_multi_device([{"laser": laser, "seed": seed, "id_base": n, "first": 0, "count": n}],
-                                        opts, d_prim)
-
-    coll = [{"laser": laser, "seed": 100, "id_base": n, "first": 0, "count": n}]
-    eng.mlp_use(True, margin=MLP_MARGIN)
-    tune, tune_ms = eng.queue_autotune(coll, opts, d_prim, sample_fraction=args.tune_fraction or 0.1)
     for w in range(args.warmup):
-        plain(100 + w)
-        learned(100 + w)
-    ms_l, ms_p, st_l, st_p = [], [], None, None
+        eng.collide_device(laser, opts, d_prim, seed=100 + w)
+    seeds = [SEED0 + k for k in range(args.steps)]
     with sampler:
-        for k in range(args.steps):
-            t, r = timed(lambda: learned(1000 + k))
-            ms_l.append(t)
-            st_l = r[3]
-            t, r = timed(lambda: plain(1000 + k))
-            ms_p.append(t)
-            st_p = r[1]
-    # statistics of one step of each, through the host entry points (same seeds)
-    eng.mlp_use(False)
-    out_p, _ = eng.collide(laser, opts, prim, seed=1000)
-    eng.mlp_use(True, margin=MLP_MARGIN)
-    parts, _, _ = eng.collide_multi([{"laser": laser, "seed": 1000, "id_base": n, "first": 0, "count": n}],
-                                    opts, prim)
-    out_l = parts[0]
-    eng.mlp_use(False)
-
-    def summary(out):
-        ph = out["species"] == abi.PHOTON
-        return {"photons": int(ph.sum()), "positrons": int((out["species"] == abi.POSITRON).sum()),
-                "stokes_mean": [float(x) for x in out["pol"][ph].mean(axis=0)],
-                "mean_electron_energy_mev": float(out["u"][out["species"] == abi.ELECTRON, 0].mean() * 0.51099895)}
-    e_p = out_p["u"][out_p["species"] == abi.PHOTON, 0]
-    e_l = out_l["u"][out_l["species"] == abi.PHOTON, 0]
-    keys = ("lepton_steps", "photon_steps", "emissions", "pair_events", "n_created", "n_out", "particle_errors")
-    line.update({"value": n / (np.mean(ms_l) / 1e3), "ms_per_step": float(np.mean(ms_l)),
-                 "plain_value": n / (np.mean(ms_p) / 1e3), "plain_ms": float(np.mean(ms_p)),
-                 "ms_each_step": {"value_path": [float(x) for x in ms_l], "plain_path": [float(x) for x in ms_p]},
-                 "ks_photon_energy_vs_plain": ks_distance(e_p, e_l),
-                 "ks_critical_1e-3": ks_critical(len(e_p), len(e_l)),
-                 "learned": summary(out_l), "plain": summary(out_p),
-                 "beam_generation_ms": {"device_ptg_build_beam": device_beam_ms, "host_numpy": host_beam_ms},
-                 "training": tr,
-                 "config": {"workload": desc, "n_primaries": n, "margin": MLP_MARGIN,
-                            "value_path": "learned proposal + persistent queue kernel (CUDA graph, autotuned)",
-                            "autotuned": tune, "autotune_sample_ms": tune_ms,
-                            "plain_path": "reference sampler + wave kernels",
-                            "events_per_step_learned": {k: st_l[k] for k in keys},
-                            "events_per_step_plain": {k: st_p[k] for k in keys}},
-                 # value path: the graph's 7 kernels and 4 to order the primaries;
-                 # plain path: loading, waves (+3 each when phase-ordered), compaction
-                 "gpu_launches": int((7 + 4 + 2 + st_p["waves"] + 3 * st_p["ordered_waves"]) * args.steps)})
-
-
-def nbytes(d):
-    return int(sum(v.nbytes for v in d.values()))
+        total, per, res = timer.run(lambda s: eng.collide_device(laser, opts, d_prim, seed=s)[1], seeds)
+    st = res[-1]
+    line.update({"value": n * len(seeds) / (total / 1e3), "ms_per_step": total / len(seeds),
+                 "step_ms": step_summary(per),
+                 "particle_errors": int(sum(r["particle_errors"] for r in res)),
+                 "max_steps_per_particle": int(max(r["max_steps"] for r in res)),
+                 "config": {"workload": desc, "n_primaries": n,
+                            "events_per_step": {k: st[k] for k in ("lepton_steps", "free_steps", "photon_steps",
+                                                                   "emissions", "n_out", "waves",
+                                                                   "particle_errors")}},
+                 "gpu_launches": int(sum(2 + r["waves"] + 3 * r["ordered_waves"] for r in res))})
+    if not args.no_cpu_baseline:
+        # the oracle on the same 1e4 primaries and seed (well under a second)
+        threads = cpu_threads()
+        ref, rst, dt = oracle_run(laser, opts, prim, SEED0, threads)
+        out, _ = eng.collide(laser, opts, prim, seed=SEED0)
+        par = equivalence.match(out, ref, 5e-7)
+        cmp_same = equivalence.compare(out, prim, ref, prim)
+        par.update({"ks_photon_energy": cmp_same["ks_photon_energy"], "gpu": cmp_same["a"],
+                    "oracle": cmp_same["b"]})
+        line["cpu_baseline"] = {"value": n / dt, "unit": "primaries/s", "cores": threads, "kind": "port",
+                                "sample": "the same %d primaries (%.2f s), oracle C++ FP64 restatement of the "
+                                          "collision loop on %d host threads" % (n, dt, threads)}
+        line["parity"] = par
 
 
 def main():
@@ -504,163 +755,68 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None, help="primaries (emissions for learned_sampler)")
-    ap.add_argument("--cpu-sample-per-core", type=int, default=1500)
+    ap.add_argument("--cpu-sample-per-core", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="lcfa_shower", choices=["lcfa_shower", "plane_wave_lma", "a0_scan",
-                                                                    "cp_shower", "learned_sampler"])
+    ap.add_argument("--workload", default="cp_shower", choices=["cp_shower", "lcfa_shower", "plane_wave_lma",
+                                                                  "a0_scan", "learned_sampler"])
     ap.add_argument("--scale", type=float, default=1.0, help="a0_scan: beam-size scale")
     ap.add_argument("--tune-fraction", type=float, default=None,
-                    help="autotuner sample fraction (a0_scan 0.02, cp_shower 0.1)")
+                    help="autotuner sample fraction (a0_scan 0.02, cp_shower 0.01)")
     ap.add_argument("--train-samples", type=int, default=0,
                     help="learned_sampler, cp_shower: training samples (default 5e7)")
     ap.add_argument("--train-epochs", type=int, default=0, help="learned_sampler, cp_shower: epochs (default 3)")
     args = ap.parse_args()
-    if args.workload != "lcfa_shower" and args.impl == "gb300":
-        args.n = args.n or 0
-        run_extra(args)
-        return
-    if args.n is None:
-        args.n = N_PRIMARIES
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
 
     import torch
     import torch.distributed as dist
-
     dist_on = world > 1
     if dist_on:
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local_rank)
-
-    from ptarmigan_gb300 import abi, build, engine
+    from ptarmigan_gb300 import build, engine
     build.build()
     eng = engine.Engine(device=local_rank)
     stream = torch.cuda.ExternalStream(eng.stream_ptr, device=local_rank)
-
-    # weak scaling: every rank collides its own, disjoint set of primaries
-    laser, opts, prim = workload(args.n, seed=1 + rank)
-    id_base = args.n * world + rank * (1 << 40)
     dev = torch.device("cuda", local_rank)
-    d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
-    torch.cuda.synchronize()
-
-    def barrier():
-        if dist_on:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    # warm-up (also sizes the shower store)
-    for w in range(args.warmup):
-        _, st = eng.collide_device(laser, opts, d_prim, seed=100 + w, id_base=id_base)
-
-    # device-resident timing: CUDA events on the engine's stream
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    stats = []
-    kern_ms = []
     sampler = ClockSampler(local_rank)
-    barrier()
-    with sampler:
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-        for k in range(args.steps):
-            _, st = eng.collide_device(laser, opts, d_prim, seed=1000 + k, id_base=id_base)
-            stats.append(st)
-            kern_ms.append(st["device_ms"])
-        with torch.cuda.stream(stream):
-            ev1.record(stream)
-        ev1.synchronize()
-    barrier()
-    t_ms = ev0.elapsed_time(ev1)
-    if dist_on:
-        t = torch.tensor([t_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = args.n * world * args.steps / (t_ms / 1e3)
-
-    # end-to-end through the host API: H2D of the primaries and D2H of the
-    # shower inside the timed region
-    h2d = nbytes(prim)
-    # the primaries in page-locked host memory, as a caller streaming
-    # batches to the device would hold them
-    prim_h = {}
-    for key, v in prim.items():
-        buf = torch.empty(max(1, v.nbytes), dtype=torch.uint8, pin_memory=True).numpy()
-        a = buf[:v.nbytes].view(v.dtype).reshape(v.shape)
-        a[...] = v
-        prim_h[key] = a
-    out, _ = eng.collide(laser, opts, prim_h, seed=1999, id_base=id_base)  # untimed warm-up
-    del out
-    barrier()
-    t0 = time.perf_counter()
-    d2h = 0
-    for k in range(max(1, min(args.steps, 2))):
-        out, st_e = eng.collide(laser, opts, prim_h, seed=2000 + k, id_base=id_base)
-        d2h = nbytes(out)
-        del out
-    e2e_steps = max(1, min(args.steps, 2))
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist_on:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = args.n * world * e2e_steps / e2e_s
-
-    # roofline of the dominant kernel (collide_wave, FP64-pipe bound): FP64
-    # operations per charged and per photon step, counted by ncu on a 1e4
-    # primary batch of this workload (profiles/collide_wave_fp64_counts_n1e4.md),
-    # times this run's step counts, over the waves' device time; peak = the
-    # device's measured FP64 FMA throughput (ptg_fp64_peak).
-    pk, pk_kind = peaks()
-    st0 = stats[-1]
-    flops = st0["lepton_steps"] * FP64_PER_LEPTON_STEP + st0["photon_steps"] * FP64_PER_PHOTON_STEP
-    kern_s = float(np.mean(kern_ms)) / 1e3
-    achieved = flops / kern_s / 1e12
-    peak = eng.fp64_peak()
-    traffic = DRAM_BYTES_PER_PRIMARY * args.n
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic,
-                "peak_source": "measured in this run: FP64 FMA throughput kernel (ptg_fp64_peak); "
-                               "MEASURED_PEAKS.json has no FP64 figure",
-                "fp64_flops_per_step": {"lepton": FP64_PER_LEPTON_STEP, "photon": FP64_PER_PHOTON_STEP},
-                "hbm_frac": (traffic / kern_s / 1e9) / pk.get("hbm_gbs", 6800.0)}
-
-    # per batch: loading, each wave (and the three kernels that put it in
-    # phase order), compaction
-    launches = int(sum(2 + s["waves"] + 3 * s["ordered_waves"] for s in stats))
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_primaries_per_gpu": args.n, "parallelism": "replicas x%d" % world,
-                   "l2": "inputs and shower store larger than L2 (no flush needed)",
-                   "events_per_step": {k: stats[-1][k] for k in ("lepton_steps", "photon_steps", "emissions",
-                                                                 "pair_events", "n_created", "n_out", "waves")}},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches,
-        "clocks": sampler.summary(),
-        "roofline": roofline,
-        "peaks": {"source": pk_kind, "hbm_gbs": pk.get("hbm_gbs")},
-    }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = cpu_threads()
-        n_sample = max(64, args.cpu_sample_per_core * threads)
-        v, st_c, dt = cpu_run(n_sample, 7, threads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "%d primaries of the same workload (%.1f s), oracle C++ FP64 restatement "
-                                          "of the collision loop on %d host threads" % (n_sample, dt, threads)}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    eng.close()
-    if dist_on:
-        dist.destroy_process_group()
+    try:
+        if args.workload == "lcfa_shower":
+            line = run_lcfa_shower(args, eng, stream, sampler, dev, rank, world, dist_on)
+        elif args.workload == "cp_shower":
+            # replicas: every rank runs the whole workload on its own GPU
+            line = run_cp_shower(args, eng, stream, sampler, dev)
+            if dist_on:
+                t = torch.tensor([line["ms_per_step"]], device=dev)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                line["ms_per_step"] = float(t.item())
+                line["value"] = line["config"]["n_primaries"] * world / (line["ms_per_step"] / 1e3)
+                line["n_gpus"] = world
+                line["config"]["parallelism"] = "replicas x%d" % world
+        else:
+            line = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic"}
+            timer = Timer(stream)
+            if args.workload == "learned_sampler":
+                run_learned_sampler(args, eng, sampler, line)
+            elif args.workload == "a0_scan":
+                run_a0_scan(args, eng, timer, sampler, line, dev)
+            else:
+                run_plane_wave(args, eng, timer, sampler, line, dev)
+            line["clocks"] = sampler.summary()
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+    finally:
+        eng.close()
+        if dist_on:
+            dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -548,6 +548,13 @@ typedef struct {
 ptg_status ptg_particle_sums(ptg_ctx* ctx, const ptg_particles* particles, const ptg_stats_spec* spec,
                              ptg_stats_sums* out);
 
+/* control:increase_pair_rate_by: auto (main.rs:294-319, 1001-1034): the
+ * ratio of the photon emission and pair creation probabilities for a
+ * particle of Lorentz factor `gamma` meeting the laser head on, from the
+ * LCFA rates (the laser's a0 and wavelength) or, for the LMA models, the
+ * LMA rates at the laser's rms amplitude (then at least 1). */
+ptg_status ptg_pair_rate_increase(ptg_ctx* ctx, const ptg_laser_desc* laser, double gamma, double* ratio);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */
 ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);

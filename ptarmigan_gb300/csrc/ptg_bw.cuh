@@ -166,30 +166,38 @@ static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, doub
     return true;
 }
 
-// A bound on each component of bw_by_summation's result.  For x >= 0 and
-// m >= 0, |J_m(x)| <= (x/2)^m / m!.  The integrand of bw_integrate is at
-// most J_n^2 (1 + k) + k (J_{n-1}^2 + J_{n+1}^2) with k = a^2 q / 2, where q
-// is at most its value at s_min (q falls on (0, 1/2]) and the Bessel
-// argument is at most n a / sqrt(1 + a^2); the quadrature weights of a
-// harmonic sum to s_max - s_min <= 1/2 and bw_integrate doubles the sum.
-// Harmonics below threshold (s_n <= 4) contribute nothing, as there.
+// A bound on each component of bw_by_summation's result, in closed form.
+// For x >= 0 and m >= 0, |J_m(x)| <= (x/2)^m / m!.  The integrand of
+// bw_integrate is at most J_n^2 (1 + k) + k (J_{n-1}^2 + J_{n+1}^2) with
+// k = a^2 q / 2, the Bessel argument is at most n c with c = a / sqrt(1 +
+// a^2), and the quadrature weights of a harmonic sum to s_max - s_min <=
+// 1/2 while bw_integrate doubles the sum.  With u_n = (n c / 2)^n / n!,
+// J_{n-1} <= u_n 2 / c, J_n <= u_n and J_{n+1} <= u_n c / 2, so harmonic n
+// contributes at most u_n^2 (1 + k_n K) with K = 1 + 4 / c^2 + c^2 / 4.
+// q falls as s_min rises and s_min >= 1 / s_n, so q <= 1 + beta n with
+// beta = 2 eta / (1 + a^2).  u_{n+1} / u_n = (c / 2)(1 + 1/n)^n < r = e c
+// / 2, and n! >= sqrt(2 pi n) (n / e)^n gives u_{n0} <= r^n0 / sqrt(2 pi
+// n0).  Summing over every n >= n0 (bw_sum_limits' first harmonic) with
+// rho = r^2 < 1 (a < 0.3 here: rho < 0.16):
+//   sum <= r^(2 n0) / (2 pi n0) [(A + B n0) / (1 - rho) + B rho / (1 - rho)^2]
+// with A = 1 + a^2 K / 2 and B = a^2 K beta / 2.  One exponential and one
+// logarithm, where a harmonic-by-harmonic bound would take one of each and
+// a log-gamma per harmonic.
 __device__ __forceinline__ double bw_summation_bound(double a, double eta) {
     int n0, n1;
     bw_sum_limits(a, eta, &n0, &n1);
-    double a2 = a * a, c = a / sqrt(1.0 + a2);
-    double total = 0.0;
-    for (int n = n0; n <= n1; ++n) {
-        double sn = 2.0 * n * eta / (1.0 + a2);
-        if (sn <= 4.0) continue;
-        double s_min = fmin(0.5 * (1.0 - sqrt(1.0 - 4.0 / sn)), 0.5);
-        double q = (1.0 - s_min) / s_min + s_min / (1.0 - s_min);
-        double x = 0.5 * n * c;
-        double bm = exp((n - 1) * log(x) - lgamma((double)n));  // bound on J_{n-1}
-        double b = bm * x / n, bp = b * x / (n + 1);             // J_n, J_{n+1}
-        double k = 0.5 * a2 * q;
-        total += b * b * (1.0 + k) + k * (bm * bm + bp * bp);
-    }
-    return total;
+    double a2 = a * a;
+    double c = a / sqrt(1.0 + a2);
+    double r = 0.5 * 2.718281828459045 * c;
+    double rho = r * r;
+    if (!(rho < 1.0)) return HUGE_VAL;
+    double K = 1.0 + 4.0 / (c * c) + 0.25 * c * c;
+    double beta = 2.0 * eta / (1.0 + a2);
+    double A = 1.0 + 0.5 * a2 * K, B = 0.5 * a2 * K * beta;
+    double n = (double)n0;
+    double lead = exp(2.0 * n * log(r)) / (2.0 * PI * n);
+    double om = 1.0 - rho;
+    return lead * ((A + B * n) / om + B * rho / (om * om));
 }
 
 // Per-step pair probabilities below this are taken as zero where the rate
@@ -199,13 +207,18 @@ __device__ __forceinline__ double bw_summation_bound(double a, double eta) {
 // the interaction count differs by less than this per step.
 constexpr double PAIR_PROB_NEGLIGIBLE = 1e-25;
 
+// exp(LN_MIN_A) of the CP total-rate table, the smallest amplitude it covers,
+// as the host's libm rounds it (0.3); evaluating it on every step cost an
+// FP64 exponential.
+constexpr double BW_CP_MIN_A = 0.3;
+
 // TotalRate::value / probability dispatch (pair_creation/cp/mod.rs:265-287)
 __device__ __forceinline__ bool bw_rates(const double* T, double a, double eta, double* f0, double* f1) {
     if (a < 0.02 || bw_is_too_small(a, eta)) {
         *f0 = *f1 = 0.0;
         return true;
     }
-    if (a < exp(PTG_BW_CP_LN_MIN_A)) {
+    if (a < BW_CP_MIN_A) {
         bw_by_summation(a, eta, f0, f1);
         return true;
     }
@@ -310,7 +323,7 @@ static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 s
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
     double f0, f1;
     double c = ALPHA_FINE * dphi / eta;
-    if (a >= 0.02 && a < exp(PTG_BW_CP_LN_MIN_A) && !bw_is_too_small(a, eta) &&
+    if (a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta) &&
         c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE) {
         // the summed rate cannot give a probability that matters: skip it
         f0 = f1 = 0.0;

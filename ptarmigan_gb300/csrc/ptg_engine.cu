@@ -209,6 +209,9 @@ static FieldParams make_field(const ptg_laser_desc& d, double* dt_max) {
     // ones fall below 2^-60 / max(1, norm a0^2).  Chirped plane waves and
     // the finite-bandwidth option (which draws a width on every step) are
     // left out.
+    f.inv_w2 = 1.0 / (d.waist * d.waist);
+    f.asq0 = (f.circular ? 1.0 : 0.5) * d.a0 * d.a0;
+    f.env_c = 4.0 * LN_2 / ((f.omega * f.duration) * (f.omega * f.duration));
     f.lma_cut = 0.0;
     if (!lcfa && f.chirp_b == 0.0 && !d.finite_bandwidth) {
         double norm = f.circular ? 1.0 : 0.5;
@@ -415,7 +418,7 @@ __global__ void k_eval_fields(FieldParams f, unsigned long long n, const double*
     } else {
         e = mk3(0, 0, 0);
         b = mk3(0, 0, 0);
-        aa = sqrt(lma_a_sqd(f, rr));
+        aa = sqrt(lma_asq(f, rr));
     }
     E[3 * i] = e.x, E[3 * i + 1] = e.y, E[3 * i + 2] = e.z;
     B[3 * i] = b.x, B[3 * i + 1] = b.y, B[3 * i + 2] = b.z;
@@ -854,6 +857,20 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
         e = cudaMemcpy(p, data.data(), 8 * data.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
         *slot = (const double*)p;
+        // FP32 copies of the emission rate tables (the per-step bound)
+        const float** slot32 = nullptr;
+        if (std::strcmp(w.name, "nlc_cp_rate") == 0) slot32 = &host.nlc_cp_rate32;
+        if (std::strcmp(w.name, "nlc_lp_rate") == 0) slot32 = &host.nlc_lp_rate32;
+        if (slot32) {
+            std::vector<float> f32(data.begin(), data.end());
+            void* q = nullptr;
+            e = cudaMalloc(&q, 4 * f32.size());
+            if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            bufs.push_back(q);
+            e = cudaMemcpy(q, f32.data(), 4 * f32.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+            *slot32 = (const float*)q;
+        }
     }
     CUDA_TRY(cudaMemcpy(c->lma_dev, &host, sizeof(LmaTables), cudaMemcpyHostToDevice));
     c->lma_host = host;
@@ -2185,6 +2202,75 @@ ptg_status ptg_lcfa_pair_t(ptg_ctx* c, size_t n, const double* chi, double* t_pa
     });
 }
 
+
+// main.rs:294-319 (increase_pair_rate_by, increase_lcfa_pair_rate_by): the
+// photon emission probability over the pair creation probability for a
+// particle of Lorentz factor gamma meeting the laser head on.  out[0] is the
+// ratio, out[1] a ptg status (the lookups the reference unwraps may leave
+// their tables).
+__global__ void k_pair_rate_increase(int lcfa, int circular, double gamma, double a0, double wavelength,
+                                     const LmaTables* lma, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (lcfa) {
+        double omega_mc2 = 1.26e-6 / (ELECTRON_MASS_MEV * 1.0e6 * wavelength);
+        double chi = 2.0 * gamma * a0 * omega_mc2;
+        double t_par, t_perp;
+        lcfa_auxiliary_t(chi, &t_par, &t_perp);
+        // lcfa::pair_creation::probability for an unpolarised photon, dt = 1
+        double pair = ALPHA_FINE * chi * (0.5 * t_par + 0.5 * t_perp) * 1.0 / (COMPTON_TIME * gamma);
+        out[0] = lcfa_photon_rate(chi, gamma) / pair;
+        out[1] = 0.0;
+        return;
+    }
+    double kk = SPEED_OF_LIGHT * COMPTON_TIME * 2.0 * PI / wavelength;
+    d4 kappa = d4{kk, 0.0, 0.0, kk};
+    d4 ell = d4{gamma, 0.0, 0.0, -gamma};
+    d4 u = d4{sqrt(1.0 + gamma * gamma), 0.0, 0.0, -gamma};
+    double a_rms = circular ? a0 : a0 / SQRT_2;
+    double sq = a_rms * a_rms / (2.0 * dot4(kappa, u));
+    d4 q = d4{u.t + sq * kappa.t, u.x + sq * kappa.x, u.y + sq * kappa.y, u.z + sq * kappa.z};
+    double dt = wavelength / SPEED_OF_LIGHT;
+    // pair_creation::probability (pair_creation/mod.rs:21-42), unpolarised
+    double eta = dot4(kappa, ell);
+    double dphi = eta * dt / (COMPTON_TIME * ell.t);
+    double f[2] = {0.0, 0.0};
+    bool ok = circular ? bw_rates(lma->bw_cp_total, a_rms, eta, &f[0], &f[1])
+                       : lpp_rates(lma->bw_lp_total, lma->bw_lp_mid_total, a_rms * SQRT_2, eta, f);
+    double pair = (ALPHA_FINE * dphi / eta) * (0.5 * (f[0] + f[1]));
+    // nonlinear_compton::probability (nonlinear_compton/mod.rs:19-47)
+    double a2 = dot4(q, q) - 1.0;
+    double a = a2 >= 0.0 ? sqrt(a2) : 0.0;
+    double eta_q = dot4(kappa, q);
+    double dphi_q = dt * eta_q / (COMPTON_TIME * q.t);
+    double rate = 0.0;
+    NlcTables nt = nlc_view(*lma);
+    bool ok_q = circular ? cp_rate(nt, a, eta_q, &rate) : lp_rate(nt, a * SQRT_2, eta_q, &rate);
+    double photon = ALPHA_FINE * rate * dphi_q / eta_q;
+    out[0] = (pair == 0.0) ? 1.0 : fmax(photon / pair, 1.0);
+    out[1] = (ok && ok_q) ? 0.0 : 2.0;  // PTG_ERR_OUT_OF_TABLE
+}
+
+ptg_status ptg_pair_rate_increase(ptg_ctx* c, const ptg_laser_desc* laser, double gamma, double* ratio) {
+    if (!c || !ratio) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    ptg_status st = check_laser(laser);
+    if (st != PTG_OK) return st;
+    if (!(gamma >= 1.0)) return set_err(PTG_ERR_INVALID_ARGUMENT, "gamma must be at least 1");
+    bool lcfa = laser->model == PTG_FAST_PLANE_WAVE || laser->model == PTG_FAST_FOCUSED_LASER;
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (!lcfa && !c->tables_loaded) {
+        st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    double out[2] = {0.0, 0.0};
+    st = with_device_buffers(c, {{out, sizeof(out)}}, [&](std::vector<void*>& d) {
+        k_pair_rate_increase<<<1, 32, 0, c->stream>>>(lcfa ? 1 : 0, laser->polarization == PTG_POL_CIRCULAR ? 1 : 0,
+                                                      gamma, laser->a0, laser->wavelength, c->lma_dev, (double*)d[0]);
+    });
+    if (st != PTG_OK) return st;
+    if (out[1] != 0.0) return set_err(PTG_ERR_OUT_OF_TABLE, "a rate lookup left its table");
+    *ratio = out[0];
+    return PTG_OK;
+}
 
 // ------------------------------------------------- table maintenance ---
 // Regenerates the CP harmonic CDF table on the device (the reference tree

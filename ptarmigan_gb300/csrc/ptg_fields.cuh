@@ -30,6 +30,7 @@ struct FieldParams {
     double chi_scale;          // field scale of lcfa_fields32 over the critical field
     double drift_ell_max;      // LCFA photons with ell^0 below this never create pairs (0 = off)
     double lma_cut;            // LMA: |phase| beyond which <a^2> < 2^-60 (0 = off)
+    double inv_w2, asq0, env_c; // focused LMA: 1 / waist^2, norm a0^2, 4 ln 2 / (omega duration)^2
     // FP32 copies for the per-step FP32 path (converted once on the host,
     // the same rounding as a conversion on the device)
     float eps32, cos_pa32, sin_pa32, inv_tau32, chi_scale32;
@@ -404,6 +405,44 @@ __device__ __forceinline__ d4 lma_grad_a_sqd(const FieldParams& f, d4 r) {
     return d4{-t, -(gb0 * env), -(gb1 * env), -t};
 }
 
+// focused_laser.rs:80-161 with the Gaussian envelope: <a^2> and its raised
+// four-gradient from one exponential (the beam's and the envelope's
+// factors combined) and one division, with the reciprocals of the waist,
+// Rayleigh range and duration formed on the host.  The same quantities as
+// lma_a_sqd and lma_grad_a_sqd to a few ulps.
+__device__ __forceinline__ double lma_fg_a_sqd(const FieldParams& f, d4 r) {
+    double zz = r.z * f.inv_zr;
+    double iw = 1.0 / (1.0 + zz * zz);
+    double rho2 = (r.x * r.x + r.y * r.y) * f.inv_w2;
+    double phase = phase_of(f, r);
+    return f.asq0 * exp(-2.0 * rho2 * iw - f.env_c * (phase * phase)) * iw;
+}
+
+__device__ __forceinline__ d4 lma_fg_grad_a_sqd(const FieldParams& f, d4 r) {
+    double zz = r.z * f.inv_zr;
+    double iw = 1.0 / (1.0 + zz * zz);
+    double rho2 = (r.x * r.x + r.y * r.y) * f.inv_w2;
+    double phase = phase_of(f, r);
+    double be = f.asq0 * exp(-2.0 * rho2 * iw - f.env_c * (phase * phase)) * iw;  // beam * envelope
+    double gx = -4.0 * be * r.x * f.inv_w2 * iw;
+    double gy = -4.0 * be * r.y * f.inv_w2 * iw;
+    double gz = (2.0 * be * r.z * (f.inv_zr * f.inv_zr) * iw) * (2.0 * rho2 * iw - 1.0);
+    double t = be * (2.0 * f.k * f.env_c * phase) + gz;
+    return d4{-t, -gx, -gy, -t};
+}
+
+__device__ __forceinline__ bool lma_fast_gauss(const FieldParams& f) {
+    return f.model == M_FOCUSED_LASER && f.envelope == ENV_GAUSSIAN;
+}
+
+// <a^2> and its gradient for any LMA model
+__device__ __forceinline__ double lma_asq(const FieldParams& f, d4 r) {
+    return lma_fast_gauss(f) ? lma_fg_a_sqd(f, r) : lma_a_sqd(f, r);
+}
+__device__ __forceinline__ d4 lma_grad(const FieldParams& f, d4 r) {
+    return lma_fast_gauss(f) ? lma_fg_grad_a_sqd(f, r) : lma_grad_a_sqd(f, r);
+}
+
 // A whole LMA step lies where <a^2> < 2^-60 (f.lma_cut): either it ends
 // before the pulse (the phase k(t - z) of a massive particle only grows, by
 // at most 2 k c dt per step) or it starts after it.
@@ -446,24 +485,24 @@ __device__ __forceinline__ void lma_push(const FieldParams& f, d4 r0, d4 u0, dou
     auto kdot = [&](d4 u) { return kk * u.t - kk * u.z; };
     d4 u_mid = d4{0.0, 0.0, 0.0, 0.0};
     if (rr) {
-        d4 g4 = lma_grad_a_sqd(f, r0);
+        d4 g4 = lma_grad(f, r0);
         double fs = 0.5 * SPEED_OF_LIGHT * scale;
         double eta = SPEED_OF_LIGHT * COMPTON_TIME * kdot(u0);
-        double llc = scale * scale * (-2.0 * ALPHA_FINE * lma_a_sqd(f, r0) * eta * eta) / (3.0 * COMPTON_TIME);
+        double llc = scale * scale * (-2.0 * ALPHA_FINE * lma_asq(f, r0) * eta * eta) / (3.0 * COMPTON_TIME);
         u_mid = d4{u0.t + 0.5 * (fs * g4.t + llc * u0.t) * dtau, u0.x + 0.5 * (fs * g4.x + llc * u0.x) * dtau,
                    u0.y + 0.5 * (fs * g4.y + llc * u0.y) * dtau, u0.z + 0.5 * (fs * g4.z + llc * u0.z) * dtau};
     }
     double h = 0.5 * SPEED_OF_LIGHT * dtau;
     d4 r = d4{r0.t + h * u0.t, r0.x + h * u0.x, r0.y + h * u0.y, r0.z + h * u0.z};
     double dt_actual = 0.5 * u0.t * dtau;
-    d4 g4 = lma_grad_a_sqd(f, r);
+    d4 g4 = lma_grad(f, r);
     double fs = 0.5 * SPEED_OF_LIGHT * scale;
     d4 fv = d4{fs * g4.t, fs * g4.x, fs * g4.y, fs * g4.z};
     d4 gv = d4{0.0, 0.0, 0.0, 0.0};
     double asq_mid = 0.0;
     if (rr) {
         double eta = SPEED_OF_LIGHT * COMPTON_TIME * kdot(u_mid);
-        asq_mid = lma_a_sqd(f, r);
+        asq_mid = lma_asq(f, r);
         double llc = scale * scale * (-2.0 * ALPHA_FINE * asq_mid * eta * eta) / (3.0 * COMPTON_TIME);
         gv = d4{llc * u_mid.t, llc * u_mid.x, llc * u_mid.y, llc * u_mid.z};
     }
@@ -479,7 +518,7 @@ __device__ __forceinline__ void lma_push(const FieldParams& f, d4 r0, d4 u0, dou
     }
     r = d4{r.t + h * u.t, r.x + h * u.x, r.y + h * u.y, r.z + h * u.z};
     dt_actual = dt_actual + 0.5 * u.t * dtau;
-    double b = 1.0 + lma_a_sqd(f, r);
+    double b = 1.0 + lma_asq(f, r);
     u.t = sqrt(b + u.x * u.x + u.y * u.y + u.z * u.z);
     *r_out = r;
     *u_out = u;

@@ -27,7 +27,23 @@ struct LmaTables {
     const double* bw_lp_mid_cdf;    // [5652][16][3] (regenerated)
     const double* nlc_cp_cl_cdf;    // [61][32][2]
     const double* nlc_lp_cl_cdf;    // [61][16][2]
+    // FP32 copies of the two emission rate tables, for the per-step bound
+    const float* nlc_lp_rate32;     // [68][61]
+    const float* nlc_cp_rate32;     // [70][61]
 };
+
+// The per-step emission probability is first evaluated in FP32 from the
+// FP32 rate tables (rate32_cp / rate32_lp).  Its relative error is below
+// 2e-5: the logarithms of a and eta are within about 1e-6 and so the table
+// coordinates within 2.1e-5 of a cell; the tables' ln-rate changes by at
+// most 0.23 per cell and has magnitude at most 16, so the interpolated
+// ln-rate is within 1.5e-5; expf and the products add under 1e-6.  A draw
+// above the FP32 probability by more than 2^-10 of it is a step without an
+// emission whatever the FP64 probability is; every other draw is decided
+// against the FP64 probability, as the reference decides it.  The decisions
+// are therefore the reference's, and the FP64 rate is evaluated on only
+// about as many steps as emit.
+constexpr double PROB32_MARGIN = 1.0 / 1024.0;
 
 __device__ __forceinline__ NlcTables nlc_view(const LmaTables& t) {
     return NlcTables{t.nlc_lp_rate,    t.nlc_lp_cdf,     t.nlc_cp_rate,   t.nlc_cp_cdf,
@@ -85,6 +101,18 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
     double eta = dot4(kappa, u);
     double dphi = dt * eta / (COMPTON_TIME * u.t);
     NlcTables nt = nlc_view(t);
+    // the event draw, then the FP32 bound on the probability: a draw well
+    // above it is a step without an emission (see PROB32_MARGIN)
+    double u_event = rng.next();
+    if (!classical) {
+        float r32;
+        bool in32 = f.circular ? rate32_cp(t.nlc_cp_rate32, aq, eta, &r32)
+                               : rate32_lp(t.nlc_lp_rate32, aq * SQRT_2, eta, &r32);
+        if (in32) {
+            float p32 = (float)(ALPHA_FINE / COMPTON_TIME) * r32 * ((float)dt / (float)u.t);
+            if (u_event > (double)p32 * (1.0 + PROB32_MARGIN)) return 0;
+        }
+    }
     double rate;
     bool ok;
     if (f.circular)
@@ -93,7 +121,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
         ok = classical ? lp_classical_rate(nt, aq * SQRT_2, eta, &rate) : lp_rate(nt, aq * SQRT_2, eta, &rate);
     if (!ok) return 2;  // PTG_ERR_OUT_OF_TABLE
     double prob = ALPHA_FINE * rate * dphi / eta;
-    if (rng.next() < prob) {
+    if (u_event < prob) {
         int n;
         double s, cphi;
         d3 sv;
@@ -136,7 +164,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
         *k_out = k;
         *u_prime = d4{u.t + n * kappa.t - k.t, u.x + n * kappa.x - k.x, u.y + n * kappa.y - k.y, u.z + n * kappa.z - k.z};
         // the local amplitude, needed only for the photon's record
-        double a = sqrt(lma_a_sqd(f, r));
+        double a = sqrt(lma_asq(f, r));
         *a_eff = a;
         *chi = a * dot4(u, kappa);
         *absorption = n * kappa.t;
@@ -192,7 +220,7 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
     *prob = 0.0;
     *pol_new = pol;
     *created = false;
-    double a = sqrt(lma_a_sqd(f, r));
+    double a = sqrt(lma_asq(f, r));
     double chirp = 1.0;
     if (f.model == M_PLANE_WAVE) {
         chirp = 1.0 + 2.0 * f.chirp_b * phase_of(f, r);

@@ -19,8 +19,13 @@ stats (electron / photon / positron, and expressions), constants,
 output:dump_all_particles: hdf5 (the final-state file of main.rs:1289-1715,
 written by ptarmigan_gb300.hdf5) and beam:from_hdf5 (particle/loader.rs,
 for files with the structures ptarmigan_gb300.hdf5 reads).
-Not supported: beam:spectrum, intermediate-particle output,
-increase_pair_rate_by: auto and stop_at_time: auto.
+Also: beam:spectrum (a function of gamma over [min, max], or a file of
+spectral values), control:increase_pair_rate_by: auto, control:
+stop_at_time: auto (every final-state particle moved to the latest time any
+of them reached) and a given stop time (every particle moved to it), and
+the decayed intermediate photons (output:intermediate distributions,
+stats:intermediate, output:dump_decayed_photons into the HDF5 file's
+intermediate-state group).
 """
 
 import math
@@ -75,7 +80,76 @@ def laser_from_input(inp, a0):
                           chirp_b=chirp, finite_bandwidth=inp.bool("control:bandwidth_correction", False))
 
 
-def beam_from_input(inp, laser):
+def spectrum_from_input(inp, n_part, input_path=""):
+    """beam:spectrum (main.rs:610-680): `function` (an expression in gamma)
+    sampled at `resolution` points (default 10 + 2 n^(1/3)) from `min` in
+    steps of (max - min) / resolution, or `file`, one spectral value per
+    line (relative to the input file), over [min, max] or from min in steps
+    of `step`.  Returns (values, min, max, step)."""
+    analytical = inp.contains("beam:spectrum:function")
+    numerical = inp.contains("beam:spectrum:file")
+    if analytical and numerical:
+        raise InputError("specify a function or a file in beam:spectrum, not both.")
+    g_min = inp.float("beam:spectrum:min")
+    if analytical:
+        g_max = inp.float("beam:spectrum:max")
+        n = inp.int("beam:spectrum:resolution") if inp.contains("beam:spectrum:resolution") else \
+            int(10.0 + 2.0 * float(n_part) ** (1.0 / 3.0))
+        step = (g_max - g_min) / n
+        func = inp.func("beam:spectrum:function", "gamma")
+        vals = [func(g_min + i * step) for i in range(n)]
+        if not all(math.isfinite(v) for v in vals):
+            raise InputError("beam:spectrum:function evaluated to non-numerical values in the specified domain.")
+        return vals, g_min, g_max, step
+    fname = inp.str("beam:spectrum:file")
+    out_dir = os.path.dirname(input_path)
+    fname = os.path.join(out_dir, fname) if out_dir else fname
+    try:
+        with open(fname) as fh:
+            text = fh.read()
+    except OSError:
+        raise InputError('Unable to open "%s": no such file or directory.' % fname)
+    try:
+        vals = [float(line) for line in text.splitlines()]
+    except ValueError:
+        raise InputError('Unable to import "%s" as a 1D array of spectral values.' % fname)
+    n = len(vals) - 1  # steps, not entries
+    if inp.contains("beam:spectrum:max"):
+        g_max = inp.float("beam:spectrum:max")
+        step = (g_max - g_min) / n
+    else:
+        step = inp.float("beam:spectrum:step")
+        g_max = g_min + n * step
+    if not all(math.isfinite(v) for v in vals):
+        raise InputError("beam:spectrum:file contains non-numerical values.")
+    return vals, g_min, g_max, step
+
+
+def custom_cdf(vals, g_min, step):
+    """GammaDistribution::custom (particle/dstr.rs:88-106): CDF nodes
+    [gamma, cumulative / total], gamma advanced by repeated addition of the
+    step.  Returns the [len][2] array for the device builder."""
+    total = sum(vals)
+    cdf = [[g_min, 0.0]]
+    g, rt = g_min, 0.0
+    for v in vals:
+        g += step
+        rt += v
+        cdf.append([g, rt / total])
+    return np.ascontiguousarray(np.array(cdf, dtype=np.float64))
+
+
+def spectrum_mean_gamma(vals, g_min, step):
+    """GammaDistribution::gamma for a custom spectrum (dstr.rs:112-125)."""
+    m0 = m1 = 0.0
+    for i, f in enumerate(vals):
+        g = g_min + i * step
+        m0 += f
+        m1 += g * f
+    return m1 / m0
+
+
+def beam_from_input(inp, laser, input_path=""):
     """main.rs:481-811 (rng-distributed beams); returns (desc, n, species)."""
     species = SPECIES.get(inp.str("beam:species", "electron"))
     if species is None:
@@ -86,11 +160,16 @@ def beam_from_input(inp, laser):
     if w1 is not None and w2 is not None and w1 != w2:
         raise InputError("conflicting values of 'n_real' and 'charge'")
     weight = w1 if w1 is not None else (w2 if w2 is not None else 1.0)
-    if inp.contains("beam:spectrum"):
-        raise InputError("beam:spectrum is not supported by this driver")
     brem = species == abi.PHOTON and inp.bool("beam:bremsstrahlung_source", False)
     kw = {}
-    if brem:
+    spectrum = spectrum_from_input(inp, n, input_path) if inp.contains("beam:spectrum") else None
+    cdf = None
+    if spectrum is not None:
+        vals, g_min, g_max, step = spectrum
+        cdf = custom_cdf(vals, g_min, step)
+        kw.update(gamma_dstr=abi.GAMMA_CUSTOM, custom_cdf=cdf)
+        brem = False
+    elif brem:
         kw.update(gamma_dstr=abi.GAMMA_BREM, gamma_min=inp.float("beam:gamma_min"), gamma_max=inp.float("beam:gamma"))
     else:
         kw.update(gamma_mean=inp.float("beam:gamma"), gamma_sigma=inp.float("beam:sigma", 0.0))
@@ -128,10 +207,47 @@ def beam_from_input(inp, laser):
                          rms_div=inp.float("beam:rms_divergence", 0.0),
                          collision_angle=inp.float("beam:collision_angle", 0.0), collision_plane=plane,
                          offset=tuple(offset), initial_z=initial_z, stokes=tuple(stokes), weight=weight, **kw)
+    desc.cdf_nodes = cdf  # the custom spectrum's nodes outlive the descriptor's use
+    desc.spectrum_gamma = spectrum_mean_gamma(spectrum[0], spectrum[1], spectrum[3]) if spectrum else None
     return desc, n, species, inp.float("beam:collision_angle", 0.0), plane
 
 
-def options_from_input(inp, keep_decayed):
+def stop_mode(inp):
+    """control:stop_at_time (main.rs:346-361): "auto" (every particle is
+    moved to the latest time any reached), a time in seconds (tracking
+    stops there and every particle is moved to it), or absent."""
+    if not inp.contains("control:stop_at_time"):
+        return None
+    s = inp.str("control:stop_at_time")
+    if s == "auto":
+        return "auto"
+    try:
+        return inp.evaluate(s)
+    except InputError:
+        raise InputError("control:stop_at_time must be a numerical value or 'auto'.")
+
+
+def rate_increase_from_input(inp, eng, laser, desc, spectrum_gamma=None):
+    """control:increase_pair_rate_by (main.rs:1001-1034): a number, or
+    "auto" for a beam built from its distributions (the ratio of the photon
+    emission and pair creation rates at the beam's mean Lorentz factor)."""
+    if not inp.contains("control:increase_pair_rate_by"):
+        return 1.0
+    v = inp.str("control:increase_pair_rate_by")
+    if v != "auto":
+        return inp.float("control:increase_pair_rate_by")
+    if desc is None:
+        raise InputError("automatic increase in pair creation not available when loading particles from file.")
+    if spectrum_gamma is not None:
+        gamma = spectrum_gamma
+    elif desc.gamma_dstr == abi.GAMMA_BREM:
+        gamma = desc.gamma_max
+    else:
+        gamma = desc.gamma_mean
+    return eng.pair_rate_increase(laser, gamma)
+
+
+def options_from_input(inp, keep_decayed, rate_increase=None):
     """main.rs:339-398, 862-880 and 1106-1124."""
     classical_s = inp.str("control:classical", "false")
     classical, gaunt = {"true": (True, False), "false": (False, False),
@@ -139,19 +255,23 @@ def options_from_input(inp, keep_decayed):
     if classical is None:
         raise InputError("control:classical must be one of 'true', 'false' or 'gaunt_factor_corrected'")
     mult = inp.int("control:select_multiplicity") if inp.contains("control:select_multiplicity") else -1
-    rate = inp.float("control:increase_pair_rate_by", 1.0)
+    if rate_increase is None:
+        if inp.str("control:increase_pair_rate_by", "") == "auto":
+            raise InputError("increase_pair_rate_by: auto is evaluated for the beam (rate_increase_from_input)")
+        rate_increase = inp.float("control:increase_pair_rate_by", 1.0)
+    rate = rate_increase
     if rate < 1.0:
-        raise InputError("increase in pair creation rate must be >= 1.0")
-    stop = inp.str("control:stop_at_time", "")
-    if stop == "auto":
-        raise InputError("control:stop_at_time: auto is not supported by this driver")
+        raise InputError("increase in pair creation rate must be >= 1.0.")
+    if rate > 1.0 and mult >= 0:
+        raise InputError("event biasing (pair rate increase > 1) is incompatible with multiplicity selection.")
+    stop = stop_mode(inp)
     if inp.contains("output:discard_background"):
         bg_e = bg_ph = inp.bool("output:discard_background")
     else:
         bg_e, bg_ph = inp.bool("output:discard_background_e", False), False
     return abi.collide_options(
         dt_multiplier=inp.float("control:dt_multiplier", 1.0), rate_increase=rate,
-        t_stop=inp.evaluate(stop) if stop else math.inf,
+        t_stop=stop if isinstance(stop, float) else math.inf,
         min_energy=1.0e-6 * inp.float("output:min_energy") / ELEMENTARY_CHARGE if inp.contains("output:min_energy")
         else 0.0,
         max_angle=inp.float("output:max_angle", math.pi), multiplicity=mult, discard_bg_e=int(bg_e),
@@ -191,6 +311,14 @@ def to_beam_basis(out, theta, phi):
     return out
 
 
+def _project_to_time(parts, ct):
+    """Moves every particle along its momentum to the time coordinate ct
+    (main.rs:1151-1187): r + u (ct - r^0) / u^0."""
+    r, u = parts["r"], parts["u"]
+    if len(r):
+        parts["r"] = r + u * ((ct - r[:, 0]) / u[:, 0])[:, None]
+
+
 def run(path, output_dir="", engine=None, log=print):
     """Runs the input file; returns the list of files written."""
     inp = Input.from_file(path)
@@ -200,16 +328,20 @@ def run(path, output_dir="", engine=None, log=print):
     dump = inp.str("output:dump_all_particles", "") if inp.contains("output:dump_all_particles") else None
     if dump is not None and dump != "hdf5":
         raise InputError("output:dump_all_particles: the only format is hdf5")
-    if inp.list("output:intermediate") or inp.list("stats:intermediate"):
-        raise InputError("intermediate-particle output is not supported by this driver")
+    dump_decayed = inp.bool("output:dump_decayed_photons", False)
     units = UnitSystem.named(inp.str("output:units", "auto"))
     fmt = inp.str("output:file_format", "plain_text")
     fmt = {"plain_text": "plain_text", "plain-text": "plain_text", "ascii": "plain_text", "fits": "fits"}.get(fmt)
     if fmt is None:
         fmt = "plain_text"
     dstrs = {sp: [DistributionFunction.load(s) for s in inp.list("output:" + sp)] for sp in SPECIES}
+    inter_dstrs = [DistributionFunction.load(s) for s in inp.list("output:intermediate")]
     stats_specs = {sp: inp.list("stats:" + sp) for sp in SPECIES}
+    inter_stats = inp.list("stats:intermediate")
     exprs = inp.list("stats:expression")
+    # decayed photons are kept when any output wants them (main.rs:981-982)
+    keep_decayed = bool(inter_dstrs) or bool(inter_stats) or dump_decayed
+    stop = stop_mode(inp)
     beam_frame = inp.str("output:coordinate_system", "laser") == "beam"
     a0s = inp.loop("laser:a0")
     eng = engine or engine_mod.Engine()
@@ -222,29 +354,45 @@ def run(path, output_dir="", engine=None, log=print):
         seed &= (1 << 64) - 1
         for a0 in a0s:
             laser = laser_from_input(inp, a0)
-            opts = options_from_input(inp, keep_decayed=False)
             if inp.contains("beam:from_hdf5"):
                 host, loaded = beam_from_hdf5_input(inp, laser, path)
                 desc, n, species, angle, plane = None, len(host["species"]), loaded["species"], loaded["angle"], \
                     loaded["plane"]
             else:
-                desc, n, species, angle, plane = beam_from_input(inp, laser)
+                desc, n, species, angle, plane = beam_from_input(inp, laser, path)
                 prim = eng.build_beam(desc, n, seed=seed)
                 host = {k: v.cpu().numpy() for k, v in prim.items()}
                 loaded = None
+            rate = rate_increase_from_input(inp, eng, laser, desc, desc.spectrum_gamma if desc is not None else None)
+            opts = options_from_input(inp, keep_decayed=keep_decayed, rate_increase=rate)
             out, st = eng.collide(laser, opts, host, seed=seed)
             log("a0 = %g: %d primaries -> %d particles (%d photons emitted, %d pairs), %.1f ms on the device"
                 % (a0, n, st["n_out"], st["emissions"], st["pair_events"], st["device_ms"]))
+            inter = (out["flags"] & 1) != 0
+            decayed = {k: v[inter] for k, v in out.items()}
+            out = {k: v[~inter] for k, v in out.items()}
+            t_stop_global = None
+            if stop == "auto":
+                ct = float(np.max(out["r"][:, 0])) if len(out["r"]) else -math.inf
+                _project_to_time(out, ct)
+                t_stop_global = ct / SPEED_OF_LIGHT
+            elif stop is not None:
+                _project_to_time(out, stop * SPEED_OF_LIGHT)
+                t_stop_global = stop
             if beam_frame:
                 to_beam_basis(out, angle, plane)
+                to_beam_basis(decayed, angle, plane)
             if dump is not None:
                 cur0 = ident if len(a0s) == 1 else "%s%sa0_%.3f" % (ident, "_" if ident else "", a0)
                 fname = os.path.join(output_dir, cur0 + ("_" if cur0 else "") + "particles.h5")
                 write_particles_hdf5(fname, inp, path, laser, a0, desc, n, species, angle, plane, opts, out, units,
-                                     not beam_frame, seed, loaded)
+                                     not beam_frame, seed, loaded, decayed=decayed, dump_decayed=dump_decayed,
+                                     t_stop_global=t_stop_global, engine=eng)
                 written.append(fname)
             import torch
-            dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to("cuda:%d" % eng.device) for k, v in out.items()}
+            device = "cuda:%d" % eng.device
+            dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device) for k, v in out.items()}
+            dev_i = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device) for k, v in decayed.items()}
             cur = ident if len(a0s) == 1 else "%s%sa0_%.3f" % (ident, "_" if ident else "", a0)
             base = os.path.join(output_dir, cur + ("_" if cur else "")) if output_dir else cur + ("_" if cur else "")
             for sp, code in SPECIES.items():
@@ -252,6 +400,10 @@ def run(path, output_dir="", engine=None, log=print):
                     f = d.write(eng, dev, code, units, base + sp, fmt)
                     if f:
                         written.append(f)
+            for d in inter_dstrs:
+                f = d.write(eng, dev_i, abi.PHOTON, units, base + "intermediate", fmt)
+                if f:
+                    written.append(f)
             stat_objs = {}
             for sp, code in SPECIES.items():
                 stat_objs[sp] = []
@@ -259,6 +411,11 @@ def run(path, output_dir="", engine=None, log=print):
                     s = SummaryStatistic(spec)
                     s.evaluate(eng, dev, code, sp)
                     stat_objs[sp].append(s)
+            # stats:intermediate is evaluated over the decayed photons but,
+            # as in the reference (main.rs:1262-1287), not written to the
+            # stats file
+            for spec in inter_stats:
+                SummaryStatistic(spec).evaluate(eng, dev_i, abi.PHOTON, "intermediate")
             lines = [str(s) for sp in ("electron", "positron", "photon") for s in stat_objs[sp]]
             for e in exprs:
                 lines.append(_expression_line(inp, e))
@@ -328,7 +485,8 @@ _SPECIES_NAME = {abi.ELECTRON: "electron", abi.POSITRON: "positron", abi.PHOTON:
 
 
 def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, angle, plane, opts, out, units,
-                         laser_defines_z, seed, loaded=None):
+                         laser_defines_z, seed, loaded=None, decayed=None, dump_decayed=False, t_stop_global=None,
+                         engine=None):
     """The final-state file of main.rs:1289-1715: build information, the
     parsed configuration, and every final-state particle by species, in the
     output unit system, each dataset with its `unit` and `desc`
@@ -356,8 +514,8 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
     c.dataset("rng_seed", inp.int("control:rng_seed", 0))
     c.dataset("increase_pair_rate_by", float(opts.rate_increase))
     c.dataset("bandwidth_correction", bool(laser.finite_bandwidth))
-    if math.isfinite(opts.t_stop):
-        c.dataset("stop_at_time", float(opts.t_stop), unit="s",
+    if t_stop_global is not None:
+        c.dataset("stop_at_time", float(t_stop_global), unit="s",
                   desc="tracking has continued until all particles have this time coordinate")
     c.dataset("select_multiplicity", int(opts.multiplicity) if opts.multiplicity >= 0 else False)
     focusing = laser.model in (abi.FOCUSED_LASER, abi.FAST_FOCUSED_LASER)
@@ -401,7 +559,7 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
         bm.dataset("max_angle", float(loaded["max_angle"]), unit="rad",
                    desc="primaries propagating at angles larger than this are discarded")
         _write_output_config(conf, opts, units, laser_defines_z)
-        _write_final_state(root, laser, out, units, focusing)
+        _write_final_state(root, laser, out, units, focusing, decayed, dump_decayed, engine)
         hdf5.write(fname, root)
         return
     bm.dataset("offset", hdf5.Vector(np.asarray(list(desc.offset)) * L.scale), unit=L.name)
@@ -432,7 +590,7 @@ def write_particles_hdf5(fname, inp, input_path, laser, a0, desc, n, species, an
     bm.dataset("transverse_distribution_is_normal", desc.radial_dstr != abi.RADIAL_UNIFORM)
     bm.dataset("longitudinal_distribution_is_normal", True)
     _write_output_config(conf, opts, units, laser_defines_z)
-    _write_final_state(root, laser, out, units, focusing)
+    _write_final_state(root, laser, out, units, focusing, decayed, dump_decayed, engine)
     hdf5.write(fname, root)
 
 
@@ -446,7 +604,59 @@ def _write_output_config(conf, opts, units, laser_defines_z):
     op.dataset("min_energy", opts.min_energy * E.scale, unit=E.name)  # opts.min_energy is in MeV
 
 
-def _write_final_state(root, laser, out, units, focusing):
+def _write_intermediate_state(root, decayed, units):
+    """main.rs:1633-1688: the photons that decayed into pairs, as they were
+    when they decayed."""
+    L, P = units.length, units.momentum
+    g = root.group("intermediate-state").group("photon")
+    g.dataset("weight", decayed["weight"], unit="1", desc="number of real photons each macrophoton represents")
+    g.dataset("a0_at_creation", decayed["payload"], unit="1",
+              desc="normalized amplitude (RMS under LMA) at point of emission", alias="xi")
+    g.dataset("parent_chi", decayed["parent_chi"], unit="1",
+              desc="quantum parameter (RMS under LMA) of parent at point of emission")
+    g.dataset("n_pos", decayed["interaction_count"], unit="1",
+              desc="total probability of pair creation for the photon")
+    g.dataset("id", decayed["id"], desc="unique ID of the photon")
+    g.dataset("parent_id", decayed["parent_id"],
+              desc="ID of the particle that created the photon (for primary particles, parent_id = id")
+    g.dataset("polarization", decayed["pol"], desc="Stokes parameters of the photon: I, Q, U, V", unit="1",
+              alias="polarisation")
+    g.dataset("position", decayed["r"] * L.scale, unit=L.name, desc="four-position of the photon")
+    g.dataset("momentum", decayed["u"] * (ELECTRON_MASS_MEV * P.scale), unit=P.name,
+              desc="four-momentum of the photon")
+
+
+def chirped_energy_flux(laser, engine):
+    """FastPlaneWave::integrated_intensity (field/fast_plane_wave.rs:56-85),
+    the energy per unit area of a chirped plane wave: the field energy
+    density at 10 (1 + 2 pi b n_cycles) points per wavelength along the
+    pulse, summed with alternating 2/3, 4/3 weights and Kahan compensation.
+    The fields are the device's FP64 FastPlaneWave fields."""
+    ppw = int(10.0 * (1.0 + 2.0 * math.pi * laser.chirp_b * laser.n_cycles))
+    nc = laser.n_cycles
+    max_phase = {abi.COS2: math.pi * nc, abi.FLATTOP: math.pi * (nc + 1.0)}.get(laser.envelope, 6.0 * math.pi * nc)
+    k = 2.0 * math.pi / laser.wavelength
+    dphi = 2.0 * math.pi / ppw
+    dz = dphi / k
+    n_pts = int(max_phase / dphi)
+    idx = np.arange(-n_pts, n_pts)
+    r = np.zeros((len(idx), 4))
+    r[:, 3] = -(idx * dphi) / k
+    fpw = abi.laser_desc(abi.FAST_PLANE_WAVE, laser.a0, laser.wavelength, laser.polarization, laser.envelope,
+                         n_cycles=nc, chirp_b=laser.chirp_b)
+    E, B, _ = engine.fields(fpw, r)
+    dens = 0.5 * VACUUM_PERMITTIVITY * (np.sum(E * E, axis=1) + SPEED_OF_LIGHT ** 2 * np.sum(B * B, axis=1))
+    flux, comp = 0.0, 0.0
+    for n, u in zip(idx, dens):
+        w = 2.0 / 3.0 if n % 2 == 0 else 4.0 / 3.0
+        y = w * float(u) * dz - comp
+        t = flux + y
+        comp = (t - flux) - y
+        flux = t
+    return flux
+
+
+def _write_final_state(root, laser, out, units, focusing, decayed=None, dump_decayed=False, engine=None):
     L, E = units.length, units.energy
     P = units.momentum
     fs = root.group("final-state")
@@ -492,14 +702,22 @@ def _write_final_state(root, laser, out, units, focusing):
                       desc="four-position at which the positron was created")
         g.dataset("momentum", q["u"] * (ELECTRON_MASS_MEV * P.scale), unit=P.name,
                   desc="four-momentum of the %s" % name)
+    if dump_decayed and decayed is not None:
+        _write_intermediate_state(root, decayed, units)
     lg = fs.group("laser")
     en = laser_energy(laser)
+    if en is None and engine is not None:
+        en = (chirped_energy_flux(laser, engine), "J/m^2")
     if en is not None:
         if focusing:
             lg.dataset("energy", en[0], unit=en[1], desc="total energy of the laser pulse")
         else:
             lg.dataset("energy_flux", en[0], unit=en[1], desc="total energy of the laser pulse, per unit area")
-    absorption = float(np.sum(out["weight"] * out["work"])) * ELECTRON_MASS_MEV * 1.0e6 * ELEMENTARY_CHARGE
+    # over every particle, the decayed photons included (main.rs:1141-1146)
+    work = float(np.sum(out["weight"] * out["work"]))
+    if decayed is not None and len(decayed["weight"]):
+        work += float(np.sum(decayed["weight"] * decayed["work"]))
+    absorption = work * ELECTRON_MASS_MEV * 1.0e6 * ELEMENTARY_CHARGE
     lg.dataset("absorption", absorption, unit="J", desc="energy absorbed from the laser")
 
 

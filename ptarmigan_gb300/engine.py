@@ -21,7 +21,7 @@ _lib = None
 _EXPORTS = [
     "ptg_abi_version", "ptg_status_string", "ptg_last_error", "ptg_context_create", "ptg_context_destroy",
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
-    "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_context_set_limits", "ptg_eval_fields", "ptg_push_steps",
+    "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_context_set_limits", "ptg_pair_rate_increase", "ptg_eval_fields", "ptg_push_steps",
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample", "ptg_lp_sample_warp",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
@@ -78,6 +78,8 @@ def load(path=None):
     L.ptg_laser_initial_z.argtypes = [C.POINTER(abi.LaserDesc), DP]
     L.ptg_context_stream.restype = C.c_void_p
     L.ptg_context_stream.argtypes = [ctxp]
+    L.ptg_pair_rate_increase.restype = st
+    L.ptg_pair_rate_increase.argtypes = [ctxp, C.POINTER(abi.LaserDesc), C.c_double, C.POINTER(C.c_double)]
     L.ptg_context_set_limits.restype = st
     L.ptg_context_set_limits.argtypes = [ctxp, C.POINTER(abi.Limits), C.POINTER(abi.Limits)]
     L.ptg_eval_fields.restype = st
@@ -219,6 +221,13 @@ class Engine:
         cur = abi.Limits()
         self._check(self.L.ptg_context_set_limits(self._h, C.byref(new), C.byref(cur)))
         return cur.as_dict()
+
+    def pair_rate_increase(self, laser, gamma):
+        """control:increase_pair_rate_by: auto for a beam of Lorentz factor
+        gamma (main.rs:294-319)."""
+        out = C.c_double()
+        self._check(self.L.ptg_pair_rate_increase(self._h, C.byref(laser), gamma, C.byref(out)))
+        return out.value
 
     def load_tables(self, directory=None):
         self._check(self.L.ptg_load_tables(self._h, directory.encode() if directory else None))

@@ -300,6 +300,19 @@ class Input:
     def evaluate(self, s):
         return evaluate(s, self.ctx)
 
+    def func(self, path, arg):
+        """Input::func (input/mod.rs:180-204): the expression at `path` as a
+        function of the variable `arg`, evaluated in the constants context."""
+        text = self._get(path)
+        if text is None or isinstance(text, (list, dict)):
+            raise InputError("%s is missing" % path)
+
+        def f(x):
+            ctx = dict(self.ctx)
+            ctx[arg] = float(x)
+            return evaluate(text, ctx)
+        return f
+
     def float(self, path, default=None):
         v = self._get(path)
         if v is None:

@@ -158,3 +158,142 @@ def test_staged_run_loads_the_dump(tmp_path):
     n2 = fs["photon"]["members"]["id"]["value"]
     assert n2.size + fs["electron"]["members"]["id"]["value"].size > 0
     assert n2.size <= n_photons
+
+
+def _auto_ratio_oracle(laser, gamma):
+    """main.rs:294-319 written out with the oracle's rates."""
+    from oracle import oracle
+    from ptarmigan_gb300 import abi
+    from ptarmigan_gb300.input import COMPTON_TIME, SPEED_OF_LIGHT
+    oracle.build()
+    lam = laser.wavelength
+    if laser.model in (abi.FAST_PLANE_WAVE, abi.FAST_FOCUSED_LASER):
+        omega_mc2 = 1.26e-6 / (0.510999 * 1.0e6 * lam)
+        chi = 2.0 * gamma * laser.a0 * omega_mc2
+        pair, _ = oracle.lcfa_pair_probability([gamma, 0.0, 0.0, -gamma], [1.0, 0.0, 0.0, 0.0], chi, [1.0, 0.0, 0.0], 1.0)
+        return oracle.lcfa_photon_rate(chi, gamma) / pair
+    kk = SPEED_OF_LIGHT * COMPTON_TIME * 2.0 * math.pi / lam
+    kappa = np.array([kk, 0.0, 0.0, kk])
+    ell = np.array([gamma, 0.0, 0.0, -gamma])
+    u = np.array([math.sqrt(1.0 + gamma * gamma), 0.0, 0.0, -gamma])
+    pol = 1 if laser.polarization == abi.CIRCULAR else 0
+    a_rms = laser.a0 if pol else laser.a0 / math.sqrt(2.0)
+    ku = kappa[0] * u[0] - kappa[3] * u[3]
+    q = u + a_rms * a_rms * kappa / (2.0 * ku)
+    dt = lam / SPEED_OF_LIGHT
+    pair, _ = oracle.bw_probability(ell, [1.0, 0.0, 0.0, 0.0], kappa, a_rms, dt, pol, 0.0)
+    photon = oracle.nlc_probability(kappa, q, dt, pol)
+    return 1.0 if pair == 0.0 else max(photon / pair, 1.0)
+
+
+@pytest.mark.parametrize("model,pol,a0,energy", [(2, 1, 5.0, 16.5), (2, 0, 2.0, 10.0), (3, 0, 10.0, 10.0),
+                                                 (0, 1, 1.0, 5.0)])
+def test_automatic_pair_rate_increase(model, pol, a0, energy):
+    """control:increase_pair_rate_by: auto (main.rs:294-319) on the device
+    against the same formula over the oracle's rates."""
+    from ptarmigan_gb300 import abi, beam, engine
+    laser = abi.laser_desc(model, a0, 0.8e-6, pol, abi.GAUSSIAN, waist=4e-6, n_cycles=10.0)
+    gamma = beam.gamma_from_energy(energy)
+    eng = engine.Engine()
+    try:
+        got = eng.pair_rate_increase(laser, gamma)
+    finally:
+        eng.close()
+    want = _auto_ratio_oracle(laser, gamma)
+    assert got == pytest.approx(want, rel=1e-9)
+    assert got >= 1.0
+
+
+AUTO = """---
+control:
+  lcfa: false
+  pair_creation: true
+  pol_resolved: true
+  increase_pair_rate_by: auto
+  stop_at_time: {stop}
+  rng_seed: 5
+laser:
+  a0: 5.0
+  wavelength: 0.8 * micro
+  waist: 3.0 * micro
+  fwhm_duration: 30.0 * femto
+  polarization: circular
+beam:
+  n: 2000
+  species: electron
+  gamma: 1.0
+  spectrum:
+    function: exp(-((gamma - 32000.0) / 300.0)^2)
+    min: 31000.0
+    max: 33000.0
+  radius: [1.0 * micro, normally_distributed]
+  length: 5.0 * micro
+output:
+  ident: auto
+  dump_all_particles: hdf5
+  dump_decayed_photons: true
+  intermediate:
+    - energy:(20;weight)
+"""
+
+
+def test_auto_rate_stop_time_spectrum_and_intermediates(tmp_path):
+    """One LMA run with a tabulated beam spectrum, the automatic pair-rate
+    increase (so that photons decay), stop_at_time: auto, decayed photons
+    kept: every final-state particle ends at the same time coordinate, the
+    decayed photons are written to the intermediate-state group and to
+    their own distribution file, and the file records the rate increase."""
+    from ptarmigan_gb300 import hdf5
+    from ptarmigan_gb300.driver import run
+    src = tmp_path / "auto.yml"
+    src.write_text(AUTO.format(stop="auto"))
+    files = run(str(src), str(tmp_path / "out"), log=lambda *a: None)
+    names = sorted(os.path.basename(f) for f in files)
+    assert "auto_particles.h5" in names and "auto_intermediate_energy.dat" in names
+    f = hdf5.read(str(tmp_path / "out" / "auto_particles.h5"))["members"]
+    ctl = f["config"]["members"]["control"]["members"]
+    assert ctl["increase_pair_rate_by"]["value"] > 1.0
+    t_stop = ctl["stop_at_time"]["value"]
+    fs = f["final-state"]["members"]
+    for sp in ("photon", "electron", "positron"):
+        x = fs[sp]["members"]["position"]["value"]
+        if x.size:
+            # positions in metres (auto units): c t = c t_stop for every particle
+            np.testing.assert_allclose(x[:, 0], 2.997925e8 * t_stop, rtol=1e-12)
+    inter = f["intermediate-state"]["members"]["photon"]["members"]
+    n_dec = inter["weight"]["value"].size
+    assert n_dec > 0
+    assert fs["positron"]["members"]["weight"]["value"].size >= n_dec
+    # the primaries' energies follow the tabulated spectrum (mean ~ 32000 m c^2)
+    el = fs["electron"]["members"]
+    assert el["id"]["value"].size >= 2000
+
+
+def test_given_stop_time_moves_every_particle(tmp_path):
+    from ptarmigan_gb300 import hdf5
+    from ptarmigan_gb300.driver import run
+    src = tmp_path / "given.yml"
+    src.write_text(AUTO.format(stop="200.0 * femto"))
+    run(str(src), str(tmp_path / "out"), log=lambda *a: None)
+    f = hdf5.read(str(tmp_path / "out" / "given_particles.h5"))["members"]
+    assert f["config"]["members"]["control"]["members"]["stop_at_time"]["value"] == pytest.approx(2e-13)
+    x = f["final-state"]["members"]["electron"]["members"]["position"]["value"]
+    np.testing.assert_allclose(x[:, 0], 2.997925e8 * 2e-13, rtol=1e-12)
+
+
+def test_chirped_plane_wave_energy_flux():
+    """FastPlaneWave::integrated_intensity (fast_plane_wave.rs:56-85) for a
+    chirp so small that the pulse is the unchirped one: the numerical
+    energy flux equals the closed form of fast_plane_wave.rs:204-236."""
+    from ptarmigan_gb300 import abi, driver, engine
+    eng = engine.Engine()
+    try:
+        for env in (abi.COS2, abi.GAUSSIAN):
+            flat = abi.laser_desc(abi.PLANE_WAVE, 2.0, 0.8e-6, abi.LINEAR, env, n_cycles=10.0)
+            chirped = abi.laser_desc(abi.PLANE_WAVE, 2.0, 0.8e-6, abi.LINEAR, env, n_cycles=10.0, chirp_b=1e-9)
+            num = driver.chirped_energy_flux(chirped, eng)
+            closed, unit = driver.laser_energy(flat)
+            assert unit == "J/m^2"
+            assert num == pytest.approx(closed, rel=2e-3)
+    finally:
+        eng.close()

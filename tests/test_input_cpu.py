@@ -100,3 +100,67 @@ def test_beam_basis_rotation_undoes_the_collision_angle():
     out["u"][0, 1:] = 100.0 * d
     to_beam_basis(out, theta, phi)
     np.testing.assert_allclose(out["u"][0, 1:] / 100.0, [0.0, 0.0, 1.0], atol=1e-12)
+
+
+SPECTRUM = """---
+beam:
+  n: 1000
+  gamma: 1.0
+  spectrum:
+    function: gamma * exp(-gamma / 2000.0)
+    min: 1000.0
+    max: 4000.0
+    resolution: 30
+control:
+  stop_at_time: auto
+"""
+
+
+def test_spectrum_function_and_cdf():
+    """beam:spectrum:function (main.rs:610-636) and GammaDistribution::custom
+    (particle/dstr.rs:88-106): 30 values from min in steps of
+    (max - min) / 30, a CDF from [min, 0] to [max, 1]."""
+    import numpy as np
+    from ptarmigan_gb300 import driver
+    inp = Input(SPECTRUM)
+    vals, g0, g1, step = driver.spectrum_from_input(inp, 1000)
+    assert len(vals) == 30 and g0 == 1000.0 and g1 == 4000.0 and step == 100.0
+    assert vals[0] == pytest.approx(1000.0 * math.exp(-0.5))
+    cdf = driver.custom_cdf(vals, g0, step)
+    assert cdf.shape == (31, 2) and cdf[0, 1] == 0.0 and cdf[-1, 1] == pytest.approx(1.0, abs=1e-15)
+    assert cdf[-1, 0] == pytest.approx(4000.0)
+    assert np.all(np.diff(cdf[:, 0]) > 0) and np.all(np.diff(cdf[:, 1]) >= 0)
+    g = np.array([g0 + i * step for i in range(30)])
+    assert driver.spectrum_mean_gamma(vals, g0, step) == pytest.approx(np.sum(g * vals) / np.sum(vals))
+    assert driver.stop_mode(inp) == "auto"
+
+
+def test_spectrum_file(tmp_path):
+    """beam:spectrum:file, one value per line relative to the input file,
+    over [min, min + n step]."""
+    from ptarmigan_gb300 import driver
+    (tmp_path / "spec.txt").write_text("1.0\n2.0\n3.0\n2.0\n1.0\n")
+    inp = Input("beam:\n  spectrum:\n    file: spec.txt\n    min: 100.0\n    step: 50.0\n")
+    vals, g0, g1, step = driver.spectrum_from_input(inp, 10, str(tmp_path / "in.yml"))
+    assert vals == [1.0, 2.0, 3.0, 2.0, 1.0] and g0 == 100.0 and step == 50.0 and g1 == 300.0
+    bad = Input("beam:\n  spectrum:\n    file: spec.txt\n    function: gamma\n    min: 1.0\n    max: 2.0\n")
+    with pytest.raises(InputError):
+        driver.spectrum_from_input(bad, 10, str(tmp_path / "in.yml"))
+
+
+def test_stop_at_time_modes():
+    from ptarmigan_gb300 import driver
+    assert driver.stop_mode(Input("control:\n  stop_at_time: 3.0e-13\n")) == pytest.approx(3.0e-13)
+    assert driver.stop_mode(Input("control:\n  dt_multiplier: 1.0\n")) is None
+    opts = driver.options_from_input(Input("control:\n  stop_at_time: 2 * femto\n"), False)
+    assert opts.t_stop == pytest.approx(2e-15)
+    assert math.isinf(driver.options_from_input(Input("control:\n  stop_at_time: auto\n"), False).t_stop)
+
+
+def test_project_to_time():
+    import numpy as np
+    from ptarmigan_gb300 import driver
+    parts = {"r": np.array([[1.0, 0.0, 0.0, 0.0], [2.0, 1.0, 0.0, 1.0]]),
+             "u": np.array([[2.0, 1.0, 1.0, 1.0], [10.0, 0.0, 6.0, 8.0]])}
+    driver._project_to_time(parts, 3.0)
+    np.testing.assert_allclose(parts["r"], [[3.0, 1.0, 1.0, 1.0], [3.0, 1.0, 0.6, 1.8]])

@@ -18,7 +18,8 @@ def _limits(a, eta):
     return int(nm), int(nm + rng)
 
 
-def _bound(a, eta):
+def _harmonic_bound(a, eta):
+    """The bound harmonic by harmonic: |J_m(x)| <= (x/2)^m / m! at each n."""
     n0, n1 = _limits(a, eta)
     a2 = a * a
     c = a / math.sqrt(1 + a2)
@@ -38,14 +39,49 @@ def _bound(a, eta):
     return total
 
 
-def test_summation_bound_lies_above_the_sum(orc):
-    rng = np.random.default_rng(7)
-    checked = 0
-    while checked < 60:
+def _bound(a, eta):
+    """ptg_bw.cuh bw_summation_bound: the geometric closed form."""
+    n0, _ = _limits(a, eta)
+    a2 = a * a
+    c = a / math.sqrt(1 + a2)
+    r = 0.5 * math.e * c
+    rho = r * r
+    K = 1 + 4 / (c * c) + 0.25 * c * c
+    beta = 2 * eta / (1 + a2)
+    A, B = 1 + 0.5 * a2 * K, 0.5 * a2 * K * beta
+    n = float(n0)
+    lead = math.exp(2 * n * math.log(r)) / (2 * math.pi * n)
+    om = 1 - rho
+    return lead * ((A + B * n) / om + B * rho / (om * om))
+
+
+def _points(seed, count):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < count:
         a = math.exp(rng.uniform(math.log(0.02), math.log(0.3)))
         eta = math.exp(rng.uniform(math.log(1e-3), math.log(2.0)))
         if math.log10(eta) < -1 - (math.log10(a) + 2) ** 2 / 4.5:
             continue  # the reference's too-small cut: no summation there
+        out.append((a, eta))
+    return out
+
+
+def test_summation_bound_lies_above_the_sum(orc):
+    for a, eta in _points(7, 60):
         f = orc.cp_pair_by_summation(a, eta)
         assert max(f[0], f[1]) <= _bound(a, eta), (a, eta, f)
-        checked += 1
+
+
+def test_closed_form_bounds_the_harmonic_bound():
+    """The closed form is above the harmonic-by-harmonic bound (so above the
+    sum) and within a small factor of it: it skips the same negligible
+    steps up to that factor."""
+    ratios = []
+    for a, eta in _points(11, 400):
+        hb = _harmonic_bound(a, eta)
+        cf = _bound(a, eta)
+        assert cf >= hb, (a, eta, cf, hb)
+        if hb > 0:
+            ratios.append(cf / hb)
+    assert max(ratios) < 10.0, max(ratios)
