@@ -369,6 +369,18 @@ ptg_status ptg_lp_sample(ptg_ctx* ctx, size_t count, const double* a, const doub
 ptg_status ptg_lp_sample_warp(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
                               const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
 
+/* Circularly polarised LMA emission sampler (nonlinear_compton/cp/mod.rs
+ * sample: the harmonic from the regenerated CDF table, v by rejection under
+ * the 32-point ceiling) at rms amplitude a[i] and eta[i], drawing from
+ * stream[i] at `step`; and the same drawn by the warp-cooperative sampler
+ * the collision kernels use (each warp samples its 32 points in turn, all
+ * lanes together), whose results equal ptg_cp_sample's.  out7 and status
+ * as for ptg_lp_sample. */
+ptg_status ptg_cp_sample(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
+                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
+ptg_status ptg_cp_sample_warp(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
+                              const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
+
 /* --------------------------------------------------- learned proposal ---
  * No reference counterpart: an MLP (six features of a, eta and n; 4 layers
  * of width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the

@@ -315,11 +315,88 @@ __device__ __forceinline__ d4 stokes_rotate_by(d4 sv, double theta) {
     return d4{sv.t, c2 * sv.x + s2 * sv.y, -s2 * sv.x + c2 * sv.y, sv.z};
 }
 
-// pair_creation/mod.rs:21-42 + cp/mod.rs:280-309 (CP).  Returns false out of table.
-static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
-                                            double pol_angle, double* prob, d4* sv_out) {
+// A photon step whose CP Breit-Wheeler rate needs the harmonic sum, left by
+// its lane for the whole warp (the wave kernel and the single-collision
+// queue kernel): the lane records a and eta and abandons the step; the warp
+// sums the harmonics with one Gauss-Legendre node per lane
+// (bw_by_summation_warp); the lane then repeats its step, which reaches the
+// same sum and takes the warp's result.
+struct BwDefer {
+    double a, eta, f0, f1;
+    int pend;  // 0: none; 1: waiting for the warp; 2: served
+};
+
+// bw_by_summation (pair_creation/cp/mod.rs:385-393) evaluated by the 32
+// lanes of a converged warp: lane k evaluates node k of every segment of
+// every harmonic (bw_integrate's 32-point rule), and the sums are reduced
+// over the lanes in a fixed order.  Equal to the serial sum up to the
+// order of its additions.
+static __device__ __noinline__ void bw_by_summation_warp(double a, double eta, double* f0, double* f1) {
+    const unsigned all = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int n0, n1;
+    bw_sum_limits(a, eta, &n0, &n1);
+    const double xk = PTG_GAUSS_32_NODES[lane], wk = PTG_GAUSS_32_WEIGHTS[lane];
+    double re = 0.0, im = 0.0;
+    for (int n = n0; n <= n1; ++n) {
+        double ell = n;
+        double sn = 2.0 * ell * eta / (1.0 + a * a);
+        if (sn <= 4.0) continue;
+        double a2 = a * a;
+        double w1 = 1.0 / ell + 1.0;
+        double beta = a2 * a2 * w1 * w1 + 16.0 * (a2 - 2.0) * (a2 - 2.0) / (sn * sn) - 8.0 * a2 * (a2 - 2.0) / sn;
+        beta = sqrt(beta) / (a2 - 2.0);
+        double alpha = (a2 + 2.0 * ell) / (ell * (2.0 - a2)) - 4.0 / sn;
+        double s_peak = 0.5 * (1.0 - sqrt(alpha + beta));
+        double s_min, s_max;
+        bw_s_bounds(n, a, eta, &s_min, &s_max);
+        double lo[3], hi[3];
+        int nseg;
+        if (isfinite(s_peak)) {
+            double s_mid = 2.0 * s_peak - s_min;
+            if (s_mid > s_max) {
+                nseg = 2;
+                lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_max;
+            } else {
+                nseg = 3;
+                lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_mid, lo[2] = s_mid, hi[2] = s_max;
+            }
+        } else {
+            nseg = 1;
+            lo[0] = s_min, hi[0] = s_max;
+        }
+        for (int g = 0; g < nseg; ++g) {
+            double h = 0.5 * (hi[g] - lo[g]), m = 0.5 * (lo[g] + hi[g]);
+            double sr, si;
+            bw_over_theta(n, a, eta, h * xk + m, &sr, &si);
+            re += h * wk * sr;
+            im += h * wk * si;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_down_sync(all, re, o);
+        im += __shfl_down_sync(all, im, o);
+    }
+    *f0 = 2.0 * __shfl_sync(all, re, 0);
+    *f1 = 2.0 * __shfl_sync(all, im, 0);
+}
+
+// The CP Breit-Wheeler rate is a harmonic sum at (a, eta) that matters.
+__device__ __forceinline__ bool bw_needs_summation(double a, double eta, double c) {
+    return a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta) &&
+           !(c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE);
+}
+
+// Status of bw_probability for a step left to the warp
+constexpr int BW_DEFERRED = -1;
+
+// pair_creation/mod.rs:21-42 + cp/mod.rs:280-309 (CP).  Returns 1, 0 out of
+// table, or BW_DEFERRED when the harmonic sum is left to the warp (bdf not
+// NULL).
+static __device__ __noinline__ int bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
+                                                  double pol_angle, double* prob, d4* sv_out,
+                                                  BwDefer* bdf = nullptr) {
     double eta = dot4(k, ell);
-    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
     double f0, f1;
     double c = ALPHA_FINE * dphi / eta;
@@ -327,9 +404,17 @@ static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 s
         c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE) {
         // the summed rate cannot give a probability that matters: skip it
         f0 = f1 = 0.0;
+    } else if (bdf != nullptr && a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta)) {
+        if (bdf->pend != 2) {
+            bdf->a = a, bdf->eta = eta, bdf->pend = 1;
+            return BW_DEFERRED;
+        }
+        f0 = bdf->f0, f1 = bdf->f1;
+        bdf->pend = 0;
     } else if (!bw_rates(T, a, eta, &f0, &f1)) {
-        return false;
+        return 0;
     }
+    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
     double p = c * (0.5 * ((f0 + f1) + sv.z * (f0 - f1)));
     double p_avg = c * (0.5 * (f0 + f1));
     double delta = c * (0.5 * (f0 - f1));
@@ -338,7 +423,7 @@ static __device__ __noinline__ bool bw_probability(const double* T, d4 ell, d4 s
     d3 g = stokes_from_lma_basis(mk3(o.x, o.y, o.z), ell);
     *sv_out = d4{o.t, g.x, g.y, g.z};
     *prob = p;
-    return true;
+    return 1;
 }
 
 // pair_creation/mod.rs:62-110: the positron momentum for a sampled

@@ -387,7 +387,8 @@ static __device__ __noinline__ unsigned long long photon_drift(const WaveArgs& a
 
 // One photon step: main.rs:214-256.
 template <int MODEL, bool QUEUE = false>
-__device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* npair) {
+__device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t* rej, uint32_t* npair,
+                                            BwDefer* bdf = nullptr) {
     const FieldParams& f = a.f;
     double dt = a.o.dt;
     Draws rng;
@@ -471,7 +472,8 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
             dbw.pool = a.dbpool;
         }
         int st = lma_pair_create(f, *a.lma, dbw, r, ell, pol, dt, rng, a.o.rate_increase, &prob, &pol_new, &created,
-                                 &ue, &up, &frac, &a_eff, &chi, &absorption, rej);
+                                 &ue, &up, &frac, &a_eff, &chi, &absorption, rej, bdf);
+        if (st == LMA_DEFERRED) return;  // the step repeats once the warp has summed the rate
         if (st != ST_OK) {
             L.status = st;
             L.r = r;
@@ -569,7 +571,8 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
     double s = 0.0, theta = 0.0;
     d3 sv = mk3(0.0, 0.0, 0.0);
     uint32_t rej = 0;
-    int st = lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
+    int st = a.f.circular ? cp_sample_warp(nlc_view(*a.lma), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej)
+                          : lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
     __syncwarp();
     if ((int)lane_id() == src) {
         d.rng = rng;
@@ -577,6 +580,51 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
         d.pend = 2;
     }
     __syncwarp();
+}
+
+// Emissions are sampled by the whole warp: LMA linear polarisation (with
+// the DoubleBessel workspaces) and the reference's circular-polarisation
+// sampler (the learned proposal samples on its lane); not classically.
+// Uniform over the grid: the kernel's arguments decide.
+__device__ __forceinline__ bool warp_samples_emissions(const WaveArgs& a) {
+    if (a.o.classical_mode) return false;
+    return a.f.circular ? !a.mlp.enabled : a.dbw != nullptr;
+}
+
+// The CP Breit-Wheeler harmonic sum left by lane `src` of this warp
+// (`warp_bdf` is the warp's array), evaluated by all 32 lanes.
+static __device__ __noinline__ void bw_defer_serve(BwDefer* warp_bdf, int src) {
+    __syncwarp();
+    BwDefer& d = warp_bdf[src];
+    double f0, f1;
+    bw_by_summation_warp(d.a, d.eta, &f0, &f1);
+    __syncwarp();
+    if ((int)lane_id() == src) {
+        d.f0 = f0, d.f1 = f1;
+        d.pend = 2;
+    }
+    __syncwarp();
+}
+
+// Serves every deferred sample and sum of this warp: all 32 lanes.
+__device__ __forceinline__ void warp_serve(const WaveArgs& a, LpDefer* dfr, BwDefer* bdf, bool have) {
+    __syncwarp();
+    if (dfr != nullptr) {
+        unsigned pending = __ballot_sync(0xffffffffu, have && dfr->pend == 1);
+        while (pending != 0u) {
+            int src = __ffs(pending) - 1;
+            pending &= pending - 1u;
+            lp_defer_serve(a, dfr - lane_id(), src);
+        }
+    }
+    if (bdf != nullptr) {
+        unsigned pending = __ballot_sync(0xffffffffu, have && bdf->pend == 1);
+        while (pending != 0u) {
+            int src = __ffs(pending) - 1;
+            pending &= pending - 1u;
+            bw_defer_serve(bdf - lane_id(), src);
+        }
+    }
 }
 
 // Wave kernel.  With the LMA models in linear polarisation, emissions are
@@ -589,12 +637,18 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
     uint32_t rej = 0, nemit = 0, npair = 0, maxst = 0;
     unsigned long long lsteps = 0, psteps = 0, fsteps = 0, nerr = 0;
     LpDefer* dfr = nullptr;
+    BwDefer* bdf = nullptr;
     if constexpr (LMA) {
         __shared__ LpDefer s_dfr[128];
+        __shared__ BwDefer s_bdf[128];
         // uniform over the grid: the kernel's arguments decide
-        if (!a.f.circular && a.dbw != nullptr && !a.o.classical_mode) {
+        if (warp_samples_emissions(a)) {
             dfr = &s_dfr[threadIdx.x];
             dfr->pend = 0;
+        }
+        if (a.f.circular && a.o.tracking_photons) {
+            bdf = &s_bdf[threadIdx.x];
+            bdf->pend = 0;
         }
     }
     bool have = lane_load(a, L);
@@ -625,10 +679,12 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                     L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
                     done = true;
                 } else if (!done) {
-                    photon_step<MODEL>(a, L, &rej, &npair);
-                    ++L.step;
-                    ++psteps;
-                    done = L.status != ST_OK;
+                    photon_step<MODEL>(a, L, &rej, &npair, bdf);
+                    if (bdf == nullptr || bdf->pend != 1) {
+                        ++L.step;
+                        ++psteps;
+                        done = L.status != ST_OK;
+                    }
                 }
             }
             if (done) {
@@ -640,14 +696,8 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                 have = lane_load(a, L);
             }
         }
-        if (LMA && dfr != nullptr) {
-            __syncwarp();
-            unsigned pending = __ballot_sync(0xffffffffu, have && dfr->pend == 1);
-            while (pending != 0u) {
-                int src = __ffs(pending) - 1;
-                pending &= pending - 1u;
-                lp_defer_serve(a, dfr - lane_id(), src);
-            }
+        if (LMA && (dfr != nullptr || bdf != nullptr)) {
+            warp_serve(a, dfr, bdf, have);
             if (!__any_sync(0xffffffffu, have)) break;
         } else if (!have) {
             break;

@@ -806,6 +806,15 @@ ptg_status ptg_context_set_limits(ptg_ctx* c, const ptg_limits* limits, ptg_limi
     return PTG_OK;
 }
 
+// The CP harmonic CDF's nodes in the coordinates of its inversion
+// (nonlinear_compton/cp/tables/mod.rs:47-121), once per load.
+__global__ void k_cp_cdf_log(const double* cdf, double* out, unsigned long long nodes) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    out[2 * i] = log(cdf[2 * i]);
+    out[2 * i + 1] = cp_cdf_log_node(cdf[2 * i + 1]);
+}
+
 ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
     if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
     std::string d = dir ? dir : default_table_dir();
@@ -871,6 +880,19 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
             if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
             *slot32 = (const float*)q;
         }
+    }
+    host.nlc_cp_cdf_log = nullptr;
+    if (host.nlc_cp_cdf) {
+        const unsigned long long nodes = 4270ull * 32;
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, 16 * nodes);
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        bufs.push_back(q);
+        k_cp_cdf_log<<<(unsigned)((nodes + 255) / 256), 256>>>(host.nlc_cp_cdf, (double*)q, nodes);
+        e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("CDF transform: ") + cudaGetErrorString(e));
+        host.nlc_cp_cdf_log = (const double*)q;
     }
     CUDA_TRY(cudaMemcpy(c->lma_dev, &host, sizeof(LmaTables), cudaMemcpyHostToDevice));
     c->lma_host = host;
@@ -2183,6 +2205,64 @@ static ptg_status lp_sample_points(ptg_ctx* c, size_t count, const double* a, co
         });
 }
 
+// One CP harmonic/s/azimuth/Stokes sample per point (cp_sample, or with
+// `warp` cp_sample_warp, each warp sampling its 32 points one after another).
+__global__ void k_cp_sample(unsigned long long m, int warp, const LmaTables* t, const double* a, const double* eta,
+                            unsigned long long seed, const unsigned long long* stream, unsigned step, double* out7,
+                            int* status) {
+    unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
+    const unsigned lane = threadIdx.x & 31u;
+    // warp: point base + q for q = 0..31, every lane together; otherwise
+    // point base + lane on its own lane
+    for (unsigned q = 0; q < (warp ? 32u : 1u); ++q) {
+        unsigned long long i = base + (warp ? q : lane);
+        if (i >= m) break;  // with warp, the same for every lane of the warp
+        Draws rng;
+        rng.begin(seed, stream[i], step);
+        int n = 0;
+        double s = 0.0, th = 0.0;
+        d3 sv = mk3(0.0, 0.0, 0.0);
+        uint32_t rej = 0;
+        int st = warp ? cp_sample_warp(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej)
+                      : cp_sample(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
+        if (!warp || lane == q) {
+            status[i] = st;
+            double* o = out7 + 7 * i;
+            o[0] = n, o[1] = s, o[2] = th, o[3] = 1.0, o[4] = sv.x, o[5] = sv.y, o[6] = sv.z;
+        }
+    }
+}
+
+static ptg_status cp_sample_points(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                                   const uint64_t* stream, uint32_t step, double* out7, int32_t* status, bool warp) {
+    if (!c || !a || !eta || !stream || !out7 || !status) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (count == 0) return PTG_OK;
+    if (!c->tables_loaded) {
+        ptg_status st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    cudaSetDevice(c->device);
+    std::vector<double> va(a, a + count), ve(eta, eta + count);
+    std::vector<unsigned long long> vs(stream, stream + count);
+    return with_device_buffers(c, {{va.data(), 8 * count}, {ve.data(), 8 * count}, {vs.data(), 8 * count},
+                                   {out7, 56 * count}, {status, 4 * count}},
+                               [&](std::vector<void*>& d) {
+                                   k_cp_sample<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
+                                       count, warp ? 1 : 0, c->lma_dev, (double*)d[0], (double*)d[1], seed,
+                                       (unsigned long long*)d[2], step, (double*)d[3], (int*)d[4]);
+                               });
+}
+
+ptg_status ptg_cp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                         const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+    return cp_sample_points(c, count, a, eta, seed, stream, step, out7, status, false);
+}
+
+ptg_status ptg_cp_sample_warp(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                              const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
+    return cp_sample_points(c, count, a, eta, seed, stream, step, out7, status, true);
+}
+
 ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
                          const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
     return lp_sample_points(c, count, a, eta, seed, stream, step, out7, status, false);
@@ -2538,6 +2618,13 @@ ptg_status ptg_histogram(ptg_ctx* c, const ptg_particles* d, const ptg_hgram_spe
         return set_err(PTG_ERR_INVALID_ARGUMENT, "a fixed number of bins must be >= 1");
     if (sp->bin_spec == PTG_BINS_FIXED_SIZE && !(sp->bin_size > 0.0))
         return set_err(PTG_ERR_INVALID_ARGUMENT, "a fixed bin size must be > 0");
+    if (d->n == 0) {
+        // no particles: an empty histogram (the reference writes none)
+        std::memset(info, 0, sizeof(*info));
+        info->dim = sp->dim;
+        info->empty = 1;
+        return PTG_OK;
+    }
     if (!d->species || !d->u || !d->r || !d->pol || !d->weight)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "particles need species, u, r, pol and weight");
     auto uses = [&](int f) {
@@ -2656,6 +2743,11 @@ ptg_status ptg_particle_sums(ptg_ctx* c, const ptg_particles* d, const ptg_stats
             return set_err(PTG_ERR_INVALID_ARGUMENT, "output function out of range");
     if (sp->filter_func < -1 || sp->filter_func > PTG_OUT_HELICITY)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "filter function out of range");
+    if (d->n == 0) {
+        // no particles: the sums of an empty set
+        *out = ptg_stats_sums{0.0, 0.0, 0.0, HUGE_VAL, -HUGE_VAL, 0.0, 0.0, 0.0, 0.0};
+        return PTG_OK;
+    }
     if (!d->species || !d->u || !d->r || !d->pol || !d->weight)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "particles need species, u, r, pol and weight");
     for (int f : {sp->var_func, sp->weight_func, sp->filter_func})

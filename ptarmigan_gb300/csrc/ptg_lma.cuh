@@ -30,6 +30,9 @@ struct LmaTables {
     // FP32 copies of the two emission rate tables, for the per-step bound
     const float* nlc_lp_rate32;     // [68][61]
     const float* nlc_cp_rate32;     // [70][61]
+    // nlc_cp_cdf's nodes as [ln n, ln(-ln(1 - cdf))], the coordinates its
+    // inversion works in, evaluated once on the device at load
+    const double* nlc_cp_cdf_log;   // [4270][32][2]
 };
 
 // The per-step emission probability is first evaluated in FP32 from the
@@ -47,7 +50,8 @@ constexpr double PROB32_MARGIN = 1.0 / 1024.0;
 
 __device__ __forceinline__ NlcTables nlc_view(const LmaTables& t) {
     return NlcTables{t.nlc_lp_rate,    t.nlc_lp_cdf,     t.nlc_cp_rate,   t.nlc_cp_cdf,
-                     t.nlc_cp_cl_rate, t.nlc_lp_cl_rate, t.nlc_cp_cl_cdf, t.nlc_lp_cl_cdf};
+                     t.nlc_cp_cl_rate, t.nlc_lp_cl_rate, t.nlc_cp_cl_cdf, t.nlc_lp_cl_cdf,
+                     t.nlc_cp_cdf_log};
 }
 
 // Standard normal from two uniforms (Box-Muller), for the finite bandwidth.
@@ -73,6 +77,49 @@ struct LpDefer {
 
 // lma_radiate's status for an emission left to the warp
 constexpr int LMA_DEFERRED = 101;
+
+// cp_sample (nonlinear_compton/cp/mod.rs:181-234) carried out by all 32
+// lanes of a converged warp for one emission whose a, eta and draws every
+// lane holds.  Every lane returns the same result, and it is cp_sample's on
+// the same draws: the harmonic comes from the same table inversion, the 32
+// points of the ceiling are spread over the lanes (the NaN-ignoring max
+// does not depend on the order), and the rejection trials are dealt out in
+// the order the serial sampler draws them, lane k evaluating the k-th of
+// each round of 32; the first accepted trial in draw order is taken, with
+// the draws as they stood after it.
+static __device__ __noinline__ int cp_sample_warp(const NlcTables& t, double a, double eta, Draws& rng, int* n_out,
+                                                  double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
+    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    double mx = fmax(-HUGE_VAL, cp_diff_partial_rate(n, a, eta, cp_ceiling_point(n, a, eta, lane)));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(all, mx, o));
+    mx = 1.2 * mx;
+    Draws r = rng;
+    for (int it0 = 0; it0 < r.cap; it0 += 32) {
+        // this lane's trial: it0 + lane, after the 2 lane draws of the trials before it
+        Draws my_r = r;
+        for (int k = 0; k < 2 * lane; ++k) my_r.next();
+        double vv = my_r.next(), u = my_r.next();
+        bool acc = it0 + lane < r.cap && u <= cp_diff_partial_rate(n, a, eta, vv) / mx;
+        unsigned m = __ballot_sync(all, acc);
+        if (m != 0u) {
+            int win = __ffs(m) - 1;
+            double v = __shfl_sync(all, vv, win);
+            rng = shfl_draws(my_r, win);
+            *rej += (uint32_t)(it0 + win);
+            cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+            *n_out = n;
+            return 0;
+        }
+        r = shfl_draws(my_r, 31);
+    }
+    rng = r;
+    *rej += (uint32_t)r.cap;
+    return 4;  // PTG_ERR_REJECTION_CAP
+}
 
 // plane_wave.rs:251-282 / focused_laser.rs:260-281 with
 // nonlinear_compton::probability (mod.rs:19-47) and generate (mod.rs:58-138).
@@ -138,6 +185,20 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
             double v = 0.0;
             st = cp_sample_v_learned(o, mlp.margin, n, aq, eta, rng, &v, rej, &lc);
             if (st == 0) cp_finish(n, aq, eta, v, rng, &s, &cphi, &sv);
+        } else if (f.circular && !classical && dfr != nullptr) {
+            // the reference's CP sampler, carried out by the whole warp
+            if (dfr->pend == 2) {
+                n = dfr->n, s = dfr->s, cphi = dfr->theta, sv = dfr->sv, st = dfr->status;
+                *rej += dfr->rej;
+                rng = dfr->rng;
+                dfr->pend = 0;
+            } else {
+                dfr->rng = rng;
+                dfr->a = aq;
+                dfr->eta = eta;
+                dfr->pend = 1;
+                return LMA_DEFERRED;
+            }
         } else if (f.circular)
             st = classical ? cp_classical_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
                            : cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
@@ -216,7 +277,7 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
                                                    d4 ell, d4 pol, double dt, Draws& rng, double rate_increase,
                                                    double* prob, d4* pol_new, bool* created, d4* ue, d4* up,
                                                    double* frac, double* a_eff, double* chi, double* absorption,
-                                                   uint32_t* rej) {
+                                                   uint32_t* rej, BwDefer* bdf = nullptr) {
     *prob = 0.0;
     *pol_new = pol;
     *created = false;
@@ -228,9 +289,13 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
     }
     double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp;
     d4 kappa = d4{kk, 0.0, 0.0, kk};
-    bool ok = f.circular ? bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)
-                         : lp_bw_probability(t, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new);
-    if (!ok) return 2;
+    if (f.circular) {
+        int ok = bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new, bdf);
+        if (ok == BW_DEFERRED) return LMA_DEFERRED;  // the step repeats once the warp has summed
+        if (!ok) return 2;
+    } else if (!lp_bw_probability(t, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)) {
+        return 2;
+    }
     double ri = (*prob * rate_increase > 0.1) ? 0.1 / *prob : rate_increase;
     if (rng.next() < *prob * ri) {
         int n;

@@ -172,6 +172,7 @@ struct NlcTables {
     const double* lp_cl_rate;  // [61]
     const double* cp_cl_cdf;   // [61][32][2]
     const double* lp_cl_cdf;   // [61][16][2]
+    const double* cp_cdf_log;  // [4270][32][2]: cp_cdf's nodes as [ln n, ln(-ln(1 - cdf))], or NULL
 };
 
 // nonlinear_compton/cp/classical.rs:22-43
@@ -232,16 +233,24 @@ __device__ __forceinline__ bool rate32_cp(const float* T32, double a, double eta
 
 // nonlinear_compton/cp/tables/mod.rs:37-121: harmonic index from the CDF
 // table (four grid corners, each inverted in [ln n, ln(-ln(1 - cdf))]).
-static __device__ __noinline__ double cp_cdf_corner(const double* table, double frac) {
+// The CDF coordinate of a harmonic-CDF node, ln(-ln(1 - cdf)).
+__device__ __forceinline__ double cp_cdf_log_node(double cdf) { return log(-1.0 * log(1.0 - cdf)); }
+
+// `logt`, when not NULL, holds the corner's nodes already transformed (the
+// same expressions evaluated once when the tables are loaded).
+static __device__ __noinline__ double cp_cdf_corner(const double* table, const double* logt, double frac) {
     if (frac <= table[1]) return 0.9;
     double rs[62];
-    for (int i = 0; i < 31; ++i) {
-        rs[2 * i] = log(table[2 * i]);
-        rs[2 * i + 1] = log(-1.0 * log(1.0 - table[2 * i + 1]));
+    if (logt == nullptr) {
+        for (int i = 0; i < 31; ++i) {
+            rs[2 * i] = log(table[2 * i]);
+            rs[2 * i + 1] = cp_cdf_log_node(table[2 * i + 1]);
+        }
+        logt = rs;
     }
     double f2 = log(-1.0 * log(1.0 - frac));
     double v = 0.0;
-    pw_invert(rs, 31, true, f2, &v);
+    pw_invert(logt, 31, true, f2, &v);
     return exp(v);
 }
 
@@ -251,17 +260,19 @@ static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, doubl
     if (la <= MIN0) return 1;
     int ix = (int)((la - MIN0) / S0);
     double dx = (la - MIN0) / S0 - ix;
+    auto corner = [&](size_t row) {
+        return cp_cdf_corner(t.cp_cdf + row * 64, t.cp_cdf_log ? t.cp_cdf_log + row * 64 : nullptr, frac);
+    };
     if (le <= MIN1) {
-        double n = cp_cdf_corner(t.cp_cdf + (size_t)ix * 64, frac) * (1.0 - dx) +
-                   cp_cdf_corner(t.cp_cdf + (size_t)(ix + 1) * 64, frac) * dx;
+        double n = corner((size_t)ix) * (1.0 - dx) + corner((size_t)(ix + 1)) * dx;
         return (int)ceil(n);
     }
     int iy = (int)((le - MIN1) / S1);
     double dy = (le - MIN1) / S1 - iy;
-    double n = cp_cdf_corner(t.cp_cdf + (size_t)(61 * iy + ix) * 64, frac) * ((1.0 - dx) * (1.0 - dy)) +
-               cp_cdf_corner(t.cp_cdf + (size_t)(61 * iy + ix + 1) * 64, frac) * (dx * (1.0 - dy)) +
-               cp_cdf_corner(t.cp_cdf + (size_t)(61 * (iy + 1) + ix) * 64, frac) * ((1.0 - dx) * dy) +
-               cp_cdf_corner(t.cp_cdf + (size_t)(61 * (iy + 1) + ix + 1) * 64, frac) * (dx * dy);
+    double n = corner((size_t)(61 * iy + ix)) * ((1.0 - dx) * (1.0 - dy)) +
+               corner((size_t)(61 * iy + ix + 1)) * (dx * (1.0 - dy)) +
+               corner((size_t)(61 * (iy + 1) + ix)) * ((1.0 - dx) * dy) +
+               corner((size_t)(61 * (iy + 1) + ix + 1)) * (dx * dy);
     return (int)ceil(n);
 }
 
@@ -435,8 +446,8 @@ static __device__ __noinline__ int cp_cl_harmonic_index(const NlcTables& t, doub
     int ix = (int)((log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP);
     double dx = (log(a) - PTG_NLC_CL_MIN) / PTG_NLC_CL_STEP - ix;
     if (ix >= 60) return -1;
-    double n = cp_cdf_corner(t.cp_cl_cdf + (size_t)ix * 64, frac) * (1.0 - dx) +
-               cp_cdf_corner(t.cp_cl_cdf + (size_t)(ix + 1) * 64, frac) * dx;
+    double n = cp_cdf_corner(t.cp_cl_cdf + (size_t)ix * 64, nullptr, frac) * (1.0 - dx) +
+               cp_cdf_corner(t.cp_cl_cdf + (size_t)(ix + 1) * 64, nullptr, frac) * dx;
     if (!isfinite(n)) return -1;
     double c = ceil(n);
     return c >= 2147483647.0 ? 2147483647 : (int)c;

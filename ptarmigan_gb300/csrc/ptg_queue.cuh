@@ -216,13 +216,17 @@ __device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs&
 }
 
 // One step of the lane's particle (main.rs:134-289's loop body); true when
-// the particle is done.
+// the particle is done.  With `bdf`, a photon step whose pair rate needs the
+// harmonic sum is left to the warp and repeats after the warp has served it.
 template <int MODEL>
-__device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCounts& pc) {
+__device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCounts& pc, BwDefer* bdf = nullptr,
+                                           LpDefer* dfr = nullptr) {
     if (lane_stops(a, L)) return true;
     if (L.species != SP_PHOTON) {
         if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop))) return true;
-        pc.fsteps += lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit) ? 1ull : 0ull;
+        bool fr = lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit, dfr);
+        if (dfr != nullptr && dfr->pend == 1) return false;  // the warp samples the emission first
+        pc.fsteps += fr ? 1ull : 0ull;
         ++L.step;
         ++pc.lsteps;
         return L.status != ST_OK;
@@ -238,7 +242,8 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
         L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
         return true;
     }
-    photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair);
+    photon_step<MODEL, true>(a, L, &pc.rej, &pc.npair, bdf);
+    if (bdf != nullptr && bdf->pend == 1) return false;
     ++L.step;
     ++pc.psteps;
     return L.status != ST_OK;
@@ -306,6 +311,22 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
     PartCounts pc{0, 0, 0, 0, 0, 0};
     uint32_t maxst = 0;
     bool have = false, holding = false, finished = false;
+    // CP LMA photons leave their Breit-Wheeler harmonic sums to the warp
+    constexpr bool LMA = MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER;
+    BwDefer* bdf = nullptr;
+    LpDefer* dfr = nullptr;
+    if constexpr (LMA) {
+        __shared__ BwDefer s_bdf[128];
+        __shared__ LpDefer s_dfr[128];
+        if (a.f.circular && a.o.tracking_photons) {
+            bdf = &s_bdf[threadIdx.x];
+            bdf->pend = 0;
+        }
+        if (warp_samples_emissions(a)) {
+            dfr = &s_dfr[threadIdx.x];
+            dfr->pend = 0;
+        }
+    }
     unsigned long long t = 0, t_end = 0, ticket = 0, wait_from = 0;
     for (;;) {
         if (__all_sync(FULL, finished)) break;
@@ -352,11 +373,12 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             __nanosleep(256);
             continue;
         }
-        if (have && queue_step<MODEL>(a, L, pc)) {
+        if (have && queue_step<MODEL>(a, L, pc, bdf, dfr)) {
             maxst = L.step > maxst ? L.step : maxst;
             queue_finish(q, a, L, pc);
             have = false;
         }
+        if (LMA && (bdf != nullptr || dfr != nullptr)) warp_serve(a, dfr, bdf, have);
     }
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }

@@ -22,7 +22,7 @@ _EXPORTS = [
     "ptg_abi_version", "ptg_status_string", "ptg_last_error", "ptg_context_create", "ptg_context_destroy",
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_context_set_limits", "ptg_pair_rate_increase", "ptg_eval_fields", "ptg_push_steps",
-    "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample", "ptg_lp_sample_warp",
+    "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample", "ptg_lp_sample_warp", "ptg_cp_sample", "ptg_cp_sample_warp",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
     "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram", "ptg_particle_sums",
@@ -95,7 +95,7 @@ def load(path=None):
     L.ptg_lcfa_pair_t.argtypes = [ctxp, C.c_size_t, DP, DP, DP]
     L.ptg_double_bessel.restype = st
     L.ptg_double_bessel.argtypes = [ctxp, C.c_int32, C.c_size_t, DP, DP, C.c_int32, DP]
-    for name in ("ptg_lp_sample", "ptg_lp_sample_warp"):
+    for name in ("ptg_lp_sample", "ptg_lp_sample_warp", "ptg_cp_sample", "ptg_cp_sample_warp"):
         getattr(L, name).restype = st
         getattr(L, name).argtypes = [ctxp, C.c_size_t, DP, DP, C.c_uint64, C.POINTER(C.c_uint64), C.c_uint32, DP,
                                      C.POINTER(C.c_int32)]
@@ -509,6 +509,19 @@ class Engine:
         out = np.zeros((len(a), 7))
         status = np.zeros(len(a), dtype=np.int32)
         fn = self.L.ptg_lp_sample_warp if warp else self.L.ptg_lp_sample
+        self._check(fn(self._h, len(a), _dp(a), _dp(eta), seed, streams.ctypes.data_as(C.POINTER(C.c_uint64)), step,
+                       _dp(out), status.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out, status
+
+    def cp_sample(self, a, eta, seed, streams, step, warp=False):
+        """CP LMA samples (the reference's sampler): ([m, 7] = n, s, theta, 1,
+        xi1, xi2, xi3; [m] status).  warp=True draws them with the
+        warp-cooperative sampler."""
+        a, eta = _f64(a, (-1,)), _f64(eta, (-1,))
+        streams = np.ascontiguousarray(streams, dtype=np.uint64)
+        out = np.zeros((len(a), 7))
+        status = np.zeros(len(a), dtype=np.int32)
+        fn = self.L.ptg_cp_sample_warp if warp else self.L.ptg_cp_sample
         self._check(fn(self._h, len(a), _dp(a), _dp(eta), seed, streams.ctypes.data_as(C.POINTER(C.c_uint64)), step,
                        _dp(out), status.ctypes.data_as(C.POINTER(C.c_int32))))
         return out, status

@@ -15,7 +15,7 @@ This script reads those literals from a ptarmigan source tree and writes:
 Run it from the repository root once; its outputs are committed because the
 reference tree does not exist where the GPU code runs::
 
-    python ptarmigan_gb300/tables/extract.py /root/reference
+    python ptarmigan_gb300/tables/extract.py <path of the reference's source tree>
 """
 
 import math
@@ -294,7 +294,9 @@ LARGE_TABLES = [
 
 
 def main(argv):
-    root = argv[1] if len(argv) > 1 else "/root/reference"
+    if len(argv) != 2:
+        sys.exit("usage: extract.py <path of the reference's source tree (the directory holding src/)>")
+    root = argv[1]
     write_small_header(root, os.path.join(HERE, "ptg_tables_small.h"))
     data = os.path.join(HERE, "data")
     os.makedirs(data, exist_ok=True)

@@ -397,6 +397,35 @@ def test_lp_warp_sampler_equals_serial_sampler(eng):
     assert np.array_equal(out_s, out_w)
 
 
+def test_cp_warp_sampler_equals_serial_sampler(eng, orc):
+    """The warp-cooperative CP sampler returns cp_sample's results bit for
+    bit (same harmonic, v, azimuth, Stokes parameters and status), and the
+    serial sampler follows the oracle's restatement of
+    nonlinear_compton/cp/mod.rs:181-234 on the same draws."""
+    a_vals = [0.05, 0.3, 1.0, 2.5, 5.0, 12.0]
+    eta_vals = [2e-3, 0.03, 0.3, 1.5]
+    a, eta, streams = [], [], []
+    for ai in a_vals:
+        for ei in eta_vals:
+            for k in range(40):
+                a.append(ai)
+                eta.append(ei)
+                streams.append(104729 * len(a) + k)
+    a, eta = np.array(a), np.array(eta)
+    streams = np.array(streams, dtype=np.uint64)
+    out_s, st_s = eng.cp_sample(a, eta, 9, streams, 4)
+    out_w, st_w = eng.cp_sample(a, eta, 9, streams, 4, warp=True)
+    assert np.array_equal(st_s, st_w)
+    assert np.count_nonzero(st_s == 0) >= 0.99 * len(a)
+    assert np.array_equal(out_s, out_w)
+    mism = 0
+    for i in range(0, len(a), 7):
+        rc, ref = orc.cp_sample(a[i], eta[i], 9, int(streams[i]), 4)
+        if rc != 0 or int(ref[0]) != int(out_s[i, 0]) or abs(out_s[i, 1] - ref[1]) > 1e-9 * max(abs(ref[1]), 1e-300):
+            mism += 1
+    assert mism <= 0.02 * (len(a) // 7 + 1), mism
+
+
 def test_lma_lp_plane_wave_matches_oracle(eng, orc):
     """Linearly polarised plane wave (LMA), emission only, as in the
     plane-wave benchmark: electrons at 5 GeV, a0 = 1."""

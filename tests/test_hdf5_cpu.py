@@ -149,3 +149,22 @@ def test_names_and_text(tmp_path):
     assert all(v["value"] == k for k, v in r["names"]["members"].items())
     assert r["empty"]["kind"] == "group" and r["empty"]["members"] == {}
     assert r["text"]["value"] == "µm, γ and χ"
+
+
+def test_files_open_in_h5py(tmp_path):
+    """Where h5py (libhdf5) is installed, the files this module writes open
+    in it with the same structure, values and attributes."""
+    h5py = pytest.importorskip("h5py")
+    from ptarmigan_gb300 import hdf5
+    root = hdf5.Group()
+    g = root.group("final-state").group("photon")
+    x = np.arange(12, dtype=np.float64).reshape(3, 4)
+    g.dataset("position", x, unit="m", desc="four-position of the photon")
+    g.dataset("id", np.arange(3, dtype=np.uint64), desc="unique ID of the photon")
+    root.group("config").dataset("input-file", "laser:\n  a0: 1.0\n")
+    fn = str(tmp_path / "f.h5")
+    hdf5.write(fn, root)
+    with h5py.File(fn, "r") as f:
+        np.testing.assert_array_equal(f["final-state/photon/position"][...], x)
+        assert f["final-state/photon/position"].attrs["unit"] in (b"m", "m")
+        np.testing.assert_array_equal(f["final-state/photon/id"][...], np.arange(3))
