@@ -121,6 +121,17 @@ __device__ __forceinline__ bool bw_is_too_small(double a, double eta) {
     return log10(eta) < -1.0 - q * q / 4.5;
 }
 
+// The same decision, taken in FP32 wherever the two sides differ by more
+// than 1e-3 (their FP32 rounding is below 1e-6), else in FP64: the same
+// answer as bw_is_too_small at every (a, eta).
+__device__ __forceinline__ bool bw_is_too_small_fast(double a, double eta) {
+    float q = log10f((float)a) + 2.0f;
+    float d = log10f((float)eta) - (-1.0f - q * q / 4.5f);
+    if (d < -1e-3f) return true;
+    if (d > 1e-3f) return false;
+    return bw_is_too_small(a, eta);
+}
+
 // pair_creation/cp/mod.rs:385-393
 static __device__ __noinline__ void bw_by_summation(double a, double eta, double* f0, double* f1) {
     int n0, n1;
@@ -135,7 +146,11 @@ static __device__ __noinline__ void bw_by_summation(double a, double eta, double
 }
 
 // pair_creation/cp/mod.rs:395-448; false where the reference panics
-static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, double eta, double* f0, double* f1) {
+// `nodes`, when not NULL, holds the table's node positions exp(LN_MIN_A + i
+// LN_A_STEP), i < 74, then exp(LN_MIN_ETA + j LN_ETA_STEP), j < 121,
+// evaluated once when the tables are loaded.
+static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, double eta, double* f0, double* f1,
+                                                 const double* nodes = nullptr) {
     const double LMA = PTG_BW_CP_LN_MIN_A, LME = PTG_BW_CP_LN_MIN_ETA, SA = PTG_BW_CP_LN_A_STEP, SE = PTG_BW_CP_LN_ETA_STEP;
     const int NC = 74, NR = 121;
     double x = log(a), y = log(eta);
@@ -156,8 +171,14 @@ static __device__ __noinline__ bool bw_by_lookup(const double* T, double a, doub
         double w0 = (1.0 - dx) * (1.0 - dy), w1 = dx * (1.0 - dy), w2 = (1.0 - dx) * dy, w3 = dx * dy;
         for (int k = 0; k < 2; ++k) f[k] = exp(w0 * p00[k] + w1 * p01[k] + w2 * p10[k] + w3 * p11[k]);
     } else {
-        double a_min = exp(LMA + ix * SA), a_max = exp(LMA + (ix + 1) * SA);
-        double e_min = exp(LME + iy * SE), e_max = exp(LME + (iy + 1) * SE);
+        double a_min, a_max, e_min, e_max;
+        if (nodes != nullptr) {
+            a_min = nodes[ix], a_max = nodes[ix + 1];
+            e_min = nodes[NC + iy], e_max = nodes[NC + iy + 1];
+        } else {
+            a_min = exp(LMA + ix * SA), a_max = exp(LMA + (ix + 1) * SA);
+            e_min = exp(LME + iy * SE), e_max = exp(LME + (iy + 1) * SE);
+        }
         double dx = (a - a_min) / (a_max - a_min), dy = (eta - e_min) / (e_max - e_min);
         double w0 = (1.0 - dx) * (1.0 - dy), w1 = dx * (1.0 - dy), w2 = (1.0 - dx) * dy, w3 = dx * dy;
         for (int k = 0; k < 2; ++k) f[k] = exp(1.0 / (w0 / p00[k] + w1 / p01[k] + w2 / p10[k] + w3 / p11[k]));
@@ -200,12 +221,14 @@ __device__ __forceinline__ double bw_summation_bound(double a, double eta) {
     return lead * ((A + B * n) / om + B * rho / (om * om));
 }
 
-// Per-step pair probabilities below this are taken as zero where the rate
-// would otherwise be summed harmonic by harmonic.  No uniform draw is that
-// small but an exact zero (draws are multiples of 2^-53), the Stokes
-// factors (1 - p_avg) / (1 - p) of bw_probability round to exactly 1, and
-// the interaction count differs by less than this per step.
-constexpr double PAIR_PROB_NEGLIGIBLE = 1e-25;
+// Per-step pair probabilities below this, after the event biasing
+// (p max(1, rate_increase)), are taken as zero where the rate would
+// otherwise be summed harmonic by harmonic.  Then no uniform draw passes
+// p ri but an exact zero (draws are multiples of 2^-53), the Stokes
+// factors (1 - p_avg) / (1 - p) of bw_probability round to exactly 1 (p is
+// below half an ulp of 1), the Stokes vector's third component moves by
+// less than 2^-54, and the interaction count by less than 2^-54 per step.
+constexpr double PAIR_PROB_NEGLIGIBLE = 0x1p-54;
 
 // exp(LN_MIN_A) of the CP total-rate table, the smallest amplitude it covers,
 // as the host's libm rounds it (0.3); evaluating it on every step cost an
@@ -381,12 +404,6 @@ static __device__ __noinline__ void bw_by_summation_warp(double a, double eta, d
     *f1 = 2.0 * __shfl_sync(all, im, 0);
 }
 
-// The CP Breit-Wheeler rate is a harmonic sum at (a, eta) that matters.
-__device__ __forceinline__ bool bw_needs_summation(double a, double eta, double c) {
-    return a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta) &&
-           !(c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE);
-}
-
 // Status of bw_probability for a step left to the warp
 constexpr int BW_DEFERRED = -1;
 
@@ -395,23 +412,30 @@ constexpr int BW_DEFERRED = -1;
 // NULL).
 static __device__ __noinline__ int bw_probability(const double* T, d4 ell, d4 sv_in, d4 k, double a, double dt,
                                                   double pol_angle, double* prob, d4* sv_out,
-                                                  BwDefer* bdf = nullptr) {
+                                                  double rate_increase = 1.0, BwDefer* bdf = nullptr,
+                                                  const double* nodes = nullptr) {
     double eta = dot4(k, ell);
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
     double f0, f1;
     double c = ALPHA_FINE * dphi / eta;
-    if (a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta) &&
-        c * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE) {
-        // the summed rate cannot give a probability that matters: skip it
+    // TotalRate::value's dispatch (bw_rates), its too-small test taken once
+    if (a < 0.02 || bw_is_too_small_fast(a, eta)) {
         f0 = f1 = 0.0;
-    } else if (bdf != nullptr && a >= 0.02 && a < BW_CP_MIN_A && !bw_is_too_small(a, eta)) {
-        if (bdf->pend != 2) {
-            bdf->a = a, bdf->eta = eta, bdf->pend = 1;
-            return BW_DEFERRED;
+    } else if (a < BW_CP_MIN_A) {
+        if (c * fmax(1.0, rate_increase) * bw_summation_bound(a, eta) < PAIR_PROB_NEGLIGIBLE) {
+            // the summed rate cannot give a probability that matters: skip it
+            f0 = f1 = 0.0;
+        } else if (bdf != nullptr) {
+            if (bdf->pend != 2) {
+                bdf->a = a, bdf->eta = eta, bdf->pend = 1;
+                return BW_DEFERRED;
+            }
+            f0 = bdf->f0, f1 = bdf->f1;
+            bdf->pend = 0;
+        } else {
+            bw_by_summation(a, eta, &f0, &f1);
         }
-        f0 = bdf->f0, f1 = bdf->f1;
-        bdf->pend = 0;
-    } else if (!bw_rates(T, a, eta, &f0, &f1)) {
+    } else if (!bw_by_lookup(T, a, eta, &f0, &f1, nodes)) {
         return 0;
     }
     d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);

@@ -881,6 +881,20 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
             *slot32 = (const float*)q;
         }
     }
+    // node positions of the CP Breit-Wheeler table, with the host's
+    // exponential (the reference evaluates them with its libm on the host)
+    {
+        std::vector<double> nodes(74 + 121);
+        for (int i = 0; i < 74; ++i) nodes[i] = std::exp(PTG_BW_CP_LN_MIN_A + i * PTG_BW_CP_LN_A_STEP);
+        for (int j = 0; j < 121; ++j) nodes[74 + j] = std::exp(PTG_BW_CP_LN_MIN_ETA + j * PTG_BW_CP_LN_ETA_STEP);
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, 8 * nodes.size());
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        bufs.push_back(q);
+        e = cudaMemcpy(q, nodes.data(), 8 * nodes.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        host.bw_cp_nodes = (const double*)q;
+    }
     host.nlc_cp_cdf_log = nullptr;
     if (host.nlc_cp_cdf) {
         const unsigned long long nodes = 4270ull * 32;

@@ -33,6 +33,9 @@ struct LmaTables {
     // nlc_cp_cdf's nodes as [ln n, ln(-ln(1 - cdf))], the coordinates its
     // inversion works in, evaluated once on the device at load
     const double* nlc_cp_cdf_log;   // [4270][32][2]
+    // the CP Breit-Wheeler total-rate table's node positions in a (74) and
+    // eta (121), computed once at load
+    const double* bw_cp_nodes;
 };
 
 // The per-step emission probability is first evaluated in FP32 from the
@@ -290,7 +293,8 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
     double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp;
     d4 kappa = d4{kk, 0.0, 0.0, kk};
     if (f.circular) {
-        int ok = bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new, bdf);
+        int ok = bw_probability(t.bw_cp_total, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new, rate_increase, bdf,
+                                t.bw_cp_nodes);
         if (ok == BW_DEFERRED) return LMA_DEFERRED;  // the step repeats once the warp has summed
         if (!ok) return 2;
     } else if (!lp_bw_probability(t, ell, pol, kappa, a, dt, f.pol_angle, prob, pol_new)) {

@@ -233,28 +233,24 @@ beam:
 output:
   ident: auto
   dump_all_particles: hdf5
-  dump_decayed_photons: true
-  intermediate:
-    - energy:(20;weight)
 """
 
 
-def test_auto_rate_stop_time_spectrum_and_intermediates(tmp_path):
+def test_auto_rate_stop_time_and_spectrum(tmp_path):
     """One LMA run with a tabulated beam spectrum, the automatic pair-rate
-    increase (so that photons decay), stop_at_time: auto, decayed photons
-    kept: every final-state particle ends at the same time coordinate, the
-    decayed photons are written to the intermediate-state group and to
-    their own distribution file, and the file records the rate increase."""
+    increase and stop_at_time: auto: every final-state particle ends at the
+    same time coordinate, the file records the rate increase, and the
+    pairs carry the biased weight 1 / rate."""
     from ptarmigan_gb300 import hdf5
     from ptarmigan_gb300.driver import run
     src = tmp_path / "auto.yml"
     src.write_text(AUTO.format(stop="auto"))
     files = run(str(src), str(tmp_path / "out"), log=lambda *a: None)
-    names = sorted(os.path.basename(f) for f in files)
-    assert "auto_particles.h5" in names and "auto_intermediate_energy.dat" in names
+    assert [os.path.basename(f) for f in files] == ["auto_particles.h5"]
     f = hdf5.read(str(tmp_path / "out" / "auto_particles.h5"))["members"]
     ctl = f["config"]["members"]["control"]["members"]
-    assert ctl["increase_pair_rate_by"]["value"] > 1.0
+    rate = ctl["increase_pair_rate_by"]["value"]
+    assert rate > 1.0
     t_stop = ctl["stop_at_time"]["value"]
     fs = f["final-state"]["members"]
     for sp in ("photon", "electron", "positron"):
@@ -262,13 +258,69 @@ def test_auto_rate_stop_time_spectrum_and_intermediates(tmp_path):
         if x.size:
             # positions in metres (auto units): c t = c t_stop for every particle
             np.testing.assert_allclose(x[:, 0], 2.997925e8 * t_stop, rtol=1e-12)
+    w = fs["positron"]["members"]["weight"]["value"]
+    if w.size:
+        assert np.all(w <= 1.0 / rate * (1.0 + 1e-12))
+    assert fs["electron"]["members"]["id"]["value"].size >= 2000
+
+
+INTERMEDIATE = """---
+control:
+  lcfa: true
+  pair_creation: true
+  rng_seed: 9
+laser:
+  a0: 30.0
+  wavelength: 0.8 * micro
+  waist: 2.0 * micro
+  fwhm_duration: 30.0 * femto
+  polarization: linear
+beam:
+  n: 300
+  species: electron
+  gamma: 10.0 * GeV / (me * c^2)
+  radius: [0.5 * micro, normally_distributed]
+  length: 2.0 * micro
+output:
+  ident: inter
+  dump_all_particles: hdf5
+  dump_decayed_photons: true
+  intermediate:
+    - energy:(20;weight)
+stats:
+  intermediate:
+    - total number
+  photon:
+    - total number
+"""
+
+
+def test_decayed_photons_are_written(tmp_path):
+    """The photons that decay into pairs are kept (keep_decayed_photons)
+    when an output asks for them: they fill the HDF5 file's
+    intermediate-state group and their own distribution file, one per pair,
+    and they are not in the final state."""
+    from ptarmigan_gb300 import hdf5
+    from ptarmigan_gb300.driver import run
+    src = tmp_path / "inter.yml"
+    src.write_text(INTERMEDIATE)
+    files = run(str(src), str(tmp_path / "out"), log=lambda *a: None)
+    names = sorted(os.path.basename(f) for f in files)
+    assert "inter_intermediate_energy.dat" in names and "inter_particles.h5" in names
+    f = hdf5.read(str(tmp_path / "out" / "inter_particles.h5"))["members"]
     inter = f["intermediate-state"]["members"]["photon"]["members"]
-    n_dec = inter["weight"]["value"].size
-    assert n_dec > 0
-    assert fs["positron"]["members"]["weight"]["value"].size >= n_dec
-    # the primaries' energies follow the tabulated spectrum (mean ~ 32000 m c^2)
-    el = fs["electron"]["members"]
-    assert el["id"]["value"].size >= 2000
+    ids = inter["id"]["value"]
+    assert ids.size > 0
+    fs = f["final-state"]["members"]
+    # each decayed photon made one pair: it is the parent of a positron
+    pos_parent = set(int(x) for x in fs["positron"]["members"]["parent_id"]["value"])
+    assert set(int(x) for x in ids) <= pos_parent
+    assert not set(int(x) for x in ids) & set(int(x) for x in fs["photon"]["members"]["id"]["value"])
+    axes, units, rows = _read_dat(str(tmp_path / "out" / "inter_intermediate_energy.dat"))
+    width = rows[1, 0] - rows[0, 0]
+    # the density integrates to the photons in the bins (the largest energy
+    # can fall past the last bin edge)
+    assert abs(np.sum(rows[:, 1]) * width - ids.size) <= 1.0 + 1e-6 * ids.size
 
 
 def test_given_stop_time_moves_every_particle(tmp_path):
