@@ -381,6 +381,13 @@ ptg_status ptg_cp_sample(ptg_ctx* ctx, size_t count, const double* a, const doub
 ptg_status ptg_cp_sample_warp(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
                               const uint64_t* stream, uint32_t step, double* out7, int32_t* status);
 
+/* The same emissions sampled with the learned proposal in use
+ * (ptg_mlp_use), as the collision kernels sample them: on each point's own
+ * lane (warp = 0) or by its warp's 32 lanes together (warp = 1), with the
+ * same results either way.  No reference counterpart. */
+ptg_status ptg_cp_sample_learned(ptg_ctx* ctx, size_t count, const double* a, const double* eta, uint64_t seed,
+                                 const uint64_t* stream, uint32_t step, int32_t warp, double* out7, int32_t* status);
+
 /* --------------------------------------------------- learned proposal ---
  * No reference counterpart: an MLP (six features of a, eta and n; 4 layers
  * of width 64, SiLU; BF16 weights, FP32 accumulation; trained and run on the

@@ -248,20 +248,57 @@ __device__ __forceinline__ bool bw_rates(const double* T, double a, double eta, 
     return bw_by_lookup(T, a, eta, f0, f1);
 }
 
-// pair_creation/cp/mod.rs:191-243: s by rejection on the theta-integrated
-// spectrum, the side of s = 1/2, then theta by rejection.
-static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3,
-                                              Draws& rng, double* s_out, double* theta_out, uint32_t* rej) {
+// Work of a photon step left by its lane for the whole warp (the wave
+// kernel and the single-collision queue kernel), in two kinds:
+//   BW_DEFER_RATE: the CP Breit-Wheeler rate needs the harmonic sum; the
+//     lane records a and eta; the warp sums the harmonics with one
+//     Gauss-Legendre node per lane (bw_by_summation_warp);
+//   BW_DEFER_HARMONIC: a pair is created and its harmonic is sampled; the
+//     lane records a, eta, S3 and its uniform draw; the warp walks the
+//     harmonics' cumulative sum (bw_sample_harmonic_warp) and evaluates the
+//     ceiling of the s spectrum for the harmonic it finds.
+// The lane abandons the step and repeats it once served; the repeat draws
+// the same numbers, reaches the same request and takes the warp's result.
+constexpr int BW_DEFER_RATE = 1;
+constexpr int BW_DEFER_HARMONIC = 2;
+struct BwDefer {
+    double a, eta, sv3, u;  // the request
+    double f0, f1, s_ceil;  // the results: the rates and the s ceiling
+    int n;                  // the sampled harmonic, -1 out of table
+    int kind;
+    int pend;  // 0: none; 1: waiting for the warp; 2: served
+};
+
+// Status of bw_probability and bw_sample for a step left to the warp
+constexpr int BW_DEFERRED = -1;
+
+// pair_creation/cp/mod.rs:199-207: the largest of the theta-integrated
+// spectrum's values at the 32 Gauss-Legendre nodes over [s_min, 1/2] (NaN
+// values are passed over, as f64::max does)
+__device__ __forceinline__ double bw_s_node_value(int n, double a, double eta, double sv3, int k) {
     double s_min, s_max;
     bw_s_bounds(n, a, eta, &s_min, &s_max);
+    double s = 0.5 * (s_max - s_min) * PTG_GAUSS_32_NODES[k] + 0.5 * (s_min + s_max);
+    double re, im;
+    bw_over_theta(n, a, eta, s, &re, &im);
+    return 0.5 * (re * (1.0 + sv3) + im * (1.0 - sv3));
+}
+
+static __device__ __noinline__ double bw_s_ceiling(int n, double a, double eta, double sv3) {
     double mx = __longlong_as_double(0x7ff8000000000000LL);
-    for (int k = 0; k < 32; ++k) {
-        double s = 0.5 * (s_max - s_min) * PTG_GAUSS_32_NODES[k] + 0.5 * (s_min + s_max);
-        double re, im;
-        bw_over_theta(n, a, eta, s, &re, &im);
-        mx = fmax(mx, 0.5 * (re * (1.0 + sv3) + im * (1.0 - sv3)));
-    }
-    mx *= 1.5;
+    for (int k = 0; k < 32; ++k) mx = fmax(mx, bw_s_node_value(n, a, eta, sv3, k));
+    return mx;
+}
+
+// pair_creation/cp/mod.rs:191-243: s by rejection on the theta-integrated
+// spectrum under 1.5 x `ceil` (bw_s_ceiling), the side of s = 1/2, then
+// theta by rejection.
+static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta, double sv1, double sv2, double sv3,
+                                                     double ceil, Draws& rng, double* s_out, double* theta_out,
+                                                     uint32_t* rej) {
+    double s_min, s_max;
+    bw_s_bounds(n, a, eta, &s_min, &s_max);
+    double mx = 1.5 * ceil;
     double s = 0.0;
     int it;
     for (it = 0; it < rng.cap; ++it) {
@@ -297,28 +334,49 @@ static __device__ __noinline__ int bw_sample_s_theta(int n, double a, double eta
     return 0;
 }
 
-// pair_creation/cp/mod.rs:314-346: harmonic by explicit summation
+// pair_creation/cp/mod.rs:314-346: harmonic by explicit summation.  With
+// `bdf`, the harmonic and the s ceiling are left to the warp
+// (BW_DEFER_HARMONIC): returns BW_DEFERRED until the warp has served them.
 static __device__ __noinline__ int bw_sample(const double* T, double a, double eta, double sv1, double sv2, double sv3,
-                                      Draws& rng, int* n_out, double* s, double* theta, uint32_t* rej) {
-    int n0, n1;
-    bw_sum_limits(a, eta, &n0, &n1);
-    double f0, f1;
-    if (!bw_rates(T, a, eta, &f0, &f1)) return 2;
-    double target = 0.5 * (f0 * (1.0 + sv3) + f1 * (1.0 - sv3)) * rng.next();
-    double cum = 0.0;
-    int index = -1;
-    for (int k = n0; k <= n1; ++k) {
-        double re, im;
-        bw_integrate(k, a, eta, &re, &im);
-        cum += 0.5 * ((1.0 + sv3) * re + (1.0 - sv3) * im);
-        if (cum > target) {
-            index = k;
-            break;
+                                             Draws& rng, int* n_out, double* s, double* theta, uint32_t* rej,
+                                             BwDefer* bdf = nullptr) {
+    double u = rng.next();
+    int index;
+    double ceil;
+    if (bdf != nullptr) {
+        if (!(bdf->pend == 2 && bdf->kind == BW_DEFER_HARMONIC && bdf->a == a && bdf->eta == eta && bdf->sv3 == sv3 &&
+              bdf->u == u)) {
+            bdf->a = a, bdf->eta = eta, bdf->sv3 = sv3, bdf->u = u;
+            bdf->kind = BW_DEFER_HARMONIC;
+            bdf->pend = 1;
+            return BW_DEFERRED;
         }
+        bdf->pend = 0;
+        if (bdf->n < 0) return 2;
+        index = bdf->n;
+        ceil = bdf->s_ceil;
+    } else {
+        int n0, n1;
+        bw_sum_limits(a, eta, &n0, &n1);
+        double f0, f1;
+        if (!bw_rates(T, a, eta, &f0, &f1)) return 2;
+        double target = 0.5 * (f0 * (1.0 + sv3) + f1 * (1.0 - sv3)) * u;
+        double cum = 0.0;
+        index = -1;
+        for (int k = n0; k <= n1; ++k) {
+            double re, im;
+            bw_integrate(k, a, eta, &re, &im);
+            cum += 0.5 * ((1.0 + sv3) * re + (1.0 - sv3) * im);
+            if (cum > target) {
+                index = k;
+                break;
+            }
+        }
+        if (index == -1) index = n1 - 1;
+        ceil = bw_s_ceiling(index, a, eta, sv3);
     }
-    if (index == -1) index = n1 - 1;
     *n_out = index;
-    return bw_sample_s_theta(index, a, eta, sv1, sv2, sv3, rng, s, theta, rej);
+    return bw_sample_s_theta(index, a, eta, sv1, sv2, sv3, ceil, rng, s, theta, rej);
 }
 
 // polarization.rs:101-130: Stokes parameters in the LMA basis
@@ -338,16 +396,46 @@ __device__ __forceinline__ d4 stokes_rotate_by(d4 sv, double theta) {
     return d4{sv.t, c2 * sv.x + s2 * sv.y, -s2 * sv.x + c2 * sv.y, sv.z};
 }
 
-// A photon step whose CP Breit-Wheeler rate needs the harmonic sum, left by
-// its lane for the whole warp (the wave kernel and the single-collision
-// queue kernel): the lane records a and eta and abandons the step; the warp
-// sums the harmonics with one Gauss-Legendre node per lane
-// (bw_by_summation_warp); the lane then repeats its step, which reaches the
-// same sum and takes the warp's result.
-struct BwDefer {
-    double a, eta, f0, f1;
-    int pend;  // 0: none; 1: waiting for the warp; 2: served
-};
+// Lane k's share of bw_integrate (pair_creation/cp/mod.rs:92-186) for
+// harmonic n: node k of each of the harmonic's segments, weighted (the
+// factor 2 of bw_integrate is left to the caller).
+__device__ __forceinline__ void bw_integrate_lane(int n, double a, double eta, double xk, double wk, double* re,
+                                                  double* im) {
+    *re = 0.0, *im = 0.0;
+    double ell = n;
+    double sn = 2.0 * ell * eta / (1.0 + a * a);
+    if (sn <= 4.0) return;
+    double a2 = a * a;
+    double w1 = 1.0 / ell + 1.0;
+    double beta = a2 * a2 * w1 * w1 + 16.0 * (a2 - 2.0) * (a2 - 2.0) / (sn * sn) - 8.0 * a2 * (a2 - 2.0) / sn;
+    beta = sqrt(beta) / (a2 - 2.0);
+    double alpha = (a2 + 2.0 * ell) / (ell * (2.0 - a2)) - 4.0 / sn;
+    double s_peak = 0.5 * (1.0 - sqrt(alpha + beta));
+    double s_min, s_max;
+    bw_s_bounds(n, a, eta, &s_min, &s_max);
+    double lo[3], hi[3];
+    int nseg;
+    if (isfinite(s_peak)) {
+        double s_mid = 2.0 * s_peak - s_min;
+        if (s_mid > s_max) {
+            nseg = 2;
+            lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_max;
+        } else {
+            nseg = 3;
+            lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_mid, lo[2] = s_mid, hi[2] = s_max;
+        }
+    } else {
+        nseg = 1;
+        lo[0] = s_min, hi[0] = s_max;
+    }
+    for (int g = 0; g < nseg; ++g) {
+        double h = 0.5 * (hi[g] - lo[g]), m = 0.5 * (lo[g] + hi[g]);
+        double sr, si;
+        bw_over_theta(n, a, eta, h * xk + m, &sr, &si);
+        *re += h * wk * sr;
+        *im += h * wk * si;
+    }
+}
 
 // bw_by_summation (pair_creation/cp/mod.rs:385-393) evaluated by the 32
 // lanes of a converged warp: lane k evaluates node k of every segment of
@@ -362,39 +450,9 @@ static __device__ __noinline__ void bw_by_summation_warp(double a, double eta, d
     const double xk = PTG_GAUSS_32_NODES[lane], wk = PTG_GAUSS_32_WEIGHTS[lane];
     double re = 0.0, im = 0.0;
     for (int n = n0; n <= n1; ++n) {
-        double ell = n;
-        double sn = 2.0 * ell * eta / (1.0 + a * a);
-        if (sn <= 4.0) continue;
-        double a2 = a * a;
-        double w1 = 1.0 / ell + 1.0;
-        double beta = a2 * a2 * w1 * w1 + 16.0 * (a2 - 2.0) * (a2 - 2.0) / (sn * sn) - 8.0 * a2 * (a2 - 2.0) / sn;
-        beta = sqrt(beta) / (a2 - 2.0);
-        double alpha = (a2 + 2.0 * ell) / (ell * (2.0 - a2)) - 4.0 / sn;
-        double s_peak = 0.5 * (1.0 - sqrt(alpha + beta));
-        double s_min, s_max;
-        bw_s_bounds(n, a, eta, &s_min, &s_max);
-        double lo[3], hi[3];
-        int nseg;
-        if (isfinite(s_peak)) {
-            double s_mid = 2.0 * s_peak - s_min;
-            if (s_mid > s_max) {
-                nseg = 2;
-                lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_max;
-            } else {
-                nseg = 3;
-                lo[0] = s_min, hi[0] = s_peak, lo[1] = s_peak, hi[1] = s_mid, lo[2] = s_mid, hi[2] = s_max;
-            }
-        } else {
-            nseg = 1;
-            lo[0] = s_min, hi[0] = s_max;
-        }
-        for (int g = 0; g < nseg; ++g) {
-            double h = 0.5 * (hi[g] - lo[g]), m = 0.5 * (lo[g] + hi[g]);
-            double sr, si;
-            bw_over_theta(n, a, eta, h * xk + m, &sr, &si);
-            re += h * wk * sr;
-            im += h * wk * si;
-        }
+        double r, i;
+        bw_integrate_lane(n, a, eta, xk, wk, &r, &i);
+        re += r, im += i;
     }
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_down_sync(all, re, o);
@@ -404,8 +462,61 @@ static __device__ __noinline__ void bw_by_summation_warp(double a, double eta, d
     *f1 = 2.0 * __shfl_sync(all, im, 0);
 }
 
-// Status of bw_probability for a step left to the warp
-constexpr int BW_DEFERRED = -1;
+// The harmonic of bw_sample (pair_creation/cp/mod.rs:314-346) and the s
+// ceiling of bw_sample_s_theta (cp/mod.rs:199-207), evaluated by the 32
+// lanes of a converged warp for one lane's request: the rates (the warp's
+// harmonic sum below a = 0.3, else the table), then the cumulative sum over
+// harmonics with lane k evaluating node k of every segment, reduced by a
+// butterfly (every lane holds the same sum, so the walk stops on the same
+// harmonic in every lane), then the ceiling's 32 nodes one per lane.  The
+// harmonic is the serial walk's up to the order of the additions; the
+// ceiling is the serial maximum exactly.  n_out is -1 where the rate
+// lookup is out of table.
+static __device__ __noinline__ void bw_sample_harmonic_warp(const double* T, const double* nodes, double a, double eta,
+                                                            double sv3, double u, int* n_out, double* ceil_out,
+                                                            double* f0_out, double* f1_out) {
+    const unsigned all = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    double f0, f1;
+    bool ok = true;
+    if (a < 0.02 || bw_is_too_small(a, eta)) {
+        f0 = f1 = 0.0;
+    } else if (a < BW_CP_MIN_A) {
+        bw_by_summation_warp(a, eta, &f0, &f1);
+    } else {
+        ok = bw_by_lookup(T, a, eta, &f0, &f1, nodes);
+    }
+    *f0_out = f0, *f1_out = f1;
+    if (!ok) {
+        *n_out = -1;
+        *ceil_out = 0.0;
+        return;
+    }
+    int n0, n1;
+    bw_sum_limits(a, eta, &n0, &n1);
+    const double xk = PTG_GAUSS_32_NODES[lane], wk = PTG_GAUSS_32_WEIGHTS[lane];
+    double target = 0.5 * (f0 * (1.0 + sv3) + f1 * (1.0 - sv3)) * u;
+    double cum = 0.0;
+    int index = -1;
+    for (int n = n0; n <= n1; ++n) {
+        double re, im;
+        bw_integrate_lane(n, a, eta, xk, wk, &re, &im);
+        for (int o = 16; o > 0; o >>= 1) {
+            re += __shfl_xor_sync(all, re, o);
+            im += __shfl_xor_sync(all, im, o);
+        }
+        cum += 0.5 * ((1.0 + sv3) * (2.0 * re) + (1.0 - sv3) * (2.0 * im));
+        if (cum > target) {
+            index = n;
+            break;
+        }
+    }
+    if (index == -1) index = n1 - 1;
+    double mx = bw_s_node_value(index, a, eta, sv3, lane);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(all, mx, o));
+    *n_out = index;
+    *ceil_out = mx;
+}
 
 // pair_creation/mod.rs:21-42 + cp/mod.rs:280-309 (CP).  Returns 1, 0 out of
 // table, or BW_DEFERRED when the harmonic sum is left to the warp (bdf not
@@ -426,12 +537,16 @@ static __device__ __noinline__ int bw_probability(const double* T, d4 ell, d4 sv
             // the summed rate cannot give a probability that matters: skip it
             f0 = f1 = 0.0;
         } else if (bdf != nullptr) {
-            if (bdf->pend != 2) {
-                bdf->a = a, bdf->eta = eta, bdf->pend = 1;
+            // the warp's sum: served for this step's rate, or with the
+            // harmonic of this step's pair (which bw_sample then takes)
+            if (!(bdf->pend == 2 && bdf->a == a && bdf->eta == eta)) {
+                bdf->a = a, bdf->eta = eta;
+                bdf->kind = BW_DEFER_RATE;
+                bdf->pend = 1;
                 return BW_DEFERRED;
             }
             f0 = bdf->f0, f1 = bdf->f1;
-            bdf->pend = 0;
+            if (bdf->kind == BW_DEFER_RATE) bdf->pend = 0;
         } else {
             bw_by_summation(a, eta, &f0, &f1);
         }
@@ -484,12 +599,12 @@ static __device__ __noinline__ int bw_kinematics(d4 ell, d4 k, double a, double 
 
 // pair_creation/mod.rs:49-110 (CP): the positron momentum
 static __device__ __noinline__ int bw_generate(const double* T, d4 ell, d4 sv_in, d4 k, double a, double pol_angle, Draws& rng,
-                                        int* n_out, d4* q_out, uint32_t* rej) {
+                                        int* n_out, d4* q_out, uint32_t* rej, BwDefer* bdf = nullptr) {
     double eta = dot4(k, ell);
     d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
     int n;
     double s, cphi;
-    int st = bw_sample(T, a, eta, sv.x, sv.y, sv.z, rng, &n, &s, &cphi, rej);
+    int st = bw_sample(T, a, eta, sv.x, sv.y, sv.z, rng, &n, &s, &cphi, rej, bdf);
     if (st != 0) return st;
     *n_out = n;
     return bw_kinematics(ell, k, a, pol_angle, n, s, cphi, q_out);

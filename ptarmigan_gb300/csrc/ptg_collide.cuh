@@ -117,7 +117,31 @@ struct Lane {
     int species, gen, status, flags;
     int coll;
     bool decayed;
+    // LMA leptons: the last step was field-free and left u^0 unchanged, so
+    // `hh` holds that step's half-drift factor (c/2)(dt / u^0) (lma_drift)
+    bool drift_cached;
 };
+
+// A field-free LMA lepton step (lma_push_field_free).  Its momentum is
+// unchanged and u^0 is recomputed from it, so once a step has left u^0 as
+// it found it, every later field-free step reproduces the same u^0, the
+// same dt / u^0 and the same half-drift factor: those steps only add h u
+// twice, with the same additions, and skip the division and the square
+// root.
+__device__ __forceinline__ void lma_drift(Lane& L, double dt) {
+    if (L.drift_cached) {
+        double h = L.hh;
+        d4 r = d4{L.r.t + h * L.u.t, L.r.x + h * L.u.x, L.r.y + h * L.u.y, L.r.z + h * L.u.z};
+        L.r = d4{r.t + h * L.u.t, r.x + h * L.u.x, r.y + h * L.u.y, r.z + h * L.u.z};
+        return;
+    }
+    double u0t = L.u.t, dt_actual;
+    lma_push_field_free(L.r, L.u, dt, &L.r, &L.u, &dt_actual);
+    if (L.u.t == u0t) {
+        L.drift_cached = true;
+        L.hh = 0.5 * SPEED_OF_LIGHT * (dt / L.u.t);
+    }
+}
 
 __device__ __forceinline__ bool lane_untracked(const WaveArgs& a, const Lane& L) {
     return (!a.o.tracking_secondaries && L.gen > 0) || (a.o.max_generation >= 0 && L.gen > a.o.max_generation);
@@ -281,9 +305,10 @@ __device__ __forceinline__ bool lepton_step(const WaveArgs& a, Lane& L, uint32_t
             // outside the pulse: the step only drifts, and its emission
             // probability (proportional to <a^2> < 2^-60) is below every
             // nonzero uniform, so it draws nothing
-            lma_push_field_free(L.r, L.u, dt, &L.r, &L.u, &dt_actual);
+            lma_drift(L, dt);
             return true;
         }
+        L.drift_cached = false;
         lma_push(f, L.r, L.u, rqm, dt, a.o.eqn, &r, &u, &dt_actual, &dwork);
         DbWork dbw{nullptr, 0, 32};
         if (a.dbw) {
@@ -530,6 +555,7 @@ __device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
     L.flags = s.flags[i];
     L.step = 0;
     L.decayed = false;
+    L.drift_cached = false;
     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
     L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
     return true;
@@ -561,9 +587,12 @@ __device__ __forceinline__ DbWork lane_dbw(const WaveArgs& a) {
     return w;
 }
 
-// The LP emission deferred by lane `src` of this warp (`warp_dfr` is the
-// warp's array), sampled by all 32 lanes.
+// The emission deferred by lane `src` of this warp (`warp_dfr` is the
+// warp's array), sampled by all 32 lanes: LP, CP with the reference's
+// sampler, or CP with the learned proposal.
 static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* warp_dfr, int src) {
+    // the learned proposal's network scratch: 2 x 64 floats per warp
+    __shared__ __align__(16) float s_mlp[4][2 * MLP_H];
     __syncwarp();
     LpDefer& d = warp_dfr[src];
     Draws rng = d.rng;
@@ -571,8 +600,14 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
     double s = 0.0, theta = 0.0;
     d3 sv = mk3(0.0, 0.0, 0.0);
     uint32_t rej = 0;
-    int st = a.f.circular ? cp_sample_warp(nlc_view(*a.lma), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej)
-                          : lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
+    int st;
+    if (!a.f.circular)
+        st = lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
+    else if (a.mlp.enabled)
+        st = cp_sample_learned_warp(*mlp_smem(), a.mlp.margin, nlc_view(*a.lma), s_mlp[threadIdx.x >> 5], d.a, d.eta,
+                                    rng, &n, &s, &theta, &sv, &rej);
+    else
+        st = cp_sample_warp(nlc_view(*a.lma), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
     __syncwarp();
     if ((int)lane_id() == src) {
         d.rng = rng;
@@ -583,24 +618,37 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
 }
 
 // Emissions are sampled by the whole warp: LMA linear polarisation (with
-// the DoubleBessel workspaces) and the reference's circular-polarisation
-// sampler (the learned proposal samples on its lane); not classically.
-// Uniform over the grid: the kernel's arguments decide.
+// the DoubleBessel workspaces) and circular polarisation (the reference's
+// sampler or the learned proposal); not classically.  Uniform over the
+// grid: the kernel's arguments decide.
 __device__ __forceinline__ bool warp_samples_emissions(const WaveArgs& a) {
     if (a.o.classical_mode) return false;
-    return a.f.circular ? !a.mlp.enabled : a.dbw != nullptr;
+    return a.f.circular ? true : a.dbw != nullptr;
 }
 
-// The CP Breit-Wheeler harmonic sum left by lane `src` of this warp
-// (`warp_bdf` is the warp's array), evaluated by all 32 lanes.
-static __device__ __noinline__ void bw_defer_serve(BwDefer* warp_bdf, int src) {
+// The learned proposal samples on the warp from the network staged in the
+// block's shared memory: staged by every thread at the kernel's start.
+__device__ __forceinline__ void stage_network(const WaveArgs& a) {
+    if (warp_samples_emissions(a) && a.f.circular && a.mlp.enabled) mlp_stage(a.mlp, mlp_smem());
+}
+
+// The CP Breit-Wheeler work left by lane `src` of this warp (`warp_bdf` is
+// the warp's array), evaluated by all 32 lanes: the rate's harmonic sum, or
+// a pair's harmonic with its s ceiling.
+static __device__ __noinline__ void bw_defer_serve(const WaveArgs& a, BwDefer* warp_bdf, int src) {
     __syncwarp();
     BwDefer& d = warp_bdf[src];
-    double f0, f1;
-    bw_by_summation_warp(d.a, d.eta, &f0, &f1);
+    double f0, f1, ceil = 0.0;
+    int n = 0;
+    if (d.kind == BW_DEFER_HARMONIC) {
+        bw_sample_harmonic_warp(a.lma->bw_cp_total, a.lma->bw_cp_nodes, d.a, d.eta, d.sv3, d.u, &n, &ceil, &f0, &f1);
+    } else {
+        bw_by_summation_warp(d.a, d.eta, &f0, &f1);
+    }
     __syncwarp();
     if ((int)lane_id() == src) {
         d.f0 = f0, d.f1 = f1;
+        d.n = n, d.s_ceil = ceil;
         d.pend = 2;
     }
     __syncwarp();
@@ -622,7 +670,7 @@ __device__ __forceinline__ void warp_serve(const WaveArgs& a, LpDefer* dfr, BwDe
         while (pending != 0u) {
             int src = __ffs(pending) - 1;
             pending &= pending - 1u;
-            bw_defer_serve(bdf - lane_id(), src);
+            bw_defer_serve(a, bdf - lane_id(), src);
         }
     }
 }
@@ -650,6 +698,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
             bdf = &s_bdf[threadIdx.x];
             bdf->pend = 0;
         }
+        stage_network(a);
     }
     bool have = lane_load(a, L);
     for (;;) {

@@ -2221,9 +2221,11 @@ static ptg_status lp_sample_points(ptg_ctx* c, size_t count, const double* a, co
 
 // One CP harmonic/s/azimuth/Stokes sample per point (cp_sample, or with
 // `warp` cp_sample_warp, each warp sampling its 32 points one after another).
-__global__ void k_cp_sample(unsigned long long m, int warp, const LmaTables* t, const double* a, const double* eta,
-                            unsigned long long seed, const unsigned long long* stream, unsigned step, double* out7,
-                            int* status) {
+__global__ void k_cp_sample(unsigned long long m, int warp, MlpParams mlp, const LmaTables* t, const double* a,
+                            const double* eta, unsigned long long seed, const unsigned long long* stream, unsigned step,
+                            double* out7, int* status) {
+    __shared__ __align__(16) float s_mlp[4][2 * MLP_H];
+    if (mlp.enabled && warp) mlp_stage(mlp, mlp_smem());
     unsigned long long base = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) & ~31ull;
     const unsigned lane = threadIdx.x & 31u;
     // warp: point base + q for q = 0..31, every lane together; otherwise
@@ -2237,7 +2239,13 @@ __global__ void k_cp_sample(unsigned long long m, int warp, const LmaTables* t, 
         double s = 0.0, th = 0.0;
         d3 sv = mk3(0.0, 0.0, 0.0);
         uint32_t rej = 0;
-        int st = warp ? cp_sample_warp(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej)
+        int st;
+        if (mlp.enabled)
+            st = warp ? cp_sample_learned_warp(*mlp_smem(), mlp.margin, nlc_view(*t), s_mlp[threadIdx.x >> 5], a[i],
+                                               eta[i], rng, &n, &s, &th, &sv, &rej)
+                      : cp_sample_learned_lane(mlp, nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
+        else
+            st = warp ? cp_sample_warp(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej)
                       : cp_sample(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
         if (!warp || lane == q) {
             status[i] = st;
@@ -2248,12 +2256,18 @@ __global__ void k_cp_sample(unsigned long long m, int warp, const LmaTables* t, 
 }
 
 static ptg_status cp_sample_points(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
-                                   const uint64_t* stream, uint32_t step, double* out7, int32_t* status, bool warp) {
+                                   const uint64_t* stream, uint32_t step, double* out7, int32_t* status, bool warp,
+                                   bool learned = false) {
     if (!c || !a || !eta || !stream || !out7 || !status) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     if (count == 0) return PTG_OK;
     if (!c->tables_loaded) {
         ptg_status st = ptg_load_tables(c, nullptr);
         if (st != PTG_OK) return st;
+    }
+    MlpParams mlp{};
+    if (learned) {
+        mlp = mlp_params(c);
+        if (!mlp.enabled) return set_err(PTG_ERR_INVALID_ARGUMENT, "no trained network in use (ptg_mlp_use)");
     }
     cudaSetDevice(c->device);
     std::vector<double> va(a, a + count), ve(eta, eta + count);
@@ -2262,7 +2276,7 @@ static ptg_status cp_sample_points(ptg_ctx* c, size_t count, const double* a, co
                                    {out7, 56 * count}, {status, 4 * count}},
                                [&](std::vector<void*>& d) {
                                    k_cp_sample<<<(unsigned)((count + 127) / 128), 128, 0, c->stream>>>(
-                                       count, warp ? 1 : 0, c->lma_dev, (double*)d[0], (double*)d[1], seed,
+                                       count, warp ? 1 : 0, mlp, c->lma_dev, (double*)d[0], (double*)d[1], seed,
                                        (unsigned long long*)d[2], step, (double*)d[3], (int*)d[4]);
                                });
 }
@@ -2275,6 +2289,11 @@ ptg_status ptg_cp_sample(ptg_ctx* c, size_t count, const double* a, const double
 ptg_status ptg_cp_sample_warp(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
                               const uint64_t* stream, uint32_t step, double* out7, int32_t* status) {
     return cp_sample_points(c, count, a, eta, seed, stream, step, out7, status, true);
+}
+
+ptg_status ptg_cp_sample_learned(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,
+                                 const uint64_t* stream, uint32_t step, int32_t warp, double* out7, int32_t* status) {
+    return cp_sample_points(c, count, a, eta, seed, stream, step, out7, status, warp != 0, true);
 }
 
 ptg_status ptg_lp_sample(ptg_ctx* c, size_t count, const double* a, const double* eta, uint64_t seed,

@@ -478,7 +478,9 @@ __device__ __forceinline__ void lma_push_field_free(d4 r0, d4 u0, double dt, d4*
 __device__ __forceinline__ void lma_push(const FieldParams& f, d4 r0, d4 u0, double rqm, double dt, int eqn,
                                          d4* r_out, d4* u_out, double* dt_out, double* dwork) {
     double dtau = dt / u0.t;
-    double q = rqm / (ELECTRON_CHARGE / ELECTRON_MASS);
+    // charge in units of e: exactly -1 or +1 for electrons and positrons
+    constexpr double RQM_E = ELECTRON_CHARGE / ELECTRON_MASS;
+    double q = rqm == RQM_E ? 1.0 : rqm == -RQM_E ? -1.0 : rqm / RQM_E;
     double scale = q * q;
     bool rr = eqn == EQN_LL;
     double kk = f.k;

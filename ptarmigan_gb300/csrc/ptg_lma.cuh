@@ -81,40 +81,39 @@ struct LpDefer {
 // lma_radiate's status for an emission left to the warp
 constexpr int LMA_DEFERRED = 101;
 
-// cp_sample (nonlinear_compton/cp/mod.rs:181-234) carried out by all 32
-// lanes of a converged warp for one emission whose a, eta and draws every
-// lane holds.  Every lane returns the same result, and it is cp_sample's on
-// the same draws: the harmonic comes from the same table inversion, the 32
-// points of the ceiling are spread over the lanes (the NaN-ignoring max
-// does not depend on the order), and the rejection trials are dealt out in
-// the order the serial sampler draws them, lane k evaluating the k-th of
-// each round of 32; the first accepted trial in draw order is taken, with
-// the draws as they stood after it.
-static __device__ __noinline__ int cp_sample_warp(const NlcTables& t, double a, double eta, Draws& rng, int* n_out,
-                                                  double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
+// cp_ceiling (nonlinear_compton/cp/mod.rs:42-75) with its 32 points spread
+// over the lanes of a converged warp; the NaN-ignoring maximum does not
+// depend on the order, so every lane returns cp_ceiling's value.
+__device__ __forceinline__ double cp_ceiling_warp(int n, double a, double eta) {
     const unsigned all = 0xffffffffu;
     const int lane = (int)(threadIdx.x & 31u);
-    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
-    int n = cp_invert(t, a, eta, rng.next());
-    if (n < 1) n = 1;
     double mx = fmax(-HUGE_VAL, cp_diff_partial_rate(n, a, eta, cp_ceiling_point(n, a, eta, lane)));
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(all, mx, o));
-    mx = 1.2 * mx;
+    return 1.2 * mx;
+}
+
+// cp_sample_v_under (v and u per trial, accepted when u <= f(v) / mx) by the
+// 32 lanes of a converged warp: the trials are dealt out in the order the
+// serial sampler draws them, lane k evaluating the k-th of each round of
+// 32; the first accepted trial in draw order is taken, with the draws as
+// they stood after it.  Every lane returns the serial sampler's result.
+static __device__ __noinline__ int cp_trials_warp(int n, double a, double eta, double mx, Draws& rng, double* v_out,
+                                                  uint32_t* rej) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
     Draws r = rng;
     for (int it0 = 0; it0 < r.cap; it0 += 32) {
-        // this lane's trial: it0 + lane, after the 2 lane draws of the trials before it
+        // this lane's trial: it0 + lane, after the 2 draws of each trial before it
         Draws my_r = r;
-        for (int k = 0; k < 2 * lane; ++k) my_r.next();
+        my_r.skip(2 * lane);
         double vv = my_r.next(), u = my_r.next();
         bool acc = it0 + lane < r.cap && u <= cp_diff_partial_rate(n, a, eta, vv) / mx;
         unsigned m = __ballot_sync(all, acc);
         if (m != 0u) {
             int win = __ffs(m) - 1;
-            double v = __shfl_sync(all, vv, win);
+            *v_out = __shfl_sync(all, vv, win);
             rng = shfl_draws(my_r, win);
             *rej += (uint32_t)(it0 + win);
-            cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
-            *n_out = n;
             return 0;
         }
         r = shfl_draws(my_r, 31);
@@ -122,6 +121,208 @@ static __device__ __noinline__ int cp_sample_warp(const NlcTables& t, double a, 
     rng = r;
     *rej += (uint32_t)r.cap;
     return 4;  // PTG_ERR_REJECTION_CAP
+}
+
+// cp_sample (nonlinear_compton/cp/mod.rs:181-234) carried out by all 32
+// lanes of a converged warp for one emission whose a, eta and draws every
+// lane holds.  Every lane returns the same result, and it is cp_sample's on
+// the same draws: the harmonic comes from the same table inversion, the 32
+// points of the ceiling are spread over the lanes (cp_ceiling_warp) and the
+// rejection trials are dealt out over them (cp_trials_warp).
+static __device__ __noinline__ int cp_sample_warp(const NlcTables& t, double a, double eta, Draws& rng, int* n_out,
+                                                  double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
+    if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    double mx = cp_ceiling_warp(n, a, eta);
+    double v = 0.0;
+    int st = cp_trials_warp(n, a, eta, mx, rng, &v, rej);
+    if (st != 0) return st;
+    cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    *n_out = n;
+    return 0;
+}
+
+// One hidden layer of the warp forward pass: this lane's units l and l + 32
+// from the 64 inputs `h` (the warp's scratch), in mlp_forward_lane's order.
+__device__ __forceinline__ void mlp_hidden_warp(const uint32_t (*w)[32], const float* b, const float* h, float* out) {
+    const int lane = (int)(threadIdx.x & 31u);
+    float z0 = b[lane], z1 = b[lane + 32];
+    const float4* h4 = reinterpret_cast<const float4*>(h);
+#pragma unroll 4
+    for (int q = 0; q < MLP_H / 4; ++q) {
+        float4 v = h4[q];
+        uint32_t w0 = w[4 * q][lane], w1 = w[4 * q + 1][lane], w2 = w[4 * q + 2][lane], w3 = w[4 * q + 3][lane];
+        z0 += bf16_lo(w0) * v.x;
+        z1 += bf16_hi(w0) * v.x;
+        z0 += bf16_lo(w1) * v.y;
+        z1 += bf16_hi(w1) * v.y;
+        z0 += bf16_lo(w2) * v.z;
+        z1 += bf16_hi(w2) * v.z;
+        z0 += bf16_lo(w3) * v.w;
+        z1 += bf16_hi(w3) * v.w;
+    }
+    out[lane] = silu(z0);
+    out[lane + 32] = silu(z1);
+}
+
+// mlp_forward_lane by the 32 lanes of a converged warp from the network
+// staged in shared memory (mlp_stage): lane l computes units l and l + 32
+// of each hidden layer (and unit l of the output for l < 16) with the same
+// products in the same order, so every lane returns the lane forward
+// pass's outputs bit for bit.  `sh` is the warp's scratch of 2 x 64 floats
+// in shared memory, 16-byte aligned.
+static __device__ __noinline__ void mlp_forward_warp(const MlpShared& net, const float x[MLP_IN], float out[MLP_OUT],
+                                                     float* sh) {
+    const int lane = (int)(threadIdx.x & 31u);
+    float* ha = sh;
+    float* hb = sh + MLP_H;
+    float z0 = net.b0[lane], z1 = net.b0[lane + 32];
+    for (int i = 0; i < MLP_IN; ++i) {
+        uint32_t w = net.w0[i][lane];
+        z0 += bf16_lo(w) * x[i];
+        z1 += bf16_hi(w) * x[i];
+    }
+    ha[lane] = silu(z0);
+    ha[lane + 32] = silu(z1);
+    __syncwarp();
+    mlp_hidden_warp(net.w1, net.b1, ha, hb);
+    __syncwarp();
+    mlp_hidden_warp(net.w2, net.b2, hb, ha);
+    __syncwarp();
+    if (lane < MLP_OUT) {
+        float z = net.b3[lane];
+        for (int i = 0; i < MLP_H; ++i) z += __bfloat162float(net.w3[i][lane]) * ha[i];
+        hb[lane] = z;
+    }
+    __syncwarp();
+    for (int q = 0; q < MLP_OUT; ++q) out[q] = hb[q];
+    __syncwarp();
+}
+
+// cp_sample_v_learned (ptg_mlp.cuh) by the 32 lanes of a converged warp,
+// with the serial sampler's draws and results: in one round lanes 0-15
+// evaluate the 16 trials under the learned envelope (trial k after the 3
+// draws of each trial before it) while lane 16 evaluates f(v*), which
+// scales the envelope; the first trial in draw order that accepts or finds
+// the envelope under the spectrum decides.  The hand-over to the
+// reference's sampler and the capped continuation run warp-wide too
+// (cp_ceiling_warp, cp_trials_warp, and rounds of 32 capped trials).
+static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OUT], float margin, int n, double a,
+                                                            double eta, Draws& rng, double* v_out, uint32_t* rej) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double v_star = (1.0 + sn) / (2.0 + sn);
+    // the trial round (and f(v*) on lane LEARNED_TRIALS)
+    Draws after_v = rng, after_u;
+    int k = 0;
+    double v = 0.0, f = 0.0, u = 0.0;
+    Envelope e;
+    float o_max = envelope_shape(o, &e);
+    if (lane < LEARNED_TRIALS) {
+        after_v.skip(3 * lane);
+        v = envelope_draw(e, after_v, &k);
+        after_u = after_v;
+        u = after_u.next();
+        f = cp_diff_partial_rate(n, a, eta, v);
+    } else {
+        after_u = after_v;
+        if (lane == LEARNED_TRIALS) f = cp_diff_partial_rate(n, a, eta, v_star);
+    }
+    double f_star = __shfl_sync(all, f, LEARNED_TRIALS);
+    if (!envelope_scale(&e, o_max, margin, f_star)) {
+        // unusable envelope: the reference's sampler from the first draw
+        return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej);
+    }
+    double g = e.scale * (double)e.w[k];
+    bool viol = lane < LEARNED_TRIALS && f > g;
+    bool acc = lane < LEARNED_TRIALS && !viol && u * g < f;
+    unsigned m = __ballot_sync(all, viol || acc);
+    if (m != 0u) {
+        int j = __ffs(m) - 1;
+        *rej += (uint32_t)j;
+        if (__shfl_sync(all, (int)viol, j)) {
+            // the envelope is under the spectrum: the reference's sampler takes over
+            rng = shfl_draws(after_v, j);
+            return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej);
+        }
+        rng = shfl_draws(after_u, j);
+        *v_out = __shfl_sync(all, v, j);
+        return 0;
+    }
+    rng = shfl_draws(after_u, LEARNED_TRIALS - 1);
+    *rej += LEARNED_TRIALS;
+    // cp_sample_v_capped: rejection under min(envelope, ceiling)
+    double ceil = cp_ceiling_warp(n, a, eta);
+    unsigned capped = envelope_cap(&e, ceil);
+    Draws r = rng;
+    for (int it0 = 0; it0 < r.cap; it0 += 32) {
+        Draws my_r = r;
+        my_r.skip(3 * lane);
+        int kb;
+        double vb = envelope_draw(e, my_r, &kb);
+        double fb = cp_diff_partial_rate(n, a, eta, vb);
+        double gb = e.scale * (double)e.w[kb];
+        int dec = 0;  // 1: accepted under the cap; 2: envelope under the spectrum; 3: accepted
+        if (fb > gb) {
+            dec = (capped & (1u << kb)) ? 1 : 2;
+        } else if (my_r.next() * gb < fb) {
+            dec = 3;
+        }
+        unsigned mb = __ballot_sync(all, it0 + lane < r.cap && dec != 0);
+        if (mb != 0u) {
+            int j = __ffs(mb) - 1;
+            rng = shfl_draws(my_r, j);
+            *rej += (uint32_t)(it0 + j);
+            if (__shfl_sync(all, dec, j) == 2) return cp_trials_warp(n, a, eta, ceil, rng, v_out, rej);
+            *v_out = __shfl_sync(all, vb, j);
+            return 0;
+        }
+        r = shfl_draws(my_r, 31);
+    }
+    rng = r;
+    *rej += (uint32_t)r.cap;
+    return 4;  // PTG_ERR_REJECTION_CAP
+}
+
+// The learned CP emission sampler: the harmonic by the table inversion
+// (the same draw as cp_sample), v from the learned envelope with the exact
+// accept/reject against the spectrum (ptg_mlp.cuh), then cp_finish.  On
+// this lane alone.
+static __device__ __noinline__ int cp_sample_learned_lane(const MlpParams& mlp, const NlcTables& t, double a, double eta,
+                                                          Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                                          d3* sv_out, uint32_t* rej) {
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    float x[MLP_IN], o[MLP_OUT];
+    mlp_features(a, eta, n, x);
+    mlp_forward_lane(mlp, x, o);
+    LearnedCounts lc{0, 0, 0, 0};
+    double v = 0.0;
+    int st = cp_sample_v_learned(o, mlp.margin, n, a, eta, rng, &v, rej, &lc);
+    if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    *n_out = n;
+    return st;
+}
+
+// The same by the 32 lanes of a converged warp, with the same draws and
+// results, from the network staged in shared memory (mlp_stage); `sh` is
+// the warp's scratch.
+static __device__ __noinline__ int cp_sample_learned_warp(const MlpShared& net, float margin, const NlcTables& t,
+                                                          float* sh, double a, double eta, Draws& rng, int* n_out,
+                                                          double* s_out, double* theta_out, d3* sv_out,
+                                                          uint32_t* rej) {
+    int n = cp_invert(t, a, eta, rng.next());
+    if (n < 1) n = 1;
+    float x[MLP_IN], o[MLP_OUT];
+    mlp_features(a, eta, n, x);
+    mlp_forward_warp(net, x, o, sh);
+    double v = 0.0;
+    int st = cp_sample_v_learned_warp(o, margin, n, a, eta, rng, &v, rej);
+    if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    *n_out = n;
+    return st;
 }
 
 // plane_wave.rs:251-282 / focused_laser.rs:260-281 with
@@ -147,22 +348,24 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
     double kk = SPEED_OF_LIGHT * COMPTON_TIME * f.k * chirp * width;
     d4 kappa = d4{kk, 0.0, 0.0, kk};
     double a2 = dot4(u, u) - 1.0;
-    double aq = a2 >= 0.0 ? sqrt(a2) : 0.0;
     double eta = dot4(kappa, u);
-    double dphi = dt * eta / (COMPTON_TIME * u.t);
-    NlcTables nt = nlc_view(t);
     // the event draw, then the FP32 bound on the probability: a draw well
-    // above it is a step without an emission (see PROB32_MARGIN)
+    // above it is a step without an emission (see PROB32_MARGIN); ln a is
+    // taken in FP32 from a^2 (within 1e-7 of ln of the FP64 a)
     double u_event = rng.next();
     if (!classical) {
         float r32;
-        bool in32 = f.circular ? rate32_cp(t.nlc_cp_rate32, aq, eta, &r32)
-                               : rate32_lp(t.nlc_lp_rate32, aq * SQRT_2, eta, &r32);
+        float ln_a = 0.5f * logf((float)a2);
+        bool in32 = f.circular ? rate32_cp(t.nlc_cp_rate32, ln_a, eta, &r32)
+                               : rate32_lp(t.nlc_lp_rate32, ln_a + 0.34657359f /* ln sqrt 2 */, eta, &r32);
         if (in32) {
             float p32 = (float)(ALPHA_FINE / COMPTON_TIME) * r32 * ((float)dt / (float)u.t);
             if (u_event > (double)p32 * (1.0 + PROB32_MARGIN)) return 0;
         }
     }
+    double aq = a2 >= 0.0 ? sqrt(a2) : 0.0;
+    double dphi = dt * eta / (COMPTON_TIME * u.t);
+    NlcTables nt = nlc_view(t);
     double rate;
     bool ok;
     if (f.circular)
@@ -176,20 +379,9 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
         double s, cphi;
         d3 sv;
         int st;
-        if (f.circular && !classical && mlp.enabled) {
-            // the learned proposal for v (ptg_mlp.cuh): same harmonic
-            // draw, exact accept/reject against the spectrum
-            n = cp_invert(nt, aq, eta, rng.next());
-            if (n < 1) n = 1;
-            float x[3], o[MLP_OUT];
-            mlp_features(aq, eta, n, x);
-            mlp_forward_lane(mlp, x, o);
-            LearnedCounts lc{0, 0, 0, 0};
-            double v = 0.0;
-            st = cp_sample_v_learned(o, mlp.margin, n, aq, eta, rng, &v, rej, &lc);
-            if (st == 0) cp_finish(n, aq, eta, v, rng, &s, &cphi, &sv);
-        } else if (f.circular && !classical && dfr != nullptr) {
-            // the reference's CP sampler, carried out by the whole warp
+        if (f.circular && !classical && dfr != nullptr) {
+            // the CP sampler (the reference's, or the learned proposal when
+            // it is on), carried out by the whole warp
             if (dfr->pend == 2) {
                 n = dfr->n, s = dfr->s, cphi = dfr->theta, sv = dfr->sv, st = dfr->status;
                 *rej += dfr->rej;
@@ -202,6 +394,8 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
                 dfr->pend = 1;
                 return LMA_DEFERRED;
             }
+        } else if (f.circular && !classical && mlp.enabled) {
+            st = cp_sample_learned_lane(mlp, nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
         } else if (f.circular)
             st = classical ? cp_classical_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej)
                            : cp_sample(nt, aq, eta, rng, &n, &s, &cphi, &sv, rej);
@@ -304,8 +498,9 @@ static __device__ __noinline__ int lma_pair_create(const FieldParams& f, const L
     if (rng.next() < *prob * ri) {
         int n;
         d4 q;
-        int st = f.circular ? bw_generate(t.bw_cp_total, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej)
+        int st = f.circular ? bw_generate(t.bw_cp_total, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej, bdf)
                             : lp_bw_generate(t, dbw, ell, pol, kappa, a, f.pol_angle, rng, &n, &q, rej);
+        if (st == BW_DEFERRED) return LMA_DEFERRED;  // the step repeats once the warp has sampled the harmonic
         if (st != 0) return st;
         *ue = d4{ell.t + n * kappa.t - q.t, ell.x + n * kappa.x - q.x, ell.y + n * kappa.y - q.y, ell.z + n * kappa.z - q.z};
         *up = q;

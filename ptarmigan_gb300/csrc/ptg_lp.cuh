@@ -506,12 +506,13 @@ __device__ __forceinline__ bool lp_rate(const NlcTables& t, double a, double eta
 
 // lp_rate's table branch in FP32, where it certainly applies (peak
 // amplitude a, strictly inside the table); false elsewhere.  T32: the LP
-// ln-rate table in FP32.
-__device__ __forceinline__ bool rate32_lp(const float* T32, double a, double eta, float* out) {
-    if (T32 == nullptr || !(a > 0.0 && eta > 0.0)) return false;
+// ln-rate table in FP32; ln_a: ln a in FP32 (NaN or -inf where a is not
+// positive).
+__device__ __forceinline__ bool rate32_lp(const float* T32, float ln_a, double eta, float* out) {
+    if (T32 == nullptr || !(eta > 0.0)) return false;
     const float MIN0 = (float)PTG_NLC_LP_MIN_0, MIN1 = (float)PTG_NLC_LP_MIN_1;
     const float I0 = (float)(1.0 / PTG_NLC_LP_STEP_0), I1 = (float)(1.0 / PTG_NLC_LP_STEP_1);
-    float ta = (logf((float)a) - MIN0) * I0, te = (logf((float)eta) - MIN1) * I1;
+    float ta = (ln_a - MIN0) * I0, te = (logf((float)eta) - MIN1) * I1;
     if (!(ta > 1e-3f && te > 1e-3f && ta < 59.99f && te < 66.99f)) return false;
     int ia = (int)ta, ie = (int)te;
     float da = ta - (float)ia, de = te - (float)ie;

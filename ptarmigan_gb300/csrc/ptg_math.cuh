@@ -132,6 +132,23 @@ struct Draws {
         pos += 2;
         return (double)m * (1.0 / 9007199254740992.0);
     }
+    // The state after d more draws (d >= 0), with at most one block
+    // generated.  Word index of the next draw: 4 (block - 1) + pos.
+    __device__ __forceinline__ void skip(int d) {
+        uint32_t at = 4u * block - 4u + (uint32_t)pos + 2u * (uint32_t)d;
+        uint32_t b = at >> 2;
+        if ((at & 3u) == 0u) {
+            block = b;  // the next draw starts block b
+            pos = 4;
+        } else if (b + 1u != block) {
+            uint4 o = philox(make_uint4(step, b, s_lo, s_hi), k0, k1);
+            w[0] = o.x, w[1] = o.y, w[2] = o.z, w[3] = o.w;
+            block = b + 1u;
+            pos = 2;
+        } else {
+            pos = 2;  // the second draw of the block already in w
+        }
+    }
 };
 
 // ---------------------------------------------------------------- pwmci --

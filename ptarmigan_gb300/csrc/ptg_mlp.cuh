@@ -78,6 +78,51 @@ static __device__ __noinline__ void mlp_forward_lane(const MlpParams& m, const f
     }
 }
 
+// The network staged in a block's shared memory for the warp forward pass
+// (mlp_forward_warp): hidden layers input-major, with units l and l + 32
+// of input i packed in one word (low and high BF16), so that for each input
+// the 32 lanes read 32 consecutive words; the output layer input-major.
+struct MlpShared {
+    uint32_t w0[MLP_IN][32];
+    uint32_t w1[MLP_H][32];
+    uint32_t w2[MLP_H][32];
+    __nv_bfloat16 w3[MLP_H][MLP_OUT];
+    float b0[MLP_H], b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+};
+
+__device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 v) { return (uint32_t)__bfloat16_as_ushort(v); }
+// the two BF16 of a packed word as FP32 (exact, as __bfloat162float)
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// The block's staged network (one per block, shared by every call site).
+__device__ __forceinline__ MlpShared* mlp_smem() {
+    __shared__ MlpShared s_net;
+    return &s_net;
+}
+
+// Copies the network into `s`: every thread of the block, then a barrier.
+__device__ __forceinline__ void mlp_stage(const MlpParams& m, MlpShared* s) {
+    for (int t = threadIdx.x; t < MLP_H * 32; t += blockDim.x) {
+        int i = t >> 5, l = t & 31;
+        if (i < MLP_IN)
+            s->w0[i][l] = bf16_bits(m.w0[l * MLP_IN_PAD + i]) | (bf16_bits(m.w0[(l + 32) * MLP_IN_PAD + i]) << 16);
+        s->w1[i][l] = bf16_bits(m.w1[l * MLP_H + i]) | (bf16_bits(m.w1[(l + 32) * MLP_H + i]) << 16);
+        s->w2[i][l] = bf16_bits(m.w2[l * MLP_H + i]) | (bf16_bits(m.w2[(l + 32) * MLP_H + i]) << 16);
+    }
+    for (int t = threadIdx.x; t < MLP_H * MLP_OUT; t += blockDim.x) {
+        int i = t / MLP_OUT, o = t % MLP_OUT;
+        s->w3[i][o] = m.w3[o * MLP_H + i];
+    }
+    for (int t = threadIdx.x; t < MLP_H; t += blockDim.x) {
+        s->b0[t] = m.b0[t];
+        s->b1[t] = m.b1[t];
+        s->b2[t] = m.b2[t];
+        if (t < MLP_OUT) s->b3[t] = m.b3[t];
+    }
+    __syncthreads();
+}
+
 // Parameter vector (FP32 master copy, gradients, Adam moments).
 enum : int {
     P_W0 = 0,
@@ -121,9 +166,9 @@ struct Envelope {
     float total;
 };
 
-// From the network's outputs o (ln heights relative to f(v*)) and f(v*).
-// Returns false when the envelope is unusable.
-__device__ __forceinline__ bool envelope_from(const float* o, float margin, double f_star, Envelope* e) {
+// The envelope's shape from the network's outputs o (ln heights relative
+// to f(v*)): relative heights w and their total.  Returns max o.
+__device__ __forceinline__ float envelope_shape(const float* o, Envelope* e) {
     float o_max = -HUGE_VALF;
     for (int q = 0; q < MLP_OUT; ++q) o_max = fmaxf(o_max, o[q]);
     e->total = 0.0f;
@@ -131,8 +176,18 @@ __device__ __forceinline__ bool envelope_from(const float* o, float margin, doub
         e->w[q] = __expf(o[q] - o_max);
         e->total += e->w[q];
     }
+    return o_max;
+}
+
+// Its scale from f(v*).  Returns false when the envelope is unusable.
+__device__ __forceinline__ bool envelope_scale(Envelope* e, float o_max, float margin, double f_star) {
     e->scale = f_star * exp((double)o_max + (double)margin);
     return f_star > 0.0 && isfinite(e->scale) && e->total > 0.0f;
+}
+
+// Both, from o and f(v*).
+__device__ __forceinline__ bool envelope_from(const float* o, float margin, double f_star, Envelope* e) {
+    return envelope_scale(e, envelope_shape(o, e), margin, f_star);
 }
 
 // The envelope capped at the flat ceiling c: heights min(scale * w, c);

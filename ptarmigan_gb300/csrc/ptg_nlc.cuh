@@ -216,12 +216,14 @@ __device__ __forceinline__ bool cp_rate(const NlcTables& t, double a, double eta
 // cp_rate's table branch in FP32, where it certainly applies: a and eta
 // strictly inside the table (away from its edges by more than the FP32
 // rounding of their logarithms).  Returns false elsewhere (the caller then
-// evaluates cp_rate).  T32: the CP ln-rate table in FP32.
-__device__ __forceinline__ bool rate32_cp(const float* T32, double a, double eta, float* out) {
-    if (T32 == nullptr || !(a < 19.99 && eta < 1.999 && a > 0.0 && eta > 0.0)) return false;
+// evaluates cp_rate).  T32: the CP ln-rate table in FP32; ln_a: ln a in
+// FP32 (NaN or -inf where a is not positive).
+__device__ __forceinline__ bool rate32_cp(const float* T32, float ln_a, double eta, float* out) {
+    const float LN_A_MAX = 2.99523f;  // ln 19.99
+    if (T32 == nullptr || !(ln_a < LN_A_MAX && eta < 1.999 && eta > 0.0)) return false;
     const float MIN0 = (float)PTG_NLC_CP_MIN_0, MIN1 = (float)PTG_NLC_CP_MIN_1;
     const float I0 = (float)(1.0 / PTG_NLC_CP_STEP_0), I1 = (float)(1.0 / PTG_NLC_CP_STEP_1);
-    float ta = (logf((float)a) - MIN0) * I0, te = (logf((float)eta) - MIN1) * I1;
+    float ta = (ln_a - MIN0) * I0, te = (logf((float)eta) - MIN1) * I1;
     if (!(ta > 1e-3f && te > 1e-3f && ta < 59.99f && te < 68.99f)) return false;
     int ia = (int)ta, ie = (int)te;
     float da = ta - (float)ia, de = te - (float)ie;

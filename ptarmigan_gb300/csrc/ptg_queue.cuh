@@ -172,6 +172,7 @@ __device__ __forceinline__ void queue_load(const WaveArgs& a, Lane& L, unsigned 
     L.coll = s.coll[i];
     L.step = 0;
     L.decayed = false;
+    L.drift_cached = false;
 }
 
 // A loaded ticket: false if it holds no particle to run (a phantom slot or
@@ -326,6 +327,7 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             dfr = &s_dfr[threadIdx.x];
             dfr->pend = 0;
         }
+        stage_network(a);
     }
     unsigned long long t = 0, t_end = 0, ticket = 0, wait_from = 0;
     for (;;) {

@@ -23,6 +23,7 @@ _EXPORTS = [
     "ptg_load_tables", "ptg_collide_batch", "ptg_collide_batch_device", "ptg_particles_free",
     "ptg_laser_timestep", "ptg_laser_initial_z", "ptg_context_stream", "ptg_context_set_limits", "ptg_pair_rate_increase", "ptg_eval_fields", "ptg_push_steps",
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample", "ptg_lp_sample_warp", "ptg_cp_sample", "ptg_cp_sample_warp",
+    "ptg_cp_sample_learned",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
     "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram", "ptg_particle_sums",
@@ -99,6 +100,9 @@ def load(path=None):
         getattr(L, name).restype = st
         getattr(L, name).argtypes = [ctxp, C.c_size_t, DP, DP, C.c_uint64, C.POINTER(C.c_uint64), C.c_uint32, DP,
                                      C.POINTER(C.c_int32)]
+    L.ptg_cp_sample_learned.restype = st
+    L.ptg_cp_sample_learned.argtypes = [ctxp, C.c_size_t, DP, DP, C.c_uint64, C.POINTER(C.c_uint64), C.c_uint32,
+                                        C.c_int32, DP, C.POINTER(C.c_int32)]
     U64P = C.POINTER(C.c_uint64)
     L.ptg_collide_multi.restype = st
     L.ptg_collide_multi.argtypes = [ctxp, C.c_size_t, C.POINTER(abi.Collision), C.POINTER(abi.CollideOptions),
@@ -513,17 +517,23 @@ class Engine:
                        _dp(out), status.ctypes.data_as(C.POINTER(C.c_int32))))
         return out, status
 
-    def cp_sample(self, a, eta, seed, streams, step, warp=False):
-        """CP LMA samples (the reference's sampler): ([m, 7] = n, s, theta, 1,
-        xi1, xi2, xi3; [m] status).  warp=True draws them with the
+    def cp_sample(self, a, eta, seed, streams, step, warp=False, learned=False):
+        """CP LMA samples: ([m, 7] = n, s, theta, 1, xi1, xi2, xi3; [m]
+        status), with the reference's sampler or (learned=True) the learned
+        proposal in use (mlp_use).  warp=True draws them with the
         warp-cooperative sampler."""
         a, eta = _f64(a, (-1,)), _f64(eta, (-1,))
         streams = np.ascontiguousarray(streams, dtype=np.uint64)
         out = np.zeros((len(a), 7))
         status = np.zeros(len(a), dtype=np.int32)
-        fn = self.L.ptg_cp_sample_warp if warp else self.L.ptg_cp_sample
-        self._check(fn(self._h, len(a), _dp(a), _dp(eta), seed, streams.ctypes.data_as(C.POINTER(C.c_uint64)), step,
-                       _dp(out), status.ctypes.data_as(C.POINTER(C.c_int32))))
+        sp = streams.ctypes.data_as(C.POINTER(C.c_uint64))
+        stp = status.ctypes.data_as(C.POINTER(C.c_int32))
+        if learned:
+            self._check(self.L.ptg_cp_sample_learned(self._h, len(a), _dp(a), _dp(eta), seed, sp, step, int(warp),
+                                                     _dp(out), stp))
+        else:
+            fn = self.L.ptg_cp_sample_warp if warp else self.L.ptg_cp_sample
+            self._check(fn(self._h, len(a), _dp(a), _dp(eta), seed, sp, step, _dp(out), stp))
         return out, status
 
     def lcfa_pair_t(self, chi):

@@ -160,3 +160,46 @@ def test_learned_collide_cp_shower_statistics(eng, trained):
     for k in range(4):
         assert abs(s0[:, k].mean() - s1[:, k].mean()) < 5.0 * np.sqrt(
             (s0[:, k].var() + s1[:, k].var()) / len(e0)) + 1e-12
+
+
+def _learned_points(m, seed):
+    rng = np.random.default_rng(seed)
+    a = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m))
+    eta = np.exp(rng.uniform(np.log(2e-3), np.log(1.0), m))
+    return a, eta, np.arange(m, dtype=np.uint64) * 7919 + 11
+
+
+@pytest.mark.parametrize("network", ["trained", "under", "over"])
+def test_learned_warp_sampler_matches_lane_sampler(eng, trained, network):
+    """The collision kernels sample CP emissions with the learned proposal
+    on the whole warp (network units, the 16 trials and f(v*) spread over
+    the lanes); the multi-collision queue kernel samples them on the
+    emitting lane.  Both draw the same numbers and return the same samples
+    bit for bit, for a trained network, for an envelope under the spectrum
+    (every emission handed over to the reference's sampler) and for one far
+    above it (16 rejections, then the capped continuation)."""
+    e = eng
+    own = None
+    if network != "trained":
+        own = type(eng)()
+        own.load_tables()
+        p = init(13)
+        p[OFF["b3"][0]:OFF["b3"][0] + 16] = -5.0 if network == "under" else 9.0
+        own.mlp_params(set_to=p)
+        e = own
+    try:
+        e.mlp_use(True, margin=0.25)
+        a, eta, streams = _learned_points(4096, 3)
+        out_l, st_l = e.cp_sample(a, eta, 17, streams, 5, learned=True)
+        out_w, st_w = e.cp_sample(a, eta, 17, streams, 5, warp=True, learned=True)
+        assert np.array_equal(st_l, st_w)
+        assert np.count_nonzero(st_l == 0) >= 0.99 * len(a), np.unique(st_l, return_counts=True)
+        assert np.array_equal(out_l, out_w)
+        # the same distribution as the reference's sampler on other draws
+        out_r, st_r = e.cp_sample(a, eta, 18, streams, 5)
+        ok = (st_l == 0) & (st_r == 0)
+        assert _ks(out_l[ok, 1], out_r[ok, 1]) < _ks_bound(ok.sum(), ok.sum())
+    finally:
+        e.mlp_use(False)
+        if own is not None:
+            own.close()
