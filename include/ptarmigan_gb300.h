@@ -448,6 +448,11 @@ ptg_status ptg_mlp_train(ptg_ctx* ctx, const ptg_mlp_train_cfg* cfg, ptg_mlp_tra
 ptg_status ptg_mlp_grad(ptg_ctx* ctx, const float* samples, size_t n, float tau, float* grad, float* loss);
 ptg_status ptg_mlp_infer(ptg_ctx* ctx, const float* x, size_t n, float* out);
 ptg_status ptg_mlp_use(ptg_ctx* ctx, int32_t enabled, float margin);
+/* The collision kernels propose v with the network only at harmonics n >=
+ * `n` and use the reference's sampler below (both exact); *previous (may be
+ * NULL) receives the setting in force before the call; n < 0 only queries.
+ * The sampler benchmark always uses the network. */
+ptg_status ptg_mlp_min_harmonic(ptg_ctx* ctx, int32_t n, int32_t* previous);
 ptg_status ptg_sampler_bench(ptg_ctx* ctx, const ptg_sampler_bench_cfg* cfg, double* v_plain, double* v_learned,
                              const ptg_sampler_bench_detail* detail, ptg_sampler_bench_stats* stats);
 

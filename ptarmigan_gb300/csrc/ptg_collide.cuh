@@ -81,6 +81,11 @@ struct WaveArgs {
     // slot order; the results do not depend on it (streams are fixed per
     // particle), only how coherently the lanes of a warp step
     const unsigned long long* order;
+    // nonzero: each warp takes 32 consecutive particles of that order and
+    // the next 32 once all of them are done (warp_load), so that its lanes
+    // stay at nearly the same laser phase; zero: each lane takes the next
+    // particle as soon as its own is done (lane_load)
+    int warp_batch;
 };
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
@@ -534,8 +539,8 @@ __device__ __forceinline__ void photon_step(const WaveArgs& a, Lane& L, uint32_t
     L.r = r;
 }
 
-__device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
-    unsigned long long k = atomicAdd(&a.c->next, 1ull);
+// Loads particle k of the wave (in its processing order) into the lane.
+__device__ __forceinline__ bool lane_load_at(const WaveArgs& a, Lane& L, unsigned long long k) {
     unsigned long long i = a.lo + k;
     if (i >= a.hi) return false;
     if (a.order) i = a.lo + a.order[k];
@@ -559,6 +564,19 @@ __device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
     L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
     return true;
+}
+
+// The next particle of the wave for this lane alone.
+__device__ __forceinline__ bool lane_load(const WaveArgs& a, Lane& L) {
+    return lane_load_at(a, L, atomicAdd(&a.c->next, 1ull));
+}
+
+// The next 32 particles of the wave for the 32 lanes of a converged warp.
+__device__ __forceinline__ bool warp_load(const WaveArgs& a, Lane& L) {
+    unsigned long long base = 0;
+    if (lane_id() == 0) base = atomicAdd(&a.c->next, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return lane_load_at(a, L, base + lane_id());
 }
 
 __device__ __forceinline__ void lane_store(const WaveArgs& a, Lane& L) {
@@ -604,8 +622,8 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
     if (!a.f.circular)
         st = lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
     else if (a.mlp.enabled)
-        st = cp_sample_learned_warp(*mlp_smem(), a.mlp.margin, nlc_view(*a.lma), s_mlp[threadIdx.x >> 5], d.a, d.eta,
-                                    rng, &n, &s, &theta, &sv, &rej);
+        st = cp_sample_learned_warp(*mlp_smem(), a.mlp, nlc_view(*a.lma), s_mlp[threadIdx.x >> 5], d.a, d.eta, rng, &n,
+                                    &s, &theta, &sv, &rej);
     else
         st = cp_sample_warp(nlc_view(*a.lma), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
     __syncwarp();
@@ -700,7 +718,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
         }
         stage_network(a);
     }
-    bool have = lane_load(a, L);
+    bool have = a.warp_batch ? warp_load(a, L) : lane_load(a, L);
     for (;;) {
         if (have) {
             bool done;
@@ -742,10 +760,17 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                 // a decayed photon leaves the output, or becomes an intermediate
                 if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
                 lane_store(a, L);
-                have = lane_load(a, L);
+                have = a.warp_batch ? false : lane_load(a, L);
             }
         }
-        if (LMA && (dfr != nullptr || bdf != nullptr)) {
+        if (a.warp_batch) {
+            // the warp steps together until all 32 particles are done
+            if (LMA && (dfr != nullptr || bdf != nullptr)) warp_serve(a, dfr, bdf, have);
+            if (!__any_sync(0xffffffffu, have)) {
+                have = warp_load(a, L);
+                if (!__any_sync(0xffffffffu, have)) break;
+            }
+        } else if (LMA && (dfr != nullptr || bdf != nullptr)) {
             warp_serve(a, dfr, bdf, have);
             if (!__any_sync(0xffffffffu, have)) break;
         } else if (!have) {

@@ -107,6 +107,9 @@ struct ptg_ctx {
     void* mlp_packed = nullptr;  // weights in fragment order for inference
     int mlp_step = 0;
     bool mlp_ready = false, mlp_enabled = false;
+    int mlp_min_harmonic = MLP_MIN_HARMONIC_DEFAULT;
+    // ordered waves: warps take 32 particles at a time (WaveArgs::warp_batch)
+    bool warp_batch = true;
     float mlp_margin = 0.25f;
     cudaGraphExec_t q_graph = nullptr;
     std::string q_graph_key;
@@ -1287,6 +1290,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
             a.lo = lo;
             a.hi = hi;
             a.order = order_wave(c, WaveKeys{c->s, nullptr}, lo, hi) ? c->d_order : nullptr;
+            a.warp_batch = (a.order != nullptr && c->warp_batch) ? 1 : 0;
             ordered += a.order ? 1u : 0u;
             CUDA_TRY(cudaMemsetAsync(&c->counters->next, 0, 8, c->stream));
             CUDA_TRY(cudaEventRecord(c->ev_wa, c->stream));
@@ -1816,8 +1820,6 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
         q.base.f = c->h_coll[0].f;
         q.base.seed = c->h_coll[0].seed;
         q.base.id_base = c->h_coll[0].id_base;
-        // primaries in order of laser phase, from the input rows (before the
-        // captured sequence loads them)
     }
     // primaries in order of laser phase within each collision, from the
     // input rows (before the captured sequence loads them)
@@ -1833,6 +1835,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     q.stats = c->d_cstats;
     q.n_coll = (int)n_coll;
     q.chunk = qc.chunk;
+    q.warp_batch = (variant == 2 && q.base.order != nullptr && c->warp_batch) ? 1 : 0;
     // longest wait any lane may legitimately see: the drain of the batch's
     // last showers; generous, but bounded
     q.wait_ns = (unsigned long long)(20.0e9 + 2.0e3 * (double)n);
@@ -2241,8 +2244,8 @@ __global__ void k_cp_sample(unsigned long long m, int warp, MlpParams mlp, const
         uint32_t rej = 0;
         int st;
         if (mlp.enabled)
-            st = warp ? cp_sample_learned_warp(*mlp_smem(), mlp.margin, nlc_view(*t), s_mlp[threadIdx.x >> 5], a[i],
-                                               eta[i], rng, &n, &s, &th, &sv, &rej)
+            st = warp ? cp_sample_learned_warp(*mlp_smem(), mlp, nlc_view(*t), s_mlp[threadIdx.x >> 5], a[i], eta[i],
+                                               rng, &n, &s, &th, &sv, &rej)
                       : cp_sample_learned_lane(mlp, nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej);
         else
             st = warp ? cp_sample_warp(nlc_view(*t), a[i], eta[i], rng, &n, &s, &th, &sv, &rej)
@@ -2939,6 +2942,7 @@ static MlpParams mlp_params(ptg_ctx* c) {
     p.b0 = c->mlp_p + P_B0, p.b1 = c->mlp_p + P_B1, p.b2 = c->mlp_p + P_B2, p.b3 = c->mlp_p + P_B3;
     p.margin = c->mlp_margin;
     p.enabled = 1;
+    p.min_harmonic = c->mlp_min_harmonic;
     return p;
 }
 
@@ -3158,6 +3162,14 @@ ptg_status ptg_mlp_use(ptg_ctx* c, int32_t enabled, float margin) {
     if (!(margin >= 0.0f && margin < 10.0f)) return set_err(PTG_ERR_INVALID_ARGUMENT, "margin out of range");
     c->mlp_enabled = enabled != 0;
     c->mlp_margin = margin;
+    return PTG_OK;
+}
+
+ptg_status ptg_mlp_min_harmonic(ptg_ctx* c, int32_t n, int32_t* previous) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (previous) *previous = c->mlp_min_harmonic;
+    if (n < 0) return PTG_OK;  // query only
+    c->mlp_min_harmonic = n;
     return PTG_OK;
 }
 

@@ -214,22 +214,21 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
     const int lane = (int)(threadIdx.x & 31u);
     double sn = 2.0 * n * eta / (1.0 + a * a);
     double v_star = (1.0 + sn) / (2.0 + sn);
-    // the trial round (and f(v*) on lane LEARNED_TRIALS)
-    Draws after_v = rng, after_u;
+    // the trial round: lanes 0-15 draw their trial, the others take v*;
+    // the spectrum is then evaluated at one call site by every lane (one
+    // pass of the warp), f(v*) read from lane LEARNED_TRIALS
+    Draws after_v = rng;
     int k = 0;
-    double v = 0.0, f = 0.0, u = 0.0;
+    double v = v_star, u = 0.0;
     Envelope e;
     float o_max = envelope_shape(o, &e);
     if (lane < LEARNED_TRIALS) {
         after_v.skip(3 * lane);
         v = envelope_draw(e, after_v, &k);
-        after_u = after_v;
-        u = after_u.next();
-        f = cp_diff_partial_rate(n, a, eta, v);
-    } else {
-        after_u = after_v;
-        if (lane == LEARNED_TRIALS) f = cp_diff_partial_rate(n, a, eta, v_star);
     }
+    Draws after_u = after_v;
+    if (lane < LEARNED_TRIALS) u = after_u.next();
+    double f = cp_diff_partial_rate(n, a, eta, v);
     double f_star = __shfl_sync(all, f, LEARNED_TRIALS);
     if (!envelope_scale(&e, o_max, margin, f_star)) {
         // unusable envelope: the reference's sampler from the first draw
@@ -288,19 +287,26 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
 
 // The learned CP emission sampler: the harmonic by the table inversion
 // (the same draw as cp_sample), v from the learned envelope with the exact
-// accept/reject against the spectrum (ptg_mlp.cuh), then cp_finish.  On
-// this lane alone.
+// accept/reject against the spectrum (ptg_mlp.cuh) from harmonic
+// mlp.min_harmonic up and with the reference's sampler below it, then
+// cp_finish.  On this lane alone.
 static __device__ __noinline__ int cp_sample_learned_lane(const MlpParams& mlp, const NlcTables& t, double a, double eta,
                                                           Draws& rng, int* n_out, double* s_out, double* theta_out,
                                                           d3* sv_out, uint32_t* rej) {
     int n = cp_invert(t, a, eta, rng.next());
     if (n < 1) n = 1;
-    float x[MLP_IN], o[MLP_OUT];
-    mlp_features(a, eta, n, x);
-    mlp_forward_lane(mlp, x, o);
-    LearnedCounts lc{0, 0, 0, 0};
     double v = 0.0;
-    int st = cp_sample_v_learned(o, mlp.margin, n, a, eta, rng, &v, rej, &lc);
+    int st;
+    if (n < mlp.min_harmonic) {
+        // a low harmonic: the reference's ceiling costs less than the network
+        st = cp_sample_v(n, a, eta, rng, &v, rej);
+    } else {
+        float x[MLP_IN], o[MLP_OUT];
+        mlp_features(a, eta, n, x);
+        mlp_forward_lane(mlp, x, o);
+        LearnedCounts lc{0, 0, 0, 0};
+        st = cp_sample_v_learned(o, mlp.margin, n, a, eta, rng, &v, rej, &lc);
+    }
     if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return st;
@@ -309,17 +315,22 @@ static __device__ __noinline__ int cp_sample_learned_lane(const MlpParams& mlp, 
 // The same by the 32 lanes of a converged warp, with the same draws and
 // results, from the network staged in shared memory (mlp_stage); `sh` is
 // the warp's scratch.
-static __device__ __noinline__ int cp_sample_learned_warp(const MlpShared& net, float margin, const NlcTables& t,
-                                                          float* sh, double a, double eta, Draws& rng, int* n_out,
-                                                          double* s_out, double* theta_out, d3* sv_out,
-                                                          uint32_t* rej) {
+static __device__ __noinline__ int cp_sample_learned_warp(const MlpShared& net, const MlpParams& mlp,
+                                                          const NlcTables& t, float* sh, double a, double eta,
+                                                          Draws& rng, int* n_out, double* s_out, double* theta_out,
+                                                          d3* sv_out, uint32_t* rej) {
     int n = cp_invert(t, a, eta, rng.next());
     if (n < 1) n = 1;
-    float x[MLP_IN], o[MLP_OUT];
-    mlp_features(a, eta, n, x);
-    mlp_forward_warp(net, x, o, sh);
     double v = 0.0;
-    int st = cp_sample_v_learned_warp(o, margin, n, a, eta, rng, &v, rej);
+    int st;
+    if (n < mlp.min_harmonic) {
+        st = cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, &v, rej);
+    } else {
+        float x[MLP_IN], o[MLP_OUT];
+        mlp_features(a, eta, n, x);
+        mlp_forward_warp(net, x, o, sh);
+        st = cp_sample_v_learned_warp(o, mlp.margin, n, a, eta, rng, &v, rej);
+    }
     if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return st;

@@ -31,21 +31,25 @@ struct MlpParams {
     const float *b0, *b1, *b2, *b3;          // [64], [64], [64], [16]
     float margin;                            // ln of the envelope's safety factor
     int enabled;
+    int min_harmonic;  // the collision kernels propose v with the network from this harmonic up
 };
 
 // Inputs, each scaled to about [-1, 1] over a in [0.05, 20], eta in
 // [1e-3, 2], n in [1, ~5e4]: ln a, ln eta, ln n, ln s_n (s_n = 2 n eta /
 // (1 + a^2), which maps v to the Bessel argument), v*, and
-// ln(n / (1 + a^2)^{3/2}), which sets how sharply J_n peaks in v.
+// ln(n / (1 + a^2)^{3/2}), which sets how sharply J_n peaks in v.  In
+// FP32 (the network is BF16): the same function makes the training
+// samples' inputs and the samplers'.
 __host__ __device__ __forceinline__ void mlp_features(double a, double eta, int n, float x[MLP_IN]) {
-    double ln_a = log(a), ln_n = log((double)n), ln_1a2 = log1p(a * a);
-    double sn = 2.0 * n * eta / (1.0 + a * a);
-    x[0] = (float)(ln_a / 3.0);
-    x[1] = (float)((log(eta) + 3.1) / 3.8);
-    x[2] = (float)(ln_n / 6.0 - 1.0);
-    x[3] = (float)(log(sn) / 6.0);
-    x[4] = (float)(2.0 * (1.0 + sn) / (2.0 + sn) - 2.0);
-    x[5] = (float)((ln_n - 1.5 * ln_1a2) / 6.0);
+    float af = (float)a, ef = (float)eta, nf = (float)n;
+    float ln_a = logf(af), ln_n = logf(nf), ln_1a2 = log1pf(af * af);
+    float sn = 2.0f * nf * ef / (1.0f + af * af);
+    x[0] = ln_a * (1.0f / 3.0f);
+    x[1] = (logf(ef) + 3.1f) * (1.0f / 3.8f);
+    x[2] = ln_n * (1.0f / 6.0f) - 1.0f;
+    x[3] = logf(sn) * (1.0f / 6.0f);
+    x[4] = 2.0f * (1.0f + sn) / (2.0f + sn) - 2.0f;
+    x[5] = (ln_n - 1.5f * ln_1a2) * (1.0f / 6.0f);
 }
 
 // SiLU with the fast FP32 exponential and division (the network only
@@ -158,6 +162,10 @@ struct LearnedCounts {
 // returns v distributed as f, so the cap costs nothing in exactness; it
 // bounds the work where the learned envelope is loose.
 constexpr int LEARNED_TRIALS = 16;
+
+// Lowest harmonic at which the collision kernels propose v with the network
+// (ptg_mlp_min_harmonic); below it the reference's ceiling costs less.
+constexpr int MLP_MIN_HARMONIC_DEFAULT = 1;
 
 // The learned envelope of one emission: bin heights scale * w[k], w <= 1.
 struct Envelope {

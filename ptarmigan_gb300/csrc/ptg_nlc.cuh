@@ -63,7 +63,9 @@ static __device__ __noinline__ void triple_j(int n, double x, double* a, double*
     }
 }
 
-// special_functions/bessel.rs:178-199: uniform asymptotic expansion (n >= 1000)
+// special_functions/bessel.rs:178-199: uniform asymptotic expansion (n >= 1000).
+// The fractional powers as cbrt(x)^2, sqrt(sqrt(x)) and w sqrt(w) (the
+// reference's powf to a few ulp; NaN where powf is NaN).
 static __device__ __noinline__ double j_asymptotic(int n, double x) {
     double m = (double)n;
     double z = x / m;
@@ -71,17 +73,19 @@ static __device__ __noinline__ double j_asymptotic(int n, double x) {
     if (z < 1.0) {
         double r = sqrt(1.0 - z * z);
         double tmp = log((1.0 + r) / z) - r;
-        zeta = pow(1.5 * tmp, 2.0 / 3.0);
+        zeta = tmp >= 0.0 ? pow_two_thirds(1.5 * tmp) : __longlong_as_double(0x7ff8000000000000LL);
     } else {
         double tmp = sqrt(z * z - 1.0) - acos(1.0 / z);
-        zeta = -pow(1.5 * tmp, 2.0 / 3.0);
+        zeta = tmp >= 0.0 ? -pow_two_thirds(1.5 * tmp) : __longlong_as_double(0x7ff8000000000000LL);
     }
-    double arg = pow(m, 2.0 / 3.0) * zeta;
+    double m13 = cbrt(m);
+    double arg = (m13 * m13) * zeta;
     double ai = arg >= 0.0 ? airy_ai(arg) : 0.0;
     double aip = arg >= 0.0 ? airy_ai_prime(arg) : 0.0;
-    double pre = 4.0 * zeta / (1.0 - z * z);
-    double bk = 5.0 / (48.0 * zeta * zeta) - (2.0 + 3.0 * z * z) / (24.0 * sqrt(zeta) * pow(1.0 - z * z, 1.5));
-    return pow(pre, 0.25) * (ai / cbrt(m) - aip * bk / pow(m, 5.0 / 3.0));
+    double w = 1.0 - z * z;
+    double pre = 4.0 * zeta / w;
+    double bk = 5.0 / (48.0 * zeta * zeta) - (2.0 + 3.0 * z * z) / (24.0 * sqrt(zeta) * (w * sqrt(w)));
+    return sqrt(sqrt(pre)) * (ai / m13 - aip * bk / (m * (m13 * m13)));
 }
 
 // bessel.rs:26-34

@@ -38,6 +38,10 @@ struct QueueArgs {
     int n_coll;
     int chunk;                 // tickets taken per grab
     unsigned long long wait_ns;  // bound on any single wait for a slot
+    // single-collision kernel: a warp takes tickets only when none of its
+    // lanes holds a particle or a ticket, so that its lanes start their
+    // particles together (consecutive tickets: nearby laser phases)
+    int warp_batch;
 };
 
 
@@ -333,7 +337,8 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
     for (;;) {
         if (__all_sync(FULL, finished)) break;
         bool leptons = __any_sync(FULL, have && L.species != SP_PHOTON);
-        if (!have && !finished) {
+        bool may_grab = !q.warp_batch || __all_sync(FULL, (!have && !holding) || finished);
+        if (!have && !finished && (holding || t != t_end || may_grab)) {
             if (!holding) {
                 if (t == t_end) {
                     t = grab_tickets(a.c, (unsigned)q.chunk);

@@ -26,6 +26,7 @@ _EXPORTS = [
     "ptg_cp_sample_learned",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
+    "ptg_mlp_min_harmonic",
     "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram", "ptg_particle_sums",
 ]
 
@@ -130,6 +131,8 @@ def load(path=None):
     L.ptg_mlp_infer.argtypes = [ctxp, FP, C.c_size_t, FP]
     L.ptg_mlp_use.restype = st
     L.ptg_mlp_use.argtypes = [ctxp, C.c_int32, C.c_float]
+    L.ptg_mlp_min_harmonic.restype = st
+    L.ptg_mlp_min_harmonic.argtypes = [ctxp, C.c_int32, C.POINTER(C.c_int32)]
     L.ptg_particle_sums.restype = st
     L.ptg_particle_sums.argtypes = [ctxp, C.POINTER(abi.Particles), C.POINTER(abi.StatsSpec),
                                     C.POINTER(abi.StatsSums)]
@@ -437,6 +440,13 @@ class Engine:
 
     def mlp_use(self, enabled=True, margin=0.25):
         self._check(self.L.ptg_mlp_use(self._h, int(enabled), margin))
+
+    def mlp_min_harmonic(self, n=-1):
+        """Sets the lowest harmonic at which the collision kernels use the
+        network (n >= 0) and returns the previous setting."""
+        prev = C.c_int32()
+        self._check(self.L.ptg_mlp_min_harmonic(self._h, int(n), C.byref(prev)))
+        return prev.value
 
     def sampler_bench(self, n, seed=3, a_range=(0.05, 20.0), eta_range=(1e-3, 2.0), margin=0.25, want_v=True,
                       detail=False):

@@ -169,26 +169,31 @@ def _learned_points(m, seed):
     return a, eta, np.arange(m, dtype=np.uint64) * 7919 + 11
 
 
-@pytest.mark.parametrize("network", ["trained", "under", "over"])
+@pytest.mark.parametrize("network", ["trained", "trained_from_8", "under", "over"])
 def test_learned_warp_sampler_matches_lane_sampler(eng, trained, network):
     """The collision kernels sample CP emissions with the learned proposal
     on the whole warp (network units, the 16 trials and f(v*) spread over
     the lanes); the multi-collision queue kernel samples them on the
     emitting lane.  Both draw the same numbers and return the same samples
-    bit for bit, for a trained network, for an envelope under the spectrum
+    bit for bit, for a trained network (used at every harmonic, or from
+    harmonic 8 up with the reference's sampler below), for an envelope under
+    the spectrum
     (every emission handed over to the reference's sampler) and for one far
     above it (16 rejections, then the capped continuation)."""
     e = eng
     own = None
-    if network != "trained":
+    if not network.startswith("trained"):
         own = type(eng)()
         own.load_tables()
         p = init(13)
         p[OFF["b3"][0]:OFF["b3"][0] + 16] = -5.0 if network == "under" else 9.0
         own.mlp_params(set_to=p)
         e = own
+    prev = None
     try:
         e.mlp_use(True, margin=0.25)
+        # the network from harmonic 8 up, the reference's sampler below
+        prev = e.mlp_min_harmonic(8 if network == "trained_from_8" else 1)
         a, eta, streams = _learned_points(4096, 3)
         out_l, st_l = e.cp_sample(a, eta, 17, streams, 5, learned=True)
         out_w, st_w = e.cp_sample(a, eta, 17, streams, 5, warp=True, learned=True)
@@ -201,5 +206,8 @@ def test_learned_warp_sampler_matches_lane_sampler(eng, trained, network):
         assert _ks(out_l[ok, 1], out_r[ok, 1]) < _ks_bound(ok.sum(), ok.sum())
     finally:
         e.mlp_use(False)
-        if own is not None:
+        if own is None:
+            if prev is not None:
+                e.mlp_min_harmonic(prev)
+        else:
             own.close()
