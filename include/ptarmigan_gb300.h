@@ -579,9 +579,29 @@ ptg_status ptg_particle_sums(ptg_ctx* ctx, const ptg_particles* particles, const
  * LMA rates at the laser's rms amplitude (then at least 1). */
 ptg_status ptg_pair_rate_increase(ptg_ctx* ctx, const ptg_laser_desc* laser, double gamma, double* ratio);
 
+/* The LMA emission step's per-step FP32 rate beside the reference's FP64
+ * rate (nonlinear_compton/cp/mod.rs:160-176, lp/mod.rs:459-553) at n points
+ * (a_sqd = u.u - 1, eta): out3[3 i] the FP32 rate the step compares its
+ * draw with (NaN where it does not apply and the FP64 rate decides),
+ * out3[3 i + 1] the FP64 rate, out3[3 i + 2] 1 where the FP64 rate is in
+ * table.  circular: the CP rate at the rms amplitude, else the LP rate at
+ * the peak amplitude.  No reference counterpart (a check of the bound). */
+ptg_status ptg_emission_rate_bound(ptg_ctx* ctx, size_t n, int32_t circular, const double* a_sqd, const double* eta,
+                                   double* out3);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): the ceiling of the
  * FP64-pipe-bound collision kernels. */
 ptg_status ptg_fp64_peak(ptg_ctx* ctx, double* tflops);
+
+/* One launch of a kernel (k_fp64_fn<op>) in which every thread of one block
+ * per SM calls one FP64 library function `iters` times; profiled, its FP64
+ * instruction counts (less PTG_FN_NONE's) give the function's executed cost
+ * per call, the weights of the collision loop's operation counts. */
+typedef enum {
+    PTG_FN_NONE = 0, PTG_FN_EXP = 1, PTG_FN_LOG = 2, PTG_FN_DIV = 3, PTG_FN_SQRT = 4, PTG_FN_CBRT = 5,
+    PTG_FN_SINCOS = 6, PTG_FN_POW = 7, PTG_FN_ATAN2 = 8, PTG_FN_HYPOT = 9, PTG_FN_LOG1P = 10, PTG_FN_ACOS = 11
+} ptg_fp64_function;
+ptg_status ptg_fp64_function_kernel(ptg_ctx* ctx, int32_t op, int32_t iters);
 
 /* Table maintenance: regenerates the CP nonlinear-Compton harmonic CDF
  * table on the device.  The reference ships it as

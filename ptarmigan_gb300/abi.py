@@ -459,3 +459,9 @@ def collide_options(**kw):
             raise KeyError(k)
         setattr(o, k, v)
     return o
+
+
+# ptg_fp64_function: the FP64 library functions whose executed cost
+# ptg_fp64_function_kernel exposes to a profiler
+FP64_FUNCTIONS = {"none": 0, "exp": 1, "log": 2, "div": 3, "sqrt": 4, "cbrt": 5, "sincos": 6, "pow": 7, "atan2": 8,
+                  "hypot": 9, "log1p": 10, "acos": 11}

@@ -818,6 +818,37 @@ __global__ void k_cp_cdf_log(const double* cdf, double* out, unsigned long long 
     out[2 * i + 1] = cp_cdf_log_node(cdf[2 * i + 1]);
 }
 
+// K(eta) of the emission rate a^2 K(eta) below the rate tables' smallest
+// amplitude: circular polarisation, nonlinear_compton/cp/mod.rs:160-176
+// (a the rms amplitude); linear, the linear rate of lp/mod.rs:459-553 for
+// eta > 1e-3 (a the peak amplitude).  Upper bounds per cell of ln eta: the
+// largest of 65 values across the cell (K increases with eta), raised by
+// 2^-8 and rounded up to FP32.
+static double small_a_factor(bool circular, double eta) {
+    double q = 1.0 + 2.0 * eta;
+    if (circular)
+        return (2.0 + 8.0 * eta + 9.0 * eta * eta + eta * eta * eta) / (2.0 * eta * q * q) -
+               (2.0 + 2.0 * eta - eta * eta) * std::log(q) / (4.0 * eta * eta);
+    return (0.5 + 4.0 / eta - 0.5 / (q * q) + (1.0 - 2.0 / eta - 2.0 / (eta * eta)) * std::log(q)) / 8.0;
+}
+
+static std::vector<float> small_a_bounds(bool circular) {
+    std::vector<float> out(SMALL_A_CELLS);
+    const double w = (SMALL_A_LN_ETA1 - SMALL_A_LN_ETA0) / SMALL_A_CELLS;
+    for (int j = 0; j < SMALL_A_CELLS; ++j) {
+        double mx = 0.0;
+        for (int k = 0; k <= 64; ++k) {
+            double le = SMALL_A_LN_ETA0 + (j + k / 64.0) * w;
+            mx = std::max(mx, small_a_factor(circular, std::exp(le)));
+        }
+        double b = mx * (1.0 + 1.0 / 256.0);
+        float f = (float)b;
+        if ((double)f < b) f = std::nextafter(f, INFINITY);
+        out[j] = f;
+    }
+    return out;
+}
+
 ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
     if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
     std::string d = dir ? dir : default_table_dir();
@@ -897,6 +928,18 @@ ptg_status ptg_load_tables(ptg_ctx* c, const char* dir) {
         e = cudaMemcpy(q, nodes.data(), 8 * nodes.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
         host.bw_cp_nodes = (const double*)q;
+    }
+    // upper bounds of the small-amplitude rate factors K(eta) per cell of
+    // ln eta (the per-step FP32 bound below the rate tables)
+    for (int pol = 0; pol < 2; ++pol) {
+        std::vector<float> k32 = small_a_bounds(pol == 0);
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, 4 * k32.size());
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        bufs.push_back(q);
+        e = cudaMemcpy(q, k32.data(), 4 * k32.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(PTG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        (pol == 0 ? host.nlc_cp_small32 : host.nlc_lp_small32) = (const float*)q;
     }
     host.nlc_cp_cdf_log = nullptr;
     if (host.nlc_cp_cdf) {
@@ -2366,6 +2409,42 @@ __global__ void k_pair_rate_increase(int lcfa, int circular, double gamma, doubl
     out[1] = (ok && ok_q) ? 0.0 : 2.0;  // PTG_ERR_OUT_OF_TABLE
 }
 
+// The emission step's FP32 rate (emission_rate32) beside the FP64 rate
+// (cp_rate / lp_rate) at a^2 = u.u - 1 and eta: out[3 i] the FP32 rate (or
+// NaN where it does not apply), out[3 i + 1] the FP64 rate, out[3 i + 2] 1
+// if the FP64 rate is in table, else 0.
+__global__ void k_emission_rate_pair(unsigned long long n, int circular, const LmaTables* t, const double* a2,
+                                     const double* eta, double* out) {
+    unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r32 = 0.0f;
+    bool in32 = emission_rate32(*t, circular != 0, a2[i], eta[i], &r32);
+    double aq = a2[i] >= 0.0 ? sqrt(a2[i]) : 0.0;
+    double rate = 0.0;
+    NlcTables nt = nlc_view(*t);
+    bool ok = circular ? cp_rate(nt, aq, eta[i], &rate) : lp_rate(nt, aq * SQRT_2, eta[i], &rate);
+    out[3 * i] = in32 ? (double)r32 : __longlong_as_double(0x7ff8000000000000LL);
+    out[3 * i + 1] = rate;
+    out[3 * i + 2] = ok ? 1.0 : 0.0;
+}
+
+ptg_status ptg_emission_rate_bound(ptg_ctx* c, size_t n, int32_t circular, const double* a_sqd, const double* eta,
+                                   double* out3) {
+    if (!c || (n && (!a_sqd || !eta || !out3))) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n == 0) return PTG_OK;
+    if (!c->tables_loaded) {
+        ptg_status st = ptg_load_tables(c, nullptr);
+        if (st != PTG_OK) return st;
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    std::vector<double> va(a_sqd, a_sqd + n), ve(eta, eta + n);
+    return with_device_buffers(c, {{va.data(), 8 * n}, {ve.data(), 8 * n}, {out3, 24 * n}},
+                               [&](std::vector<void*>& d) {
+                                   k_emission_rate_pair<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(
+                                       n, circular ? 1 : 0, c->lma_dev, (double*)d[0], (double*)d[1], (double*)d[2]);
+                               });
+}
+
 ptg_status ptg_pair_rate_increase(ptg_ctx* c, const ptg_laser_desc* laser, double gamma, double* ratio) {
     if (!c || !ratio) return set_err(PTG_ERR_INVALID_ARGUMENT, "NULL argument");
     ptg_status st = check_laser(laser);
@@ -2894,6 +2973,74 @@ ptg_status ptg_build_beam(ptg_ctx* c, const ptg_beam_desc* d, uint64_t n, uint64
     cleanup();
     if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
     if (nerr) return set_err(PTG_ERR_REJECTION_CAP, std::to_string(nerr) + " primaries could not be sampled");
+    return PTG_OK;
+}
+
+// One FP64 library function per kernel, called `iters` times by every
+// thread on inputs inside all the functions' domains, so that a profiler's
+// FP64 instruction counts per launch, less those of PTG_FN_NONE, divided by
+// the calls, give each function's executed cost on this device.
+template <int OP>
+__device__ __forceinline__ double fp64_fn(double x) {
+    switch (OP) {
+        case PTG_FN_EXP: return exp(-x);
+        case PTG_FN_LOG: return log(x);
+        case PTG_FN_DIV: return 1.0 / x;
+        case PTG_FN_SQRT: return sqrt(x);
+        case PTG_FN_CBRT: return cbrt(x);
+        case PTG_FN_SINCOS: {
+            double s, c;
+            sincos(x, &s, &c);
+            return s + c;
+        }
+        case PTG_FN_POW: return pow(x, 1.0 / 6.0);
+        case PTG_FN_ATAN2: return atan2(x, 1.3);
+        case PTG_FN_HYPOT: return hypot(x, 1.3);
+        case PTG_FN_LOG1P: return log1p(x);
+        case PTG_FN_ACOS: return acos(x);
+        default: return x;
+    }
+}
+
+template <int OP>
+__global__ void k_fp64_fn(int iters, double x0, double* sink) {
+    double x = x0 + 1e-9 * (double)(blockIdx.x * blockDim.x + threadIdx.x);
+    double acc = 0.0;
+    for (int i = 0; i < iters; ++i) {
+        acc += fp64_fn<OP>(x);
+        x += 1e-12;
+    }
+    if (acc == 12345.678) *sink = acc;  // keeps the loop; never true
+}
+
+ptg_status ptg_fp64_function_kernel(ptg_ctx* c, int32_t op, int32_t iters) {
+    if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (iters < 1 || iters > (1 << 20)) return set_err(PTG_ERR_INVALID_ARGUMENT, "iters out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    double* sink = nullptr;
+    CUDA_TRY(cudaMalloc(&sink, 8));
+    const int block = 256, grid = c->num_sms;
+    const double x0 = 0.37;
+    switch (op) {
+        case PTG_FN_NONE: k_fp64_fn<PTG_FN_NONE><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_EXP: k_fp64_fn<PTG_FN_EXP><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_LOG: k_fp64_fn<PTG_FN_LOG><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_DIV: k_fp64_fn<PTG_FN_DIV><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_SQRT: k_fp64_fn<PTG_FN_SQRT><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_CBRT: k_fp64_fn<PTG_FN_CBRT><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_SINCOS: k_fp64_fn<PTG_FN_SINCOS><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_POW: k_fp64_fn<PTG_FN_POW><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_ATAN2: k_fp64_fn<PTG_FN_ATAN2><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_HYPOT: k_fp64_fn<PTG_FN_HYPOT><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_LOG1P: k_fp64_fn<PTG_FN_LOG1P><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        case PTG_FN_ACOS: k_fp64_fn<PTG_FN_ACOS><<<grid, block, 0, c->stream>>>(iters, x0, sink); break;
+        default:
+            cudaFree(sink);
+            return set_err(PTG_ERR_INVALID_ARGUMENT, "unknown function");
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(sink);
+    if (e != cudaSuccess) return set_err(PTG_ERR_CUDA, cudaGetErrorString(e));
     return PTG_OK;
 }
 

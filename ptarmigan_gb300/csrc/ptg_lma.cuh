@@ -36,14 +36,45 @@ struct LmaTables {
     // the CP Breit-Wheeler total-rate table's node positions in a (74) and
     // eta (121), computed once at load
     const double* bw_cp_nodes;
+    // below the rate tables' smallest amplitude the emission rate is
+    // a^2 K(eta) (cp: nonlinear_compton/cp/mod.rs:160-176; lp: the linear
+    // rate of lp/mod.rs:459-553); upper bounds of K over SMALL_A_CELLS cells
+    // of ln eta, in FP32, built at load (small_a_bounds)
+    const float* nlc_cp_small32;    // [SMALL_A_CELLS]
+    const float* nlc_lp_small32;    // [SMALL_A_CELLS]
 };
+
+// The cells of the small-amplitude bound tables: ln eta from ln 1e-3 (where
+// both rates' formulas change) to ln 2.
+constexpr int SMALL_A_CELLS = 512;
+constexpr double SMALL_A_LN_ETA0 = -6.907755278982137;
+constexpr double SMALL_A_LN_ETA1 = 0.6931471805599453;
+
+// An upper bound on the emission rate where the amplitude lies below the
+// rate table (ln a below ln_a_min by more than FP32 rounding): (float)a^2
+// times the bound on K for eta's cell.  False where it does not certainly
+// apply (then the FP64 rate is evaluated).  `a2` is the square of the
+// amplitude the rate formula takes.
+__device__ __forceinline__ bool rate32_small_a(const float* K32, float ln_a, float ln_a_min, double a2, double eta,
+                                               float* out) {
+    if (K32 == nullptr || !(ln_a < ln_a_min - 1e-5f) || !(a2 > 0.0) || !(eta > 0.0)) return false;
+    const float L0 = (float)SMALL_A_LN_ETA0;
+    const float INV = (float)(SMALL_A_CELLS / (SMALL_A_LN_ETA1 - SMALL_A_LN_ETA0));
+    float x = (logf((float)eta) - L0) * INV;
+    if (!(x > 1e-3f && x < (float)SMALL_A_CELLS - 1e-3f)) return false;
+    *out = (float)a2 * K32[(int)x];
+    return true;
+}
 
 // The per-step emission probability is first evaluated in FP32 from the
 // FP32 rate tables (rate32_cp / rate32_lp).  Its relative error is below
 // 2e-5: the logarithms of a and eta are within about 1e-6 and so the table
 // coordinates within 2.1e-5 of a cell; the tables' ln-rate changes by at
 // most 0.23 per cell and has magnitude at most 16, so the interpolated
-// ln-rate is within 1.5e-5; expf and the products add under 1e-6.  A draw
+// ln-rate is within 1.5e-5; expf and the products add under 1e-6.  Below
+// the tables' smallest amplitude an upper bound takes its place
+// (rate32_small_a: at least the rate, within 2^-8 plus K's variation over
+// a cell of it, and within a few ulp of FP32 rounding).  A draw
 // above the FP32 probability by more than 2^-10 of it is a step without an
 // emission whatever the FP64 probability is; every other draw is decided
 // against the FP64 probability, as the reference decides it.  The decisions
@@ -97,8 +128,14 @@ __device__ __forceinline__ double cp_ceiling_warp(int n, double a, double eta) {
 // serial sampler draws them, lane k evaluating the k-th of each round of
 // 32; the first accepted trial in draw order is taken, with the draws as
 // they stood after it.  Every lane returns the serial sampler's result.
+__device__ __forceinline__ Jtrip shfl_jtrip(const Jtrip& t, int src) {
+    const unsigned all = 0xffffffffu;
+    return Jtrip{__shfl_sync(all, t.m, src), __shfl_sync(all, t.j, src), __shfl_sync(all, t.p, src)};
+}
+
+// `jt`, when not NULL, receives the accepted trial's Bessel triple.
 static __device__ __noinline__ int cp_trials_warp(int n, double a, double eta, double mx, Draws& rng, double* v_out,
-                                                  uint32_t* rej) {
+                                                  uint32_t* rej, Jtrip* jt = nullptr) {
     const unsigned all = 0xffffffffu;
     const int lane = (int)(threadIdx.x & 31u);
     Draws r = rng;
@@ -107,11 +144,14 @@ static __device__ __noinline__ int cp_trials_warp(int n, double a, double eta, d
         Draws my_r = r;
         my_r.skip(2 * lane);
         double vv = my_r.next(), u = my_r.next();
-        bool acc = it0 + lane < r.cap && u <= cp_diff_partial_rate(n, a, eta, vv) / mx;
+        Jtrip tj{0.0, 0.0, 0.0};
+        bool acc = it0 + lane < r.cap && u <= cp_diff_partial_rate_j(n, a, eta, vv, &tj) / mx;
         unsigned m = __ballot_sync(all, acc);
         if (m != 0u) {
             int win = __ffs(m) - 1;
             *v_out = __shfl_sync(all, vv, win);
+            Jtrip w = shfl_jtrip(tj, win);
+            if (jt) *jt = w;
             rng = shfl_draws(my_r, win);
             *rej += (uint32_t)(it0 + win);
             return 0;
@@ -123,6 +163,39 @@ static __device__ __noinline__ int cp_trials_warp(int n, double a, double eta, d
     return 4;  // PTG_ERR_REJECTION_CAP
 }
 
+// cp_invert (nonlinear_compton/cp/tables/mod.rs:37-121) by a converged
+// warp: the (up to) four grid corners are inverted on lanes 0-3 at once
+// and combined in cp_invert's order and expression, so every lane returns
+// cp_invert's harmonic.
+static __device__ __noinline__ int cp_invert_warp(const NlcTables& t, double a, double eta, double frac) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
+    const double MIN0 = PTG_NLC_CP_MIN_0, MIN1 = PTG_NLC_CP_MIN_1, S0 = PTG_NLC_CP_STEP_0, S1 = PTG_NLC_CP_STEP_1;
+    double la = log(a), le = log(eta);
+    if (la <= MIN0) return 1;
+    int ix = (int)((la - MIN0) / S0);
+    double dx = (la - MIN0) / S0 - ix;
+    bool edge = le <= MIN1;
+    int iy = edge ? 0 : (int)((le - MIN1) / S1);
+    double dy = edge ? 0.0 : (le - MIN1) / S1 - iy;
+    // lane c < 4: corner (ix + (c & 1), iy + (c >> 1)); on the eta edge only
+    // the two corners of row ix, ix + 1
+    double v = 0.0;
+    if (lane < (edge ? 2 : 4)) {
+        size_t row = edge ? (size_t)(ix + lane) : (size_t)(61 * (iy + (lane >> 1)) + ix + (lane & 1));
+        v = cp_cdf_corner(t.cp_cdf + row * 64, t.cp_cdf_log ? t.cp_cdf_log + row * 64 : nullptr, frac);
+    }
+    double c0 = __shfl_sync(all, v, 0), c1 = __shfl_sync(all, v, 1);
+    double n;
+    if (edge) {
+        n = c0 * (1.0 - dx) + c1 * dx;
+    } else {
+        double c2 = __shfl_sync(all, v, 2), c3 = __shfl_sync(all, v, 3);
+        n = c0 * ((1.0 - dx) * (1.0 - dy)) + c1 * (dx * (1.0 - dy)) + c2 * ((1.0 - dx) * dy) + c3 * (dx * dy);
+    }
+    return (int)ceil(n);
+}
+
 // cp_sample (nonlinear_compton/cp/mod.rs:181-234) carried out by all 32
 // lanes of a converged warp for one emission whose a, eta and draws every
 // lane holds.  Every lane returns the same result, and it is cp_sample's on
@@ -132,13 +205,14 @@ static __device__ __noinline__ int cp_trials_warp(int n, double a, double eta, d
 static __device__ __noinline__ int cp_sample_warp(const NlcTables& t, double a, double eta, Draws& rng, int* n_out,
                                                   double* s_out, double* theta_out, d3* sv_out, uint32_t* rej) {
     if (t.cp_cdf == nullptr) return 8;  // PTG_ERR_TABLES
-    int n = cp_invert(t, a, eta, rng.next());
+    int n = cp_invert_warp(t, a, eta, rng.next());
     if (n < 1) n = 1;
     double mx = cp_ceiling_warp(n, a, eta);
     double v = 0.0;
-    int st = cp_trials_warp(n, a, eta, mx, rng, &v, rej);
+    Jtrip jt;
+    int st = cp_trials_warp(n, a, eta, mx, rng, &v, rej, &jt);
     if (st != 0) return st;
-    cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    cp_finish_j(n, a, eta, v, jt, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return 0;
 }
@@ -209,7 +283,8 @@ static __device__ __noinline__ void mlp_forward_warp(const MlpShared& net, const
 // reference's sampler and the capped continuation run warp-wide too
 // (cp_ceiling_warp, cp_trials_warp, and rounds of 32 capped trials).
 static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OUT], float margin, int n, double a,
-                                                            double eta, Draws& rng, double* v_out, uint32_t* rej) {
+                                                            double eta, Draws& rng, double* v_out, uint32_t* rej,
+                                                            Jtrip* jt) {
     const unsigned all = 0xffffffffu;
     const int lane = (int)(threadIdx.x & 31u);
     double sn = 2.0 * n * eta / (1.0 + a * a);
@@ -228,11 +303,12 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
     }
     Draws after_u = after_v;
     if (lane < LEARNED_TRIALS) u = after_u.next();
-    double f = cp_diff_partial_rate(n, a, eta, v);
+    Jtrip tj;
+    double f = cp_diff_partial_rate_j(n, a, eta, v, &tj);
     double f_star = __shfl_sync(all, f, LEARNED_TRIALS);
     if (!envelope_scale(&e, o_max, margin, f_star)) {
         // unusable envelope: the reference's sampler from the first draw
-        return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej);
+        return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej, jt);
     }
     double g = e.scale * (double)e.w[k];
     bool viol = lane < LEARNED_TRIALS && f > g;
@@ -244,10 +320,11 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
         if (__shfl_sync(all, (int)viol, j)) {
             // the envelope is under the spectrum: the reference's sampler takes over
             rng = shfl_draws(after_v, j);
-            return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej);
+            return cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, v_out, rej, jt);
         }
         rng = shfl_draws(after_u, j);
         *v_out = __shfl_sync(all, v, j);
+        *jt = shfl_jtrip(tj, j);
         return 0;
     }
     rng = shfl_draws(after_u, LEARNED_TRIALS - 1);
@@ -261,7 +338,8 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
         my_r.skip(3 * lane);
         int kb;
         double vb = envelope_draw(e, my_r, &kb);
-        double fb = cp_diff_partial_rate(n, a, eta, vb);
+        Jtrip tb;
+        double fb = cp_diff_partial_rate_j(n, a, eta, vb, &tb);
         double gb = e.scale * (double)e.w[kb];
         int dec = 0;  // 1: accepted under the cap; 2: envelope under the spectrum; 3: accepted
         if (fb > gb) {
@@ -274,8 +352,9 @@ static __device__ __noinline__ int cp_sample_v_learned_warp(const float o[MLP_OU
             int j = __ffs(mb) - 1;
             rng = shfl_draws(my_r, j);
             *rej += (uint32_t)(it0 + j);
-            if (__shfl_sync(all, dec, j) == 2) return cp_trials_warp(n, a, eta, ceil, rng, v_out, rej);
+            if (__shfl_sync(all, dec, j) == 2) return cp_trials_warp(n, a, eta, ceil, rng, v_out, rej, jt);
             *v_out = __shfl_sync(all, vb, j);
+            *jt = shfl_jtrip(tb, j);
             return 0;
         }
         r = shfl_draws(my_r, 31);
@@ -296,18 +375,19 @@ static __device__ __noinline__ int cp_sample_learned_lane(const MlpParams& mlp, 
     int n = cp_invert(t, a, eta, rng.next());
     if (n < 1) n = 1;
     double v = 0.0;
+    Jtrip jt;
     int st;
     if (n < mlp.min_harmonic) {
         // a low harmonic: the reference's ceiling costs less than the network
-        st = cp_sample_v(n, a, eta, rng, &v, rej);
+        st = cp_sample_v(n, a, eta, rng, &v, rej, &jt);
     } else {
         float x[MLP_IN], o[MLP_OUT];
         mlp_features(a, eta, n, x);
         mlp_forward_lane(mlp, x, o);
         LearnedCounts lc{0, 0, 0, 0};
-        st = cp_sample_v_learned(o, mlp.margin, n, a, eta, rng, &v, rej, &lc);
+        st = cp_sample_v_learned(o, mlp.margin, n, a, eta, rng, &v, rej, &lc, &jt);
     }
-    if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    if (st == 0) cp_finish_j(n, a, eta, v, jt, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return st;
 }
@@ -319,21 +399,36 @@ static __device__ __noinline__ int cp_sample_learned_warp(const MlpShared& net, 
                                                           const NlcTables& t, float* sh, double a, double eta,
                                                           Draws& rng, int* n_out, double* s_out, double* theta_out,
                                                           d3* sv_out, uint32_t* rej) {
-    int n = cp_invert(t, a, eta, rng.next());
+    int n = cp_invert_warp(t, a, eta, rng.next());
     if (n < 1) n = 1;
     double v = 0.0;
+    Jtrip jt;
     int st;
     if (n < mlp.min_harmonic) {
-        st = cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, &v, rej);
+        st = cp_trials_warp(n, a, eta, cp_ceiling_warp(n, a, eta), rng, &v, rej, &jt);
     } else {
         float x[MLP_IN], o[MLP_OUT];
         mlp_features(a, eta, n, x);
         mlp_forward_warp(net, x, o, sh);
-        st = cp_sample_v_learned_warp(o, mlp.margin, n, a, eta, rng, &v, rej);
+        st = cp_sample_v_learned_warp(o, mlp.margin, n, a, eta, rng, &v, rej, &jt);
     }
-    if (st == 0) cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    if (st == 0) cp_finish_j(n, a, eta, v, jt, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return st;
+}
+
+// The quantum emission rate in FP32 where it certainly applies (the table,
+// or the bound below the table's smallest amplitude), from a^2 = u.u - 1
+// and eta; false elsewhere.  `circular` selects the CP rate at the rms
+// amplitude or the LP rate at the peak amplitude a sqrt 2.
+__device__ __forceinline__ bool emission_rate32(const LmaTables& t, bool circular, double a2, double eta, float* r32) {
+    float ln_a = 0.5f * logf((float)a2);
+    if (circular)
+        return rate32_cp(t.nlc_cp_rate32, ln_a, eta, r32) ||
+               rate32_small_a(t.nlc_cp_small32, ln_a, (float)PTG_NLC_CP_MIN_0, a2, eta, r32);
+    float ln_pk = ln_a + 0.34657359f;  // ln sqrt 2
+    return rate32_lp(t.nlc_lp_rate32, ln_pk, eta, r32) ||
+           rate32_small_a(t.nlc_lp_small32, ln_pk, (float)PTG_NLC_LP_MIN_0, 2.0 * a2, eta, r32);
 }
 
 // plane_wave.rs:251-282 / focused_laser.rs:260-281 with
@@ -366,9 +461,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
     double u_event = rng.next();
     if (!classical) {
         float r32;
-        float ln_a = 0.5f * logf((float)a2);
-        bool in32 = f.circular ? rate32_cp(t.nlc_cp_rate32, ln_a, eta, &r32)
-                               : rate32_lp(t.nlc_lp_rate32, ln_a + 0.34657359f /* ln sqrt 2 */, eta, &r32);
+        bool in32 = emission_rate32(t, f.circular, a2, eta, &r32);
         if (in32) {
             float p32 = (float)(ALPHA_FINE / COMPTON_TIME) * r32 * ((float)dt / (float)u.t);
             if (u_event > (double)p32 * (1.0 + PROB32_MARGIN)) return 0;

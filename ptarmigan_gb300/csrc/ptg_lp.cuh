@@ -563,6 +563,40 @@ static __device__ __noinline__ int lp_harmonic_index(const NlcTables& t, double 
     return isfinite(n) ? (int)ceil(n) : -1;
 }
 
+// lp_harmonic_index by a converged warp: the (up to) four grid corners
+// are inverted on lanes 0-3 at once and combined in lp_harmonic_index's
+// order and expression, so every lane returns its harmonic (or -1).
+static __device__ __noinline__ int lp_harmonic_index_warp(const NlcTables& t, double a, double eta, double frac) {
+    const unsigned all = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31u);
+    const double MIN0 = PTG_NLC_LP_CDF_MIN_0, MIN1 = PTG_NLC_LP_CDF_MIN_1, S0 = PTG_NLC_LP_CDF_STEP_0,
+                 S1 = PTG_NLC_LP_CDF_STEP_1;
+    const double* T = t.lp_cdf;
+    double la = log(a), le = log(eta);
+    if (la <= MIN0) return 1;
+    int ix = (int)((la - MIN0) / S0);
+    double dx = (la - MIN0) / S0 - ix;
+    if (ix >= 60) return -1;
+    bool edge = le <= MIN1;
+    int iy = edge ? 0 : (int)((le - MIN1) / S1);
+    if (!edge && (size_t)(61 * (iy + 1) + ix + 1) >= 4148) return -1;
+    double dy = edge ? 0.0 : (le - MIN1) / S1 - iy;
+    double v = 0.0;
+    if (lane < (edge ? 2 : 4)) {
+        size_t row = edge ? (size_t)(ix + lane) : (size_t)(61 * (iy + (lane >> 1)) + ix + (lane & 1));
+        v = lp_cdf_corner(T + row * 32, frac, a);
+    }
+    double c0 = __shfl_sync(all, v, 0), c1 = __shfl_sync(all, v, 1);
+    double n;
+    if (edge) {
+        n = c0 * (1.0 - dx) + c1 * dx;
+    } else {
+        double c2 = __shfl_sync(all, v, 2), c3 = __shfl_sync(all, v, 3);
+        n = c0 * ((1.0 - dx) * (1.0 - dy)) + c1 * (dx * (1.0 - dy)) + c2 * ((1.0 - dx) * dy) + c3 * (dx * dy);
+    }
+    return isfinite(n) ? (int)ceil(n) : -1;
+}
+
 static __device__ __noinline__ int lp_sample_n(const NlcTables& t, const DbWork& w, const DbGeom& g, double a,
                                                double eta, Draws& rng, int* n_out, double* s_out, double* theta_out,
                                                d3* sv_out, uint32_t* rej);
@@ -706,7 +740,7 @@ static __device__ __noinline__ int lp_sample_warp(const NlcTables& t, const DbWo
     const unsigned all = 0xffffffffu;
     const int lane = (int)(threadIdx.x & 31u);
     if (t.lp_cdf == nullptr || w.base == nullptr) return 8;  // PTG_ERR_TABLES
-    int n = lp_harmonic_index(t, a, eta, rng.next());
+    int n = lp_harmonic_index_warp(t, a, eta, rng.next());
     if (n < 1) return 2;  // PTG_ERR_OUT_OF_TABLE
     DbGeom g;
     if (!db_geom(n, w.cap, &g)) {

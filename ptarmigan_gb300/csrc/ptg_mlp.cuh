@@ -234,9 +234,9 @@ __device__ __forceinline__ double envelope_draw(const Envelope& e, Draws& rng, i
 // The reference's sampler taking over one emission; counts its spectrum
 // evaluations (the 32-point ceiling and one per trial).
 static __device__ __noinline__ int cp_hand_over(int n, double a, double eta, Draws& rng, double* v_out,
-                                                uint32_t* rej, LearnedCounts* c) {
+                                                uint32_t* rej, LearnedCounts* c, Jtrip* jt = nullptr) {
     uint32_t before = *rej;
-    int st = cp_sample_v(n, a, eta, rng, v_out, rej);
+    int st = cp_sample_v(n, a, eta, rng, v_out, rej, jt);
     c->evals += 32u + (*rej - before) + 1u;
     return st;
 }
@@ -247,31 +247,35 @@ static __device__ __noinline__ int cp_hand_over(int n, double a, double eta, Dra
 // learned height applies and f exceeds it, the envelope is under the
 // spectrum and the reference's sampler takes over with the same c.
 static __device__ __noinline__ int cp_sample_v_capped(Envelope e, int n, double a, double eta, Draws& rng,
-                                                      double* v_out, uint32_t* rej, LearnedCounts* c) {
+                                                      double* v_out, uint32_t* rej, LearnedCounts* c,
+                                                      Jtrip* jt = nullptr) {
     double ceil = cp_ceiling(n, a, eta);
     c->evals += 32u;
     unsigned capped = envelope_cap(&e, ceil);
     for (int it = 0; it < rng.cap; ++it) {
         int k;
         double v = envelope_draw(e, rng, &k);
-        double f = cp_diff_partial_rate(n, a, eta, v);
+        Jtrip tj;
+        double f = cp_diff_partial_rate_j(n, a, eta, v, &tj);
         c->evals += 1;
         double g = e.scale * (double)e.w[k];
         if (f > g) {
             if (capped & (1u << k)) {
                 *v_out = v;
+                if (jt) *jt = tj;
                 *rej += it;
                 return 0;
             }
             c->fallbacks += 1;
             *rej += it;
             uint32_t before = *rej;
-            int st = cp_sample_v_under(n, a, eta, ceil, rng, v_out, rej);
+            int st = cp_sample_v_under(n, a, eta, ceil, rng, v_out, rej, jt);
             c->evals += (*rej - before) + 1u;
             return st;
         }
         if (rng.next() * g < f) {
             *v_out = v;
+            if (jt) *jt = tj;
             *rej += it;
             return 0;
         }
@@ -283,20 +287,23 @@ static __device__ __noinline__ int cp_sample_v_capped(Envelope e, int n, double 
 // v at harmonic n from the learned envelope `o` (16 log-heights relative
 // to ln f(v*)).  Returns a ptg status.
 static __device__ __noinline__ int cp_sample_v_learned(const float o[MLP_OUT], float margin, int n, double a, double eta,
-                                                       Draws& rng, double* v_out, uint32_t* rej, LearnedCounts* c) {
+                                                       Draws& rng, double* v_out, uint32_t* rej, LearnedCounts* c,
+                                                       Jtrip* jt = nullptr) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     double v_star = (1.0 + sn) / (2.0 + sn);
-    double f_star = cp_diff_partial_rate(n, a, eta, v_star);
+    Jtrip jstar;
+    double f_star = cp_diff_partial_rate_j(n, a, eta, v_star, &jstar);  // as the warp sampler evaluates it
     c->evals += 1;
     Envelope e;
     if (!envelope_from(o, margin, f_star, &e)) {
         c->fallbacks += 1;
-        return cp_hand_over(n, a, eta, rng, v_out, rej, c);
+        return cp_hand_over(n, a, eta, rng, v_out, rej, c, jt);
     }
     for (int it = 0; it < LEARNED_TRIALS; ++it) {
         int k;
         double v = envelope_draw(e, rng, &k);
-        double f = cp_diff_partial_rate(n, a, eta, v);
+        Jtrip tj;
+        double f = cp_diff_partial_rate_j(n, a, eta, v, &tj);
         c->evals += 1;
         c->trials += 1;
         double g = e.scale * (double)e.w[k];
@@ -304,17 +311,18 @@ static __device__ __noinline__ int cp_sample_v_learned(const float o[MLP_OUT], f
             // the envelope is under the spectrum here
             c->fallbacks += 1;
             *rej += it;
-            return cp_hand_over(n, a, eta, rng, v_out, rej, c);
+            return cp_hand_over(n, a, eta, rng, v_out, rej, c, jt);
         }
         if (rng.next() * g < f) {
             *v_out = v;
+            if (jt) *jt = tj;
             *rej += it;
             return 0;
         }
     }
     *rej += LEARNED_TRIALS;
     c->exhausted += 1;
-    return cp_sample_v_capped(e, n, a, eta, rng, v_out, rej, c);
+    return cp_sample_v_capped(e, n, a, eta, rng, v_out, rej, c, jt);
 }
 
 }  // namespace ptg

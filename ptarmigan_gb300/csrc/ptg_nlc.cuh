@@ -102,7 +102,33 @@ __device__ __forceinline__ void j_pm(double x, int n, double* jm1, double* j, do
 }
 
 // ------------------------------------------------- CP partial rates ----
-// nonlinear_compton/cp/mod.rs:17-38: dW_n/dv, v = s / s_max
+// J_{n-1}, J_n, J_{n+1} at one argument
+struct Jtrip {
+    double m, j, p;
+};
+
+// nonlinear_compton/cp/mod.rs:17-38: dW_n/dv, v = s / s_max, with the
+// Bessel triple it evaluates (at the same argument as cp_finish forms from
+// the same v, so that an accepted sample's triple serves cp_finish_j).  One
+// out-of-line copy: every sampler, on a lane or a warp, gets the same
+// rounding (inlined, the compiler may contract 1 + a a differently).
+static __device__ __noinline__ double cp_diff_partial_rate_j(int n, double a, double eta, double v, Jtrip* jt) {
+    if (v < 0.0 || v >= 1.0) {
+        *jt = Jtrip{0.0, 0.0, 0.0};
+        return 0.0;
+    }
+    double sn = 2.0 * n * eta / (1.0 + a * a);
+    double smax = sn / (1.0 + sn);
+    double vs = v * smax;
+    double w = vs / (sn * (1.0 - vs));
+    double z = sqrt(4.0 * ((double)n * (double)n) * (a * a / (1.0 + a * a)) * w * (1.0 - w));
+    double jm, j, jp;
+    j_pm(z, n, &jm, &j, &jp);
+    *jt = Jtrip{jm, j, jp};
+    return -smax * (j * j + 0.5 * a * a * (1.0 + 0.5 * vs * vs / (1.0 - vs)) * (2.0 * j * j - jp * jp - jm * jm));
+}
+
+// The same without the triple, inline (the ceilings' 32 points)
 __device__ __forceinline__ double cp_diff_partial_rate(int n, double a, double eta, double v) {
     if (v < 0.0 || v >= 1.0) return 0.0;
     double sn = 2.0 * n * eta / (1.0 + a * a);
@@ -285,13 +311,16 @@ static __device__ __noinline__ int cp_invert(const NlcTables& t, double a, doubl
 // nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
 // nonlinear_compton/cp/mod.rs:181-200: v = s / s_max by rejection under
 // the flat ceiling mx.  Returns a ptg status.
+// `jt`, when not NULL, receives the accepted trial's Bessel triple.
 static __device__ __noinline__ int cp_sample_v_under(int n, double a, double eta, double mx, Draws& rng,
-                                                     double* v_out, uint32_t* rej) {
+                                                     double* v_out, uint32_t* rej, Jtrip* jt = nullptr) {
     int it;
     for (it = 0; it < rng.cap; ++it) {
         double vv = rng.next(), u = rng.next();
-        if (u <= cp_diff_partial_rate(n, a, eta, vv) / mx) {
+        Jtrip tj;
+        if (u <= cp_diff_partial_rate_j(n, a, eta, vv, &tj) / mx) {
             *v_out = vv;
+            if (jt) *jt = tj;
             break;
         }
     }
@@ -300,21 +329,22 @@ static __device__ __noinline__ int cp_sample_v_under(int n, double a, double eta
 }
 
 // The same under the reference's ceiling.
-static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draws& rng, double* v_out, uint32_t* rej) {
-    return cp_sample_v_under(n, a, eta, cp_ceiling(n, a, eta), rng, v_out, rej);
+static __device__ __noinline__ int cp_sample_v(int n, double a, double eta, Draws& rng, double* v_out, uint32_t* rej,
+                                               Jtrip* jt = nullptr) {
+    return cp_sample_v_under(n, a, eta, cp_ceiling(n, a, eta), rng, v_out, rej, jt);
 }
 
 // nonlinear_compton/cp/mod.rs:200-234: s, the azimuth and the Stokes
-// parameters once v is sampled.
-static __device__ __noinline__ void cp_finish(int n, double a, double eta, double v, Draws& rng, double* s_out,
-                                              double* theta_out, d3* sv_out) {
+// parameters once v is sampled, given the Bessel triple at the emission's
+// argument (the accepted trial's, from cp_diff_partial_rate_j).
+static __device__ __noinline__ void cp_finish_j(int n, double a, double eta, double v, Jtrip jt, Draws& rng,
+                                                double* s_out, double* theta_out, d3* sv_out) {
     double sn = 2.0 * n * eta / (1.0 + a * a);
     double s = v * (sn / (1.0 + sn));
     double theta = 2.0 * PI * rng.next();
     double w = s / (sn * (1.0 - s));
     double z = sqrt((double)(4 * n) * (double)n * (a * a / (1.0 + a * a)) * w * (1.0 - w));
-    double jm, j, jp;
-    j_pm(z, n, &jm, &j, &jp);
+    double jm = jt.m, j = jt.j, jp = jt.p;
     const double LASER_S3 = -1.0;
     double nz = (double)n / z;
     double xi0 = (1.0 - s + 1.0 / (1.0 - s)) * (jm * jm + jp * jp - 2.0 * j * j) - (2.0 * j / a) * (2.0 * j / a);
@@ -329,6 +359,14 @@ static __device__ __noinline__ void cp_finish(int n, double a, double eta, doubl
     *theta_out = theta;
 }
 
+// The same, evaluating the Bessel triple at the emission's argument.
+static __device__ __noinline__ void cp_finish(int n, double a, double eta, double v, Draws& rng, double* s_out,
+                                              double* theta_out, d3* sv_out) {
+    Jtrip jt;
+    cp_diff_partial_rate_j(n, a, eta, v, &jt);
+    cp_finish_j(n, a, eta, v, jt, rng, s_out, theta_out, sv_out);
+}
+
 // nonlinear_compton/cp/mod.rs:181-234.  Returns a ptg status.
 static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, double eta, Draws& rng, int* n_out, double* s_out,
                                       double* theta_out, d3* sv_out, uint32_t* rej) {
@@ -336,9 +374,10 @@ static __device__ __noinline__ int cp_sample(const NlcTables& t, double a, doubl
     int n = cp_invert(t, a, eta, rng.next());
     if (n < 1) n = 1;
     double v = 0.0;
-    int st = cp_sample_v(n, a, eta, rng, &v, rej);
+    Jtrip jt;
+    int st = cp_sample_v(n, a, eta, rng, &v, rej, &jt);
     if (st != 0) return st;
-    cp_finish(n, a, eta, v, rng, s_out, theta_out, sv_out);
+    cp_finish_j(n, a, eta, v, jt, rng, s_out, theta_out, sv_out);
     *n_out = n;
     return 0;
 }

@@ -25,6 +25,7 @@ _EXPORTS = [
     "ptg_lcfa_photon_rate", "ptg_lcfa_photon_sample", "ptg_lcfa_pair_t", "ptg_double_bessel", "ptg_lp_sample", "ptg_lp_sample_warp", "ptg_cp_sample", "ptg_cp_sample_warp",
     "ptg_cp_sample_learned",
     "ptg_collide_multi", "ptg_collide_multi_device", "ptg_queue_config", "ptg_queue_autotune", "ptg_fp64_peak",
+    "ptg_fp64_function_kernel", "ptg_emission_rate_bound",
     "ptg_mlp_init", "ptg_mlp_params", "ptg_mlp_train", "ptg_mlp_grad", "ptg_mlp_infer", "ptg_mlp_use",
     "ptg_mlp_min_harmonic",
     "ptg_sampler_bench", "ptg_build_beam", "ptg_histogram", "ptg_particle_sums",
@@ -118,6 +119,10 @@ def load(path=None):
                                      C.POINTER(abi.Particles), C.c_double, C.POINTER(abi.QueueCfg), DP]
     L.ptg_fp64_peak.restype = st
     L.ptg_fp64_peak.argtypes = [ctxp, DP]
+    L.ptg_emission_rate_bound.restype = st
+    L.ptg_emission_rate_bound.argtypes = [ctxp, C.c_size_t, C.c_int32, DP, DP, DP]
+    L.ptg_fp64_function_kernel.restype = st
+    L.ptg_fp64_function_kernel.argtypes = [ctxp, C.c_int32, C.c_int32]
     FP = C.POINTER(C.c_float)
     L.ptg_mlp_init.restype = st
     L.ptg_mlp_init.argtypes = [ctxp, C.c_uint64]
@@ -472,6 +477,20 @@ class Engine:
         if detail:
             return v0, v1, st.as_dict(), det
         return v0, v1, st.as_dict()
+
+    def emission_rate_bound(self, a_sqd, eta, circular=True):
+        """(FP32 per-step rate or NaN, FP64 rate, in-table flag) at each
+        (a^2, eta): the emission step's bound against the reference's rate."""
+        a_sqd, eta = _f64(a_sqd, (-1,)), _f64(eta, (-1,))
+        out = np.zeros((len(a_sqd), 3))
+        self._check(self.L.ptg_emission_rate_bound(self._h, len(a_sqd), int(bool(circular)), _dp(a_sqd), _dp(eta),
+                                                   _dp(out)))
+        return out[:, 0], out[:, 1], out[:, 2] > 0.5
+
+    def fp64_function_kernel(self, op, iters=64):
+        """One launch of k_fp64_fn<op> (abi.FP64_FUNCTIONS names the ops),
+        to be profiled for the function's executed FP64 cost."""
+        self._check(self.L.ptg_fp64_function_kernel(self._h, int(op), int(iters)))
 
     def fp64_peak(self):
         """Measured FP64 FMA throughput, TFLOP/s."""

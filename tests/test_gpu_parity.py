@@ -492,3 +492,26 @@ def test_lma_classical_matches_oracle(eng, orc, pol):
     assert ost["emissions"] > 30
     _compare_showers(gout, oout, tol=LMA_TOL)
     assert gst["emissions"] == pytest.approx(ost["emissions"], rel=0.03, abs=2)
+
+
+@pytest.mark.parametrize("circular", [True, False])
+def test_emission_rate_bound_covers_the_rate(eng, circular):
+    """The emission step compares its draw first with an FP32 rate and
+    decides in FP64 only where the draw falls within 2^-10 of it; the
+    decision is the reference's only if the FP32 rate times (1 + 2^-10) is
+    never below the FP64 rate.  Checked across the rate table and below its
+    smallest amplitude (where the FP32 rate is an upper bound), and the
+    bound is tight enough to spare the FP64 rate on most steps."""
+    rng = np.random.default_rng(11 if circular else 12)
+    m = 200_000
+    a = np.exp(rng.uniform(np.log(1e-9), np.log(19.0), m))
+    eta = np.exp(rng.uniform(np.log(1.1e-3), np.log(1.9), m))
+    r32, r64, ok = eng.emission_rate_bound(a * a, eta, circular=circular)
+    use = ~np.isnan(r32)
+    assert use.mean() > 0.95, use.mean()
+    assert np.all(ok[use])
+    ratio = r32[use] / r64[use]
+    assert np.all(ratio * (1.0 + 2.0 ** -10) >= 1.0), ratio.min()
+    small = use & (a < 0.02)
+    assert small.sum() > 1000
+    assert np.all(r32[small] / r64[small] < 1.02)
