@@ -72,24 +72,50 @@ METRIC = "collided primaries/s incl. showers: learned vs table sampler at fixed 
 UNIT = "primaries/s"
 SEED0 = 1000
 
-# Algorithmic FP64 operations per event of the collision loop, counted by
-# hand from the reference's formulas (roofline/opcounts.md: +, -, *, /,
-# sqrt and compare count 1, a fused multiply-add 2, exp/log/sin/cos 20;
-# cross-checked against ncu's executed FP64 instruction counts).
+# Algorithmic FP64 flops per event of the collision loop: the reference's
+# formulas counted by hand (+, -, * one flop each, a fused multiply-add two;
+# each library call at its executed cost on this GPU, measured with
+# ptg_fp64_function_kernel under ncu: exp 30, log 44, division 10, sqrt 13,
+# cbrt 16, sincos 37, pow 121, atan2 57, hypot 16, log1p 37, acos 31).
+# Cross-checked against ncu's executed DFMA/DMUL/DADD counts: the LMA push
+# alone (ptg_push_steps) executes 204.5 flops per step against 208 counted;
+# the CP lepton wave with emission switched off executes 13.8 GFLOP per 2e5
+# primaries against 14.6 counted.
 OPS = {
-    # FocusedLaser (LMA, CP): lma_push (gradient at the midpoint, <a^2> at the
-    # end) + the emission probability (rate-table lookup); a field-free step
-    # is two half drifts and gamma
-    "lma_lepton_step": 303.0,
-    "free_lepton_step": 16.0,
-    # photon step in the LMA field with the Breit-Wheeler lookup and the
-    # Stokes update into and out of the LMA basis
-    "lma_photon_step": 260.0,
-    # FastFocusedLaser (LCFA): Salamin fields at the half step, Vay push,
-    # chi and the rate; the drift of a photon step; the photon's pair step
-    "lcfa_lepton_step": 780.0,
-    "lcfa_photon_step": 420.0,
+    # FocusedLaser (LMA, CP), a step in the pulse: lma_push (gradient of
+    # <a^2> at the midpoint, <a^2> at the end: 105 + 3 div + 2 exp + sqrt =
+    # 208), the emission step up to its FP32 bound (a^2, eta, kappa and the
+    # draw: 20) and the loop's phase tests (10)
+    "lma_lepton_step": 238.0,
+    # outside the pulse: two half drifts (16) and the phase tests (8)
+    "free_lepton_step": 24.0,
+    # a photon step in the LMA field: the drift (8), the phase test (3),
+    # <a^2> and its root (70), eta, the phase step and the rate prefactor
+    # (33), the Stokes parameters into and out of the LMA basis with their
+    # rotations (270); the Breit-Wheeler table lookup (170) where the rate
+    # is not negligible: 384 without, 554 with (the photon wave of the CP
+    # shower executes 480 per step)
+    "lma_photon_step": 480.0,
+    # one emission sampled by the reference's CP sampler (table inversion,
+    # the 32-point ceiling, the trials, the finish and the kinematics):
+    # about 15.9 kflop per emission at a in [0.5, 5] and eta in [0.1, 0.2]
+    # (the serial sampler, ncu)
+    "cp_emission": 15.9e3,
+    # FastFocusedLaser (LCFA, LP): the half drift (8), the fields at the
+    # half step in FP64 (271: phase, envelope, the paraxial beam and its
+    # complex products; the eps^2..eps^4 corrections are FP32) and the Vay
+    # push (206, with three reciprocal square roots), the emission step's
+    # draw (its probability is FP32): 488 (the push alone executes 439.5)
+    "lcfa_lepton_step": 488.0,
+    # outside the envelope: the half drifts, gamma and the phase test
+    "lcfa_free_lepton_step": 40.0,
+    # a photon step: the drift and the phase test in FP64 (the fields, chi
+    # and the pair rate are FP32)
+    "lcfa_photon_step": 12.0,
+    # a drifting photon's step: the drift
     "free_photon_step": 8.0,
+    # one LCFA emission sampled (lcfa_photon_sample, ncu: 2686 per call)
+    "lcfa_emission": 2686.0,
 }
 
 
@@ -347,18 +373,25 @@ class Timer:
 
 
 def roofline_fp64(stats, kern_ms, peak_tflops, kind):
-    """The dominant kernel's algorithmic FP64 work per launch over its
-    duration, against the device's measured FP64 FMA throughput."""
-    lep, pho, free = stats["lepton_steps"], stats["photon_steps"], stats.get("free_steps", 0)
+    """The dominant kernel's algorithmic FP64 work per launch (OPS times the
+    launch's event counts) over its duration, against the device's measured
+    FP64 FMA throughput."""
+    lep, pho, emis = stats["lepton_steps"], stats["photon_steps"], stats.get("emissions", 0)
+    # free steps: leptons outside the pulse, and drifting photons
+    drift = stats.get("drift_steps", 0)
+    lfree = stats.get("free_steps", 0) - drift
     if kind == "lma":
-        # free steps are lepton steps outside the pulse here
-        flops = (lep - free) * OPS["lma_lepton_step"] + free * OPS["free_lepton_step"] + pho * OPS["lma_photon_step"]
-        model = {k: OPS[k] for k in ("lma_lepton_step", "free_lepton_step", "lma_photon_step")}
+        flops = ((lep - lfree) * OPS["lma_lepton_step"] + lfree * OPS["free_lepton_step"] +
+                 (pho - drift) * OPS["lma_photon_step"] + drift * OPS["free_photon_step"] +
+                 emis * OPS["cp_emission"])
+        model = {k: OPS[k] for k in ("lma_lepton_step", "free_lepton_step", "lma_photon_step", "free_photon_step",
+                                     "cp_emission")}
     else:
-        flops = lep * OPS["lcfa_lepton_step"] + pho * OPS["lcfa_photon_step"]
-        # drifting photons' steps cost a drift, not a pair step
-        flops -= free * (OPS["lcfa_photon_step"] - OPS["free_photon_step"]) if free <= pho else 0.0
-        model = {k: OPS[k] for k in ("lcfa_lepton_step", "lcfa_photon_step", "free_photon_step")}
+        flops = ((lep - lfree) * OPS["lcfa_lepton_step"] + lfree * OPS["lcfa_free_lepton_step"] +
+                 (pho - drift) * OPS["lcfa_photon_step"] + drift * OPS["free_photon_step"] +
+                 emis * OPS["lcfa_emission"])
+        model = {k: OPS[k] for k in ("lcfa_lepton_step", "lcfa_free_lepton_step", "lcfa_photon_step",
+                                     "free_photon_step", "lcfa_emission")}
     achieved = flops / (kern_ms / 1e3) / 1e12
     return {"bound": "fp64", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
             "frac": achieved / peak_tflops, "algorithmic_flops_per_launch": flops, "flops_per_event": model,
@@ -748,6 +781,29 @@ def run_plane_wave(args, eng, timer, sampler, line, dev):
         line["parity"] = par
 
 
+def run_profile_case(args, eng, dev):
+    """For profilers: one batch of the workload (--n primaries, default
+    2e5, seed 1000, the reference's sampler) through the wave kernels, then
+    the same batch through the single-collision queue kernel (no graph, so
+    its launch is visible): a short, fixed launch sequence.  Prints their
+    event counts."""
+    import torch
+    name = args.workload if args.workload in WORKLOADS else "cp_shower"
+    desc, make, _n = WORKLOADS[name]
+    n = args.n or 200_000
+    laser, opts, prim = make(n, 1)
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
+    eng.mlp_use(False)
+    _, st = eng.collide_device(laser, opts, d, seed=SEED0, id_base=n)
+    eng.queue_config(variant=2, blocks_per_sm=0, chunk=1, use_graph=0)
+    _, _, _, qt = eng.collide_multi_device([{"laser": laser, "seed": SEED0, "id_base": n, "first": 0, "count": n}],
+                                           opts, d)
+    keys = ("lepton_steps", "photon_steps", "free_steps", "drift_steps", "emissions", "pair_events", "n_out",
+            "particle_errors", "device_ms", "wave_ms")
+    print(json.dumps({"profile_case": desc, "n_primaries": n, "waves": {k: st[k] for k in keys},
+                      "queue": {k: qt[k] for k in keys}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -765,6 +821,8 @@ def main():
     ap.add_argument("--train-samples", type=int, default=0,
                     help="learned_sampler, cp_shower: training samples (default 5e7)")
     ap.add_argument("--train-epochs", type=int, default=0, help="learned_sampler, cp_shower: epochs (default 3)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one wave batch and one queue batch of --workload at --n primaries, for profilers")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -787,6 +845,9 @@ def main():
     dev = torch.device("cuda", local_rank)
     sampler = ClockSampler(local_rank)
     try:
+        if args.profile_case:
+            run_profile_case(args, eng, dev)
+            return
         if args.workload == "lcfa_shower":
             line = run_lcfa_shower(args, eng, stream, sampler, dev, rank, world, dist_on)
         elif args.workload == "cp_shower":

@@ -154,6 +154,7 @@ typedef struct {
                                   photon whose pair probability is zero wherever it goes */
     double wave_ms[8];         /* device time of each wave kernel (waves past the eighth add to the last
                                   entry); zero for the queue, which runs no waves */
+    uint64_t drift_steps;      /* of free_steps, those of photons that only drift */
 } ptg_run_stats;
 
 typedef struct ptg_ctx ptg_ctx;
@@ -261,9 +262,12 @@ typedef struct {
 
 /* Launch shape of the queue kernel. */
 typedef struct {
-    int32_t variant;        /* 0: registers as needed; 1: capped for 3 blocks of 128 threads per SM;
+    int32_t variant;        /* 0: registers as needed; 1: capped for 3 blocks of 128 threads per SM
+                               (both run whole particles lane by lane);
                                2: the single-collision kernel, for a batch of one collision
-                               (larger batches run variant 0) */
+                               (larger batches run variant 0);
+                               3: many collisions stepped in lockstep, one step per pass,
+                               emissions sampled by the warp */
     int32_t blocks_per_sm;  /* 0 = occupancy maximum of the variant */
     int32_t chunk;          /* tickets (store slots) a lane takes per grab: 1..64 */
     int32_t use_graph;      /* replay the batch as a captured CUDA graph */

@@ -115,6 +115,7 @@ class RunStats(C.Structure):
         ("max_steps", C.c_uint64),
         ("free_steps", C.c_uint64),
         ("wave_ms", C.c_double * 8),
+        ("drift_steps", C.c_uint64),
     ]
 
     def as_dict(self):

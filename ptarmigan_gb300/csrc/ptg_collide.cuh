@@ -42,6 +42,7 @@ struct Counters {
     unsigned long long timeouts;  // queue: bounded waits that ran out
     unsigned long long max_steps; // most steps any one particle took
     unsigned long long free_steps; // steps that only drifted (outside the pulse, drifting photons)
+    unsigned long long drift_steps; // of those, the drifting photons' steps
 };
 
 struct StepOptions {
@@ -619,7 +620,7 @@ static __device__ __noinline__ void lp_defer_serve(const WaveArgs& a, LpDefer* w
     d3 sv = mk3(0.0, 0.0, 0.0);
     uint32_t rej = 0;
     int st;
-    if (!a.f.circular)
+    if (!d.circular)
         st = lp_sample_warp(nlc_view(*a.lma), lane_dbw(a), d.a, d.eta, rng, &n, &s, &theta, &sv, &rej);
     else if (a.mlp.enabled)
         st = cp_sample_learned_warp(*mlp_smem(), a.mlp, nlc_view(*a.lma), s_mlp[threadIdx.x >> 5], d.a, d.eta, rng, &n,
@@ -701,7 +702,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
     constexpr bool LMA = MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER;
     Lane L;
     uint32_t rej = 0, nemit = 0, npair = 0, maxst = 0;
-    unsigned long long lsteps = 0, psteps = 0, fsteps = 0, nerr = 0;
+    unsigned long long lsteps = 0, psteps = 0, fsteps = 0, dsteps = 0, nerr = 0;
     LpDefer* dfr = nullptr;
     BwDefer* bdf = nullptr;
     if constexpr (LMA) {
@@ -742,6 +743,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                     unsigned long long ds = photon_drift(a, L);
                     psteps += ds;
                     fsteps += ds;
+                    dsteps += ds;
                     ds += L.step;
                     L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
                     done = true;
@@ -784,6 +786,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
         lsteps += __shfl_down_sync(m, lsteps, o);
         psteps += __shfl_down_sync(m, psteps, o);
         fsteps += __shfl_down_sync(m, fsteps, o);
+        dsteps += __shfl_down_sync(m, dsteps, o);
         nerr += __shfl_down_sync(m, nerr, o);
         rej += __shfl_down_sync(m, rej, o);
         nemit += __shfl_down_sync(m, nemit, o);
@@ -795,6 +798,7 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
         atomicAdd(&a.c->lepton_steps, lsteps);
         atomicAdd(&a.c->photon_steps, psteps);
         atomicAdd(&a.c->free_steps, fsteps);
+        atomicAdd(&a.c->drift_steps, dsteps);
         atomicAdd(&a.c->errors, nerr);
         atomicAdd(&a.c->rejections, (unsigned long long)rej);
         atomicAdd(&a.c->emissions, (unsigned long long)nemit);

@@ -1397,6 +1397,7 @@ static ptg_status run_batch(ptg_ctx* c, const ptg_laser_desc* laser, const ptg_c
             stats->ordered_waves = ordered;
             stats->max_steps = c->h_counters->max_steps;
             stats->free_steps = c->h_counters->free_steps;
+            stats->drift_steps = c->h_counters->drift_steps;
             for (int w = 0; w < 8; ++w) stats->wave_ms[w] = wave_ms[w];
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -1742,12 +1743,14 @@ static bool lma_model(int model) { return model == M_PLANE_WAVE || model == M_FO
 // single-collision kernel's instantiation for variant 2.
 static const void* queue_kernel_of(int variant, int model) {
     if (variant == 2) return lma_model(model) ? queue_kernel_single_lma(model) : queue_kernel_single_lcfa(model);
+    if (variant == 3) return queue_kernel_v3();
     return variant == 1 ? queue_kernel_v1() : queue_kernel_v0();
 }
 
 static cudaError_t launch_queue(int variant, int model, int grid, cudaStream_t s, const QueueArgs& q) {
     if (variant == 2)
         return lma_model(model) ? launch_queue_single_lma(model, grid, s, q) : launch_queue_single_lcfa(model, grid, s, q);
+    if (variant == 3) return launch_queue_v3(grid, s, q);
     return variant == 1 ? launch_queue_v1(grid, s, q) : launch_queue_v0(grid, s, q);
 }
 
@@ -1813,7 +1816,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     if (n_coll == 0 || n_coll > (1u << 20)) return set_err(PTG_ERR_INVALID_ARGUMENT, "number of collisions out of range");
     if (!d_in->species || !d_in->r || !d_in->u)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "primaries need species, r and u");
-    if (qc.variant < 0 || qc.variant > 2 || qc.chunk < 1 || qc.chunk > 64 || qc.blocks_per_sm < 0)
+    if (qc.variant < 0 || qc.variant > 3 || qc.chunk < 1 || qc.chunk > 64 || qc.blocks_per_sm < 0)
         return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
     CUDA_TRY(cudaSetDevice(c->device));
     cudaGetLastError();  // no stale error may reach the capture below
@@ -1878,7 +1881,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
     q.stats = c->d_cstats;
     q.n_coll = (int)n_coll;
     q.chunk = qc.chunk;
-    q.warp_batch = (variant == 2 && q.base.order != nullptr && c->warp_batch) ? 1 : 0;
+    q.warp_batch = ((variant == 2 || variant == 3) && q.base.order != nullptr && c->warp_batch) ? 1 : 0;
     // longest wait any lane may legitimately see: the drain of the batch's
     // last showers; generous, but bounded
     q.wait_ns = (unsigned long long)(20.0e9 + 2.0e3 * (double)n);
@@ -1969,6 +1972,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
             r.lepton_steps = cs.lepton_steps;
             r.photon_steps = cs.photon_steps;
             r.free_steps = cs.free_steps;
+            r.drift_steps = cs.drift_steps;
             r.emissions = cs.emissions;
             r.pair_events = cs.pair_events;
             r.rejections = cs.rejections;
@@ -1983,6 +1987,7 @@ static ptg_status run_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* coll
                 total->lepton_steps += r.lepton_steps;
                 total->photon_steps += r.photon_steps;
                 total->free_steps += r.free_steps;
+                total->drift_steps += r.drift_steps;
                 total->emissions += r.emissions;
                 total->pair_events += r.pair_events;
                 total->rejections += r.rejections;
@@ -2042,7 +2047,7 @@ ptg_status ptg_collide_multi(ptg_ctx* c, size_t n_coll, const ptg_collision* col
 ptg_status ptg_queue_config(ptg_ctx* c, const ptg_queue_cfg* cfg, ptg_queue_cfg* cfg_out) {
     if (!c) return set_err(PTG_ERR_INVALID_ARGUMENT, "ctx is NULL");
     if (cfg) {
-        if (cfg->variant < 0 || cfg->variant > 2 || cfg->chunk < 1 || cfg->chunk > 64 || cfg->blocks_per_sm < 0)
+        if (cfg->variant < 0 || cfg->variant > 3 || cfg->chunk < 1 || cfg->chunk > 64 || cfg->blocks_per_sm < 0)
             return set_err(PTG_ERR_INVALID_ARGUMENT, "queue launch shape out of range");
         c->qcfg = *cfg;
     }
@@ -2069,20 +2074,20 @@ ptg_status ptg_queue_autotune(ptg_ctx* c, size_t n_coll, const ptg_collision* co
         uint64_t m = (uint64_t)std::ceil(sample_fraction * (double)s.count);
         s.count = std::min<uint64_t>(s.count, std::max<uint64_t>(m, floor_count));
     }
-    // the single-collision variant is a candidate for a batch of one
+    // the single-collision variant is a candidate for a batch of one, the
+    // lockstep multi-collision variant for larger batches
     double dt_max;
     int model = make_field(coll[0].laser, &dt_max).model;
-    int n_var = n_coll == 1 ? 3 : 2;
-    int occ[3] = {0, 0, 0};
-    for (int v = 0; v < n_var; ++v) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], queue_kernel_of(v, model), 128, 0);
-        if (occ[v] < 1) occ[v] = 1;
-    }
+    std::vector<int> vars = n_coll == 1 ? std::vector<int>{0, 1, 2} : std::vector<int>{0, 1, 3};
     std::vector<ptg_queue_cfg> cands;
-    for (int v = 0; v < n_var; ++v)
-        for (int bps : {occ[v], occ[v] > 1 ? occ[v] - 1 : 0})
+    for (int v : vars) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, queue_kernel_of(v, model), 128, 0);
+        if (occ < 1) occ = 1;
+        for (int bps : {occ, occ > 1 ? occ - 1 : 0})
             for (int chunk : {1, 2})
                 if (bps > 0) cands.push_back(ptg_queue_cfg{v, bps, chunk, 1});
+    }
     double best_t = 1e300;
     ptg_queue_cfg best_c = c->qcfg;
     for (const auto& cand : cands) {
@@ -3621,6 +3626,7 @@ ptg_status ptg_collide_batch_noalloc(const ptg_laser_desc* laser, const ptg_coll
         stats->waves = waves;
         stats->max_steps = h.max_steps;
         stats->free_steps = h.free_steps;
+        stats->drift_steps = h.drift_steps;
     }
     if (h.n_out > out_capacity)
         return set_err(PTG_ERR_QUEUE_OVERFLOW, "the output needs " + std::to_string(h.n_out) + " rows, out_capacity is " +

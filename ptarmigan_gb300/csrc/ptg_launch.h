@@ -25,6 +25,9 @@ cudaError_t launch_queue_v0(int grid, cudaStream_t s, const QueueArgs& q);
 cudaError_t launch_queue_v1(int grid, cudaStream_t s, const QueueArgs& q);
 const void* queue_kernel_v0();
 const void* queue_kernel_v1();
+// variant 3: many collisions stepped in lockstep (ptg_queue_v3.cu)
+cudaError_t launch_queue_v3(int grid, cudaStream_t s, const QueueArgs& q);
+const void* queue_kernel_v3();
 cudaError_t launch_queue_single_lma(int model, int grid, cudaStream_t s, const QueueArgs& q);
 cudaError_t launch_queue_single_lcfa(int model, int grid, cudaStream_t s, const QueueArgs& q);
 const void* queue_kernel_single_lma(int model);

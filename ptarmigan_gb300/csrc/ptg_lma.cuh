@@ -101,11 +101,12 @@ __device__ __forceinline__ double std_normal(Draws& rng) {
 // takes the stored sample with the draws as they stood after it.
 struct LpDefer {
     Draws rng;      // the draws at the sample; after it, once served
-    double a, eta;  // peak amplitude (a sqrt 2) and eta of the emission
+    double a, eta;  // amplitude (LP: the peak a sqrt 2) and eta of the emission
     double s, theta;
     d3 sv;
     int n, status;
     int pend;  // 0: none; 1: waiting for the warp; 2: served
+    int circular;  // the emitting lane's laser polarisation
     uint32_t rej;
 };
 
@@ -495,6 +496,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
                 dfr->rng = rng;
                 dfr->a = aq;
                 dfr->eta = eta;
+                dfr->circular = 1;
                 dfr->pend = 1;
                 return LMA_DEFERRED;
             }
@@ -516,6 +518,7 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
             dfr->rng = rng;
             dfr->a = aq * SQRT_2;
             dfr->eta = eta;
+            dfr->circular = 0;
             dfr->pend = 1;
             return LMA_DEFERRED;
         }

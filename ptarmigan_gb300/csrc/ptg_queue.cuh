@@ -28,7 +28,7 @@ struct CollParams {
 struct CollStats {
     unsigned long long lepton_steps, photon_steps, emissions, pair_events, rejections, errors;
     unsigned long long n_created, n_out;
-    unsigned long long free_steps;
+    unsigned long long free_steps, drift_steps;
 };
 
 struct QueueArgs {
@@ -117,7 +117,7 @@ __device__ __forceinline__ int poll_slot(const WaveArgs& a, unsigned long long t
 
 struct PartCounts {
     uint32_t rej, nemit, npair;
-    unsigned long long lsteps, psteps, fsteps;
+    unsigned long long lsteps, psteps, fsteps, dsteps;
 };
 
 // main.rs:134-289 for one particle: steps it until it leaves the field,
@@ -143,6 +143,7 @@ static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, Par
                 unsigned long long ds = photon_drift(a, L);
                 pc.psteps += ds;
                 pc.fsteps += ds;
+                pc.dsteps += ds;
                 ds += L.step;
                 L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
                 return;
@@ -212,6 +213,7 @@ __device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs&
     if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
     if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
     if (pc.fsteps) atomicAdd(&cs->free_steps, pc.fsteps);
+    if (pc.dsteps) atomicAdd(&cs->drift_steps, pc.dsteps);
     if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
     if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
     if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
@@ -243,6 +245,7 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
         unsigned long long ds = photon_drift(a, L);
         pc.psteps += ds;
         pc.fsteps += ds;
+        pc.dsteps += ds;
         ds += L.step;
         L.step = ds < 0xffffffffull ? (uint32_t)ds : 0xffffffffu;
         return true;
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
         Lane L;
         queue_load(a, L, slot);
         if (!queue_begin(q, a, L, cur)) continue;
-        PartCounts pc{0, 0, 0, 0, 0, 0};
+        PartCounts pc{0, 0, 0, 0, 0, 0, 0};
         switch (a.f.model) {
             case M_PLANE_WAVE: run_particle<M_PLANE_WAVE>(a, L, pc); break;
             case M_FAST_PLANE_WAVE: run_particle<M_FAST_PLANE_WAVE>(a, L, pc); break;
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
     const unsigned FULL = 0xffffffffu;
     const WaveArgs& a = q.base;
     Lane L;
-    PartCounts pc{0, 0, 0, 0, 0, 0};
+    PartCounts pc{0, 0, 0, 0, 0, 0, 0};
     uint32_t maxst = 0;
     bool have = false, holding = false, finished = false;
     // CP LMA photons leave their Breit-Wheeler harmonic sums to the warp
@@ -371,7 +374,7 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
                 } else {
                     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
                     L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
-                    pc = PartCounts{0, 0, 0, 0, 0, 0};
+                    pc = PartCounts{0, 0, 0, 0, 0, 0, 0};
                     have = true;
                 }
             }
@@ -386,6 +389,96 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             have = false;
         }
         if (LMA && (bdf != nullptr || dfr != nullptr)) warp_serve(a, dfr, bdf, have);
+    }
+    if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
+}
+
+// One step of a particle of any field model (the lockstep multi-collision
+// kernel, whose lanes may hold particles of different collisions).
+static __device__ __noinline__ bool queue_step_any(const WaveArgs& a, Lane& L, PartCounts& pc, BwDefer* bdf,
+                                                   LpDefer* dfr) {
+    switch (a.f.model) {
+        case M_PLANE_WAVE: return queue_step<M_PLANE_WAVE>(a, L, pc, bdf, dfr);
+        case M_FOCUSED_LASER: return queue_step<M_FOCUSED_LASER>(a, L, pc, bdf, dfr);
+        case M_FAST_PLANE_WAVE: return queue_step<M_FAST_PLANE_WAVE>(a, L, pc);
+        default: return queue_step<M_FAST_FOCUSED_LASER>(a, L, pc);
+    }
+}
+
+// Variant 3: many collisions (the a0 scan), stepped as the single-collision
+// kernel steps one: one pass of the loop is one step of every lane's
+// particle, a warp takes tickets together when none of its lanes holds a
+// particle or a ticket (with q.warp_batch), and emissions, pair harmonics
+// and Breit-Wheeler sums are served by the whole warp after each pass.
+// Each lane keeps a copy of the step parameters that follows its current
+// collision (queue_begin), as variant 0 does; a deferred emission records
+// its polarisation, so that a warp may serve lanes of different
+// collisions.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) collide_queue_lockstep(QueueArgs q) {
+    const unsigned FULL = 0xffffffffu;
+    WaveArgs a = q.base;
+    int cur = -1;
+    Lane L;
+    PartCounts pc{0, 0, 0, 0, 0, 0, 0};
+    uint32_t maxst = 0;
+    bool have = false, holding = false, finished = false;
+    __shared__ BwDefer s_bdf[128];
+    __shared__ LpDefer s_dfr[128];
+    BwDefer* bdf = &s_bdf[threadIdx.x];
+    bdf->pend = 0;
+    // emissions go to the warp unless the rates are classical (uniform over
+    // the grid: the batch's options decide)
+    LpDefer* dfr = a.o.classical_mode ? nullptr : &s_dfr[threadIdx.x];
+    if (dfr) dfr->pend = 0;
+    if (dfr && a.mlp.enabled) mlp_stage(a.mlp, mlp_smem());
+    unsigned long long t = 0, t_end = 0, ticket = 0, wait_from = 0;
+    for (;;) {
+        if (__all_sync(FULL, finished)) break;
+        bool leptons = __any_sync(FULL, have && L.species != SP_PHOTON);
+        bool may_grab = !q.warp_batch || __all_sync(FULL, (!have && !holding) || finished);
+        if (!have && !finished && (holding || t != t_end || may_grab)) {
+            if (!holding) {
+                if (t == t_end) {
+                    t = grab_tickets(a.c, (unsigned)q.chunk);
+                    t_end = t + (unsigned long long)q.chunk;
+                }
+                ticket = t++;
+                holding = true;
+                wait_from = global_ns();
+            }
+            // primaries in each collision's order of laser phase (a.order),
+            // the rest in ticket order
+            unsigned long long slot = (a.order && ticket < a.n_primaries) ? a.order[ticket] : ticket;
+            int w = (leptons && ticket >= a.n_primaries) ? POLL_NOT_YET : poll_slot(a, slot);
+            if (w == WAIT_DRAINED) {
+                finished = true;
+            } else if (w == WAIT_SKIP) {
+                holding = false;
+            } else if (w == POLL_NOT_YET) {
+                if (global_ns() - wait_from > q.wait_ns) {
+                    atomicAdd(&a.c->timeouts, 1ull);
+                    finished = true;
+                }
+            } else {
+                holding = false;
+                queue_load(a, L, slot);
+                if (queue_begin(q, a, L, cur)) {
+                    pc = PartCounts{0, 0, 0, 0, 0, 0, 0};
+                    have = true;
+                }
+            }
+        }
+        if (__all_sync(FULL, !have)) {
+            __nanosleep(256);
+            continue;
+        }
+        if (have && queue_step_any(a, L, pc, bdf, dfr)) {
+            maxst = L.step > maxst ? L.step : maxst;
+            queue_finish(q, a, L, pc);
+            have = false;
+        }
+        warp_serve(a, dfr, bdf, have);
     }
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }

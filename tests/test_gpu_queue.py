@@ -70,12 +70,15 @@ def _mixed_specs():
     return [(ffl, 40, 10.0, 1), (fl_cp, 30, 16.5, 2), (fpw, 30, 10.0, 3), (fl_lp, 30, 16.5, 4)]
 
 
-@pytest.mark.parametrize("use_graph", [0, 1])
-def test_queue_matches_single_collisions(eng, use_graph):
+@pytest.mark.parametrize("variant,use_graph", [(0, 0), (0, 1), (3, 0), (3, 1)])
+def test_queue_matches_single_collisions(eng, variant, use_graph):
+    """Four collisions of the four field models in one launch: whole
+    particles per lane (variant 0) or every lane one step per pass with the
+    warp sampling emissions (variant 3)."""
     # emission only: linearly polarised LMA pair creation is not built
     colls, prim = _batch(_mixed_specs())
     opts = abi.collide_options(max_generation=2, tracking_photons=0)
-    eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=use_graph)
+    eng.queue_config(variant=variant, blocks_per_sm=0, chunk=1, use_graph=use_graph)
     parts, stats, total = eng.collide_multi(colls, opts, prim)
     assert total["particle_errors"] == 0
     for k, c in enumerate(colls):
@@ -126,7 +129,8 @@ def test_queue_overflow_reruns(eng):
         fresh.close()
 
 
-def test_queue_a0_scan_uneven(eng):
+@pytest.mark.parametrize("variant", [0, 3])
+def test_queue_a0_scan_uneven(eng, variant):
     """A small a0 scan in one launch: 16 collisions, a0 log-spaced 0.5..20,
     LMA (circular) below a0 = 5 and LCFA above, uneven beam sizes."""
     rng = np.random.default_rng(3)
@@ -138,8 +142,9 @@ def test_queue_a0_scan_uneven(eng):
         specs.append((laser, int(rng.integers(1, 40)), 16.5, 10 + k))
     colls, prim = _batch(specs)
     opts = abi.collide_options()
-    eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
+    eng.queue_config(variant=variant, blocks_per_sm=0, chunk=1, use_graph=1)
     parts, stats, total = eng.collide_multi(colls, opts, prim)
+    eng.queue_config(variant=0)
     assert total["particle_errors"] == 0
     for k in (0, 7, 15):
         c = colls[k]
@@ -155,8 +160,8 @@ def test_queue_autotune_picks_a_valid_shape(eng):
     dev = torch.device("cuda", 0)
     d_prim = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in prim.items()}
     best, ms = eng.queue_autotune(colls, opts, d_prim, sample_fraction=0.5)
-    # a mixed batch: the flat variant is not a candidate
-    assert best["variant"] in (0, 1) and 1 <= best["chunk"] <= 64 and best["blocks_per_sm"] >= 1
+    # a mixed batch: the single-collision variant is not a candidate
+    assert best["variant"] in (0, 1, 3) and 1 <= best["chunk"] <= 64 and best["blocks_per_sm"] >= 1
     assert ms > 0.0 and math.isfinite(ms)
     assert eng.queue_config() == best
     out, offs, stats, total = eng.collide_multi_device(colls, opts, d_prim)
@@ -239,3 +244,29 @@ def test_graph_replay_follows_seed_and_sampler(eng):
                 assert all(total[k] == ref[k] for k in keys), (variant, learned, seed, total, ref)
     eng.mlp_use(False)
     eng.queue_config(variant=0, blocks_per_sm=0, chunk=1, use_graph=1)
+
+
+def test_lockstep_queue_lp_a0_scan_matches_single_collisions(eng):
+    """Linearly polarised collisions (LMA below a0 = 5, LCFA above) in one
+    lockstep launch (variant 3): the warp samples the LP emissions of lanes
+    that belong to different collisions, and every collision reproduces its
+    single-collision run."""
+    specs = []
+    for k, a0 in enumerate((0.8, 1.5, 3.0, 6.0, 12.0)):
+        model = abi.FOCUSED_LASER if a0 < 5.0 else abi.FAST_FOCUSED_LASER
+        laser = abi.laser_desc(model, a0, 0.8e-6, abi.LINEAR, abi.GAUSSIAN, waist=5e-6, fwhm_duration=25e-15)
+        specs.append((laser, 120, 16.5, 40 + k))
+    colls, prim = _batch(specs)
+    opts = abi.collide_options(max_generation=2, tracking_photons=0)
+    eng.queue_config(variant=3, blocks_per_sm=0, chunk=1, use_graph=1)
+    try:
+        parts, stats, total = eng.collide_multi(colls, opts, prim)
+    finally:
+        eng.queue_config(variant=0)
+    assert total["particle_errors"] == 0
+    assert sum(s["emissions"] for s in stats[:3]) > 20
+    for k, c in enumerate(colls):
+        sub = {name: v[c["first"]:c["first"] + c["count"]] for name, v in prim.items()}
+        single, sst = eng.collide(c["laser"], opts, sub, seed=c["seed"], id_base=c["id_base"])
+        _compare(parts[k], single, TOL[c["laser"].model], 0.02)
+        assert stats[k]["emissions"] == pytest.approx(sst["emissions"], rel=0.03, abs=2)
