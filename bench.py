@@ -39,7 +39,9 @@ Other workloads (--workload), each one JSON line of the same metric:
   lcfa_shower     1e6 electrons at 10 GeV, 1% spread, 2 x 2 x 20 um, 50 urad,
                   on a linearly polarised focused Gaussian laser (LCFA,
                   FastFocusedLaser) a0 = 10, w0 = 4 um, 0.8 um, 30 fs; pairs
-                  on, secondaries tracked to generation 2.
+                  on, secondaries tracked to generation 2.  `value` runs the
+                  wave kernels, `queue_value` the same batches through the
+                  single-collision queue kernel.
   plane_wave_lma  1e4 electrons at 5 GeV, 0.1% spread, 1 x 1 x 10 um, on a
                   linearly polarised plane wave (LMA), a0 = 1, 0.8 um, cos^2
                   envelope of 30 fs intensity FWHM (30.9 cycles), emission
@@ -620,6 +622,22 @@ def run_lcfa_shower(args, eng, stream, sampler, dev, rank, world, dist_on):
         total = float(t.item())
     value = n * world * len(seeds) / (total / 1e3)
 
+    # the same batches through the single-collision queue kernel (one
+    # persistent launch per batch, graph replay)
+    eng.queue_config(variant=2, blocks_per_sm=0, chunk=1, use_graph=1)
+    coll = [{"laser": laser, "seed": 0, "id_base": id_base, "first": 0, "count": n}]
+
+    def queue_batch(s):
+        coll[0]["seed"] = s
+        return eng.collide_multi_device(coll, opts, d_prim)[3]
+
+    queue_batch(1998)
+    barrier()
+    q_total, q_per, _ = timer.run(queue_batch, seeds)
+    barrier()
+    queue_value = n * world * len(seeds) / (q_total / 1e3)
+    eng.queue_config(variant=0)
+
     prim_h = pinned_copy(prim)
     out, _ = eng.collide(laser, opts, prim_h, seed=1999, id_base=id_base)  # untimed warm-up
     del out
@@ -654,6 +672,7 @@ def run_lcfa_shower(args, eng, stream, sampler, dev, rank, world, dist_on):
         "config": {"workload": desc, "n_primaries_per_gpu": n, "parallelism": "replicas x%d" % world,
                    "seeds": [seeds[0], seeds[-1]], "l2": "inputs and shower store larger than L2 (no flush needed)"},
         "step_ms": step_summary(per),
+        "queue_value": queue_value, "queue_step_ms": step_summary(q_per),
         "wave_ms_per_step": [[round(x, 2) for x in r["wave_ms"][:max(1, r["waves"])]] for r in res],
         "particle_errors": agg["particle_errors"], "max_steps_per_particle": agg["max_steps"],
         "events_per_step": {k: res[-1][k] for k in keys},
