@@ -257,6 +257,10 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
     return L.status != ST_OK;
 }
 
+// Steps a lane of the single-collision and lockstep queue kernels takes per
+// pass of their loops, between two rounds of ticket logic.
+constexpr int QUEUE_STEPS_PER_PASS = 8;
+
 // Kernel variants: MINB > 1 caps the registers so that MINB blocks of 128
 // threads fit on an SM (the LCFA paths need fewer registers than LMA's).
 template <int MINB>
@@ -296,9 +300,10 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }
 
-// The single-collision variant (a batch of one collision): one pass of a
-// single loop is one step of every lane's particle, as in collide_wave, so
-// a lane whose particle ends takes its next ticket at once, and the step
+// The single-collision variant (a batch of one collision): one pass of its
+// loop is up to QUEUE_STEPS_PER_PASS steps of every lane's particle, each
+// followed by the warp's service as in collide_wave, so a lane whose
+// particle ends takes its next ticket within a few steps, and the step
 // code reads the collision's parameters from the kernel's parameter space
 // (as collide_wave does) rather than from a per-lane copy that follows the
 // lane's current collision.  A lane whose ticket is not yet published looks
@@ -383,12 +388,18 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             __nanosleep(256);
             continue;
         }
-        if (have && queue_step<MODEL>(a, L, pc, bdf, dfr)) {
-            maxst = L.step > maxst ? L.step : maxst;
-            queue_finish(q, a, L, pc);
-            have = false;
+        // up to QUEUE_STEPS_PER_PASS steps before the ticket logic runs
+        // again (its votes then cost once per several steps); a warp whose
+        // particles are all done leaves early
+        for (int k = 0; k < QUEUE_STEPS_PER_PASS; ++k) {
+            if (have && queue_step<MODEL>(a, L, pc, bdf, dfr)) {
+                maxst = L.step > maxst ? L.step : maxst;
+                queue_finish(q, a, L, pc);
+                have = false;
+            }
+            if (LMA && (bdf != nullptr || dfr != nullptr)) warp_serve(a, dfr, bdf, have);
+            if (!__any_sync(FULL, have)) break;
         }
-        if (LMA && (bdf != nullptr || dfr != nullptr)) warp_serve(a, dfr, bdf, have);
     }
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }
@@ -406,8 +417,9 @@ static __device__ __noinline__ bool queue_step_any(const WaveArgs& a, Lane& L, P
 }
 
 // Variant 3: many collisions (the a0 scan), stepped as the single-collision
-// kernel steps one: one pass of the loop is one step of every lane's
-// particle, a warp takes tickets together when none of its lanes holds a
+// kernel steps one: one pass of the loop is up to QUEUE_STEPS_PER_PASS
+// steps of every lane's particle, a warp takes tickets together when none
+// of its lanes holds a
 // particle or a ticket (with q.warp_batch), and emissions, pair harmonics
 // and Breit-Wheeler sums are served by the whole warp after each pass.
 // Each lane keeps a copy of the step parameters that follows its current
@@ -473,12 +485,15 @@ __global__ void __launch_bounds__(128, MINB) collide_queue_lockstep(QueueArgs q)
             __nanosleep(256);
             continue;
         }
-        if (have && queue_step_any(a, L, pc, bdf, dfr)) {
-            maxst = L.step > maxst ? L.step : maxst;
-            queue_finish(q, a, L, pc);
-            have = false;
+        for (int k = 0; k < QUEUE_STEPS_PER_PASS; ++k) {
+            if (have && queue_step_any(a, L, pc, bdf, dfr)) {
+                maxst = L.step > maxst ? L.step : maxst;
+                queue_finish(q, a, L, pc);
+                have = false;
+            }
+            warp_serve(a, dfr, bdf, have);
+            if (!__any_sync(FULL, have)) break;
         }
-        warp_serve(a, dfr, bdf, have);
     }
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
 }
