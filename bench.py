@@ -49,8 +49,10 @@ Other workloads (--workload), each one JSON line of the same metric:
   a0_scan         64 collisions in one persistent queue launch: a0
                   log-spaced 0.5..20, beams log-uniform 1e3..1e6 electrons
                   (seeded) at 16.5 GeV, 0.1% spread, 2 x 2 x 20 um, 8 urad, on
-                  a circularly polarised focused Gaussian laser, w0 = 5 um,
+                  a linearly polarised focused Gaussian laser, w0 = 5 um,
                   0.8 um, 25 fs; LMA below a0 = 5, LCFA above; pairs on.
+                  The autotuner picks the queue kernel's launch shape
+                  (usually the lockstep multi-collision variant);
                   `plain_value` runs the same collisions one call each.
   learned_sampler the CP photon-energy sampler alone, learned proposal
                   against the table sampler on 1e7 emissions per step.
