@@ -423,6 +423,14 @@ static __device__ __noinline__ int cp_sample_learned_warp(const MlpShared& net, 
 // and eta; false elsewhere.  `circular` selects the CP rate at the rms
 // amplitude or the LP rate at the peak amplitude a sqrt 2.
 __device__ __forceinline__ bool emission_rate32(const LmaTables& t, bool circular, double a2, double eta, float* r32) {
+    // a^2 at or below zero: the rounding of u.u - 1 where <a^2> is below
+    // about 1e-7 (u^0 ~ 3e4 in the pulse's wings).  The rate is then that of
+    // a = 0 (nonlinear_compton/mod.rs:22-27), which is zero in every branch
+    // for 0 < eta < 2, so the step cannot emit.
+    if (a2 <= 0.0 && eta > 0.0 && eta < 2.0) {
+        *r32 = 0.0f;
+        return true;
+    }
     float ln_a = 0.5f * logf((float)a2);
     if (circular)
         return rate32_cp(t.nlc_cp_rate32, ln_a, eta, r32) ||

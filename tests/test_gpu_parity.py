@@ -515,3 +515,9 @@ def test_emission_rate_bound_covers_the_rate(eng, circular):
     small = use & (a < 0.02)
     assert small.sum() > 1000
     assert np.all(r32[small] / r64[small] < 1.02)
+    # a^2 = u.u - 1 at or below zero (rounding in the pulse's wings): both
+    # rates are zero there, and the FP32 one applies
+    a2 = np.concatenate([np.zeros(100), -np.exp(rng.uniform(np.log(1e-14), np.log(1e-6), 900))])
+    eta = np.exp(rng.uniform(np.log(1e-4), np.log(1.9), a2.size))
+    r32, r64, ok = eng.emission_rate_bound(a2, eta, circular=circular)
+    assert np.all(ok) and np.all(r64 == 0.0) and np.all(r32 == 0.0)
