@@ -168,6 +168,35 @@ __device__ __forceinline__ bool lane_stops(const WaveArgs& a, Lane& L) {
     return L.status != ST_OK || lane_untracked(a, L);
 }
 
+// Longest run of field-free steps lma_free_run takes at once.
+constexpr uint32_t FREE_RUN_MAX = 4096;
+
+// The field-free LMA lepton steps that follow a field-free step, taken as
+// one run.  The phase k(t - z) of a massive particle grows by at most
+// 2 omega dt per step and never falls (lma_step_field_free).  So a lepton
+// at phase p, before the pulse or after it, stays field-free and inside the
+// field (Field::contains: phase < max_phase) for the next m steps, where m
+// follows from p alone with a margin of 1 for rounding.  The run then takes
+// m steps with lma_drift's own arithmetic and no per-step checks: r, u and
+// the step count are bit for bit those of stepping.  Returns m; 0 with a
+// t_stop, outside the LMA models, or when the bound leaves no room.
+__device__ __forceinline__ uint32_t lma_free_run(const WaveArgs& a, Lane& L) {
+    const FieldParams& f = a.f;
+    if (!(f.lma_cut > 0.0) || a.o.has_t_stop || L.status != ST_OK) return 0;
+    const double dt = a.o.dt;
+    const double dphase = 2.0 * f.omega * dt;
+    const double phase = phase_of(f, L.r);
+    double room = f.max_phase - 1.0 - phase;                          // contains, before every step
+    if (!(phase > f.lma_cut + 1.0)) room = fmin(room, -f.lma_cut - 2.0 - phase);  // ends before the pulse
+    if (!(dphase > 0.0) || !(room >= dphase)) return 0;
+    double mm = floor(room / dphase);
+    uint32_t m = mm < (double)FREE_RUN_MAX ? (uint32_t)mm : FREE_RUN_MAX;
+    uint32_t left = L.step < a.o.step_cap ? a.o.step_cap - L.step : 0u;  // lane_stops' cap
+    m = m < left ? m : left;
+    for (uint32_t k = 0; k < m; ++k) lma_drift(L, dt);
+    return m;
+}
+
 __device__ __forceinline__ void spawn(const WaveArgs& a, unsigned long long slot, int species, d4 r, d4 u, d4 u0,
                                       d4 pol, double weight, double payload, double parent_chi, double work,
                                       unsigned long long parent_id, unsigned long long primary,
@@ -734,6 +763,12 @@ __global__ void __launch_bounds__(128) collide_wave(WaveArgs a) {
                         ++lsteps;
                         fsteps += fr ? 1ull : 0ull;
                         done = L.status != ST_OK;
+                        if (LMA && fr && !done) {
+                            uint32_t m = lma_free_run(a, L);
+                            L.step += m;
+                            lsteps += m;
+                            fsteps += m;
+                        }
                     }
                 }
             } else {

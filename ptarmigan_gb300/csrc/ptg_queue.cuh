@@ -131,10 +131,17 @@ static __device__ __noinline__ void run_particle(const WaveArgs& a, Lane& L, Par
         } else if (L.species != SP_PHOTON) {
             done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop));
             if (!done) {
-                pc.fsteps += lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit) ? 1ull : 0ull;
+                bool fr = lepton_step<MODEL, true>(a, L, &pc.rej, &pc.nemit);
+                pc.fsteps += fr ? 1ull : 0ull;
                 ++L.step;
                 ++pc.lsteps;
                 done = L.status != ST_OK;
+                if ((MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER) && fr && !done) {
+                    uint32_t m = lma_free_run(a, L);
+                    L.step += m;
+                    pc.lsteps += m;
+                    pc.fsteps += m;
+                }
             }
         } else {
             done = !(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
@@ -236,7 +243,14 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
         pc.fsteps += fr ? 1ull : 0ull;
         ++L.step;
         ++pc.lsteps;
-        return L.status != ST_OK;
+        if (L.status != ST_OK) return true;
+        if ((MODEL == M_PLANE_WAVE || MODEL == M_FOCUSED_LASER) && fr) {
+            uint32_t m = lma_free_run(a, L);
+            L.step += m;
+            pc.lsteps += m;
+            pc.fsteps += m;
+        }
+        return false;
     }
     if (!(contains(a.f, L.r) && (!a.o.has_t_stop || L.r.t / SPEED_OF_LIGHT < a.o.t_stop) && !L.decayed &&
           a.o.tracking_photons))
