@@ -91,8 +91,9 @@ OPS = {
     # 208), the emission step up to its FP32 bound (a^2, eta, kappa and the
     # draw: 20) and the loop's phase tests (10)
     "lma_lepton_step": 238.0,
-    # outside the pulse: two half drifts (16) and the phase tests (8)
-    "free_lepton_step": 24.0,
+    # outside the pulse: two half drifts (16); the phase tests run once per
+    # run of field-free steps (lma_free_run), not per step
+    "free_lepton_step": 16.0,
     # a photon step in the LMA field: the drift (8), the phase test (3),
     # <a^2> and its root (70), eta, the phase step and the rate prefactor
     # (33), the Stokes parameters into and out of the LMA basis with their

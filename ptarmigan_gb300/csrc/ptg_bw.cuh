@@ -381,18 +381,21 @@ static __device__ __noinline__ int bw_sample(const double* T, double a, double e
 
 // polarization.rs:101-130: Stokes parameters in the LMA basis
 __device__ __forceinline__ d4 stokes_in_lma_basis(d4 sv, d4 k) {
-    double k_minus = k.t - k.z;
-    double c = (k.z * k_minus - k.x * k.x) / (k_minus * hypot(k.x, k.z));
-    double sign = dsign(k.x * k.y);
-    c = fmin(fmax(c, -1.0), 1.0);
-    double s = sign * sqrt(1.0 - c * c);
-    double c2 = c * c - s * s, s2 = 2.0 * c * s;
-    return d4{sv.t, c2 * sv.x - s2 * sv.y, s2 * sv.x + c2 * sv.y, sv.z};
+    StokesBasis b = lma_stokes_basis(k);
+    d3 g = stokes_rotate_cs(mk3(sv.x, sv.y, sv.z), b.c2, b.s2);
+    return d4{sv.t, g.x, g.y, g.z};
 }
 
+// polarization.rs:132-141.  At theta = +-0 (the default polarisation angle)
+// sincos(2 theta) is (+-0, 1) exactly, so the call is skipped.
 __device__ __forceinline__ d4 stokes_rotate_by(d4 sv, double theta) {
     double s2, c2;
-    sincos(2.0 * theta, &s2, &c2);
+    if (theta == 0.0) {
+        s2 = 2.0 * theta;
+        c2 = 1.0;
+    } else {
+        sincos(2.0 * theta, &s2, &c2);
+    }
     return d4{sv.t, c2 * sv.x + s2 * sv.y, -s2 * sv.x + c2 * sv.y, sv.z};
 }
 
@@ -553,13 +556,15 @@ static __device__ __noinline__ int bw_probability(const double* T, d4 ell, d4 sv
     } else if (!bw_by_lookup(T, a, eta, &f0, &f1, nodes)) {
         return 0;
     }
-    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    StokesBasis bs = lma_stokes_basis(ell);
+    d3 g0 = stokes_rotate_cs(mk3(sv_in.x, sv_in.y, sv_in.z), bs.c2, bs.s2);
+    d4 sv = stokes_rotate_by(d4{sv_in.t, g0.x, g0.y, g0.z}, pol_angle);
     double p = c * (0.5 * ((f0 + f1) + sv.z * (f0 - f1)));
     double p_avg = c * (0.5 * (f0 + f1));
     double delta = c * (0.5 * (f0 - f1));
     d4 o = d4{sv.t, sv.x * (1.0 - p_avg) / (1.0 - p), sv.y * (1.0 - p_avg) / (1.0 - p), (sv.z * (1.0 - p_avg) - delta) / (1.0 - p)};
     o = stokes_rotate_by(o, -pol_angle);
-    d3 g = stokes_from_lma_basis(mk3(o.x, o.y, o.z), ell);
+    d3 g = stokes_rotate_cs(mk3(o.x, o.y, o.z), bs.c2, -bs.s2);
     *sv_out = d4{o.t, g.x, g.y, g.z};
     *prob = p;
     return 1;

@@ -551,7 +551,9 @@ static __device__ __noinline__ int lma_radiate(const FieldParams& f, const LmaTa
 static __device__ __noinline__ bool lp_bw_probability(const LmaTables& t, d4 ell, d4 sv_in, d4 k, double a, double dt,
                                                       double pol_angle, double* prob, d4* sv_out) {
     double eta = dot4(k, ell);
-    d4 sv = stokes_rotate_by(stokes_in_lma_basis(sv_in, ell), pol_angle);
+    StokesBasis bs = lma_stokes_basis(ell);
+    d3 g0 = stokes_rotate_cs(mk3(sv_in.x, sv_in.y, sv_in.z), bs.c2, bs.s2);
+    d4 sv = stokes_rotate_by(d4{sv_in.t, g0.x, g0.y, g0.z}, pol_angle);
     double dphi = eta * dt / (COMPTON_TIME * ell.t);
     double f[2];
     if (!lpp_rates(t.bw_lp_total, t.bw_lp_mid_total, a * SQRT_2, eta, f)) return false;
@@ -563,7 +565,7 @@ static __device__ __noinline__ bool lp_bw_probability(const LmaTables& t, d4 ell
     d4 o = d4{sv.t, (sv.x * (1.0 - p_avg) - delta) / (1.0 - p), sv.y * (1.0 - p_avg) / (1.0 - p),
               sv.z * (1.0 - p_avg) / (1.0 - p)};
     o = stokes_rotate_by(o, -pol_angle);
-    d3 g = stokes_from_lma_basis(mk3(o.x, o.y, o.z), ell);
+    d3 g = stokes_rotate_cs(mk3(o.x, o.y, o.z), bs.c2, -bs.s2);
     *sv_out = d4{o.t, g.x, g.y, g.z};
     *prob = p;
     return true;

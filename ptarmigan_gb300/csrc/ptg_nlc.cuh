@@ -397,15 +397,30 @@ __device__ __forceinline__ d4 boost_by(d4 v, d4 u) {
               z.z + (gamma - 1.0) * nz * n.z - gamma * beta * v.t * n.z};
 }
 
-// polarization.rs:101-155: Stokes parameters from the LMA basis
-__device__ __forceinline__ d3 stokes_from_lma_basis(d3 sv, d4 k) {
+// polarization.rs:101-155: the rotation between the global Stokes basis and
+// the LMA basis of a photon of momentum k, as (cos, sin) of twice the
+// angle.  Into the LMA basis it is (c2, s2); out of it the reference's sine
+// changes sign and its cosine does not, so it is (c2, -s2) exactly.
+struct StokesBasis {
+    double c2, s2;
+};
+__device__ __forceinline__ StokesBasis lma_stokes_basis(d4 k) {
     double k_minus = k.t - k.z;
     double c = (k.z * k_minus - k.x * k.x) / (k_minus * hypot(k.x, k.z));
     double sign = dsign(k.x * k.y);
     c = fmin(fmax(c, -1.0), 1.0);
-    double s = -(sign * sqrt(1.0 - c * c));
-    double c2 = c * c - s * s, s2 = 2.0 * c * s;
+    double s = sign * sqrt(1.0 - c * c);
+    return StokesBasis{c * c - s * s, 2.0 * c * s};
+}
+
+__device__ __forceinline__ d3 stokes_rotate_cs(d3 sv, double c2, double s2) {
     return mk3(c2 * sv.x - s2 * sv.y, s2 * sv.x + c2 * sv.y, sv.z);
+}
+
+// Stokes parameters from the LMA basis
+__device__ __forceinline__ d3 stokes_from_lma_basis(d3 sv, d4 k) {
+    StokesBasis b = lma_stokes_basis(k);
+    return stokes_rotate_cs(sv, b.c2, -b.s2);
 }
 
 // nonlinear_compton/mod.rs:58-138 for a sampled (n, s, cphi, Stokes):
