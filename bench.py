@@ -83,8 +83,8 @@ SEED0 = 1000
 # cbrt 16, sincos 37, pow 121, atan2 57, hypot 16, log1p 37, acos 31).
 # Cross-checked against ncu's executed DFMA/DMUL/DADD counts: the LMA push
 # alone (ptg_push_steps) executes 204.5 flops per step against 208 counted;
-# the CP lepton wave with emission switched off executes 13.8 GFLOP per 2e5
-# primaries against 14.6 counted.
+# the CP lepton wave of 2e5 primaries, emissions included, executes 16.25
+# GFLOP against 14.7 counted.
 OPS = {
     # FocusedLaser (LMA, CP), a step in the pulse: lma_push (gradient of
     # <a^2> at the midpoint, <a^2> at the end: 105 + 3 div + 2 exp + sqrt =
@@ -96,11 +96,13 @@ OPS = {
     "free_lepton_step": 16.0,
     # a photon step in the LMA field: the drift (8), the phase test (3),
     # <a^2> and its root (70), eta, the phase step and the rate prefactor
-    # (33), the Stokes parameters into and out of the LMA basis with their
-    # rotations (270); the Breit-Wheeler table lookup (170) where the rate
-    # is not negligible: 384 without, 554 with (the photon wave of the CP
-    # shower executes 480 per step)
-    "lma_photon_step": 480.0,
+    # (33), the Stokes parameters into and out of the LMA basis (one basis,
+    # 68), the rotations by the polarisation angle (16 at angle zero, where
+    # sincos is exact and skipped), the probability and the Stokes update
+    # (50); the Breit-Wheeler table lookup (170) where the rate is not
+    # negligible: 258 without, 428 with.  The mean, 354, is the earlier
+    # build's measured 480 per step less the 126 those two changes removed.
+    "lma_photon_step": 354.0,
     # one emission sampled by the reference's CP sampler (table inversion,
     # the 32-point ceiling, the trials, the finish and the kinematics):
     # about 15.9 kflop per emission at a in [0.5, 5] and eta in [0.1, 0.2]
