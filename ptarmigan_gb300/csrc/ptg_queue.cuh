@@ -213,10 +213,20 @@ __device__ __forceinline__ bool queue_begin(const QueueArgs& q, WaveArgs& a, Lan
 // A particle that has left the field, decayed or failed: its record back to
 // the store, its counts to its collision, then `completed` (after its
 // children, which were appended and published while it ran).
-__device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs& a, Lane& L, const PartCounts& pc) {
+// The particle's final state written back, its failure counted, and its
+// slot completed (after a fence, so that a lane that sees every slot
+// completed also sees every child the particle appended).
+__device__ __forceinline__ void queue_retire(const QueueArgs& q, const WaveArgs& a, Lane& L) {
     if (L.species == SP_PHOTON && L.decayed) L.flags |= a.o.keep_decayed ? FLAG_INTERMEDIATE : FLAG_DROP;
     lane_store(a, L);
-    CollStats* cs = q.stats + L.coll;
+    if (L.status != ST_OK) atomicAdd(&q.stats[L.coll].errors, 1ull);
+    __threadfence();
+    atomicAdd(&a.c->completed, 1ull);
+}
+
+// Adds a lane's event counters to collision `coll`'s statistics.
+__device__ __forceinline__ void queue_count(const QueueArgs& q, int coll, const PartCounts& pc) {
+    CollStats* cs = q.stats + coll;
     if (pc.lsteps) atomicAdd(&cs->lepton_steps, pc.lsteps);
     if (pc.psteps) atomicAdd(&cs->photon_steps, pc.psteps);
     if (pc.fsteps) atomicAdd(&cs->free_steps, pc.fsteps);
@@ -224,9 +234,11 @@ __device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs&
     if (pc.nemit) atomicAdd(&cs->emissions, (unsigned long long)pc.nemit);
     if (pc.npair) atomicAdd(&cs->pair_events, (unsigned long long)pc.npair);
     if (pc.rej) atomicAdd(&cs->rejections, (unsigned long long)pc.rej);
-    if (L.status != ST_OK) atomicAdd(&cs->errors, 1ull);
-    __threadfence();
-    atomicAdd(&a.c->completed, 1ull);
+}
+
+__device__ __forceinline__ void queue_finish(const QueueArgs& q, const WaveArgs& a, Lane& L, const PartCounts& pc) {
+    queue_count(q, L.coll, pc);
+    queue_retire(q, a, L);
 }
 
 // One step of the lane's particle (main.rs:134-289's loop body); true when
@@ -271,9 +283,11 @@ __device__ __forceinline__ bool queue_step(const WaveArgs& a, Lane& L, PartCount
     return L.status != ST_OK;
 }
 
-// Steps a lane of the single-collision and lockstep queue kernels takes per
-// pass of their loops, between two rounds of ticket logic.
+// Steps a lane of the lockstep queue kernel takes per pass of its loop,
+// between two rounds of ticket logic.
 constexpr int QUEUE_STEPS_PER_PASS = 8;
+// The same for the single-collision kernel.
+constexpr int QUEUE_SINGLE_STEPS_PER_PASS = 16;
 
 // Kernel variants: MINB > 1 caps the registers so that MINB blocks of 128
 // threads fit on an SM (the LCFA paths need fewer registers than LMA's).
@@ -315,14 +329,16 @@ __global__ void __launch_bounds__(128, MINB) collide_queue(QueueArgs q) {
 }
 
 // The single-collision variant (a batch of one collision): one pass of its
-// loop is up to QUEUE_STEPS_PER_PASS steps of every lane's particle, each
+// loop is up to QUEUE_SINGLE_STEPS_PER_PASS steps of every lane's particle, each
 // followed by the warp's service as in collide_wave, so a lane whose
 // particle ends takes its next ticket within a few steps, and the step
 // code reads the collision's parameters from the kernel's parameter space
 // (as collide_wave does) rather than from a per-lane copy that follows the
 // lane's current collision.  A lane whose ticket is not yet published looks
 // again on the next pass; the warp sleeps only when none of its lanes has a
-// particle.  Every wait is bounded by q.wait_ns of wall time.
+// particle.  Every wait is bounded by q.wait_ns of wall time.  The event
+// counters stay per lane over all the lane's particles and are added to
+// the collision's statistics once per warp at the kernel's end.
 //
 // Tickets past the primaries are secondaries, mostly photons, whose steps
 // are a different code path from a lepton's: a lane holding such a ticket
@@ -393,7 +409,6 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
                 } else {
                     L.hph = SPEED_OF_LIGHT * a.o.dt / L.u.t;
                     L.hh = 0.5 * SPEED_OF_LIGHT * a.o.dt / L.u.t;
-                    pc = PartCounts{0, 0, 0, 0, 0, 0, 0};
                     have = true;
                 }
             }
@@ -402,13 +417,13 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
             __nanosleep(256);
             continue;
         }
-        // up to QUEUE_STEPS_PER_PASS steps before the ticket logic runs
-        // again (its votes then cost once per several steps); a warp whose
-        // particles are all done leaves early
-        for (int k = 0; k < QUEUE_STEPS_PER_PASS; ++k) {
+        // up to QUEUE_SINGLE_STEPS_PER_PASS steps before the ticket logic
+        // runs again (its votes then cost once per several steps); a warp
+        // whose particles are all done leaves early
+        for (int k = 0; k < QUEUE_SINGLE_STEPS_PER_PASS; ++k) {
             if (have && queue_step<MODEL>(a, L, pc, bdf, dfr)) {
                 maxst = L.step > maxst ? L.step : maxst;
-                queue_finish(q, a, L, pc);
+                queue_retire(q, a, L);
                 have = false;
             }
             if (LMA && (bdf != nullptr || dfr != nullptr)) warp_serve(a, dfr, bdf, have);
@@ -416,6 +431,17 @@ __global__ void __launch_bounds__(128) collide_queue_single(const __grid_constan
         }
     }
     if (maxst) atomicMax(&a.c->max_steps, (unsigned long long)maxst);
+    // the lane's counters over all its particles: one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        pc.lsteps += __shfl_down_sync(FULL, pc.lsteps, o);
+        pc.psteps += __shfl_down_sync(FULL, pc.psteps, o);
+        pc.fsteps += __shfl_down_sync(FULL, pc.fsteps, o);
+        pc.dsteps += __shfl_down_sync(FULL, pc.dsteps, o);
+        pc.nemit += __shfl_down_sync(FULL, pc.nemit, o);
+        pc.npair += __shfl_down_sync(FULL, pc.npair, o);
+        pc.rej += __shfl_down_sync(FULL, pc.rej, o);
+    }
+    if (lane_id() == 0) queue_count(q, 0, pc);
 }
 
 // One step of a particle of any field model (the lockstep multi-collision
