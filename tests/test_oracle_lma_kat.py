@@ -285,3 +285,54 @@ def test_classical_samplers_run_and_stay_in_range(orc, pol):
             smax = 2.0 * n * eta / ((1.0 + a * a) if pol == 1 else (1.0 + 0.5 * a * a))
             assert n >= 1 and 0.0 <= s <= smax * (1.0 + 1e-12)
             assert np.all(np.isfinite(out[3:7])) and out[3] == 1.0
+
+
+# nonlinear_compton/mod.rs:22-27 takes a = 0 where u.u - 1 is not positive
+# (rounding in the pulse's wings); the device's FP32 emission bound returns
+# a zero rate there, which holds only if both quantum rates are exactly zero
+# at a = 0 for every eta it may meet (0 < eta < 2), in every branch of their
+# dispatch: below the tables' smallest eta, below their smallest amplitude.
+@pytest.mark.parametrize("eta", [1e-6, 1e-4, 9.9e-4, 1e-3, 1.1e-3, 0.01, 0.196, 0.5, 1.0, 1.5, 1.999])
+def test_rates_vanish_at_zero_amplitude(orc, eta):
+    assert orc.cp_rate(0.0, eta) == 0.0
+    assert orc.lp_rate(0.0, eta) == 0.0
+
+
+# The device runs field-free LMA lepton steps in one loop once the
+# lepton's phase k(t - z) shows that the next m steps stay before the pulse
+# (or after it) and inside the field.  The premise: under the reference's
+# LMA push (focused_laser.rs:205-258) a massive particle's phase never falls
+# and grows by at most 2 omega dt per step, omega = c k.  Checked here on
+# the oracle's push, far from the pulse on both sides, for beams moving
+# against the laser, with it and across it.
+@pytest.mark.parametrize("side", [-1.0, 1.0])
+def test_field_free_phase_growth_bound(orc, side):
+    from ptarmigan_gb300 import abi
+    c = 299792458.0
+    laser = abi.laser_desc(abi.FOCUSED_LASER, 5.0, 0.8e-6, abi.CIRCULAR, abi.GAUSSIAN, waist=3e-6,
+                           fwhm_duration=30e-15)
+    k = 2.0 * math.pi / 0.8e-6
+    omega = c * k
+    dt = 1.0 / omega  # Field::max_timestep of FocusedLaser (Gaussian)
+    rng = np.random.default_rng(5 if side > 0 else 6)
+    rqm = -1.602176634e-19 / 9.1093837015e-31
+    for i in range(48):
+        gamma = 10.0 ** rng.uniform(0.5, 4.8)
+        direction = rng.normal(size=3)
+        if i % 3 == 0:
+            direction = np.array([0.0, 0.0, -1.0]) + 0.01 * direction  # against the laser
+        elif i % 3 == 1:
+            direction = np.array([0.0, 0.0, 1.0]) + 0.01 * direction  # with it
+        direction /= np.linalg.norm(direction)
+        p = math.sqrt(gamma * gamma - 1.0) * direction
+        u = np.array([math.sqrt(1.0 + p @ p), *p])
+        # phase far beyond the pulse's 2^-60 edge (about 284 rad here)
+        phase0 = side * rng.uniform(600.0, 2000.0)
+        z = rng.uniform(-20e-6, 20e-6)
+        r = np.array([z + phase0 / k, rng.uniform(-5e-6, 5e-6), rng.uniform(-5e-6, 5e-6), z])
+        for _ in range(64):
+            before = k * r[0] - k * r[3]
+            r, u, _, _ = orc.push(laser, r, u, rqm, dt)
+            grew = (k * r[0] - k * r[3]) - before
+            assert grew >= -1e-9, grew
+            assert grew <= 2.0 * omega * dt * (1.0 + 1e-12), grew
