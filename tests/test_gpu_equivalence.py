@@ -77,7 +77,7 @@ def _shared_batch(eng, make, n, tol):
 
 
 def test_cp_shower_equivalence(eng):
-    """configs[4]: the CP LMA shower with Stokes parameters tracked, pairs
+    """The CP LMA shower (a0 = 5 CP focused laser) with Stokes parameters tracked, pairs
     on.  Both the reference sampler (waves) and the learned proposal
     (persistent queue) against the oracle."""
     import bench
@@ -100,7 +100,7 @@ def test_cp_shower_equivalence(eng):
 
 
 def test_lcfa_shower_equivalence(eng):
-    """configs[1]: the focused LCFA shower, pairs on, generations <= 2."""
+    """The focused LCFA shower (a0 = 10 LP), pairs on, generations <= 2."""
     import bench
     make = bench.lcfa_workload
     ref, prim_r = _oracle(make, N_ORACLE, 2, 3)
@@ -112,7 +112,7 @@ def test_lcfa_shower_equivalence(eng):
 
 
 def test_plane_wave_equivalence(eng):
-    """configs[0]: the LP plane wave in the LMA, emission only."""
+    """The LP plane wave (a0 = 1, cos^2 envelope) in the LMA, emission only."""
     import bench
     make = bench.plane_wave_lma_workload
     ref, prim_r = _oracle(make, N_ORACLE, 2, 3)
